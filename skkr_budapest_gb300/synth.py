@@ -1,0 +1,510 @@
+"""Seeded synthetic inputs for the 2D-BZ tau path (host side, numpy).
+
+The reference obtains its inputs from self-consistent potentials (radial
+solvers, Madelung, ...), which lie outside the hot path.  The workloads here
+replace them with seeded, physically consistent stand-ins:
+
+* complex energies on the reference's semicircle contour (main/zmesh.f:55-83,
+  Gauss-Legendre nodes of main/legzero.f);
+* IBZ k meshes of main/speck2.f (square lattice, C4v wedge) with the weights
+  of main/kmesh2d.f:139-251;
+* single-site t-matrices of spherical square wells, in the reference's
+  convention t_l = -(1/kappa) sin(delta) exp(i delta) and screened as
+  (t - alpha)^-1 (nrsp-scf/tmat.f, rsp-scf/tmat.f:75-92); the screening
+  alpha_l is the t-matrix of a repulsive square barrier (main/alphamat.f);
+* screened structure constants in real space, G_scr(R) = [G0 (1 - alpha G0)^-1]
+  restricted to the central row of a cluster of the first three neighbour
+  shells.  This is the lattice-Fourier-transform form of G_scr(k); the
+  reference instead evaluates layer-pair Kambe sums per k (main/gstore.f).
+* point-group matrices D(g) of C4v in the complex-harmonic lm basis and, for
+  the relativistic case, in the (kappa,mu) basis of main/clebsch.f.
+
+Conventions: complex spherical harmonics with the Condon-Shortley phase,
+lm index l*l+l+m; free-space structure constants
+G0_{LL'}(R) = -4 pi i kappa sum_L'' i^(-l+l'-l'') <Y_L Y*_L' Y_L''> h_l''(kappa R) Y_L''(R),
+which expands -exp(i kappa |r-r'|)/(4 pi |r-r'|) between two sites (checked in
+tests/test_synth.py).  G(k) = sum_R exp(+i k.R_par) G_scr(R).
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+C_LIGHT = 274.072  # rsp-scf/cpacoord_ksave.f:93 (Rydberg units)
+
+
+# --------------------------------------------------------------------------
+# special functions
+# --------------------------------------------------------------------------
+def _plm_all(lmax: int, x: np.ndarray) -> np.ndarray:
+    """Associated Legendre P_l^m(x), m >= 0, Condon-Shortley phase."""
+    x = np.asarray(x, float)
+    P = np.zeros((lmax + 1, lmax + 1) + x.shape)
+    sx = np.sqrt(np.maximum(0.0, 1.0 - x * x))
+    P[0, 0] = 1.0
+    for m in range(1, lmax + 1):
+        P[m, m] = -(2 * m - 1) * sx * P[m - 1, m - 1]
+    for m in range(lmax):
+        P[m + 1, m] = (2 * m + 1) * x * P[m, m]
+    for m in range(lmax + 1):
+        for l in range(m + 2, lmax + 1):
+            P[l, m] = ((2 * l - 1) * x * P[l - 1, m] - (l + m - 1) * P[l - 2, m]) / (l - m)
+    return P
+
+
+def ylm(lmax: int, v) -> np.ndarray:
+    """Complex Y_lm(v) for unit or non-unit vectors v (N,3) -> (N,(lmax+1)^2)."""
+    v = np.atleast_2d(np.asarray(v, float))
+    r = np.linalg.norm(v, axis=1)
+    r = np.where(r == 0.0, 1.0, r)
+    ct = np.clip(v[:, 2] / r, -1.0, 1.0)
+    ph = np.arctan2(v[:, 1], v[:, 0])
+    P = _plm_all(lmax, ct)
+    out = np.zeros((len(v), (lmax + 1) ** 2), complex)
+    for l in range(lmax + 1):
+        for m in range(-l, l + 1):
+            am = abs(m)
+            nrm = math.sqrt((2 * l + 1) / (4 * math.pi) * math.factorial(l - am) / math.factorial(l + am))
+            y = nrm * P[l, am] * np.exp(1j * am * ph)
+            if m < 0:
+                y = (-1) ** am * np.conj(y)
+            out[:, l * l + l + m] = y
+    return out
+
+
+def sph_bessel(lmax: int, x):
+    """j_l, n_l, h_l = j_l + i n_l of complex argument (upward recurrence, as main/csbf.f)."""
+    x = np.asarray(x, complex)
+    j = np.zeros((lmax + 1,) + x.shape, complex)
+    n = np.zeros_like(j)
+    j[0] = np.sin(x) / x
+    n[0] = -np.cos(x) / x
+    if lmax >= 1:
+        j[1] = np.sin(x) / x ** 2 - np.cos(x) / x
+        n[1] = -np.cos(x) / x ** 2 - np.sin(x) / x
+    for l in range(2, lmax + 1):
+        j[l] = (2 * l - 1) * j[l - 1] / x - j[l - 2]
+        n[l] = (2 * l - 1) * n[l - 1] / x - n[l - 2]
+    return j, n, j + 1j * n
+
+
+def lm_l(lmmax: int) -> np.ndarray:
+    return np.array([int(math.isqrt(i)) for i in range(lmmax)])
+
+
+def _sphere_quadrature(deg: int):
+    nq = deg // 2 + 2
+    xg, wg = np.polynomial.legendre.leggauss(nq)
+    nph = deg + 2
+    ph = 2 * math.pi * np.arange(nph) / nph
+    ct = np.repeat(xg, nph)
+    w = np.repeat(wg, nph) * 2 * math.pi / nph
+    phi = np.tile(ph, nq)
+    st = np.sqrt(1 - ct * ct)
+    return np.stack([st * np.cos(phi), st * np.sin(phi), ct], 1), w
+
+
+_GAUNT_CACHE: dict = {}
+
+
+def gaunt_g0(lmax: int) -> np.ndarray:
+    """C[L, L', L''] = <Y_L Y*_L' Y_L''> over the sphere, L'' up to 2*lmax."""
+    if lmax in _GAUNT_CACHE:
+        return _GAUNT_CACHE[lmax]
+    l2 = 2 * lmax
+    v, w = _sphere_quadrature(2 * lmax + l2 + 2)
+    y1 = ylm(lmax, v)
+    y3 = ylm(l2, v)
+    c = np.einsum("q,qa,qb,qc->abc", w, y1, np.conj(y1), y3)
+    c[np.abs(c) < 1e-13] = 0.0
+    _GAUNT_CACHE[lmax] = c
+    return c
+
+
+def kappa_of(e: complex) -> complex:
+    k = np.sqrt(complex(e))
+    return -k if k.imag < 0 else k
+
+
+def free_g0(e: complex, rvecs: np.ndarray, lmax: int) -> np.ndarray:
+    """Free-space structure constants G0_{LL'}(R) for R (N,3) -> (N, LM, LM)."""
+    kap = kappa_of(e)
+    l2 = 2 * lmax
+    lmmax = (lmax + 1) ** 2
+    c = gaunt_g0(lmax)
+    lv = lm_l(lmmax)
+    lv2 = lm_l((l2 + 1) ** 2)
+    rvecs = np.atleast_2d(rvecs)
+    r = np.linalg.norm(rvecs, axis=1)
+    _, _, h = sph_bessel(l2, kap * r)          # (l2+1, N)
+    yr = ylm(l2, rvecs)                        # (N, LM2)
+    ph = (1j) ** ((-lv[:, None, None] + lv[None, :, None] - lv2[None, None, :]) % 4)
+    coef = -4 * math.pi * 1j * kap * c * ph    # (LM, LM, LM2)
+    hy = h[lv2, :].T * yr                      # (N, LM2)
+    return np.einsum("abc,nc->nab", coef, hy)
+
+
+# --------------------------------------------------------------------------
+# contour and k mesh (main/zmesh.f, main/legzero.f, main/speck2.f, main/kmesh2d.f)
+# --------------------------------------------------------------------------
+def legzero(ng: int):
+    """Gauss-Legendre nodes/weights by Newton from the A&S starting values."""
+    x = np.zeros(ng)
+    w = np.zeros(ng)
+
+    def legpol(xv, l):
+        pnm1, pn = 1.0, xv
+        for n in range(1, l):
+            pnm1, pn = pn, ((2 * n + 1) * xv * pn - n * pnm1) / (n + 1.0)
+        return pn, pnm1, l * (xv * pn - pnm1) / (xv * xv - 1.0)
+
+    n = ng // 2
+    for i in range(1, n + 1):
+        phi = (4 * i - 1) * math.pi / (4 * ng + 2.0)
+        xv = math.cos(phi + 1.0 / (8.0 * ng * ng * math.tan(phi)))
+        for _ in range(100):
+            pl, plm1, dpl = legpol(xv, ng)
+            dx = pl / dpl
+            xv -= dx
+            if abs(dx) <= 1e-14:
+                break
+        # the weight uses P_{n-1} of the last Newton step, as the reference does
+        wv = 2.0 * (1.0 - xv * xv) / (ng * ng * plm1 * plm1)
+        x[ng - i], x[i - 1], w[ng - i], w[i - 1] = xv, -xv, wv, wv
+    if 2 * n != ng:
+        pl, plm1, dpl = legpol(0.0, ng)
+        x[n], w[n] = 0.0, 2.0 / (ng * ng * plm1 * plm1)
+    return x, w
+
+
+def zmesh_semicircle(nepanel: int, ebottom: float, etop: float, epsilon: float):
+    """Semicircle contour energies and weights (imesh=1, one panel)."""
+    x, w = legzero(nepanel)
+    r = (etop - ebottom) / 2.0
+    z0 = ebottom + r
+    if epsilon > 1e-5:
+        eps = 1.0 / epsilon
+        y1 = -math.log(1.0 + math.pi / eps)
+        y2 = 0.0
+        y = 0.5 * (y2 - y1) * x + 0.5 * (y2 + y1)
+        phi = eps * (np.exp(-y) - 1.0)
+        z = r * np.exp(1j * phi) + z0
+        ww = -0.5 * (y2 - y1) * eps * np.exp(-y) * 1j * (z - z0) * w
+    else:
+        phi = 0.5 * (0.0 - math.pi) * x + 0.5 * math.pi
+        z = r * np.exp(1j * phi) + z0
+        ww = 0.5 * (0.0 - math.pi) * 1j * (z - z0) * w
+    return z, ww
+
+
+def kmesh_square_c4v(nset: int, a2d: float):
+    """IBZ of the square lattice (C4v wedge 0 < y <= x < pi/a), weights
+    normalised to 1: interior 1, diagonal 1/2 (kmesh2d.f:191-199)."""
+    pts = []
+    for i in range(1, nset + 1):
+        x = 0.5 * (2 * i - 1) / nset
+        for j in range(1, i + 1):
+            y = 0.5 * (2 * j - 1) / nset
+            pts.append((x, y, 0.5 if i == j else 1.0))
+    a = np.array(pts)
+    xk = a[:, :2] * (math.pi / a2d)
+    wk = a[:, 2] / a[:, 2].sum()
+    return xk, wk
+
+
+def kmesh_square_full(nset: int, a2d: float):
+    """Full-BZ grid whose C4v-irreducible part is kmesh_square_c4v(nset)."""
+    v = (2 * np.arange(1, nset + 1) - 1) / (2.0 * nset)
+    v = np.concatenate([-v[::-1], v])
+    xx, yy = np.meshgrid(v, v, indexing="ij")
+    xk = np.stack([xx.ravel(), yy.ravel()], 1) * (math.pi / a2d)
+    return xk, np.full(len(xk), 1.0 / len(xk))
+
+
+def nk_of_nset(nset: int) -> int:
+    return nset * (nset + 1) // 2
+
+
+# --------------------------------------------------------------------------
+# single-site: screening alpha and square-well t-matrices
+# --------------------------------------------------------------------------
+def _tan_delta(ck, q, r, lmax):
+    fb, fn, _ = sph_bessel(lmax + 1, ck * r)
+    gb, _, _ = sph_bessel(lmax + 1, q * r)
+    l = np.arange(lmax + 1)
+    return (ck * fb[l + 1] * gb[l] - q * fb[l] * gb[l + 1]) / (ck * fn[l + 1] * gb[l] - q * fn[l] * gb[l + 1])
+
+
+def alpha_sqwell(e: complex, vscreen: float, rs: float, lmax: int) -> np.ndarray:
+    """main/alphamat.f (iscreen<=1): alpha_l(E) of a barrier vscreen, radius rs."""
+    ck = kappa_of(e)
+    csk = kappa_of(complex(e) - vscreen)
+    tand = _tan_delta(ck, csk, rs, lmax)
+    react = -tand / ck
+    return react / (1.0 + 1j * ck * react)
+
+
+def tinv_sqwell_l(e: complex, depth: float, radius: float, lmax: int) -> np.ndarray:
+    """Inverse (unscreened) t_l^-1 of an attractive well V=depth<0."""
+    ck = kappa_of(e)
+    q = kappa_of(complex(e) - depth)
+    tand = _tan_delta(ck, q, radius, lmax)
+    react = -tand / ck
+    t = react / (1.0 + 1j * ck * react)
+    return 1.0 / t
+
+
+def screened_tinv_nonrel(e, depth, radius, alpha, lmax) -> np.ndarray:
+    """nrsp-scf/tmat.f: tminv(lm,lm) = tml/(1 - tml*alpha_l), lm-diagonal."""
+    tml = tinv_sqwell_l(e, depth, radius, lmax)
+    d = tml / (1.0 - tml * alpha)
+    lv = lm_l((lmax + 1) ** 2)
+    return np.diag(d[lv]).astype(complex)
+
+
+def kmy_l_kappa(lmax: int):
+    """(l, kappa, mu2) of each (kappa,mu) index of main/clebsch.f, ir = 2k^2+k+mu+1/2."""
+    n = 2 * (lmax + 1) ** 2
+    lv = np.zeros(n, int)
+    kv = np.zeros(n, int)
+    for l in range(lmax + 1):
+        for kap in ([l] if l > 0 else []) + [-l - 1]:
+            j2 = 2 * abs(kap) - 1
+            for mu2 in range(-j2, j2 + 1, 2):
+                m = (mu2 - 1) // 2
+                ir = 2 * kap * kap + kap + m + 1  # 1-based index of (kappa, mu=m+1/2)
+                if ir - 1 < n:
+                    lv[ir - 1] = l
+                    kv[ir - 1] = kap
+    return lv, kv
+
+
+def screened_tinv_rel(e, psq, depth, radius, so_split, alpha, lmax) -> np.ndarray:
+    """(kappa,mu)-diagonal screened t^-1 of a square well whose depth is split
+    for j = l +- 1/2 by so_split * <l.s> (rsp-scf/tmat.f:75-92 screening)."""
+    lv, kv = kmy_l_kappa(lmax)
+    ck = kappa_of(psq)
+    d = np.zeros(len(lv), complex)
+    for i, (l, kap) in enumerate(zip(lv, kv)):
+        ls = 0.5 * l if kap < 0 else -0.5 * (l + 1)
+        q = kappa_of(complex(psq) - (depth + so_split * ls))
+        tand = _tan_delta(ck, q, radius, l)[l]
+        react = -tand / ck
+        t = react / (1.0 + 1j * ck * react)
+        d[i] = 1.0 / (t - alpha[l])
+    return np.diag(d)
+
+
+# --------------------------------------------------------------------------
+# lattice, cluster and real-space screened structure constants
+# --------------------------------------------------------------------------
+@dataclass
+class Stacking:
+    """A Bravais stacking of identical square layers, ABAB with (1/2,1/2) shift."""
+    a2d: float      # in-plane square lattice constant
+    dz: float       # interlayer spacing
+    name: str = ""
+
+    def site(self, n: int, i: int, j: int) -> np.ndarray:
+        s = 0.5 * (n % 2)
+        return np.array([(i + s) * self.a2d, (j + s) * self.a2d, n * self.dz])
+
+
+def fcc001(a: float) -> Stacking:
+    return Stacking(a / math.sqrt(2.0), a / 2.0, "fcc(001)")
+
+
+def bcc001(a: float) -> Stacking:
+    return Stacking(a, a / 2.0, "bcc(001)")
+
+
+def cluster(st: Stacking, nshell: int = 3):
+    """Sites within the first nshell neighbour shells of the origin (with it).
+    Returns (vectors (N,3), layer offsets (N,), nn distance)."""
+    vs, ns = [], []
+    rng = range(-6, 7)
+    for n in range(-6, 7):
+        for i in rng:
+            for j in rng:
+                v = st.site(n, i, j) - st.site(0, 0, 0)
+                vs.append(v)
+                ns.append(n)
+    vs = np.array(vs)
+    ns = np.array(ns)
+    d = np.round(np.linalg.norm(vs, axis=1), 8)
+    shells = np.unique(d)
+    cut = shells[nshell] + 1e-6
+    sel = d <= cut
+    order = np.lexsort((vs[sel][:, 1], vs[sel][:, 0], d[sel]))
+    return vs[sel][order], ns[sel][order], shells[1]
+
+
+def screened_realspace(e_struct: complex, vecs: np.ndarray, alpha: np.ndarray, lmax: int) -> np.ndarray:
+    """Central row of G_scr = (1 - G0 alpha)^-1 G0 on the cluster `vecs`
+    (vecs[0] must be the origin).  Returns (N, LM, LM): G_scr(0 -> R_n)."""
+    lmmax = (lmax + 1) ** 2
+    nsite = len(vecs)
+    lv = lm_l(lmmax)
+    al = np.asarray(alpha)[lv]
+    big = np.zeros((nsite * lmmax, nsite * lmmax), complex)
+    pair_n, pair_m = np.nonzero(~np.eye(nsite, dtype=bool))
+    g = free_g0(e_struct, vecs[pair_n] - vecs[pair_m], lmax)
+    for idx, (n, m) in enumerate(zip(pair_n, pair_m)):
+        big[n * lmmax:(n + 1) * lmmax, m * lmmax:(m + 1) * lmmax] = g[idx]
+    # (1 - G0 alpha) X = G0, alpha diagonal per site
+    amat = np.eye(nsite * lmmax, dtype=complex) - big * np.tile(al, nsite)[None, :]
+    x = np.linalg.solve(amat, big)
+    row = x[:lmmax, :].reshape(lmmax, nsite, lmmax).transpose(1, 0, 2)
+    # G_scr(0 -> R_n) couples site 0 (row) to site n (column): G_{0n}
+    return np.ascontiguousarray(row)
+
+
+@dataclass
+class RTable:
+    """Real-space screened table grouped by structure-constant block."""
+    lmax: int
+    nblk: int
+    rstart: np.ndarray     # int32 (nblk+1)
+    rvec: np.ndarray       # float64 (nR, 2) in-plane displacement
+    gR: np.ndarray         # complex128 (nR, LM, LM), element [r, a, b] = G_ab
+    jmax: int
+    blk_of_j: dict = field(default_factory=dict)
+
+
+def build_rtable(st: Stacking, e_struct: complex, alpha: np.ndarray, lmax: int, nshell: int = 3) -> RTable:
+    vecs, ns, _ = cluster(st, nshell)
+    g = screened_realspace(e_struct, vecs, alpha, lmax)
+    jmax = int(np.max(np.abs(ns)))
+    starts, rv, gr, blk_of_j = [0], [], [], {}
+    for j in range(-jmax, jmax + 1):
+        sel = np.nonzero(ns == j)[0]
+        if len(sel) == 0:
+            continue
+        blk_of_j[j] = len(starts) - 1
+        rv.append(vecs[sel, :2])
+        gr.append(g[sel])
+        starts.append(starts[-1] + len(sel))
+    return RTable(lmax, len(starts) - 1, np.array(starts, np.int32), np.concatenate(rv),
+                  np.concatenate(gr), jmax, blk_of_j)
+
+
+def blkmap_translation_invariant(rt: RTable, nslot: int, mi: int) -> np.ndarray:
+    """blkmap[slot][i][j+jmax] for a stacking where every layer is equivalent."""
+    nj = 2 * rt.jmax + 1
+    m = -np.ones((nslot, mi, nj), np.int32)
+    for j, b in rt.blk_of_j.items():
+        m[:, :, j + rt.jmax] = b
+    return m
+
+
+def gk_blocks(rt: RTable, k: np.ndarray) -> np.ndarray:
+    """numpy G(k) blocks (nblk, LM, LM) -- used by the synthetic checks only."""
+    ph = np.exp(1j * (rt.rvec @ np.asarray(k, float)))
+    out = np.zeros((rt.nblk,) + rt.gR.shape[1:], complex)
+    for b in range(rt.nblk):
+        s, e = rt.rstart[b], rt.rstart[b + 1]
+        out[b] = np.einsum("r,rab->ab", ph[s:e], rt.gR[s:e])
+    return out
+
+
+# --------------------------------------------------------------------------
+# point group C4v: lm and (kappa,mu) representations
+# --------------------------------------------------------------------------
+def c4v_ops():
+    """3x3 matrices of C4v about z (E, C4, C2, C4^3, sx, sy, sd, sd')."""
+    def rz(t):
+        c, s = round(math.cos(t)), round(math.sin(t))
+        return np.array([[c, -s, 0], [s, c, 0], [0, 0, 1]], float)
+    ops = [rz(0), rz(math.pi / 2), rz(math.pi), rz(3 * math.pi / 2)]
+    ops += [np.diag([-1.0, 1, 1]), np.diag([1.0, -1, 1]),
+            np.array([[0, 1, 0], [1, 0, 0], [0, 0, 1]], float),
+            np.array([[0, -1, 0], [-1, 0, 0], [0, 0, 1]], float)]
+    return ops
+
+
+def d_orbital(op: np.ndarray, lmax: int) -> np.ndarray:
+    """D_{L'L}(g) with Y_L(g^-1 r) = sum_L' Y_L'(r) D_{L'L}(g)."""
+    v, w = _sphere_quadrature(4 * lmax + 4)
+    y = ylm(lmax, v)
+    yg = ylm(lmax, v @ op)   # rows: (g^-1 v)^T = v^T g for orthogonal g
+    return np.einsum("q,qa,qb->ab", w, np.conj(y), yg)
+
+
+def _su2(op: np.ndarray) -> np.ndarray:
+    """Spin-1/2 matrix of the proper part of op, basis (up, down)."""
+    r = op * np.linalg.det(op)
+    ang = math.acos(max(-1.0, min(1.0, (np.trace(r) - 1) / 2)))
+    if abs(ang) < 1e-12:
+        return np.eye(2, dtype=complex)
+    if abs(ang - math.pi) < 1e-9:
+        axis = np.sqrt(np.maximum(0.0, (np.diag(r) + 1) / 2))
+        i0 = int(np.argmax(axis))
+        for k in range(3):
+            if k != i0 and r[i0, k] < 0:
+                axis[k] = -axis[k]
+    else:
+        axis = np.array([r[2, 1] - r[1, 2], r[0, 2] - r[2, 0], r[1, 0] - r[0, 1]]) / (2 * math.sin(ang))
+    sx = np.array([[0, 1], [1, 0]], complex)
+    sy = np.array([[0, -1j], [1j, 0]], complex)
+    sz = np.array([[1, 0], [0, -1]], complex)
+    ns = axis[0] * sx + axis[1] * sy + axis[2] * sz
+    return math.cos(ang / 2) * np.eye(2) - 1j * math.sin(ang / 2) * ns
+
+
+def clebsch_u(lmax: int) -> np.ndarray:
+    """U[(s, lm), kmy] mapping (lm x spin) to (kappa,mu) as main/clebsch.f:
+    |kmy> = u1 |lm=ind1, s=-1/2> + u2 |lm=ind2, s=+1/2>; row index s*LM + lm
+    with s=0 for spin down, 1 for spin up."""
+    lmmax = (lmax + 1) ** 2
+    n = 2 * lmmax
+    u1 = np.zeros(72)
+    u2 = np.zeros(72)
+    i1 = np.zeros(72, int)
+    i2 = np.zeros(72, int)
+    inr = 0
+    for l in range(6):
+        tl = 2 * l + 1.0
+        for m in range(-l, l + 1):
+            inr += 1
+            kap = l
+            if kap != 0:
+                ir = 2 * kap * kap + kap + m
+                u1[ir - 1], i1[ir - 1] = math.sqrt((l + m) / tl), inr
+                ir += 1
+                u2[ir - 1], i2[ir - 1] = -math.sqrt((l - m) / tl), inr
+            kap = -l - 1
+            ir = 2 * kap * kap + kap + m
+            u1[ir - 1], i1[ir - 1] = math.sqrt((l - m + 1) / tl), inr
+            ir += 1
+            u2[ir - 1], i2[ir - 1] = math.sqrt((l + m + 1) / tl), inr
+    i1[i1 == 0] = 1
+    i2[i2 == 0] = 1
+    U = np.zeros((2 * lmmax, n))
+    for k in range(n):
+        U[0 * lmmax + i1[k] - 1, k] += u1[k]
+        U[1 * lmmax + i2[k] - 1, k] += u2[k]
+    return U
+
+
+def d_relativistic(op: np.ndarray, lmax: int) -> np.ndarray:
+    lmmax = (lmax + 1) ** 2
+    do = d_orbital(op, lmax)
+    s = _su2(op)                      # (up, down)
+    sd = s[::-1, ::-1]                # reorder to (down, up)
+    full = np.kron(sd, do)            # row index s*LM + lm
+    U = clebsch_u(lmax)
+    return U.T @ full @ U
+
+
+def point_group_mats(lmax: int, irel: int):
+    """L_g = D(g), R_g = D(g)^dagger for the C4v operations."""
+    ops = c4v_ops()
+    if irel:
+        ds = [d_relativistic(o, lmax) for o in ops]
+    else:
+        ds = [d_orbital(o, lmax) for o in ops]
+    lg = np.array(ds)
+    rg = np.conj(np.transpose(lg, (0, 2, 1)))
+    return lg, rg

@@ -1,0 +1,205 @@
+"""Seeded workloads of the 2D-BZ tau path (one object per contour energy).
+
+Each workload restates one benchmark configuration of the path with
+synthetic inputs (see synth.py): a Bravais (001) stacking of identical square
+layers, a semicircle contour, C4v IBZ k meshes with per-energy sizes, seeded
+square-well t-matrices and real-space screened structure constants.
+
+  plain_fcc   fcc(001) a=6.8, non-relativistic lmax=2 (9/site), PL2, 6-layer
+              interface, 16 energies -0.5..0.7 Ry, 253 k per energy.
+  rel_bcc     bcc(001) a=6.0, relativistic lmax=3 (32/site), PL4, 12-layer
+              interface, 24 energies, 210..12090 k per energy (uneven).
+  rel_bcc_cpa rel_bcc with 4 alloy layers A_c B_(1-c).
+  nonrel_pl2 / rel_pl3_l2   the two extra systems of the batched run.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import synth as S
+
+
+@dataclass
+class EnergyProblem:
+    name: str
+    ie: int
+    ce: complex
+    psq: complex
+    fac: complex
+    irel: int
+    lmax: int
+    lkmax: int
+    nprc: int
+    ninprc: np.ndarray          # int32 (nprc+2,)
+    bulkgeo: int
+    nintfc: int
+    blkmap: np.ndarray          # int32 (nslot, mi, 2*jmax+1)
+    rt: S.RTable
+    xk: np.ndarray              # (nk, 2)
+    wk: np.ndarray              # (nk,)
+    lg: np.ndarray              # (ngeff, lk, lk)
+    rg: np.ndarray
+    tminvl: np.ndarray          # (ninprc[0], lk, lk)
+    tminvr: np.ndarray          # (ninprc[-1], lk, lk)
+    tminv: np.ndarray           # (nintfc, lk, lk)  initial coherent (ATA for alloys)
+    tminva: np.ndarray
+    tminvb: np.ndarray
+    conc: np.ndarray            # (nintfc,)
+    alpha: np.ndarray           # (nintfc, lmax+1) screening per interface layer
+    itermaxl: int = 50
+    itermaxr: int = 50
+    errmax: float = 1.0e-8
+    itcpam: int = 50
+    cpatol: float = 1.0e-10
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def nk(self) -> int:
+        return len(self.xk)
+
+    @property
+    def n_pl(self) -> int:
+        return int(max(self.ninprc)) * self.lkmax
+
+    def with_k(self, xk, wk) -> "EnergyProblem":
+        import copy
+        c = copy.copy(self)
+        c.xk = np.ascontiguousarray(xk, float)
+        c.wk = np.ascontiguousarray(wk, float)
+        return c
+
+
+@dataclass
+class SystemSpec:
+    name: str
+    stacking: S.Stacking
+    irel: int
+    lmax: int
+    pl: int                   # layers per principal layer
+    nprc: int
+    energies: np.ndarray
+    nsets: list               # per energy IBZ subdivision
+    seed: int
+    depth_range: tuple = (-1.0, -0.5)
+    radius: float = 2.5
+    so_split: float = 0.03
+    vscreen: float = 2.0
+    alloy_layers: tuple = ()
+    conc_range: tuple = (0.1, 0.9)
+    alloy_depth_range: tuple = (-1.2, -0.4)
+    cpatol: float = 1.0e-10
+
+
+def _contour(ne, eb, et, eps):
+    z, _ = S.zmesh_semicircle(ne, eb, et, eps)
+    return z
+
+
+def plain_fcc(nset: int = 22) -> SystemSpec:
+    return SystemSpec("plain_fcc", S.fcc001(6.8), 0, 2, 2, 3, _contour(16, -0.5, 0.7, 150.0),
+                      [nset] * 16, seed=0)
+
+
+# per-energy IBZ subdivisions of the relativistic interface: 210 k far from the
+# real axis up to 12090 k at the contour point nearest E_F (Im E ~ 5e-3 Ry),
+# grouped like the reference's KSETTAB/INTAB table
+REL_NSETS = [20] * 12 + [32] * 4 + [48] * 3 + [70] * 2 + [100, 125, 155]
+
+
+def rel_bcc(nsets=None) -> SystemSpec:
+    z = _contour(24, -0.5, 0.7, 10.0)
+    return SystemSpec("rel_bcc", S.bcc001(6.0), 1, 3, 4, 3, z,
+                      list(REL_NSETS if nsets is None else nsets), seed=1)
+
+
+def rel_bcc_cpa(nsets=None) -> SystemSpec:
+    s = rel_bcc(nsets)
+    s.name = "rel_bcc_cpa"
+    s.seed = 2
+    s.alloy_layers = (4, 5, 6, 7)
+    return s
+
+
+def nonrel_pl2() -> SystemSpec:
+    z = _contour(16, -0.5, 0.7, 10.0)
+    return SystemSpec("nonrel_pl2", S.fcc001(6.8), 0, 2, 2, 3, z,
+                      [14] * 8 + [20] * 4 + [40] * 2 + [80, 126], seed=3)
+
+
+def rel_pl3_l2() -> SystemSpec:
+    z = _contour(20, -0.5, 0.7, 10.0)
+    return SystemSpec("rel_pl3_l2", S.bcc001(6.0), 1, 2, 3, 3, z,
+                      [14] * 10 + [20] * 4 + [40] * 3 + [60, 90, 126], seed=4)
+
+
+def system_layers(spec: SystemSpec):
+    ninprc = np.array([spec.pl] * (spec.nprc + 2), np.int32)
+    return ninprc, spec.pl * spec.nprc
+
+
+def energy_problem(spec: SystemSpec, ie: int, nset: int | None = None, kmesh: str = "ibz") -> EnergyProblem:
+    """Build the inputs of contour point ie of a system (seeded, deterministic)."""
+    ce = complex(spec.energies[ie])
+    lmax = spec.lmax
+    irel = spec.irel
+    if irel:
+        psq = ce + ce * ce / (S.C_LIGHT * S.C_LIGHT)
+        lk = 2 * (lmax + 1) ** 2
+    else:
+        psq = ce
+        lk = (lmax + 1) ** 2
+    fac = psq / ce
+    st = spec.stacking
+    _, _, dnn = S.cluster(st, 1)
+    rs = 0.7 * dnn
+    alpha = S.alpha_sqwell(ce, spec.vscreen, rs, lmax)
+    rt = S.build_rtable(st, psq, alpha, lmax)
+    ninprc, nintfc = system_layers(spec)
+    blkmap = S.blkmap_translation_invariant(rt, spec.nprc + 2, int(max(ninprc)))
+
+    rng = np.random.default_rng(spec.seed)
+    d_bulk = rng.uniform(*spec.depth_range)
+    d_int = rng.uniform(*spec.depth_range, size=nintfc)
+    conc = np.ones(nintfc)
+    d_a = d_int.copy()
+    d_b = d_int.copy()
+    for li in spec.alloy_layers:
+        conc[li] = rng.uniform(*spec.conc_range)
+        d_a[li] = rng.uniform(*spec.alloy_depth_range)
+        d_b[li] = rng.uniform(*spec.alloy_depth_range)
+
+    def tinv(depth):
+        if irel:
+            return S.screened_tinv_rel(ce, psq, depth, spec.radius, spec.so_split, alpha, lmax)
+        return S.screened_tinv_nonrel(ce, depth, spec.radius, alpha, lmax)
+
+    tb = tinv(d_bulk)
+    tminvl = np.array([tb] * ninprc[0])
+    tminvr = np.array([tb] * ninprc[-1])
+    ta = np.array([tinv(d) for d in d_a])
+    tbb = np.array([tinv(d) for d in d_b])
+    tm = ta.copy()
+    for li in spec.alloy_layers:
+        tm[li] = ata(conc[li], ta[li], tbb[li])
+
+    ns = spec.nsets[ie] if nset is None else nset
+    if kmesh == "ibz":
+        xk, wk = S.kmesh_square_c4v(ns, st.a2d)
+        lg, rg = S.point_group_mats(lmax, irel)
+    else:
+        xk, wk = S.kmesh_square_full(ns, st.a2d)
+        lg, rg = S.point_group_mats(lmax, irel)
+        lg, rg = lg[:1], rg[:1]
+    return EnergyProblem(spec.name, ie, ce, psq, fac, irel, lmax, lk, spec.nprc, ninprc, 1, nintfc,
+                         blkmap, rt, xk, wk, lg, rg, tminvl, tminvr, tm, ta, tbb, conc,
+                         np.array([alpha] * nintfc), cpatol=spec.cpatol,
+                         meta=dict(nset=ns, depth_bulk=d_bulk))
+
+
+def ata(conc: float, ma: np.ndarray, mb: np.ndarray) -> np.ndarray:
+    """rsp-scf/fullcpa.f:2-23 tata: m_c = m_B (c m_B + (1-c) m_A)^-1 m_A."""
+    mc = conc * mb + (1.0 - conc) * ma
+    return mb @ np.linalg.inv(mc) @ ma
