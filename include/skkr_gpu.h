@@ -1,0 +1,161 @@
+/*
+ * skkr_gpu.h -- C ABI of the GB300 2D-Brillouin-zone tau / CPA library.
+ *
+ * Drop-in for the per-energy k integration and CPA loop of the screened-KKR
+ * layer code laszloffy/skkr_budapest:
+ *
+ *   subroutine cpacoord(itscf,ie,ce,lmax,nintfc,eta,rightm,bulk,bulkgeo,wrel,
+ *                       kset,xk,wk,nk,intbz,iek,conc,itcpam,cpatol,cpatest,
+ *                       dmata,dmatb,dmatpa,dmatpb,tminvl,tminvr,tminv,tminva,
+ *                       tminvb,taua,taub,gtaua,gtaub)
+ *     skkr_kpar_v6/rsp-scf/cpacoord_ksave.f:3-9     (relativistic, kappa-mu)
+ *     skkr_kpar_v6/nrsp-scf/cpacoord.f:2-6          (non-relativistic, lm)
+ *
+ * Plain pointers and sizes only.  Matrices are complex*16 (interleaved
+ * re/im doubles, C `double _Complex`), column-major, leading dimension `ld`
+ * (the Fortran kmymaxp / lmmaxp may be passed as-is).  All host buffers are
+ * owned by the caller and read/written synchronously; no pointer is kept
+ * after a call returns.  The library never aborts the process: every entry
+ * point returns SKKR_OK or a negative error code and, where it takes one,
+ * fills an skkr_status.
+ *
+ * Everything runs on the CUDA device current when skkr_gpu_create is called;
+ * there is no CPU fallback.
+ */
+#ifndef SKKR_GPU_H
+#define SKKR_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SKKR_MAX_PRC 16   /* interface principal layers (param.h mprc) */
+#define SKKR_MAX_G 12     /* point-group operations (param.h melem)     */
+
+enum skkr_mode { SKKR_NONREL = 0, SKKR_REL = 1 };
+enum skkr_precision { SKKR_FP64 = 0, SKKR_MIXED = 1 };
+
+enum skkr_error {
+  SKKR_OK = 0,
+  SKKR_ERR_ARG = -1,          /* bad size / pointer / layout              */
+  SKKR_ERR_CUDA = -2,         /* CUDA runtime error (message via skkr_gpu_last_error) */
+  SKKR_ERR_SGF_ITERMAX = -3,  /* decimation hit itermax (main/surfgf.f:98-101 `stop`) */
+  SKKR_ERR_SGF_DIVERGED = -4, /* decimation error > 1e10 (main/surfgf.f:88-93)        */
+  SKKR_ERR_UNSUPPORTED = -5,  /* input outside the implemented scope                  */
+  SKKR_ERR_NOMEM = -6,
+  SKKR_ERR_NONFINITE = -7     /* NaN/Inf in a result                                  */
+};
+
+/* Sizes of one system: the runtime equivalent of param.h plus the
+ * /lay2d/ and /iterpar/ COMMON blocks read by cpacoord
+ * (rsp-scf/cpacoord_ksave.f:71-80). */
+typedef struct {
+  int mode;                       /* skkr_mode; kappa-mu block 2(lmax+1)^2 or lm (lmax+1)^2 */
+  int lmax;                       /* <= 3 */
+  int nprc;                       /* interface principal layers, 1..SKKR_MAX_PRC */
+  int ninprc[SKKR_MAX_PRC + 2];   /* layers per PL: [0] left lead, [1..nprc], [nprc+1] right lead */
+  int bulkgeo;                    /* 1: every interface PL uses structure-constant slot 1 */
+  int ngeff;                      /* point-group operations summed in the k integral */
+  int itermaxl, itermaxr;         /* decimation caps (/iterpar/) */
+  double errmax;                  /* decimation tolerance (/iterpar/) */
+  int itcpam;                     /* CPA iteration cap */
+  double cpatol;                  /* CPA tolerance on error3 (rsp-scf/fullcpa.f:142) */
+  int precision;                  /* skkr_precision */
+  int nk_chunk;                   /* k points per device batch (0: automatic) */
+} skkr_sizes;
+
+/* Real-space screened structure constants of one energy, grouped in
+ * lm x lm blocks: block b of G_scr(k) = sum over r in [rstart[b], rstart[b+1])
+ * of exp(+i k.rvec[r]) gR[r].  blkmap[(slot*mi + i-1)*(2*jmax+1) + j+jmax]
+ * is the block coupling layer i of a principal layer of structure-constant
+ * slot `slot` (0 left lead, 1.. interface, nprc+1 right lead) to layer i+j,
+ * or -1.  This replaces the per-k Kambe evaluation of main/gstore.f:6-283
+ * (g2d(lmmaxp,lmmaxp,-minprc:minprc,minprc,0:mprc1+1)). */
+typedef struct {
+  int nblk;
+  int nr;
+  const int *rstart;          /* [nblk+1] */
+  const double *rvec;         /* [nr][2] */
+  const double *gR;           /* [nr] column-major (lmax+1)^2 square complex blocks */
+  int nslot, mi, jmax;
+  const int *blkmap;          /* [nslot][mi][2*jmax+1] */
+} skkr_rtable;
+
+typedef struct {
+  int code;                   /* skkr_error of the call */
+  int ik;                     /* first failing k point (0-based) or -1 */
+  int cpa_iterations;         /* itcpa-1 on exit, as printed by cpacoord */
+  double cpa_error;           /* last max error3 */
+  int max_dec_iters;          /* largest decimation iteration count */
+  long long dec_iters_total;  /* summed decimation iterations */
+  long long gpu_launches;     /* kernels launched by this call */
+  double max_refine_resid;    /* mixed precision: largest final refinement residual */
+} skkr_status;
+
+typedef struct skkr_ctx skkr_ctx;
+
+/* Create a context on the current CUDA device (replaces the Fortran `save`
+ * arrays xsave, ysave, g2d of cpacoord_ksave.f:86). */
+int skkr_gpu_create(const skkr_sizes *sizes, skkr_ctx **ctx);
+int skkr_gpu_destroy(skkr_ctx *ctx);
+
+/* One energy: the CPA loop around the k loop, k-sum with point-group
+ * rotation and the CPA update (cpacoord_ksave.f:139-419).
+ *   ce, fac        complex energy and relmtrx factor psq/ce (1 non-rel)
+ *   rt             structure-constant table of this energy
+ *   nk, xk, wk     k points [nk][2] and normalised weights
+ *   lg, rg         [ngeff] ld x ld: k-sum adds lg*tau*rg; t^-1 rotates as rg*t*lg
+ *                  (rmatp(invg(g)), rmat(invg(g)) of the reference)
+ *   conc           [nintfc] concentration of species A
+ *   tminvl/tminvr  [ninprc[0]] / [ninprc[nprc+1]] lead screened t^-1
+ *   tminv          [nintfc] in: starting coherent t^-1, out: converged
+ *   tminva/tminvb  [nintfc] species t^-1
+ *   tauc           [nintfc] out: k-summed screened coherent tau
+ *   taua/taub      [nintfc] out: screened species tau (before phystau, as cpacor leaves them)
+ */
+int skkr_gpu_cpacoord(skkr_ctx *ctx, double ce_re, double ce_im, double fac_re,
+                      double fac_im, const skkr_rtable *rt, int nk,
+                      const double *xk, const double *wk, const double *lg,
+                      const double *rg, const double *conc,
+                      const double *tminvl, const double *tminvr,
+                      double *tminv, const double *tminva,
+                      const double *tminvb, double *tauc, double *taua,
+                      double *taub, int ld, skkr_status *status);
+
+/* Split form for callers that keep inputs resident on the device across
+ * calls: stage (host -> device), run (device only), fetch (device -> host).
+ * skkr_gpu_cpacoord == stage + run + fetch. */
+int skkr_gpu_stage(skkr_ctx *ctx, double ce_re, double ce_im, double fac_re,
+                   double fac_im, const skkr_rtable *rt, int nk,
+                   const double *xk, const double *wk, const double *lg,
+                   const double *rg, const double *conc,
+                   const double *tminvl, const double *tminvr,
+                   const double *tminv, const double *tminva,
+                   const double *tminvb, int ld);
+int skkr_gpu_run(skkr_ctx *ctx, skkr_status *status);
+int skkr_gpu_fetch(skkr_ctx *ctx, double *tminv, double *tauc, double *taua,
+                   double *taub, int ld);
+
+/* Screened -> physical tau of one layer on the device
+ * (rsp-scf/phystau.f:2-61, nrsp-scf/phystau.f): tau := (1+a t)tau(1+t a) - (a + a t a). */
+int skkr_gpu_phystau(int mode, int lmax, double *tau, const double *tinv,
+                     const double *alpha, int ld);
+
+/* Lower-level batched kernels, exported for tests. */
+/* In-place inverses of `batch` n x n matrices (main/gjinv.f:2-59, column pivoting). */
+int skkr_gpu_gjinv_batch(int n, int batch, double *a, int ld);
+/* Decimation of `batch` (ml, m0, mr) triples -> x = (m0 - ...)^-1 (main/surfgf.f:2-108).
+ * iters[b] receives the iteration count, stat[b] 0 / SKKR_ERR_SGF_*. */
+int skkr_gpu_surfgf_batch(int n, int batch, const double *ml, const double *m0,
+                          const double *mr, double *x, int ld, int itermax,
+                          double errmax, int *iters, int *stat);
+/* G_scr(k) blocks of nk k points: out [nk][nblk] lm x lm column-major. */
+int skkr_gpu_gk(const skkr_rtable *rt, int lmax, int nk, const double *xk, double *out);
+
+/* Text of the last CUDA error seen by the library in this process. */
+const char *skkr_gpu_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

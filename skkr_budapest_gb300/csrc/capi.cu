@@ -1,0 +1,1112 @@
+// C ABI and host orchestration of the 2D-BZ tau / CPA path.
+//
+// One context owns the device state that the reference keeps in Fortran
+// `save` arrays (rsp-scf/cpacoord_ksave.f:86: xsave, ysave, g2d): the
+// structure-constant blocks of every k and the surface scattering-path
+// operators of every k, which the CPA iterations after the first reuse.
+// All dense work runs in the batched kernels of kernels_fp64.cu (FP64 path)
+// or kernels_mixed.cu (split precision); the host only sequences launches
+// and reads back small control values (decimation / CPA convergence).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/skkr_gpu.h"
+#include "kernels.h"
+
+long long g_skkr_launches = 0;
+static thread_local std::string g_last_error;
+
+#define CK(x)                                                                          \
+  do {                                                                                 \
+    cudaError_t e_ = (x);                                                              \
+    if (e_ != cudaSuccess) {                                                           \
+      g_last_error = std::string(#x) + ": " + cudaGetErrorString(e_);                 \
+      return SKKR_ERR_CUDA;                                                            \
+    }                                                                                  \
+  } while (0)
+#define CKR(x)                      \
+  do {                              \
+    int r_ = (x);                   \
+    if (r_ != SKKR_OK) return r_;   \
+  } while (0)
+
+extern "C" const char *skkr_gpu_last_error(void) { return g_last_error.c_str(); }
+
+static int g_sync_check = -1;
+static void trace_point(const char *what) {
+  if (g_sync_check != 1) return;
+  cudaError_t e = cudaPeekAtLastError();
+  fprintf(stderr, "skkr trace: %s: %s\n", what, cudaGetErrorString(e));
+}
+void skkr_after_launch(const char *file, int line) {
+  ++g_skkr_launches;
+  if (g_sync_check < 0) {
+    const char *e = getenv("SKKR_SYNC_CHECK");
+    g_sync_check = (e && e[0] == '1') ? 1 : 0;
+  }
+  if (!g_sync_check) return;
+  cudaError_t e1 = cudaGetLastError();
+  cudaError_t e2 = cudaDeviceSynchronize();
+  if ((e1 != cudaSuccess || e2 != cudaSuccess) && g_last_error.find("launch at") == std::string::npos) {
+    g_last_error = std::string("launch at ") + file + ":" + std::to_string(line) + ": " +
+                   cudaGetErrorString(e1 != cudaSuccess ? e1 : e2);
+    fprintf(stderr, "skkr: %s\n", g_last_error.c_str());
+  }
+}
+
+namespace {
+
+// growable device buffer
+struct DBuf {
+  void *p = nullptr;
+  size_t cap = 0;
+  int ensure(size_t bytes) {
+    if (bytes <= cap) return SKKR_OK;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    cudaError_t e = cudaMalloc(&p, bytes ? bytes : 16);
+    if (e != cudaSuccess) {
+      g_last_error = std::string("cudaMalloc: ") + cudaGetErrorString(e);
+      return SKKR_ERR_NOMEM;
+    }
+    cap = bytes;
+    return SKKR_OK;
+  }
+  template <class T>
+  T *as() const { return (T *)p; }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+};
+
+}  // namespace
+
+struct skkr_ctx {
+  skkr_sizes sz;
+  int lk = 0, lmmax = 0, pl = 0, n = 0, nintfc = 0, nprc = 0, ngeff = 1;
+  cudaStream_t st = nullptr;
+  // staged energy
+  int staged = 0;
+  int nk = 0, nblk = 0, nrt = 0, nslot = 0, mi = 0, jmax = 0, maxr = 0;
+  zd fac, ce;
+  std::vector<int> blkmap;
+  std::vector<double> conc_h;
+  DBuf gR, rvec, rstart, blkmap_d, xk, wk, lg, rg, conc;
+  DBuf tcat;      // [nl + nr + nintfc][lk^2]: lead L, lead R, interface coherent
+  DBuf tab;       // [nintfc][2][lk^2]: species A, B
+  DBuf trot, trtmp;  // [ngeff][nlay][lk^2]
+  DBuf pnorm;     // sorttmat / compmat norms
+  // per-energy caches over all k
+  DBuf G;         // [nk][nblk][lmmax^2]
+  DBuf sspo;      // [nk][nsl][n^2]
+  // chunk work
+  DBuf pool, jobs, dec, decf, deci, tauw, tauk;
+  DBuf S, T1, T2, tauc, cpa, cpan, cpaact;
+  std::vector<PackJob> jobs_h;
+  int nmat = 0;
+  int idx00 = 0, idx10 = 0, idx01 = 0, idxmtL = 0, idxmtR = 0;
+  // classes (rsp-scf/sorttmat.f)
+  std::vector<int> ieqg, ieqgl, ieqgr, igordl, igordr;
+  int nsl = 0;    // SSPO slots (L then R)
+  int nls = 0;    // left-lead SSPO slots
+  int kc = 0;     // chunk size
+  // status accumulation
+  int max_dec = 0;
+  long long tot_dec = 0;
+  int first_bad_k = -1;
+  int err_code = 0;
+};
+
+// ---------------------------------------------------------------------------
+extern "C" int skkr_gpu_create(const skkr_sizes *sizes, skkr_ctx **out) {
+  if (!sizes || !out) return SKKR_ERR_ARG;
+  const skkr_sizes &s = *sizes;
+  if (s.mode != SKKR_NONREL && s.mode != SKKR_REL) return SKKR_ERR_ARG;
+  if (s.lmax < 0 || s.lmax > 3 || s.nprc < 1 || s.nprc > SKKR_MAX_PRC) return SKKR_ERR_ARG;
+  if (s.ngeff < 1 || s.ngeff > 8) return SKKR_ERR_ARG;
+  if (s.precision != SKKR_FP64 && s.precision != SKKR_MIXED) return SKKR_ERR_ARG;
+  // uniform principal layers (the reference's dugo.f bulk branch sizes both
+  // leads with ninprc(1); tau2d.f then needs ninprc(1)=ninprc(nprc))
+  for (int i = 0; i <= s.nprc + 1; i++)
+    if (s.ninprc[i] != s.ninprc[1] || s.ninprc[i] < 1) return SKKR_ERR_UNSUPPORTED;
+  skkr_ctx *c = new skkr_ctx();
+  c->sz = s;
+  c->lmmax = (s.lmax + 1) * (s.lmax + 1);
+  c->lk = s.mode == SKKR_REL ? 2 * c->lmmax : c->lmmax;
+  c->pl = s.ninprc[1];
+  c->n = c->pl * c->lk;
+  c->nprc = s.nprc;
+  c->nintfc = c->pl * s.nprc;
+  c->ngeff = s.ngeff;
+  if (c->n > 256) {
+    delete c;
+    return SKKR_ERR_UNSUPPORTED;
+  }
+  if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return SKKR_ERR_CUDA;
+  }
+  cudaError_t e = pack_set_tables(s.mode == SKKR_REL, s.lmax);
+  if (e != cudaSuccess) {
+    g_last_error = std::string("pack_set_tables: ") + cudaGetErrorString(e);
+    cudaStreamDestroy(c->st);
+    delete c;
+    return SKKR_ERR_CUDA;
+  }
+  *out = c;
+  return SKKR_OK;
+}
+
+extern "C" int skkr_gpu_destroy(skkr_ctx *c) {
+  if (!c) return SKKR_OK;
+  DBuf *all[] = {&c->gR, &c->rvec, &c->rstart, &c->blkmap_d, &c->xk, &c->wk, &c->lg, &c->rg,
+                 &c->conc, &c->tcat, &c->tab, &c->trot, &c->trtmp, &c->pnorm, &c->G, &c->sspo,
+                 &c->pool, &c->jobs, &c->dec, &c->decf, &c->deci, &c->tauw, &c->tauk, &c->S,
+                 &c->T1, &c->T2, &c->tauc, &c->cpa, &c->cpan, &c->cpaact};
+  for (DBuf *b : all) b->release();
+  if (c->st) cudaStreamDestroy(c->st);
+  delete c;
+  return SKKR_OK;
+}
+
+// copy ld-strided column-major host matrices into packed lk x lk device blocks
+static int put_mats(DBuf &dst, size_t off_elems, const double *src, int count, int lk, int ld,
+                    cudaStream_t st) {
+  if (count <= 0) return SKKR_OK;
+  std::vector<zd> tmp((size_t)count * lk * lk);
+  for (int m = 0; m < count; m++)
+    for (int c = 0; c < lk; c++)
+      for (int r = 0; r < lk; r++) {
+        size_t s = ((size_t)m * ld * ld + r + (size_t)c * ld) * 2;
+        tmp[(size_t)m * lk * lk + r + (size_t)c * lk] = zmk(src[s], src[s + 1]);
+      }
+  CK(cudaMemcpyAsync(dst.as<zd>() + off_elems, tmp.data(), tmp.size() * sizeof(zd),
+                     cudaMemcpyHostToDevice, st));
+  CK(cudaStreamSynchronize(st));
+  return SKKR_OK;
+}
+
+static int get_mats(double *dst, const zd *src_dev, int count, int lk, int ld, cudaStream_t st,
+                    long long src_stride = -1) {
+  if (count <= 0) return SKKR_OK;
+  long long sstride = src_stride < 0 ? (long long)lk * lk : src_stride;
+  std::vector<zd> tmp((size_t)(count - 1) * sstride + (size_t)lk * lk);
+  CK(cudaMemcpyAsync(tmp.data(), src_dev, tmp.size() * sizeof(zd), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  for (int m = 0; m < count; m++)
+    for (int c = 0; c < lk; c++)
+      for (int r = 0; r < lk; r++) {
+        zd v = tmp[(size_t)m * sstride + r + (size_t)c * lk];
+        size_t d = ((size_t)m * ld * ld + r + (size_t)c * ld) * 2;
+        dst[d] = v.x;
+        dst[d + 1] = v.y;
+      }
+  return SKKR_OK;
+}
+
+// ---------------------------------------------------------------------------
+extern "C" int skkr_gpu_stage(skkr_ctx *c, double ce_re, double ce_im, double fac_re,
+                              double fac_im, const skkr_rtable *rt, int nk, const double *xk,
+                              const double *wk, const double *lg, const double *rg,
+                              const double *conc, const double *tminvl, const double *tminvr,
+                              const double *tminv, const double *tminva, const double *tminvb,
+                              int ld) {
+  if (!c || !rt || nk < 1 || !xk || !wk || !lg || !rg || !conc || !tminvl || !tminvr || !tminv ||
+      !tminva || !tminvb)
+    return SKKR_ERR_ARG;
+  if (ld < c->lk) return SKKR_ERR_ARG;
+  if (rt->nslot < c->nprc + 2 || rt->mi < c->pl || rt->nblk < 1 || rt->jmax < 0) return SKKR_ERR_ARG;
+  const int lk = c->lk, lk2 = lk * lk, ng = c->ngeff;
+  c->ce = zmk(ce_re, ce_im);
+  c->fac = zmk(fac_re, fac_im);
+  c->nk = nk;
+  c->nblk = rt->nblk;
+  c->nrt = rt->rstart[rt->nblk];
+  c->nslot = rt->nslot;
+  c->mi = rt->mi;
+  c->jmax = rt->jmax;
+  c->maxr = 0;
+  for (int b = 0; b < rt->nblk; b++) c->maxr = std::max(c->maxr, rt->rstart[b + 1] - rt->rstart[b]);
+  if (c->maxr > 64) return SKKR_ERR_UNSUPPORTED;
+  const int nj = 2 * rt->jmax + 1;
+  c->blkmap.assign(rt->blkmap, rt->blkmap + (size_t)rt->nslot * rt->mi * nj);
+  for (int v : c->blkmap)
+    if (v >= rt->nblk) return SKKR_ERR_ARG;
+  const size_t bs = (size_t)c->lmmax * c->lmmax;
+  CKR(c->gR.ensure(c->nrt * bs * sizeof(zd)));
+  CKR(c->rvec.ensure(c->nrt * 2 * sizeof(double)));
+  CKR(c->rstart.ensure((rt->nblk + 1) * sizeof(int)));
+  CKR(c->blkmap_d.ensure(c->blkmap.size() * sizeof(int)));
+  CKR(c->xk.ensure((size_t)nk * 2 * sizeof(double)));
+  CKR(c->wk.ensure((size_t)nk * sizeof(double)));
+  CKR(c->lg.ensure((size_t)ng * lk2 * sizeof(zd)));
+  CKR(c->rg.ensure((size_t)ng * lk2 * sizeof(zd)));
+  CKR(c->conc.ensure((size_t)c->nintfc * sizeof(double)));
+  const int nlay = 2 * c->pl + c->nintfc;
+  CKR(c->tcat.ensure((size_t)nlay * lk2 * sizeof(zd)));
+  CKR(c->tab.ensure((size_t)c->nintfc * 2 * lk2 * sizeof(zd)));
+  cudaStream_t st = c->st;
+  CK(cudaMemcpyAsync(c->gR.p, rt->gR, c->nrt * bs * sizeof(zd), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(c->rvec.p, rt->rvec, c->nrt * 2 * sizeof(double), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(c->rstart.p, rt->rstart, (rt->nblk + 1) * sizeof(int), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(c->blkmap_d.p, c->blkmap.data(), c->blkmap.size() * sizeof(int),
+                     cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(c->xk.p, xk, (size_t)nk * 2 * sizeof(double), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(c->wk.p, wk, (size_t)nk * sizeof(double), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(c->conc.p, conc, (size_t)c->nintfc * sizeof(double), cudaMemcpyHostToDevice, st));
+  c->conc_h.assign(conc, conc + c->nintfc);
+  CKR(put_mats(c->lg, 0, lg, ng, lk, ld, st));
+  CKR(put_mats(c->rg, 0, rg, ng, lk, ld, st));
+  CKR(put_mats(c->tcat, 0, tminvl, c->pl, lk, ld, st));
+  CKR(put_mats(c->tcat, (size_t)c->pl * lk2, tminvr, c->pl, lk, ld, st));
+  CKR(put_mats(c->tcat, (size_t)2 * c->pl * lk2, tminv, c->nintfc, lk, ld, st));
+  // species: [layer][2]
+  {
+    std::vector<zd> tmp((size_t)c->nintfc * 2 * lk2);
+    for (int l = 0; l < c->nintfc; l++)
+      for (int sdx = 0; sdx < 2; sdx++) {
+        const double *src = sdx == 0 ? tminva : tminvb;
+        for (int cc = 0; cc < lk; cc++)
+          for (int r = 0; r < lk; r++) {
+            size_t s = ((size_t)l * ld * ld + r + (size_t)cc * ld) * 2;
+            tmp[((size_t)l * 2 + sdx) * lk2 + r + (size_t)cc * lk] = zmk(src[s], src[s + 1]);
+          }
+      }
+    CK(cudaMemcpyAsync(c->tab.p, tmp.data(), tmp.size() * sizeof(zd), cudaMemcpyHostToDevice, st));
+  }
+  CK(cudaStreamSynchronize(st));
+  c->staged = 1;
+  return SKKR_OK;
+}
+
+// ---------------------------------------------------------------------------
+// packing plan: dedupe structure-constant slots with identical block maps
+static void plan_pack(skkr_ctx *c) {
+  const int nj = 2 * c->jmax + 1, rowlen = c->mi * nj;
+  auto canon = [&](int slot) {
+    for (int s2 = 0; s2 < slot; s2++)
+      if (std::equal(c->blkmap.begin() + (size_t)s2 * rowlen, c->blkmap.begin() + (size_t)(s2 + 1) * rowlen,
+                     c->blkmap.begin() + (size_t)slot * rowlen))
+        return s2;
+    return slot;
+  };
+  c->jobs_h.clear();
+  auto job = [&](int slot, int which) {
+    slot = canon(slot);
+    for (auto &j : c->jobs_h)
+      if (j.slot == slot && j.which == which) return j.dest;
+    PackJob j{slot, c->pl, c->pl, c->pl, which, (int)c->jobs_h.size()};
+    c->jobs_h.push_back(j);
+    return j.dest;
+  };
+  // bulkgeo: interface PLs use slot 1 (tau2d.f:51-52)
+  c->idx00 = job(1, 0);
+  c->idx10 = job(1, 1);
+  c->idx01 = job(1, 2);
+  c->idxmtL = job(0, 2);                  // dugo.f 'L': packer(..,g2d slot 0,..,mt) -> M01
+  c->idxmtR = job(c->nprc + 1, 1);        // dugo.f 'R': M10 of the right lead slot
+  c->nmat = (int)c->jobs_h.size();
+}
+
+// rsp-scf/sorttmat.f on device data: rotate t^-1 by every g, compare.
+__global__ void k_pair_norms(const zd *trot, int ng, int nlay, int lk2, double *out) {
+  // out[(pair*nlay + layer)*2 + {0: ||x-y||^2, 1: ||x||^2}], pair over iig<ig
+  const int layer = blockIdx.y, pair = blockIdx.x;
+  int ig = 1, acc = 0;
+  while (acc + ig <= pair) { acc += ig; ig++; }
+  const int iig = pair - acc;
+  const zd *x = trot + ((long long)iig * nlay + layer) * lk2;
+  const zd *y = trot + ((long long)ig * nlay + layer) * lk2;
+  double dn = 0, xn = 0;
+  for (int e = threadIdx.x; e < lk2; e += blockDim.x) {
+    zd a = x[e], b = y[e];
+    xn += a.x * a.x + a.y * a.y;
+    double dx = a.x - b.x, dy = a.y - b.y;
+    dn += dx * dx + dy * dy;
+  }
+  __shared__ double s1[256], s2[256];
+  s1[threadIdx.x] = dn;
+  s2[threadIdx.x] = xn;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      s1[threadIdx.x] += s1[threadIdx.x + o];
+      s2[threadIdx.x] += s2[threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    out[((long long)pair * nlay + layer) * 2] = s1[0];
+    out[((long long)pair * nlay + layer) * 2 + 1] = s2[0];
+  }
+}
+
+static int sorttmat_dev(skkr_ctx *c) {
+  const int lk = c->lk, lk2 = lk * lk, ng = c->ngeff;
+  const int nl = c->pl, nr = c->pl, ni = c->nintfc, nlay = nl + nr + ni;
+  cudaStream_t st = c->st;
+  CKR(c->trot.ensure((size_t)ng * nlay * lk2 * sizeof(zd)));
+  CKR(c->trtmp.ensure((size_t)ng * nlay * lk2 * sizeof(zd)));
+  // tmp[g][layer] = R_g t ; trot[g][layer] = tmp L_g
+  MatRef R = mref(c->rg.as<zd>(), 0, lk2, lk);
+  MatRef Tc = mref(c->tcat.as<zd>(), lk2, 0, lk);
+  MatRef Tm = mref(c->trtmp.as<zd>(), lk2, (long long)nlay * lk2, lk);
+  MatRef L = mref(c->lg.as<zd>(), 0, lk2, lk);
+  MatRef Tr = mref(c->trot.as<zd>(), lk2, (long long)nlay * lk2, lk);
+  launch_zgemm(0, R, Tc, Tm, Tm, Tm, lk, lk, lk, nlay, ng, nullptr, st);
+  launch_zgemm(0, Tm, L, Tr, Tr, Tr, lk, lk, lk, nlay, ng, nullptr, st);
+  c->ieqg.assign(ng, 1);
+  c->ieqgl.assign(ng, 1);
+  c->ieqgr.assign(ng, 1);
+  c->igordl.assign(ng, 1);
+  c->igordr.assign(ng, 1);
+  if (ng > 1) {
+    const int npair = ng * (ng - 1) / 2;
+    CKR(c->pnorm.ensure((size_t)npair * nlay * 2 * sizeof(double)));
+    dim3 grid(npair, nlay);
+    k_pair_norms<<<grid, 256, 0, st>>>(c->trot.as<zd>(), ng, nlay, lk2, c->pnorm.as<double>());
+    SKKR_LAUNCHED();
+    std::vector<double> pn((size_t)npair * nlay * 2);
+    CK(cudaMemcpyAsync(pn.data(), c->pnorm.p, pn.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    const double tol = 1.0e-8;  // sorttmat.f:27
+    auto eq = [&](int iig, int ig, int layer) {
+      int pair = ig * (ig - 1) / 2 + iig;
+      double dn = pn[((size_t)pair * nlay + layer) * 2], xn = pn[((size_t)pair * nlay + layer) * 2 + 1];
+      return std::sqrt(dn) < tol * std::sqrt(xn);  // matops.f compmat
+    };
+    auto all_eq = [&](int iig, int ig, int l0, int l1) {
+      for (int l = l0; l < l1; l++)
+        if (!eq(iig, ig, l)) return false;
+      return true;
+    };
+    for (int ig = 1; ig < ng; ig++) {
+      int f = -1;
+      for (int iig = 0; iig < ig && f < 0; iig++)
+        if (all_eq(iig, ig, 0, nl) && all_eq(iig, ig, nl, nl + nr) && all_eq(iig, ig, nl + nr, nlay)) f = iig;
+      c->ieqg[ig] = f < 0 ? ig + 1 : f + 1;
+    }
+    for (int ig = 1; ig < ng; ig++) {
+      int f = -1;
+      for (int iig = 0; iig < ig && f < 0; iig++)
+        if (all_eq(iig, ig, 0, nl)) f = iig;
+      if (f < 0) {
+        c->ieqgl[ig] = ig + 1;
+        c->igordl[ig] = c->igordl[c->ieqgl[ig - 1] - 1] + 1;
+      } else c->ieqgl[ig] = f + 1;
+    }
+    for (int ig = 1; ig < ng; ig++) {
+      int f = -1;
+      for (int iig = 0; iig < ig && f < 0; iig++)
+        if (all_eq(iig, ig, nl, nl + nr)) f = iig;
+      if (f < 0) {
+        c->ieqgr[ig] = ig + 1;
+        c->igordr[ig] = c->igordr[c->ieqgr[ig - 1] - 1] + 1;
+      } else c->ieqgr[ig] = f + 1;
+    }
+  }
+  return SKKR_OK;
+}
+
+// L/R lead classes computed on the first pass: list of g with ieqgl(g)==g
+static void lead_classes(const skkr_ctx *c, std::vector<int> &lg_of, std::vector<int> &rg_of) {
+  lg_of.clear();
+  rg_of.clear();
+  for (int g = 0; g < c->ngeff; g++) {
+    if (c->ieqgl[g] == g + 1) lg_of.push_back(g);
+    if (c->ieqgr[g] == g + 1) rg_of.push_back(g);
+  }
+}
+
+static int check_slot_quirk(const skkr_ctx *c) {
+  // igordl/igordr must give distinct cache slots to distinct classes; the
+  // reference's formula (sorttmat.f:167,191) can collide for non-monotone
+  // class patterns, which this library refuses instead of reproducing.
+  std::vector<int> seen;
+  for (int g = 0; g < c->ngeff; g++)
+    if (c->ieqgl[g] == g + 1) {
+      int s = c->igordl[g];
+      if (std::find(seen.begin(), seen.end(), s) != seen.end()) return SKKR_ERR_UNSUPPORTED;
+      seen.push_back(s);
+    }
+  seen.clear();
+  for (int g = 0; g < c->ngeff; g++)
+    if (c->ieqgr[g] == g + 1) {
+      int s = c->igordr[g];
+      if (std::find(seen.begin(), seen.end(), s) != seen.end()) return SKKR_ERR_UNSUPPORTED;
+      seen.push_back(s);
+    }
+  return SKKR_OK;
+}
+
+// ---------------------------------------------------------------------------
+// decimation (main/dugo.f + main/surfgf.f) for the k points [k0, k0+nkc)
+// items (k, s): s < nLc left-lead classes, then right-lead classes.
+static int run_decimation(skkr_ctx *c, int k0, int nkc, const std::vector<int> &lcls,
+                          const std::vector<int> &rcls) {
+  const int n = c->n, n2 = n * n, lk = c->lk, lk2 = lk * lk, pl = c->pl;
+  const int nLc = (int)lcls.size(), nRc = (int)rcls.size(), nc = nLc + nRc;
+  const int nit = nkc * nc;
+  const long long MB = n2;  // elements per matrix
+  CKR(c->dec.ensure((size_t)nit * 9 * MB * sizeof(zd)));
+  CKR(c->decf.ensure((size_t)nit * sizeof(double)));
+  CKR(c->deci.ensure((size_t)nit * 3 * sizeof(int)));
+  cudaStream_t st = c->st;
+  zd *W = c->dec.as<zd>();
+  // buffers per item: 0 eps, 1 alfa0, 2 alfa1, 3 beta0, 4 beta1, 5 x, 6 y1, 7 P, 8 Q
+  auto buf = [&](int b) { return mref(W + (long long)b * MB, (long long)nc * 9 * MB, 9 * MB, n); };
+  int *act = c->deci.as<int>(), *stat = act + nit, *iters = act + 2 * nit;
+  double *err = c->decf.as<double>();
+  zd *poolk = c->pool.as<zd>();
+  const long long psk = (long long)c->nmat * MB;
+  int mapml[SKKR_MAPN], mapm0[SKKR_MAPN], mapmr[SKKR_MAPN], mapt[SKKR_MAPN], mapmt[SKKR_MAPN],
+      mapsl[SKKR_MAPN];
+  for (int s = 0; s < nc; s++) {
+    bool L = s < nLc;
+    int g = L ? lcls[s] : rcls[s - nLc];
+    mapml[s] = L ? c->idx10 : c->idx01;
+    mapm0[s] = c->idx00;
+    mapmr[s] = L ? c->idx01 : c->idx10;
+    mapmt[s] = L ? c->idxmtL : c->idxmtR;
+    // rotated lead t: trot[g][layer], layers 0..pl-1 left lead, pl..2pl-1 right lead
+    mapt[s] = g * 2 + (L ? 0 : 1);
+    mapsl[s] = L ? (c->igordl[g] - 1) : (c->nls + c->igordr[g] - 1);
+  }
+  const int nlay = 2 * pl + c->nintfc;
+  MatRef Pml = mref_map(poolk, psk, MB, n, mapml, nc);
+  MatRef Pm0 = mref_map(poolk, psk, MB, n, mapm0, nc);
+  MatRef Pmr = mref_map(poolk, psk, MB, n, mapmr, nc);
+  MatRef Pmt = mref_map(poolk, psk, MB, n, mapmt, nc);
+  // trot layout [g][layer][lk2]: item t base = trot + g*nlay*lk2 + side*pl*lk2
+  int mapt2[SKKR_MAPN];
+  for (int s = 0; s < nc; s++) mapt2[s] = (mapt[s] / 2) * nlay + (mapt[s] % 2) * pl;
+  MatRef Tt = mref_map(c->trot.as<zd>(), 0, lk2, lk, mapt2, nc);
+  MatRef eps = buf(0), a0 = buf(1), a1 = buf(2), b0 = buf(3), b1 = buf(4), x = buf(5), y1 = buf(6),
+         P = buf(7), Q = buf(8);
+  // init: eps = m0 + t ; x = eps ; alfa = -ml ; beta = -mr   (surfgf.f:37-45)
+  launch_add_tblocks(eps, Pm0, Tt, lk, pl, n, nkc, nc, nullptr, st);
+  launch_zaxpby(x, eps, nullptr, 0, nullptr, 0, n, nkc, nc, nullptr, st);
+  // ml + (-2) ml is exactly -ml in floating point
+  launch_zaxpby(a0, Pml, &Pml, -2.0, nullptr, 0, n, nkc, nc, nullptr, st);
+  launch_zaxpby(b0, Pmr, &Pmr, -2.0, nullptr, 0, n, nkc, nc, nullptr, st);
+  {
+    std::vector<int> ones(nit, 1);
+    CK(cudaMemcpyAsync(act, ones.data(), nit * sizeof(int), cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(stat, 0, nit * sizeof(int), st));
+    CK(cudaMemsetAsync(iters, 0, nit * sizeof(int), st));
+  }
+  const int itermax = std::max(c->sz.itermaxl, c->sz.itermaxr);
+  int iter = 1;
+  for (;; iter++) {
+    MatRef &ac = (iter & 1) ? a0 : a1, &an = (iter & 1) ? a1 : a0;
+    MatRef &bc = (iter & 1) ? b0 : b1, &bn = (iter & 1) ? b1 : b0;
+    launch_zaxpby(y1, eps, nullptr, 0, nullptr, 0, n, nkc, nc, act, st);
+    launch_zgj(y1, n, nkc, nc, act, st);
+    launch_zgemm(0, ac, y1, P, P, P, n, n, n, nkc, nc, act, st);   // P = alfa y1
+    launch_zgemm(0, bc, y1, Q, Q, Q, n, n, n, nkc, nc, act, st);   // Q = beta y1
+    launch_zgemm(0, P, ac, an, an, an, n, n, n, nkc, nc, act, st); // alfa' = P alfa
+    launch_zgemm(0, Q, bc, bn, bn, bn, n, n, n, nkc, nc, act, st); // beta' = Q beta
+    launch_zgemm(2, P, bc, P, eps, x, n, n, n, nkc, nc, act, st);  // y3: eps -= y3, x -= y3
+    launch_zgemm(1, Q, ac, eps, eps, eps, n, n, n, nkc, nc, act, st);  // eps -= y4
+    launch_fnorm(an, n, nkc, nc, act, err, st);
+    // the two leads may carry different caps (itermaxl / itermaxr)
+    launch_dec_state(err, act, stat, iters, nit, iter, itermax, c->sz.errmax, st);
+    int any = 0;
+    {
+      std::vector<int> h(nit);
+      CK(cudaMemcpyAsync(h.data(), act, nit * sizeof(int), cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+      for (int v : h) any |= v;
+    }
+    if (!any || iter > itermax + 1) break;
+  }
+  // statuses
+  {
+    std::vector<int> hs(nit), hi(nit);
+    CK(cudaMemcpyAsync(hs.data(), stat, nit * sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(hi.data(), iters, nit * sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    for (int it = 0; it < nit; it++) {
+      int kk = it / nc, s = it % nc;
+      int cap = s < nLc ? c->sz.itermaxl : c->sz.itermaxr;
+      int code = hs[it];
+      if (code == 0 && hi[it] > cap) code = SKKR_ERR_SGF_ITERMAX;
+      c->max_dec = std::max(c->max_dec, hi[it]);
+      c->tot_dec += hi[it];
+      if (code != 0 && c->err_code == 0) {
+        c->err_code = code;
+        c->first_bad_k = k0 + kk;
+      }
+    }
+  }
+  // X = x^-1 ; xy = ml X mt (tripmt2) into the SSPO cache
+  launch_zgj(x, n, nkc, nc, nullptr, st);
+  launch_zgemm(0, Pml, x, y1, y1, y1, n, n, n, nkc, nc, nullptr, st);
+  MatRef SS = mref_map(c->sspo.as<zd>() + (long long)k0 * c->nsl * MB, (long long)c->nsl * MB, MB, n,
+                       mapsl, nc);
+  launch_zgemm(0, y1, Pmt, SS, SS, SS, n, n, n, nkc, nc, nullptr, st);
+  return SKKR_OK;
+}
+
+// ---------------------------------------------------------------------------
+// tau2d (main/tau2d.f) for k in [k0, k0+nkc), items (k, class)
+static int run_tau2d(skkr_ctx *c, int k0, int nkc, const std::vector<int> &icls) {
+  const int n = c->n, lk = c->lk, lk2 = lk * lk, pl = c->pl, nprc = c->nprc, ni = c->nintfc;
+  const int nc = (int)icls.size();
+  const long long MB = (long long)n * n;
+  const int nbuf = 5 * nprc + 1;
+  CKR(c->tauw.ensure((size_t)nkc * nc * nbuf * MB * sizeof(zd)));
+  CKR(c->tauk.ensure((size_t)nkc * nc * ni * lk2 * sizeof(zd)));
+  cudaStream_t st = c->st;
+  zd *Wb = c->tauw.as<zd>();
+  auto buf = [&](int b) { return mref(Wb + (long long)b * MB, (long long)nc * nbuf * MB, nbuf * MB, n); };
+  // buffers: T00[p]=p, YY[p]=nprc+p, Yraw[p]=2nprc+p, XX[p]=3nprc+p, Xraw[p]=4nprc+p, W=5nprc
+  auto T00 = [&](int p) { return buf(p); };
+  auto YY = [&](int p) { return buf(nprc + p); };
+  auto Yr = [&](int p) { return buf(2 * nprc + p); };
+  auto XX = [&](int p) { return buf(3 * nprc + p); };
+  auto Xr = [&](int p) { return buf(4 * nprc + p); };
+  MatRef Wm = buf(5 * nprc);
+  zd *poolk = c->pool.as<zd>();
+  const long long psk = (long long)c->nmat * MB;
+  int m00[SKKR_MAPN], m10[SKKR_MAPN], m01[SKKR_MAPN], ysl[SKKR_MAPN], xsl[SKKR_MAPN], tmap[SKKR_MAPN];
+  const int nlay = 2 * pl + ni;
+  for (int s = 0; s < nc; s++) {
+    int g = icls[s];
+    m00[s] = c->idx00;
+    m10[s] = c->idx10;
+    m01[s] = c->idx01;
+    ysl[s] = c->igordl[c->ieqgl[g] - 1] - 1;
+    xsl[s] = c->nls + c->igordr[c->ieqgr[g] - 1] - 1;
+    tmap[s] = g * nlay + 2 * pl;  // interface layers of trot[g]
+  }
+  MatRef M00 = mref_map(poolk, psk, MB, n, m00, nc);
+  MatRef M10 = mref_map(poolk, psk, MB, n, m10, nc);
+  MatRef M01 = mref_map(poolk, psk, MB, n, m01, nc);
+  zd *sbase = c->sspo.as<zd>() + (long long)k0 * c->nsl * MB;
+  MatRef Ys = mref_map(sbase, (long long)c->nsl * MB, MB, n, ysl, nc);
+  MatRef Xs = mref_map(sbase, (long long)c->nsl * MB, MB, n, xsl, nc);
+  // forward (tau2d.f:53-85)
+  for (int p = 0; p < nprc; p++) {
+    int tm2[SKKR_MAPN];
+    for (int s = 0; s < nc; s++) tm2[s] = tmap[s] + p * pl;
+    MatRef Tt = mref_map(c->trot.as<zd>(), 0, lk2, lk, tm2, nc);
+    launch_add_tblocks(T00(p), M00, Tt, lk, pl, n, nkc, nc, nullptr, st);
+    if (p == 0) {
+      launch_zaxpby(YY(0), Ys, nullptr, 0, nullptr, 0, n, nkc, nc, nullptr, st);
+    } else {
+      launch_zgemm(0, M10, Yr(p), YY(p), YY(p), YY(p), n, n, n, nkc, nc, nullptr, st);
+    }
+    if (p < nprc - 1) {
+      MatRef yy = YY(p);
+      launch_zaxpby(Wm, T00(p), &yy, -1.0, nullptr, 0, n, nkc, nc, nullptr, st);
+      launch_zgj(Wm, n, nkc, nc, nullptr, st);
+      launch_zgemm(0, Wm, M01, Yr(p + 1), Yr(p + 1), Yr(p + 1), n, n, n, nkc, nc, nullptr, st);
+    }
+  }
+  // backward (tau2d.f:89-109)
+  for (int p = nprc - 1; p >= 0; p--) {
+    if (p == nprc - 1) {
+      launch_zaxpby(XX(p), Xs, nullptr, 0, nullptr, 0, n, nkc, nc, nullptr, st);
+    } else {
+      launch_zgemm(0, M01, Xr(p), XX(p), XX(p), XX(p), n, n, n, nkc, nc, nullptr, st);
+    }
+    if (p > 0) {
+      MatRef xx = XX(p);
+      launch_zaxpby(Wm, T00(p), &xx, -1.0, nullptr, 0, n, nkc, nc, nullptr, st);
+      launch_zgj(Wm, n, nkc, nc, nullptr, st);
+      launch_zgemm(0, Wm, M10, Xr(p - 1), Xr(p - 1), Xr(p - 1), n, n, n, nkc, nc, nullptr, st);
+    }
+  }
+  // diagonal blocks (tau2d.f:114-149), weight wk/ngeff
+  for (int p = 0; p < nprc; p++) {
+    MatRef xx = XX(p), yy = YY(p);
+    launch_zaxpby(Wm, T00(p), &xx, -1.0, &yy, -1.0, n, nkc, nc, nullptr, st);
+    launch_zgj(Wm, n, nkc, nc, nullptr, st);
+    launch_extract_tau(Wm, lk, pl, p * pl, c->wk.as<double>() + k0, 1.0 / c->ngeff, c->tauk.as<zd>(),
+                       (long long)nc * ni * lk2, (long long)ni * lk2, nkc, nc, st);
+  }
+  return SKKR_OK;
+}
+
+// ---------------------------------------------------------------------------
+// CPA update (rsp-scf/fullcpa.f cpacor/cpasol) on the device
+__global__ void k_cpa_norms(const zd *mc, const zd *tab, int lk2, double *out) {
+  // out[l*4 + {0 ||ma-mc||^2, 1 ||ma||^2, 2 ||mb-mc||^2, 3 ||mb||^2}]
+  const int l = blockIdx.x;
+  const zd *m = mc + (long long)l * lk2, *a = tab + (long long)(2 * l) * lk2, *b = tab + (long long)(2 * l + 1) * lk2;
+  double s[4] = {0, 0, 0, 0};
+  for (int e = threadIdx.x; e < lk2; e += blockDim.x) {
+    zd va = a[e], vb = b[e], vm = m[e];
+    double dx = va.x - vm.x, dy = va.y - vm.y;
+    s[0] += dx * dx + dy * dy;
+    s[1] += va.x * va.x + va.y * va.y;
+    dx = vb.x - vm.x;
+    dy = vb.y - vm.y;
+    s[2] += dx * dx + dy * dy;
+    s[3] += vb.x * vb.x + vb.y * vb.y;
+  }
+  __shared__ double sh[4][256];
+  for (int q = 0; q < 4; q++) sh[q][threadIdx.x] = s[q];
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o)
+      for (int q = 0; q < 4; q++) sh[q][threadIdx.x] += sh[q][threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x < 4) out[l * 4 + threadIdx.x] = sh[threadIdx.x][0];
+}
+
+static int cpa_step(skkr_ctx *c, int *itcpa, int *cpacon, int *concpa, double *error) {
+  const int lk = c->lk, lk2 = lk * lk, ni = c->nintfc;
+  cudaStream_t st = c->st;
+  zd *mc = c->tcat.as<zd>() + (size_t)2 * c->pl * lk2;  // coherent t^-1 (in place)
+  zd *tauc = c->tauc.as<zd>();
+  // buffers: [ni][2] xa/xb, [ni][2] da/db, [ni] xc/h, [ni][2] tmp, [ni][2] tauab
+  CKR(c->cpa.ensure((size_t)ni * 9 * lk2 * sizeof(zd)));
+  CKR(c->cpan.ensure((size_t)ni * 6 * sizeof(double)));
+  // flags: act [ni], act2 [2 ni], not-act2 [2 ni]
+  CKR(c->cpaact.ensure((size_t)ni * 5 * sizeof(int)));
+  zd *X = c->cpa.as<zd>(), *Dd = X + (size_t)ni * 2 * lk2, *H = Dd + (size_t)ni * 2 * lk2,
+     *Tm = H + (size_t)ni * lk2, *TAB = Tm + (size_t)ni * 2 * lk2;
+  double *nrm = c->cpan.as<double>();
+  k_cpa_norms<<<ni, 256, 0, st>>>(mc, c->tab.as<zd>(), lk2, nrm);
+  SKKR_LAUNCHED();
+  std::vector<double> hn((size_t)ni * 4);
+  CK(cudaMemcpyAsync(hn.data(), nrm, hn.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  const double tiny = 1.0e-6, tol = 1.0e-10;  // fullcpa.f:41
+  std::vector<int> act(ni), act2(2 * ni), nact2(2 * ni);
+  int nalloy = 0;
+  for (int l = 0; l < ni; l++) {
+    bool cpalay = (1.0 - c->conc_h[l]) > tiny;
+    bool ica = std::sqrt(hn[l * 4 + 0]) < tol * std::sqrt(hn[l * 4 + 1]);
+    bool icb = std::sqrt(hn[l * 4 + 2]) < tol * std::sqrt(hn[l * 4 + 3]);
+    act[l] = (cpalay && !ica && !icb) ? 1 : 0;
+    nalloy += act[l];
+    act2[2 * l] = act2[2 * l + 1] = act[l];
+    nact2[2 * l] = nact2[2 * l + 1] = !act[l];
+  }
+  int *dact = c->cpaact.as<int>(), *dact2 = dact + ni, *dnact2 = dact + 3 * ni;
+  CK(cudaMemcpyAsync(dact, act.data(), ni * sizeof(int), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(dact2, act2.data(), 2 * ni * sizeof(int), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(dnact2, nact2.data(), 2 * ni * sizeof(int), cudaMemcpyHostToDevice, st));
+  // non-alloy layers: taua = taub = tauc (fullcpa.f:45-48)
+  MatRef TABm = mref(TAB, 2LL * lk2, lk2, lk);
+  MatRef tauc2 = mref(tauc, lk2, 0, lk);
+  launch_zaxpby(TABm, tauc2, nullptr, 0, nullptr, 0, lk, ni, 2, dnact2, st);
+  *error = 0.0;
+  if (nalloy > 0) {
+    MatRef Xm = mref(X, 2LL * lk2, lk2, lk), Dm = mref(Dd, 2LL * lk2, lk2, lk);
+    MatRef mc2 = mref(mc, lk2, 0, lk), tab2 = mref(c->tab.as<zd>(), 2LL * lk2, lk2, lk);
+    (void)Dd;
+    // da = mc - ma ; db = mc - mb ; xa = da ; xb = db   (cpasol.f:94-99)
+    launch_zaxpby(Dm, mc2, &tab2, -1.0, nullptr, 0, lk, ni, 2, dact2, st);
+    launch_zaxpby(Xm, Dm, nullptr, 0, nullptr, 0, lk, ni, 2, dact2, st);
+    launch_zgj(Xm, lk, ni, 2, dact2, st);
+    launch_zaxpby(Xm, Xm, &tauc2, -1.0, nullptr, 0, lk, ni, 2, dact2, st);
+    launch_zgj(Xm, lk, ni, 2, dact2, st);
+    // xc = c xa + (1-c) xb ; h = (xc^-1 + tauc)^-1 ; mc -= h   (:109-124)
+    MatRef Hm = mref(H, lk2, 0, lk), mc1 = mref(mc, lk2, 0, lk), tauc1 = mref(tauc, lk2, 0, lk);
+    launch_cpa_mix(X, c->conc.as<double>(), dact, lk, ni, H, st);
+    launch_zgj(Hm, lk, ni, 1, dact, st);
+    launch_zaxpby(Hm, Hm, &tauc1, 1.0, nullptr, 0, lk, ni, 1, dact, st);
+    launch_zgj(Hm, lk, ni, 1, dact, st);
+    launch_zaxpby(mc1, mc1, &Hm, -1.0, nullptr, 0, lk, ni, 1, dact, st);
+    // error3 = ||h||_F / ||mc||_F (:126-142)
+    CK(cudaMemsetAsync(nrm, 0, 2 * ni * sizeof(double), st));
+    launch_fnorm(Hm, lk, ni, 1, dact, nrm, st);
+    launch_fnorm(mc1, lk, ni, 1, dact, nrm + ni, st);
+    // tau_A = tauc + tauc xa tauc ; tau_B likewise (:145-150)
+    MatRef Tmm = mref(Tm, 2LL * lk2, lk2, lk);
+    launch_zgemm(0, tauc2, Xm, Tmm, Tmm, Tmm, lk, lk, lk, ni, 2, dact2, st);
+    launch_zgemm(0, Tmm, tauc2, TABm, TABm, TABm, lk, lk, lk, ni, 2, dact2, st);
+    launch_zaxpby(TABm, TABm, &tauc2, 1.0, nullptr, 0, lk, ni, 2, dact2, st);
+    std::vector<double> hn2(2 * ni);
+    CK(cudaMemcpyAsync(hn2.data(), nrm, 2 * ni * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    for (int l = 0; l < ni; l++)
+      if (act[l]) {
+        double e3 = hn2[l] / hn2[ni + l];
+        if (e3 >= *error) *error = e3;
+      }
+  }
+  if (*error <= c->sz.cpatol) *concpa = 0;
+  if (*itcpa >= c->sz.itcpam) *cpacon = 0;
+  (*itcpa)++;
+  return SKKR_OK;
+}
+
+// ---------------------------------------------------------------------------
+extern "C" int skkr_gpu_run(skkr_ctx *c, skkr_status *status) {
+  if (!c || !c->staged) return SKKR_ERR_ARG;
+  const long long l0 = g_skkr_launches;
+  const int n = c->n, lk = c->lk, lk2 = lk * lk, ni = c->nintfc, nk = c->nk;
+  const long long MB = (long long)n * n;
+  const size_t bs = (size_t)c->lmmax * c->lmmax;
+  cudaStream_t st = c->st;
+  c->max_dec = 0;
+  c->tot_dec = 0;
+  c->err_code = 0;
+  c->first_bad_k = -1;
+  plan_pack(c);
+  CKR(c->jobs.ensure(c->jobs_h.size() * sizeof(PackJob)));
+  CK(cudaMemcpyAsync(c->jobs.p, c->jobs_h.data(), c->jobs_h.size() * sizeof(PackJob),
+                     cudaMemcpyHostToDevice, st));
+  CKR(c->G.ensure((size_t)nk * c->nblk * bs * sizeof(zd)));
+  // chunk size: keep the per-chunk work within a fixed budget
+  {
+    const int ncmax = 2 * c->ngeff;
+    double per_k = (double)MB * sizeof(zd) * (c->nmat + 9.0 * ncmax + (5.0 * c->nprc + 1) * c->ngeff) +
+                   (double)c->ngeff * ni * lk2 * sizeof(zd);
+    double budget = 24.0e9;
+    int kc = c->sz.nk_chunk > 0 ? c->sz.nk_chunk : (int)std::max(1.0, std::floor(budget / per_k));
+    // grid.y of the batched kernels holds k_chunk * items-per-k (<= 2 * ngeff)
+    kc = std::min(kc, 65535 / (2 * c->ngeff));
+    c->kc = std::max(1, std::min(kc, nk));
+  }
+  CKR(c->pool.ensure((size_t)c->kc * c->nmat * MB * sizeof(zd)));
+
+  int itcpa = 1, cpacon = 1, concpa = 1;
+  double cpaerr = 0.0;
+  std::vector<int> lcls, rcls, icls;
+  for (;;) {
+    trace_point("loop top");
+    CKR(sorttmat_dev(c));
+    trace_point("after sorttmat");
+    CKR(check_slot_quirk(c));
+    lead_classes(c, lcls, rcls);
+    icls.clear();
+    for (int g = 0; g < c->ngeff; g++)
+      if (c->ieqg[g] == g + 1) icls.push_back(g);
+    const int ncls = (int)icls.size();
+    if (itcpa == 1) {
+      int nLs = 0, nRs = 0;
+      for (int g : lcls) nLs = std::max(nLs, c->igordl[g]);
+      for (int g : rcls) nRs = std::max(nRs, c->igordr[g]);
+      c->nls = nLs;
+      c->nsl = nLs + nRs;
+      CKR(c->sspo.ensure((size_t)nk * c->nsl * MB * sizeof(zd)));
+      launch_gk_ft(c->gR.as<zd>(), c->rvec.as<double>(), c->rstart.as<int>(), c->nblk, c->lmmax,
+                   c->xk.as<double>(), nk, c->G.as<zd>(), st);
+    }
+    CKR(c->S.ensure((size_t)ncls * ni * lk2 * sizeof(zd)));
+    for (int k0 = 0; k0 < nk; k0 += c->kc) {
+      const int nkc = std::min(c->kc, nk - k0);
+      launch_pack(c->G.as<zd>() + (size_t)k0 * c->nblk * bs, c->nblk, c->blkmap_d.as<int>(), c->mi,
+                  c->jmax, c->jobs.as<PackJob>(), c->nmat, lk, c->lmmax, c->sz.mode == SKKR_REL,
+                  c->fac, nkc, c->pool.as<zd>(), c->nmat, n, st);
+      if (itcpa == 1) CKR(run_decimation(c, k0, nkc, lcls, rcls));
+      if (c->err_code) break;
+      CKR(run_tau2d(c, k0, nkc, icls));
+      launch_ksum(c->tauk.as<zd>(), nkc, (long long)ncls * ni * lk2, c->S.as<zd>(), k0 > 0, st);
+    }
+    if (c->err_code) break;
+    // rotation of the class sums: tauc = sum_g L_g S[class(g)] R_g   (cpacoord_ksave.f:382-391)
+    CKR(c->T1.ensure((size_t)ni * c->ngeff * lk2 * sizeof(zd)));
+    CKR(c->T2.ensure((size_t)ni * c->ngeff * lk2 * sizeof(zd)));
+    CKR(c->tauc.ensure((size_t)ni * lk2 * sizeof(zd)));
+    {
+      int cmap[SKKR_MAPN];
+      for (int g = 0; g < c->ngeff; g++) {
+        int cls = c->ieqg[g] - 1;
+        cmap[g] = (int)(std::find(icls.begin(), icls.end(), cls) - icls.begin());
+      }
+      MatRef Lm = mref(c->lg.as<zd>(), 0, lk2, lk);
+      MatRef Sm = mref_map(c->S.as<zd>(), lk2, (long long)ni * lk2, lk, cmap, c->ngeff);
+      MatRef T1m = mref(c->T1.as<zd>(), (long long)c->ngeff * lk2, lk2, lk);
+      MatRef Rm = mref(c->rg.as<zd>(), 0, lk2, lk);
+      MatRef T2m = mref(c->T2.as<zd>(), (long long)c->ngeff * lk2, lk2, lk);
+      launch_zgemm(0, Lm, Sm, T1m, T1m, T1m, lk, lk, lk, ni, c->ngeff, nullptr, st);
+      launch_zgemm(0, T1m, Rm, T2m, T2m, T2m, lk, lk, lk, ni, c->ngeff, nullptr, st);
+      launch_gsum(c->T2.as<zd>(), c->ngeff, lk, ni, c->tauc.as<zd>(), st);
+    }
+    trace_point("before cpa_step");
+    int rc = cpa_step(c, &itcpa, &cpacon, &concpa, &cpaerr);
+    trace_point("after cpa_step");
+    if (rc != SKKR_OK) {
+      c->err_code = rc;
+      break;
+    }
+    if (!(concpa && cpacon)) break;
+  }
+  trace_point("after CPA loop");
+  CK(cudaStreamSynchronize(st));
+  CK(cudaGetLastError());
+  if (status) {
+    status->code = c->err_code;
+    status->ik = c->first_bad_k;
+    status->cpa_iterations = itcpa - 1;
+    status->cpa_error = cpaerr;
+    status->max_dec_iters = c->max_dec;
+    status->dec_iters_total = c->tot_dec;
+    status->gpu_launches = g_skkr_launches - l0;
+    status->max_refine_resid = 0.0;
+  }
+  return c->err_code;
+}
+
+extern "C" int skkr_gpu_fetch(skkr_ctx *c, double *tminv, double *tauc, double *taua, double *taub,
+                              int ld) {
+  if (!c || !c->staged || ld < c->lk) return SKKR_ERR_ARG;
+  const int lk = c->lk, lk2 = lk * lk, ni = c->nintfc;
+  cudaStream_t st = c->st;
+  if (tminv) CKR(get_mats(tminv, c->tcat.as<zd>() + (size_t)2 * c->pl * lk2, ni, lk, ld, st));
+  if (tauc) CKR(get_mats(tauc, c->tauc.as<zd>(), ni, lk, ld, st));
+  zd *TAB = c->cpa.as<zd>() + (size_t)ni * 7 * lk2;
+  if (taua) CKR(get_mats(taua, TAB, ni, lk, ld, st, 2LL * lk2));
+  if (taub) CKR(get_mats(taub, TAB + lk2, ni, lk, ld, st, 2LL * lk2));
+  return SKKR_OK;
+}
+
+extern "C" int skkr_gpu_cpacoord(skkr_ctx *c, double ce_re, double ce_im, double fac_re,
+                                 double fac_im, const skkr_rtable *rt, int nk, const double *xk,
+                                 const double *wk, const double *lg, const double *rg,
+                                 const double *conc, const double *tminvl, const double *tminvr,
+                                 double *tminv, const double *tminva, const double *tminvb,
+                                 double *tauc, double *taua, double *taub, int ld,
+                                 skkr_status *status) {
+  int rc = skkr_gpu_stage(c, ce_re, ce_im, fac_re, fac_im, rt, nk, xk, wk, lg, rg, conc, tminvl,
+                          tminvr, tminv, tminva, tminvb, ld);
+  if (rc != SKKR_OK) {
+    if (status) status->code = rc;
+    return rc;
+  }
+  rc = skkr_gpu_run(c, status);
+  if (rc != SKKR_OK) return rc;
+  return skkr_gpu_fetch(c, tminv, tauc, taua, taub, ld);
+}
+
+// ---------------------------------------------------------------------------
+// Stand-alone batched entry points (tests, callers that drive their own loop).
+// Each allocates its device buffers for the duration of the call.
+namespace {
+struct Scoped {
+  std::vector<void *> ptrs;
+  ~Scoped() {
+    for (void *p : ptrs) cudaFree(p);
+  }
+  template <class T>
+  int alloc(T **p, size_t count) {
+    void *q = nullptr;
+    cudaError_t e = cudaMalloc(&q, count * sizeof(T) + 16);
+    if (e != cudaSuccess) {
+      g_last_error = std::string("cudaMalloc: ") + cudaGetErrorString(e);
+      return SKKR_ERR_NOMEM;
+    }
+    ptrs.push_back(q);
+    *p = (T *)q;
+    return SKKR_OK;
+  }
+};
+
+int upload_mats(zd *dst, const double *src, int count, int n, int ld) {
+  std::vector<zd> tmp((size_t)count * n * n);
+  for (int m = 0; m < count; m++)
+    for (int c = 0; c < n; c++)
+      for (int r = 0; r < n; r++) {
+        size_t s = ((size_t)m * ld * ld + r + (size_t)c * ld) * 2;
+        tmp[(size_t)m * n * n + r + (size_t)c * n] = zmk(src[s], src[s + 1]);
+      }
+  CK(cudaMemcpy(dst, tmp.data(), tmp.size() * sizeof(zd), cudaMemcpyHostToDevice));
+  return SKKR_OK;
+}
+int download_mats(double *dst, const zd *src, int count, int n, int ld) {
+  std::vector<zd> tmp((size_t)count * n * n);
+  CK(cudaMemcpy(tmp.data(), src, tmp.size() * sizeof(zd), cudaMemcpyDeviceToHost));
+  for (int m = 0; m < count; m++)
+    for (int c = 0; c < n; c++)
+      for (int r = 0; r < n; r++) {
+        zd v = tmp[(size_t)m * n * n + r + (size_t)c * n];
+        size_t d = ((size_t)m * ld * ld + r + (size_t)c * ld) * 2;
+        dst[d] = v.x;
+        dst[d + 1] = v.y;
+      }
+  return SKKR_OK;
+}
+}  // namespace
+
+extern "C" int skkr_gpu_gjinv_batch(int n, int batch, double *a, int ld) {
+  if (n < 1 || n > 256 || batch < 1 || !a || ld < n) return SKKR_ERR_ARG;
+  Scoped s;
+  zd *d;
+  CKR(s.alloc(&d, (size_t)batch * n * n));
+  CKR(upload_mats(d, a, batch, n, ld));
+  launch_zgj(mref(d, (long long)n * n, 0, n), n, batch, 1, nullptr, 0);
+  CK(cudaDeviceSynchronize());
+  CK(cudaGetLastError());
+  return download_mats(a, d, batch, n, ld);
+}
+
+extern "C" int skkr_gpu_gk(const skkr_rtable *rt, int lmax, int nk, const double *xk, double *out) {
+  if (!rt || nk < 1 || !xk || !out || lmax < 0 || lmax > 3) return SKKR_ERR_ARG;
+  const int lmmax = (lmax + 1) * (lmax + 1), nr = rt->rstart[rt->nblk];
+  for (int b = 0; b < rt->nblk; b++)
+    if (rt->rstart[b + 1] - rt->rstart[b] > 64) return SKKR_ERR_UNSUPPORTED;
+  const size_t bs = (size_t)lmmax * lmmax;
+  Scoped s;
+  zd *gR, *o;
+  double *rv, *kx;
+  int *rs;
+  CKR(s.alloc(&gR, nr * bs));
+  CKR(s.alloc(&o, (size_t)nk * rt->nblk * bs));
+  CKR(s.alloc(&rv, 2 * (size_t)nr));
+  CKR(s.alloc(&kx, 2 * (size_t)nk));
+  CKR(s.alloc(&rs, rt->nblk + 1));
+  CK(cudaMemcpy(gR, rt->gR, nr * bs * sizeof(zd), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(rv, rt->rvec, 2 * (size_t)nr * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(kx, xk, 2 * (size_t)nk * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(rs, rt->rstart, (rt->nblk + 1) * sizeof(int), cudaMemcpyHostToDevice));
+  launch_gk_ft(gR, rv, rs, rt->nblk, lmmax, kx, nk, o, 0);
+  CK(cudaDeviceSynchronize());
+  CK(cudaGetLastError());
+  CK(cudaMemcpy(out, o, (size_t)nk * rt->nblk * bs * sizeof(zd), cudaMemcpyDeviceToHost));
+  return SKKR_OK;
+}
+
+extern "C" int skkr_gpu_surfgf_batch(int n, int batch, const double *ml, const double *m0,
+                                     const double *mr, double *x, int ld, int itermax,
+                                     double errmax, int *iters, int *stat) {
+  if (n < 1 || n > 256 || batch < 1 || !ml || !m0 || !mr || !x || ld < n) return SKKR_ERR_ARG;
+  const long long MB = (long long)n * n;
+  Scoped s;
+  zd *W;
+  double *err;
+  int *flags;
+  CKR(s.alloc(&W, (size_t)batch * 12 * MB));
+  CKR(s.alloc(&err, batch));
+  CKR(s.alloc(&flags, 3 * (size_t)batch));
+  // per item: 0 ml 1 m0 2 mr 3 eps 4 a0 5 a1 6 b0 7 b1 8 x 9 y1 10 P 11 Q
+  auto buf = [&](int b) { return mref(W + (long long)b * MB, 12 * MB, 0, n); };
+  {
+    std::vector<zd> tmp((size_t)batch * 12 * MB);
+    const double *srcs[3] = {ml, m0, mr};
+    for (int q = 0; q < 3; q++)
+      for (int m = 0; m < batch; m++)
+        for (int c = 0; c < n; c++)
+          for (int r = 0; r < n; r++) {
+            size_t si = ((size_t)m * ld * ld + r + (size_t)c * ld) * 2;
+            tmp[(size_t)m * 12 * MB + q * MB + r + (size_t)c * n] = zmk(srcs[q][si], srcs[q][si + 1]);
+          }
+    CK(cudaMemcpy(W, tmp.data(), tmp.size() * sizeof(zd), cudaMemcpyHostToDevice));
+  }
+  int *act = flags, *st = flags + batch, *it = flags + 2 * batch;
+  std::vector<int> ones(batch, 1);
+  CK(cudaMemcpy(act, ones.data(), batch * sizeof(int), cudaMemcpyHostToDevice));
+  CK(cudaMemset(st, 0, batch * sizeof(int)));
+  CK(cudaMemset(it, 0, batch * sizeof(int)));
+  MatRef Ml = buf(0), M0 = buf(1), Mr = buf(2), eps = buf(3), a0 = buf(4), a1 = buf(5), b0 = buf(6),
+         b1 = buf(7), X = buf(8), y1 = buf(9), P = buf(10), Q = buf(11);
+  launch_zaxpby(eps, M0, nullptr, 0, nullptr, 0, n, batch, 1, nullptr, 0);
+  launch_zaxpby(X, M0, nullptr, 0, nullptr, 0, n, batch, 1, nullptr, 0);
+  launch_zaxpby(a0, Ml, &Ml, -2.0, nullptr, 0, n, batch, 1, nullptr, 0);
+  launch_zaxpby(b0, Mr, &Mr, -2.0, nullptr, 0, n, batch, 1, nullptr, 0);
+  for (int iter = 1;; iter++) {
+    MatRef &ac = (iter & 1) ? a0 : a1, &an = (iter & 1) ? a1 : a0;
+    MatRef &bc = (iter & 1) ? b0 : b1, &bn = (iter & 1) ? b1 : b0;
+    launch_zaxpby(y1, eps, nullptr, 0, nullptr, 0, n, batch, 1, act, 0);
+    launch_zgj(y1, n, batch, 1, act, 0);
+    launch_zgemm(0, ac, y1, P, P, P, n, n, n, batch, 1, act, 0);
+    launch_zgemm(0, bc, y1, Q, Q, Q, n, n, n, batch, 1, act, 0);
+    launch_zgemm(0, P, ac, an, an, an, n, n, n, batch, 1, act, 0);
+    launch_zgemm(0, Q, bc, bn, bn, bn, n, n, n, batch, 1, act, 0);
+    launch_zgemm(2, P, bc, P, eps, X, n, n, n, batch, 1, act, 0);
+    launch_zgemm(1, Q, ac, eps, eps, eps, n, n, n, batch, 1, act, 0);
+    launch_fnorm(an, n, batch, 1, act, err, 0);
+    launch_dec_state(err, act, st, it, batch, iter, itermax, errmax, 0);
+    std::vector<int> h(batch);
+    CK(cudaMemcpy(h.data(), act, batch * sizeof(int), cudaMemcpyDeviceToHost));
+    int any = 0;
+    for (int v : h) any |= v;
+    if (!any || iter > itermax + 1) break;
+  }
+  launch_zgj(X, n, batch, 1, nullptr, 0);
+  CK(cudaDeviceSynchronize());
+  CK(cudaGetLastError());
+  if (iters) CK(cudaMemcpy(iters, it, batch * sizeof(int), cudaMemcpyDeviceToHost));
+  if (stat) CK(cudaMemcpy(stat, st, batch * sizeof(int), cudaMemcpyDeviceToHost));
+  {
+    std::vector<zd> tmp((size_t)batch * 12 * MB);
+    CK(cudaMemcpy(tmp.data(), W, tmp.size() * sizeof(zd), cudaMemcpyDeviceToHost));
+    for (int m = 0; m < batch; m++)
+      for (int c = 0; c < n; c++)
+        for (int r = 0; r < n; r++) {
+          zd v = tmp[(size_t)m * 12 * MB + 8 * MB + r + (size_t)c * n];
+          size_t d = ((size_t)m * ld * ld + r + (size_t)c * ld) * 2;
+          x[d] = v.x;
+          x[d + 1] = v.y;
+        }
+  }
+  return SKKR_OK;
+}
+
+// rsp-scf/phystau.f / nrsp-scf/phystau.f on the device
+__global__ void k_phys_mats(const zd *tinv, const zd *alpha, const int *lof, int nd, zd *lmat,
+                            zd *rmat, zd *cmat) {
+  for (int e = threadIdx.x + blockIdx.x * blockDim.x; e < nd * nd; e += blockDim.x * gridDim.x) {
+    const int a = e % nd, b = e / nd;
+    zd al = alpha[lof[a]], alp = alpha[lof[b]], t = tinv[e];
+    zd lv = zmul(al, t), rv = zmul(t, alp), cv = zmul(zmul(al, t), alp);
+    if (a == b) {
+      lv.x += 1.0;
+      rv.x += 1.0;
+      cv = zadd(al, cv);
+    }
+    lmat[e] = lv;
+    rmat[e] = rv;
+    cmat[e] = cv;
+  }
+}
+
+extern "C" int skkr_gpu_phystau(int mode, int lmax, double *tau, const double *tinv,
+                                const double *alpha, int ld) {
+  if (!tau || !tinv || !alpha || lmax < 0 || lmax > 3) return SKKR_ERR_ARG;
+  const int lmmax = (lmax + 1) * (lmax + 1), nd = mode == SKKR_REL ? 2 * lmmax : lmmax;
+  if (ld < nd) return SKKR_ERR_ARG;
+  std::vector<int> lof(nd);
+  if (mode == SKKR_REL) {
+    int k = 0;  // ldex of rsp-scf/phystau.f: 2 entries for l=0, 4l+2 for l>0
+    for (int l = 0; k < nd; l++)
+      for (int q = 0; q < (l == 0 ? 2 : 4 * l + 2) && k < nd; q++) lof[k++] = l;
+  } else {
+    for (int l = 0, k = 0; l <= lmax; l++)
+      for (int m = -l; m <= l; m++) lof[k++] = l;
+  }
+  const long long MB = (long long)nd * nd;
+  Scoped s;
+  zd *T, *Ti, *Al, *Lm, *Rm, *Cm, *H;
+  int *Lo;
+  CKR(s.alloc(&T, MB));
+  CKR(s.alloc(&Ti, MB));
+  CKR(s.alloc(&Al, lmax + 1));
+  CKR(s.alloc(&Lm, MB));
+  CKR(s.alloc(&Rm, MB));
+  CKR(s.alloc(&Cm, MB));
+  CKR(s.alloc(&H, MB));
+  CKR(s.alloc(&Lo, nd));
+  CKR(upload_mats(T, tau, 1, nd, ld));
+  CKR(upload_mats(Ti, tinv, 1, nd, ld));
+  CK(cudaMemcpy(Al, alpha, (lmax + 1) * sizeof(zd), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(Lo, lof.data(), nd * sizeof(int), cudaMemcpyHostToDevice));
+  k_phys_mats<<<4, 256>>>(Ti, Al, Lo, nd, Lm, Rm, Cm);
+  SKKR_LAUNCHED();
+  // tripmt(lmat, tau, rmat): (lmat tau) rmat ; then tau - cmat
+  launch_zgemm(0, mref(Lm, 0, 0, nd), mref(T, 0, 0, nd), mref(H, 0, 0, nd), mref(H, 0, 0, nd),
+               mref(H, 0, 0, nd), nd, nd, nd, 1, 1, nullptr, 0);
+  launch_zgemm(0, mref(H, 0, 0, nd), mref(Rm, 0, 0, nd), mref(T, 0, 0, nd), mref(T, 0, 0, nd),
+               mref(T, 0, 0, nd), nd, nd, nd, 1, 1, nullptr, 0);
+  MatRef Tm = mref(T, 0, 0, nd), Cmm = mref(Cm, 0, 0, nd);
+  launch_zaxpby(Tm, Tm, &Cmm, -1.0, nullptr, 0, nd, 1, 1, nullptr, 0);
+  CK(cudaDeviceSynchronize());
+  CK(cudaGetLastError());
+  return download_mats(tau, T, 1, nd, ld);
+}

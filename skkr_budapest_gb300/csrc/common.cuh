@@ -1,0 +1,69 @@
+// Shared device helpers of the 2D-BZ tau library.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+
+typedef double2 zd;  // complex*16, interleaved re/im
+
+__host__ __device__ inline zd zmk(double r, double i) { return make_double2(r, i); }
+__device__ inline zd zadd(zd a, zd b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ inline zd zsub(zd a, zd b) { return make_double2(a.x - b.x, a.y - b.y); }
+__device__ inline zd zmul(zd a, zd b) { return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+__device__ inline zd zscale(double s, zd a) { return make_double2(s * a.x, s * a.y); }
+__device__ inline double zabs2(zd a) { return a.x * a.x + a.y * a.y; }
+// c += a*b (four FMAs, real part first)
+__device__ inline void zfma(zd &c, zd a, zd b) {
+  c.x = fma(a.x, b.x, c.x);
+  c.x = fma(-a.y, b.y, c.x);
+  c.y = fma(a.x, b.y, c.y);
+  c.y = fma(a.y, b.x, c.y);
+}
+// 1/q by Smith's scaled division
+__device__ inline zd zrecip(zd q) {
+  if (fabs(q.x) >= fabs(q.y)) {
+    double r = q.y / q.x, den = q.x + q.y * r;
+    return make_double2(1.0 / den, -r / den);
+  }
+  double r = q.x / q.y, den = q.x * r + q.y;
+  return make_double2(r / den, -1.0 / den);
+}
+
+#define SKKR_MAPN 16
+
+// A batch operand: matrix of item (k, c) starts at base + k*sk + map[c]*sc,
+// column-major with leading dimension ld.
+struct MatRef {
+  zd *base;
+  long long sk;
+  long long sc;
+  int ld;
+  int map[SKKR_MAPN];
+};
+
+__device__ inline zd *mat_ptr(const MatRef &m, int k, int c) {
+  return m.base + (long long)k * m.sk + (long long)m.map[c] * m.sc;
+}
+
+// host-side constructors
+inline MatRef mref(zd *base, long long sk, long long sc, int ld) {
+  MatRef r;
+  r.base = base;
+  r.sk = sk;
+  r.sc = sc;
+  r.ld = ld;
+  for (int i = 0; i < SKKR_MAPN; i++) r.map[i] = i;
+  return r;
+}
+inline MatRef mref_map(zd *base, long long sk, long long sc, int ld, const int *map, int nmap) {
+  MatRef r = mref(base, sk, sc, ld);
+  for (int i = 0; i < nmap && i < SKKR_MAPN; i++) r.map[i] = map[i];
+  return r;
+}
+
+// kernel launch bookkeeping (defined in capi.cu).  With SKKR_SYNC_CHECK=1 in
+// the environment every launch is followed by a device synchronisation and
+// the first failing launch site is recorded (diagnostics only).
+extern long long g_skkr_launches;
+void skkr_after_launch(const char *file, int line);
+#define SKKR_LAUNCHED() skkr_after_launch(__FILE__, __LINE__)

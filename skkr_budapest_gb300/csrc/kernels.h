@@ -1,0 +1,53 @@
+// Host launch wrappers of the batched device kernels.
+#pragma once
+#include "common.cuh"
+
+// G_scr(k): out[(k*nblk + b)] lm x lm blocks (column-major, ld = lmmax)
+void launch_gk_ft(const zd *gR, const double *rvec, const int *rstart, int nblk, int lmmax,
+                  const double *xk, int nk, zd *out, cudaStream_t st);
+
+// packer.f jobs: one n x n matrix per (k, job)
+struct PackJob {
+  int slot, ni, nim, nip;
+  int which;  // 0: M00, 1: M10 (M0-1), 2: M01
+  int dest;   // matrix index in the per-k pool
+};
+cudaError_t pack_set_tables(int irel, int lmax);
+void launch_pack(const zd *G, int nblk, const int *d_blkmap, int mi, int jmax, const PackJob *d_jobs,
+                 int njobs, int lk, int lmmax, int irel, zd fac, int nk, zd *pool, int nmat, int npl,
+                 cudaStream_t st);
+
+// batched complex GEMM, items (k, c) with k < nk, c < nc; act[k*nc+c]==0 skips.
+// mode 0: C = A*B        1: C = C - A*B
+// mode 2: y = A*B ; D -= y ; E -= y  (C unused)
+// mode 3: C = D - A*B
+void launch_zgemm(int mode, const MatRef &A, const MatRef &B, const MatRef &C, const MatRef &D,
+                  const MatRef &E, int m, int n, int kdim, int nk, int nc, const int *act,
+                  cudaStream_t st);
+
+// in-place Gauss-Jordan inverses (gjinv.f), one CTA per item
+void launch_zgj(const MatRef &A, int n, int nk, int nc, const int *act, cudaStream_t st);
+
+// elementwise: out = a + s1*b + s2*d over n x n (b/d may be null)
+void launch_zaxpby(const MatRef &out, const MatRef &a, const MatRef *b, double s1, const MatRef *d,
+                   double s2, int n, int nk, int nc, const int *act, cudaStream_t st);
+// out = in + block-diagonal t (nl layers of lk x lk, t base from tref for item)
+void launch_add_tblocks(const MatRef &out, const MatRef &in, const MatRef &t, int lk, int nl,
+                        int n, int nk, int nc, const int *act, cudaStream_t st);
+// Frobenius norms of items -> out[k*nc+c]
+void launch_fnorm(const MatRef &a, int n, int nk, int nc, const int *act, double *out,
+                  cudaStream_t st);
+// decimation state update (surfgf.f:81-96)
+void launch_dec_state(const double *err, int *act, int *stat, int *iters, int nitems, int iter,
+                      int itermax, double errmax, cudaStream_t st);
+// tau(k) diagonal-block extraction: out[k][c][layer] = (wk[k]*wscale) * W(layer block)
+void launch_extract_tau(const MatRef &W, int lk, int nl, int layer0, const double *wk,
+                        double wscale, zd *out, long long out_sk, long long out_sc, int nk,
+                        int nc, cudaStream_t st);
+// deterministic k-sum (warp-shuffle): S[e] (+)= sum_k tk[k*E + e]
+void launch_ksum(const zd *tk, int nk, long long E, zd *S, int accumulate, cudaStream_t st);
+// sum over g of T[layer][g] -> out[layer]
+void launch_gsum(const zd *T, int ng, int lk, int nl, zd *out, cudaStream_t st);
+// CPA helpers
+void launch_cpa_mix(const zd *X, const double *conc, const int *act, int lk, int nl, zd *xc,
+                    cudaStream_t st);

@@ -1,0 +1,148 @@
+"""ctypes binding of the C ABI in include/skkr_gpu.h (libskkr_gpu.so).
+
+There is no fallback: if the CUDA library is missing or no device is
+present, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libskkr_gpu.so")
+
+SKKR_MAX_PRC = 16
+NONREL, REL = 0, 1
+FP64, MIXED = 0, 1
+ERRORS = {0: "ok", -1: "bad argument", -2: "CUDA error", -3: "decimation hit itermax",
+          -4: "decimation diverged (error > 1e10)", -5: "unsupported input", -6: "out of device memory",
+          -7: "non-finite result"}
+
+I, D, P = C.c_int, C.c_double, C.c_void_p
+
+
+class Sizes(C.Structure):
+    _fields_ = [("mode", I), ("lmax", I), ("nprc", I), ("ninprc", I * (SKKR_MAX_PRC + 2)),
+                ("bulkgeo", I), ("ngeff", I), ("itermaxl", I), ("itermaxr", I), ("errmax", D),
+                ("itcpam", I), ("cpatol", D), ("precision", I), ("nk_chunk", I)]
+
+
+class RTable(C.Structure):
+    _fields_ = [("nblk", I), ("nr", I), ("rstart", P), ("rvec", P), ("gR", P), ("nslot", I),
+                ("mi", I), ("jmax", I), ("blkmap", P)]
+
+
+class Status(C.Structure):
+    _fields_ = [("code", I), ("ik", I), ("cpa_iterations", I), ("cpa_error", D),
+                ("max_dec_iters", I), ("dec_iters_total", C.c_longlong),
+                ("gpu_launches", C.c_longlong), ("max_refine_resid", D)]
+
+
+class SkkrError(RuntimeError):
+    def __init__(self, code, where=""):
+        msg = "%s: %s (%d)" % (where, ERRORS.get(code, "error"), code)
+        if code == -2:
+            msg += ": " + last_error()
+        super().__init__(msg)
+        self.code = code
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libskkr_gpu.so not built (run __graft_entry__.build()); "
+                               "there is no CPU fallback")
+        L = C.CDLL(LIB_PATH)
+        L.skkr_gpu_create.argtypes = [P, P]
+        L.skkr_gpu_destroy.argtypes = [P]
+        L.skkr_gpu_stage.argtypes = [P, D, D, D, D, P, I, P, P, P, P, P, P, P, P, P, P, I]
+        L.skkr_gpu_run.argtypes = [P, P]
+        L.skkr_gpu_fetch.argtypes = [P, P, P, P, P, I]
+        L.skkr_gpu_cpacoord.argtypes = [P, D, D, D, D, P, I, P, P, P, P, P, P, P, P, P, P, P, P, P, I, P]
+        L.skkr_gpu_phystau.argtypes = [I, I, P, P, P, I]
+        L.skkr_gpu_gjinv_batch.argtypes = [I, I, P, I]
+        L.skkr_gpu_surfgf_batch.argtypes = [I, I, P, P, P, P, I, I, D, P, P]
+        L.skkr_gpu_gk.argtypes = [P, I, I, P, P]
+        L.skkr_gpu_last_error.restype = C.c_char_p
+        _lib = L
+    return _lib
+
+
+def last_error() -> str:
+    return lib().skkr_gpu_last_error().decode()
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def cm(a):
+    """(..., n, n) [row, col] -> column-major complex128 copy."""
+    return np.array(np.swapaxes(np.asarray(a, np.complex128), -1, -2), order="C", copy=True)
+
+
+def uncm(a):
+    return np.ascontiguousarray(np.swapaxes(a, -1, -2))
+
+
+def _check(rc, where):
+    if rc != 0:
+        raise SkkrError(rc, where)
+
+
+class RTableHolder:
+    """Keeps the numpy buffers of an skkr_rtable alive."""
+
+    def __init__(self, rt, blkmap):
+        self.rstart = np.ascontiguousarray(rt.rstart, np.int32)
+        self.rvec = np.ascontiguousarray(rt.rvec, np.float64)
+        self.gR = cm(rt.gR)
+        self.blkmap = np.ascontiguousarray(blkmap, np.int32)
+        ns, mi, nj = self.blkmap.shape
+        self.s = RTable(rt.nblk, len(self.rvec), _p(self.rstart), _p(self.rvec), _p(self.gR), ns, mi,
+                        (nj - 1) // 2, _p(self.blkmap))
+
+    def ptr(self):
+        return C.cast(C.pointer(self.s), C.c_void_p)
+
+
+def gjinv_batch(a):
+    a = np.asarray(a, np.complex128)
+    b, n, _ = a.shape
+    buf = cm(a)
+    _check(lib().skkr_gpu_gjinv_batch(n, b, _p(buf), n), "skkr_gpu_gjinv_batch")
+    return uncm(buf)
+
+
+def surfgf_batch(ml, m0, mr, itermax=50, errmax=1e-8):
+    b, n, _ = m0.shape
+    bl, b0, br = cm(ml), cm(m0), cm(mr)
+    x = np.zeros_like(b0)
+    it = np.zeros(b, np.int32)
+    st = np.zeros(b, np.int32)
+    _check(lib().skkr_gpu_surfgf_batch(n, b, _p(bl), _p(b0), _p(br), _p(x), n, itermax, errmax, _p(it),
+                                       _p(st)), "skkr_gpu_surfgf_batch")
+    return uncm(x), st, it
+
+
+def gk(rt, blkmap, lmax, xk):
+    h = RTableHolder(rt, blkmap)
+    xk = np.ascontiguousarray(xk, np.float64)
+    lm = (lmax + 1) ** 2
+    out = np.zeros((len(xk), rt.nblk, lm, lm), np.complex128)
+    _check(lib().skkr_gpu_gk(h.ptr(), lmax, len(xk), _p(xk), _p(out)), "skkr_gpu_gk")
+    return uncm(out)
+
+
+def phystau(tau, tinv, alpha, lmax, irel):
+    t = cm(tau)
+    ti = cm(tinv)
+    al = np.ascontiguousarray(alpha, np.complex128)
+    _check(lib().skkr_gpu_phystau(irel, lmax, _p(t), _p(ti), _p(al), t.shape[-1]), "skkr_gpu_phystau")
+    return uncm(t)

@@ -1,0 +1,52 @@
+"""The C-ABI library loads and exports every entry point include/skkr_gpu.h
+declares (CPU only: no compute call)."""
+import ctypes
+import os
+import re
+
+from skkr_budapest_gb300 import native
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    hdr = open(os.path.join(ROOT, "include", "skkr_gpu.h")).read()
+    hdr = re.sub(r"/\*.*?\*/", "", hdr, flags=re.S)
+    return sorted(set(re.findall(r"\b(skkr_gpu_\w+)\s*\(", hdr)))
+
+
+def test_library_exports_every_declared_symbol():
+    import __graft_entry__
+    __graft_entry__.build()
+    lib = ctypes.CDLL(native.LIB_PATH)
+    syms = declared_symbols()
+    assert len(syms) >= 10
+    missing = [s for s in syms if not hasattr(lib, s)]
+    assert not missing, missing
+
+
+def test_struct_layouts_match_header(tmp_path):
+    # compile a probe against the header and compare sizes/offsets with ctypes
+    import subprocess
+    src = tmp_path / "probe.c"
+    src.write_text(
+        '#include <stdio.h>\n#include <stddef.h>\n#include "skkr_gpu.h"\n'
+        'int main(void){printf("%zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(skkr_sizes),'
+        ' offsetof(skkr_sizes, errmax), offsetof(skkr_sizes, cpatol), offsetof(skkr_sizes, nk_chunk),'
+        ' sizeof(skkr_rtable), offsetof(skkr_rtable, blkmap), sizeof(skkr_status),'
+        ' offsetof(skkr_status, max_refine_resid)); return 0;}\n')
+    exe = tmp_path / "probe"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True).stdout.split()]
+    S, R, T = native.Sizes, native.RTable, native.Status
+    want = [ctypes.sizeof(S), S.errmax.offset, S.cpatol.offset, S.nk_chunk.offset, ctypes.sizeof(R),
+            R.blkmap.offset, ctypes.sizeof(T), T.max_refine_resid.offset]
+    assert got == want
+
+
+def test_no_cpu_fallback_when_library_missing(monkeypatch, tmp_path):
+    monkeypatch.setattr(native, "LIB_PATH", str(tmp_path / "missing.so"))
+    monkeypatch.setattr(native, "_lib", None)
+    import pytest
+    with pytest.raises(RuntimeError):
+        native.lib()
