@@ -90,6 +90,7 @@ typedef struct {
   long long dec_iters_total;  /* summed decimation iterations */
   long long gpu_launches;     /* kernels launched by this call */
   double max_refine_resid;    /* mixed precision: largest final refinement residual */
+  double run_ms;              /* device time of the call (CUDA events on the library stream) */
 } skkr_status;
 
 typedef struct skkr_ctx skkr_ctx;
@@ -135,6 +136,26 @@ int skkr_gpu_stage(skkr_ctx *ctx, double ce_re, double ce_im, double fac_re,
 int skkr_gpu_run(skkr_ctx *ctx, skkr_status *status);
 int skkr_gpu_fetch(skkr_ctx *ctx, double *tminv, double *tauc, double *taua,
                    double *taub, int ld);
+
+/* The same split form for several energies kept resident at once: each
+ * `slot` (0, 1, ...) holds one staged energy's inputs and results; the work
+ * buffers of the context are shared, so slots cost only their inputs. */
+int skkr_gpu_stage_slot(skkr_ctx *ctx, int slot, double ce_re, double ce_im,
+                        double fac_re, double fac_im, const skkr_rtable *rt,
+                        int nk, const double *xk, const double *wk,
+                        const double *lg, const double *rg, const double *conc,
+                        const double *tminvl, const double *tminvr,
+                        const double *tminv, const double *tminva,
+                        const double *tminvb, int ld);
+int skkr_gpu_run_slot(skkr_ctx *ctx, int slot, skkr_status *status);
+int skkr_gpu_fetch_slot(skkr_ctx *ctx, int slot, double *tminv, double *tauc,
+                        double *taua, double *taub, int ld);
+
+/* Per-kernel-class timing with CUDA events (process wide).  enable=1 resets
+ * and starts; enable=0 stops and writes out[cls*3 + {launches, total ms,
+ * algorithmic work}] for cls = 0 complex GEMM (FLOP), 1 Gauss-Jordan
+ * inverse (FLOP), 2 G(k) transform (bytes written), 3 other. */
+int skkr_gpu_kernel_stats(int enable, double *out);
 
 /* Screened -> physical tau of one layer on the device
  * (rsp-scf/phystau.f:2-61, nrsp-scf/phystau.f): tau := (1+a t)tau(1+t a) - (a + a t a). */

@@ -94,6 +94,35 @@ class Context:
         N._check(rc, "skkr_gpu_fetch")
         return {k: N.uncm(v) for k, v in out.items()}
 
+    # -- several energies resident at once -----------------------------------
+    def stage_slot(self, slot, ep, tminv=None):
+        rt, a = self._host_inputs(ep, tminv)
+        if not hasattr(self, "_slot_keep"):
+            self._slot_keep = {}
+        self._slot_keep[slot] = (rt, a)
+        p = N._p
+        rc = N.lib().skkr_gpu_stage_slot(self.h, slot, ep.ce.real, ep.ce.imag, ep.fac.real, ep.fac.imag,
+                                         rt.ptr(), len(a["xk"]), p(a["xk"]), p(a["wk"]), p(a["lg"]),
+                                         p(a["rg"]), p(a["conc"]), p(a["tl"]), p(a["tr"]), p(a["ti"]),
+                                         p(a["ta"]), p(a["tb"]), self.lk)
+        N._check(rc, "skkr_gpu_stage_slot")
+
+    def run_slot(self, slot, check=True):
+        st = N.Status()
+        rc = N.lib().skkr_gpu_run_slot(self.h, slot, C.cast(C.pointer(st), C.c_void_p))
+        if check:
+            N._check(rc, "skkr_gpu_run_slot")
+        return st
+
+    def fetch_slot(self, slot):
+        n, lk = self.nintfc, self.lk
+        out = {k: np.zeros((n, lk, lk), np.complex128) for k in ("tminv", "tauc", "taua", "taub")}
+        p = N._p
+        rc = N.lib().skkr_gpu_fetch_slot(self.h, slot, p(out["tminv"]), p(out["tauc"]), p(out["taua"]),
+                                         p(out["taub"]), lk)
+        N._check(rc, "skkr_gpu_fetch_slot")
+        return {k: N.uncm(v) for k, v in out.items()}
+
     # -- one call, host buffers in and out (the drop-in form) ---------------
     def cpacoord(self, ep, tminv=None, check=True):
         rt, a = self._host_inputs(ep, tminv)
@@ -112,7 +141,9 @@ class Context:
         res["tminv"] = N.uncm(a["ti"])
         res.update(status=rc, cpa_iterations=st.cpa_iterations, cpa_error=st.cpa_error,
                    max_dec_iters=st.max_dec_iters, dec_iters_total=st.dec_iters_total,
-                   gpu_launches=st.gpu_launches, ik=st.ik)
+                   gpu_launches=st.gpu_launches, ik=st.ik, run_ms=st.run_ms,
+                   h2d_bytes=sum(v.nbytes for v in a.values()) + rt.gR.nbytes + rt.rvec.nbytes,
+                   d2h_bytes=sum(v.nbytes for v in out.values()))
         return res
 
 

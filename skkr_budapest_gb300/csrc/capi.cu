@@ -39,6 +39,71 @@ static thread_local std::string g_last_error;
 extern "C" const char *skkr_gpu_last_error(void) { return g_last_error.c_str(); }
 
 static int g_sync_check = -1;
+// ---- per-kernel-class event timing --------------------------------------
+namespace {
+struct KStats {
+  int on = 0;
+  std::vector<cudaEvent_t> ev;
+  size_t used = 0;
+  std::vector<int> cls;
+  std::vector<double> work;
+  int open = 0;
+};
+KStats g_ks;
+long long g_active_hint = -1;
+}  // namespace
+
+void skkr_set_active_items(long long n) { g_active_hint = n; }
+long long skkr_active_items(long long all) { return g_active_hint >= 0 ? g_active_hint : all; }
+
+void kstat_begin(int cls, double work, cudaStream_t st) {
+  if (!g_ks.on) return;
+  if (g_ks.used + 2 > g_ks.ev.size()) {
+    for (int i = 0; i < 256; i++) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      g_ks.ev.push_back(e);
+    }
+  }
+  cudaEventRecord(g_ks.ev[g_ks.used], st);
+  g_ks.cls.push_back(cls);
+  g_ks.work.push_back(work);
+  g_ks.open = 1;
+}
+
+void kstat_end(cudaStream_t st) {
+  if (!g_ks.on || !g_ks.open) return;
+  cudaEventRecord(g_ks.ev[g_ks.used + 1], st);
+  g_ks.used += 2;
+  g_ks.open = 0;
+}
+
+// enable=1: reset and start; enable=0: stop and report out[cls*3 + {0 launches,
+// 1 total ms, 2 total algorithmic work}] for the KS_NCLS classes.
+extern "C" int skkr_gpu_kernel_stats(int enable, double *out) {
+  if (enable) {
+    g_ks.on = 1;
+    g_ks.used = 0;
+    g_ks.cls.clear();
+    g_ks.work.clear();
+    return SKKR_OK;
+  }
+  g_ks.on = 0;
+  CK(cudaDeviceSynchronize());
+  if (out)
+    for (int i = 0; i < KS_NCLS * 3; i++) out[i] = 0.0;
+  for (size_t i = 0; i < g_ks.cls.size() && 2 * i + 1 < g_ks.used + 1; i++) {
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, g_ks.ev[2 * i], g_ks.ev[2 * i + 1]));
+    if (out) {
+      out[g_ks.cls[i] * 3 + 0] += 1.0;
+      out[g_ks.cls[i] * 3 + 1] += ms;
+      out[g_ks.cls[i] * 3 + 2] += g_ks.work[i];
+    }
+  }
+  return SKKR_OK;
+}
+
 static void trace_point(const char *what) {
   if (g_sync_check != 1) return;
   cudaError_t e = cudaPeekAtLastError();
@@ -124,7 +189,47 @@ struct skkr_ctx {
   long long tot_dec = 0;
   int first_bad_k = -1;
   int err_code = 0;
+  std::vector<struct SlotStore *> slots;
 };
+
+// Inputs and outputs of one staged energy.  A context keeps any number of
+// them resident on the device (skkr_gpu_stage_slot); run/fetch swap a slot
+// into the working fields, so the per-energy work buffers are shared.
+struct SlotStore {
+  DBuf gR, rvec, rstart, blkmap_d, xk, wk, lg, rg, conc, tcat, tab, tauc, cpa;
+  int staged = 0, nk = 0, nblk = 0, nrt = 0, nslot = 0, mi = 0, jmax = 0, maxr = 0;
+  zd fac = {0, 0}, ce = {0, 0};
+  std::vector<int> blkmap;
+  std::vector<double> conc_h;
+};
+
+static void swap_slot(skkr_ctx *c, SlotStore &s) {
+  std::swap(c->gR, s.gR);
+  std::swap(c->rvec, s.rvec);
+  std::swap(c->rstart, s.rstart);
+  std::swap(c->blkmap_d, s.blkmap_d);
+  std::swap(c->xk, s.xk);
+  std::swap(c->wk, s.wk);
+  std::swap(c->lg, s.lg);
+  std::swap(c->rg, s.rg);
+  std::swap(c->conc, s.conc);
+  std::swap(c->tcat, s.tcat);
+  std::swap(c->tab, s.tab);
+  std::swap(c->tauc, s.tauc);
+  std::swap(c->cpa, s.cpa);
+  std::swap(c->staged, s.staged);
+  std::swap(c->nk, s.nk);
+  std::swap(c->nblk, s.nblk);
+  std::swap(c->nrt, s.nrt);
+  std::swap(c->nslot, s.nslot);
+  std::swap(c->mi, s.mi);
+  std::swap(c->jmax, s.jmax);
+  std::swap(c->maxr, s.maxr);
+  std::swap(c->fac, s.fac);
+  std::swap(c->ce, s.ce);
+  std::swap(c->blkmap, s.blkmap);
+  std::swap(c->conc_h, s.conc_h);
+}
 
 // ---------------------------------------------------------------------------
 extern "C" int skkr_gpu_create(const skkr_sizes *sizes, skkr_ctx **out) {
@@ -173,6 +278,12 @@ extern "C" int skkr_gpu_destroy(skkr_ctx *c) {
                  &c->pool, &c->jobs, &c->dec, &c->decf, &c->deci, &c->tauw, &c->tauk, &c->S,
                  &c->T1, &c->T2, &c->tauc, &c->cpa, &c->cpan, &c->cpaact};
   for (DBuf *b : all) b->release();
+  for (SlotStore *sl : c->slots) {
+    DBuf *sb[] = {&sl->gR, &sl->rvec, &sl->rstart, &sl->blkmap_d, &sl->xk, &sl->wk, &sl->lg,
+                  &sl->rg, &sl->conc, &sl->tcat, &sl->tab, &sl->tauc, &sl->cpa};
+    for (DBuf *b : sb) b->release();
+    delete sl;
+  }
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
   return SKKR_OK;
@@ -506,6 +617,7 @@ static int run_decimation(skkr_ctx *c, int k0, int nkc, const std::vector<int> &
   }
   const int itermax = std::max(c->sz.itermaxl, c->sz.itermaxr);
   int iter = 1;
+  skkr_set_active_items(nit);
   for (;; iter++) {
     MatRef &ac = (iter & 1) ? a0 : a1, &an = (iter & 1) ? a1 : a0;
     MatRef &bc = (iter & 1) ? b0 : b1, &bn = (iter & 1) ? b1 : b0;
@@ -525,10 +637,16 @@ static int run_decimation(skkr_ctx *c, int k0, int nkc, const std::vector<int> &
       std::vector<int> h(nit);
       CK(cudaMemcpyAsync(h.data(), act, nit * sizeof(int), cudaMemcpyDeviceToHost, st));
       CK(cudaStreamSynchronize(st));
-      for (int v : h) any |= v;
+      long long cnt = 0;
+      for (int v : h) {
+        any |= v;
+        cnt += v;
+      }
+      skkr_set_active_items(cnt);
     }
     if (!any || iter > itermax + 1) break;
   }
+  skkr_set_active_items(-1);
   // statuses
   {
     std::vector<int> hs(nit), hi(nit);
@@ -710,6 +828,7 @@ static int cpa_step(skkr_ctx *c, int *itcpa, int *cpacon, int *concpa, double *e
     MatRef mc2 = mref(mc, lk2, 0, lk), tab2 = mref(c->tab.as<zd>(), 2LL * lk2, lk2, lk);
     (void)Dd;
     // da = mc - ma ; db = mc - mb ; xa = da ; xb = db   (cpasol.f:94-99)
+    skkr_set_active_items(2LL * nalloy);
     launch_zaxpby(Dm, mc2, &tab2, -1.0, nullptr, 0, lk, ni, 2, dact2, st);
     launch_zaxpby(Xm, Dm, nullptr, 0, nullptr, 0, lk, ni, 2, dact2, st);
     launch_zgj(Xm, lk, ni, 2, dact2, st);
@@ -718,6 +837,7 @@ static int cpa_step(skkr_ctx *c, int *itcpa, int *cpacon, int *concpa, double *e
     // xc = c xa + (1-c) xb ; h = (xc^-1 + tauc)^-1 ; mc -= h   (:109-124)
     MatRef Hm = mref(H, lk2, 0, lk), mc1 = mref(mc, lk2, 0, lk), tauc1 = mref(tauc, lk2, 0, lk);
     launch_cpa_mix(X, c->conc.as<double>(), dact, lk, ni, H, st);
+    skkr_set_active_items(nalloy);
     launch_zgj(Hm, lk, ni, 1, dact, st);
     launch_zaxpby(Hm, Hm, &tauc1, 1.0, nullptr, 0, lk, ni, 1, dact, st);
     launch_zgj(Hm, lk, ni, 1, dact, st);
@@ -727,10 +847,12 @@ static int cpa_step(skkr_ctx *c, int *itcpa, int *cpacon, int *concpa, double *e
     launch_fnorm(Hm, lk, ni, 1, dact, nrm, st);
     launch_fnorm(mc1, lk, ni, 1, dact, nrm + ni, st);
     // tau_A = tauc + tauc xa tauc ; tau_B likewise (:145-150)
+    skkr_set_active_items(2LL * nalloy);
     MatRef Tmm = mref(Tm, 2LL * lk2, lk2, lk);
     launch_zgemm(0, tauc2, Xm, Tmm, Tmm, Tmm, lk, lk, lk, ni, 2, dact2, st);
     launch_zgemm(0, Tmm, tauc2, TABm, TABm, TABm, lk, lk, lk, ni, 2, dact2, st);
     launch_zaxpby(TABm, TABm, &tauc2, 1.0, nullptr, 0, lk, ni, 2, dact2, st);
+    skkr_set_active_items(-1);
     std::vector<double> hn2(2 * ni);
     CK(cudaMemcpyAsync(hn2.data(), nrm, 2 * ni * sizeof(double), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
@@ -750,6 +872,10 @@ static int cpa_step(skkr_ctx *c, int *itcpa, int *cpacon, int *concpa, double *e
 extern "C" int skkr_gpu_run(skkr_ctx *c, skkr_status *status) {
   if (!c || !c->staged) return SKKR_ERR_ARG;
   const long long l0 = g_skkr_launches;
+  cudaEvent_t ev0, ev1;
+  CK(cudaEventCreate(&ev0));
+  CK(cudaEventCreate(&ev1));
+  CK(cudaEventRecord(ev0, c->st));
   const int n = c->n, lk = c->lk, lk2 = lk * lk, ni = c->nintfc, nk = c->nk;
   const long long MB = (long long)n * n;
   const size_t bs = (size_t)c->lmmax * c->lmmax;
@@ -840,8 +966,13 @@ extern "C" int skkr_gpu_run(skkr_ctx *c, skkr_status *status) {
     if (!(concpa && cpacon)) break;
   }
   trace_point("after CPA loop");
+  CK(cudaEventRecord(ev1, st));
   CK(cudaStreamSynchronize(st));
   CK(cudaGetLastError());
+  float run_ms = 0.f;
+  CK(cudaEventElapsedTime(&run_ms, ev0, ev1));
+  cudaEventDestroy(ev0);
+  cudaEventDestroy(ev1);
   if (status) {
     status->code = c->err_code;
     status->ik = c->first_bad_k;
@@ -851,6 +982,7 @@ extern "C" int skkr_gpu_run(skkr_ctx *c, skkr_status *status) {
     status->dec_iters_total = c->tot_dec;
     status->gpu_launches = g_skkr_launches - l0;
     status->max_refine_resid = 0.0;
+    status->run_ms = run_ms;
   }
   return c->err_code;
 }
@@ -884,6 +1016,58 @@ extern "C" int skkr_gpu_cpacoord(skkr_ctx *c, double ce_re, double ce_im, double
   rc = skkr_gpu_run(c, status);
   if (rc != SKKR_OK) return rc;
   return skkr_gpu_fetch(c, tminv, tauc, taua, taub, ld);
+}
+
+// ---------------------------------------------------------------------------
+// multi-energy residency: stage several energies, run / fetch any of them
+static SlotStore *get_slot(skkr_ctx *c, int slot, bool create) {
+  if (slot < 0 || slot > 4096) return nullptr;
+  if ((int)c->slots.size() <= slot) {
+    if (!create) return nullptr;
+    c->slots.resize(slot + 1, nullptr);
+  }
+  if (!c->slots[slot]) {
+    if (!create) return nullptr;
+    c->slots[slot] = new SlotStore();
+  }
+  return c->slots[slot];
+}
+
+extern "C" int skkr_gpu_stage_slot(skkr_ctx *c, int slot, double ce_re, double ce_im, double fac_re,
+                                   double fac_im, const skkr_rtable *rt, int nk, const double *xk,
+                                   const double *wk, const double *lg, const double *rg,
+                                   const double *conc, const double *tminvl,
+                                   const double *tminvr, const double *tminv,
+                                   const double *tminva, const double *tminvb, int ld) {
+  if (!c) return SKKR_ERR_ARG;
+  SlotStore *s = get_slot(c, slot, true);
+  if (!s) return SKKR_ERR_ARG;
+  swap_slot(c, *s);
+  int rc = skkr_gpu_stage(c, ce_re, ce_im, fac_re, fac_im, rt, nk, xk, wk, lg, rg, conc, tminvl,
+                          tminvr, tminv, tminva, tminvb, ld);
+  swap_slot(c, *s);
+  return rc;
+}
+
+extern "C" int skkr_gpu_run_slot(skkr_ctx *c, int slot, skkr_status *status) {
+  if (!c) return SKKR_ERR_ARG;
+  SlotStore *s = get_slot(c, slot, false);
+  if (!s || !s->staged) return SKKR_ERR_ARG;
+  swap_slot(c, *s);
+  int rc = skkr_gpu_run(c, status);
+  swap_slot(c, *s);
+  return rc;
+}
+
+extern "C" int skkr_gpu_fetch_slot(skkr_ctx *c, int slot, double *tminv, double *tauc,
+                                   double *taua, double *taub, int ld) {
+  if (!c) return SKKR_ERR_ARG;
+  SlotStore *s = get_slot(c, slot, false);
+  if (!s || !s->staged) return SKKR_ERR_ARG;
+  swap_slot(c, *s);
+  int rc = skkr_gpu_fetch(c, tminv, tauc, taua, taub, ld);
+  swap_slot(c, *s);
+  return rc;
 }
 
 // ---------------------------------------------------------------------------

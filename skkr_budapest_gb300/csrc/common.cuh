@@ -67,3 +67,13 @@ inline MatRef mref_map(zd *base, long long sk, long long sc, int ld, const int *
 extern long long g_skkr_launches;
 void skkr_after_launch(const char *file, int line);
 #define SKKR_LAUNCHED() skkr_after_launch(__FILE__, __LINE__)
+
+// Per-kernel-class timing with CUDA events on the launching stream (off by
+// default; bench.py switches it on for the timed region).  `work` is the
+// algorithmic FLOP (or byte) count of the launch.  Masked launches count the
+// active items the host announced through skkr_set_active_items (-1: all).
+enum { KS_GEMM = 0, KS_GJ = 1, KS_GKFT = 2, KS_OTHER = 3, KS_NCLS = 4 };
+void kstat_begin(int cls, double work, cudaStream_t st);
+void kstat_end(cudaStream_t st);
+long long skkr_active_items(long long all);
+void skkr_set_active_items(long long n);

@@ -40,7 +40,9 @@ void launch_gk_ft(const zd *gR, const double *rvec, const int *rstart, int nblk,
                   const double *xk, int nk, zd *out, cudaStream_t st) {
   if (nk <= 0) return;
   dim3 grid(nblk, nk);
+  kstat_begin(KS_GKFT, (double)nk * nblk * lmmax * lmmax * sizeof(zd), st);
   k_gk_ft<<<grid, 256, 0, st>>>(gR, rvec, rstart, nblk, lmmax, xk, out);
+  kstat_end(st);
   SKKR_LAUNCHED();
 }
 
@@ -234,12 +236,15 @@ void launch_zgemm(int mode, const MatRef &A, const MatRef &B, const MatRef &C, c
                   cudaStream_t st) {
   if (nk <= 0 || nc <= 0 || m <= 0 || n <= 0) return;
   dim3 grid(((m + 31) / 32) * ((n + 31) / 32), nk * nc);
+  const long long items = act ? skkr_active_items((long long)nk * nc) : (long long)nk * nc;
+  kstat_begin(KS_GEMM, 8.0 * m * n * kdim * (double)items, st);
   switch (mode) {
     case 0: k_zgemm<0><<<grid, 256, 0, st>>>(A, B, C, D, E, m, n, kdim, nc, act); break;
     case 1: k_zgemm<1><<<grid, 256, 0, st>>>(A, B, C, D, E, m, n, kdim, nc, act); break;
     case 2: k_zgemm<2><<<grid, 256, 0, st>>>(A, B, C, D, E, m, n, kdim, nc, act); break;
     default: k_zgemm<3><<<grid, 256, 0, st>>>(A, B, C, D, E, m, n, kdim, nc, act); break;
   }
+  kstat_end(st);
   SKKR_LAUNCHED();
 }
 
@@ -328,7 +333,10 @@ __global__ void __launch_bounds__(512) k_zgj(MatRef A, int n, int nc, const int 
 void launch_zgj(const MatRef &A, int n, int nk, int nc, const int *act, cudaStream_t st) {
   if (nk <= 0 || nc <= 0 || n <= 0) return;
   int th = n * n >= 4096 ? 512 : 256;
+  const long long items = act ? skkr_active_items((long long)nk * nc) : (long long)nk * nc;
+  kstat_begin(KS_GJ, 8.0 * n * n * (double)n * (double)items, st);
   k_zgj<<<nk * nc, th, 0, st>>>(A, n, nc, act);
+  kstat_end(st);
   SKKR_LAUNCHED();
 }
 

@@ -37,7 +37,7 @@ class RTable(C.Structure):
 class Status(C.Structure):
     _fields_ = [("code", I), ("ik", I), ("cpa_iterations", I), ("cpa_error", D),
                 ("max_dec_iters", I), ("dec_iters_total", C.c_longlong),
-                ("gpu_launches", C.c_longlong), ("max_refine_resid", D)]
+                ("gpu_launches", C.c_longlong), ("max_refine_resid", D), ("run_ms", D)]
 
 
 class SkkrError(RuntimeError):
@@ -70,6 +70,10 @@ def lib():
         L.skkr_gpu_surfgf_batch.argtypes = [I, I, P, P, P, P, I, I, D, P, P]
         L.skkr_gpu_gk.argtypes = [P, I, I, P, P]
         L.skkr_gpu_last_error.restype = C.c_char_p
+        L.skkr_gpu_stage_slot.argtypes = [P, I, D, D, D, D, P, I, P, P, P, P, P, P, P, P, P, P, I]
+        L.skkr_gpu_run_slot.argtypes = [P, I, P]
+        L.skkr_gpu_fetch_slot.argtypes = [P, I, P, P, P, P, I]
+        L.skkr_gpu_kernel_stats.argtypes = [I, P]
         _lib = L
     return _lib
 
@@ -146,3 +150,17 @@ def phystau(tau, tinv, alpha, lmax, irel):
     al = np.ascontiguousarray(alpha, np.complex128)
     _check(lib().skkr_gpu_phystau(irel, lmax, _p(t), _p(ti), _p(al), t.shape[-1]), "skkr_gpu_phystau")
     return uncm(t)
+
+
+KSTAT_CLASSES = ("zgemm", "gjinv", "gk_ft", "other")
+
+
+def kernel_stats_start():
+    _check(lib().skkr_gpu_kernel_stats(1, None), "skkr_gpu_kernel_stats")
+
+
+def kernel_stats_stop():
+    out = np.zeros(12)
+    _check(lib().skkr_gpu_kernel_stats(0, _p(out)), "skkr_gpu_kernel_stats")
+    return {name: dict(launches=int(out[3 * i]), ms=float(out[3 * i + 1]), work=float(out[3 * i + 2]))
+            for i, name in enumerate(KSTAT_CLASSES)}
