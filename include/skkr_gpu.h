@@ -170,6 +170,29 @@ int skkr_gpu_gjinv_batch(int n, int batch, double *a, int ld);
 int skkr_gpu_surfgf_batch(int n, int batch, const double *ml, const double *m0,
                           const double *mr, double *x, int ld, int itermax,
                           double errmax, int *iters, int *stat);
+/* Decimation exactly like skkr_gpu_surfgf_batch, for callers that are not
+ * allowed to allocate device memory (a host code whose device memory belongs
+ * to another layer, such as an OpenACC / CUDA Fortran data region or the
+ * application's own pool, or a run with a fixed device-memory budget).
+ * No counterpart in the reference.
+ *   ml, m0, mr, x  DEVICE pointers owned by the caller: `batch` column-major
+ *                  n x n matrices, leading dimension ld, one ld*ld block each
+ *   iters, stat    host arrays [batch] or NULL;  stream: a cudaStream_t or NULL
+ * It calls no cudaMalloc / cudaFree: its work space is one static device array
+ * of SKKR_NOALLOC_SCRATCH_BYTES (32 MiB, held by every GPU that loads the
+ * library until the process exits).  A request needing more than
+ * batch * (8 * n * n * 16 + 20) + 64 > SKKR_NOALLOC_SCRATCH_BYTES bytes is
+ * rejected with SKKR_ERR_NOMEM before anything runs.  The first call on each
+ * device looks up the array's device address (cudaGetSymbolAddress); make
+ * that first call before any stream capture.  All calls share the one array:
+ * calls that overlap on the GPU (several streams or host threads) race. */
+#define SKKR_NOALLOC_SCRATCH_BYTES (32u << 20)
+int skkr_gpu_surfgf_batch_noalloc(int n, int batch, const double *ml,
+                                  const double *m0, const double *mr,
+                                  double *x, int ld, int itermax,
+                                  double errmax, int *iters, int *stat,
+                                  void *stream);
+
 /* G_scr(k) blocks of nk k points: out [nk][nblk] lm x lm column-major. */
 int skkr_gpu_gk(const skkr_rtable *rt, int lmax, int nk, const double *xk, double *out);
 
