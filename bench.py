@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--energies", default="", help="comma list overriding the step energies")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="only the device loop of the timed steps (for ncu captures); prints a short line")
     return ap.parse_args()
 
 
@@ -276,6 +278,11 @@ def run_ours(args, rank, ws):
     torch.cuda.synchronize()
     wall = time.perf_counter() - w0
     ks = N.kernel_stats_stop()
+    if args.profile:
+        clocks.stop()
+        ctx.close()
+        print(json.dumps({"profile_run": True, "points": pts, "device_ms": t_dev, "launches": launches}))
+        return
     clk = clocks.stop()
     barrier(ws)
     t_max = max_over_ranks(t_dev, ws)
@@ -298,7 +305,12 @@ def run_ours(args, rank, ws):
     # roofline of the dominant kernel class, from the live event timings
     dom = max(ks.items(), key=lambda kv: kv[1]["ms"])
     name, d = dom
-    traffic = traffic_from_profiles().get(name)
+    # DRAM bytes of one launch from the committed ncu capture, scaled to this
+    # run's average work per launch (traffic grows with the matrices processed)
+    tr = traffic_from_profiles().get(name)
+    traffic = None
+    if tr and d["launches"]:
+        traffic = tr["dram_bytes"] * (d["work"] / d["launches"]) / tr["work"]
     if name == "gk_ft":
         peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"] if os.path.exists(
             os.path.join(ROOT, "MEASURED_PEAKS.json")) else 6800.0

@@ -19,6 +19,13 @@ __device__ inline void zfma(zd &c, zd a, zd b) {
   c.y = fma(a.x, b.y, c.y);
   c.y = fma(a.y, b.x, c.y);
 }
+// c -= a*b (four FMAs)
+__device__ inline void zfms(zd &c, zd a, zd b) {
+  c.x = fma(-a.x, b.x, c.x);
+  c.x = fma(a.y, b.y, c.x);
+  c.y = fma(-a.x, b.y, c.y);
+  c.y = fma(-a.y, b.x, c.y);
+}
 // 1/q by Smith's scaled division
 __device__ inline zd zrecip(zd q) {
   if (fabs(q.x) >= fabs(q.y)) {

@@ -313,8 +313,9 @@ __global__ void __launch_bounds__(512) k_zgj(MatRef A, int n, int nc, const int 
       const int r = e % n, j = e / n;
       if (j == i) continue;
       zd *p = a + r + (long long)j * ld;
-      zd base = (r == i) ? make_double2(0.0, 0.0) : *p;
-      *p = zsub(base, zmul(coli[r], rowi[j]));
+      zd v = (r == i) ? make_double2(0.0, 0.0) : *p;
+      zfms(v, coli[r], rowi[j]);
+      *p = v;
     }
     __syncthreads();
   }
