@@ -62,6 +62,7 @@ typedef struct {
   double cpatol;                  /* CPA tolerance on error3 (rsp-scf/fullcpa.f:142) */
   int precision;                  /* skkr_precision */
   int nk_chunk;                   /* k points per device batch (0: automatic) */
+  int slices;                     /* SKKR_MIXED: BF16 slices per product operand, 3..7 (0: 6) */
 } skkr_sizes;
 
 /* Real-space screened structure constants of one energy, grouped in
@@ -192,6 +193,18 @@ int skkr_gpu_surfgf_batch_noalloc(int n, int batch, const double *ml,
                                   double *x, int ld, int itermax,
                                   double errmax, int *iters, int *stat,
                                   void *stream);
+
+/* c = a*b for `batch` complex n x n matrices (host arrays, ld), in FP64 or
+ * split precision (`slices` 3 or 5 BF16 slices per operand on the tensor
+ * cores).  Test and benchmark entry point of the products used by
+ * surfgf / tau2d (main/matops.f doubmt2 / tripmt). */
+int skkr_gpu_zgemm_batch(int precision, int slices, int n, int batch,
+                         const double *a, const double *b, double *c, int ld);
+/* In-place inverses in FP64 (main/gjinv.f) or split precision (FP32
+ * Gauss-Jordan + `newton` refinement steps; n <= 128).  max_resid (may be
+ * NULL) receives the largest ||I - A X||_F before the last step. */
+int skkr_gpu_zinv_batch(int precision, int n, int batch, double *a, int ld,
+                        int newton, double *max_resid);
 
 /* G_scr(k) blocks of nk k points: out [nk][nblk] lm x lm column-major. */
 int skkr_gpu_gk(const skkr_rtable *rt, int lmax, int nk, const double *xk, double *out);

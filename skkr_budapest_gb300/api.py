@@ -20,7 +20,7 @@ class Context:
     """Device context for one system (sizes fixed, energies vary)."""
 
     def __init__(self, irel, lmax, nprc, ninprc, ngeff, itermaxl=50, itermaxr=50, errmax=1e-8,
-                 itcpam=50, cpatol=1e-10, precision="fp64", nk_chunk=0):
+                 itcpam=50, cpatol=1e-10, precision="fp64", nk_chunk=0, slices=0):
         s = N.Sizes()
         s.mode = N.REL if irel else N.NONREL
         s.lmax = lmax
@@ -33,6 +33,7 @@ class Context:
         s.itcpam, s.cpatol = itcpam, cpatol
         s.precision = {"fp64": N.FP64, "mixed": N.MIXED}[precision]
         s.nk_chunk = nk_chunk
+        s.slices = slices
         self.sizes = s
         self.lk = 2 * (lmax + 1) ** 2 if irel else (lmax + 1) ** 2
         self.nintfc = int(sum(ninprc[1:nprc + 1]))
@@ -43,9 +44,9 @@ class Context:
         self._keep = None
 
     @classmethod
-    def for_problem(cls, ep, precision="fp64", nk_chunk=0):
+    def for_problem(cls, ep, precision="fp64", nk_chunk=0, slices=0):
         return cls(ep.irel, ep.lmax, ep.nprc, ep.ninprc, len(ep.lg), ep.itermaxl, ep.itermaxr, ep.errmax,
-                   ep.itcpam, ep.cpatol, precision, nk_chunk)
+                   ep.itcpam, ep.cpatol, precision, nk_chunk, slices)
 
     def close(self):
         if self.h:
@@ -147,9 +148,9 @@ class Context:
         return res
 
 
-def cpacoord(ep, precision="fp64", tminv=None, check=True):
+def cpacoord(ep, precision="fp64", tminv=None, check=True, slices=0):
     """One energy through the GPU path (creates a context for the call)."""
-    ctx = Context.for_problem(ep, precision)
+    ctx = Context.for_problem(ep, precision, slices=slices)
     try:
         return ctx.cpacoord(ep, tminv=tminv, check=check)
     finally:

@@ -190,6 +190,9 @@ struct skkr_ctx {
   int first_bad_k = -1;
   int err_code = 0;
   std::vector<struct SlotStore *> slots;
+  MixedWork *mw = nullptr;   // split-precision engine (precision == SKKR_MIXED)
+  int slices = 6, slices_res = 7;  // BF16 slices of products / of Newton residuals
+  double max_resid = 0.0;    // largest Newton residual seen in this run
 };
 
 // Inputs and outputs of one staged energy.  A context keeps any number of
@@ -252,6 +255,14 @@ extern "C" int skkr_gpu_create(const skkr_sizes *sizes, skkr_ctx **out) {
   c->nprc = s.nprc;
   c->nintfc = c->pl * s.nprc;
   c->ngeff = s.ngeff;
+  if (s.slices != 0) {
+    if (s.slices < 3 || s.slices > 7) {
+      delete c;
+      return SKKR_ERR_ARG;
+    }
+    c->slices = s.slices;
+    c->slices_res = s.slices < 7 ? s.slices + 1 : 7;
+  }
   if (c->n > 256) {
     delete c;
     return SKKR_ERR_UNSUPPORTED;
@@ -278,6 +289,7 @@ extern "C" int skkr_gpu_destroy(skkr_ctx *c) {
                  &c->pool, &c->jobs, &c->dec, &c->decf, &c->deci, &c->tauw, &c->tauk, &c->S,
                  &c->T1, &c->T2, &c->tauc, &c->cpa, &c->cpan, &c->cpaact};
   for (DBuf *b : all) b->release();
+  if (c->mw) mixed_destroy(c->mw);
   for (SlotStore *sl : c->slots) {
     DBuf *sb[] = {&sl->gR, &sl->rvec, &sl->rstart, &sl->blkmap_d, &sl->xk, &sl->wk, &sl->lg,
                   &sl->rg, &sl->conc, &sl->tcat, &sl->tab, &sl->tauc, &sl->cpa};
@@ -560,6 +572,33 @@ static int check_slot_quirk(const skkr_ctx *c) {
 }
 
 // ---------------------------------------------------------------------------
+// engine: the dense operations of decimation and tau2d in FP64 or split
+// precision (tcgen05 sliced products, FP32 inverse + Newton refinement)
+static int eng_gemm(skkr_ctx *c, bool mixed, int mode, const MatRef &A, const MatRef &B, const MatRef &C,
+                    const MatRef &D, const MatRef &E, int n, int nk, int nc, const int *act) {
+  if (mixed) return mixed_zgemm(c->mw, mode, c->slices, A, B, C, D, E, n, nk, nc, act, c->st);
+  launch_zgemm(mode, A, B, C, D, E, n, n, n, nk, nc, act, c->st);
+  return SKKR_OK;
+}
+
+// X = A^-1 (X may be the same matrices as A when inplace)
+static int eng_inv(skkr_ctx *c, bool mixed, const MatRef &A, const MatRef &X, bool inplace, int n, int nk,
+                   int nc, const int *act) {
+  if (mixed && n <= 128)
+    return mixed_zinv(c->mw, A, X, n, nk, nc, act, 2, c->slices_res, &c->max_resid, c->st);
+  if (!inplace) launch_zaxpby(X, A, nullptr, 0, nullptr, 0, n, nk, nc, act, c->st);
+  launch_zgj(X, n, nk, nc, act, c->st);
+  return SKKR_OK;
+}
+
+static bool use_mixed(const skkr_ctx *c, bool decimation) {
+  if (c->sz.precision != SKKR_MIXED) return false;
+  // decimation within 1e-3 Ry of the real axis stays in FP64
+  if (decimation && std::fabs(c->ce.y) < 1.0e-3) return false;
+  return true;
+}
+
+// ---------------------------------------------------------------------------
 // decimation (main/dugo.f + main/surfgf.f) for the k points [k0, k0+nkc)
 // items (k, s): s < nLc left-lead classes, then right-lead classes.
 static int run_decimation(skkr_ctx *c, int k0, int nkc, const std::vector<int> &lcls,
@@ -616,19 +655,19 @@ static int run_decimation(skkr_ctx *c, int k0, int nkc, const std::vector<int> &
     CK(cudaMemsetAsync(iters, 0, nit * sizeof(int), st));
   }
   const int itermax = std::max(c->sz.itermaxl, c->sz.itermaxr);
+  const bool mx = use_mixed(c, true);
   int iter = 1;
   skkr_set_active_items(nit);
   for (;; iter++) {
     MatRef &ac = (iter & 1) ? a0 : a1, &an = (iter & 1) ? a1 : a0;
     MatRef &bc = (iter & 1) ? b0 : b1, &bn = (iter & 1) ? b1 : b0;
-    launch_zaxpby(y1, eps, nullptr, 0, nullptr, 0, n, nkc, nc, act, st);
-    launch_zgj(y1, n, nkc, nc, act, st);
-    launch_zgemm(0, ac, y1, P, P, P, n, n, n, nkc, nc, act, st);   // P = alfa y1
-    launch_zgemm(0, bc, y1, Q, Q, Q, n, n, n, nkc, nc, act, st);   // Q = beta y1
-    launch_zgemm(0, P, ac, an, an, an, n, n, n, nkc, nc, act, st); // alfa' = P alfa
-    launch_zgemm(0, Q, bc, bn, bn, bn, n, n, n, nkc, nc, act, st); // beta' = Q beta
-    launch_zgemm(2, P, bc, P, eps, x, n, n, n, nkc, nc, act, st);  // y3: eps -= y3, x -= y3
-    launch_zgemm(1, Q, ac, eps, eps, eps, n, n, n, nkc, nc, act, st);  // eps -= y4
+    CKR(eng_inv(c, mx, eps, y1, false, n, nkc, nc, act));              // y1 = eps^-1
+    CKR(eng_gemm(c, mx, 0, ac, y1, P, P, P, n, nkc, nc, act));        // P = alfa y1
+    CKR(eng_gemm(c, mx, 0, bc, y1, Q, Q, Q, n, nkc, nc, act));        // Q = beta y1
+    CKR(eng_gemm(c, mx, 0, P, ac, an, an, an, n, nkc, nc, act));      // alfa' = P alfa
+    CKR(eng_gemm(c, mx, 0, Q, bc, bn, bn, bn, n, nkc, nc, act));      // beta' = Q beta
+    CKR(eng_gemm(c, mx, 2, P, bc, P, eps, x, n, nkc, nc, act));       // y3: eps -= y3, x -= y3
+    CKR(eng_gemm(c, mx, 1, Q, ac, eps, eps, eps, n, nkc, nc, act));   // eps -= y4
     launch_fnorm(an, n, nkc, nc, act, err, st);
     // the two leads may carry different caps (itermaxl / itermaxr)
     launch_dec_state(err, act, stat, iters, nit, iter, itermax, c->sz.errmax, st);
@@ -667,11 +706,11 @@ static int run_decimation(skkr_ctx *c, int k0, int nkc, const std::vector<int> &
     }
   }
   // X = x^-1 ; xy = ml X mt (tripmt2) into the SSPO cache
-  launch_zgj(x, n, nkc, nc, nullptr, st);
-  launch_zgemm(0, Pml, x, y1, y1, y1, n, n, n, nkc, nc, nullptr, st);
+  CKR(eng_inv(c, mx, x, x, true, n, nkc, nc, nullptr));
+  CKR(eng_gemm(c, mx, 0, Pml, x, y1, y1, y1, n, nkc, nc, nullptr));
   MatRef SS = mref_map(c->sspo.as<zd>() + (long long)k0 * c->nsl * MB, (long long)c->nsl * MB, MB, n,
                        mapsl, nc);
-  launch_zgemm(0, y1, Pmt, SS, SS, SS, n, n, n, nkc, nc, nullptr, st);
+  CKR(eng_gemm(c, mx, 0, y1, Pmt, SS, SS, SS, n, nkc, nc, nullptr));
   return SKKR_OK;
 }
 
@@ -713,6 +752,7 @@ static int run_tau2d(skkr_ctx *c, int k0, int nkc, const std::vector<int> &icls)
   zd *sbase = c->sspo.as<zd>() + (long long)k0 * c->nsl * MB;
   MatRef Ys = mref_map(sbase, (long long)c->nsl * MB, MB, n, ysl, nc);
   MatRef Xs = mref_map(sbase, (long long)c->nsl * MB, MB, n, xsl, nc);
+  const bool mx = use_mixed(c, false);
   // forward (tau2d.f:53-85)
   for (int p = 0; p < nprc; p++) {
     int tm2[SKKR_MAPN];
@@ -722,13 +762,13 @@ static int run_tau2d(skkr_ctx *c, int k0, int nkc, const std::vector<int> &icls)
     if (p == 0) {
       launch_zaxpby(YY(0), Ys, nullptr, 0, nullptr, 0, n, nkc, nc, nullptr, st);
     } else {
-      launch_zgemm(0, M10, Yr(p), YY(p), YY(p), YY(p), n, n, n, nkc, nc, nullptr, st);
+      CKR(eng_gemm(c, mx, 0, M10, Yr(p), YY(p), YY(p), YY(p), n, nkc, nc, nullptr));
     }
     if (p < nprc - 1) {
       MatRef yy = YY(p);
       launch_zaxpby(Wm, T00(p), &yy, -1.0, nullptr, 0, n, nkc, nc, nullptr, st);
-      launch_zgj(Wm, n, nkc, nc, nullptr, st);
-      launch_zgemm(0, Wm, M01, Yr(p + 1), Yr(p + 1), Yr(p + 1), n, n, n, nkc, nc, nullptr, st);
+      CKR(eng_inv(c, mx, Wm, Wm, true, n, nkc, nc, nullptr));
+      CKR(eng_gemm(c, mx, 0, Wm, M01, Yr(p + 1), Yr(p + 1), Yr(p + 1), n, nkc, nc, nullptr));
     }
   }
   // backward (tau2d.f:89-109)
@@ -736,20 +776,20 @@ static int run_tau2d(skkr_ctx *c, int k0, int nkc, const std::vector<int> &icls)
     if (p == nprc - 1) {
       launch_zaxpby(XX(p), Xs, nullptr, 0, nullptr, 0, n, nkc, nc, nullptr, st);
     } else {
-      launch_zgemm(0, M01, Xr(p), XX(p), XX(p), XX(p), n, n, n, nkc, nc, nullptr, st);
+      CKR(eng_gemm(c, mx, 0, M01, Xr(p), XX(p), XX(p), XX(p), n, nkc, nc, nullptr));
     }
     if (p > 0) {
       MatRef xx = XX(p);
       launch_zaxpby(Wm, T00(p), &xx, -1.0, nullptr, 0, n, nkc, nc, nullptr, st);
-      launch_zgj(Wm, n, nkc, nc, nullptr, st);
-      launch_zgemm(0, Wm, M10, Xr(p - 1), Xr(p - 1), Xr(p - 1), n, n, n, nkc, nc, nullptr, st);
+      CKR(eng_inv(c, mx, Wm, Wm, true, n, nkc, nc, nullptr));
+      CKR(eng_gemm(c, mx, 0, Wm, M10, Xr(p - 1), Xr(p - 1), Xr(p - 1), n, nkc, nc, nullptr));
     }
   }
   // diagonal blocks (tau2d.f:114-149), weight wk/ngeff
   for (int p = 0; p < nprc; p++) {
     MatRef xx = XX(p), yy = YY(p);
     launch_zaxpby(Wm, T00(p), &xx, -1.0, &yy, -1.0, n, nkc, nc, nullptr, st);
-    launch_zgj(Wm, n, nkc, nc, nullptr, st);
+    CKR(eng_inv(c, mx, Wm, Wm, true, n, nkc, nc, nullptr));
     launch_extract_tau(Wm, lk, pl, p * pl, c->wk.as<double>() + k0, 1.0 / c->ngeff, c->tauk.as<zd>(),
                        (long long)nc * ni * lk2, (long long)ni * lk2, nkc, nc, st);
   }
@@ -884,6 +924,11 @@ extern "C" int skkr_gpu_run(skkr_ctx *c, skkr_status *status) {
   c->tot_dec = 0;
   c->err_code = 0;
   c->first_bad_k = -1;
+  c->max_resid = 0.0;
+  if (c->sz.precision == SKKR_MIXED && !c->mw) {
+    c->mw = mixed_create();
+    if (!c->mw) return SKKR_ERR_NOMEM;
+  }
   plan_pack(c);
   CKR(c->jobs.ensure(c->jobs_h.size() * sizeof(PackJob)));
   CK(cudaMemcpyAsync(c->jobs.p, c->jobs_h.data(), c->jobs_h.size() * sizeof(PackJob),
@@ -966,6 +1011,13 @@ extern "C" int skkr_gpu_run(skkr_ctx *c, skkr_status *status) {
     if (!(concpa && cpacon)) break;
   }
   trace_point("after CPA loop");
+  if (c->mw && c->err_code == 0) {
+    int f = mixed_error_flag(c->mw);
+    if (f != 0) {
+      g_last_error = "tensor-core kernel: bounded wait expired";
+      c->err_code = SKKR_ERR_CUDA;
+    }
+  }
   CK(cudaEventRecord(ev1, st));
   CK(cudaStreamSynchronize(st));
   CK(cudaGetLastError());
@@ -981,7 +1033,7 @@ extern "C" int skkr_gpu_run(skkr_ctx *c, skkr_status *status) {
     status->max_dec_iters = c->max_dec;
     status->dec_iters_total = c->tot_dec;
     status->gpu_launches = g_skkr_launches - l0;
-    status->max_refine_resid = 0.0;
+    status->max_refine_resid = c->max_resid;
     status->run_ms = run_ms;
   }
   return c->err_code;
@@ -1293,4 +1345,61 @@ extern "C" int skkr_gpu_phystau(int mode, int lmax, double *tau, const double *t
   CK(cudaDeviceSynchronize());
   CK(cudaGetLastError());
   return download_mats(tau, T, 1, nd, ld);
+}
+
+// ---------------------------------------------------------------------------
+// batched complex products and inverses on host arrays (tests, benchmarks)
+extern "C" int skkr_gpu_zgemm_batch(int precision, int slices, int n, int batch, const double *a,
+                                    const double *b, double *cmat, int ld) {
+  if (n < 1 || n > 256 || batch < 1 || batch > 65535 || !a || !b || !cmat || ld < n) return SKKR_ERR_ARG;
+  Scoped s;
+  zd *A, *B, *C;
+  CKR(s.alloc(&A, (size_t)batch * n * n));
+  CKR(s.alloc(&B, (size_t)batch * n * n));
+  CKR(s.alloc(&C, (size_t)batch * n * n));
+  CKR(upload_mats(A, a, batch, n, ld));
+  CKR(upload_mats(B, b, batch, n, ld));
+  const long long MB = (long long)n * n;
+  MatRef Am = mref(A, MB, 0, n), Bm = mref(B, MB, 0, n), Cm = mref(C, MB, 0, n);
+  if (precision == SKKR_MIXED) {
+    MixedWork *w = mixed_create();
+    if (!w) return SKKR_ERR_NOMEM;
+    int rc = mixed_zgemm(w, 0, slices, Am, Bm, Cm, Cm, Cm, n, batch, 1, nullptr, 0);
+    if (rc == SKKR_OK && cudaDeviceSynchronize() != cudaSuccess) rc = SKKR_ERR_CUDA;
+    if (rc == SKKR_OK && mixed_error_flag(w) != 0) rc = SKKR_ERR_CUDA;
+    mixed_destroy(w);
+    CKR(rc);
+  } else {
+    launch_zgemm(0, Am, Bm, Cm, Cm, Cm, n, n, n, batch, 1, nullptr, 0);
+  }
+  CK(cudaDeviceSynchronize());
+  CK(cudaGetLastError());
+  return download_mats(cmat, C, batch, n, ld);
+}
+
+extern "C" int skkr_gpu_zinv_batch(int precision, int n, int batch, double *a, int ld, int newton,
+                                   double *max_resid) {
+  if (n < 1 || n > 256 || batch < 1 || batch > 65535 || !a || ld < n) return SKKR_ERR_ARG;
+  if (precision == SKKR_MIXED && n > 128) return SKKR_ERR_UNSUPPORTED;
+  Scoped s;
+  zd *A;
+  CKR(s.alloc(&A, (size_t)batch * n * n));
+  CKR(upload_mats(A, a, batch, n, ld));
+  MatRef Am = mref(A, (long long)n * n, 0, n);
+  if (precision == SKKR_MIXED) {
+    MixedWork *w = mixed_create();
+    if (!w) return SKKR_ERR_NOMEM;
+    double r = 0.0;
+    int rc = mixed_zinv(w, Am, Am, n, batch, 1, nullptr, newton, 7, &r, 0);
+    if (rc == SKKR_OK && cudaDeviceSynchronize() != cudaSuccess) rc = SKKR_ERR_CUDA;
+    if (rc == SKKR_OK && mixed_error_flag(w) != 0) rc = SKKR_ERR_CUDA;
+    mixed_destroy(w);
+    CKR(rc);
+    if (max_resid) *max_resid = r;
+  } else {
+    launch_zgj(Am, n, batch, 1, nullptr, 0);
+  }
+  CK(cudaDeviceSynchronize());
+  CK(cudaGetLastError());
+  return download_mats(a, A, batch, n, ld);
 }

@@ -51,3 +51,14 @@ void launch_gsum(const zd *T, int ng, int lk, int nl, zd *out, cudaStream_t st);
 // CPA helpers
 void launch_cpa_mix(const zd *X, const double *conc, const int *act, int lk, int nl, zd *xc,
                     cudaStream_t st);
+
+// split-precision engine (kernels_mixed.cu)
+struct MixedWork;
+MixedWork *mixed_create();
+void mixed_destroy(MixedWork *w);
+int mixed_error_flag(MixedWork *w);
+// modes as launch_zgemm plus 4: C = I - A*B, 5: C = C + A*B; S = slices (3..7)
+int mixed_zgemm(MixedWork *w, int mode, int S, const MatRef &A, const MatRef &B, const MatRef &C,
+                const MatRef &D, const MatRef &E, int n, int nk, int nc, const int *act, cudaStream_t st);
+int mixed_zinv(MixedWork *w, const MatRef &A, const MatRef &X, int n, int nk, int nc, const int *act,
+               int newton, int sres, double *max_resid, cudaStream_t st);

@@ -26,7 +26,7 @@ I, D, P = C.c_int, C.c_double, C.c_void_p
 class Sizes(C.Structure):
     _fields_ = [("mode", I), ("lmax", I), ("nprc", I), ("ninprc", I * (SKKR_MAX_PRC + 2)),
                 ("bulkgeo", I), ("ngeff", I), ("itermaxl", I), ("itermaxr", I), ("errmax", D),
-                ("itcpam", I), ("cpatol", D), ("precision", I), ("nk_chunk", I)]
+                ("itcpam", I), ("cpatol", D), ("precision", I), ("nk_chunk", I), ("slices", I)]
 
 
 class RTable(C.Structure):
@@ -164,3 +164,27 @@ def kernel_stats_stop():
     _check(lib().skkr_gpu_kernel_stats(0, _p(out)), "skkr_gpu_kernel_stats")
     return {name: dict(launches=int(out[3 * i]), ms=float(out[3 * i + 1]), work=float(out[3 * i + 2]))
             for i, name in enumerate(KSTAT_CLASSES)}
+
+
+def zgemm_batch(a, b, precision="fp64", slices=5):
+    a = np.asarray(a, np.complex128)
+    nb, n, _ = a.shape
+    A, B = cm(a), cm(b)
+    Cm = np.zeros_like(A)
+    L = lib()
+    L.skkr_gpu_zgemm_batch.argtypes = [I, I, I, I, P, P, P, I]
+    _check(L.skkr_gpu_zgemm_batch({"fp64": FP64, "mixed": MIXED}[precision], slices, n, nb, _p(A), _p(B),
+                                  _p(Cm), n), "skkr_gpu_zgemm_batch")
+    return uncm(Cm)
+
+
+def zinv_batch(a, precision="fp64", newton=2):
+    a = np.asarray(a, np.complex128)
+    nb, n, _ = a.shape
+    A = cm(a)
+    r = np.zeros(1)
+    L = lib()
+    L.skkr_gpu_zinv_batch.argtypes = [I, I, I, P, I, I, P]
+    _check(L.skkr_gpu_zinv_batch({"fp64": FP64, "mixed": MIXED}[precision], n, nb, _p(A), n, newton, _p(r)),
+           "skkr_gpu_zinv_batch")
+    return uncm(A), float(r[0])

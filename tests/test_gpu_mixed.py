@@ -1,0 +1,89 @@
+"""Split-precision path (tcgen05 sliced products, FP32 inverse + Newton):
+against numpy FP64 for the kernels and against the CPU oracle for the whole
+CPA pass, at the mixed-path tolerance 1e-9 (relative Frobenius)."""
+import numpy as np
+import pytest
+
+import oracle as O
+from skkr_budapest_gb300 import api, native
+from skkr_budapest_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+TOL_MIXED = 1e-9
+rng = np.random.default_rng(5)
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+def crand(*s):
+    return rng.normal(size=s) + 1j * rng.normal(size=s)
+
+
+@pytest.mark.parametrize("n", [18, 54, 128, 256])
+@pytest.mark.parametrize("slices,tol", [(5, 5e-11), (6, 3e-13), (7, 3e-14)])
+def test_sliced_zgemm_is_fp64_accurate(n, slices, tol):
+    # S slices: about 2^(-8S) sigma tau per term, random-walk summed over K = 2n
+    a, b = crand(3, n, n), crand(3, n, n)
+    c = native.zgemm_batch(a, b, precision="mixed", slices=slices)
+    ref = a @ b
+    if n == 256 and slices > 5:
+        tol = 3e-12  # K = 512: level-2 sums exceed FP32's 24 bits by a bit
+    for i in range(3):
+        assert rel(c[i], ref[i]) < tol, rel(c[i], ref[i])
+
+
+def test_sliced_zgemm_three_slices_is_fp32_class():
+    n = 64
+    a, b = crand(2, n, n), crand(2, n, n)
+    c = native.zgemm_batch(a, b, precision="mixed", slices=3)
+    e = max(rel(c[i], (a @ b)[i]) for i in range(2))
+    assert 1e-12 < e < 1e-5
+
+
+def test_sliced_zgemm_scaled_rows():
+    # rows and columns spanning 12 orders of magnitude: per-row/column scales
+    n = 40
+    a = crand(2, n, n) * np.logspace(-6, 6, n)[None, :, None]
+    b = crand(2, n, n) * np.logspace(4, -8, n)[None, None, :]
+    c = native.zgemm_batch(a, b, precision="mixed", slices=5)
+    ref = a @ b
+    for i in range(2):
+        err = np.abs(c[i] - ref[i]) / (np.abs(a[i]) @ np.abs(b[i]))
+        assert err.max() < 5e-11
+
+
+@pytest.mark.parametrize("n", [18, 54, 128])
+def test_mixed_inverse_refined_to_fp64(n):
+    a = crand(4, n, n) + 3 * np.eye(n)
+    x, resid = native.zinv_batch(a, precision="mixed", newton=2)
+    for i in range(4):
+        assert rel(x[i], np.linalg.inv(a[i])) < 1e-12
+    assert resid < 1e-5
+
+
+def _compare_mixed(ep):
+    g = api.cpacoord(ep, precision="mixed")
+    o = O.cpacoord(ep, nthreads=8)
+    assert o["status"] == 0 and g["status"] == 0
+    assert g["cpa_iterations"] == o["cpa_iterations"]
+    for key in ("tauc", "taua", "taub", "tminv"):
+        assert rel(g[key], o[key]) < TOL_MIXED, (key, rel(g[key], o[key]))
+    return g, o
+
+
+@pytest.mark.parametrize("ie", [2, 15])
+def test_mixed_cpacoord_plain_fcc(ie):
+    _compare_mixed(W.energy_problem(W.plain_fcc(nset=6), ie))
+
+
+def test_mixed_cpacoord_relativistic_pl4_lmax3():
+    _compare_mixed(W.energy_problem(W.rel_bcc(nsets=[3] * 24), 18))
+
+
+def test_mixed_cpacoord_cpa_alloy():
+    spec = W.rel_bcc_cpa(nsets=[2] * 24)
+    spec.lmax = 2
+    g, o = _compare_mixed(W.energy_problem(spec, 14))
+    assert g["cpa_iterations"] > 1

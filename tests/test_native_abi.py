@@ -32,14 +32,14 @@ def test_struct_layouts_match_header(tmp_path):
     src.write_text(
         '#include <stdio.h>\n#include <stddef.h>\n#include "skkr_gpu.h"\n'
         'int main(void){printf("%zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(skkr_sizes),'
-        ' offsetof(skkr_sizes, errmax), offsetof(skkr_sizes, cpatol), offsetof(skkr_sizes, nk_chunk),'
+        ' offsetof(skkr_sizes, errmax), offsetof(skkr_sizes, cpatol), offsetof(skkr_sizes, slices),'
         ' sizeof(skkr_rtable), offsetof(skkr_rtable, blkmap), sizeof(skkr_status),'
         ' offsetof(skkr_status, max_refine_resid)); return 0;}\n')
     exe = tmp_path / "probe"
     subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
     got = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True).stdout.split()]
     S, R, T = native.Sizes, native.RTable, native.Status
-    want = [ctypes.sizeof(S), S.errmax.offset, S.cpatol.offset, S.nk_chunk.offset, ctypes.sizeof(R),
+    want = [ctypes.sizeof(S), S.errmax.offset, S.cpatol.offset, S.slices.offset, ctypes.sizeof(R),
             R.blkmap.offset, ctypes.sizeof(T), T.max_refine_resid.offset]
     assert got == want
 
