@@ -48,7 +48,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
+    ap.add_argument("--no-fp64-compare", action="store_true")
     ap.add_argument("--energies", default="", help="comma list overriding the step energies")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", action="store_true",
@@ -235,6 +236,71 @@ def run_reference(args, rank, ws):
     print(json.dumps(line), flush=True)
 
 
+def timed_steps(ctx, order, slot_of, eps, args, flush, stats=False):
+    """Run warmup + timed steps on staged slots; device time from CUDA events
+    on the library stream (max over ranks done by the caller)."""
+    import torch
+    from skkr_budapest_gb300 import native as N
+    for i in range(args.warmup):
+        ctx.run_slot(slot_of[order[i]])
+    torch.cuda.synchronize()
+    if stats:
+        N.kernel_stats_start()
+    t_dev, pts, launches, dec_iters, resid = 0.0, 0, 0, 0, 0.0
+    w0 = time.perf_counter()
+    for i in range(args.steps):
+        ie = order[args.warmup + i]
+        l2_flush(flush)
+        torch.cuda.synchronize()
+        st = ctx.run_slot(slot_of[ie])
+        t_dev += st.run_ms
+        pts += eps[ie].nk
+        launches += st.gpu_launches
+        dec_iters += st.dec_iters_total
+        resid = max(resid, st.max_refine_resid)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - w0
+    ks = N.kernel_stats_stop() if stats else None
+    return dict(t_dev=t_dev, pts=pts, launches=launches, dec_iters=dec_iters, wall=wall, ks=ks, resid=resid)
+
+
+def roofline(ks, precision):
+    dom = max(ks.items(), key=lambda kv: kv[1]["ms"])
+    name, d = dom
+    # DRAM bytes of one launch from the committed ncu capture, scaled to this
+    # run's average work per launch (traffic grows with the matrices processed)
+    tr = traffic_from_profiles().get(name)
+    traffic = None
+    if tr and d["launches"]:
+        traffic = tr["dram_bytes"] * (d["work"] / d["launches"]) / tr["work"]
+    peaks = {}
+    if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")):
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    if name in ("gk_ft", "other"):
+        peak = peaks.get("hbm_gbs", 6800.0)
+        ach = d["work"] / (d["ms"] * 1e-3) / 1e9
+        roof = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                "traffic": traffic, "kernel": name}
+    elif name == "ozaki":
+        # algorithmic BF16 tensor FLOP/s of the sliced complex products:
+        # S(S+1)/2 real GEMMs of n x 2n x 2n per complex product
+        peak = peaks.get("bf16_tflops", 1889.5)
+        ach = d["work"] / (d["ms"] * 1e-3) / 1e12
+        roof = {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
+                "traffic": traffic, "kernel": "k_ozaki (sliced complex GEMM, tcgen05)",
+                "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst); frac is of measured"}
+    else:
+        peak = fp64_peak_tflops()
+        ach = d["work"] / (d["ms"] * 1e-3) / 1e12
+        roof = {"bound": "fp64", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
+                "traffic": traffic, "kernel": name,
+                "peak_source": "cuBLAS ZGEMM 2048^3 measured in this run (no FP64 figure in MEASURED_PEAKS.json)"}
+    tot = max(1e-9, sum(x["ms"] for x in ks.values()))
+    roof["per_kernel"] = {k: {"launches": v["launches"], "ms": round(v["ms"], 3), "share": round(v["ms"] / tot, 4)}
+                          for k, v in ks.items()}
+    return roof
+
+
 def run_ours(args, rank, ws):
     import torch
     from skkr_budapest_gb300 import api, native as N
@@ -253,41 +319,40 @@ def run_ours(args, rank, ws):
             slot_of[ie] = len(slot_of)
             ctx.stage_slot(slot_of[ie], eps[ie])
     flush = torch.empty(256 * 2 ** 20 // 4, dtype=torch.float32, device="cuda")  # > L2 (129 MB)
-    for i in range(args.warmup):
-        ctx.run_slot(slot_of[order[i]])
-    torch.cuda.synchronize()
     barrier(ws)
     clocks = Clocks()
     clocks.start()
-    N.kernel_stats_start()
-    t_dev = 0.0
-    pts = 0
-    launches = 0
-    dec_iters = 0
-    torch.cuda.synchronize()
-    w0 = time.perf_counter()
-    for i in range(args.steps):
-        ie = order[args.warmup + i]
-        l2_flush(flush)
-        torch.cuda.synchronize()
-        st = ctx.run_slot(slot_of[ie])
-        t_dev += st.run_ms
-        pts += eps[ie].nk
-        launches += st.gpu_launches
-        dec_iters += st.dec_iters_total
-    torch.cuda.synchronize()
-    wall = time.perf_counter() - w0
-    ks = N.kernel_stats_stop()
-    if args.profile:
-        clocks.stop()
-        ctx.close()
-        print(json.dumps({"profile_run": True, "points": pts, "device_ms": t_dev, "launches": launches}))
-        return
+    r = timed_steps(ctx, order, slot_of, eps, args, flush, stats=True)
     clk = clocks.stop()
+    if args.profile:
+        ctx.close()
+        print(json.dumps({"profile_run": True, "points": r["pts"], "device_ms": r["t_dev"],
+                          "launches": r["launches"]}))
+        return
     barrier(ws)
-    t_max = max_over_ranks(t_dev, ws)
-    pts_all = sum_over_ranks(pts, ws)
+    t_max = max_over_ranks(r["t_dev"], ws)
+    pts_all = sum_over_ranks(r["pts"], ws)
     value = pts_all / (t_max * 1e-3)
+
+    # the same steps through the plain FP64 GPU path: the metric's denominator,
+    # and the error of the k-summed tau against it
+    fp64 = None
+    if args.precision == "mixed" and not args.no_fp64_compare:
+        cref = api.Context.for_problem(eps[order[0]], precision="fp64")
+        for ie, sl in slot_of.items():
+            cref.stage_slot(sl, eps[ie])
+        r64 = timed_steps(cref, order, slot_of, eps, args, flush)
+        errs = []
+        for ie, sl in slot_of.items():
+            if ie in order[args.warmup:]:
+                a = ctx.fetch_slot(sl)["tauc"]
+                b = cref.fetch_slot(sl)["tauc"]
+                errs.append(float(np.linalg.norm(a - b) / np.linalg.norm(b)))
+        cref.close()
+        t64 = max_over_ranks(r64["t_dev"], ws)
+        v64 = pts_all / (t64 * 1e-3)
+        fp64 = {"value": v64, "unit": UNIT, "ms_per_step": t64 / args.steps, "speedup": value / v64,
+                "max_rel_err_tau_vs_fp64": max(errs) if errs else None}
 
     # e2e: the reference-facing call with host buffers, same steps
     barrier(ws)
@@ -295,49 +360,29 @@ def run_ours(args, rank, ws):
     h2d = d2h = 0
     for i in range(args.steps):
         ie = order[args.warmup + i]
-        r = ctx.cpacoord(eps[ie])
-        h2d += r["h2d_bytes"]
-        d2h += r["d2h_bytes"]
+        rr = ctx.cpacoord(eps[ie])
+        h2d += rr["h2d_bytes"]
+        d2h += rr["d2h_bytes"]
     torch.cuda.synchronize()
     e_wall = max_over_ranks(time.perf_counter() - e0, ws)
     e2e = pts_all / e_wall
 
-    # roofline of the dominant kernel class, from the live event timings
-    dom = max(ks.items(), key=lambda kv: kv[1]["ms"])
-    name, d = dom
-    # DRAM bytes of one launch from the committed ncu capture, scaled to this
-    # run's average work per launch (traffic grows with the matrices processed)
-    tr = traffic_from_profiles().get(name)
-    traffic = None
-    if tr and d["launches"]:
-        traffic = tr["dram_bytes"] * (d["work"] / d["launches"]) / tr["work"]
-    if name == "gk_ft":
-        peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"] if os.path.exists(
-            os.path.join(ROOT, "MEASURED_PEAKS.json")) else 6800.0
-        ach = d["work"] / (d["ms"] * 1e-3) / 1e9
-        roof = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                "traffic": traffic, "kernel": name}
-    else:
-        peak = fp64_peak_tflops()
-        ach = d["work"] / (d["ms"] * 1e-3) / 1e12
-        roof = {"bound": "fp64", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
-                "traffic": traffic, "kernel": name,
-                "peak_source": "cuBLAS ZGEMM 2048^3 measured in this run (no FP64 figure in MEASURED_PEAKS.json)"}
-    roof["per_kernel"] = {k: {"launches": v["launches"], "ms": round(v["ms"], 3),
-                              "share": round(v["ms"] / max(1e-9, sum(x["ms"] for x in ks.values())), 4)}
-                          for k, v in ks.items()}
+    roof = roofline(r["ks"], args.precision)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "c128" if args.precision == "fp64" else "c128-mixed",
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "c128" if args.precision == "fp64" else "c128 via BF16x6 slices + FP64 refinement",
             "data": "synthetic (seeded square wells, real-space screened structure constants)",
             "config": {"workload": WORKLOAD, "precision": args.precision,
                        "step": "one contour energy, all k, full CPA pass",
-                       "step_energies": order[args.warmup:], "points": pts,
+                       "step_energies": order[args.warmup:], "points": r["pts"],
                        "l2": "256 MB buffer written between steps; per-step working set > 1 GB",
-                       "wall_s": round(wall, 3), "dec_iters": dec_iters},
+                       "wall_s": round(r["wall"], 3), "dec_iters": r["dec_iters"],
+                       "max_newton_resid": r["resid"]},
+            "fp64_gpu": fp64,
             "roofline": roof, "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d // args.steps,
                                       "d2h_bytes_per_step": d2h // args.steps},
-            "gpu_launches": launches, "clocks": clk}
+            "gpu_launches": r["launches"], "clocks": clk}
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(os.cpu_count() or 1)
     ctx.close()

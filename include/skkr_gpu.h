@@ -154,8 +154,9 @@ int skkr_gpu_fetch_slot(skkr_ctx *ctx, int slot, double *tminv, double *tauc,
 
 /* Per-kernel-class timing with CUDA events (process wide).  enable=1 resets
  * and starts; enable=0 stops and writes out[cls*3 + {launches, total ms,
- * algorithmic work}] for cls = 0 complex GEMM (FLOP), 1 Gauss-Jordan
- * inverse (FLOP), 2 G(k) transform (bytes written), 3 other. */
+ * algorithmic work}] for cls = 0 FP64 complex GEMM (FLOP), 1 Gauss-Jordan
+ * inverse (FP64-equivalent FLOP), 2 G(k) transform (bytes written), 3 other,
+ * 4 sliced complex GEMM on the tensor cores (BF16 FLOP). */
 int skkr_gpu_kernel_stats(int enable, double *out);
 
 /* Screened -> physical tau of one layer on the device

@@ -79,7 +79,7 @@ void skkr_after_launch(const char *file, int line);
 // default; bench.py switches it on for the timed region).  `work` is the
 // algorithmic FLOP (or byte) count of the launch.  Masked launches count the
 // active items the host announced through skkr_set_active_items (-1: all).
-enum { KS_GEMM = 0, KS_GJ = 1, KS_GKFT = 2, KS_OTHER = 3, KS_NCLS = 4 };
+enum { KS_GEMM = 0, KS_GJ = 1, KS_GKFT = 2, KS_OTHER = 3, KS_OZAKI = 4, KS_NCLS = 5 };
 void kstat_begin(int cls, double work, cudaStream_t st);
 void kstat_end(cudaStream_t st);
 long long skkr_active_items(long long all);

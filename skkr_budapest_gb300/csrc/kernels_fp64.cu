@@ -291,10 +291,11 @@ __global__ void __launch_bounds__(512) k_zgj(MatRef A, int n, int nc, const int 
         int oj = __shfl_down_sync(0xffffffffu, bj, o);
         if (ob > best || (ob == best && oj < bj)) { best = ob; bj = oj; }
       }
-      if (lane == 0) { ri[0] = bj; ind[i] = bj; }
+      if (lane == 0) { ri[0] = bj < n ? bj : i; ind[i] = bj < n ? bj : i; }
     }
     __syncthreads();
-    const int kp = ri[0];
+    int kp = ri[0];
+    if (kp >= n) kp = i;  // all candidates NaN: keep the index in range
     if (kp != i) {
       for (int r = tid; r < n; r += nth) {
         zd t = a[r + (long long)i * ld];
@@ -368,8 +369,11 @@ void launch_zaxpby(const MatRef &out, const MatRef &a, const MatRef *b, double s
   if (nk <= 0 || nc <= 0) return;
   int per = (n * n + 255) / 256;
   dim3 grid(per < 32 ? per : 32, nk * nc);
+  const long long items = act ? skkr_active_items((long long)nk * nc) : (long long)nk * nc;
+  kstat_begin(KS_OTHER, (double)items * n * n * 16.0 * (2 + (b != nullptr) + (d != nullptr)), st);
   k_zaxpby<<<grid, 256, 0, st>>>(out, a, b ? *b : a, s1, d ? *d : a, s2, b != nullptr, d != nullptr,
                                  n, nc, act);
+  kstat_end(st);
   SKKR_LAUNCHED();
 }
 

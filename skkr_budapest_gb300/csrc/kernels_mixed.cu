@@ -22,10 +22,11 @@
 // M = n, N = 2n, K = 2n; the epilogue writes column jj < n into Re C(:,jj) and
 // column n+j into Im C(:,j).
 //
-// Staging layouts (bf16, K contiguous = K-major for both UMMA operands):
-//   A'[item][s][M'][K']   M' = 128 * mtiles, K' = 64 * kblocks (zero padded)
-//   B'[item][s][N'][K']   N' = NT * ntiles (zero padded)
-// Tiles reach shared memory by TMA (3-D tensor maps, 128-byte swizzle).
+// Staging layouts (bf16, K-major for both UMMA operands, tiled by k-block so
+// that one TMA box is one contiguous block):
+//   A'[item][s][kb][M'][32]   M' = 128 * mtiles, kb < kblocks = ceil(2n/32)
+//   B'[item][s][kb][N'][32]   N' = NT * ntiles (zero padded)
+// Tiles reach shared memory by TMA (3-D tensor maps, 64-byte swizzle).
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
@@ -41,7 +42,8 @@ namespace {
 
 constexpr int NT = 96;            // N tile (TMEM columns per accumulator)
 constexpr int MT = 128;           // M tile (UMMA M)
-constexpr int KB = 64;            // K per k-block (one 128-byte swizzle row of bf16)
+constexpr int KB = 32;            // K per k-block (one 64-byte swizzle row of bf16)
+constexpr int NSTAGE = 2;         // shared-memory pipeline stages
 constexpr int NACC = 5;           // TMEM accumulators: one per level p+q = 0..4
 constexpr long long WAIT_LIMIT = 1LL << 22;
 
@@ -128,15 +130,15 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
   for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
 }
 
-// UMMA shared-memory descriptor: K-major, 128-byte swizzle, 8-row groups
-// 1024 bytes apart (tile base 1024-byte aligned).
-__device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
+// UMMA shared-memory descriptor: K-major, 64-byte swizzle (rows of 32 bf16),
+// 8-row groups 512 bytes apart (tile base 512-byte aligned).
+__device__ __forceinline__ uint64_t sdesc_sw64(uint32_t saddr) {
   uint64_t d = 0;
   d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
-  d |= (uint64_t)1 << 16;            // leading byte offset (unused for swizzled K-major)
-  d |= (uint64_t)(1024 >> 4) << 32;  // stride byte offset
-  d |= (uint64_t)1 << 46;            // descriptor version
-  d |= (uint64_t)2 << 61;            // 128-byte swizzle
+  d |= (uint64_t)1 << 16;           // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(512 >> 4) << 32;  // stride byte offset: 8 rows x 64 bytes
+  d |= (uint64_t)1 << 46;           // descriptor version
+  d |= (uint64_t)4 << 61;           // 64-byte swizzle
   return d;
 }
 // instruction descriptor: BF16 x BF16 -> FP32, K-major A and B, M x N
@@ -145,55 +147,109 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int m, int n) {
 }
 
 // ------------------------------------------------------------------ slicing
-__device__ __forceinline__ double pow2_scale(double amax) {
-  if (!(amax > 0.0) || !isfinite(amax)) return 1.0;
-  int e;
-  frexp(amax, &e);  // amax = m 2^e, m in [0.5, 1)
-  return ldexp(1.0, e);
-}
+// All element-wise work below uses integer arithmetic on the IEEE bit
+// patterns: this GPU issues about 2 FP64 operations per clock per SM against
+// 64 integer operations, so a single FP64 multiply per element would dominate.
+//
+// Scales are powers of two kept as exponents: sigma = 2^es with
+// es = (biased exponent of max |x|) - 1022, i.e. sigma >= max |x| > sigma/2.
 
+// |x| bits of a double (non-negative doubles order like their bit patterns)
+__device__ __forceinline__ unsigned long long abs_bits(double x) {
+  return (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
+}
+// log2 of the power-of-two scale for a max-|x| bit pattern (0 for zero)
+__device__ __forceinline__ int scale_exp(unsigned long long amax_bits) {
+  const int ex = (int)(amax_bits >> 52);
+  return ex == 0 ? 0 : ex - 1022;
+}
+// round(x * 2^E) as a signed 64-bit integer (|result| < 2^62 assumed), using
+// only integer operations; zero and subnormal inputs give 0
+__device__ __forceinline__ long long fix_round(double x, int E) {
+  const long long b = __double_as_longlong(x);
+  const int ex = (int)((b >> 52) & 0x7FF);
+  if (ex == 0) return 0;
+  const long long mant = (b & 0xFFFFFFFFFFFFFll) | 0x10000000000000ll;
+  const int sh = ex - 1075 + E;
+  long long m;
+  if (sh >= 0) {
+    m = sh >= 11 ? 0 : mant << sh;  // callers keep |x 2^E| < 2^62
+  } else {
+    const int r = -sh;
+    m = r >= 63 ? 0 : (mant + (1ll << (r - 1))) >> r;
+  }
+  return b < 0 ? -m : m;
+}
+__device__ __forceinline__ float pow2f(int e) { return __int_as_float((127 + e) << 23); }
+
+// balanced base-256 digits of Y = round(x 2^(7+8(S-1)) / sigma), most
+// significant first (|d| <= 128), from the two 32-bit halves of |Y|
 template <int S>
-__device__ __forceinline__ void slice_store(double x, double inv_scale, int wshift, __nv_bfloat16 *dst,
-                                            long long sstride) {
-  double y = x * inv_scale * 128.0;
+__device__ __forceinline__ void slice_digits(double x, int es, float *dig) {
+  const long long Y = fix_round(x, 7 + 8 * (S - 1) - es);
+  const unsigned long long u = (unsigned long long)(Y < 0 ? -Y : Y);
+  const uint32_t lo = (uint32_t)u, hi = (uint32_t)(u >> 32);
+  const bool neg = Y < 0;
+  int carry = 0;
 #pragma unroll
-  for (int p = 0; p < S; p++) {
-    double s = rint(y);
-    dst[p * sstride] = __double2bfloat16(ldexp(s, wshift - 8 * p));
-    y = (y - s) * 256.0;
+  for (int q = 0; q < S; q++) {  // q = 0: least significant digit
+    const int bit = 8 * q;
+    const uint32_t raw = bit < 32 ? (lo >> bit) & 0xFFu : (hi >> (bit - 32)) & 0xFFu;
+    int d = (int)raw + carry;
+    carry = d > 128;
+    d -= carry << 8;
+    dig[S - 1 - q] = (float)(neg ? -d : d);
   }
 }
 
-// A' from complex A (n x n, MatRef): one CTA per (item, 32-row block).
-// Row scales over re/im of the whole row, then a shared-memory transpose so
-// that both the FP64 reads (along rows i) and the bf16 writes (along kk)
-// are coalesced.
+template <int S>
+__device__ __forceinline__ void store_digits(const float *dig, float sign, int wshift, __nv_bfloat16 *dst,
+                                             long long sstride) {
+#pragma unroll
+  for (int p = 0; p < S; p++) dst[p * sstride] = __float2bfloat16_rn(sign * dig[p] * pow2f(wshift - 8 * p));
+}
+
+template <int S>
+__device__ __forceinline__ void slice_store(double x, int es, int wshift, __nv_bfloat16 *dst,
+                                            long long sstride) {
+  float dig[S];
+  slice_digits<S>(x, es, dig);
+  store_digits<S>(dig, 1.0f, wshift, dst, sstride);
+}
+
+// element (row r, K index kk) of one slice region in the k-block tiled layout
+__device__ __forceinline__ long long tiled(int r, int kk, int rows) {
+  return ((long long)(kk >> 5) * rows + r) * 32 + (kk & 31);
+}
+
 template <int S>
 __global__ void __launch_bounds__(256) k_split_a(MatRef A, int n, int nc, const int *__restrict__ act,
                                                  __nv_bfloat16 *__restrict__ out, int Mp, int Kp,
-                                                 double *__restrict__ sigma) {
+                                                 int *__restrict__ sigma) {
   const int item = blockIdx.y, kk0 = item / nc, cc = item % nc;
   if (act && !act[item]) return;
   const zd *a = mat_ptr(A, kk0, cc);
   const int r0 = blockIdx.x * 32, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  __shared__ double red[8][32];
-  __shared__ double sc[32];
+  __shared__ unsigned long long red[8][32];
+  __shared__ int sc[32];
   __shared__ zd T[32][33];
-  double m = 0.0;
+  unsigned long long m = 0;
   const int row = r0 + lane;
   if (row < n)
     for (int k = w; k < n; k += 8) {
       zd v = a[row + (long long)k * A.ld];
-      m = fmax(m, fmax(fabs(v.x), fabs(v.y)));
+      const unsigned long long bx = abs_bits(v.x), by = abs_bits(v.y);
+      m = bx > m ? bx : m;
+      m = by > m ? by : m;
     }
   red[w][lane] = m;
   __syncthreads();
   if (w == 0) {
-    double mm = 0.0;
-    for (int q = 0; q < 8; q++) mm = fmax(mm, red[q][lane]);
-    double s = pow2_scale(mm);
-    sc[lane] = s;
-    if (r0 + lane < Mp) sigma[(long long)item * Mp + r0 + lane] = s;
+    unsigned long long mm = 0;
+    for (int q = 0; q < 8; q++) mm = red[q][lane] > mm ? red[q][lane] : mm;
+    const int es = scale_exp(mm);
+    sc[lane] = es;
+    if (r0 + lane < Mp) sigma[(long long)item * Mp + r0 + lane] = es;
   }
   __syncthreads();
   const long long sstride = (long long)Mp * Kp;
@@ -207,10 +263,10 @@ __global__ void __launch_bounds__(256) k_split_a(MatRef A, int n, int nc, const 
     for (int q = w; q < 32; q += 8) {
       const int r = r0 + q, col = c0 + lane;
       if (r < n && col < n) {
-        const double inv = 1.0 / sc[q];
+        const int es = sc[q];
         zd v = T[q][lane];
-        slice_store<S>(v.x, inv, 0, base + (long long)r * Kp + col, sstride);
-        slice_store<S>(v.y, inv, 0, base + (long long)r * Kp + n + col, sstride);
+        slice_store<S>(v.x, es, 0, base + tiled(r, col, Mp), sstride);
+        slice_store<S>(v.y, es, 0, base + tiled(r, n + col, Mp), sstride);
       }
     }
     __syncthreads();
@@ -222,42 +278,67 @@ __global__ void __launch_bounds__(256) k_split_a(MatRef A, int n, int nc, const 
 template <int S>
 __global__ void __launch_bounds__(256) k_split_b(MatRef B, int n, int nc, const int *__restrict__ act,
                                                  __nv_bfloat16 *__restrict__ out, int Np, int Kp,
-                                                 double *__restrict__ tau) {
+                                                 int *__restrict__ tau) {
   const int item = blockIdx.y, kk0 = item / nc, cc = item % nc;
   if (act && !act[item]) return;
   const int lane = threadIdx.x & 31, j = blockIdx.x * 8 + (threadIdx.x >> 5);
   if (j >= n) return;
   const zd *b = mat_ptr(B, kk0, cc) + (long long)j * B.ld;
-  double m = 0.0;
+  unsigned long long m = 0;
   for (int k = lane; k < n; k += 32) {
     zd v = b[k];
-    m = fmax(m, fmax(fabs(v.x), fabs(v.y)));
+    const unsigned long long bx = abs_bits(v.x), by = abs_bits(v.y);
+    m = bx > m ? bx : m;
+    m = by > m ? by : m;
   }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-  const double s = pow2_scale(m), inv = 1.0 / s;
-  if (lane == 0) tau[(long long)item * n + j] = s;
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long t = __shfl_xor_sync(0xffffffffu, m, o);
+    m = t > m ? t : m;
+  }
+  const int es = scale_exp(m);
+  if (lane == 0) tau[(long long)item * n + j] = es;
   const long long sstride = (long long)Np * Kp;
   __nv_bfloat16 *base = out + (long long)item * S * sstride;
-  __nv_bfloat16 *rj = base + (long long)j * Kp, *rjn = base + (long long)(n + j) * Kp;
   for (int k = lane; k < n; k += 32) {
     zd v = b[k];
-    slice_store<S>(v.x, inv, 16, rj + k, sstride);
-    slice_store<S>(-v.y, inv, 16, rj + n + k, sstride);
-    slice_store<S>(v.y, inv, 16, rjn + k, sstride);
-    slice_store<S>(v.x, inv, 16, rjn + n + k, sstride);
+    float dr[S], di[S];
+    slice_digits<S>(v.x, es, dr);
+    slice_digits<S>(v.y, es, di);
+    store_digits<S>(dr, 1.0f, 16, base + tiled(j, k, Np), sstride);
+    store_digits<S>(di, -1.0f, 16, base + tiled(j, n + k, Np), sstride);
+    store_digits<S>(di, 1.0f, 16, base + tiled(n + j, k, Np), sstride);
+    store_digits<S>(dr, 1.0f, 16, base + tiled(n + j, n + k, Np), sstride);
   }
 }
 
 // ------------------------------------------------------------------ the GEMM
 struct OzArgs {
   int n, mtiles, ntiles, kblocks, nc, mode;
-  const double *sigma;  // [item][M']
-  const double *tau;    // [item][n]
+  const int *sigma;     // [item][M']  row scale exponents of A
+  const int *tau;       // [item][n]   column scale exponents of B
   MatRef C, D, E;
   const int *act;
   int *err;
 };
+
+// FP32 accumulator value -> int64 in units of 2^-16 (bit manipulation only).
+// Levels 0..3 hold exact multiples of 2^(16-8l) >= 2^-8; the shared tail
+// level is truncated at 2^-16, 2^-55 below the leading level.
+__device__ __forceinline__ long long f2fix16(float v) {
+  const int b = __float_as_int(v);
+  const int ex = (b >> 23) & 0xFF;
+  if (ex == 0) return 0;
+  const long long mant = (b & 0x7FFFFF) | 0x800000;
+  const int sh = ex - 150 + 16;
+  const long long m = sh >= 0 ? (mant << sh) : (sh > -31 ? (mant >> -sh) : 0);
+  return b < 0 ? -m : m;
+}
+// x * 2^e for a normal double x by exponent addition (x == 0 stays 0)
+__device__ __forceinline__ double scale_pow2(double x, int e) {
+  if (x == 0.0) return 0.0;
+  return __longlong_as_double(__double_as_longlong(x) + ((long long)e << 52));
+}
 
 // accumulator of product (p, q), 0-based slices: its level p+q; levels >= 4
 // share the last accumulator (they sit 2^-32 and further below the leading
@@ -273,23 +354,28 @@ __global__ void __launch_bounds__(128, 1) k_ozaki(const __grid_constant__ CUtens
   if (g.act && !g.act[item]) return;
   const int mt = blockIdx.x / g.ntiles, nt = blockIdx.x % g.ntiles;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
-  // 1024-byte aligned tile area: S A tiles (MT x KB) then S B tiles (NT x KB)
+  // NSTAGE stages, each: S A tiles (MT x KB) then S B tiles (NT x KB), 1024-byte aligned
   unsigned char *tiles = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   constexpr uint32_t A_BYTES = MT * KB * 2, B_BYTES = NT * KB * 2;
-  unsigned char *tA = tiles, *tB = tiles + S * A_BYTES;
-  __shared__ __align__(8) uint64_t bar_load, bar_mma;
+  constexpr uint32_t STAGE_BYTES = S * (A_BYTES + B_BYTES);
+  __shared__ __align__(8) uint64_t bar_full[NSTAGE], bar_empty[NSTAGE], bar_acc;
   __shared__ uint32_t tmem_base;
-  __shared__ int failed;
+  __shared__ volatile int failed, issued_kb, consumed_kb;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
   if (warp == 0) {
     tmem_alloc(&tmem_base, 512);
     tmem_relinquish();
   }
-  if (threadIdx.x == 0) {
+  if (threadIdx.x == 32) {
     failed = 0;
-    mbar_init(&bar_load, 1);
-    mbar_init(&bar_mma, 1);
+    issued_kb = -1;
+    consumed_kb = -1;
+    for (int i = 0; i < NSTAGE; i++) {
+      mbar_init(&bar_full[i], 1);
+      mbar_init(&bar_empty[i], 1);
+    }
+    mbar_init(&bar_acc, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
@@ -298,56 +384,78 @@ __global__ void __launch_bounds__(128, 1) k_ozaki(const __grid_constant__ CUtens
   tc_fence_after();
   const uint32_t tbase = tmem_base;
   constexpr uint32_t IDESC = idesc_bf16(MT, NT);
+  const int nkb = g.kblocks;
 
-  for (int kb = 0; kb < g.kblocks; kb++) {
-    const uint32_t phase = kb & 1;
-    if (threadIdx.x == 0 && !failed) {
-      mbar_expect_tx(&bar_load, S * (A_BYTES + B_BYTES));
-#pragma unroll
-      for (int s = 0; s < S; s++) {
-        tma_load_3d(tA + s * A_BYTES, &tmA, kb * KB, mt * MT, item * S + s, &bar_load);
-        tma_load_3d(tB + s * B_BYTES, &tmB, kb * KB, nt * NT, item * S + s, &bar_load);
-      }
-      if (!mbar_wait(&bar_load, phase)) {
+  if (warp == 0 && lane == 0) {
+    // TMA producer
+    for (int kb = 0; kb < nkb && !failed; kb++) {
+      const int st = kb % NSTAGE;
+      if (kb >= NSTAGE && !mbar_wait(&bar_empty[st], ((kb / NSTAGE) - 1) & 1)) {
         failed = 1;
-        mbar_wait(&bar_load, phase);  // give in-flight copies a second bounded chance to land
+        break;
       }
-      if (!failed) {
-        tc_fence_after();
-        bool first[NACC] = {kb == 0, kb == 0, kb == 0, kb == 0, kb == 0};
+      unsigned char *sA = tiles + st * STAGE_BYTES, *sB = sA + S * A_BYTES;
+      mbar_expect_tx(&bar_full[st], STAGE_BYTES);
 #pragma unroll
-        for (int p = 0; p < S; p++)
-#pragma unroll
-          for (int q = 0; q < S; q++) {
-            if (p + q > S - 1) continue;  // keep p+q <= S+1 in 1-based slices
-            const int lv = level_of(p, q);
-            const uint32_t a0 = smem_u32(tA + p * A_BYTES), b0 = smem_u32(tB + q * B_BYTES);
-#pragma unroll
-            for (int k = 0; k < KB / 16; k++) {
-              umma_bf16(tbase + lv * NT, sdesc_sw128(a0 + 32 * k), sdesc_sw128(b0 + 32 * k), IDESC,
-                        first[lv] ? 0u : 1u);
-              first[lv] = false;
-            }
-          }
+      for (int sl = 0; sl < S; sl++) {
+        const int z = (item * S + sl) * nkb + kb;
+        tma_load_3d(sA + sl * A_BYTES, &tmA, 0, mt * MT, z, &bar_full[st]);
+        tma_load_3d(sB + sl * B_BYTES, &tmB, 0, nt * NT, z, &bar_full[st]);
       }
-      umma_commit(&bar_mma);
-      if (!mbar_wait(&bar_mma, phase)) {
-        failed = 1;
-        mbar_wait(&bar_mma, phase);  // MMAs must be done before TMEM is released
-      }
+      issued_kb = kb;
     }
-    __syncthreads();
-    if (failed) break;
+  } else if (warp == 1 && lane == 0) {
+    // MMA issuer
+    bool first[NACC] = {true, true, true, true, true};
+    for (int kb = 0; kb < nkb; kb++) {
+      const int st = kb % NSTAGE;
+      if (failed || !mbar_wait(&bar_full[st], (kb / NSTAGE) & 1)) {
+        failed = 1;
+        break;
+      }
+      tc_fence_after();
+      const uint32_t a0 = smem_u32(tiles + st * STAGE_BYTES), b0 = a0 + S * A_BYTES;
+#pragma unroll
+      for (int p = 0; p < S; p++)
+#pragma unroll
+        for (int q = 0; q < S; q++) {
+          if (p + q > S - 1) continue;  // keep p+q <= S+1 in 1-based slices
+          const int lv = level_of(p, q);
+#pragma unroll
+          for (int k = 0; k < KB / 16; k++) {
+            umma_bf16(tbase + lv * NT, sdesc_sw64(a0 + p * A_BYTES + 32 * k),
+                      sdesc_sw64(b0 + q * B_BYTES + 32 * k), IDESC, first[lv] ? 0u : 1u);
+            first[lv] = false;
+          }
+        }
+      umma_commit(&bar_empty[st]);  // stage free once these MMAs have read it
+      consumed_kb = kb;
+    }
+    umma_commit(&bar_acc);  // accumulators complete
+  }
+  __syncthreads();
+  // all MMAs (and with them every TMA load they consumed) are done once
+  // bar_acc completes; a bounded wait, then a second one if the first expired
+  if (!mbar_wait(&bar_acc, 0)) {
+    failed = 1;
+    mbar_wait(&bar_acc, 0);
   }
   tc_fence_after();
+  __syncthreads();
   if (failed) {
-    if (threadIdx.x == 0) atomicOr(g.err, 1);
+    if (threadIdx.x == 0) {
+      atomicOr(g.err, 1);
+      // TMA loads issued but never consumed: let them land (bounded) before exit
+      for (int kb = consumed_kb + 1; kb <= issued_kb; kb++)
+        mbar_wait(&bar_full[kb % NSTAGE], (kb / NSTAGE) & 1);
+    }
   } else {
     // epilogue: warp w owns TMEM lanes 32w..32w+31 = rows of this M tile
     const int row = mt * MT + warp * 32 + lane;
     const uint32_t lane_addr = tbase + ((uint32_t)(warp * 32) << 16);
     const int kk = item / g.nc, cc = item % g.nc;
-    const double srow = row < g.n ? g.sigma[(long long)item * (g.mtiles * MT) + row] * 0x1p-30 : 0.0;
+    // accumulators carry 2^-30 sigma_i tau_j; the int64 sum is in units of 2^-16
+    const int erow = row < g.n ? g.sigma[(long long)item * (g.mtiles * MT) + row] - 46 : 0;
     for (int c0 = 0; c0 < NT; c0 += 32) {
       float v[NACC][32];
       constexpr int NL = nlevels(S);
@@ -359,11 +467,10 @@ __global__ void __launch_bounds__(128, 1) k_ozaki(const __grid_constant__ CUtens
         const int jj = nt * NT + c0 + t;
         if (jj < 2 * g.n) {
           const int j = jj < g.n ? jj : jj - g.n, im = jj >= g.n;
-          // smallest level first; every addend is exact in FP64
-          double acc = (double)v[NL - 1][t];
+          long long acc = 0;
 #pragma unroll
-          for (int l = NL - 2; l >= 0; l--) acc += (double)v[l][t];
-          const double val = acc * srow * g.tau[(long long)item * g.n + j];
+          for (int l = 0; l < NL; l++) acc += f2fix16(v[l][t]);
+          const double val = scale_pow2(__ll2double_rn(acc), erow + g.tau[(long long)item * g.n + j]);
           const long long off = 2 * (row + (long long)j * g.C.ld) + im;
           if (g.mode == 0) {
             ((double *)mat_ptr(g.C, kk, cc))[off] = val;
@@ -392,98 +499,166 @@ __global__ void __launch_bounds__(128, 1) k_ozaki(const __grid_constant__ CUtens
 }
 
 // ------------------------------------------------------------------ FP32 GJ
-// Gauss-Jordan with column pivoting (main/gjinv.f) in complex FP32, matrix in
-// shared memory; result written as FP64 into X.  n <= 128.
-__global__ void __launch_bounds__(512) k_cgj32(MatRef A, MatRef X, int n, int nc, const int *__restrict__ act) {
+// Gauss-Jordan with column pivoting (main/gjinv.f) in complex FP32, the
+// matrix held in registers: TY*16 threads as a TY x 16 grid, thread (ty, tx)
+// owning rows ty + TY a (a < RA) and columns tx + 16 b (b < RB).  A step
+// stages the pivot column, the old column i and row i in shared memory (only
+// the owning threads write), then every thread updates its RA x RB block with
+// straight-line FMAs and selects (no per-element branches, so the compiler
+// interleaves the independent chains); the pivot of the next step (largest
+// |a(i+1, j)|^2, j > i, first index on ties) is reduced by the 16 threads
+// that own row i+1.  Two block barriers per step.  The result (written as
+// FP64) only seeds the Newton refinement.
+// Pivot of row `rowidx` (held by the 16 threads of one half warp): the
+// largest |a(rowidx, j)|^2 over jmin <= j < n, first index on ties.
+template <int TY, int RA, int RB>
+__device__ __forceinline__ void gj_row_pivot(const float2 (&m)[RA][RB], int rowidx, int jmin, int n, int tx,
+                                             unsigned hmask, int *kp_out) {
+  const int iar = rowidx / TY;
+  float best = -1.f;
+  int bj = 0x7FFFFFFF;
+#pragma unroll
+  for (int ib = 0; ib < RB; ib++) {
+    float2 v = m[0][ib];
+#pragma unroll
+    for (int ia = 1; ia < RA; ia++) v = (ia == iar) ? m[ia][ib] : v;  // static indices keep m in registers
+    const int j = tx + 16 * ib;
+    const float mm = v.x * v.x + v.y * v.y;
+    const bool ok = j >= jmin && j < n && (mm > best || (mm == best && j < bj));
+    best = ok ? mm : best;
+    bj = ok ? j : bj;
+  }
+#pragma unroll
+  for (int o = 8; o > 0; o >>= 1) {
+    const float ob = __shfl_xor_sync(hmask, best, o, 16);
+    const int oj = __shfl_xor_sync(hmask, bj, o, 16);
+    const bool take = ob > best || (ob == best && oj < bj);
+    best = take ? ob : best;
+    bj = take ? oj : bj;
+  }
+  if (bj >= n) bj = jmin;  // all candidates NaN: keep the index in range
+  if (tx == 0) *kp_out = bj;
+}
+
+template <int TY, int RA, int RB>
+__global__ void __launch_bounds__(TY * 16, 1) k_cgj32(MatRef A, MatRef X, int n, int nc,
+                                                      const int *__restrict__ act) {
+  constexpr int NR = TY * RA, NCOL = 16 * RB;
   const int item = blockIdx.x, kk = item / nc, cc = item % nc;
   if (act && !act[item]) return;
-  extern __shared__ float2 sa[];  // n*n column-major
-  __shared__ int ind[128];
-  __shared__ float2 coli[128], rowi[128];
-  __shared__ float rv[16];
-  __shared__ int ri[16];
-  const int tid = threadIdx.x, nth = blockDim.x, lane = tid & 31, wid = tid >> 5, nw = nth >> 5;
+  __shared__ float2 pc[NR], oc[NR], rowi[NCOL];
+  __shared__ int ind[NR], dest[NR];
+  __shared__ int kp_next;
+  const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
   const zd *a = mat_ptr(A, kk, cc);
-  for (int e = tid; e < n * n; e += nth) {
-    zd v = a[(e % n) + (long long)(e / n) * A.ld];
-    sa[e] = make_float2((float)v.x, (float)v.y);
-  }
+  float2 m[RA][RB];
+#pragma unroll
+  for (int ia = 0; ia < RA; ia++)
+#pragma unroll
+    for (int ib = 0; ib < RB; ib++) {
+      const int r = ty + TY * ia, j = tx + 16 * ib;
+      float2 v = make_float2(0.f, 0.f);
+      if (r < n && j < n) {
+        const zd w = a[r + (long long)j * A.ld];
+        v = make_float2((float)w.x, (float)w.y);
+      }
+      m[ia][ib] = v;
+    }
+  const unsigned hmask = (ty & 1) ? 0xFFFF0000u : 0x0000FFFFu;  // the 16 threads of this ty
+  if (ty == 0) gj_row_pivot<TY, RA, RB>(m, 0, 0, n, tx, hmask, &kp_next);
   __syncthreads();
   for (int i = 0; i < n; i++) {
-    float best = -1.f;
-    int bj = n;
-    for (int j = i + tid; j < n; j += nth) {
-      float2 v = sa[i + j * n];
-      float m = hypotf(v.x, v.y);
-      if (m > best || (m == best && j < bj)) { best = m; bj = j; }
+    const int kp = kp_next;
+    // stage: pivot column kp -> pc, old column i -> oc, row i -> rowi (owners
+    // only); select chains over static indices keep m in registers
+    if (tx == (kp & 15)) {
+      const int kb = kp >> 4;
+#pragma unroll
+      for (int ia = 0; ia < RA; ia++) {
+        float2 v = m[ia][0];
+#pragma unroll
+        for (int ib = 1; ib < RB; ib++) v = (ib == kb) ? m[ia][ib] : v;
+        pc[ty + TY * ia] = v;
+      }
+    }
+    if (tx == (i & 15)) {
+      const int ibi = i >> 4;
+#pragma unroll
+      for (int ia = 0; ia < RA; ia++) {
+        float2 v = m[ia][0];
+#pragma unroll
+        for (int ib = 1; ib < RB; ib++) v = (ib == ibi) ? m[ia][ib] : v;
+        oc[ty + TY * ia] = v;
+      }
+    }
+    if (ty == i % TY) {
+      const int iai = i / TY;
+#pragma unroll
+      for (int ib = 0; ib < RB; ib++) {
+        float2 v = m[0][ib];
+#pragma unroll
+        for (int ia = 1; ia < RA; ia++) v = (ia == iai) ? m[ia][ib] : v;
+        rowi[tx + 16 * ib] = v;
+      }
+    }
+    if (tid == 0) ind[i] = kp;
+    __syncthreads();
+    const float2 piv = pc[i];
+    const float den = piv.x * piv.x + piv.y * piv.y;
+    const float2 q = make_float2(piv.x / den, -piv.y / den);
+    const float2 rw_i = rowi[i], rw_kp = rowi[kp];
+    float2 cr[RA], ocr[RA], rj[RB];
+#pragma unroll
+    for (int ia = 0; ia < RA; ia++) {
+      const int r = ty + TY * ia;
+      const float2 v = pc[r];
+      cr[ia] = (r == i) ? q : make_float2(v.x * q.x - v.y * q.y, v.x * q.y + v.y * q.x);
+      ocr[ia] = oc[r];
     }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      float ob = __shfl_down_sync(0xffffffffu, best, o);
-      int oj = __shfl_down_sync(0xffffffffu, bj, o);
-      if (ob > best || (ob == best && oj < bj)) { best = ob; bj = oj; }
+    for (int ib = 0; ib < RB; ib++) {
+      const int j = tx + 16 * ib;
+      const float2 w = rowi[j];
+      rj[ib] = (j == i) ? rw_kp : ((j == kp) ? rw_i : w);
     }
-    if (lane == 0) { rv[wid] = best; ri[wid] = bj; }
-    __syncthreads();
-    if (wid == 0) {
-      best = lane < nw ? rv[lane] : -2.f;
-      bj = lane < nw ? ri[lane] : n;
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        float ob = __shfl_down_sync(0xffffffffu, best, o);
-        int oj = __shfl_down_sync(0xffffffffu, bj, o);
-        if (ob > best || (ob == best && oj < bj)) { best = ob; bj = oj; }
+    for (int ia = 0; ia < RA; ia++) {
+      const bool isrow = (ty + TY * ia) == i;
+#pragma unroll
+      for (int ib = 0; ib < RB; ib++) {
+        const int j = tx + 16 * ib;
+        float2 v = (j == kp) ? ocr[ia] : m[ia][ib];  // the old column i moves to kp
+        v = isrow ? make_float2(0.f, 0.f) : v;
+        v.x = fmaf(-cr[ia].x, rj[ib].x, v.x);
+        v.x = fmaf(cr[ia].y, rj[ib].y, v.x);
+        v.y = fmaf(-cr[ia].x, rj[ib].y, v.y);
+        v.y = fmaf(-cr[ia].y, rj[ib].x, v.y);
+        m[ia][ib] = (j == i) ? cr[ia] : v;
       }
-      if (lane == 0) { ri[0] = bj; ind[i] = bj; }
     }
-    __syncthreads();
-    const int kp = ri[0];
-    if (kp != i) {
-      for (int r = tid; r < n; r += nth) {
-        float2 t = sa[r + i * n];
-        sa[r + i * n] = sa[r + kp * n];
-        sa[r + kp * n] = t;
-      }
-      __syncthreads();
-    }
-    float2 piv = sa[i + i * n];
-    float den = piv.x * piv.x + piv.y * piv.y;
-    float2 q = make_float2(piv.x / den, -piv.y / den);
-    for (int j = tid; j < n; j += nth) rowi[j] = sa[i + j * n];
-    for (int r = tid; r < n; r += nth) {
-      float2 v = sa[r + i * n];
-      coli[r] = (r == i) ? q : make_float2(v.x * q.x - v.y * q.y, v.x * q.y + v.y * q.x);
-    }
-    __syncthreads();
-    for (int r = tid; r < n; r += nth) sa[r + i * n] = coli[r];
-    for (int e = tid; e < n * n; e += nth) {
-      const int r = e % n, j = e / n;
-      if (j == i) continue;
-      float2 v = (r == i) ? make_float2(0.f, 0.f) : sa[e];
-      const float2 c = coli[r], w = rowi[j];
-      v.x = fmaf(-c.x, w.x, v.x);
-      v.x = fmaf(c.y, w.y, v.x);
-      v.y = fmaf(-c.x, w.y, v.y);
-      v.y = fmaf(-c.y, w.x, v.y);
-      sa[e] = v;
-    }
+    if (i + 1 < n && ty == ((i + 1) % TY)) gj_row_pivot<TY, RA, RB>(m, i + 1, i + 1, n, tx, hmask, &kp_next);
     __syncthreads();
   }
-  for (int i = n - 1; i >= 0; i--) {
-    const int j = ind[i];
-    if (j == i) continue;
-    for (int c = tid; c < n; c += nth) {
-      float2 t = sa[i + c * n];
-      sa[i + c * n] = sa[j + c * n];
-      sa[j + c * n] = t;
+  // final row swaps of gjinv.f (i = n-1 .. 0: rows i <-> ind[i]) as one permutation
+  if (tid == 0) {
+    for (int r = 0; r < n; r++) dest[r] = r;  // dest[pos] = original row now at pos
+    for (int i2 = n - 1; i2 >= 0; i2--) {
+      const int j = ind[i2];
+      const int t = dest[i2];
+      dest[i2] = dest[j];
+      dest[j] = t;
     }
-    __syncthreads();
+    for (int pos = 0; pos < n; pos++) ind[dest[pos]] = pos;  // ind[orig row] = final position
   }
+  __syncthreads();
   zd *x = mat_ptr(X, kk, cc);
-  for (int e = tid; e < n * n; e += nth) {
-    float2 v = sa[e];
-    x[(e % n) + (long long)(e / n) * X.ld] = make_double2((double)v.x, (double)v.y);
-  }
+#pragma unroll
+  for (int ia = 0; ia < RA; ia++)
+#pragma unroll
+    for (int ib = 0; ib < RB; ib++) {
+      const int r = ty + TY * ia, j = tx + 16 * ib;
+      if (r < n && j < n) x[ind[r] + (long long)j * X.ld] = make_double2((double)m[ia][ib].x, (double)m[ia][ib].y);
+    }
 }
 
 // ------------------------------------------------------------------ host side
@@ -501,13 +676,14 @@ int get_encoder() {
   return 0;
 }
 
-int make_map(CUtensorMap *m, void *base, int K, int rows, long long depth, int boxrows) {
-  cuuint64_t dims[3] = {(cuuint64_t)K, (cuuint64_t)rows, (cuuint64_t)depth};
-  cuuint64_t strides[2] = {(cuuint64_t)K * 2, (cuuint64_t)K * 2 * rows};
+// tiled staging: dims {32, rows, regions * kblocks}; one box = one contiguous block
+int make_map(CUtensorMap *m, void *base, int rows, long long depth, int boxrows) {
+  cuuint64_t dims[3] = {(cuuint64_t)KB, (cuuint64_t)rows, (cuuint64_t)depth};
+  cuuint64_t strides[2] = {(cuuint64_t)KB * 2, (cuuint64_t)KB * 2 * rows};
   cuuint32_t box[3] = {(cuuint32_t)KB, (cuuint32_t)boxrows, 1};
   cuuint32_t es[3] = {1, 1, 1};
   CUresult r = g_encode(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, base, dims, strides, box, es,
-                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS ? 0 : -1;
 }
@@ -515,7 +691,7 @@ int make_map(CUtensorMap *m, void *base, int K, int rows, long long depth, int b
 // at least 120 KB so that only one CTA (and one 512-column TMEM allocation)
 // is resident per SM
 size_t oz_smem_bytes(int S) {
-  size_t b = (size_t)S * (MT * KB * 2 + NT * KB * 2) + 1024;
+  size_t b = (size_t)NSTAGE * S * (MT * KB * 2 + NT * KB * 2) + 1024;
   return b < 120 * 1024 ? 120 * 1024 : b;
 }
 
@@ -525,7 +701,7 @@ size_t oz_smem_bytes(int S) {
 struct MixedWork {
   void *sa = nullptr, *sb = nullptr;  // slice staging
   size_t sa_cap = 0, sb_cap = 0;
-  double *sigma = nullptr, *tau = nullptr;
+  int *sigma = nullptr, *tau = nullptr;
   size_t sig_cap = 0, tau_cap = 0;
   zd *acopy = nullptr, *rbuf = nullptr;
   size_t ac_cap = 0, rb_cap = 0;
@@ -593,23 +769,32 @@ static int zgemm_s(MixedWork *w, int mode, const MatRef &A, const MatRef &B, con
   // staging sized for S slices; the zero padding is redone when the layout changes
   if ((rc = grow(&w->sa, &w->sa_cap, (size_t)items * S * Mp * Kp * 2, true))) return rc;
   if ((rc = grow(&w->sb, &w->sb_cap, (size_t)items * S * Np * Kp * 2, true))) return rc;
-  if (w->last_n != n * 16 + S) {
-    // padding must be zero for this layout: clear what earlier layouts wrote
+  if (w->last_n != n) {
+    // padding (row >= n, column >= 2n of every slice region) must be zero;
+    // the region layout depends on n only, so a new n clears what an earlier
+    // layout wrote there
     if (cudaMemsetAsync(w->sa, 0, w->sa_cap, st) != cudaSuccess ||
         cudaMemsetAsync(w->sb, 0, w->sb_cap, st) != cudaSuccess)
       return SKKR_ERR_CUDA;
-    w->last_n = n * 16 + S;
+    w->last_n = n;
   }
-  if ((rc = grow((void **)&w->sigma, &w->sig_cap, (size_t)items * Mp * sizeof(double), false))) return rc;
-  if ((rc = grow((void **)&w->tau, &w->tau_cap, (size_t)items * n * sizeof(double), false))) return rc;
+  if ((rc = grow((void **)&w->sigma, &w->sig_cap, (size_t)items * Mp * sizeof(int), false))) return rc;
+  if ((rc = grow((void **)&w->tau, &w->tau_cap, (size_t)items * n * sizeof(int), false))) return rc;
+  const long long active_s = act ? skkr_active_items(items) : items;
+  // split traffic: FP64 operand read + S bf16 slices of the real embedding written
+  const double split_bytes = (double)active_s * n * n * (16.0 + S * 2.0 * 2.0);
   dim3 ga((n + 31) / 32, items);
+  kstat_begin(KS_OTHER, split_bytes, st);
   k_split_a<S><<<ga, 256, 0, st>>>(A, n, nc, act, (__nv_bfloat16 *)w->sa, Mp, Kp, w->sigma);
+  kstat_end(st);
   SKKR_LAUNCHED();
   dim3 gb((n + 7) / 8, items);
+  kstat_begin(KS_OTHER, 2.0 * split_bytes, st);
   k_split_b<S><<<gb, 256, 0, st>>>(B, n, nc, act, (__nv_bfloat16 *)w->sb, Np, Kp, w->tau);
+  kstat_end(st);
   SKKR_LAUNCHED();
   CUtensorMap ma, mb;
-  if (make_map(&ma, w->sa, Kp, Mp, items * S, MT) || make_map(&mb, w->sb, Kp, Np, items * S, NT))
+  if (make_map(&ma, w->sa, Mp, items * S * kblocks, MT) || make_map(&mb, w->sb, Np, items * S * kblocks, NT))
     return SKKR_ERR_CUDA;
   const size_t smem = oz_smem_bytes(S);
   if (!w->smem_set[S]) {
@@ -634,7 +819,8 @@ static int zgemm_s(MixedWork *w, int mode, const MatRef &A, const MatRef &B, con
   g.err = w->err;
   dim3 grid(mtiles * ntiles, items);
   const long long active = act ? skkr_active_items(items) : items;
-  kstat_begin(KS_GEMM, 8.0 * n * (double)n * n * (double)active, st);
+  // algorithmic BF16 tensor work: S(S+1)/2 real products of n x 2n x 2n per item
+  kstat_begin(KS_OZAKI, (double)(S * (S + 1) / 2) * 8.0 * n * (double)n * n * (double)active, st);
   k_ozaki<S><<<grid, 128, smem, st>>>(ma, mb, g);
   kstat_end(st);
   SKKR_LAUNCHED();
@@ -668,12 +854,10 @@ int mixed_zinv(MixedWork *w, const MatRef &A, const MatRef &X, int n, int nk, in
   MatRef Ac = mref(w->acopy, (long long)nc * MB, MB, n);
   MatRef R = mref(w->rbuf, (long long)nc * MB, MB, n);
   launch_zaxpby(Ac, A, nullptr, 0, nullptr, 0, n, nk, nc, act, st);
-  const size_t smem = (size_t)n * n * sizeof(float2);
-  if (cudaFuncSetAttribute(k_cgj32, cudaFuncAttributeMaxDynamicSharedMemorySize, 128 * 128 * 8) !=
-      cudaSuccess)
-    return SKKR_ERR_CUDA;
   kstat_begin(KS_GJ, 8.0 * n * (double)n * n * (double)(act ? skkr_active_items(items) : items), st);
-  k_cgj32<<<(unsigned)items, 512, smem, st>>>(Ac, X, n, nc, act);
+  if (n <= 32) k_cgj32<16, 2, 2><<<(unsigned)items, 256, 0, st>>>(Ac, X, n, nc, act);
+  else if (n <= 64) k_cgj32<16, 4, 4><<<(unsigned)items, 256, 0, st>>>(Ac, X, n, nc, act);
+  else k_cgj32<32, 4, 8><<<(unsigned)items, 512, 0, st>>>(Ac, X, n, nc, act);
   kstat_end(st);
   SKKR_LAUNCHED();
   for (int it = 0; it < newton; it++) {

@@ -152,7 +152,7 @@ def phystau(tau, tinv, alpha, lmax, irel):
     return uncm(t)
 
 
-KSTAT_CLASSES = ("zgemm", "gjinv", "gk_ft", "other")
+KSTAT_CLASSES = ("zgemm", "gjinv", "gk_ft", "other", "ozaki")
 
 
 def kernel_stats_start():
@@ -160,7 +160,7 @@ def kernel_stats_start():
 
 
 def kernel_stats_stop():
-    out = np.zeros(12)
+    out = np.zeros(3 * len(KSTAT_CLASSES))
     _check(lib().skkr_gpu_kernel_stats(0, _p(out)), "skkr_gpu_kernel_stats")
     return {name: dict(launches=int(out[3 * i]), ms=float(out[3 * i + 1]), work=float(out[3 * i + 2]))
             for i, name in enumerate(KSTAT_CLASSES)}
