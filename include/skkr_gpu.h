@@ -43,7 +43,8 @@ enum skkr_error {
   SKKR_ERR_SGF_DIVERGED = -4, /* decimation error > 1e10 (main/surfgf.f:88-93)        */
   SKKR_ERR_UNSUPPORTED = -5,  /* input outside the implemented scope                  */
   SKKR_ERR_NOMEM = -6,
-  SKKR_ERR_NONFINITE = -7     /* NaN/Inf in a result                                  */
+  SKKR_ERR_NONFINITE = -7,    /* NaN/Inf in a result                                  */
+  SKKR_ERR_PEER = -8          /* another rank of a k-split energy failed, or the reduction hook did */
 };
 
 /* Sizes of one system: the runtime equivalent of param.h plus the
@@ -100,6 +101,21 @@ typedef struct skkr_ctx skkr_ctx;
  * arrays xsave, ysave, g2d of cpacoord_ksave.f:86). */
 int skkr_gpu_create(const skkr_sizes *sizes, skkr_ctx **ctx);
 int skkr_gpu_destroy(skkr_ctx *ctx);
+
+/* Host reduction for an energy whose k points are split over ranks (the
+ * modulo(ik-1,nprocs) split of cpacoord_ksave.f:189 with the mpi_allreduce of
+ * the k-summed tau at :406).  When set, every CPA iteration calls
+ *   fn(user, buf, n)   with n = 2*nintfc*lk*lk + 1 doubles:
+ *   buf[0 .. n-2]  this rank's k-summed screened tau, [nintfc][col][row] re/im,
+ *   buf[n-1]       1.0 if this rank failed (decimation cap / divergence), else 0.0,
+ * and fn must overwrite buf with the element-wise sum over all ranks (an
+ * allreduce SUM) and return 0.  Each rank passes only its own k points and
+ * their global weights; the CPA update then runs replicated on identical
+ * data, so all ranks take the same number of CPA iterations.  A rank that
+ * fails still calls fn (with the flag set) before it returns its own code;
+ * the other ranks then return SKKR_ERR_PEER.  fn = NULL switches it off. */
+typedef int (*skkr_reduce_fn)(void *user, double *buf, long long n);
+int skkr_gpu_set_reduce(skkr_ctx *ctx, skkr_reduce_fn fn, void *user);
 
 /* One energy: the CPA loop around the k loop, k-sum with point-group
  * rotation and the CPA update (cpacoord_ksave.f:139-419).
@@ -163,6 +179,18 @@ int skkr_gpu_kernel_stats(int enable, double *out);
  * (rsp-scf/phystau.f:2-61, nrsp-scf/phystau.f): tau := (1+a t)tau(1+t a) - (a + a t a). */
 int skkr_gpu_phystau(int mode, int lmax, double *tau, const double *tinv,
                      const double *alpha, int ld);
+
+/* Layer DOS of nlay layers from their physical site-diagonal tau (replaces
+ * the lambda = 0 moment of nrsp-scf/moment.f:47-110 with locquant.f:86-126,
+ * and rsp-scf/moment.f:60-140 with locquant.f:197-232):
+ *   zmom[li][i]   = fac (F[li][i] tau_li(i,i) - G[li][i])   per basis index,
+ *   zdos_l[li][l] = sum of zmom over the indices of orbital l,
+ * fac = -1/pi, doubled for para != 0 in the lm basis.  F, G are the
+ * single-site radial integrals int Z^2 r^2 dr, int Z J r^2 dr per basis index
+ * (complex, [nlay][nd]); tau is [nlay][ld][ld].  The DOS is Im(zmom) /
+ * Im(zdos_l); the host accumulates the contour sums of locquant.f itself. */
+int skkr_gpu_layer_dos(int mode, int lmax, int nlay, const double *tau, int ld, const double *F,
+                       const double *G, int para, double *zmom, double *zdos_l);
 
 /* Lower-level batched kernels, exported for tests. */
 /* In-place inverses of `batch` n x n matrices (main/gjinv.f:2-59, column pivoting). */

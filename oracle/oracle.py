@@ -88,6 +88,8 @@ def _setup(L):
     L.orc_kmesh2d_ibz.argtypes = [I, I, C.c_char_p, D, D, D, P, P, P, I]
     L.orc_kmesh2d_ibz.restype = I
     L.orc_alpha_sqwell.argtypes = [ZC, D, D, I, P]
+    L.orc_layer_dos.argtypes = [I, I, I, P, I, P, P, I, P, P]
+    L.orc_set_reduce.argtypes = [P, P]
 
 
 def _ptr(a):
@@ -149,6 +151,19 @@ def phystau(tau, tinv, alpha, lmax, irel):
     return from_cm(t)
 
 
+def layer_dos(tau, F, G, lmax, irel, para=False):
+    """orc_layer_dos: (zmom [nlay, nd], zdos_l [nlay, lmax+1]) from physical tau [nlay, nd, nd]."""
+    tau = np.asarray(tau, np.complex128)
+    nlay, nd = tau.shape[0], tau.shape[-1]
+    t = to_cm(tau)
+    f = np.ascontiguousarray(F, np.complex128).reshape(nlay, nd).copy()
+    g = np.ascontiguousarray(G, np.complex128).reshape(nlay, nd).copy()
+    zm = np.zeros((nlay, nd), np.complex128)
+    zl = np.zeros((nlay, lmax + 1), np.complex128)
+    lib().orc_layer_dos(irel, lmax, nlay, _ptr(t), nd, _ptr(f), _ptr(g), int(bool(para)), _ptr(zm), _ptr(zl))
+    return zm, zl
+
+
 def gk_blocks(rt, k):
     lmmax = rt.gR.shape[1]
     g = to_cm(rt.gR)
@@ -202,10 +217,26 @@ def alpha_sqwell(e, vscreen, rs, lmax):
 
 
 # ----------------------------------------------------------------- cpacoord
-def cpacoord(ep, nthreads=1, tminv=None):
+REDUCE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.POINTER(C.c_double), C.c_longlong)
+
+
+def _reduce_cb(fn):
+    """C callback around fn(buf: ndarray) that sums buf over ranks in place."""
+    def cb(_user, buf, n):
+        try:
+            fn(np.ctypeslib.as_array(buf, shape=(int(n),)))
+            return 0
+        except Exception:  # noqa: BLE001 - reported to the C side as a failed reduction
+            return 1
+    return REDUCE_FN(cb)
+
+
+def cpacoord(ep, nthreads=1, tminv=None, reduce=None):
     """Run the CPA + k loop of one energy problem (a workloads.EnergyProblem).
     Returns dict with tauc, taua, taub (k-summed screened, [layer,row,col]),
-    tminv (converged coherent t^-1) and the loop counters."""
+    tminv (converged coherent t^-1) and the loop counters.  `reduce`
+    (fn(buf) summing buf over ranks in place) makes this one rank of a k-split
+    energy: ep then holds this rank's k points only."""
     keep = []
 
     def arr(a, dt):
@@ -240,9 +271,16 @@ def cpacoord(ep, nthreads=1, tminv=None):
     taua = np.zeros_like(tauc)
     taub = np.zeros_like(tauc)
     res = Result()
-    st = lib().orc_cpacoord(C.cast(C.pointer(pr), C.c_void_p), _ptr(conc), _ptr(tl), _ptr(tr),
-                            _ptr(ti), _ptr(ta), _ptr(tb), _ptr(tauc), _ptr(taua), _ptr(taub), lk,
-                            C.cast(C.pointer(res), C.c_void_p), nthreads)
+    cb = _reduce_cb(reduce) if reduce is not None else None
+    if cb is not None:
+        lib().orc_set_reduce(C.cast(cb, C.c_void_p), None)
+    try:
+        st = lib().orc_cpacoord(C.cast(C.pointer(pr), C.c_void_p), _ptr(conc), _ptr(tl), _ptr(tr),
+                                _ptr(ti), _ptr(ta), _ptr(tb), _ptr(tauc), _ptr(taua), _ptr(taub), lk,
+                                C.cast(C.pointer(res), C.c_void_p), nthreads)
+    finally:
+        if cb is not None:
+            lib().orc_set_reduce(None, None)
     return dict(status=st, tauc=from_cm(tauc), taua=from_cm(taua), taub=from_cm(taub),
                 tminv=from_cm(ti), cpa_iterations=res.cpa_iterations, cpa_error=res.cpa_error,
                 sgf_status=res.sgf_status, max_dec_iters=res.max_dec_iters,

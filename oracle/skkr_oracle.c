@@ -689,6 +689,13 @@ void orc_gk_from_rtable(int nblk, const int *rstart, const double *rvec,
   }
 }
 
+static orc_reduce_fn g_red_fn = NULL;
+static void *g_red_user = NULL;
+void orc_set_reduce(orc_reduce_fn fn, void *user) {
+  g_red_fn = fn;
+  g_red_user = user;
+}
+
 /* ===================================================================== *
  * rsp-scf/cpacoord_ksave.f:139-419  CPA loop around the k loop           *
  * ===================================================================== */
@@ -786,6 +793,19 @@ int orc_cpacoord(const orc_problem *p, const double *conc, const zc *tminvl,
       for (size_t q = 0; q < sz * nintfc; q++) tauc[q] += taupart[sz * nintfc * t + q];
     for (int t = 0; t < nthreads; t++)
       if (stat_thr[t] && !status) status = stat_thr[t];
+    if (g_red_fn) {
+      /* the allreduce across ranks of a k-split energy; a failed rank sends its flag */
+      const long long nz = (long long)(sz * nintfc);
+      double *buf = calloc((size_t)(2 * nz + 1), sizeof(double));
+      if (!status) memcpy(buf, tauc, (size_t)nz * sizeof(zc));
+      buf[2 * nz] = status ? 1.0 : 0.0;
+      int rrc = g_red_fn(g_red_user, buf, 2 * nz + 1);
+      if (!status) {
+        if (rrc != 0 || buf[2 * nz] != 0.0) status = 3;
+        else memcpy(tauc, buf, (size_t)nz * sizeof(zc));
+      }
+      free(buf);
+    }
     if (status) break;
     orc_cpacor(conc, tminv, tminva, tminvb, tauc, taua, taub, lkmax, ld, nintfc, &itcpa,
                p->itcpam, p->cpatol, &cpacon, &concpa, &cpaerr);
@@ -1061,4 +1081,49 @@ void orc_alpha_sqwell(zc ce, double vscreen, double rs, int lmax, zc *alpha) {
     zc react = -tand / ck;
     alpha[l] = react / (1.0 + I * ck * react);
   }
+}
+
+/* ---------------------------------------------------------------------------
+ * Layer DOS from the physical site-diagonal tau (lambda = 0 moment).
+ * nrsp-scf/moment.f:47-110: gf = fac*(Rreg o coeff) tau - fac*(Rirr o coeff),
+ * coeff = sqrt(4 pi) Gaunt(l,0,l') = identity (main/gafill.f:14-35), so
+ * gf_ii = fac (F_i tau_ii - G_i); the real-harmonic transform of moment.f:96-98
+ * keeps the sum over m.  locquant.f:115-122 sums zqmom over m into zdos(l).
+ * rsp-scf/moment.f keeps the (kappa,mu) diagonal (rgacoeff = identity).
+ */
+void orc_layer_dos(int mode, int lmax, int nlay, const zc *tau, int ld, const zc *F,
+                   const zc *G, int para, zc *zmom, zc *zdos_l) {
+  const int lmmax = (lmax + 1) * (lmax + 1);
+  const int nd = mode ? 2 * lmmax : lmmax;
+  double fac = -1.0 / (4.0 * atan(1.0));
+  if (para && !mode) fac *= 2.0;
+  int *lof = malloc(sizeof(int) * nd);
+  if (mode) {
+    /* (kappa,mu) order of main/clebsch.f: kappa = -1, 1, -2, 2, -3, ... with
+       2|kappa| components each; l = kappa for kappa > 0, -kappa-1 otherwise */
+    int k = 0;
+    for (int a = 1; k < nd; a++) {
+      for (int s = 0; s < 2 && k < nd; s++) {
+        int kap = s == 0 ? -a : a;
+        if (kap == 0) continue;
+        int l = kap > 0 ? kap : -kap - 1;
+        int cnt = 2 * (kap > 0 ? kap : -kap);
+        for (int c = 0; c < cnt && k < nd; c++) lof[k++] = l;
+      }
+    }
+  } else {
+    for (int l = 0, k = 0; l <= lmax; l++)
+      for (int m = -l; m <= l; m++) lof[k++] = l;
+  }
+  for (int li = 0; li < nlay; li++) {
+    const zc *t = tau + (size_t)li * ld * ld;
+    for (int l = 0; l <= lmax; l++) zdos_l[(size_t)li * (lmax + 1) + l] = 0;
+    for (int i = 0; i < nd; i++) {
+      size_t q = (size_t)li * nd + i;
+      zc z = fac * (F[q] * t[IX(i, i, ld)] - G[q]);
+      zmom[q] = z;
+      zdos_l[(size_t)li * (lmax + 1) + lof[i]] += z;
+    }
+  }
+  free(lof);
 }

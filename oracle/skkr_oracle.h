@@ -87,6 +87,14 @@ void orc_cpacor(const double *conc, zc *mc, const zc *ma, const zc *mb,
 void orc_phystau(zc *tau, const zc *tinv1, const zc *tinv2, const zc *alpha,
                  int lmax, int irel, int ld, int idiag);
 
+/* ---- layer DOS: nrsp-scf/moment.f:47-110 + locquant.f:86-126 (lm),
+ *      rsp-scf/moment.f:60-140 + locquant.f:197-232 (kappa,mu) ----------
+ * zmom[li][i] = fac (F[li][i] tau_ii - G[li][i]), fac = -1/pi (x2 if para and
+ * mode 0); zdos_l[li][l] = sum of zmom over the basis indices of orbital l.
+ * The DOS is the imaginary part.  tau: physical tau [nlay][ld][ld]. */
+void orc_layer_dos(int mode, int lmax, int nlay, const zc *tau, int ld, const zc *F,
+                   const zc *G, int para, zc *zmom, zc *zdos_l);
+
 /* ---- sorttmat: rsp-scf/sorttmat.f ------------------------------------- */
 void orc_sorttmat(int lkmax, int ld, int nintfc, int nl, int nr, int ngeff,
                   const zc *rg /*R_g [ngeff][ld][ld]*/,
@@ -138,6 +146,15 @@ typedef struct {
 /* tminv: inout [nintfc][ld][ld] coherent screened t^-1; tminva/b [nintfc];
  * tminvl [ninprc0], tminvr [ninprc(nprc+1)]; taua/taub out (screened, k-summed,
  * after the CPA; phystau NOT applied); tauc out (last k-summed coherent tau). */
+/* Host reduction for a k-split energy (cpacoord_ksave.f:189 k split with the
+ * mpi_allreduce of :406): when set, orc_cpacoord calls fn(user, buf, n) once
+ * per CPA iteration with buf = [tauc (2*nintfc*ld*ld doubles), failed flag],
+ * and fn must replace buf by its sum over the ranks.  A rank whose
+ * decimation failed sends the flag and returns its own status; the others
+ * return status 3.  fn = NULL switches it off (process wide). */
+typedef int (*orc_reduce_fn)(void *user, double *buf, long long n);
+void orc_set_reduce(orc_reduce_fn fn, void *user);
+
 int orc_cpacoord(const orc_problem *p, const double *conc, const zc *tminvl,
                  const zc *tminvr, zc *tminv, const zc *tminva,
                  const zc *tminvb, zc *tauc, zc *taua, zc *taub, int ld,

@@ -48,6 +48,14 @@ class Context:
         return cls(ep.irel, ep.lmax, ep.nprc, ep.ninprc, len(ep.lg), ep.itermaxl, ep.itermaxr, ep.errmax,
                    ep.itcpam, ep.cpatol, precision, nk_chunk, slices)
 
+    def set_reduce(self, fn):
+        """Make this context one rank of a k-split energy: fn(buf) must sum
+        the float64 host buffer over the ranks in place (an allreduce) and is
+        called once per CPA iteration (skkr_gpu_set_reduce).  None clears it."""
+        self._reduce_cb = N.reduce_callback(fn) if fn is not None else None
+        N._check(N.lib().skkr_gpu_set_reduce(self.h, C.cast(self._reduce_cb, C.c_void_p) if fn else None, None),
+                 "skkr_gpu_set_reduce")
+
     def close(self):
         if self.h:
             N.lib().skkr_gpu_destroy(self.h)
@@ -148,6 +156,53 @@ class Context:
         return res
 
 
+def ksplit_indices(nk, rank, world):
+    """k points of `rank` in the round-robin split of cpacoord_ksave.f:189
+    (modulo(ik-1, nprocs) == myrank)."""
+    return np.arange(rank, nk, world)
+
+
+def ksplit_problem(ep, rank, world):
+    """The EnergyProblem of one rank of a k-split energy: its own k points
+    with their global weights (the k-sum is completed by the allreduce)."""
+    idx = ksplit_indices(ep.nk, rank, world)
+    if len(idx) == 0:
+        raise ValueError("rank %d of %d has no k points (nk=%d)" % (rank, world, ep.nk))
+    return ep.with_k(ep.xk[idx], ep.wk[idx])
+
+
+def torch_allreduce(group=None):
+    """fn(buf) that sums a float64 host buffer over the ranks of a
+    torch.distributed group in place: gloo on the host tensor, NCCL through a
+    device copy."""
+    import torch
+    import torch.distributed as dist
+
+    def fn(buf):
+        t = torch.from_numpy(buf)
+        if dist.get_backend(group) == "nccl":
+            d = t.to("cuda")
+            dist.all_reduce(d, group=group)
+            t.copy_(d.cpu())
+        else:
+            dist.all_reduce(t, group=group)
+    return fn
+
+
+def cpacoord_ksplit(ep, rank, world, allreduce, precision="fp64", slices=0, check=True):
+    """One rank of an energy whose k points are split over `world` ranks:
+    the library runs this rank's k points and calls `allreduce` on the
+    k-summed tau before every CPA update, so every rank returns the full
+    result."""
+    epl = ksplit_problem(ep, rank, world)
+    ctx = Context.for_problem(epl, precision, slices=slices)
+    try:
+        ctx.set_reduce(allreduce)
+        return ctx.cpacoord(epl, check=check)
+    finally:
+        ctx.close()
+
+
 def cpacoord(ep, precision="fp64", tminv=None, check=True, slices=0):
     """One energy through the GPU path (creates a context for the call)."""
     ctx = Context.for_problem(ep, precision, slices=slices)
@@ -155,3 +210,18 @@ def cpacoord(ep, precision="fp64", tminv=None, check=True, slices=0):
         return ctx.cpacoord(ep, tminv=tminv, check=check)
     finally:
         ctx.close()
+
+
+def layer_dos(ep, tau, which="a", para=False):
+    """Layer DOS of the interface layers of one energy, as locquant.f does
+    after cpacoord: screened -> physical tau (phystau) per layer, then
+    zmom_i = -1/pi (F_i tau_ii - G_i) and its sums per orbital l, both on the
+    device.  `tau` is the k-summed screened tau of species `which` (taua or
+    taub of cpacoord); F, G are the square-well radial integrals of that
+    species.  Returns (zmom [nintfc, lk], zdos_l [nintfc, lmax+1]); the DOS is
+    the imaginary part."""
+    from . import synth as S
+    tinv = ep.tminva if which == "a" else ep.tminvb
+    phys = np.array([N.phystau(tau[li], tinv[li], ep.alpha[li], ep.lmax, ep.irel) for li in range(ep.nintfc)])
+    F, G = S.layer_dos_inputs(ep, which)
+    return N.layer_dos(phys, F, G, ep.lmax, ep.irel, para)

@@ -192,6 +192,9 @@ struct skkr_ctx {
   std::vector<struct SlotStore *> slots;
   MixedWork *mw = nullptr;   // split-precision engine (precision == SKKR_MIXED)
   int slices = 6, slices_res = 7;  // BF16 slices of products / of Newton residuals
+  skkr_reduce_fn red_fn = nullptr;  // host allreduce of tauc for a k-split energy
+  void *red_user = nullptr;
+  std::vector<double> red_buf;
   double max_resid = 0.0;    // largest Newton residual seen in this run
 };
 
@@ -909,6 +912,36 @@ static int cpa_step(skkr_ctx *c, int *itcpa, int *cpacon, int *concpa, double *e
 }
 
 // ---------------------------------------------------------------------------
+// Sum of the k-summed tau over the ranks of a k-split energy through the
+// host hook (cpacoord_ksave.f:406).  `failed` ranks send the flag only.
+static int reduce_tauc(skkr_ctx *c, bool failed) {
+  const size_t nz = (size_t)c->nintfc * c->lk * c->lk;
+  c->red_buf.assign(2 * nz + 1, 0.0);
+  if (!failed) {
+    CK(cudaMemcpyAsync(c->red_buf.data(), c->tauc.p, nz * sizeof(zd), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+  }
+  c->red_buf[2 * nz] = failed ? 1.0 : 0.0;
+  if (c->red_fn(c->red_user, c->red_buf.data(), (long long)(2 * nz + 1)) != 0) {
+    g_last_error = "reduction hook returned an error";
+    return SKKR_ERR_PEER;
+  }
+  if (failed) return SKKR_OK;
+  if (c->red_buf[2 * nz] != 0.0) {
+    g_last_error = "another rank of the k-split energy failed";
+    return SKKR_ERR_PEER;
+  }
+  CK(cudaMemcpyAsync(c->tauc.p, c->red_buf.data(), nz * sizeof(zd), cudaMemcpyHostToDevice, c->st));
+  return SKKR_OK;
+}
+
+extern "C" int skkr_gpu_set_reduce(skkr_ctx *c, skkr_reduce_fn fn, void *user) {
+  if (!c) return SKKR_ERR_ARG;
+  c->red_fn = fn;
+  c->red_user = user;
+  return SKKR_OK;
+}
+
 extern "C" int skkr_gpu_run(skkr_ctx *c, skkr_status *status) {
   if (!c || !c->staged) return SKKR_ERR_ARG;
   const long long l0 = g_skkr_launches;
@@ -981,7 +1014,10 @@ extern "C" int skkr_gpu_run(skkr_ctx *c, skkr_status *status) {
       CKR(run_tau2d(c, k0, nkc, icls));
       launch_ksum(c->tauk.as<zd>(), nkc, (long long)ncls * ni * lk2, c->S.as<zd>(), k0 > 0, st);
     }
-    if (c->err_code) break;
+    if (c->err_code) {
+      if (c->red_fn) reduce_tauc(c, true);  // tell the other ranks before returning
+      break;
+    }
     // rotation of the class sums: tauc = sum_g L_g S[class(g)] R_g   (cpacoord_ksave.f:382-391)
     CKR(c->T1.ensure((size_t)ni * c->ngeff * lk2 * sizeof(zd)));
     CKR(c->T2.ensure((size_t)ni * c->ngeff * lk2 * sizeof(zd)));
@@ -1000,6 +1036,13 @@ extern "C" int skkr_gpu_run(skkr_ctx *c, skkr_status *status) {
       launch_zgemm(0, Lm, Sm, T1m, T1m, T1m, lk, lk, lk, ni, c->ngeff, nullptr, st);
       launch_zgemm(0, T1m, Rm, T2m, T2m, T2m, lk, lk, lk, ni, c->ngeff, nullptr, st);
       launch_gsum(c->T2.as<zd>(), c->ngeff, lk, ni, c->tauc.as<zd>(), st);
+    }
+    if (c->red_fn) {
+      int rrc = reduce_tauc(c, false);
+      if (rrc != SKKR_OK) {
+        c->err_code = rrc;
+        break;
+      }
     }
     trace_point("before cpa_step");
     int rc = cpa_step(c, &itcpa, &cpacon, &concpa, &cpaerr);
@@ -1345,6 +1388,33 @@ extern "C" int skkr_gpu_phystau(int mode, int lmax, double *tau, const double *t
   CK(cudaDeviceSynchronize());
   CK(cudaGetLastError());
   return download_mats(tau, T, 1, nd, ld);
+}
+
+extern "C" int skkr_gpu_layer_dos(int mode, int lmax, int nlay, const double *tau, int ld,
+                                  const double *F, const double *G, int para, double *zmom,
+                                  double *zdos_l) {
+  if (!tau || !F || !G || !zmom || !zdos_l || lmax < 0 || lmax > 3 || nlay < 1) return SKKR_ERR_ARG;
+  const int lmmax = (lmax + 1) * (lmax + 1), rel = mode == SKKR_REL,
+            nd = rel ? 2 * lmmax : lmmax, nl = lmax + 1;
+  if (ld < nd) return SKKR_ERR_ARG;
+  double fac = -1.0 / 3.14159265358979323846;
+  if (para && !rel) fac *= 2.0;  // spin degeneracy of the non-relativistic DOS
+  Scoped s;
+  zd *T, *Fd, *Gd, *Zm, *Zl;
+  CKR(s.alloc(&T, (long long)nlay * nd * nd));
+  CKR(s.alloc(&Fd, (long long)nlay * nd));
+  CKR(s.alloc(&Gd, (long long)nlay * nd));
+  CKR(s.alloc(&Zm, (long long)nlay * nd));
+  CKR(s.alloc(&Zl, (long long)nlay * nl));
+  CKR(upload_mats(T, tau, nlay, nd, ld));
+  CK(cudaMemcpy(Fd, F, (size_t)nlay * nd * sizeof(zd), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(Gd, G, (size_t)nlay * nd * sizeof(zd), cudaMemcpyHostToDevice));
+  launch_layer_dos(rel, nd, nl, nlay, T, nd, Fd, Gd, fac, Zm, Zl, 0);
+  CK(cudaDeviceSynchronize());
+  CK(cudaGetLastError());
+  CK(cudaMemcpy(zmom, Zm, (size_t)nlay * nd * sizeof(zd), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(zdos_l, Zl, (size_t)nlay * nl * sizeof(zd), cudaMemcpyDeviceToHost));
+  return SKKR_OK;
 }
 
 // ---------------------------------------------------------------------------

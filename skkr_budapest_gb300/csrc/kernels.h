@@ -49,6 +49,8 @@ void launch_ksum(const zd *tk, int nk, long long E, zd *S, int accumulate, cudaS
 // sum over g of T[layer][g] -> out[layer]
 void launch_gsum(const zd *T, int ng, int lk, int nl, zd *out, cudaStream_t st);
 // CPA helpers
+void launch_layer_dos(int rel, int nd, int nl, int nlay, const zd *tau, int ld, const zd *F,
+                      const zd *G, double fac, zd *zmom, zd *zdos_l, cudaStream_t st);
 void launch_cpa_mix(const zd *X, const double *conc, const int *act, int lk, int nl, zd *xc,
                     cudaStream_t st);
 

@@ -558,3 +558,36 @@ void launch_cpa_mix(const zd *X, const double *conc, const int *act, int lk, int
   k_cpa_mix<<<grid, 256, 0, st>>>(X, conc, act, lk, xc);
   SKKR_LAUNCHED();
 }
+
+// ---------------------------------------------------------------------------
+// Layer DOS (lambda = 0 moment of nrsp-scf/moment.f:47-110, rsp-scf/moment.f:
+// 60-140): zmom_i = fac (F_i tau_ii - G_i) per basis index, and per orbital l
+// the sum over its indices in increasing order (locquant.f:115-122).  One CTA
+// per layer; basis index i has l = floor(sqrt(i)) in the lm basis and
+// floor(sqrt(i/2)) in the (kappa,mu) basis (l blocks start at 2 l^2).
+__global__ void k_layer_dos(int rel, int nd, int nl, const zd *__restrict__ tau, int ld,
+                            const zd *__restrict__ F, const zd *__restrict__ G, double fac,
+                            zd *__restrict__ zmom, zd *__restrict__ zdos_l) {
+  const int li = blockIdx.x;
+  __shared__ zd z[128];
+  const zd *t = tau + (long long)li * ld * ld;
+  for (int i = threadIdx.x; i < nd; i += blockDim.x) {
+    const long long q = (long long)li * nd + i;
+    const zd v = zscale(fac, zsub(zmul(F[q], t[i + (long long)i * ld]), G[q]));
+    z[i] = v;
+    zmom[q] = v;
+  }
+  __syncthreads();
+  for (int l = threadIdx.x; l < nl; l += blockDim.x) {
+    const int i0 = rel ? 2 * l * l : l * l, i1 = rel ? 2 * (l + 1) * (l + 1) : (l + 1) * (l + 1);
+    zd acc = make_double2(0.0, 0.0);
+    for (int i = i0; i < i1 && i < nd; i++) acc = zadd(acc, z[i]);
+    zdos_l[(long long)li * nl + l] = acc;
+  }
+}
+
+void launch_layer_dos(int rel, int nd, int nl, int nlay, const zd *tau, int ld, const zd *F,
+                      const zd *G, double fac, zd *zmom, zd *zdos_l, cudaStream_t st) {
+  k_layer_dos<<<nlay, 128, 0, st>>>(rel, nd, nl, tau, ld, F, G, fac, zmom, zdos_l);
+  SKKR_LAUNCHED();
+}

@@ -18,7 +18,7 @@ NONREL, REL = 0, 1
 FP64, MIXED = 0, 1
 ERRORS = {0: "ok", -1: "bad argument", -2: "CUDA error", -3: "decimation hit itermax",
           -4: "decimation diverged (error > 1e10)", -5: "unsupported input", -6: "out of device memory",
-          -7: "non-finite result"}
+          -7: "non-finite result", -8: "another rank failed (or the reduction hook did)"}
 
 I, D, P = C.c_int, C.c_double, C.c_void_p
 
@@ -66,6 +66,8 @@ def lib():
         L.skkr_gpu_fetch.argtypes = [P, P, P, P, P, I]
         L.skkr_gpu_cpacoord.argtypes = [P, D, D, D, D, P, I, P, P, P, P, P, P, P, P, P, P, P, P, P, I, P]
         L.skkr_gpu_phystau.argtypes = [I, I, P, P, P, I]
+        L.skkr_gpu_layer_dos.argtypes = [I, I, I, P, I, P, P, I, P, P]
+        L.skkr_gpu_set_reduce.argtypes = [P, P, P]
         L.skkr_gpu_gjinv_batch.argtypes = [I, I, P, I]
         L.skkr_gpu_surfgf_batch.argtypes = [I, I, P, P, P, P, I, I, D, P, P]
         L.skkr_gpu_gk.argtypes = [P, I, I, P, P]
@@ -150,6 +152,36 @@ def phystau(tau, tinv, alpha, lmax, irel):
     al = np.ascontiguousarray(alpha, np.complex128)
     _check(lib().skkr_gpu_phystau(irel, lmax, _p(t), _p(ti), _p(al), t.shape[-1]), "skkr_gpu_phystau")
     return uncm(t)
+
+
+REDUCE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.POINTER(C.c_double), C.c_longlong)
+
+
+def reduce_callback(fn):
+    """skkr_reduce_fn around fn(buf: ndarray) that sums buf over the ranks in
+    place; an exception is reported to the library as a failed reduction."""
+    def cb(_user, buf, n):
+        try:
+            fn(np.ctypeslib.as_array(buf, shape=(int(n),)))
+            return 0
+        except Exception:  # noqa: BLE001
+            return 1
+    return REDUCE_FN(cb)
+
+
+def layer_dos(tau, F, G, lmax, irel, para=False):
+    """Layer DOS on the device from physical tau [nlay, nd, nd] and the radial
+    integrals F, G [nlay, nd]: returns (zmom [nlay, nd], zdos_l [nlay, lmax+1]);
+    the DOS is their imaginary part."""
+    t = cm(np.asarray(tau, np.complex128).reshape((-1,) + np.shape(tau)[-2:]))
+    nlay, nd = t.shape[0], t.shape[-1]
+    f = np.ascontiguousarray(F, np.complex128).reshape(nlay, nd)
+    g = np.ascontiguousarray(G, np.complex128).reshape(nlay, nd)
+    zm = np.zeros((nlay, nd), np.complex128)
+    zl = np.zeros((nlay, lmax + 1), np.complex128)
+    _check(lib().skkr_gpu_layer_dos(irel, lmax, nlay, _p(t), nd, _p(f), _p(g), int(bool(para)), _p(zm), _p(zl)),
+           "skkr_gpu_layer_dos")
+    return zm, zl
 
 
 KSTAT_CLASSES = ("zgemm", "gjinv", "gk_ft", "other", "ozaki")

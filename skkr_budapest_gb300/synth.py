@@ -298,6 +298,82 @@ def screened_tinv_rel(e, psq, depth, radius, so_split, alpha, lmax) -> np.ndarra
 
 
 # --------------------------------------------------------------------------
+# single-site radial integrals of the square well (layer DOS inputs)
+# --------------------------------------------------------------------------
+def _bessel_l_pm(l: int, x):
+    """f_{l-1}, f_l, f_{l+1} for f = j and f = n, with j_{-1} = cos x/x, n_{-1} = sin x/x."""
+    j, n, _ = sph_bessel(l + 1, x)
+    jm = np.cos(x) / x if l == 0 else j[l - 1]
+    nm = np.sin(x) / x if l == 0 else n[l - 1]
+    return jm, j[l], j[l + 1], nm, n[l], n[l + 1]
+
+
+def sqwell_fg(p2: complex, vwell: float, radius: float, l: int):
+    """Radial integrals F_l = int_0^R Z_l^2 r^2 dr and G_l = int_0^R Z_l J_l r^2 dr
+    of a square well V = vwell (r < R) at squared momentum p2, the inputs of the
+    layer DOS of nrsp-scf/moment.f:47-110 (lambda = 0) over the well's sphere.
+
+    Normalisation follows the Green function G = Z tau Z - Z J that belongs to
+    t = -(1/k) sin(delta) e^{i delta}: outside the well Z_l = j_l(kr) t_l^-1 -
+    i k h_l(kr) and J_l = j_l(kr); inside Z_l = A j_l(qr) and J_l = B j_l(qr) +
+    C n_l(qr) continue them with matching value and slope at R.  The integrals
+    are the closed Lommel forms int t^2 f_l g_l dt = t^3/4 (2 f_l g_l - f_{l-1}
+    g_{l+1} - f_{l+1} g_{l-1}); the j_l n_l form tends to (2l+1)/4 at t = 0.
+    Products are complex (no conjugation), as in the reference."""
+    ck = kappa_of(p2)
+    q = kappa_of(complex(p2) - vwell)
+    tand = _tan_delta(ck, q, radius, l)[l]
+    react = -tand / ck
+    t = react / (1.0 + 1j * ck * react)
+    xk = ck * radius
+    jkm, jk0, _, nkm, nk0, _ = _bessel_l_pm(l, xk)
+    x = q * radius
+    jm, j0, jp, nm, n0, np_ = _bessel_l_pm(l, x)
+    a = (jk0 / t - 1j * ck * (jk0 + 1j * nk0)) / j0
+    jr = jk0                                        # J(R)
+    djr = ck * (jkm - (l + 1) / xk * jk0)           # J'(R)
+    f, df = j0, q * (jm - (l + 1) / x * j0)
+    g, dg = n0, q * (nm - (l + 1) / x * n0)
+    det = f * dg - df * g                           # = 1 / (q R^2)
+    b = (jr * dg - djr * g) / det
+    c = (f * djr - df * jr) / det
+    ijj = x ** 3 / 2.0 * (j0 * j0 - jm * jp) / q ** 3
+    ijn = (x ** 3 / 4.0 * (2.0 * j0 * n0 - jm * np_ - jp * nm) - (2 * l + 1) / 4.0) / q ** 3
+    return complex(a * a * ijj), complex(a * (b * ijj + c * ijn))
+
+
+def layer_dos_inputs(ep, which: str = "a"):
+    """Per-basis-index F, G (nintfc, lk) of the interface layers of an
+    EnergyProblem for species `which` ('a' or 'b'): lm-resolved F_l, G_l
+    (non-relativistic) or (kappa,mu)-resolved F_kappa, G_kappa of the j-split
+    well (relativistic, momentum psq, large component only)."""
+    depths = ep.meta["depth_" + which]
+    radius, so = ep.meta["radius"], ep.meta["so_split"]
+    lk = ep.lkmax
+    F = np.zeros((ep.nintfc, lk), complex)
+    G = np.zeros_like(F)
+    if ep.irel:
+        lv, kv = kmy_l_kappa(ep.lmax)
+    else:
+        lv = lm_l(lk)
+        kv = None
+    for li in range(ep.nintfc):
+        cache = {}
+        for i in range(lk):
+            l = int(lv[i])
+            if kv is None:
+                key, v = l, depths[li]
+            else:
+                kap = int(kv[i])
+                ls = 0.5 * l if kap < 0 else -0.5 * (l + 1)
+                key, v = kap, depths[li] + so * ls
+            if key not in cache:
+                cache[key] = sqwell_fg(ep.psq, v, radius, l)
+            F[li, i], G[li, i] = cache[key]
+    return F, G
+
+
+# --------------------------------------------------------------------------
 # lattice, cluster and real-space screened structure constants
 # --------------------------------------------------------------------------
 @dataclass

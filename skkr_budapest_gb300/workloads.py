@@ -196,7 +196,8 @@ def energy_problem(spec: SystemSpec, ie: int, nset: int | None = None, kmesh: st
     return EnergyProblem(spec.name, ie, ce, psq, fac, irel, lmax, lk, spec.nprc, ninprc, 1, nintfc,
                          blkmap, rt, xk, wk, lg, rg, tminvl, tminvr, tm, ta, tbb, conc,
                          np.array([alpha] * nintfc), cpatol=spec.cpatol,
-                         meta=dict(nset=ns, depth_bulk=d_bulk))
+                         meta=dict(nset=ns, depth_bulk=d_bulk, depth_a=d_a, depth_b=d_b,
+                                   radius=spec.radius, so_split=spec.so_split))
 
 
 def ata(conc: float, ma: np.ndarray, mb: np.ndarray) -> np.ndarray:

@@ -115,3 +115,38 @@ def test_decimation_divergence_is_reported_not_trapped():
     with pytest.raises(native.SkkrError) as ei:
         api.cpacoord(ep)
     assert ei.value.code == -4
+
+
+@pytest.mark.parametrize("irel,lmax,para", [(0, 2, True), (1, 3, False)])
+def test_layer_dos_kernel_matches_oracle(irel, lmax, para):
+    nd = (2 if irel else 1) * (lmax + 1) ** 2
+    tau = rng.normal(size=(5, nd, nd)) + 1j * rng.normal(size=(5, nd, nd))
+    F = rng.normal(size=(5, nd)) + 1j * rng.normal(size=(5, nd))
+    G = rng.normal(size=(5, nd)) + 1j * rng.normal(size=(5, nd))
+    zm, zl = native.layer_dos(tau, F, G, lmax, irel, para)
+    om, ol = O.layer_dos(tau, F, G, lmax, irel, para)
+    assert rel(zm, om) < 1e-14 and rel(zl, ol) < 1e-14
+
+
+def _rel_cpa_l2():
+    spec = W.rel_bcc_cpa(nsets=[2] * 24)
+    spec.lmax = 2
+    return spec
+
+
+@pytest.mark.parametrize("system,ie", [("plain", 6), ("relcpa", 14)])
+def test_layer_dos_after_cpacoord(system, ie):
+    """tau of cpacoord -> phystau -> layer DOS, GPU against the oracle chain."""
+    from skkr_budapest_gb300 import synth as S
+    spec = W.plain_fcc(nset=4) if system == "plain" else _rel_cpa_l2()
+    ep = W.energy_problem(spec, ie)
+    g = api.cpacoord(ep)
+    o = O.cpacoord(ep, nthreads=8)
+    for which in ("a", "b"):
+        key = "tau" + which
+        zm, zl = api.layer_dos(ep, g[key], which, para=not ep.irel)
+        tinv = ep.tminva if which == "a" else ep.tminvb
+        phys = np.array([O.phystau(o[key][li], tinv[li], ep.alpha[li], ep.lmax, ep.irel) for li in range(ep.nintfc)])
+        F, G = S.layer_dos_inputs(ep, which)
+        om, ol = O.layer_dos(phys, F, G, ep.lmax, ep.irel, not ep.irel)
+        assert rel(zm, om) < TOL and rel(zl, ol) < TOL, (rel(zm, om), rel(zl, ol))
