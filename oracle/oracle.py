@@ -51,7 +51,8 @@ def _zc(z):
 
 
 class G2DMap(C.Structure):
-    _fields_ = [("lmax", I), ("lmmax", I), ("nslot", I), ("mi", I), ("jmax", I), ("blkmap", P)]
+    _fields_ = [("lmax", I), ("lmmax", I), ("nslot", I), ("mi", I), ("jmax", I), ("blkmap", P),
+                ("bdg", I), ("nblk", I), ("fach", ZC)]
 
 
 class Problem(C.Structure):
@@ -246,8 +247,9 @@ def cpacoord(ep, nthreads=1, tminv=None, reduce=None):
 
     lk = ep.lkmax
     blk = arr(ep.blkmap, np.int32)
+    bdg = ep.irel == 2
     gmap = G2DMap(ep.lmax, (ep.lmax + 1) ** 2, blk.shape[0], blk.shape[1], (blk.shape[2] - 1) // 2,
-                  _ptr(blk))
+                  _ptr(blk), int(bdg), ep.rt.nblk, _zc(ep.fach if bdg else 0.0))
     nin = arr(ep.ninprc, np.int32)
     xk = arr(ep.xk, np.float64)
     wk = arr(ep.wk, np.float64)
@@ -255,7 +257,7 @@ def cpacoord(ep, nthreads=1, tminv=None, reduce=None):
     rg = arr(to_cm(ep.rg), np.complex128)
     rs = arr(ep.rt.rstart, np.int32)
     rv = arr(ep.rt.rvec, np.float64)
-    gR = arr(to_cm(ep.rt.gR), np.complex128)
+    gR = arr(to_cm(np.concatenate([ep.rt.gR, ep.rt_h.gR]) if bdg else ep.rt.gR), np.complex128)
     pr = Problem(ep.irel, ep.lmax, lk, ep.nprc, _ptr(nin), int(ep.bulkgeo), ep.nintfc,
                  C.cast(C.pointer(gmap), C.c_void_p), len(xk), _ptr(xk), _ptr(wk), len(lg), _ptr(lg),
                  _ptr(rg), ep.itermaxl, ep.itermaxr, ep.errmax, ep.itcpam, ep.cpatol, _zc(ep.fac),

@@ -215,14 +215,27 @@ static const zc *g2d_block(const orc_g2dmap *map, const zc *blocks, int slot, in
 }
 
 static void put_block(zc *m, int mdim, int kki, int kkj, int lkmax, const zc *g,
-                      int lmmax, int irel, zc fac, int lmax) {
+                      const orc_g2dmap *map, int irel, zc fac) {
   zc rg[72 * 72];
+  const int lmmax = map->lmmax, lmax = map->lmax;
   if (g == NULL) {
     for (int k1 = 0; k1 < lkmax; k1++)
       for (int k2 = 0; k2 < lkmax; k2++) m[IX(k1 + kki, k2 + kkj, mdim)] = 0.0;
     return;
   }
-  if (irel == 1) {
+  if (irel == 2) {
+    /* g2d_pack.f: blockdiag(G_e, G_h), then relmtrx.f with fac (e) / fach (h) */
+    const int km = lkmax / 2;
+    const zc *gh = g + (size_t)map->nblk * lmmax * lmmax;
+    for (int k1 = 0; k1 < lkmax; k1++)
+      for (int k2 = 0; k2 < lkmax; k2++) m[IX(k1 + kki, k2 + kkj, mdim)] = 0.0;
+    orc_relmtrx(g, lmmax, rg, 72, fac, lmax);
+    for (int k1 = 0; k1 < km; k1++)
+      for (int k2 = 0; k2 < km; k2++) m[IX(k1 + kki, k2 + kkj, mdim)] = -rg[IX(k1, k2, 72)];
+    orc_relmtrx(gh, lmmax, rg, 72, map->fach, lmax);
+    for (int k1 = 0; k1 < km; k1++)
+      for (int k2 = 0; k2 < km; k2++) m[IX(k1 + km + kki, k2 + km + kkj, mdim)] = -rg[IX(k1, k2, 72)];
+  } else if (irel == 1) {
     orc_relmtrx(g, lmmax, rg, 72, fac, lmax);
     for (int k1 = 0; k1 < lkmax; k1++)
       for (int k2 = 0; k2 < lkmax; k2++) m[IX(k1 + kki, k2 + kkj, mdim)] = -rg[IX(k1, k2, 72)];
@@ -247,17 +260,17 @@ void orc_packer(int ni, int nim, int nip, const orc_g2dmap *map, int slot,
     for (int j = jmin; j <= -i; j++) {           /* M0-1 */
       int jp = nim + i + j;
       put_block(m10, mdim, kki, (jp - 1) * lkmax, lkmax, g2d_block(map, blocks, slot, i, j),
-                map->lmmax, irel, fac, map->lmax);
+                map, irel, fac);
     }
     for (int j = 1 - i; j <= ni - i; j++) {      /* M00 */
       int jp = j + i;
       put_block(m00, mdim, kki, (jp - 1) * lkmax, lkmax, g2d_block(map, blocks, slot, i, j),
-                map->lmmax, irel, fac, map->lmax);
+                map, irel, fac);
     }
     for (int j = ni - i + 1; j <= jmax; j++) {   /* M01 */
       int jp = j + i - ni;
       put_block(m01, mdim, kki, (jp - 1) * lkmax, lkmax, g2d_block(map, blocks, slot, i, j),
-                map->lmmax, irel, fac, map->lmax);
+                map, irel, fac);
     }
   }
 }
@@ -563,17 +576,20 @@ void orc_cpacor(const double *conc, zc *mc, const zc *ma, const zc *mb,
 void orc_phystau(zc *tau, const zc *tinv1, const zc *tinv2, const zc *alpha,
                  int lmax, int irel, int ld, int idiag) {
   int lmmax = (lmax + 1) * (lmax + 1);
-  int nd = irel ? 2 * lmmax : lmmax;
+  int nd = irel == 2 ? 4 * lmmax : irel ? 2 * lmmax : lmmax;
   size_t sz = (size_t)ld * ld;
   zc *lmat = calloc(sz, sizeof(zc)), *rmat = calloc(sz, sizeof(zc)), *cmat = calloc(sz, sizeof(zc));
   int *ldex = malloc(sizeof(int) * nd);
   if (irel) {
-    /* ldex table of rsp-scf/phystau.f: 2,6,10,14,18 entries per l */
-    int k = 0;
-    for (int l = 0; k < nd; l++) {
+    /* ldex table of rsp-scf/phystau.f: 2,6,10,14,18 entries per l; BdG
+       (skkr_dbogo_bsf cpacoord_ksave.f:497): the hole half uses alpha_h,
+       stored after alpha_e as alpha[lmax+1+l] */
+    int kmymax = 2 * lmmax, k = 0;
+    for (int l = 0; k < kmymax; l++) {
       int cnt = (l == 0) ? 2 : 4 * l + 2;
-      for (int c = 0; c < cnt && k < nd; c++) ldex[k++] = l;
+      for (int c = 0; c < cnt && k < kmymax; c++) ldex[k++] = l;
     }
+    for (int q = kmymax; q < nd; q++) ldex[q] = ldex[q - kmymax] + lmax + 1;
   } else {
     for (int l = 0, k = 0; l <= lmax; l++)
       for (int m = -l; m <= l; m++) ldex[k++] = l;
@@ -718,7 +734,8 @@ int orc_cpacoord(const orc_problem *p, const double *conc, const zc *tminvl,
   int *ieqg = malloc(sizeof(int) * ngeff), *ieqgl = malloc(sizeof(int) * ngeff),
       *ieqgr = malloc(sizeof(int) * ngeff), *igordl = malloc(sizeof(int) * ngeff),
       *igordr = malloc(sizeof(int) * ngeff);
-  zc *gcache = calloc(bsz * p->nblk * (size_t)nk, sizeof(zc));
+  const int nbk = p->irel == 2 ? 2 * p->nblk : p->nblk; /* blocks per k */
+  zc *gcache = calloc(bsz * nbk * (size_t)nk, sizeof(zc));
   zc *ysave = calloc(msz * ngeff * (size_t)nk, sizeof(zc));
   zc *xsave = calloc(msz * ngeff * (size_t)nk, sizeof(zc));
   zc *taupart = calloc(sz * nintfc * (size_t)nthreads, sizeof(zc));
@@ -743,10 +760,14 @@ int orc_cpacoord(const orc_problem *p, const double *conc, const zc *tminvl,
       zc *mytau = taupart + sz * nintfc * tid;
       /* round-robin k split, as modulo(ik-1,nprocs)==myrank */
       for (int ik = tid; ik < nk; ik += nthreads) {
-        zc *blocks = gcache + bsz * p->nblk * (size_t)ik;
-        if (first)
+        zc *blocks = gcache + bsz * nbk * (size_t)ik;
+        if (first) {
           orc_gk_from_rtable(p->nblk, p->rstart, p->rvec, p->gR, p->map->lmmax, p->xk[2 * ik],
                              p->xk[2 * ik + 1], blocks);
+          if (p->irel == 2) /* hole table: same R vectors, entries after the electron ones */
+            orc_gk_from_rtable(p->nblk, p->rstart, p->rvec, p->gR + bsz * p->rstart[p->nblk],
+                               p->map->lmmax, p->xk[2 * ik], p->xk[2 * ik + 1], blocks + bsz * p->nblk);
+        }
         for (int ig = 0; ig < ngeff; ig++) {
           int ige = ieqg[ig] - 1, igel = ieqgl[ig] - 1, iger = ieqgr[ig] - 1;
           zc *ys = ysave + msz * ((size_t)ik * ngeff + (igordl[igel] - 1));

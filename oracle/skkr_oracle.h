@@ -52,6 +52,10 @@ typedef struct {
   int mi;            /* max layers per principal layer */
   int jmax;          /* max |layer offset| kept */
   const int *blkmap; /* [nslot][mi][2*jmax+1] */
+  /* BdG (skkr_dbogo_bsf): the hole block of block b sits at b + nblk and is
+   * mapped to (kappa,mu) with fach (main/g2d_pack.f + main/relmtrx.f) */
+  int bdg, nblk;
+  zc fach;
 } orc_g2dmap;
 
 /* ---- per-principal-layer packing: main/packer.f ------------------------ */
@@ -111,8 +115,8 @@ void orc_gk_from_rtable(int nblk, const int *rstart /*[nblk+1]*/,
 
 /* ---- the CPA + k loop: rsp-scf/cpacoord_ksave.f:139-489 --------------- */
 typedef struct {
-  int irel;            /* 0 non-relativistic (lm), 1 relativistic (kappa,mu) */
-  int lmax, lkmax;     /* lkmax = (lmax+1)^2 or 2(lmax+1)^2 */
+  int irel;            /* 0 non-relativistic (lm), 1 relativistic (kappa,mu), 2 BdG (e + h kappa,mu) */
+  int lmax, lkmax;     /* lkmax = (lmax+1)^2, 2(lmax+1)^2 or 4(lmax+1)^2 */
   int nprc;            /* interface principal layers */
   const int *ninprc;   /* [nprc+2]: layers per PL, 0 = left bulk, nprc+1 = right */
   int bulkgeo;         /* 1: every interface PL uses slot 1 */
@@ -132,7 +136,7 @@ typedef struct {
   int nblk;
   const int *rstart;
   const double *rvec;
-  const zc *gR;
+  const zc *gR;        /* [nR] (BdG: [2][nR], electron then hole table) */
 } orc_problem;
 
 typedef struct {

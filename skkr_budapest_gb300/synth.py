@@ -246,6 +246,19 @@ def alpha_sqwell(e: complex, vscreen: float, rs: float, lmax: int) -> np.ndarray
     return react / (1.0 + 1j * ck * react)
 
 
+def alpha_sqwell_hole(x: complex, vscreen: float, rs: float, lmax: int) -> np.ndarray:
+    """Hole screening parameters of skkr_dbogo_bsf main/alphamat.f (holes
+    branch): at the energy x = E_F - E (relativistic form x + x^2/c^2, as
+    alphamat.f forms it), with the negative square-root branches
+    ck = -sqrt(x), csk = -sqrt(x - V), and alpha_h = -react/(1 + i ck react)."""
+    ee = complex(x) + complex(x) * complex(x) / (C_LIGHT * C_LIGHT)
+    ck = -np.sqrt(ee)
+    csk = -np.sqrt(ee - vscreen)
+    tand = _tan_delta(ck, csk, rs, lmax)
+    react = -tand / ck
+    return -react / (1.0 + 1j * ck * react)
+
+
 def tinv_sqwell_l(e: complex, depth: float, radius: float, lmax: int) -> np.ndarray:
     """Inverse (unscreened) t_l^-1 of an attractive well V=depth<0."""
     ck = kappa_of(e)
@@ -262,6 +275,50 @@ def screened_tinv_nonrel(e, depth, radius, alpha, lmax) -> np.ndarray:
     d = tml / (1.0 - tml * alpha)
     lv = lm_l((lmax + 1) ** 2)
     return np.diag(d[lv]).astype(complex)
+
+
+def pairing_metric(lmax: int) -> np.ndarray:
+    """epsilon(kappa mu, kappa -mu) = (-1)^(j-mu): the singlet pairing matrix
+    in the (kappa,mu) basis, D epsilon D^T = epsilon for every double-group
+    matrix D of the (kappa,mu) representation."""
+    lv, kv = kmy_l_kappa(lmax)
+    n = len(lv)
+    eps = np.zeros((n, n))
+    for kap in sorted(set(kv.tolist())):
+        a = abs(kap)
+        for m in range(-a, a):            # mu = m + 1/2, j = |kappa| - 1/2
+            ir = 2 * kap * kap + kap + m       # 0-based index of (kappa, mu)
+            irp = 2 * kap * kap + kap - m - 1  # (kappa, -mu)
+            if ir < n and irp < n:
+                eps[ir, irp] = (-1.0) ** (a - 1 - m)
+    return eps
+
+
+def bdg_tinv(celoc, psq, celoch, psqh, depth, radius, so_split, alpha_e, alpha_h, lmax, delta):
+    """Screened BdG t^-1 (4 (lmax+1)^2 square, electron (kappa,mu) block then
+    hole block) of a j-split square well.  The physical inverse is
+        m = [[t_e^-1(E), delta eps], [delta eps^T, -conj(t_e^-1(E_F - conj E))]]
+    (hole t of BdG: t_h(E) = -t_e(-E*)^*, energies relative to E_F; eps the
+    singlet pairing metric, so that m is invariant under blockdiag(D, D*), the
+    representation under which the electron and the lmtolmconj-transformed
+    hole structure constants transform), and the screening of skkr_dbogo_bsf
+    rsp-scf/tmat.f subtracts alpha_e / alpha_h on the diagonal of t before
+    re-inverting."""
+    zero = np.zeros(lmax + 1, complex)
+    te = np.diag(screened_tinv_rel(celoc, psq, depth, radius, so_split, zero, lmax))
+    th = -np.conj(np.diag(screened_tinv_rel(celoch, psqh, depth, radius, so_split, zero, lmax)))
+    km = len(te)
+    m = np.zeros((2 * km, 2 * km), complex)
+    m[:km, :km] = np.diag(te)
+    m[km:, km:] = np.diag(th)
+    eps = pairing_metric(lmax)
+    m[:km, km:] = delta * eps
+    m[km:, :km] = delta * eps.T
+    lv, _ = kmy_l_kappa(lmax)
+    t = np.linalg.inv(m)
+    t[np.arange(km), np.arange(km)] -= np.asarray(alpha_e)[lv]
+    t[km + np.arange(km), km + np.arange(km)] -= np.asarray(alpha_h)[lv]
+    return np.linalg.inv(t)
 
 
 def kmy_l_kappa(lmax: int):
@@ -417,9 +474,23 @@ def cluster(st: Stacking, nshell: int = 3):
     return vs[sel][order], ns[sel][order], shells[1]
 
 
-def screened_realspace(e_struct: complex, vecs: np.ndarray, alpha: np.ndarray, lmax: int) -> np.ndarray:
+def lm_conj_matrix(lmax: int) -> np.ndarray:
+    """T of main/relmtrx.f lmtolmconj (skkr_dbogo_bsf): |lm> -> |lm>*, T(lm, l -m) = (-1)^m;
+    T is its own inverse."""
+    lmmax = (lmax + 1) ** 2
+    t = np.zeros((lmmax, lmmax))
+    for l in range(lmax + 1):
+        for m in range(-l, l + 1):
+            t[l * l + l + m, l * l + l - m] = (-1.0) ** m
+    return t
+
+
+def screened_realspace(e_struct: complex, vecs: np.ndarray, alpha: np.ndarray, lmax: int,
+                       hole: bool = False) -> np.ndarray:
     """Central row of G_scr = (1 - G0 alpha)^-1 G0 on the cluster `vecs`
-    (vecs[0] must be the origin).  Returns (N, LM, LM): G_scr(0 -> R_n)."""
+    (vecs[0] must be the origin).  Returns (N, LM, LM): G_scr(0 -> R_n).
+    hole=True screens the hole structure constants of skkr_dbogo_bsf
+    main/gstore.f:208-216, G0_h(n, m) = -T G0(m, n)^dagger T, with the hole alpha."""
     lmmax = (lmax + 1) ** 2
     nsite = len(vecs)
     lv = lm_l(lmmax)
@@ -429,6 +500,9 @@ def screened_realspace(e_struct: complex, vecs: np.ndarray, alpha: np.ndarray, l
     g = free_g0(e_struct, vecs[pair_n] - vecs[pair_m], lmax)
     for idx, (n, m) in enumerate(zip(pair_n, pair_m)):
         big[n * lmmax:(n + 1) * lmmax, m * lmmax:(m + 1) * lmmax] = g[idx]
+    if hole:
+        tm = np.kron(np.eye(nsite), lm_conj_matrix(lmax))
+        big = -tm @ big.conj().T @ tm
     # (1 - G0 alpha) X = G0, alpha diagonal per site
     amat = np.eye(nsite * lmmax, dtype=complex) - big * np.tile(al, nsite)[None, :]
     x = np.linalg.solve(amat, big)
@@ -449,9 +523,10 @@ class RTable:
     blk_of_j: dict = field(default_factory=dict)
 
 
-def build_rtable(st: Stacking, e_struct: complex, alpha: np.ndarray, lmax: int, nshell: int = 3) -> RTable:
+def build_rtable(st: Stacking, e_struct: complex, alpha: np.ndarray, lmax: int, nshell: int = 3,
+                 hole: bool = False) -> RTable:
     vecs, ns, _ = cluster(st, nshell)
-    g = screened_realspace(e_struct, vecs, alpha, lmax)
+    g = screened_realspace(e_struct, vecs, alpha, lmax, hole)
     jmax = int(np.max(np.abs(ns)))
     starts, rv, gr, blk_of_j = [0], [], [], {}
     for j in range(-jmax, jmax + 1):

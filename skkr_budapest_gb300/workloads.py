@@ -48,13 +48,15 @@ class EnergyProblem:
     tminva: np.ndarray
     tminvb: np.ndarray
     conc: np.ndarray            # (nintfc,)
-    alpha: np.ndarray           # (nintfc, lmax+1) screening per interface layer
+    alpha: np.ndarray           # (nintfc, lmax+1) screening per interface layer (BdG: alpha_e, alpha_h)
     itermaxl: int = 50
     itermaxr: int = 50
     errmax: float = 1.0e-8
     itcpam: int = 50
     cpatol: float = 1.0e-10
     meta: dict = field(default_factory=dict)
+    rt_h: S.RTable | None = None    # BdG: hole structure-constant table (same R vectors as rt)
+    fach: complex = 0.0             # BdG: relmtrx factor of the hole block
 
     @property
     def nk(self) -> int:
@@ -91,6 +93,12 @@ class SystemSpec:
     conc_range: tuple = (0.1, 0.9)
     alloy_depth_range: tuple = (-1.2, -0.4)
     cpatol: float = 1.0e-10
+    # BdG (irel=2): energies relative to e_fermi, pairing delta on sc_layers
+    # (interface layer indices) and on the leads flagged in sc_leads (L, R)
+    e_fermi: float = 0.0
+    delta: float = 0.0
+    sc_layers: tuple = ()
+    sc_leads: tuple = (False, False)
 
 
 def _contour(ne, eb, et, eps):
@@ -135,6 +143,20 @@ def rel_pl3_l2() -> SystemSpec:
                       [14] * 10 + [20] * 4 + [40] * 3 + [60, 90, 126], seed=4)
 
 
+def bdg_bcc(nsets=None, lmax: int = 3, pl: int = 4, ne: int = 64, im_e: float = 1.0e-4) -> SystemSpec:
+    """BdG interface (skkr_dbogo_bsf layout: electron (kappa,mu) block then hole
+    block, 4 (lmax+1)^2 per site): bcc(001) a=6.0, PL4 (n_PL = 256 at lmax=3),
+    3 interface PLs; superconducting left lead and first half of the interface
+    (delta = 1e-3 Ry), normal right lead and second half.  ne energies at
+    Im E = im_e spread over +-5 delta around E_F = 0.7 Ry."""
+    delta = 1.0e-3
+    z = np.linspace(-5 * delta, 5 * delta, ne) + 1j * im_e
+    nintfc = pl * 3
+    return SystemSpec("bdg_bcc", S.bcc001(6.0), 2, lmax, pl, 3, z,
+                      list([6] * ne if nsets is None else nsets), seed=5, e_fermi=0.7, delta=delta,
+                      sc_layers=tuple(range(nintfc // 2)), sc_leads=(True, False))
+
+
 def system_layers(spec: SystemSpec):
     ninprc = np.array([spec.pl] * (spec.nprc + 2), np.int32)
     return ninprc, spec.pl * spec.nprc
@@ -142,6 +164,8 @@ def system_layers(spec: SystemSpec):
 
 def energy_problem(spec: SystemSpec, ie: int, nset: int | None = None, kmesh: str = "ibz") -> EnergyProblem:
     """Build the inputs of contour point ie of a system (seeded, deterministic)."""
+    if spec.irel == 2:
+        return _bdg_problem(spec, ie, nset, kmesh)
     ce = complex(spec.energies[ie])
     lmax = spec.lmax
     irel = spec.irel
@@ -198,6 +222,64 @@ def energy_problem(spec: SystemSpec, ie: int, nset: int | None = None, kmesh: st
                          np.array([alpha] * nintfc), cpatol=spec.cpatol,
                          meta=dict(nset=ns, depth_bulk=d_bulk, depth_a=d_a, depth_b=d_b,
                                    radius=spec.radius, so_split=spec.so_split))
+
+
+def _bdg_problem(spec: SystemSpec, ie: int, nset, kmesh) -> EnergyProblem:
+    """Energy point of a BdG system, with the electron/hole energies and
+    factors of skkr_dbogo_bsf rsp-scf/cpacoord_ksave.f:160-169:
+    celoc = E_F + E, fac = psq/celoc; celoch = E_F - conj(E),
+    fach = conj(psqh)/conj(celoch)."""
+    c = S.C_LIGHT
+    ce = complex(spec.energies[ie])
+    ef = spec.e_fermi
+    celoc = ef + ce
+    psq = celoc + celoc * celoc / (c * c)
+    fac = psq / celoc
+    celoch = ef - ce.conjugate()
+    psqh = celoch + celoch * celoch / (c * c)
+    fach = psqh.conjugate() / celoch.conjugate()
+    lmax = spec.lmax
+    lk = 4 * (lmax + 1) ** 2
+    st = spec.stacking
+    _, _, dnn = S.cluster(st, 1)
+    rs = 0.7 * dnn
+    alpha_e = S.alpha_sqwell(psq, spec.vscreen, rs, lmax)
+    alpha_h = S.alpha_sqwell_hole(ef - ce, spec.vscreen, rs, lmax)
+    rt = S.build_rtable(st, psq, alpha_e, lmax)
+    rt_h = S.build_rtable(st, psqh, alpha_h, lmax, hole=True)
+    ninprc, nintfc = system_layers(spec)
+    blkmap = S.blkmap_translation_invariant(rt, spec.nprc + 2, int(max(ninprc)))
+    rng = np.random.default_rng(spec.seed)
+    d_bulk_l, d_bulk_r = rng.uniform(*spec.depth_range, size=2)
+    d_int = rng.uniform(*spec.depth_range, size=nintfc)
+
+    def tinv(depth, sc):
+        return S.bdg_tinv(celoc, psq, celoch, psqh, depth, spec.radius, spec.so_split, alpha_e, alpha_h,
+                          lmax, spec.delta if sc else 0.0)
+
+    tl = tinv(d_bulk_l, spec.sc_leads[0])
+    tr = tinv(d_bulk_r, spec.sc_leads[1])
+    tm = np.array([tinv(d, li in spec.sc_layers) for li, d in enumerate(d_int)])
+    ns = spec.nsets[ie] if nset is None else nset
+    # electron block transforms with D, the hole block (structure constants
+    # after lmtolmconj) with D*: blockdiag(D, D*) (the reference's sphbas.f
+    # uses blockdiag(D, D), which only holds while the blocks decouple)
+    lg1, rg1 = S.point_group_mats(lmax, 1)
+    z = np.zeros_like(lg1)
+    lg = np.block([[lg1, z], [z, lg1.conj()]])
+    rg = np.block([[rg1, z], [z, rg1.conj()]])
+    if kmesh == "ibz":
+        xk, wk = S.kmesh_square_c4v(ns, st.a2d)
+    else:
+        xk, wk = S.kmesh_square_full(ns, st.a2d)
+        lg, rg = lg[:1], rg[:1]
+    return EnergyProblem(spec.name, ie, ce, psq, fac, 2, lmax, lk, spec.nprc, ninprc, 1, nintfc,
+                         blkmap, rt, xk, wk, lg, rg, np.array([tl] * ninprc[0]), np.array([tr] * ninprc[-1]),
+                         tm, tm.copy(), tm.copy(), np.ones(nintfc),
+                         np.array([np.concatenate([alpha_e, alpha_h])] * nintfc), cpatol=spec.cpatol,
+                         meta=dict(nset=ns, celoc=celoc, celoch=celoch, psqh=psqh, depth_int=d_int,
+                                   radius=spec.radius, so_split=spec.so_split),
+                         rt_h=rt_h, fach=fach)
 
 
 def ata(conc: float, ma: np.ndarray, mb: np.ndarray) -> np.ndarray:
