@@ -32,7 +32,9 @@ extern "C" {
 #define SKKR_MAX_PRC 16   /* interface principal layers (param.h mprc) */
 #define SKKR_MAX_G 12     /* point-group operations (param.h melem)     */
 
-enum skkr_mode { SKKR_NONREL = 0, SKKR_REL = 1 };
+/* NONREL: lm basis (nrsp-scf); REL: (kappa,mu) (rsp-scf); BDG: electron
+ * (kappa,mu) block then hole block, 4 (lmax+1)^2 per site (skkr_dbogo_bsf) */
+enum skkr_mode { SKKR_NONREL = 0, SKKR_REL = 1, SKKR_BDG = 2 };
 enum skkr_precision { SKKR_FP64 = 0, SKKR_MIXED = 1 };
 
 enum skkr_error {
@@ -63,7 +65,9 @@ typedef struct {
   double cpatol;                  /* CPA tolerance on error3 (rsp-scf/fullcpa.f:142) */
   int precision;                  /* skkr_precision */
   int nk_chunk;                   /* k points per device batch (0: automatic) */
-  int slices;                     /* SKKR_MIXED: BF16 slices per product operand, 3..7 (0: 6) */
+  int slices;                     /* SKKR_MIXED: BF16 slices per product operand, 3..8 (0: 6;
+                                     8 for SKKR_BDG, whose e-h block is ~1e-2 of the rest).  Digits
+                                     are 8-bit for n_PL <= 128 (8 slices act as 7), 7-bit above */
 } skkr_sizes;
 
 /* Real-space screened structure constants of one energy, grouped in
@@ -140,6 +144,22 @@ int skkr_gpu_cpacoord(skkr_ctx *ctx, double ce_re, double ce_im, double fac_re,
                       const double *tminvb, double *tauc, double *taua,
                       double *taub, int ld, skkr_status *status);
 
+/* BdG energy (skkr_dbogo_bsf/rsp-scf/cpacoord_ksave.f): as skkr_gpu_cpacoord
+ * on a SKKR_BDG context, with the hole factor fach = conj(psqh)/conj(celoch)
+ * (:160-169).  rt->gR holds 2 * rstart[nblk] blocks: the electron table, then
+ * the hole table (main/gstore.f:208-216: conjugate-transposed and
+ * lmtolmconj-transformed, screened with the hole alpha) on the same R
+ * vectors; site blocks are blockdiag(relmtrx(G_e, fac), relmtrx(G_h, fach))
+ * (main/g2d_pack.f, main/relmtrx.f).  lg / rg are the BdG point-group
+ * matrices, e.g. blockdiag(D, D*).  The slot API does not take BdG energies. */
+int skkr_gpu_cpacoord_bdg(skkr_ctx *ctx, double ce_re, double ce_im, double fac_re,
+                          double fac_im, double fach_re, double fach_im, const skkr_rtable *rt,
+                          int nk, const double *xk, const double *wk, const double *lg,
+                          const double *rg, const double *conc, const double *tminvl,
+                          const double *tminvr, double *tminv, const double *tminva,
+                          const double *tminvb, double *tauc, double *taua, double *taub, int ld,
+                          skkr_status *st);
+
 /* Split form for callers that keep inputs resident on the device across
  * calls: stage (host -> device), run (device only), fetch (device -> host).
  * skkr_gpu_cpacoord == stage + run + fetch. */
@@ -176,7 +196,9 @@ int skkr_gpu_fetch_slot(skkr_ctx *ctx, int slot, double *tminv, double *tauc,
 int skkr_gpu_kernel_stats(int enable, double *out);
 
 /* Screened -> physical tau of one layer on the device
- * (rsp-scf/phystau.f:2-61, nrsp-scf/phystau.f): tau := (1+a t)tau(1+t a) - (a + a t a). */
+ * (rsp-scf/phystau.f:2-61, nrsp-scf/phystau.f): tau := (1+a t)tau(1+t a) - (a + a t a).
+ * alpha[l], l = 0..lmax; SKKR_BDG: alpha_e[0..lmax] then alpha_h[0..lmax]
+ * (skkr_dbogo_bsf cpacoord_ksave.f:497). */
 int skkr_gpu_phystau(int mode, int lmax, double *tau, const double *tinv,
                      const double *alpha, int ld);
 

@@ -22,7 +22,7 @@ class Context:
     def __init__(self, irel, lmax, nprc, ninprc, ngeff, itermaxl=50, itermaxr=50, errmax=1e-8,
                  itcpam=50, cpatol=1e-10, precision="fp64", nk_chunk=0, slices=0):
         s = N.Sizes()
-        s.mode = N.REL if irel else N.NONREL
+        s.mode = {0: N.NONREL, 1: N.REL, 2: N.BDG}[int(irel)]
         s.lmax = lmax
         s.nprc = nprc
         for i, v in enumerate(ninprc):
@@ -35,7 +35,7 @@ class Context:
         s.nk_chunk = nk_chunk
         s.slices = slices
         self.sizes = s
-        self.lk = 2 * (lmax + 1) ** 2 if irel else (lmax + 1) ** 2
+        self.lk = (4 if irel == 2 else 2 if irel else 1) * (lmax + 1) ** 2
         self.nintfc = int(sum(ninprc[1:nprc + 1]))
         h = C.c_void_p()
         rc = N.lib().skkr_gpu_create(C.cast(C.pointer(s), C.c_void_p), C.cast(C.pointer(h), C.c_void_p))
@@ -69,7 +69,7 @@ class Context:
 
     # -- split form -------------------------------------------------------
     def _host_inputs(self, ep, tminv=None):
-        rt = N.RTableHolder(ep.rt, ep.blkmap)
+        rt = N.RTableHolder(ep.rt, ep.blkmap, hole=ep.rt_h if ep.irel == 2 else None)
         arrs = dict(
             xk=np.ascontiguousarray(ep.xk, np.float64), wk=np.ascontiguousarray(ep.wk, np.float64),
             lg=N.cm(ep.lg), rg=N.cm(ep.rg), conc=np.ascontiguousarray(ep.conc, np.float64),
@@ -139,11 +139,15 @@ class Context:
         out = {k: np.zeros((n, lk, lk), np.complex128) for k in ("tauc", "taua", "taub")}
         st = N.Status()
         p = N._p
-        rc = N.lib().skkr_gpu_cpacoord(self.h, ep.ce.real, ep.ce.imag, ep.fac.real, ep.fac.imag,
-                                       rt.ptr(), len(a["xk"]), p(a["xk"]), p(a["wk"]), p(a["lg"]),
-                                       p(a["rg"]), p(a["conc"]), p(a["tl"]), p(a["tr"]), p(a["ti"]),
-                                       p(a["ta"]), p(a["tb"]), p(out["tauc"]), p(out["taua"]),
-                                       p(out["taub"]), lk, C.cast(C.pointer(st), C.c_void_p))
+        tail = (rt.ptr(), len(a["xk"]), p(a["xk"]), p(a["wk"]), p(a["lg"]), p(a["rg"]), p(a["conc"]),
+                p(a["tl"]), p(a["tr"]), p(a["ti"]), p(a["ta"]), p(a["tb"]), p(out["tauc"]), p(out["taua"]),
+                p(out["taub"]), lk, C.cast(C.pointer(st), C.c_void_p))
+        if ep.irel == 2:
+            fach = complex(ep.fach)
+            rc = N.lib().skkr_gpu_cpacoord_bdg(self.h, ep.ce.real, ep.ce.imag, ep.fac.real, ep.fac.imag,
+                                               fach.real, fach.imag, *tail)
+        else:
+            rc = N.lib().skkr_gpu_cpacoord(self.h, ep.ce.real, ep.ce.imag, ep.fac.real, ep.fac.imag, *tail)
         if check:
             N._check(rc, "skkr_gpu_cpacoord")
         res = {k: N.uncm(v) for k, v in out.items()}

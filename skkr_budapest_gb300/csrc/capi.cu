@@ -162,7 +162,9 @@ struct skkr_ctx {
   // staged energy
   int staged = 0;
   int nk = 0, nblk = 0, nrt = 0, nslot = 0, mi = 0, jmax = 0, maxr = 0;
+  int nbk = 0;    // structure-constant blocks per k (BdG: electron then hole, 2 nblk)
   zd fac, ce;
+  zd fach = {1.0, 0.0};  // BdG: relmtrx factor of the hole block
   std::vector<int> blkmap;
   std::vector<double> conc_h;
   DBuf gR, rvec, rstart, blkmap_d, xk, wk, lg, rg, conc;
@@ -171,7 +173,7 @@ struct skkr_ctx {
   DBuf trot, trtmp;  // [ngeff][nlay][lk^2]
   DBuf pnorm;     // sorttmat / compmat norms
   // per-energy caches over all k
-  DBuf G;         // [nk][nblk][lmmax^2]
+  DBuf G;         // [nk][nbk][lmmax^2]
   DBuf sspo;      // [nk][nsl][n^2]
   // chunk work
   DBuf pool, jobs, dec, decf, deci, tauw, tauk;
@@ -203,8 +205,8 @@ struct skkr_ctx {
 // into the working fields, so the per-energy work buffers are shared.
 struct SlotStore {
   DBuf gR, rvec, rstart, blkmap_d, xk, wk, lg, rg, conc, tcat, tab, tauc, cpa;
-  int staged = 0, nk = 0, nblk = 0, nrt = 0, nslot = 0, mi = 0, jmax = 0, maxr = 0;
-  zd fac = {0, 0}, ce = {0, 0};
+  int staged = 0, nk = 0, nblk = 0, nrt = 0, nslot = 0, mi = 0, jmax = 0, maxr = 0, nbk = 0;
+  zd fac = {0, 0}, ce = {0, 0}, fach = {1, 0};
   std::vector<int> blkmap;
   std::vector<double> conc_h;
 };
@@ -226,6 +228,8 @@ static void swap_slot(skkr_ctx *c, SlotStore &s) {
   std::swap(c->staged, s.staged);
   std::swap(c->nk, s.nk);
   std::swap(c->nblk, s.nblk);
+  std::swap(c->nbk, s.nbk);
+  std::swap(c->fach, s.fach);
   std::swap(c->nrt, s.nrt);
   std::swap(c->nslot, s.nslot);
   std::swap(c->mi, s.mi);
@@ -241,7 +245,7 @@ static void swap_slot(skkr_ctx *c, SlotStore &s) {
 extern "C" int skkr_gpu_create(const skkr_sizes *sizes, skkr_ctx **out) {
   if (!sizes || !out) return SKKR_ERR_ARG;
   const skkr_sizes &s = *sizes;
-  if (s.mode != SKKR_NONREL && s.mode != SKKR_REL) return SKKR_ERR_ARG;
+  if (s.mode != SKKR_NONREL && s.mode != SKKR_REL && s.mode != SKKR_BDG) return SKKR_ERR_ARG;
   if (s.lmax < 0 || s.lmax > 3 || s.nprc < 1 || s.nprc > SKKR_MAX_PRC) return SKKR_ERR_ARG;
   if (s.ngeff < 1 || s.ngeff > 8) return SKKR_ERR_ARG;
   if (s.precision != SKKR_FP64 && s.precision != SKKR_MIXED) return SKKR_ERR_ARG;
@@ -252,19 +256,24 @@ extern "C" int skkr_gpu_create(const skkr_sizes *sizes, skkr_ctx **out) {
   skkr_ctx *c = new skkr_ctx();
   c->sz = s;
   c->lmmax = (s.lmax + 1) * (s.lmax + 1);
-  c->lk = s.mode == SKKR_REL ? 2 * c->lmmax : c->lmmax;
+  c->lk = s.mode == SKKR_BDG ? 4 * c->lmmax : s.mode == SKKR_REL ? 2 * c->lmmax : c->lmmax;
   c->pl = s.ninprc[1];
   c->n = c->pl * c->lk;
   c->nprc = s.nprc;
   c->nintfc = c->pl * s.nprc;
   c->ngeff = s.ngeff;
-  if (s.slices != 0) {
-    if (s.slices < 3 || s.slices > 7) {
+  if (s.slices == 0 && s.mode == SKKR_BDG) {
+    // the anomalous block is ~1e-2 of the row scales the slicing is set by;
+    // n_PL > 128 runs 7-bit digits: 7 slices
+    c->slices = 7;
+    c->slices_res = 8;
+  } else if (s.slices != 0) {
+    if (s.slices < 3 || s.slices > 8) {
       delete c;
       return SKKR_ERR_ARG;
     }
     c->slices = s.slices;
-    c->slices_res = s.slices < 7 ? s.slices + 1 : 7;
+    c->slices_res = s.slices < 8 ? s.slices + 1 : 8;
   }
   if (c->n > 256) {
     delete c;
@@ -274,7 +283,7 @@ extern "C" int skkr_gpu_create(const skkr_sizes *sizes, skkr_ctx **out) {
     delete c;
     return SKKR_ERR_CUDA;
   }
-  cudaError_t e = pack_set_tables(s.mode == SKKR_REL, s.lmax);
+  cudaError_t e = pack_set_tables(s.mode != SKKR_NONREL, s.lmax);
   if (e != cudaSuccess) {
     g_last_error = std::string("pack_set_tables: ") + cudaGetErrorString(e);
     cudaStreamDestroy(c->st);
@@ -356,6 +365,8 @@ extern "C" int skkr_gpu_stage(skkr_ctx *c, double ce_re, double ce_im, double fa
   c->fac = zmk(fac_re, fac_im);
   c->nk = nk;
   c->nblk = rt->nblk;
+  const bool bdg = c->sz.mode == SKKR_BDG;
+  c->nbk = bdg ? 2 * rt->nblk : rt->nblk;
   c->nrt = rt->rstart[rt->nblk];
   c->nslot = rt->nslot;
   c->mi = rt->mi;
@@ -368,9 +379,10 @@ extern "C" int skkr_gpu_stage(skkr_ctx *c, double ce_re, double ce_im, double fa
   for (int v : c->blkmap)
     if (v >= rt->nblk) return SKKR_ERR_ARG;
   const size_t bs = (size_t)c->lmmax * c->lmmax;
-  CKR(c->gR.ensure(c->nrt * bs * sizeof(zd)));
-  CKR(c->rvec.ensure(c->nrt * 2 * sizeof(double)));
-  CKR(c->rstart.ensure((rt->nblk + 1) * sizeof(int)));
+  const int ntab = bdg ? 2 : 1;  // BdG: electron table, then the hole table on the same R
+  CKR(c->gR.ensure(ntab * c->nrt * bs * sizeof(zd)));
+  CKR(c->rvec.ensure(ntab * c->nrt * 2 * sizeof(double)));
+  CKR(c->rstart.ensure((c->nbk + 1) * sizeof(int)));
   CKR(c->blkmap_d.ensure(c->blkmap.size() * sizeof(int)));
   CKR(c->xk.ensure((size_t)nk * 2 * sizeof(double)));
   CKR(c->wk.ensure((size_t)nk * sizeof(double)));
@@ -381,9 +393,19 @@ extern "C" int skkr_gpu_stage(skkr_ctx *c, double ce_re, double ce_im, double fa
   CKR(c->tcat.ensure((size_t)nlay * lk2 * sizeof(zd)));
   CKR(c->tab.ensure((size_t)c->nintfc * 2 * lk2 * sizeof(zd)));
   cudaStream_t st = c->st;
-  CK(cudaMemcpyAsync(c->gR.p, rt->gR, c->nrt * bs * sizeof(zd), cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(c->rvec.p, rt->rvec, c->nrt * 2 * sizeof(double), cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(c->rstart.p, rt->rstart, (rt->nblk + 1) * sizeof(int), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(c->gR.p, rt->gR, ntab * c->nrt * bs * sizeof(zd), cudaMemcpyHostToDevice, st));
+  {
+    // block b >= nblk (hole) reads rows nrt + rstart[b - nblk] .. of the doubled table
+    std::vector<int> rs(c->nbk + 1);
+    std::vector<double> rv((size_t)ntab * c->nrt * 2);
+    for (int b = 0; b <= c->nbk; b++)
+      rs[b] = b <= rt->nblk ? rt->rstart[b] : c->nrt + rt->rstart[b - rt->nblk];
+    for (int t = 0; t < ntab; t++)
+      std::copy(rt->rvec, rt->rvec + (size_t)c->nrt * 2, rv.begin() + (size_t)t * c->nrt * 2);
+    CK(cudaMemcpyAsync(c->rvec.p, rv.data(), rv.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->rstart.p, rs.data(), rs.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    CK(cudaStreamSynchronize(st));  // rs / rv are host temporaries
+  }
   CK(cudaMemcpyAsync(c->blkmap_d.p, c->blkmap.data(), c->blkmap.size() * sizeof(int),
                      cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(c->xk.p, xk, (size_t)nk * 2 * sizeof(double), cudaMemcpyHostToDevice, st));
@@ -966,7 +988,7 @@ extern "C" int skkr_gpu_run(skkr_ctx *c, skkr_status *status) {
   CKR(c->jobs.ensure(c->jobs_h.size() * sizeof(PackJob)));
   CK(cudaMemcpyAsync(c->jobs.p, c->jobs_h.data(), c->jobs_h.size() * sizeof(PackJob),
                      cudaMemcpyHostToDevice, st));
-  CKR(c->G.ensure((size_t)nk * c->nblk * bs * sizeof(zd)));
+  CKR(c->G.ensure((size_t)nk * c->nbk * bs * sizeof(zd)));
   // chunk size: keep the per-chunk work within a fixed budget
   {
     const int ncmax = 2 * c->ngeff;
@@ -1000,15 +1022,15 @@ extern "C" int skkr_gpu_run(skkr_ctx *c, skkr_status *status) {
       c->nls = nLs;
       c->nsl = nLs + nRs;
       CKR(c->sspo.ensure((size_t)nk * c->nsl * MB * sizeof(zd)));
-      launch_gk_ft(c->gR.as<zd>(), c->rvec.as<double>(), c->rstart.as<int>(), c->nblk, c->lmmax,
+      launch_gk_ft(c->gR.as<zd>(), c->rvec.as<double>(), c->rstart.as<int>(), c->nbk, c->lmmax,
                    c->xk.as<double>(), nk, c->G.as<zd>(), st);
     }
     CKR(c->S.ensure((size_t)ncls * ni * lk2 * sizeof(zd)));
     for (int k0 = 0; k0 < nk; k0 += c->kc) {
       const int nkc = std::min(c->kc, nk - k0);
-      launch_pack(c->G.as<zd>() + (size_t)k0 * c->nblk * bs, c->nblk, c->blkmap_d.as<int>(), c->mi,
-                  c->jmax, c->jobs.as<PackJob>(), c->nmat, lk, c->lmmax, c->sz.mode == SKKR_REL,
-                  c->fac, nkc, c->pool.as<zd>(), c->nmat, n, st);
+      launch_pack(c->G.as<zd>() + (size_t)k0 * c->nbk * bs, c->nblk, c->nbk, c->blkmap_d.as<int>(),
+                  c->mi, c->jmax, c->jobs.as<PackJob>(), c->nmat, lk, c->lmmax, c->sz.mode, c->fac,
+                  c->fach, nkc, c->pool.as<zd>(), c->nmat, n, st);
       if (itcpa == 1) CKR(run_decimation(c, k0, nkc, lcls, rcls));
       if (c->err_code) break;
       CKR(run_tau2d(c, k0, nkc, icls));
@@ -1113,6 +1135,20 @@ extern "C" int skkr_gpu_cpacoord(skkr_ctx *c, double ce_re, double ce_im, double
   return skkr_gpu_fetch(c, tminv, tauc, taua, taub, ld);
 }
 
+extern "C" int skkr_gpu_cpacoord_bdg(skkr_ctx *c, double ce_re, double ce_im, double fac_re,
+                                     double fac_im, double fach_re, double fach_im,
+                                     const skkr_rtable *rt, int nk, const double *xk,
+                                     const double *wk, const double *lg, const double *rg,
+                                     const double *conc, const double *tminvl,
+                                     const double *tminvr, double *tminv, const double *tminva,
+                                     const double *tminvb, double *tauc, double *taua,
+                                     double *taub, int ld, skkr_status *status) {
+  if (!c || c->sz.mode != SKKR_BDG) return SKKR_ERR_ARG;
+  c->fach = zmk(fach_re, fach_im);
+  return skkr_gpu_cpacoord(c, ce_re, ce_im, fac_re, fac_im, rt, nk, xk, wk, lg, rg, conc, tminvl,
+                           tminvr, tminv, tminva, tminvb, tauc, taua, taub, ld, status);
+}
+
 // ---------------------------------------------------------------------------
 // multi-energy residency: stage several energies, run / fetch any of them
 static SlotStore *get_slot(skkr_ctx *c, int slot, bool create) {
@@ -1135,6 +1171,7 @@ extern "C" int skkr_gpu_stage_slot(skkr_ctx *c, int slot, double ce_re, double c
                                    const double *tminvr, const double *tminv,
                                    const double *tminva, const double *tminvb, int ld) {
   if (!c) return SKKR_ERR_ARG;
+  if (c->sz.mode == SKKR_BDG) return SKKR_ERR_UNSUPPORTED;  // BdG energies go through cpacoord_bdg
   SlotStore *s = get_slot(c, slot, true);
   if (!s) return SKKR_ERR_ARG;
   swap_slot(c, *s);
@@ -1349,13 +1386,17 @@ __global__ void k_phys_mats(const zd *tinv, const zd *alpha, const int *lof, int
 extern "C" int skkr_gpu_phystau(int mode, int lmax, double *tau, const double *tinv,
                                 const double *alpha, int ld) {
   if (!tau || !tinv || !alpha || lmax < 0 || lmax > 3) return SKKR_ERR_ARG;
-  const int lmmax = (lmax + 1) * (lmax + 1), nd = mode == SKKR_REL ? 2 * lmmax : lmmax;
+  if (mode != SKKR_NONREL && mode != SKKR_REL && mode != SKKR_BDG) return SKKR_ERR_ARG;
+  const int lmmax = (lmax + 1) * (lmax + 1),
+            nd = mode == SKKR_BDG ? 4 * lmmax : mode == SKKR_REL ? 2 * lmmax : lmmax;
+  const int nal = mode == SKKR_BDG ? 2 * (lmax + 1) : lmax + 1;  // BdG: alpha_e then alpha_h
   if (ld < nd) return SKKR_ERR_ARG;
   std::vector<int> lof(nd);
-  if (mode == SKKR_REL) {
+  if (mode != SKKR_NONREL) {
     int k = 0;  // ldex of rsp-scf/phystau.f: 2 entries for l=0, 4l+2 for l>0
-    for (int l = 0; k < nd; l++)
-      for (int q = 0; q < (l == 0 ? 2 : 4 * l + 2) && k < nd; q++) lof[k++] = l;
+    for (int l = 0; k < 2 * lmmax; l++)
+      for (int q = 0; q < (l == 0 ? 2 : 4 * l + 2) && k < 2 * lmmax; q++) lof[k++] = l;
+    for (int q = 2 * lmmax; q < nd; q++) lof[q] = lof[q - 2 * lmmax] + lmax + 1;
   } else {
     for (int l = 0, k = 0; l <= lmax; l++)
       for (int m = -l; m <= l; m++) lof[k++] = l;
@@ -1366,7 +1407,7 @@ extern "C" int skkr_gpu_phystau(int mode, int lmax, double *tau, const double *t
   int *Lo;
   CKR(s.alloc(&T, MB));
   CKR(s.alloc(&Ti, MB));
-  CKR(s.alloc(&Al, lmax + 1));
+  CKR(s.alloc(&Al, nal));
   CKR(s.alloc(&Lm, MB));
   CKR(s.alloc(&Rm, MB));
   CKR(s.alloc(&Cm, MB));
@@ -1374,7 +1415,7 @@ extern "C" int skkr_gpu_phystau(int mode, int lmax, double *tau, const double *t
   CKR(s.alloc(&Lo, nd));
   CKR(upload_mats(T, tau, 1, nd, ld));
   CKR(upload_mats(Ti, tinv, 1, nd, ld));
-  CK(cudaMemcpy(Al, alpha, (lmax + 1) * sizeof(zd), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(Al, alpha, nal * sizeof(zd), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(Lo, lof.data(), nd * sizeof(int), cudaMemcpyHostToDevice));
   k_phys_mats<<<4, 256>>>(Ti, Al, Lo, nd, Lm, Rm, Cm);
   SKKR_LAUNCHED();

@@ -13,9 +13,9 @@ struct PackJob {
   int dest;   // matrix index in the per-k pool
 };
 cudaError_t pack_set_tables(int irel, int lmax);
-void launch_pack(const zd *G, int nblk, const int *d_blkmap, int mi, int jmax, const PackJob *d_jobs,
-                 int njobs, int lk, int lmmax, int irel, zd fac, int nk, zd *pool, int nmat, int npl,
-                 cudaStream_t st);
+void launch_pack(const zd *G, int nblk, int nbk, const int *d_blkmap, int mi, int jmax,
+                 const PackJob *d_jobs, int njobs, int lk, int lmmax, int mode, zd fac, zd fach, int nk,
+                 zd *pool, int nmat, int npl, cudaStream_t st);
 
 // batched complex GEMM, items (k, c) with k < nk, c < nc; act[k*nc+c]==0 skips.
 // mode 0: C = A*B        1: C = C - A*B

@@ -95,18 +95,21 @@ cudaError_t pack_set_tables(int irel, int lmax) {
   return e;
 }
 
-__global__ void __launch_bounds__(256) k_pack(const zd *__restrict__ G, int nblk,
+// mode 0: lm, 1: (kappa,mu), 2: BdG -- blockdiag of the electron block b
+// (fac) and the hole block b + nblk (fach), each mapped to (kappa,mu)
+// (skkr_dbogo_bsf main/g2d_pack.f + main/relmtrx.f).  nbk: blocks per k.
+__global__ void __launch_bounds__(256) k_pack(const zd *__restrict__ G, int nblk, int nbk,
                                               const int *__restrict__ blkmap, int mi, int jmax,
                                               const PackJob *__restrict__ jobs, int lk, int lmmax,
-                                              int irel, zd fac, zd *__restrict__ pool, int nmat,
-                                              int npl) {
+                                              int mode, zd fac, zd fach, zd *__restrict__ pool,
+                                              int nmat, int npl) {
   const int kk = blockIdx.y;
   const PackJob jb = jobs[blockIdx.z];
   const int nrow = jb.ni * lk;
   const int ncol = (jb.which == 0 ? jb.ni : jb.which == 1 ? jb.nim : jb.nip) * lk;
   const int nj = 2 * jmax + 1;
   zd *out = pool + ((long long)kk * nmat + jb.dest) * (long long)npl * npl;
-  const zd *Gk = G + (long long)kk * nblk * lmmax * lmmax;
+  const zd *Gk = G + (long long)kk * nbk * lmmax * lmmax;
   const int total = npl * npl;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
     const int r = e % npl, c = e / npl;
@@ -133,7 +136,20 @@ __global__ void __launch_bounds__(256) k_pack(const zd *__restrict__ G, int nblk
         if (b >= 0) {
           const zd *g = Gk + (long long)b * lmmax * lmmax;
           zd val;
-          if (irel) {
+          if (mode == 2) {
+            const int km = lk >> 1;
+            if ((k1 < km) == (k2 < km)) {
+              const bool h = k1 >= km;
+              const zd *gg = h ? g + (long long)nblk * lmmax * lmmax : g;
+              const int q1 = h ? k1 - km : k1, q2 = h ? k2 - km : k2;
+              const zd f = h ? fach : fac;
+              zd a1 = zmul(f, gg[c_ind1[q1] + c_ind1[q2] * lmmax]);
+              zd a2 = zmul(f, gg[c_ind2[q1] + c_ind2[q2] * lmmax]);
+              val = zadd(zscale(c_u1[q2], zscale(c_u1[q1], a1)), zscale(c_u2[q2], zscale(c_u2[q1], a2)));
+            } else {
+              val = make_double2(0.0, 0.0);
+            }
+          } else if (mode == 1) {
             // relmtrx.f: b = u1 (fac a) u1 + u2 (fac a) u2
             zd a1 = zmul(fac, g[c_ind1[k1] + c_ind1[k2] * lmmax]);
             zd a2 = zmul(fac, g[c_ind2[k1] + c_ind2[k2] * lmmax]);
@@ -149,14 +165,14 @@ __global__ void __launch_bounds__(256) k_pack(const zd *__restrict__ G, int nblk
   }
 }
 
-void launch_pack(const zd *G, int nblk, const int *d_blkmap, int mi, int jmax, const PackJob *d_jobs,
-                 int njobs, int lk, int lmmax, int irel, zd fac, int nk, zd *pool, int nmat, int npl,
-                 cudaStream_t st) {
+void launch_pack(const zd *G, int nblk, int nbk, const int *d_blkmap, int mi, int jmax,
+                 const PackJob *d_jobs, int njobs, int lk, int lmmax, int mode, zd fac, zd fach, int nk,
+                 zd *pool, int nmat, int npl, cudaStream_t st) {
   if (nk <= 0 || njobs <= 0) return;
   int per = (npl * npl + 255) / 256;
   dim3 grid(per < 64 ? per : 64, nk, njobs);
-  k_pack<<<grid, 256, 0, st>>>(G, nblk, d_blkmap, mi, jmax, d_jobs, lk, lmmax, irel, fac, pool,
-                               nmat, npl);
+  k_pack<<<grid, 256, 0, st>>>(G, nblk, nbk, d_blkmap, mi, jmax, d_jobs, lk, lmmax, mode, fac, fach,
+                               pool, nmat, npl);
   SKKR_LAUNCHED();
 }
 

@@ -182,39 +182,40 @@ __device__ __forceinline__ long long fix_round(double x, int E) {
 }
 __device__ __forceinline__ float pow2f(int e) { return __int_as_float((127 + e) << 23); }
 
-// balanced base-256 digits of Y = round(x 2^(7+8(S-1)) / sigma), most
-// significant first (|d| <= 128), from the two 32-bit halves of |Y|
-template <int S>
+// balanced base-2^DB digits of Y = round(x 2^((DB-1) + DB(S-1)) / sigma),
+// most significant first (|d| <= 2^(DB-1)).  DB = 8 for K = 2n <= 256; DB = 7
+// above, so that every FP32 level accumulator (at most 4 (p,q) pairs of
+// |d d| <= 2^(2DB-2) over K terms) stays an exact integer below 2^24.
+template <int S, int DB>
 __device__ __forceinline__ void slice_digits(double x, int es, float *dig) {
-  const long long Y = fix_round(x, 7 + 8 * (S - 1) - es);
+  static_assert(DB * S <= 62, "digits must fit the 62-bit fixed-point value");
+  const long long Y = fix_round(x, (DB - 1) + DB * (S - 1) - es);
   const unsigned long long u = (unsigned long long)(Y < 0 ? -Y : Y);
-  const uint32_t lo = (uint32_t)u, hi = (uint32_t)(u >> 32);
   const bool neg = Y < 0;
+  constexpr int HALF = 1 << (DB - 1);
   int carry = 0;
 #pragma unroll
   for (int q = 0; q < S; q++) {  // q = 0: least significant digit
-    const int bit = 8 * q;
-    const uint32_t raw = bit < 32 ? (lo >> bit) & 0xFFu : (hi >> (bit - 32)) & 0xFFu;
-    int d = (int)raw + carry;
-    carry = d > 128;
-    d -= carry << 8;
+    int d = (int)((u >> (DB * q)) & ((1ull << DB) - 1)) + carry;
+    carry = d > HALF;
+    d -= carry << DB;
     dig[S - 1 - q] = (float)(neg ? -d : d);
   }
 }
 
-template <int S>
+template <int S, int DB>
 __device__ __forceinline__ void store_digits(const float *dig, float sign, int wshift, __nv_bfloat16 *dst,
                                              long long sstride) {
 #pragma unroll
-  for (int p = 0; p < S; p++) dst[p * sstride] = __float2bfloat16_rn(sign * dig[p] * pow2f(wshift - 8 * p));
+  for (int p = 0; p < S; p++) dst[p * sstride] = __float2bfloat16_rn(sign * dig[p] * pow2f(wshift - DB * p));
 }
 
-template <int S>
+template <int S, int DB>
 __device__ __forceinline__ void slice_store(double x, int es, int wshift, __nv_bfloat16 *dst,
                                             long long sstride) {
   float dig[S];
-  slice_digits<S>(x, es, dig);
-  store_digits<S>(dig, 1.0f, wshift, dst, sstride);
+  slice_digits<S, DB>(x, es, dig);
+  store_digits<S, DB>(dig, 1.0f, wshift, dst, sstride);
 }
 
 // element (row r, K index kk) of one slice region in the k-block tiled layout
@@ -222,7 +223,7 @@ __device__ __forceinline__ long long tiled(int r, int kk, int rows) {
   return ((long long)(kk >> 5) * rows + r) * 32 + (kk & 31);
 }
 
-template <int S>
+template <int S, int DB>
 __global__ void __launch_bounds__(256) k_split_a(MatRef A, int n, int nc, const int *__restrict__ act,
                                                  __nv_bfloat16 *__restrict__ out, int Mp, int Kp,
                                                  int *__restrict__ sigma) {
@@ -265,8 +266,8 @@ __global__ void __launch_bounds__(256) k_split_a(MatRef A, int n, int nc, const 
       if (r < n && col < n) {
         const int es = sc[q];
         zd v = T[q][lane];
-        slice_store<S>(v.x, es, 0, base + tiled(r, col, Mp), sstride);
-        slice_store<S>(v.y, es, 0, base + tiled(r, n + col, Mp), sstride);
+        slice_store<S, DB>(v.x, es, 0, base + tiled(r, col, Mp), sstride);
+        slice_store<S, DB>(v.y, es, 0, base + tiled(r, n + col, Mp), sstride);
       }
     }
     __syncthreads();
@@ -275,7 +276,7 @@ __global__ void __launch_bounds__(256) k_split_a(MatRef A, int n, int nc, const 
 
 // B'^T from complex B (n x n, MatRef): one warp per column j; rows j and n+j
 // of B'^T are [Re B(:,j), -Im B(:,j)] and [Im B(:,j), Re B(:,j)].
-template <int S>
+template <int S, int DB>
 __global__ void __launch_bounds__(256) k_split_b(MatRef B, int n, int nc, const int *__restrict__ act,
                                                  __nv_bfloat16 *__restrict__ out, int Np, int Kp,
                                                  int *__restrict__ tau) {
@@ -303,18 +304,19 @@ __global__ void __launch_bounds__(256) k_split_b(MatRef B, int n, int nc, const 
   for (int k = lane; k < n; k += 32) {
     zd v = b[k];
     float dr[S], di[S];
-    slice_digits<S>(v.x, es, dr);
-    slice_digits<S>(v.y, es, di);
-    store_digits<S>(dr, 1.0f, 16, base + tiled(j, k, Np), sstride);
-    store_digits<S>(di, -1.0f, 16, base + tiled(j, n + k, Np), sstride);
-    store_digits<S>(di, 1.0f, 16, base + tiled(n + j, k, Np), sstride);
-    store_digits<S>(dr, 1.0f, 16, base + tiled(n + j, n + k, Np), sstride);
+    slice_digits<S, DB>(v.x, es, dr);
+    slice_digits<S, DB>(v.y, es, di);
+    store_digits<S, DB>(dr, 1.0f, 16, base + tiled(j, k, Np), sstride);
+    store_digits<S, DB>(di, -1.0f, 16, base + tiled(j, n + k, Np), sstride);
+    store_digits<S, DB>(di, 1.0f, 16, base + tiled(n + j, k, Np), sstride);
+    store_digits<S, DB>(dr, 1.0f, 16, base + tiled(n + j, n + k, Np), sstride);
   }
 }
 
 // ------------------------------------------------------------------ the GEMM
 struct OzArgs {
   int n, mtiles, ntiles, kblocks, nc, mode;
+  int eoff;             // 32 + 2 (DB - 1): result = acc 2^(sigma_i + tau_j - eoff), acc in 2^-16 units
   const int *sigma;     // [item][M']  row scale exponents of A
   const int *tau;       // [item][n]   column scale exponents of B
   MatRef C, D, E;
@@ -323,8 +325,8 @@ struct OzArgs {
 };
 
 // FP32 accumulator value -> int64 in units of 2^-16 (bit manipulation only).
-// Levels 0..3 hold exact multiples of 2^(16-8l) >= 2^-8; the shared tail
-// level is truncated at 2^-16, 2^-55 below the leading level.
+// Levels 0..3 hold exact multiples of 2^(16-DB l) >= 2^-8; the shared tail
+// level is truncated at 2^-16, about 2^-53 below the leading level.
 __device__ __forceinline__ long long f2fix16(float v) {
   const int b = __float_as_int(v);
   const int ex = (b >> 23) & 0xFF;
@@ -455,7 +457,7 @@ __global__ void __launch_bounds__(128, 1) k_ozaki(const __grid_constant__ CUtens
     const uint32_t lane_addr = tbase + ((uint32_t)(warp * 32) << 16);
     const int kk = item / g.nc, cc = item % g.nc;
     // accumulators carry 2^-30 sigma_i tau_j; the int64 sum is in units of 2^-16
-    const int erow = row < g.n ? g.sigma[(long long)item * (g.mtiles * MT) + row] - 46 : 0;
+    const int erow = row < g.n ? g.sigma[(long long)item * (g.mtiles * MT) + row] - g.eoff : 0;
     for (int c0 = 0; c0 < NT; c0 += 32) {
       float v[NACC][32];
       constexpr int NL = nlevels(S);
@@ -757,7 +759,7 @@ static void oz_dims(int n, int *Mp, int *Np, int *Kp, int *mtiles, int *ntiles, 
   *Kp = *kblocks * KB;
 }
 
-template <int S>
+template <int S, int DB>
 static int zgemm_s(MixedWork *w, int mode, const MatRef &A, const MatRef &B, const MatRef &C,
                    const MatRef &D, const MatRef &E, int n, int nk, int nc, const int *act,
                    cudaStream_t st) {
@@ -785,12 +787,12 @@ static int zgemm_s(MixedWork *w, int mode, const MatRef &A, const MatRef &B, con
   const double split_bytes = (double)active_s * n * n * (16.0 + S * 2.0 * 2.0);
   dim3 ga((n + 31) / 32, items);
   kstat_begin(KS_OTHER, split_bytes, st);
-  k_split_a<S><<<ga, 256, 0, st>>>(A, n, nc, act, (__nv_bfloat16 *)w->sa, Mp, Kp, w->sigma);
+  k_split_a<S, DB><<<ga, 256, 0, st>>>(A, n, nc, act, (__nv_bfloat16 *)w->sa, Mp, Kp, w->sigma);
   kstat_end(st);
   SKKR_LAUNCHED();
   dim3 gb((n + 7) / 8, items);
   kstat_begin(KS_OTHER, 2.0 * split_bytes, st);
-  k_split_b<S><<<gb, 256, 0, st>>>(B, n, nc, act, (__nv_bfloat16 *)w->sb, Np, Kp, w->tau);
+  k_split_b<S, DB><<<gb, 256, 0, st>>>(B, n, nc, act, (__nv_bfloat16 *)w->sb, Np, Kp, w->tau);
   kstat_end(st);
   SKKR_LAUNCHED();
   CUtensorMap ma, mb;
@@ -810,6 +812,7 @@ static int zgemm_s(MixedWork *w, int mode, const MatRef &A, const MatRef &B, con
   g.kblocks = kblocks;
   g.nc = nc;
   g.mode = mode;
+  g.eoff = 32 + 2 * (DB - 1);
   g.sigma = w->sigma;
   g.tau = w->tau;
   g.C = C;
@@ -830,12 +833,24 @@ static int zgemm_s(MixedWork *w, int mode, const MatRef &A, const MatRef &B, con
 int mixed_zgemm(MixedWork *w, int mode, int S, const MatRef &A, const MatRef &B, const MatRef &C,
                 const MatRef &D, const MatRef &E, int n, int nk, int nc, const int *act, cudaStream_t st) {
   if (n < 1 || n > 256 || nk * (long long)nc > 65535) return SKKR_ERR_ARG;
-  switch (S) {
-    case 3: return zgemm_s<3>(w, mode, A, B, C, D, E, n, nk, nc, act, st);
-    case 4: return zgemm_s<4>(w, mode, A, B, C, D, E, n, nk, nc, act, st);
-    case 5: return zgemm_s<5>(w, mode, A, B, C, D, E, n, nk, nc, act, st);
-    case 6: return zgemm_s<6>(w, mode, A, B, C, D, E, n, nk, nc, act, st);
-    case 7: return zgemm_s<7>(w, mode, A, B, C, D, E, n, nk, nc, act, st);
+  if (n <= 128) {  // K = 2n <= 256: 8-bit digits (8 slices would exceed the 62-bit value: use 7)
+    switch (S) {
+      case 3: return zgemm_s<3, 8>(w, mode, A, B, C, D, E, n, nk, nc, act, st);
+      case 4: return zgemm_s<4, 8>(w, mode, A, B, C, D, E, n, nk, nc, act, st);
+      case 5: return zgemm_s<5, 8>(w, mode, A, B, C, D, E, n, nk, nc, act, st);
+      case 6: return zgemm_s<6, 8>(w, mode, A, B, C, D, E, n, nk, nc, act, st);
+      case 7:
+      case 8: return zgemm_s<7, 8>(w, mode, A, B, C, D, E, n, nk, nc, act, st);
+      default: return SKKR_ERR_ARG;
+    }
+  }
+  switch (S) {  // K = 2n > 256: 7-bit digits keep the level sums exact
+    case 3: return zgemm_s<3, 7>(w, mode, A, B, C, D, E, n, nk, nc, act, st);
+    case 4: return zgemm_s<4, 7>(w, mode, A, B, C, D, E, n, nk, nc, act, st);
+    case 5: return zgemm_s<5, 7>(w, mode, A, B, C, D, E, n, nk, nc, act, st);
+    case 6: return zgemm_s<6, 7>(w, mode, A, B, C, D, E, n, nk, nc, act, st);
+    case 7: return zgemm_s<7, 7>(w, mode, A, B, C, D, E, n, nk, nc, act, st);
+    case 8: return zgemm_s<8, 7>(w, mode, A, B, C, D, E, n, nk, nc, act, st);
     default: return SKKR_ERR_ARG;
   }
 }

@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "libskkr_gpu.so")
 
 SKKR_MAX_PRC = 16
-NONREL, REL = 0, 1
+NONREL, REL, BDG = 0, 1, 2
 FP64, MIXED = 0, 1
 ERRORS = {0: "ok", -1: "bad argument", -2: "CUDA error", -3: "decimation hit itermax",
           -4: "decimation diverged (error > 1e10)", -5: "unsupported input", -6: "out of device memory",
@@ -65,6 +65,8 @@ def lib():
         L.skkr_gpu_run.argtypes = [P, P]
         L.skkr_gpu_fetch.argtypes = [P, P, P, P, P, I]
         L.skkr_gpu_cpacoord.argtypes = [P, D, D, D, D, P, I, P, P, P, P, P, P, P, P, P, P, P, P, P, I, P]
+        L.skkr_gpu_cpacoord_bdg.argtypes = [P, D, D, D, D, D, D, P, I, P, P, P, P, P, P, P, P, P, P, P, P, P,
+                                            I, P]
         L.skkr_gpu_phystau.argtypes = [I, I, P, P, P, I]
         L.skkr_gpu_layer_dos.argtypes = [I, I, I, P, I, P, P, I, P, P]
         L.skkr_gpu_set_reduce.argtypes = [P, P, P]
@@ -105,10 +107,11 @@ def _check(rc, where):
 class RTableHolder:
     """Keeps the numpy buffers of an skkr_rtable alive."""
 
-    def __init__(self, rt, blkmap):
+    def __init__(self, rt, blkmap, hole=None):
         self.rstart = np.ascontiguousarray(rt.rstart, np.int32)
         self.rvec = np.ascontiguousarray(rt.rvec, np.float64)
-        self.gR = cm(rt.gR)
+        # BdG: the hole table follows the electron table on the same R vectors
+        self.gR = cm(rt.gR if hole is None else np.concatenate([rt.gR, hole.gR]))
         self.blkmap = np.ascontiguousarray(blkmap, np.int32)
         ns, mi, nj = self.blkmap.shape
         self.s = RTable(rt.nblk, len(self.rvec), _p(self.rstart), _p(self.rvec), _p(self.gR), ns, mi,

@@ -22,14 +22,16 @@ def crand(*s):
 
 
 @pytest.mark.parametrize("n", [18, 54, 128, 256])
-@pytest.mark.parametrize("slices,tol", [(5, 5e-11), (6, 3e-13), (7, 3e-14)])
+@pytest.mark.parametrize("slices,tol", [(5, 5e-11), (6, 3e-13), (7, 3e-14), (8, 3e-14)])
 def test_sliced_zgemm_is_fp64_accurate(n, slices, tol):
-    # S slices: about 2^(-8S) sigma tau per term, random-walk summed over K = 2n
+    # S slices: about 2^(-8S) sigma tau per term, random-walk summed over K = 2n;
+    # n <= 128 runs 8-bit digits (8 slices act as 7), n > 128 7-bit digits
+    # (2^(-7S)) so that the FP32 level sums over K = 512 stay exact
     a, b = crand(3, n, n), crand(3, n, n)
     c = native.zgemm_batch(a, b, precision="mixed", slices=slices)
     ref = a @ b
-    if n == 256 and slices > 5:
-        tol = 3e-12  # K = 512: level-2 sums exceed FP32's 24 bits by a bit
+    if n == 256:
+        tol = {5: 2e-9, 6: 3e-11, 7: 5e-13, 8: 3e-14}[slices]
     for i in range(3):
         assert rel(c[i], ref[i]) < tol, rel(c[i], ref[i])
 
