@@ -65,9 +65,10 @@ typedef struct {
   double cpatol;                  /* CPA tolerance on error3 (rsp-scf/fullcpa.f:142) */
   int precision;                  /* skkr_precision */
   int nk_chunk;                   /* k points per device batch (0: automatic) */
-  int slices;                     /* SKKR_MIXED: BF16 slices per product operand, 3..8 (0: 6;
-                                     8 for SKKR_BDG, whose e-h block is ~1e-2 of the rest).  Digits
-                                     are 8-bit for n_PL <= 128 (8 slices act as 7), 7-bit above */
+  int slices;                     /* SKKR_MIXED: BF16 slices per product operand, 3..8 (0: 6).
+                                     Digits are 8-bit for a product depth K <= 128 (8 slices act
+                                     as 7), 7-bit above.  SKKR_BDG splits every product into its
+                                     electron and hole K halves, each with its own scales */
 } skkr_sizes;
 
 /* Real-space screened structure constants of one energy, grouped in

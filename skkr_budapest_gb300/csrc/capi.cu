@@ -262,12 +262,7 @@ extern "C" int skkr_gpu_create(const skkr_sizes *sizes, skkr_ctx **out) {
   c->nprc = s.nprc;
   c->nintfc = c->pl * s.nprc;
   c->ngeff = s.ngeff;
-  if (s.slices == 0 && s.mode == SKKR_BDG) {
-    // the anomalous block is ~1e-2 of the row scales the slicing is set by;
-    // n_PL > 128 runs 7-bit digits: 7 slices
-    c->slices = 7;
-    c->slices_res = 8;
-  } else if (s.slices != 0) {
+  if (s.slices != 0) {
     if (s.slices < 3 || s.slices > 8) {
       delete c;
       return SKKR_ERR_ARG;
@@ -599,8 +594,35 @@ static int check_slot_quirk(const skkr_ctx *c) {
 // ---------------------------------------------------------------------------
 // engine: the dense operations of decimation and tau2d in FP64 or split
 // precision (tcgen05 sliced products, FP32 inverse + Newton refinement)
+// electron-first principal-layer layout: BdG on the split-precision path
+static int ehsplit(const skkr_ctx *c) {
+  return c->sz.mode == SKKR_BDG && c->sz.precision == SKKR_MIXED;
+}
+
+static MatRef offset(const MatRef &m, long long elems) {
+  MatRef r = m;
+  r.base += elems;
+  return r;
+}
+
 static int eng_gemm(skkr_ctx *c, bool mixed, int mode, const MatRef &A, const MatRef &B, const MatRef &C,
                     const MatRef &D, const MatRef &E, int n, int nk, int nc, const int *act) {
+  if (mixed && ehsplit(c)) {
+    // BdG: A B = A[:, e] B[e, :] + A[:, h] B[h, :] over the electron and hole
+    // K halves of the electron-first layout, each half with its own operand
+    // scales (the O(delta) e-h blocks keep their full relative precision)
+    const int h = n / 2;
+    const MatRef A2 = offset(A, (long long)h * A.ld), B2 = offset(B, h);
+    int m2;
+    switch (mode) {
+      case 0: m2 = 5; break;   // C = A1 B1, then C += A2 B2
+      case 4: m2 = 1; break;   // C = I - A1 B1, then C -= A2 B2
+      default: m2 = mode;      // 1 (C -=), 2 (D -=, E -=), 5 (C +=) are additive per half
+    }
+    int rc = mixed_zgemm_k(c->mw, mode, c->slices, A, B, C, D, E, n, h, nk, nc, act, c->st);
+    if (rc) return rc;
+    return mixed_zgemm_k(c->mw, m2, c->slices, A2, B2, C, D, E, n, h, nk, nc, act, c->st);
+  }
   if (mixed) return mixed_zgemm(c->mw, mode, c->slices, A, B, C, D, E, n, nk, nc, act, c->st);
   launch_zgemm(mode, A, B, C, D, E, n, n, n, nk, nc, act, c->st);
   return SKKR_OK;
@@ -668,7 +690,7 @@ static int run_decimation(skkr_ctx *c, int k0, int nkc, const std::vector<int> &
   MatRef eps = buf(0), a0 = buf(1), a1 = buf(2), b0 = buf(3), b1 = buf(4), x = buf(5), y1 = buf(6),
          P = buf(7), Q = buf(8);
   // init: eps = m0 + t ; x = eps ; alfa = -ml ; beta = -mr   (surfgf.f:37-45)
-  launch_add_tblocks(eps, Pm0, Tt, lk, pl, n, nkc, nc, nullptr, st);
+  launch_add_tblocks(eps, Pm0, Tt, lk, pl, n, nkc, nc, nullptr, ehsplit(c), st);
   launch_zaxpby(x, eps, nullptr, 0, nullptr, 0, n, nkc, nc, nullptr, st);
   // ml + (-2) ml is exactly -ml in floating point
   launch_zaxpby(a0, Pml, &Pml, -2.0, nullptr, 0, n, nkc, nc, nullptr, st);
@@ -783,7 +805,7 @@ static int run_tau2d(skkr_ctx *c, int k0, int nkc, const std::vector<int> &icls)
     int tm2[SKKR_MAPN];
     for (int s = 0; s < nc; s++) tm2[s] = tmap[s] + p * pl;
     MatRef Tt = mref_map(c->trot.as<zd>(), 0, lk2, lk, tm2, nc);
-    launch_add_tblocks(T00(p), M00, Tt, lk, pl, n, nkc, nc, nullptr, st);
+    launch_add_tblocks(T00(p), M00, Tt, lk, pl, n, nkc, nc, nullptr, ehsplit(c), st);
     if (p == 0) {
       launch_zaxpby(YY(0), Ys, nullptr, 0, nullptr, 0, n, nkc, nc, nullptr, st);
     } else {
@@ -816,7 +838,7 @@ static int run_tau2d(skkr_ctx *c, int k0, int nkc, const std::vector<int> &icls)
     launch_zaxpby(Wm, T00(p), &xx, -1.0, &yy, -1.0, n, nkc, nc, nullptr, st);
     CKR(eng_inv(c, mx, Wm, Wm, true, n, nkc, nc, nullptr));
     launch_extract_tau(Wm, lk, pl, p * pl, c->wk.as<double>() + k0, 1.0 / c->ngeff, c->tauk.as<zd>(),
-                       (long long)nc * ni * lk2, (long long)ni * lk2, nkc, nc, st);
+                       (long long)nc * ni * lk2, (long long)ni * lk2, nkc, nc, ehsplit(c), st);
   }
   return SKKR_OK;
 }
@@ -1030,7 +1052,7 @@ extern "C" int skkr_gpu_run(skkr_ctx *c, skkr_status *status) {
       const int nkc = std::min(c->kc, nk - k0);
       launch_pack(c->G.as<zd>() + (size_t)k0 * c->nbk * bs, c->nblk, c->nbk, c->blkmap_d.as<int>(),
                   c->mi, c->jmax, c->jobs.as<PackJob>(), c->nmat, lk, c->lmmax, c->sz.mode, c->fac,
-                  c->fach, nkc, c->pool.as<zd>(), c->nmat, n, st);
+                  c->fach, nkc, c->pool.as<zd>(), c->nmat, n, ehsplit(c), st);
       if (itcpa == 1) CKR(run_decimation(c, k0, nkc, lcls, rcls));
       if (c->err_code) break;
       CKR(run_tau2d(c, k0, nkc, icls));

@@ -15,7 +15,7 @@ struct PackJob {
 cudaError_t pack_set_tables(int irel, int lmax);
 void launch_pack(const zd *G, int nblk, int nbk, const int *d_blkmap, int mi, int jmax,
                  const PackJob *d_jobs, int njobs, int lk, int lmmax, int mode, zd fac, zd fach, int nk,
-                 zd *pool, int nmat, int npl, cudaStream_t st);
+                 zd *pool, int nmat, int npl, int ehsplit, cudaStream_t st);
 
 // batched complex GEMM, items (k, c) with k < nk, c < nc; act[k*nc+c]==0 skips.
 // mode 0: C = A*B        1: C = C - A*B
@@ -31,9 +31,10 @@ void launch_zgj(const MatRef &A, int n, int nk, int nc, const int *act, cudaStre
 // elementwise: out = a + s1*b + s2*d over n x n (b/d may be null)
 void launch_zaxpby(const MatRef &out, const MatRef &a, const MatRef *b, double s1, const MatRef *d,
                    double s2, int n, int nk, int nc, const int *act, cudaStream_t st);
-// out = in + block-diagonal t (nl layers of lk x lk, t base from tref for item)
+// out = in + block-diagonal t (nl layers of lk x lk, t base from tref for item);
+// ehsplit: principal-layer matrices in the electron-first BdG layout
 void launch_add_tblocks(const MatRef &out, const MatRef &in, const MatRef &t, int lk, int nl,
-                        int n, int nk, int nc, const int *act, cudaStream_t st);
+                        int n, int nk, int nc, const int *act, int ehsplit, cudaStream_t st);
 // Frobenius norms of items -> out[k*nc+c]
 void launch_fnorm(const MatRef &a, int n, int nk, int nc, const int *act, double *out,
                   cudaStream_t st);
@@ -43,7 +44,7 @@ void launch_dec_state(const double *err, int *act, int *stat, int *iters, int ni
 // tau(k) diagonal-block extraction: out[k][c][layer] = (wk[k]*wscale) * W(layer block)
 void launch_extract_tau(const MatRef &W, int lk, int nl, int layer0, const double *wk,
                         double wscale, zd *out, long long out_sk, long long out_sc, int nk,
-                        int nc, cudaStream_t st);
+                        int nc, int ehsplit, cudaStream_t st);
 // deterministic k-sum (warp-shuffle): S[e] (+)= sum_k tk[k*E + e]
 void launch_ksum(const zd *tk, int nk, long long E, zd *S, int accumulate, cudaStream_t st);
 // sum over g of T[layer][g] -> out[layer]
@@ -60,6 +61,11 @@ MixedWork *mixed_create();
 void mixed_destroy(MixedWork *w);
 int mixed_error_flag(MixedWork *w);
 // modes as launch_zgemm plus 4: C = I - A*B, 5: C = C + A*B; S = slices (3..7)
+// C (op) A[:, 0:K] B[0:K, :] for n x K by K x n blocks (A, B already offset
+// to the K range): the operand scales cover these K columns / rows only
+int mixed_zgemm_k(MixedWork *w, int mode, int S, const MatRef &A, const MatRef &B, const MatRef &C,
+                  const MatRef &D, const MatRef &E, int n, int K, int nk, int nc, const int *act,
+                  cudaStream_t st);
 int mixed_zgemm(MixedWork *w, int mode, int S, const MatRef &A, const MatRef &B, const MatRef &C,
                 const MatRef &D, const MatRef &E, int n, int nk, int nc, const int *act, cudaStream_t st);
 int mixed_zinv(MixedWork *w, const MatRef &A, const MatRef &X, int n, int nk, int nc, const int *act,

@@ -95,6 +95,28 @@ cudaError_t pack_set_tables(int irel, int lmax) {
   return e;
 }
 
+// Row of component k (0..lk-1) of site i in a principal-layer matrix of nl
+// sites: site-major i lk + k, or with ehsplit (BdG on the split-precision
+// path) electron-first -- every site's electron half, then every site's hole
+// half -- so that the two K halves of a product carry their own operand
+// scales.  The two layouts are a permutation similarity of each other.
+__device__ __forceinline__ int pl_row(int i, int k, int lk, int nl, int ehsplit) {
+  if (!ehsplit) return i * lk + k;
+  const int km = lk >> 1;
+  return k < km ? i * km + k : nl * km + i * km + (k - km);
+}
+__device__ __forceinline__ void pl_site(int r, int lk, int nl, int ehsplit, int &i, int &k) {
+  if (!ehsplit) {
+    i = r / lk;
+    k = r % lk;
+    return;
+  }
+  const int km = lk >> 1, half = nl * km;
+  const int h = r >= half, rr = h ? r - half : r;
+  i = rr / km;
+  k = rr % km + (h ? km : 0);
+}
+
 // mode 0: lm, 1: (kappa,mu), 2: BdG -- blockdiag of the electron block b
 // (fac) and the hole block b + nblk (fach), each mapped to (kappa,mu)
 // (skkr_dbogo_bsf main/g2d_pack.f + main/relmtrx.f).  nbk: blocks per k.
@@ -102,7 +124,7 @@ __global__ void __launch_bounds__(256) k_pack(const zd *__restrict__ G, int nblk
                                               const int *__restrict__ blkmap, int mi, int jmax,
                                               const PackJob *__restrict__ jobs, int lk, int lmmax,
                                               int mode, zd fac, zd fach, zd *__restrict__ pool,
-                                              int nmat, int npl) {
+                                              int nmat, int npl, int ehsplit) {
   const int kk = blockIdx.y;
   const PackJob jb = jobs[blockIdx.z];
   const int nrow = jb.ni * lk;
@@ -115,8 +137,11 @@ __global__ void __launch_bounds__(256) k_pack(const zd *__restrict__ G, int nblk
     const int r = e % npl, c = e / npl;
     zd v = make_double2(0.0, 0.0);
     if (r < nrow && c < ncol) {
-      const int i = r / lk + 1, k1 = r % lk;
-      const int jp = c / lk + 1, k2 = c % lk;
+      int i, k1, jp, k2;
+      pl_site(r, lk, jb.ni, ehsplit, i, k1);
+      pl_site(c, lk, ncol / lk, ehsplit, jp, k2);
+      i++;
+      jp++;
       int j;
       bool inrange;
       if (jb.which == 0) {
@@ -167,12 +192,12 @@ __global__ void __launch_bounds__(256) k_pack(const zd *__restrict__ G, int nblk
 
 void launch_pack(const zd *G, int nblk, int nbk, const int *d_blkmap, int mi, int jmax,
                  const PackJob *d_jobs, int njobs, int lk, int lmmax, int mode, zd fac, zd fach, int nk,
-                 zd *pool, int nmat, int npl, cudaStream_t st) {
+                 zd *pool, int nmat, int npl, int ehsplit, cudaStream_t st) {
   if (nk <= 0 || njobs <= 0) return;
   int per = (npl * npl + 255) / 256;
   dim3 grid(per < 64 ? per : 64, nk, njobs);
   k_pack<<<grid, 256, 0, st>>>(G, nblk, nbk, d_blkmap, mi, jmax, d_jobs, lk, lmmax, mode, fac, fach,
-                               pool, nmat, npl);
+                               pool, nmat, npl, ehsplit);
   SKKR_LAUNCHED();
 }
 
@@ -394,7 +419,7 @@ void launch_zaxpby(const MatRef &out, const MatRef &a, const MatRef *b, double s
 }
 
 __global__ void k_add_tblocks(MatRef O, MatRef In, MatRef T, int lk, int nl, int n, int nc,
-                              const int *__restrict__ act) {
+                              const int *__restrict__ act, int ehsplit) {
   const int item = blockIdx.y;
   const int kk = item / nc, cc = item % nc;
   if (act && !act[item]) return;
@@ -405,10 +430,12 @@ __global__ void k_add_tblocks(MatRef O, MatRef In, MatRef T, int lk, int nl, int
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += gridDim.x * blockDim.x) {
     const int r = e % n, c = e / n;
     zd v = in[r + (long long)c * In.ld];
-    const int lr = r / lk, lc = c / lk;
+    int lr, kr, lc, kc;
+    pl_site(r, lk, nl, ehsplit, lr, kr);
+    pl_site(c, lk, nl, ehsplit, lc, kc);
     if (lr == lc && lr < nl) {
       // tau2d.f:72-78 / dugo.f:82-89: m00 = tminv + m00
-      zd tv = t[(long long)lr * lk * lk + (r % lk) + (c % lk) * lk];
+      zd tv = t[(long long)lr * lk * lk + kr + kc * lk];
       v = zadd(tv, v);
     }
     o[r + (long long)c * O.ld] = v;
@@ -416,11 +443,11 @@ __global__ void k_add_tblocks(MatRef O, MatRef In, MatRef T, int lk, int nl, int
 }
 
 void launch_add_tblocks(const MatRef &out, const MatRef &in, const MatRef &t, int lk, int nl,
-                        int n, int nk, int nc, const int *act, cudaStream_t st) {
+                        int n, int nk, int nc, const int *act, int ehsplit, cudaStream_t st) {
   if (nk <= 0 || nc <= 0) return;
   int per = (n * n + 255) / 256;
   dim3 grid(per < 32 ? per : 32, nk * nc);
-  k_add_tblocks<<<grid, 256, 0, st>>>(out, in, t, lk, nl, n, nc, act);
+  k_add_tblocks<<<grid, 256, 0, st>>>(out, in, t, lk, nl, n, nc, act, ehsplit);
   SKKR_LAUNCHED();
 }
 
@@ -487,7 +514,7 @@ void launch_dec_state(const double *err, int *act, int *stat, int *iters, int ni
 
 // tau2d.f:137-147: tau(l,lp,ilay) = wgeff * tau00(il0+l, il0+lp)
 __global__ void k_extract_tau(MatRef W, int lk, int nl, int layer0, const double *wk, double wscale,
-                              zd *out, long long out_sk, long long out_sc, int nc) {
+                              zd *out, long long out_sk, long long out_sc, int nc, int ehsplit) {
   const int item = blockIdx.y;
   const int kk = item / nc, cc = item % nc;
   const zd *w = mat_ptr(W, kk, cc);
@@ -497,18 +524,18 @@ __global__ void k_extract_tau(MatRef W, int lk, int nl, int layer0, const double
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += gridDim.x * blockDim.x) {
     const int l = e / (lk * lk), rem = e % (lk * lk);
     const int r = rem % lk, c = rem / lk;
-    zd v = w[(l * lk + r) + (long long)(l * lk + c) * W.ld];
+    zd v = w[pl_row(l, r, lk, nl, ehsplit) + (long long)pl_row(l, c, lk, nl, ehsplit) * W.ld];
     o[e] = zscale(wg, v);
   }
 }
 
 void launch_extract_tau(const MatRef &W, int lk, int nl, int layer0, const double *wk,
                         double wscale, zd *out, long long out_sk, long long out_sc, int nk,
-                        int nc, cudaStream_t st) {
+                        int nc, int ehsplit, cudaStream_t st) {
   if (nk <= 0 || nc <= 0) return;
   int per = (nl * lk * lk + 255) / 256;
   dim3 grid(per < 16 ? per : 16, nk * nc);
-  k_extract_tau<<<grid, 256, 0, st>>>(W, lk, nl, layer0, wk, wscale, out, out_sk, out_sc, nc);
+  k_extract_tau<<<grid, 256, 0, st>>>(W, lk, nl, layer0, wk, wscale, out, out_sk, out_sc, nc, ehsplit);
   SKKR_LAUNCHED();
 }
 

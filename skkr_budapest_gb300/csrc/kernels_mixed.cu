@@ -223,8 +223,10 @@ __device__ __forceinline__ long long tiled(int r, int kk, int rows) {
   return ((long long)(kk >> 5) * rows + r) * 32 + (kk & 31);
 }
 
+// A' = [Re A, Im A] (n x 2K) from the n x K complex A; rows scaled by their
+// max over these K columns
 template <int S, int DB>
-__global__ void __launch_bounds__(256) k_split_a(MatRef A, int n, int nc, const int *__restrict__ act,
+__global__ void __launch_bounds__(256) k_split_a(MatRef A, int n, int K, int nc, const int *__restrict__ act,
                                                  __nv_bfloat16 *__restrict__ out, int Mp, int Kp,
                                                  int *__restrict__ sigma) {
   const int item = blockIdx.y, kk0 = item / nc, cc = item % nc;
@@ -237,7 +239,7 @@ __global__ void __launch_bounds__(256) k_split_a(MatRef A, int n, int nc, const 
   unsigned long long m = 0;
   const int row = r0 + lane;
   if (row < n)
-    for (int k = w; k < n; k += 8) {
+    for (int k = w; k < K; k += 8) {
       zd v = a[row + (long long)k * A.ld];
       const unsigned long long bx = abs_bits(v.x), by = abs_bits(v.y);
       m = bx > m ? bx : m;
@@ -255,29 +257,30 @@ __global__ void __launch_bounds__(256) k_split_a(MatRef A, int n, int nc, const 
   __syncthreads();
   const long long sstride = (long long)Mp * Kp;
   __nv_bfloat16 *base = out + (long long)item * S * sstride;
-  for (int c0 = 0; c0 < n; c0 += 32) {
+  for (int c0 = 0; c0 < K; c0 += 32) {
     for (int q = w; q < 32; q += 8) {
       int col = c0 + q;
-      T[lane][q] = (row < n && col < n) ? a[row + (long long)col * A.ld] : make_double2(0.0, 0.0);
+      T[lane][q] = (row < n && col < K) ? a[row + (long long)col * A.ld] : make_double2(0.0, 0.0);
     }
     __syncthreads();
     for (int q = w; q < 32; q += 8) {
       const int r = r0 + q, col = c0 + lane;
-      if (r < n && col < n) {
+      if (r < n && col < K) {
         const int es = sc[q];
         zd v = T[q][lane];
         slice_store<S, DB>(v.x, es, 0, base + tiled(r, col, Mp), sstride);
-        slice_store<S, DB>(v.y, es, 0, base + tiled(r, n + col, Mp), sstride);
+        slice_store<S, DB>(v.y, es, 0, base + tiled(r, K + col, Mp), sstride);
       }
     }
     __syncthreads();
   }
 }
 
-// B'^T from complex B (n x n, MatRef): one warp per column j; rows j and n+j
-// of B'^T are [Re B(:,j), -Im B(:,j)] and [Im B(:,j), Re B(:,j)].
+// B'^T from the K x n complex B: one warp per column j; rows j and n+j of
+// B'^T are [Re B(:,j), -Im B(:,j)] and [Im B(:,j), Re B(:,j)] (columns scaled
+// by their max over these K rows)
 template <int S, int DB>
-__global__ void __launch_bounds__(256) k_split_b(MatRef B, int n, int nc, const int *__restrict__ act,
+__global__ void __launch_bounds__(256) k_split_b(MatRef B, int n, int K, int nc, const int *__restrict__ act,
                                                  __nv_bfloat16 *__restrict__ out, int Np, int Kp,
                                                  int *__restrict__ tau) {
   const int item = blockIdx.y, kk0 = item / nc, cc = item % nc;
@@ -286,7 +289,7 @@ __global__ void __launch_bounds__(256) k_split_b(MatRef B, int n, int nc, const 
   if (j >= n) return;
   const zd *b = mat_ptr(B, kk0, cc) + (long long)j * B.ld;
   unsigned long long m = 0;
-  for (int k = lane; k < n; k += 32) {
+  for (int k = lane; k < K; k += 32) {
     zd v = b[k];
     const unsigned long long bx = abs_bits(v.x), by = abs_bits(v.y);
     m = bx > m ? bx : m;
@@ -301,15 +304,15 @@ __global__ void __launch_bounds__(256) k_split_b(MatRef B, int n, int nc, const 
   if (lane == 0) tau[(long long)item * n + j] = es;
   const long long sstride = (long long)Np * Kp;
   __nv_bfloat16 *base = out + (long long)item * S * sstride;
-  for (int k = lane; k < n; k += 32) {
+  for (int k = lane; k < K; k += 32) {
     zd v = b[k];
     float dr[S], di[S];
     slice_digits<S, DB>(v.x, es, dr);
     slice_digits<S, DB>(v.y, es, di);
     store_digits<S, DB>(dr, 1.0f, 16, base + tiled(j, k, Np), sstride);
-    store_digits<S, DB>(di, -1.0f, 16, base + tiled(j, n + k, Np), sstride);
+    store_digits<S, DB>(di, -1.0f, 16, base + tiled(j, K + k, Np), sstride);
     store_digits<S, DB>(di, 1.0f, 16, base + tiled(n + j, k, Np), sstride);
-    store_digits<S, DB>(dr, 1.0f, 16, base + tiled(n + j, n + k, Np), sstride);
+    store_digits<S, DB>(dr, 1.0f, 16, base + tiled(n + j, K + k, Np), sstride);
   }
 }
 
@@ -711,7 +714,7 @@ struct MixedWork {
   size_t rn_cap = 0;
   int *err = nullptr;
   int smem_set[16] = {0};
-  int last_n = -1;   // staging layout the zero padding was made for
+  int last_n = -1, last_k = -1;   // staging layout the zero padding was made for
 };
 
 static int grow(void **p, size_t *cap, size_t bytes, bool zero) {
@@ -749,50 +752,51 @@ int mixed_error_flag(MixedWork *w) {
   return h;
 }
 
-// dims of the staged real problem for complex n
-static void oz_dims(int n, int *Mp, int *Np, int *Kp, int *mtiles, int *ntiles, int *kblocks) {
+// dims of the staged real problem for complex n x K times K x n
+static void oz_dims(int n, int K, int *Mp, int *Np, int *Kp, int *mtiles, int *ntiles, int *kblocks) {
   *mtiles = (n + MT - 1) / MT;
   *Mp = *mtiles * MT;
   *ntiles = (2 * n + NT - 1) / NT;
   *Np = *ntiles * NT;
-  *kblocks = (2 * n + KB - 1) / KB;
+  *kblocks = (2 * K + KB - 1) / KB;
   *Kp = *kblocks * KB;
 }
 
 template <int S, int DB>
 static int zgemm_s(MixedWork *w, int mode, const MatRef &A, const MatRef &B, const MatRef &C,
-                   const MatRef &D, const MatRef &E, int n, int nk, int nc, const int *act,
+                   const MatRef &D, const MatRef &E, int n, int K, int nk, int nc, const int *act,
                    cudaStream_t st) {
   if (get_encoder()) return SKKR_ERR_CUDA;
   int Mp, Np, Kp, mtiles, ntiles, kblocks;
-  oz_dims(n, &Mp, &Np, &Kp, &mtiles, &ntiles, &kblocks);
+  oz_dims(n, K, &Mp, &Np, &Kp, &mtiles, &ntiles, &kblocks);
   const long long items = (long long)nk * nc;
   int rc;
   // staging sized for S slices; the zero padding is redone when the layout changes
   if ((rc = grow(&w->sa, &w->sa_cap, (size_t)items * S * Mp * Kp * 2, true))) return rc;
   if ((rc = grow(&w->sb, &w->sb_cap, (size_t)items * S * Np * Kp * 2, true))) return rc;
-  if (w->last_n != n) {
-    // padding (row >= n, column >= 2n of every slice region) must be zero;
-    // the region layout depends on n only, so a new n clears what an earlier
-    // layout wrote there
+  if (w->last_n != n || w->last_k != K) {
+    // padding (row >= n, column >= 2K of every slice region) must be zero;
+    // the region layout depends on n and K only, so a new layout clears what
+    // an earlier one wrote there
     if (cudaMemsetAsync(w->sa, 0, w->sa_cap, st) != cudaSuccess ||
         cudaMemsetAsync(w->sb, 0, w->sb_cap, st) != cudaSuccess)
       return SKKR_ERR_CUDA;
     w->last_n = n;
+    w->last_k = K;
   }
   if ((rc = grow((void **)&w->sigma, &w->sig_cap, (size_t)items * Mp * sizeof(int), false))) return rc;
   if ((rc = grow((void **)&w->tau, &w->tau_cap, (size_t)items * n * sizeof(int), false))) return rc;
   const long long active_s = act ? skkr_active_items(items) : items;
   // split traffic: FP64 operand read + S bf16 slices of the real embedding written
-  const double split_bytes = (double)active_s * n * n * (16.0 + S * 2.0 * 2.0);
+  const double split_bytes = (double)active_s * n * K * (16.0 + S * 2.0 * 2.0);
   dim3 ga((n + 31) / 32, items);
   kstat_begin(KS_OTHER, split_bytes, st);
-  k_split_a<S, DB><<<ga, 256, 0, st>>>(A, n, nc, act, (__nv_bfloat16 *)w->sa, Mp, Kp, w->sigma);
+  k_split_a<S, DB><<<ga, 256, 0, st>>>(A, n, K, nc, act, (__nv_bfloat16 *)w->sa, Mp, Kp, w->sigma);
   kstat_end(st);
   SKKR_LAUNCHED();
   dim3 gb((n + 7) / 8, items);
   kstat_begin(KS_OTHER, 2.0 * split_bytes, st);
-  k_split_b<S, DB><<<gb, 256, 0, st>>>(B, n, nc, act, (__nv_bfloat16 *)w->sb, Np, Kp, w->tau);
+  k_split_b<S, DB><<<gb, 256, 0, st>>>(B, n, K, nc, act, (__nv_bfloat16 *)w->sb, Np, Kp, w->tau);
   kstat_end(st);
   SKKR_LAUNCHED();
   CUtensorMap ma, mb;
@@ -822,37 +826,43 @@ static int zgemm_s(MixedWork *w, int mode, const MatRef &A, const MatRef &B, con
   g.err = w->err;
   dim3 grid(mtiles * ntiles, items);
   const long long active = act ? skkr_active_items(items) : items;
-  // algorithmic BF16 tensor work: S(S+1)/2 real products of n x 2n x 2n per item
-  kstat_begin(KS_OZAKI, (double)(S * (S + 1) / 2) * 8.0 * n * (double)n * n * (double)active, st);
+  // algorithmic BF16 tensor work: S(S+1)/2 real products of n x 2K x 2n per item
+  kstat_begin(KS_OZAKI, (double)(S * (S + 1) / 2) * 8.0 * n * (double)n * K * (double)active, st);
   k_ozaki<S><<<grid, 128, smem, st>>>(ma, mb, g);
   kstat_end(st);
   SKKR_LAUNCHED();
   return 0;
 }
 
-int mixed_zgemm(MixedWork *w, int mode, int S, const MatRef &A, const MatRef &B, const MatRef &C,
-                const MatRef &D, const MatRef &E, int n, int nk, int nc, const int *act, cudaStream_t st) {
-  if (n < 1 || n > 256 || nk * (long long)nc > 65535) return SKKR_ERR_ARG;
-  if (n <= 128) {  // K = 2n <= 256: 8-bit digits (8 slices would exceed the 62-bit value: use 7)
+int mixed_zgemm_k(MixedWork *w, int mode, int S, const MatRef &A, const MatRef &B, const MatRef &C,
+                  const MatRef &D, const MatRef &E, int n, int K, int nk, int nc, const int *act,
+                  cudaStream_t st) {
+  if (n < 1 || n > 256 || K < 1 || K > 256 || nk * (long long)nc > 65535) return SKKR_ERR_ARG;
+  if (K <= 128) {  // 2K <= 256: 8-bit digits (8 slices would exceed the 62-bit value: use 7)
     switch (S) {
-      case 3: return zgemm_s<3, 8>(w, mode, A, B, C, D, E, n, nk, nc, act, st);
-      case 4: return zgemm_s<4, 8>(w, mode, A, B, C, D, E, n, nk, nc, act, st);
-      case 5: return zgemm_s<5, 8>(w, mode, A, B, C, D, E, n, nk, nc, act, st);
-      case 6: return zgemm_s<6, 8>(w, mode, A, B, C, D, E, n, nk, nc, act, st);
+      case 3: return zgemm_s<3, 8>(w, mode, A, B, C, D, E, n, K, nk, nc, act, st);
+      case 4: return zgemm_s<4, 8>(w, mode, A, B, C, D, E, n, K, nk, nc, act, st);
+      case 5: return zgemm_s<5, 8>(w, mode, A, B, C, D, E, n, K, nk, nc, act, st);
+      case 6: return zgemm_s<6, 8>(w, mode, A, B, C, D, E, n, K, nk, nc, act, st);
       case 7:
-      case 8: return zgemm_s<7, 8>(w, mode, A, B, C, D, E, n, nk, nc, act, st);
+      case 8: return zgemm_s<7, 8>(w, mode, A, B, C, D, E, n, K, nk, nc, act, st);
       default: return SKKR_ERR_ARG;
     }
   }
-  switch (S) {  // K = 2n > 256: 7-bit digits keep the level sums exact
-    case 3: return zgemm_s<3, 7>(w, mode, A, B, C, D, E, n, nk, nc, act, st);
-    case 4: return zgemm_s<4, 7>(w, mode, A, B, C, D, E, n, nk, nc, act, st);
-    case 5: return zgemm_s<5, 7>(w, mode, A, B, C, D, E, n, nk, nc, act, st);
-    case 6: return zgemm_s<6, 7>(w, mode, A, B, C, D, E, n, nk, nc, act, st);
-    case 7: return zgemm_s<7, 7>(w, mode, A, B, C, D, E, n, nk, nc, act, st);
-    case 8: return zgemm_s<8, 7>(w, mode, A, B, C, D, E, n, nk, nc, act, st);
+  switch (S) {  // 2K > 256: 7-bit digits keep the level sums exact
+    case 3: return zgemm_s<3, 7>(w, mode, A, B, C, D, E, n, K, nk, nc, act, st);
+    case 4: return zgemm_s<4, 7>(w, mode, A, B, C, D, E, n, K, nk, nc, act, st);
+    case 5: return zgemm_s<5, 7>(w, mode, A, B, C, D, E, n, K, nk, nc, act, st);
+    case 6: return zgemm_s<6, 7>(w, mode, A, B, C, D, E, n, K, nk, nc, act, st);
+    case 7: return zgemm_s<7, 7>(w, mode, A, B, C, D, E, n, K, nk, nc, act, st);
+    case 8: return zgemm_s<8, 7>(w, mode, A, B, C, D, E, n, K, nk, nc, act, st);
     default: return SKKR_ERR_ARG;
   }
+}
+
+int mixed_zgemm(MixedWork *w, int mode, int S, const MatRef &A, const MatRef &B, const MatRef &C,
+                const MatRef &D, const MatRef &E, int n, int nk, int nc, const int *act, cudaStream_t st) {
+  return mixed_zgemm_k(w, mode, S, A, B, C, D, E, n, n, nk, nc, act, st);
 }
 
 // X = A^-1: FP32 Gauss-Jordan, then `newton` steps X += X (I - A X) with the

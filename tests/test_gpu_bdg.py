@@ -1,7 +1,9 @@
 """BdG path (skkr_dbogo_bsf layout, SKKR_BDG) on the GPU against the oracle:
 the full k-summed tau and its electron-hole (anomalous) block at <= 1e-10 on
 the FP64 path, at the C5 size (lmax=3, n_s=64, PL4: n_PL=256, Im E=1e-4) and
-on a small lmax=1 stack; the split-precision path against FP64 at <= 1e-9."""
+on a small lmax=1 stack; the split-precision path (electron-first layout,
+products split into electron and hole K halves) against FP64 at <= 1e-9 on
+the full tau and on the anomalous block alone."""
 import numpy as np
 import pytest
 
@@ -38,15 +40,16 @@ def test_bdg_c5_size(ie):
     _check(api.cpacoord(ep), O.cpacoord(ep, nthreads=16), ep.lkmax // 2)
 
 
-@pytest.mark.parametrize("ie", [10, 50])
-def test_bdg_mixed_against_fp64(ie):
-    # Im E = 5e-3 >= 1e-3: decimation runs on the split-precision engine too
-    ep = W.energy_problem(W.bdg_bcc(im_e=5e-3), ie, nset=2)
+@pytest.mark.parametrize("ie,im_e", [(10, 5e-3), (50, 5e-3), (10, 5e-4)])
+def test_bdg_mixed_against_fp64(ie, im_e):
+    # Im E >= 1e-3: decimation runs on the split-precision engine too;
+    # closer to the axis it stays in FP64 and only tau2d is split precision
+    ep = W.energy_problem(W.bdg_bcc(im_e=im_e), ie, nset=2)
     a = api.cpacoord(ep)
     b = api.cpacoord(ep, precision="mixed")
     km = ep.lkmax // 2
     assert rel(b["tauc"], a["tauc"]) < 1e-9
-    assert rel(b["tauc"][:, :km, km:], a["tauc"][:, :km, km:]) < 3e-8
+    assert rel(b["tauc"][:, :km, km:], a["tauc"][:, :km, km:]) < 1e-9
 
 
 def test_bdg_phystau():
