@@ -54,6 +54,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", action="store_true",
                     help="only the device loop of the timed steps (for ncu captures); prints a short line")
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3"],
+                    help="c3: one energy of each of three systems per step through skkr_gpu_cpacoord_many")
     return ap.parse_args()
 
 
@@ -390,8 +392,56 @@ def run_ours(args, rank, ws):
         print(json.dumps(line), flush=True)
 
 
+def run_c3(args):
+    """Three interfaces in one call per step (relativistic PL4 lmax=3,
+    non-relativistic PL2 lmax=2, relativistic PL3 lmax=2), host buffers in and
+    out, against the same calls made one after the other."""
+    import torch
+    from skkr_budapest_gb300 import api
+    from skkr_budapest_gb300 import workloads as W
+    specs = [W.rel_bcc(), W.nonrel_pl2(), W.rel_pl3_l2()]
+    plan = [[12, 16, 4, 14, 8], [12, 14, 6, 10, 3], [14, 17, 8, 12, 4]]
+    eps = [[W.energy_problem(sp, ie) for ie in pl] for sp, pl in zip(specs, plan)]
+    ctxs = [api.Context.for_problem(e[0], args.precision) for e in eps]
+    nsteps = args.warmup + args.steps
+
+    def step(i, concurrent):
+        group = [e[i % len(e)] for e in eps]
+        if concurrent:
+            return api.cpacoord_many(group, contexts=ctxs)
+        return [c.cpacoord(ep) for c, ep in zip(ctxs, group)]
+
+    out = {}
+    for mode in (True, False):
+        for i in range(args.warmup):
+            step(i, mode)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        pts = 0
+        for i in range(args.warmup, nsteps):
+            step(i, mode)
+            pts += sum(e[i % len(e)].nk for e in eps)
+        torch.cuda.synchronize()
+        out[mode] = (pts, time.perf_counter() - t0)
+    for c in ctxs:
+        c.close()
+    v = out[True][0] / out[True][1]
+    seq = out[False][0] / out[False][1]
+    print(json.dumps({"metric": "(E,k) points/s of three interface systems in one call", "value": v,
+                      "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+                      "ms_per_step": 1e3 * out[True][1] / args.steps, "higher_is_better": True,
+                      "dtype": "c128 via BF16x6 slices" if args.precision == "mixed" else "c128",
+                      "data": "synthetic", "sequential_value": seq, "concurrency_gain": v / seq,
+                      "config": {"workload": "c3: rel_bcc lmax3 PL4 + nonrel fcc lmax2 PL2 + rel bcc lmax2 PL3",
+                                 "precision": args.precision, "energies": plan,
+                                 "timing": "host wall clock around whole calls (host buffers)"}}), flush=True)
+
+
 def main():
     args = parse()
+    if args.workload == "c3":
+        run_c3(args)
+        return
     rank, ws = dist_init(args.gpus)
     if args.impl == "reference":
         run_reference(args, rank, ws)

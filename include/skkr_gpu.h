@@ -161,6 +161,28 @@ int skkr_gpu_cpacoord_bdg(skkr_ctx *ctx, double ce_re, double ce_im, double fac_
                           const double *tminvb, double *tauc, double *taua, double *taub, int ld,
                           skkr_status *st);
 
+/* The arguments of one skkr_gpu_cpacoord / skkr_gpu_cpacoord_bdg call
+ * (fach is read for SKKR_BDG contexts only). */
+typedef struct {
+  double ce_re, ce_im, fac_re, fac_im, fach_re, fach_im;
+  const skkr_rtable *rt;
+  int nk;
+  const double *xk, *wk, *lg, *rg, *conc, *tminvl, *tminvr;
+  double *tminv;
+  const double *tminva, *tminvb;
+  double *tauc, *taua, *taub;
+  int ld;
+} skkr_energy_args;
+
+/* Several systems in one call (e.g. interfaces of different lmax / PL size):
+ * energy args[e] runs on context ctx[e] (n distinct contexts, each of its
+ * own system) concurrently, each context on its own stream driven by its own
+ * host thread, so that small systems fill the SMs a large one leaves idle.
+ * Results and st[e] are those of the single calls; returns the first
+ * nonzero code. */
+int skkr_gpu_cpacoord_many(int n, skkr_ctx *const *ctx, const skkr_energy_args *args,
+                           skkr_status *st);
+
 /* Split form for callers that keep inputs resident on the device across
  * calls: stage (host -> device), run (device only), fetch (device -> host).
  * skkr_gpu_cpacoord == stage + run + fetch. */

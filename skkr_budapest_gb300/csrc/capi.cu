@@ -11,6 +11,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <mutex>
+#include <thread>
 #include <cstdlib>
 #include <cstring>
 #include <string>
@@ -19,7 +21,7 @@
 #include "../../include/skkr_gpu.h"
 #include "kernels.h"
 
-long long g_skkr_launches = 0;
+thread_local long long g_skkr_launches = 0;
 static thread_local std::string g_last_error;
 
 #define CK(x)                                                                          \
@@ -41,22 +43,28 @@ extern "C" const char *skkr_gpu_last_error(void) { return g_last_error.c_str(); 
 static int g_sync_check = -1;
 // ---- per-kernel-class event timing --------------------------------------
 namespace {
+// shared by all host threads (contexts may run concurrently): guarded by mu;
+// each thread keeps the slot of its own open begin/end pair
 struct KStats {
+  std::mutex mu;
   int on = 0;
   std::vector<cudaEvent_t> ev;
   size_t used = 0;
   std::vector<int> cls;
   std::vector<double> work;
-  int open = 0;
+  std::vector<char> done;   // end event recorded
 };
 KStats g_ks;
-long long g_active_hint = -1;
+thread_local long long g_active_hint = -1;
+thread_local long long g_ks_open = -1;
 }  // namespace
 
 void skkr_set_active_items(long long n) { g_active_hint = n; }
 long long skkr_active_items(long long all) { return g_active_hint >= 0 ? g_active_hint : all; }
 
 void kstat_begin(int cls, double work, cudaStream_t st) {
+  if (!g_ks.on) return;
+  std::lock_guard<std::mutex> lk(g_ks.mu);
   if (!g_ks.on) return;
   if (g_ks.used + 2 > g_ks.ev.size()) {
     for (int i = 0; i < 256; i++) {
@@ -65,34 +73,42 @@ void kstat_begin(int cls, double work, cudaStream_t st) {
       g_ks.ev.push_back(e);
     }
   }
+  g_ks_open = (long long)g_ks.used;
   cudaEventRecord(g_ks.ev[g_ks.used], st);
   g_ks.cls.push_back(cls);
   g_ks.work.push_back(work);
-  g_ks.open = 1;
+  g_ks.done.push_back(0);
+  g_ks.used += 2;
 }
 
 void kstat_end(cudaStream_t st) {
-  if (!g_ks.on || !g_ks.open) return;
-  cudaEventRecord(g_ks.ev[g_ks.used + 1], st);
-  g_ks.used += 2;
-  g_ks.open = 0;
+  if (g_ks_open < 0) return;
+  std::lock_guard<std::mutex> lk(g_ks.mu);
+  if (g_ks.on && (size_t)g_ks_open + 1 < g_ks.used) {
+    cudaEventRecord(g_ks.ev[g_ks_open + 1], st);
+    g_ks.done[g_ks_open / 2] = 1;
+  }
+  g_ks_open = -1;
 }
 
 // enable=1: reset and start; enable=0: stop and report out[cls*3 + {0 launches,
 // 1 total ms, 2 total algorithmic work}] for the KS_NCLS classes.
 extern "C" int skkr_gpu_kernel_stats(int enable, double *out) {
+  std::lock_guard<std::mutex> lk(g_ks.mu);
   if (enable) {
     g_ks.on = 1;
     g_ks.used = 0;
     g_ks.cls.clear();
     g_ks.work.clear();
+    g_ks.done.clear();
     return SKKR_OK;
   }
   g_ks.on = 0;
   CK(cudaDeviceSynchronize());
   if (out)
     for (int i = 0; i < KS_NCLS * 3; i++) out[i] = 0.0;
-  for (size_t i = 0; i < g_ks.cls.size() && 2 * i + 1 < g_ks.used + 1; i++) {
+  for (size_t i = 0; i < g_ks.cls.size() && 2 * i + 1 < g_ks.used; i++) {
+    if (!g_ks.done[i]) continue;
     float ms = 0.f;
     CK(cudaEventElapsedTime(&ms, g_ks.ev[2 * i], g_ks.ev[2 * i + 1]));
     if (out) {
@@ -158,6 +174,7 @@ struct DBuf {
 struct skkr_ctx {
   skkr_sizes sz;
   int lk = 0, lmmax = 0, pl = 0, n = 0, nintfc = 0, nprc = 0, ngeff = 1;
+  int dev = 0;    // CUDA device current at creation
   cudaStream_t st = nullptr;
   // staged energy
   int staged = 0;
@@ -274,11 +291,14 @@ extern "C" int skkr_gpu_create(const skkr_sizes *sizes, skkr_ctx **out) {
     delete c;
     return SKKR_ERR_UNSUPPORTED;
   }
-  if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess) {
+  if (cudaGetDevice(&c->dev) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess) {
     delete c;
     return SKKR_ERR_CUDA;
   }
-  cudaError_t e = pack_set_tables(s.mode != SKKR_NONREL, s.lmax);
+  // always the full (kappa,mu) tables: contexts of different modes may be
+  // alive at once and the lm packer never reads them
+  cudaError_t e = pack_set_tables(1, s.lmax);
   if (e != cudaSuccess) {
     g_last_error = std::string("pack_set_tables: ") + cudaGetErrorString(e);
     cudaStreamDestroy(c->st);
@@ -632,7 +652,7 @@ static int eng_gemm(skkr_ctx *c, bool mixed, int mode, const MatRef &A, const Ma
 static int eng_inv(skkr_ctx *c, bool mixed, const MatRef &A, const MatRef &X, bool inplace, int n, int nk,
                    int nc, const int *act) {
   if (mixed && n <= 128)
-    return mixed_zinv(c->mw, A, X, n, nk, nc, act, 2, c->slices_res, &c->max_resid, c->st);
+    return mixed_zinv(c->mw, A, X, n, nk, nc, act, 2, c->slices_res, true, c->st);
   if (!inplace) launch_zaxpby(X, A, nullptr, 0, nullptr, 0, n, nk, nc, act, c->st);
   launch_zgj(X, n, nk, nc, act, c->st);
   return SKKR_OK;
@@ -1006,6 +1026,7 @@ extern "C" int skkr_gpu_run(skkr_ctx *c, skkr_status *status) {
     c->mw = mixed_create();
     if (!c->mw) return SKKR_ERR_NOMEM;
   }
+  if (c->mw) CKR(mixed_resid_reset(c->mw, st));
   plan_pack(c);
   CKR(c->jobs.ensure(c->jobs_h.size() * sizeof(PackJob)));
   CK(cudaMemcpyAsync(c->jobs.p, c->jobs_h.data(), c->jobs_h.size() * sizeof(PackJob),
@@ -1098,6 +1119,7 @@ extern "C" int skkr_gpu_run(skkr_ctx *c, skkr_status *status) {
     if (!(concpa && cpacon)) break;
   }
   trace_point("after CPA loop");
+  if (c->mw) CKR(mixed_resid_read(c->mw, &c->max_resid, st));
   if (c->mw && c->err_code == 0) {
     int f = mixed_error_flag(c->mw);
     if (f != 0) {
@@ -1169,6 +1191,44 @@ extern "C" int skkr_gpu_cpacoord_bdg(skkr_ctx *c, double ce_re, double ce_im, do
   c->fach = zmk(fach_re, fach_im);
   return skkr_gpu_cpacoord(c, ce_re, ce_im, fac_re, fac_im, rt, nk, xk, wk, lg, rg, conc, tminvl,
                            tminvr, tminv, tminva, tminvb, tauc, taua, taub, ld, status);
+}
+
+// Several systems at once: context e runs args[e] on its own stream from its
+// own host thread, so the kernels of a small system fill the SMs a large one
+// leaves idle.  The contexts must be distinct.
+extern "C" int skkr_gpu_cpacoord_many(int n, skkr_ctx *const *ctx, const skkr_energy_args *args,
+                                      skkr_status *st) {
+  if (n < 1 || !ctx || !args) return SKKR_ERR_ARG;
+  for (int e = 0; e < n; e++) {
+    if (!ctx[e]) return SKKR_ERR_ARG;
+    for (int f = 0; f < e; f++)
+      if (ctx[f] == ctx[e]) return SKKR_ERR_ARG;
+  }
+  std::vector<int> rc(n, SKKR_OK);
+  auto one = [&](int e) {
+    skkr_ctx *c = ctx[e];
+    const skkr_energy_args &a = args[e];
+    if (cudaSetDevice(c->dev) != cudaSuccess) {
+      rc[e] = SKKR_ERR_CUDA;
+      return;
+    }
+    skkr_status *s = st ? st + e : nullptr;
+    if (c->sz.mode == SKKR_BDG)
+      rc[e] = skkr_gpu_cpacoord_bdg(c, a.ce_re, a.ce_im, a.fac_re, a.fac_im, a.fach_re, a.fach_im, a.rt,
+                                    a.nk, a.xk, a.wk, a.lg, a.rg, a.conc, a.tminvl, a.tminvr, a.tminv,
+                                    a.tminva, a.tminvb, a.tauc, a.taua, a.taub, a.ld, s);
+    else
+      rc[e] = skkr_gpu_cpacoord(c, a.ce_re, a.ce_im, a.fac_re, a.fac_im, a.rt, a.nk, a.xk, a.wk, a.lg,
+                                a.rg, a.conc, a.tminvl, a.tminvr, a.tminv, a.tminva, a.tminvb, a.tauc,
+                                a.taua, a.taub, a.ld, s);
+  };
+  std::vector<std::thread> th;
+  for (int e = 1; e < n; e++) th.emplace_back(one, e);
+  one(0);
+  for (auto &t : th) t.join();
+  for (int e = 0; e < n; e++)
+    if (rc[e] != SKKR_OK) return rc[e];
+  return SKKR_OK;
 }
 
 // ---------------------------------------------------------------------------
@@ -1523,7 +1583,9 @@ extern "C" int skkr_gpu_zinv_batch(int precision, int n, int batch, double *a, i
     MixedWork *w = mixed_create();
     if (!w) return SKKR_ERR_NOMEM;
     double r = 0.0;
-    int rc = mixed_zinv(w, Am, Am, n, batch, 1, nullptr, newton, 7, &r, 0);
+    int rc = mixed_resid_reset(w, 0);
+    if (!rc) rc = mixed_zinv(w, Am, Am, n, batch, 1, nullptr, newton, 7, true, 0);
+    if (!rc) rc = mixed_resid_read(w, &r, 0);
     if (rc == SKKR_OK && cudaDeviceSynchronize() != cudaSuccess) rc = SKKR_ERR_CUDA;
     if (rc == SKKR_OK && mixed_error_flag(w) != 0) rc = SKKR_ERR_CUDA;
     mixed_destroy(w);

@@ -71,7 +71,7 @@ inline MatRef mref_map(zd *base, long long sk, long long sc, int ld, const int *
 // kernel launch bookkeeping (defined in capi.cu).  With SKKR_SYNC_CHECK=1 in
 // the environment every launch is followed by a device synchronisation and
 // the first failing launch site is recorded (diagnostics only).
-extern long long g_skkr_launches;
+extern thread_local long long g_skkr_launches;  // launches made by this host thread
 void skkr_after_launch(const char *file, int line);
 #define SKKR_LAUNCHED() skkr_after_launch(__FILE__, __LINE__)
 

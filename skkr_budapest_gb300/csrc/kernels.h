@@ -69,4 +69,8 @@ int mixed_zgemm_k(MixedWork *w, int mode, int S, const MatRef &A, const MatRef &
 int mixed_zgemm(MixedWork *w, int mode, int S, const MatRef &A, const MatRef &B, const MatRef &C,
                 const MatRef &D, const MatRef &E, int n, int nk, int nc, const int *act, cudaStream_t st);
 int mixed_zinv(MixedWork *w, const MatRef &A, const MatRef &X, int n, int nk, int nc, const int *act,
-               int newton, int sres, double *max_resid, cudaStream_t st);
+               int newton, int sres, bool track_resid, cudaStream_t st);
+// running maximum of the final Newton residual norms (device scalar): reset
+// asynchronously, read with a stream synchronisation
+int mixed_resid_reset(MixedWork *w, cudaStream_t st);
+int mixed_resid_read(MixedWork *w, double *out, cudaStream_t st);

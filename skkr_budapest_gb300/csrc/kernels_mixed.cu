@@ -667,19 +667,22 @@ __global__ void __launch_bounds__(TY * 16, 1) k_cgj32(MatRef A, MatRef X, int n,
 }
 
 // ------------------------------------------------------------------ host side
-PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 
-int get_encoder() {
-  if (g_encode) return 0;
-  cudaDriverEntryPointQueryResult q;
-  void *fn = nullptr;
-  if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
-          cudaSuccess ||
-      q != cudaDriverEntryPointSuccess || !fn)
-    return -1;
-  g_encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
-  return 0;
+// resolved once per process (thread-safe static initialisation: contexts may
+// run from several host threads)
+static PFN_cuTensorMapEncodeTiled_v12000 encoder() {
+  static const PFN_cuTensorMapEncodeTiled_v12000 fn = []() -> PFN_cuTensorMapEncodeTiled_v12000 {
+    cudaDriverEntryPointQueryResult q;
+    void *p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      return nullptr;
+    return (PFN_cuTensorMapEncodeTiled_v12000)p;
+  }();
+  return fn;
 }
+int get_encoder() { return encoder() ? 0 : -1; }
 
 // tiled staging: dims {32, rows, regions * kblocks}; one box = one contiguous block
 int make_map(CUtensorMap *m, void *base, int rows, long long depth, int boxrows) {
@@ -687,7 +690,7 @@ int make_map(CUtensorMap *m, void *base, int rows, long long depth, int boxrows)
   cuuint64_t strides[2] = {(cuuint64_t)KB * 2, (cuuint64_t)KB * 2 * rows};
   cuuint32_t box[3] = {(cuuint32_t)KB, (cuuint32_t)boxrows, 1};
   cuuint32_t es[3] = {1, 1, 1};
-  CUresult r = g_encode(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, base, dims, strides, box, es,
+  CUresult r = encoder()(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, base, dims, strides, box, es,
                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS ? 0 : -1;
@@ -713,6 +716,7 @@ struct MixedWork {
   double *rnorm = nullptr;
   size_t rn_cap = 0;
   int *err = nullptr;
+  unsigned long long *dmax = nullptr;  // running max of Newton residual norms (double bits)
   int smem_set[16] = {0};
   int last_n = -1, last_k = -1;   // staging layout the zero padding was made for
 };
@@ -730,17 +734,35 @@ static int grow(void **p, size_t *cap, size_t bytes, bool zero) {
 
 MixedWork *mixed_create() {
   MixedWork *w = new MixedWork();
-  if (cudaMalloc(&w->err, sizeof(int)) != cudaSuccess) {
+  if (cudaMalloc(&w->err, sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&w->dmax, sizeof(unsigned long long)) != cudaSuccess) {
+    if (w->err) cudaFree(w->err);
     delete w;
     return nullptr;
   }
   cudaMemset(w->err, 0, sizeof(int));
+  cudaMemset(w->dmax, 0, sizeof(unsigned long long));
   return w;
+}
+
+int mixed_resid_reset(MixedWork *w, cudaStream_t st) {
+  return cudaMemsetAsync(w->dmax, 0, sizeof(unsigned long long), st) == cudaSuccess ? 0 : SKKR_ERR_CUDA;
+}
+
+int mixed_resid_read(MixedWork *w, double *out, cudaStream_t st) {
+  unsigned long long h = 0;
+  if (cudaMemcpyAsync(&h, w->dmax, sizeof(h), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return SKKR_ERR_CUDA;
+  double v;
+  memcpy(&v, &h, sizeof(v));
+  *out = v;
+  return 0;
 }
 
 void mixed_destroy(MixedWork *w) {
   if (!w) return;
-  void *ps[] = {w->sa, w->sb, w->sigma, w->tau, w->acopy, w->rbuf, w->rnorm, w->err};
+  void *ps[] = {w->sa, w->sb, w->sigma, w->tau, w->acopy, w->rbuf, w->rnorm, w->err, w->dmax};
   for (void *p : ps)
     if (p) cudaFree(p);
   delete w;
@@ -865,11 +887,37 @@ int mixed_zgemm(MixedWork *w, int mode, int S, const MatRef &A, const MatRef &B,
   return mixed_zgemm_k(w, mode, S, A, B, C, D, E, n, n, nk, nc, act, st);
 }
 
+// Frobenius norm of every item's residual folded into a running maximum
+// (non-negative doubles order like their bit patterns: integer atomicMax)
+__global__ void k_fnorm_max(MatRef A, int n, int nc, const int *__restrict__ act,
+                            unsigned long long *dmax) {
+  const int item = blockIdx.x;
+  const int kk = item / nc, cc = item % nc;
+  if (act && !act[item]) return;
+  const zd *a = mat_ptr(A, kk, cc);
+  double s = 0.0;
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    zd v = a[(e % n) + (long long)(e / n) * A.ld];
+    s += v.x * v.x + v.y * v.y;
+  }
+  __shared__ double red[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    s = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (threadIdx.x == 0) atomicMax(dmax, (unsigned long long)__double_as_longlong(sqrt(s)));
+  }
+}
+
 // X = A^-1: FP32 Gauss-Jordan, then `newton` steps X += X (I - A X) with the
 // residual product at S = sres slices and the correction at S = 3.  X may
 // alias A.
 int mixed_zinv(MixedWork *w, const MatRef &A, const MatRef &X, int n, int nk, int nc, const int *act,
-               int newton, int sres, double *max_resid, cudaStream_t st) {
+               int newton, int sres, bool track_resid, cudaStream_t st) {
   if (n < 1 || n > 128) return SKKR_ERR_ARG;
   const long long items = (long long)nk * nc, MB = (long long)n * n;
   int rc;
@@ -888,22 +936,12 @@ int mixed_zinv(MixedWork *w, const MatRef &A, const MatRef &X, int n, int nk, in
   for (int it = 0; it < newton; it++) {
     // R = I - A X
     if ((rc = mixed_zgemm(w, 4, sres, Ac, X, R, R, R, n, nk, nc, act, st))) return rc;
-    if (max_resid && it == newton - 1) {
-      cudaMemsetAsync(w->rnorm, 0, items * sizeof(double), st);
-      launch_fnorm(R, n, nk, nc, act, w->rnorm, st);
+    if (track_resid && it == newton - 1) {
+      k_fnorm_max<<<(unsigned)items, 256, 0, st>>>(R, n, nc, act, w->dmax);
+      SKKR_LAUNCHED();
     }
     // X = X + X R
     if ((rc = mixed_zgemm(w, 5, 3, X, R, X, X, X, n, nk, nc, act, st))) return rc;
-  }
-  if (max_resid) {
-    std::vector<double> h(items);
-    if (cudaMemcpyAsync(h.data(), w->rnorm, items * sizeof(double), cudaMemcpyDeviceToHost, st) !=
-            cudaSuccess ||
-        cudaStreamSynchronize(st) != cudaSuccess)
-      return SKKR_ERR_CUDA;
-    double m = 0.0;
-    for (double v : h) m = std::fmax(m, v);
-    *max_resid = std::fmax(*max_resid, m);
   }
   return 0;
 }

@@ -70,6 +70,7 @@ def lib():
         L.skkr_gpu_phystau.argtypes = [I, I, P, P, P, I]
         L.skkr_gpu_layer_dos.argtypes = [I, I, I, P, I, P, P, I, P, P]
         L.skkr_gpu_set_reduce.argtypes = [P, P, P]
+        L.skkr_gpu_cpacoord_many.argtypes = [I, P, P, P]
         L.skkr_gpu_gjinv_batch.argtypes = [I, I, P, I]
         L.skkr_gpu_surfgf_batch.argtypes = [I, I, P, P, P, P, I, I, D, P, P]
         L.skkr_gpu_gk.argtypes = [P, I, I, P, P]
@@ -102,6 +103,13 @@ def uncm(a):
 def _check(rc, where):
     if rc != 0:
         raise SkkrError(rc, where)
+
+
+class EnergyArgs(C.Structure):
+    _fields_ = [("ce_re", D), ("ce_im", D), ("fac_re", D), ("fac_im", D), ("fach_re", D), ("fach_im", D),
+                ("rt", P), ("nk", I), ("xk", P), ("wk", P), ("lg", P), ("rg", P), ("conc", P),
+                ("tminvl", P), ("tminvr", P), ("tminv", P), ("tminva", P), ("tminvb", P),
+                ("tauc", P), ("taua", P), ("taub", P), ("ld", I)]
 
 
 class RTableHolder:

@@ -150,3 +150,13 @@ def test_layer_dos_after_cpacoord(system, ie):
         F, G = S.layer_dos_inputs(ep, which)
         om, ol = O.layer_dos(phys, F, G, ep.lmax, ep.irel, not ep.irel)
         assert rel(zm, om) < TOL and rel(zl, ol) < TOL, (rel(zm, om), rel(zl, ol))
+
+
+def test_cpa_from_learned_start_converges_to_the_same_tau():
+    from skkr_budapest_gb300 import cpa_warmstart as CW
+    ep = W.energy_problem(CW._spec(9001), 10, nset=4)
+    a = api.cpacoord(ep)
+    b = api.cpacoord(ep, tminv=CW.warm_start(ep, CW.Model()))
+    assert a["status"] == 0 and b["status"] == 0
+    assert b["cpa_error"] < ep.cpatol
+    assert rel(b["tauc"], a["tauc"]) < 1e-7
