@@ -130,6 +130,19 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
   for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
 }
 
+// 16 consecutive accumulator columns of this warp's 32 TMEM lanes, without
+// the wait (tmem_ld_wait after a batch of loads)
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t *r) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+        "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+}
+__device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
 // UMMA shared-memory descriptor: K-major, 64-byte swizzle (rows of 32 bf16),
 // 8-row groups 512 bytes apart (tile base 512-byte aligned).
 __device__ __forceinline__ uint64_t sdesc_sw64(uint32_t saddr) {
@@ -276,9 +289,10 @@ __global__ void __launch_bounds__(256) k_split_a(MatRef A, int n, int K, int nc,
   }
 }
 
-// B'^T from the K x n complex B: one warp per column j; rows j and n+j of
+// B'^T from the K x n complex B: one warp per column j; rows 2j and 2j+1 of
 // B'^T are [Re B(:,j), -Im B(:,j)] and [Im B(:,j), Re B(:,j)] (columns scaled
-// by their max over these K rows)
+// by their max over these K rows), so that the real and imaginary parts of an
+// output element land in adjacent accumulator columns of one thread
 template <int S, int DB>
 __global__ void __launch_bounds__(256) k_split_b(MatRef B, int n, int K, int nc, const int *__restrict__ act,
                                                  __nv_bfloat16 *__restrict__ out, int Np, int Kp,
@@ -309,10 +323,10 @@ __global__ void __launch_bounds__(256) k_split_b(MatRef B, int n, int K, int nc,
     float dr[S], di[S];
     slice_digits<S, DB>(v.x, es, dr);
     slice_digits<S, DB>(v.y, es, di);
-    store_digits<S, DB>(dr, 1.0f, 16, base + tiled(j, k, Np), sstride);
-    store_digits<S, DB>(di, -1.0f, 16, base + tiled(j, K + k, Np), sstride);
-    store_digits<S, DB>(di, 1.0f, 16, base + tiled(n + j, k, Np), sstride);
-    store_digits<S, DB>(dr, 1.0f, 16, base + tiled(n + j, K + k, Np), sstride);
+    store_digits<S, DB>(dr, 1.0f, 16, base + tiled(2 * j, k, Np), sstride);
+    store_digits<S, DB>(di, -1.0f, 16, base + tiled(2 * j, K + k, Np), sstride);
+    store_digits<S, DB>(di, 1.0f, 16, base + tiled(2 * j + 1, k, Np), sstride);
+    store_digits<S, DB>(dr, 1.0f, 16, base + tiled(2 * j + 1, K + k, Np), sstride);
   }
 }
 
@@ -345,6 +359,28 @@ __device__ __forceinline__ double scale_pow2(double x, int e) {
   return __longlong_as_double(__double_as_longlong(x) + ((long long)e << 52));
 }
 
+// round-to-nearest-even double of a * 2^e from integer operations only (the
+// FP64 pipe of this GPU is ~1/40 of the integer rate): normalise with a
+// leading-zero count, keep 53 bits, round on the dropped 11, add e to the
+// exponent.  Equal to scale_pow2(__ll2double_rn(a), e) for normal results.
+__device__ __forceinline__ double fix_to_double(long long a, int e) {
+  if (a == 0) return 0.0;
+  const unsigned long long sign = a < 0 ? 0x8000000000000000ull : 0ull;
+  unsigned long long m = a < 0 ? 0ull - (unsigned long long)a : (unsigned long long)a;
+  const int lz = __clzll((long long)m);
+  m <<= lz;                                    // leading one at bit 63
+  unsigned long long mant = m >> 11;           // 53 significant bits
+  const unsigned long long rem = m & 0x7FFull;
+  int ex = 63 - lz + e;
+  mant += (rem > 0x400ull || (rem == 0x400ull && (mant & 1ull))) ? 1ull : 0ull;
+  if (mant >> 53) {                            // rounding carried into bit 53
+    mant >>= 1;
+    ex++;
+  }
+  return __longlong_as_double((long long)(sign | ((unsigned long long)(ex + 1023) << 52) |
+                                          (mant & 0xFFFFFFFFFFFFFull)));
+}
+
 // accumulator of product (p, q), 0-based slices: its level p+q; levels >= 4
 // share the last accumulator (they sit 2^-32 and further below the leading
 // level, so the truncation of the shared sum is far below the slice error)
@@ -353,7 +389,7 @@ __host__ __device__ constexpr int level_of(int p, int q) { return p + q < NACC ?
 __host__ __device__ constexpr int nlevels(int S) { return S < NACC ? S : NACC; }
 
 template <int S>
-__global__ void __launch_bounds__(128, 1) k_ozaki(const __grid_constant__ CUtensorMap tmA,
+__global__ void __launch_bounds__(256, 1) k_ozaki(const __grid_constant__ CUtensorMap tmA,
                                                   const __grid_constant__ CUtensorMap tmB, OzArgs g) {
   const int item = blockIdx.y;
   if (g.act && !g.act[item]) return;
@@ -366,11 +402,18 @@ __global__ void __launch_bounds__(128, 1) k_ozaki(const __grid_constant__ CUtens
   __shared__ __align__(8) uint64_t bar_full[NSTAGE], bar_empty[NSTAGE], bar_acc;
   __shared__ uint32_t tmem_base;
   __shared__ volatile int failed, issued_kb, consumed_kb;
+  __shared__ int col_exp[NT / 2];  // column scale exponents of this tile's complex columns
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
   if (warp == 0) {
     tmem_alloc(&tmem_base, 512);
     tmem_relinquish();
+  }
+  if (threadIdx.x >= 64) {  // warps 2-7: column scales of the tile (read by the epilogue)
+    for (int t = threadIdx.x - 64; t < NT / 2; t += blockDim.x - 64) {
+      const int j = (nt * NT) / 2 + t;
+      col_exp[t] = j < g.n ? g.tau[(long long)item * g.n + j] : 0;
+    }
   }
   if (threadIdx.x == 32) {
     failed = 0;
@@ -455,44 +498,57 @@ __global__ void __launch_bounds__(128, 1) k_ozaki(const __grid_constant__ CUtens
         mbar_wait(&bar_full[kb % NSTAGE], (kb / NSTAGE) & 1);
     }
   } else {
-    // epilogue: warp w owns TMEM lanes 32w..32w+31 = rows of this M tile
-    const int row = mt * MT + warp * 32 + lane;
-    const uint32_t lane_addr = tbase + ((uint32_t)(warp * 32) << 16);
+    // epilogue, 8 warps: warp w reads TMEM lanes 32 (w % 4) .. +31 (rows of
+    // this M tile) and accumulator columns [48 (w / 4), +48)
+    const int quarter = warp & 3, half = warp >> 2;
+    const int row = mt * MT + quarter * 32 + lane;
+    const uint32_t lane_addr = tbase + ((uint32_t)(quarter * 32) << 16);
     const int kk = item / g.nc, cc = item % g.nc;
     // accumulators carry 2^-30 sigma_i tau_j; the int64 sum is in units of 2^-16
     const int erow = row < g.n ? g.sigma[(long long)item * (g.mtiles * MT) + row] - g.eoff : 0;
-    for (int c0 = 0; c0 < NT; c0 += 32) {
-      float v[NACC][32];
-      constexpr int NL = nlevels(S);
+    double *pc = (double *)mat_ptr(g.C, kk, cc);
+    double *pd = (double *)mat_ptr(g.D, kk, cc);
+    double *pe = (double *)mat_ptr(g.E, kk, cc);
+    constexpr int NL = nlevels(S);
+#pragma unroll 1
+    for (int c0 = half * (NT / 2); c0 < (half + 1) * (NT / 2); c0 += 16) {
+      uint32_t v[NACC][16];
 #pragma unroll
-      for (int l = 0; l < NL; l++) tmem_ld32(lane_addr + l * NT + c0, v[l]);
+      for (int l = 0; l < NL; l++) tmem_ld16(lane_addr + l * NT + c0, v[l]);
+      tmem_ld_wait();
       if (row >= g.n) continue;
 #pragma unroll
-      for (int t = 0; t < 32; t++) {
-        const int jj = nt * NT + c0 + t;
-        if (jj < 2 * g.n) {
-          const int j = jj < g.n ? jj : jj - g.n, im = jj >= g.n;
-          long long acc = 0;
+      for (int t = 0; t < 16; t += 2) {  // accumulator columns 2j, 2j+1 = Re, Im of column j
+        const int j = (nt * NT + c0 + t) >> 1;
+        if (j < g.n) {
+          long long ar = 0, ai = 0;
 #pragma unroll
-          for (int l = 0; l < NL; l++) acc += f2fix16(v[l][t]);
-          const double val = scale_pow2(__ll2double_rn(acc), erow + g.tau[(long long)item * g.n + j]);
-          const long long off = 2 * (row + (long long)j * g.C.ld) + im;
+          for (int l = 0; l < NL; l++) {
+            ar += f2fix16(__uint_as_float(v[l][t]));
+            ai += f2fix16(__uint_as_float(v[l][t + 1]));
+          }
+          const int e = erow + col_exp[(c0 + t) >> 1];
+          const double2 val = make_double2(fix_to_double(ar, e), fix_to_double(ai, e));
+          double2 *oc = (double2 *)pc + row + (long long)j * g.C.ld;
           if (g.mode == 0) {
-            ((double *)mat_ptr(g.C, kk, cc))[off] = val;
+            *oc = val;
           } else if (g.mode == 1) {
-            ((double *)mat_ptr(g.C, kk, cc))[off] -= val;
+            const double2 o = *oc;
+            *oc = make_double2(o.x - val.x, o.y - val.y);
           } else if (g.mode == 2) {
-            const long long od = 2 * (row + (long long)j * g.D.ld) + im;
-            const long long oe = 2 * (row + (long long)j * g.E.ld) + im;
-            ((double *)mat_ptr(g.D, kk, cc))[od] -= val;
-            ((double *)mat_ptr(g.E, kk, cc))[oe] -= val;
+            double2 *od = (double2 *)pd + row + (long long)j * g.D.ld;
+            double2 *oe = (double2 *)pe + row + (long long)j * g.E.ld;
+            const double2 d = *od, x = *oe;
+            *od = make_double2(d.x - val.x, d.y - val.y);
+            *oe = make_double2(x.x - val.x, x.y - val.y);
           } else if (g.mode == 3) {
-            const long long od = 2 * (row + (long long)j * g.D.ld) + im;
-            ((double *)mat_ptr(g.C, kk, cc))[off] = ((const double *)mat_ptr(g.D, kk, cc))[od] - val;
+            const double2 d = ((const double2 *)pd)[row + (long long)j * g.D.ld];
+            *oc = make_double2(d.x - val.x, d.y - val.y);
           } else if (g.mode == 4) {
-            ((double *)mat_ptr(g.C, kk, cc))[off] = ((row == j && !im) ? 1.0 : 0.0) - val;
+            *oc = make_double2((row == j ? 1.0 : 0.0) - val.x, -val.y);
           } else {
-            ((double *)mat_ptr(g.C, kk, cc))[off] += val;
+            const double2 o = *oc;
+            *oc = make_double2(o.x + val.x, o.y + val.y);
           }
         }
       }
@@ -850,7 +906,7 @@ static int zgemm_s(MixedWork *w, int mode, const MatRef &A, const MatRef &B, con
   const long long active = act ? skkr_active_items(items) : items;
   // algorithmic BF16 tensor work: S(S+1)/2 real products of n x 2K x 2n per item
   kstat_begin(KS_OZAKI, (double)(S * (S + 1) / 2) * 8.0 * n * (double)n * K * (double)active, st);
-  k_ozaki<S><<<grid, 128, smem, st>>>(ma, mb, g);
+  k_ozaki<S><<<grid, 256, smem, st>>>(ma, mb, g);
   kstat_end(st);
   SKKR_LAUNCHED();
   return 0;
