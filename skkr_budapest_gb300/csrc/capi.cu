@@ -729,12 +729,32 @@ static int run_decimation(skkr_ctx *c, int k0, int nkc, const std::vector<int> &
     MatRef &ac = (iter & 1) ? a0 : a1, &an = (iter & 1) ? a1 : a0;
     MatRef &bc = (iter & 1) ? b0 : b1, &bn = (iter & 1) ? b1 : b0;
     CKR(eng_inv(c, mx, eps, y1, false, n, nkc, nc, act));              // y1 = eps^-1
-    CKR(eng_gemm(c, mx, 0, ac, y1, P, P, P, n, nkc, nc, act));        // P = alfa y1
-    CKR(eng_gemm(c, mx, 0, bc, y1, Q, Q, Q, n, nkc, nc, act));        // Q = beta y1
-    CKR(eng_gemm(c, mx, 0, P, ac, an, an, an, n, nkc, nc, act));      // alfa' = P alfa
-    CKR(eng_gemm(c, mx, 0, Q, bc, bn, bn, bn, n, nkc, nc, act));      // beta' = Q beta
-    CKR(eng_gemm(c, mx, 2, P, bc, P, eps, x, n, nkc, nc, act));       // y3: eps -= y3, x -= y3
-    CKR(eng_gemm(c, mx, 1, Q, ac, eps, eps, eps, n, nkc, nc, act));   // eps -= y4
+    if (mx && !ehsplit(c)) {
+      // split-precision engine: each operand split once (B slots 1-3: y1,
+      // alfa, beta; A slots 1-4: alfa, beta, P, Q) for the six products
+      MixedWork *w = c->mw;
+      const int S = c->slices;
+      CKR(mixed_split(w, 1, 1, S, y1, n, n, nkc, nc, act, st));
+      CKR(mixed_split(w, 0, 1, S, ac, n, n, nkc, nc, act, st));
+      CKR(mixed_split(w, 0, 2, S, bc, n, n, nkc, nc, act, st));
+      CKR(mixed_gemm_staged(w, 0, S, 1, 1, P, P, P, n, n, nkc, nc, act, st));        // P = alfa y1
+      CKR(mixed_gemm_staged(w, 0, S, 2, 1, Q, Q, Q, n, n, nkc, nc, act, st));        // Q = beta y1
+      CKR(mixed_split(w, 1, 2, S, ac, n, n, nkc, nc, act, st));
+      CKR(mixed_split(w, 1, 3, S, bc, n, n, nkc, nc, act, st));
+      CKR(mixed_split(w, 0, 3, S, P, n, n, nkc, nc, act, st));
+      CKR(mixed_split(w, 0, 4, S, Q, n, n, nkc, nc, act, st));
+      CKR(mixed_gemm_staged(w, 0, S, 3, 2, an, an, an, n, n, nkc, nc, act, st));     // alfa' = P alfa
+      CKR(mixed_gemm_staged(w, 0, S, 4, 3, bn, bn, bn, n, n, nkc, nc, act, st));     // beta' = Q beta
+      CKR(mixed_gemm_staged(w, 2, S, 3, 3, P, eps, x, n, n, nkc, nc, act, st));      // eps, x -= P beta
+      CKR(mixed_gemm_staged(w, 1, S, 4, 2, eps, eps, eps, n, n, nkc, nc, act, st));  // eps -= Q alfa
+    } else {
+      CKR(eng_gemm(c, mx, 0, ac, y1, P, P, P, n, nkc, nc, act));        // P = alfa y1
+      CKR(eng_gemm(c, mx, 0, bc, y1, Q, Q, Q, n, nkc, nc, act));        // Q = beta y1
+      CKR(eng_gemm(c, mx, 0, P, ac, an, an, an, n, nkc, nc, act));      // alfa' = P alfa
+      CKR(eng_gemm(c, mx, 0, Q, bc, bn, bn, bn, n, nkc, nc, act));      // beta' = Q beta
+      CKR(eng_gemm(c, mx, 2, P, bc, P, eps, x, n, nkc, nc, act));       // y3: eps -= y3, x -= y3
+      CKR(eng_gemm(c, mx, 1, Q, ac, eps, eps, eps, n, nkc, nc, act));   // eps -= y4
+    }
     launch_fnorm(an, n, nkc, nc, act, err, st);
     // the two leads may carry different caps (itermaxl / itermaxr)
     launch_dec_state(err, act, stat, iters, nit, iter, itermax, c->sz.errmax, st);
@@ -820,6 +840,21 @@ static int run_tau2d(skkr_ctx *c, int k0, int nkc, const std::vector<int> &icls)
   MatRef Ys = mref_map(sbase, (long long)c->nsl * MB, MB, n, ysl, nc);
   MatRef Xs = mref_map(sbase, (long long)c->nsl * MB, MB, n, xsl, nc);
   const bool mx = use_mixed(c, false);
+  // split-precision engine: M10 and M01 enter every step on the same side,
+  // so they are split once (A slot 1 = M10, B slot 1 = M01, A slot 3 = M01,
+  // B slot 3 = M10); the per-step operands use slot 2
+  const bool staged = mx && !ehsplit(c);
+  MixedWork *w = c->mw;
+  const int S = c->slices;
+  auto prod = [&](int sa, const MatRef *A, int sb, const MatRef *B, const MatRef &C) -> int {
+    if (A) CKR(mixed_split(w, 0, sa, S, *A, n, n, nkc, nc, nullptr, st));
+    if (B) CKR(mixed_split(w, 1, sb, S, *B, n, n, nkc, nc, nullptr, st));
+    return mixed_gemm_staged(w, 0, S, sa, sb, C, C, C, n, n, nkc, nc, nullptr, st);
+  };
+  if (staged) {
+    CKR(mixed_split(w, 0, 1, S, M10, n, n, nkc, nc, nullptr, st));
+    CKR(mixed_split(w, 1, 1, S, M01, n, n, nkc, nc, nullptr, st));
+  }
   // forward (tau2d.f:53-85)
   for (int p = 0; p < nprc; p++) {
     int tm2[SKKR_MAPN];
@@ -828,6 +863,9 @@ static int run_tau2d(skkr_ctx *c, int k0, int nkc, const std::vector<int> &icls)
     launch_add_tblocks(T00(p), M00, Tt, lk, pl, n, nkc, nc, nullptr, ehsplit(c), st);
     if (p == 0) {
       launch_zaxpby(YY(0), Ys, nullptr, 0, nullptr, 0, n, nkc, nc, nullptr, st);
+    } else if (staged) {
+      MatRef yr = Yr(p);
+      CKR(prod(1, nullptr, 2, &yr, YY(p)));                       // YY = M10 Yr
     } else {
       CKR(eng_gemm(c, mx, 0, M10, Yr(p), YY(p), YY(p), YY(p), n, nkc, nc, nullptr));
     }
@@ -835,13 +873,23 @@ static int run_tau2d(skkr_ctx *c, int k0, int nkc, const std::vector<int> &icls)
       MatRef yy = YY(p);
       launch_zaxpby(Wm, T00(p), &yy, -1.0, nullptr, 0, n, nkc, nc, nullptr, st);
       CKR(eng_inv(c, mx, Wm, Wm, true, n, nkc, nc, nullptr));
-      CKR(eng_gemm(c, mx, 0, Wm, M01, Yr(p + 1), Yr(p + 1), Yr(p + 1), n, nkc, nc, nullptr));
+      if (staged)
+        CKR(prod(2, &Wm, 1, nullptr, Yr(p + 1)));                  // Yr(p+1) = W M01
+      else
+        CKR(eng_gemm(c, mx, 0, Wm, M01, Yr(p + 1), Yr(p + 1), Yr(p + 1), n, nkc, nc, nullptr));
     }
+  }
+  if (staged) {
+    CKR(mixed_split(w, 0, 3, S, M01, n, n, nkc, nc, nullptr, st));
+    CKR(mixed_split(w, 1, 3, S, M10, n, n, nkc, nc, nullptr, st));
   }
   // backward (tau2d.f:89-109)
   for (int p = nprc - 1; p >= 0; p--) {
     if (p == nprc - 1) {
       launch_zaxpby(XX(p), Xs, nullptr, 0, nullptr, 0, n, nkc, nc, nullptr, st);
+    } else if (staged) {
+      MatRef xr = Xr(p);
+      CKR(prod(3, nullptr, 2, &xr, XX(p)));                       // XX = M01 Xr
     } else {
       CKR(eng_gemm(c, mx, 0, M01, Xr(p), XX(p), XX(p), XX(p), n, nkc, nc, nullptr));
     }
@@ -849,7 +897,10 @@ static int run_tau2d(skkr_ctx *c, int k0, int nkc, const std::vector<int> &icls)
       MatRef xx = XX(p);
       launch_zaxpby(Wm, T00(p), &xx, -1.0, nullptr, 0, n, nkc, nc, nullptr, st);
       CKR(eng_inv(c, mx, Wm, Wm, true, n, nkc, nc, nullptr));
-      CKR(eng_gemm(c, mx, 0, Wm, M10, Xr(p - 1), Xr(p - 1), Xr(p - 1), n, nkc, nc, nullptr));
+      if (staged)
+        CKR(prod(2, &Wm, 3, nullptr, Xr(p - 1)));                  // Xr(p-1) = W M10
+      else
+        CKR(eng_gemm(c, mx, 0, Wm, M10, Xr(p - 1), Xr(p - 1), Xr(p - 1), n, nkc, nc, nullptr));
     }
   }
   // diagonal blocks (tau2d.f:114-149), weight wk/ngeff
@@ -1037,7 +1088,14 @@ extern "C" int skkr_gpu_run(skkr_ctx *c, skkr_status *status) {
     const int ncmax = 2 * c->ngeff;
     double per_k = (double)MB * sizeof(zd) * (c->nmat + 9.0 * ncmax + (5.0 * c->nprc + 1) * c->ngeff) +
                    (double)c->ngeff * ni * lk2 * sizeof(zd);
-    double budget = 24.0e9;
+    if (c->sz.precision == SKKR_MIXED) {
+      // BF16 slice staging: up to MIXED_SLOTS operands per side, S slices of
+      // the padded real embedding (A: 128-row tiles, B: 96-row tiles, K: 2n)
+      const double Mp = 128.0 * ((n + 127) / 128), Np = 96.0 * ((2 * n + 95) / 96),
+                   Kp = 32.0 * ((2 * n + 31) / 32);
+      per_k += (double)ncmax * MIXED_SLOTS * c->slices_res * (Mp + Np) * Kp * 2.0;
+    }
+    double budget = 64.0e9;  // of the 280 GB: the estimate counts every class slot as used
     int kc = c->sz.nk_chunk > 0 ? c->sz.nk_chunk : (int)std::max(1.0, std::floor(budget / per_k));
     // grid.y of the batched kernels holds k_chunk * items-per-k (<= 2 * ngeff)
     kc = std::min(kc, 65535 / (2 * c->ngeff));

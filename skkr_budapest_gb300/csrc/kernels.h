@@ -61,6 +61,14 @@ MixedWork *mixed_create();
 void mixed_destroy(MixedWork *w);
 int mixed_error_flag(MixedWork *w);
 // modes as launch_zgemm plus 4: C = I - A*B, 5: C = C + A*B; S = slices (3..7)
+// Split operands live in MIXED_SLOTS staging slots per side (0: A, 1: B);
+// slot 0 is the one mixed_zgemm / mixed_zgemm_k / mixed_zinv use.  Splitting
+// once and multiplying several times reuses an operand's slices.
+constexpr int MIXED_SLOTS = 6;
+int mixed_split(MixedWork *w, int side, int slot, int S, const MatRef &M, int n, int K, int nk, int nc,
+                const int *act, cudaStream_t st);
+int mixed_gemm_staged(MixedWork *w, int mode, int S, int sa, int sb, const MatRef &C, const MatRef &D,
+                      const MatRef &E, int n, int K, int nk, int nc, const int *act, cudaStream_t st);
 // C (op) A[:, 0:K] B[0:K, :] for n x K by K x n blocks (A, B already offset
 // to the K range): the operand scales cover these K columns / rows only
 int mixed_zgemm_k(MixedWork *w, int mode, int S, const MatRef &A, const MatRef &B, const MatRef &C,

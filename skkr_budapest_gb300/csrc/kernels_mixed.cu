@@ -762,11 +762,21 @@ size_t oz_smem_bytes(int S) {
 }  // namespace
 
 // ---------------------------------------------------------------------------
+// Split operands live in staging slots (MIXED_SLOTS per side) so that an
+// operand used by several products is split once.  A slot records the layout
+// its zero padding was made for and the slices / digit base of its contents.
+struct Stage {
+  void *p = nullptr;       // [item][S][kblocks][rows][32] bf16 slices
+  size_t cap = 0;
+  int *scale = nullptr;    // row (A) / column (B) scale exponents
+  size_t scap = 0;
+  int n = -1, K = -1;      // padding layout
+  int S = 0, DB = 0;
+  long long items = 0;
+};
+
 struct MixedWork {
-  void *sa = nullptr, *sb = nullptr;  // slice staging
-  size_t sa_cap = 0, sb_cap = 0;
-  int *sigma = nullptr, *tau = nullptr;
-  size_t sig_cap = 0, tau_cap = 0;
+  Stage A[MIXED_SLOTS], B[MIXED_SLOTS];
   zd *acopy = nullptr, *rbuf = nullptr;
   size_t ac_cap = 0, rb_cap = 0;
   double *rnorm = nullptr;
@@ -774,7 +784,6 @@ struct MixedWork {
   int *err = nullptr;
   unsigned long long *dmax = nullptr;  // running max of Newton residual norms (double bits)
   int smem_set[16] = {0};
-  int last_n = -1, last_k = -1;   // staging layout the zero padding was made for
 };
 
 static int grow(void **p, size_t *cap, size_t bytes, bool zero) {
@@ -818,7 +827,12 @@ int mixed_resid_read(MixedWork *w, double *out, cudaStream_t st) {
 
 void mixed_destroy(MixedWork *w) {
   if (!w) return;
-  void *ps[] = {w->sa, w->sb, w->sigma, w->tau, w->acopy, w->rbuf, w->rnorm, w->err, w->dmax};
+  for (int i = 0; i < MIXED_SLOTS; i++) {
+    void *q[] = {w->A[i].p, w->A[i].scale, w->B[i].p, w->B[i].scale};
+    for (void *p : q)
+      if (p) cudaFree(p);
+  }
+  void *ps[] = {w->acopy, w->rbuf, w->rnorm, w->err, w->dmax};
   for (void *p : ps)
     if (p) cudaFree(p);
   delete w;
@@ -840,45 +854,66 @@ static void oz_dims(int n, int K, int *Mp, int *Np, int *Kp, int *mtiles, int *n
   *Kp = *kblocks * KB;
 }
 
+// digit base for depth K: 8 bits while 2K <= 256 (8 slices then act as 7:
+// the fixed-point value is limited to 62 bits), 7 bits above so that the FP32
+// level sums stay exact integers
+static void oz_digits(int S, int K, int *Se, int *DB) {
+  *DB = K <= 128 ? 8 : 7;
+  *Se = (*DB == 8 && S > 7) ? 7 : S;
+}
+
 template <int S, int DB>
-static int zgemm_s(MixedWork *w, int mode, const MatRef &A, const MatRef &B, const MatRef &C,
-                   const MatRef &D, const MatRef &E, int n, int K, int nk, int nc, const int *act,
-                   cudaStream_t st) {
+static int split_s(MixedWork *w, int side, int slot, const MatRef &M, int n, int K, int nk, int nc,
+                   const int *act, cudaStream_t st) {
+  int Mp, Np, Kp, mtiles, ntiles, kblocks;
+  oz_dims(n, K, &Mp, &Np, &Kp, &mtiles, &ntiles, &kblocks);
+  const long long items = (long long)nk * nc;
+  Stage &sg = side == 0 ? w->A[slot] : w->B[slot];
+  const int rows = side == 0 ? Mp : Np;
+  int rc;
+  if ((rc = grow(&sg.p, &sg.cap, (size_t)items * S * rows * Kp * 2, true))) return rc;
+  if ((rc = grow((void **)&sg.scale, &sg.scap, (size_t)items * (side == 0 ? Mp : n) * sizeof(int), false)))
+    return rc;
+  if (sg.n != n || sg.K != K) {
+    // padding (rows beyond the operand, columns >= 2K of every slice region)
+    // must be zero; a new layout clears what an earlier one wrote there
+    if (cudaMemsetAsync(sg.p, 0, sg.cap, st) != cudaSuccess) return SKKR_ERR_CUDA;
+    sg.n = n;
+    sg.K = K;
+  }
+  const long long active_s = act ? skkr_active_items(items) : items;
+  // split traffic: FP64 operand read + S bf16 slices of the real embedding written
+  const double split_bytes = (double)active_s * n * K * (16.0 + S * 2.0 * 2.0);
+  if (side == 0) {
+    dim3 ga((n + 31) / 32, items);
+    kstat_begin(KS_OTHER, split_bytes, st);
+    k_split_a<S, DB><<<ga, 256, 0, st>>>(M, n, K, nc, act, (__nv_bfloat16 *)sg.p, Mp, Kp, sg.scale);
+  } else {
+    dim3 gb((n + 7) / 8, items);
+    kstat_begin(KS_OTHER, 2.0 * split_bytes, st);
+    k_split_b<S, DB><<<gb, 256, 0, st>>>(M, n, K, nc, act, (__nv_bfloat16 *)sg.p, Np, Kp, sg.scale);
+  }
+  kstat_end(st);
+  SKKR_LAUNCHED();
+  sg.S = S;
+  sg.DB = DB;
+  sg.items = items;
+  return 0;
+}
+
+template <int S>
+static int gemm_s(MixedWork *w, int mode, int sa, int sb, const MatRef &C, const MatRef &D, const MatRef &E,
+                  int n, int K, int nk, int nc, const int *act, cudaStream_t st) {
   if (get_encoder()) return SKKR_ERR_CUDA;
   int Mp, Np, Kp, mtiles, ntiles, kblocks;
   oz_dims(n, K, &Mp, &Np, &Kp, &mtiles, &ntiles, &kblocks);
   const long long items = (long long)nk * nc;
-  int rc;
-  // staging sized for S slices; the zero padding is redone when the layout changes
-  if ((rc = grow(&w->sa, &w->sa_cap, (size_t)items * S * Mp * Kp * 2, true))) return rc;
-  if ((rc = grow(&w->sb, &w->sb_cap, (size_t)items * S * Np * Kp * 2, true))) return rc;
-  if (w->last_n != n || w->last_k != K) {
-    // padding (row >= n, column >= 2K of every slice region) must be zero;
-    // the region layout depends on n and K only, so a new layout clears what
-    // an earlier one wrote there
-    if (cudaMemsetAsync(w->sa, 0, w->sa_cap, st) != cudaSuccess ||
-        cudaMemsetAsync(w->sb, 0, w->sb_cap, st) != cudaSuccess)
-      return SKKR_ERR_CUDA;
-    w->last_n = n;
-    w->last_k = K;
-  }
-  if ((rc = grow((void **)&w->sigma, &w->sig_cap, (size_t)items * Mp * sizeof(int), false))) return rc;
-  if ((rc = grow((void **)&w->tau, &w->tau_cap, (size_t)items * n * sizeof(int), false))) return rc;
-  const long long active_s = act ? skkr_active_items(items) : items;
-  // split traffic: FP64 operand read + S bf16 slices of the real embedding written
-  const double split_bytes = (double)active_s * n * K * (16.0 + S * 2.0 * 2.0);
-  dim3 ga((n + 31) / 32, items);
-  kstat_begin(KS_OTHER, split_bytes, st);
-  k_split_a<S, DB><<<ga, 256, 0, st>>>(A, n, K, nc, act, (__nv_bfloat16 *)w->sa, Mp, Kp, w->sigma);
-  kstat_end(st);
-  SKKR_LAUNCHED();
-  dim3 gb((n + 7) / 8, items);
-  kstat_begin(KS_OTHER, 2.0 * split_bytes, st);
-  k_split_b<S, DB><<<gb, 256, 0, st>>>(B, n, K, nc, act, (__nv_bfloat16 *)w->sb, Np, Kp, w->tau);
-  kstat_end(st);
-  SKKR_LAUNCHED();
+  const Stage &A = w->A[sa], &B = w->B[sb];
+  if (A.S != S || B.S != S || A.DB != B.DB || A.n != n || B.n != n || A.K != K || B.K != K ||
+      A.items != items || B.items != items)
+    return SKKR_ERR_ARG;  // the slots do not hold splits of this product's operands
   CUtensorMap ma, mb;
-  if (make_map(&ma, w->sa, Mp, items * S * kblocks, MT) || make_map(&mb, w->sb, Np, items * S * kblocks, NT))
+  if (make_map(&ma, A.p, Mp, items * S * kblocks, MT) || make_map(&mb, B.p, Np, items * S * kblocks, NT))
     return SKKR_ERR_CUDA;
   const size_t smem = oz_smem_bytes(S);
   if (!w->smem_set[S]) {
@@ -894,9 +929,9 @@ static int zgemm_s(MixedWork *w, int mode, const MatRef &A, const MatRef &B, con
   g.kblocks = kblocks;
   g.nc = nc;
   g.mode = mode;
-  g.eoff = 32 + 2 * (DB - 1);
-  g.sigma = w->sigma;
-  g.tau = w->tau;
+  g.eoff = 32 + 2 * (A.DB - 1);
+  g.sigma = A.scale;
+  g.tau = B.scale;
   g.C = C;
   g.D = D;
   g.E = E;
@@ -912,30 +947,57 @@ static int zgemm_s(MixedWork *w, int mode, const MatRef &A, const MatRef &B, con
   return 0;
 }
 
-int mixed_zgemm_k(MixedWork *w, int mode, int S, const MatRef &A, const MatRef &B, const MatRef &C,
-                  const MatRef &D, const MatRef &E, int n, int K, int nk, int nc, const int *act,
-                  cudaStream_t st) {
-  if (n < 1 || n > 256 || K < 1 || K > 256 || nk * (long long)nc > 65535) return SKKR_ERR_ARG;
-  if (K <= 128) {  // 2K <= 256: 8-bit digits (8 slices would exceed the 62-bit value: use 7)
-    switch (S) {
-      case 3: return zgemm_s<3, 8>(w, mode, A, B, C, D, E, n, K, nk, nc, act, st);
-      case 4: return zgemm_s<4, 8>(w, mode, A, B, C, D, E, n, K, nk, nc, act, st);
-      case 5: return zgemm_s<5, 8>(w, mode, A, B, C, D, E, n, K, nk, nc, act, st);
-      case 6: return zgemm_s<6, 8>(w, mode, A, B, C, D, E, n, K, nk, nc, act, st);
-      case 7:
-      case 8: return zgemm_s<7, 8>(w, mode, A, B, C, D, E, n, K, nk, nc, act, st);
+int mixed_split(MixedWork *w, int side, int slot, int S, const MatRef &M, int n, int K, int nk, int nc,
+                const int *act, cudaStream_t st) {
+  if (n < 1 || n > 256 || K < 1 || K > 256 || nk * (long long)nc > 65535 || slot < 0 ||
+      slot >= MIXED_SLOTS || (side != 0 && side != 1))
+    return SKKR_ERR_ARG;
+  int Se, DB;
+  oz_digits(S, K, &Se, &DB);
+  if (DB == 8) {
+    switch (Se) {
+      case 3: return split_s<3, 8>(w, side, slot, M, n, K, nk, nc, act, st);
+      case 4: return split_s<4, 8>(w, side, slot, M, n, K, nk, nc, act, st);
+      case 5: return split_s<5, 8>(w, side, slot, M, n, K, nk, nc, act, st);
+      case 6: return split_s<6, 8>(w, side, slot, M, n, K, nk, nc, act, st);
+      case 7: return split_s<7, 8>(w, side, slot, M, n, K, nk, nc, act, st);
       default: return SKKR_ERR_ARG;
     }
   }
-  switch (S) {  // 2K > 256: 7-bit digits keep the level sums exact
-    case 3: return zgemm_s<3, 7>(w, mode, A, B, C, D, E, n, K, nk, nc, act, st);
-    case 4: return zgemm_s<4, 7>(w, mode, A, B, C, D, E, n, K, nk, nc, act, st);
-    case 5: return zgemm_s<5, 7>(w, mode, A, B, C, D, E, n, K, nk, nc, act, st);
-    case 6: return zgemm_s<6, 7>(w, mode, A, B, C, D, E, n, K, nk, nc, act, st);
-    case 7: return zgemm_s<7, 7>(w, mode, A, B, C, D, E, n, K, nk, nc, act, st);
-    case 8: return zgemm_s<8, 7>(w, mode, A, B, C, D, E, n, K, nk, nc, act, st);
+  switch (Se) {
+    case 3: return split_s<3, 7>(w, side, slot, M, n, K, nk, nc, act, st);
+    case 4: return split_s<4, 7>(w, side, slot, M, n, K, nk, nc, act, st);
+    case 5: return split_s<5, 7>(w, side, slot, M, n, K, nk, nc, act, st);
+    case 6: return split_s<6, 7>(w, side, slot, M, n, K, nk, nc, act, st);
+    case 7: return split_s<7, 7>(w, side, slot, M, n, K, nk, nc, act, st);
+    case 8: return split_s<8, 7>(w, side, slot, M, n, K, nk, nc, act, st);
     default: return SKKR_ERR_ARG;
   }
+}
+
+int mixed_gemm_staged(MixedWork *w, int mode, int S, int sa, int sb, const MatRef &C, const MatRef &D,
+                      const MatRef &E, int n, int K, int nk, int nc, const int *act, cudaStream_t st) {
+  if (sa < 0 || sa >= MIXED_SLOTS || sb < 0 || sb >= MIXED_SLOTS) return SKKR_ERR_ARG;
+  int Se, DB;
+  oz_digits(S, K, &Se, &DB);
+  switch (Se) {
+    case 3: return gemm_s<3>(w, mode, sa, sb, C, D, E, n, K, nk, nc, act, st);
+    case 4: return gemm_s<4>(w, mode, sa, sb, C, D, E, n, K, nk, nc, act, st);
+    case 5: return gemm_s<5>(w, mode, sa, sb, C, D, E, n, K, nk, nc, act, st);
+    case 6: return gemm_s<6>(w, mode, sa, sb, C, D, E, n, K, nk, nc, act, st);
+    case 7: return gemm_s<7>(w, mode, sa, sb, C, D, E, n, K, nk, nc, act, st);
+    case 8: return gemm_s<8>(w, mode, sa, sb, C, D, E, n, K, nk, nc, act, st);
+    default: return SKKR_ERR_ARG;
+  }
+}
+
+int mixed_zgemm_k(MixedWork *w, int mode, int S, const MatRef &A, const MatRef &B, const MatRef &C,
+                  const MatRef &D, const MatRef &E, int n, int K, int nk, int nc, const int *act,
+                  cudaStream_t st) {
+  int rc = mixed_split(w, 0, 0, S, A, n, K, nk, nc, act, st);
+  if (!rc) rc = mixed_split(w, 1, 0, S, B, n, K, nk, nc, act, st);
+  if (!rc) rc = mixed_gemm_staged(w, mode, S, 0, 0, C, D, E, n, K, nk, nc, act, st);
+  return rc;
 }
 
 int mixed_zgemm(MixedWork *w, int mode, int S, const MatRef &A, const MatRef &B, const MatRef &C,
@@ -989,15 +1051,20 @@ int mixed_zinv(MixedWork *w, const MatRef &A, const MatRef &X, int n, int nk, in
   else k_cgj32<32, 4, 8><<<(unsigned)items, 512, 0, st>>>(Ac, X, n, nc, act);
   kstat_end(st);
   SKKR_LAUNCHED();
+  // A is split once (A slot 0) for the residuals of every Newton step
+  if ((rc = mixed_split(w, 0, 0, sres, Ac, n, n, nk, nc, act, st))) return rc;
   for (int it = 0; it < newton; it++) {
     // R = I - A X
-    if ((rc = mixed_zgemm(w, 4, sres, Ac, X, R, R, R, n, nk, nc, act, st))) return rc;
+    if ((rc = mixed_split(w, 1, 0, sres, X, n, n, nk, nc, act, st))) return rc;
+    if ((rc = mixed_gemm_staged(w, 4, sres, 0, 0, R, R, R, n, n, nk, nc, act, st))) return rc;
     if (track_resid && it == newton - 1) {
       k_fnorm_max<<<(unsigned)items, 256, 0, st>>>(R, n, nc, act, w->dmax);
       SKKR_LAUNCHED();
     }
-    // X = X + X R
-    if ((rc = mixed_zgemm(w, 5, 3, X, R, X, X, X, n, nk, nc, act, st))) return rc;
+    // X = X + X R (slot 5: slot 0 keeps A)
+    if ((rc = mixed_split(w, 0, 5, 3, X, n, n, nk, nc, act, st))) return rc;
+    if ((rc = mixed_split(w, 1, 5, 3, R, n, n, nk, nc, act, st))) return rc;
+    if ((rc = mixed_gemm_staged(w, 5, 3, 5, 5, X, X, X, n, n, nk, nc, act, st))) return rc;
   }
   return 0;
 }
