@@ -96,8 +96,12 @@ typedef struct {
   int max_dec_iters;          /* largest decimation iteration count */
   long long dec_iters_total;  /* summed decimation iterations */
   long long gpu_launches;     /* kernels launched by this call */
-  double max_refine_resid;    /* mixed precision: largest final refinement residual */
+  double max_refine_resid;    /* mixed precision: largest accepted Newton residual |I - AX|_F
+                                 (before the last correction) */
   double run_ms;              /* device time of the call (CUDA events on the library stream) */
+  long long inv_fallbacks;    /* mixed precision: inverses whose residual stayed above 1e-6
+                                 and were redone in FP64 */
+  long long k_fp64;           /* mixed precision: k points redone in FP64 (dominant contributions) */
 } skkr_status;
 
 typedef struct skkr_ctx skkr_ctx;
@@ -106,6 +110,17 @@ typedef struct skkr_ctx skkr_ctx;
  * arrays xsave, ysave, g2d of cpacoord_ksave.f:86). */
 int skkr_gpu_create(const skkr_sizes *sizes, skkr_ctx **ctx);
 int skkr_gpu_destroy(skkr_ctx *ctx);
+
+/* Split-precision policy near the real axis, where the lead and slab
+ * matrices become ill-conditioned and rounding of the products is amplified
+ * by their condition number: decimation runs in FP64 when |Im E| < dec_fp64_im
+ * (default 1e-3 Ry); the products use slices_near BF16 slices on the
+ * exact-level tile when |Im E| < near_im (default: never; 3..8, 0 = off);
+ * every k point whose contribution exceeds dominant_frac (default 1e-2) of
+ * the norm of the k-summed tau is recomputed in FP64 (0 = off).  Inverses
+ * whose Newton residual stays above 1e-6 are always redone in FP64. */
+int skkr_gpu_set_mixed_policy(skkr_ctx *ctx, double dec_fp64_im, double near_im, int slices_near,
+                              double dominant_frac);
 
 /* Host reduction for an energy whose k points are split over ranks (the
  * modulo(ik-1,nprocs) split of cpacoord_ksave.f:189 with the mpi_allreduce of

@@ -48,6 +48,14 @@ class Context:
         return cls(ep.irel, ep.lmax, ep.nprc, ep.ninprc, len(ep.lg), ep.itermaxl, ep.itermaxr, ep.errmax,
                    ep.itcpam, ep.cpatol, precision, nk_chunk, slices)
 
+    def set_mixed_policy(self, dec_fp64_im=1e-3, near_im=0.0, slices_near=0, dominant_frac=1e-2):
+        """Precision near the real axis (skkr_gpu_set_mixed_policy): FP64
+        decimation below |Im E| = dec_fp64_im, slices_near BF16 slices for the
+        products below |Im E| = near_im, FP64 redo of every k point carrying
+        more than dominant_frac of the k-summed tau."""
+        N._check(N.lib().skkr_gpu_set_mixed_policy(self.h, dec_fp64_im, near_im, slices_near, dominant_frac),
+                 "skkr_gpu_set_mixed_policy")
+
     def set_reduce(self, fn):
         """Make this context one rank of a k-split energy: fn(buf) must sum
         the float64 host buffer over the ranks in place (an allreduce) and is
@@ -155,6 +163,7 @@ class Context:
         res.update(status=rc, cpa_iterations=st.cpa_iterations, cpa_error=st.cpa_error,
                    max_dec_iters=st.max_dec_iters, dec_iters_total=st.dec_iters_total,
                    gpu_launches=st.gpu_launches, ik=st.ik, run_ms=st.run_ms,
+                   max_refine_resid=st.max_refine_resid, inv_fallbacks=st.inv_fallbacks, k_fp64=st.k_fp64,
                    h2d_bytes=sum(v.nbytes for v in a.values()) + rt.gR.nbytes + rt.rvec.nbytes,
                    d2h_bytes=sum(v.nbytes for v in out.values()))
         return res

@@ -123,7 +123,8 @@ def warm_start(ep, model: Model, prev=None) -> np.ndarray:
 
 
 def _spec(seed: int, lmax: int = 3):
-    spec = W.rel_bcc_cpa(nsets=[4] * 24)
+    # the committed models were trained on the j-split (0.03 Ry) inputs
+    spec = W.rel_bcc_cpa(nsets=[4] * 24, so_split=0.03)
     spec.seed = seed
     spec.lmax = lmax
     return spec

@@ -211,10 +211,19 @@ struct skkr_ctx {
   std::vector<struct SlotStore *> slots;
   MixedWork *mw = nullptr;   // split-precision engine (precision == SKKR_MIXED)
   int slices = 6, slices_res = 7;  // BF16 slices of products / of Newton residuals
+  // split-precision policy near the real axis (skkr_gpu_set_mixed_policy)
+  double dec_fp64_im = 1.0e-3;   // decimation in FP64 when |Im E| is below
+  double near_im = 0.0;          // products use slices_near when |Im E| is below
+  int slices_near = 0;
+  double dominant_frac = 1.0e-2; // k points carrying more of |sum_k tau_k| are redone in FP64
+  bool force_fp64 = false;       // set while such a k point is redone
+  DBuf knorm;                    // [nk] norms of the k-resolved tau contributions
+  long long k_fp64 = 0;          // k points redone in FP64 in this run
   skkr_reduce_fn red_fn = nullptr;  // host allreduce of tauc for a k-split energy
   void *red_user = nullptr;
   std::vector<double> red_buf;
-  double max_resid = 0.0;    // largest Newton residual seen in this run
+  double max_resid = 0.0;    // largest accepted Newton residual seen in this run
+  long long inv_fallbacks = 0;  // inverses redone in FP64 in this run
 };
 
 // Inputs and outputs of one staged energy.  A context keeps any number of
@@ -619,6 +628,11 @@ static int ehsplit(const skkr_ctx *c) {
   return c->sz.mode == SKKR_BDG && c->sz.precision == SKKR_MIXED;
 }
 
+// slices of the products of the staged energy (more near the real axis)
+static int slices_for(const skkr_ctx *c) {
+  return (c->slices_near > 0 && std::fabs(c->ce.y) < c->near_im) ? c->slices_near : c->slices;
+}
+
 static MatRef offset(const MatRef &m, long long elems) {
   MatRef r = m;
   r.base += elems;
@@ -639,11 +653,11 @@ static int eng_gemm(skkr_ctx *c, bool mixed, int mode, const MatRef &A, const Ma
       case 4: m2 = 1; break;   // C = I - A1 B1, then C -= A2 B2
       default: m2 = mode;      // 1 (C -=), 2 (D -=, E -=), 5 (C +=) are additive per half
     }
-    int rc = mixed_zgemm_k(c->mw, mode, c->slices, A, B, C, D, E, n, h, nk, nc, act, c->st);
+    int rc = mixed_zgemm_k(c->mw, mode, slices_for(c), A, B, C, D, E, n, h, nk, nc, act, c->st);
     if (rc) return rc;
-    return mixed_zgemm_k(c->mw, m2, c->slices, A2, B2, C, D, E, n, h, nk, nc, act, c->st);
+    return mixed_zgemm_k(c->mw, m2, slices_for(c), A2, B2, C, D, E, n, h, nk, nc, act, c->st);
   }
-  if (mixed) return mixed_zgemm(c->mw, mode, c->slices, A, B, C, D, E, n, nk, nc, act, c->st);
+  if (mixed) return mixed_zgemm(c->mw, mode, slices_for(c), A, B, C, D, E, n, nk, nc, act, c->st);
   launch_zgemm(mode, A, B, C, D, E, n, n, n, nk, nc, act, c->st);
   return SKKR_OK;
 }
@@ -652,18 +666,20 @@ static int eng_gemm(skkr_ctx *c, bool mixed, int mode, const MatRef &A, const Ma
 static int eng_inv(skkr_ctx *c, bool mixed, const MatRef &A, const MatRef &X, bool inplace, int n, int nk,
                    int nc, const int *act) {
   if (mixed && n <= 128)
-    return mixed_zinv(c->mw, A, X, n, nk, nc, act, 2, c->slices_res, true, c->st);
+    return mixed_zinv(c->mw, A, X, n, nk, nc, act, 2, std::min(8, std::max(c->slices_res, slices_for(c) + 1)),
+                      true, c->st);
   if (!inplace) launch_zaxpby(X, A, nullptr, 0, nullptr, 0, n, nk, nc, act, c->st);
   launch_zgj(X, n, nk, nc, act, c->st);
   return SKKR_OK;
 }
 
 static bool use_mixed(const skkr_ctx *c, bool decimation) {
-  if (c->sz.precision != SKKR_MIXED) return false;
-  // decimation within 1e-3 Ry of the real axis stays in FP64
-  if (decimation && std::fabs(c->ce.y) < 1.0e-3) return false;
+  if (c->sz.precision != SKKR_MIXED || c->force_fp64) return false;
+  // decimation near the real axis stays in FP64 (default: within 1e-3 Ry)
+  if (decimation && std::fabs(c->ce.y) < c->dec_fp64_im) return false;
   return true;
 }
+
 
 // ---------------------------------------------------------------------------
 // decimation (main/dugo.f + main/surfgf.f) for the k points [k0, k0+nkc)
@@ -733,7 +749,7 @@ static int run_decimation(skkr_ctx *c, int k0, int nkc, const std::vector<int> &
       // split-precision engine: each operand split once (B slots 1-3: y1,
       // alfa, beta; A slots 1-4: alfa, beta, P, Q) for the six products
       MixedWork *w = c->mw;
-      const int S = c->slices;
+      const int S = slices_for(c);
       CKR(mixed_split(w, 1, 1, S, y1, n, n, nkc, nc, act, st));
       CKR(mixed_split(w, 0, 1, S, ac, n, n, nkc, nc, act, st));
       CKR(mixed_split(w, 0, 2, S, bc, n, n, nkc, nc, act, st));
@@ -845,7 +861,7 @@ static int run_tau2d(skkr_ctx *c, int k0, int nkc, const std::vector<int> &icls)
   // B slot 3 = M10); the per-step operands use slot 2
   const bool staged = mx && !ehsplit(c);
   MixedWork *w = c->mw;
-  const int S = c->slices;
+  const int S = slices_for(c);
   auto prod = [&](int sa, const MatRef *A, int sb, const MatRef *B, const MatRef &C) -> int {
     if (A) CKR(mixed_split(w, 0, sa, S, *A, n, n, nkc, nc, nullptr, st));
     if (B) CKR(mixed_split(w, 1, sb, S, *B, n, n, nkc, nc, nullptr, st));
@@ -1050,6 +1066,105 @@ static int reduce_tauc(skkr_ctx *c, bool failed) {
   return SKKR_OK;
 }
 
+// Accuracy guard of the split-precision path: near the real axis a few k
+// points sit close to an interface resonance, carry much of |sum_k tau_k| and
+// see the product rounding amplified by their conditioning.  Every k whose
+// contribution exceeds dominant_frac of the k-summed norm is recomputed in
+// FP64 and its contribution swapped in the class sums: the selected k are
+// gathered into compact buffers (structure-constant blocks, cached surface
+// operators, weights) that stand in for the context's, their mixed
+// contribution is recomputed from the same cached state and subtracted, the
+// decimation and tau2d are redone in FP64 and added, and the FP64 surface
+// operators are scattered back for the later CPA iterations.
+static int redo_dominant_k(skkr_ctx *c, int itcpa, const std::vector<int> &lcls, const std::vector<int> &rcls,
+                           const std::vector<int> &icls) {
+  (void)itcpa;
+  const int nk = c->nk, ni = c->nintfc, lk2 = c->lk * c->lk, ncls = (int)icls.size();
+  const long long E = (long long)ncls * ni * lk2;
+  const size_t bs = (size_t)c->lmmax * c->lmmax, gk = (size_t)c->nbk * bs;
+  const size_t sk = (size_t)c->nsl * c->n * c->n;   // SSPO elements per k
+  cudaStream_t st = c->st;
+  std::vector<double> kn(nk);
+  std::vector<zd> Sh((size_t)E);
+  CK(cudaMemcpyAsync(kn.data(), c->knorm.p, nk * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(Sh.data(), c->S.p, (size_t)E * sizeof(zd), cudaMemcpyDeviceToHost, st));
+  std::vector<double> wkh(nk);
+  CK(cudaMemcpyAsync(wkh.data(), c->wk.p, nk * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  double s2 = 0.0;
+  for (const zd &v : Sh) s2 += v.x * v.x + v.y * v.y;
+  const double lim = c->dominant_frac * std::sqrt(s2);
+  std::vector<int> sel;
+  for (int k = 0; k < nk; k++)
+    if (kn[k] > lim) sel.push_back(k);
+  if (sel.empty()) return SKKR_OK;
+  DBuf Gc, Sc, Wc, T;
+  struct Release {  // compact buffers are local (cudaFree waits for their last use)
+    DBuf *b[4];
+    ~Release() {
+      for (DBuf *x : b) x->release();
+    }
+  } release_on_return{{&Gc, &Sc, &Wc, &T}};
+  for (size_t g0 = 0; g0 < sel.size(); g0 += (size_t)c->kc) {
+    const int m = (int)std::min<size_t>((size_t)c->kc, sel.size() - g0);
+    CKR(Gc.ensure((size_t)m * gk * sizeof(zd)));
+    CKR(Sc.ensure((size_t)m * sk * sizeof(zd)));
+    CKR(Wc.ensure((size_t)m * sizeof(double)));
+    CKR(T.ensure((size_t)E * sizeof(zd)));
+    std::vector<double> w(m);
+    for (int i = 0; i < m; i++) {
+      const int k = sel[g0 + i];
+      w[i] = wkh[k];
+      CK(cudaMemcpyAsync(Gc.as<zd>() + (size_t)i * gk, c->G.as<zd>() + (size_t)k * gk, gk * sizeof(zd),
+                         cudaMemcpyDeviceToDevice, st));
+      CK(cudaMemcpyAsync(Sc.as<zd>() + (size_t)i * sk, c->sspo.as<zd>() + (size_t)k * sk, sk * sizeof(zd),
+                         cudaMemcpyDeviceToDevice, st));
+    }
+    CK(cudaMemcpyAsync(Wc.p, w.data(), m * sizeof(double), cudaMemcpyHostToDevice, st));
+    std::swap(c->G, Gc);
+    std::swap(c->sspo, Sc);
+    std::swap(c->wk, Wc);
+    int rc = SKKR_OK;
+    launch_pack(c->G.as<zd>(), c->nblk, c->nbk, c->blkmap_d.as<int>(), c->mi, c->jmax, c->jobs.as<PackJob>(),
+                c->nmat, c->lk, c->lmmax, c->sz.mode, c->fac, c->fach, m, c->pool.as<zd>(), c->nmat, c->n,
+                ehsplit(c), st);
+    rc = run_tau2d(c, 0, m, icls);            // the mixed contributions summed above
+    if (rc == SKKR_OK) {
+      launch_ksum(c->tauk.as<zd>(), m, E, T.as<zd>(), 0, st);
+      launch_axpy_flat(c->S.as<zd>(), T.as<zd>(), E, -1.0, st);
+      c->force_fp64 = true;
+      rc = run_decimation(c, 0, m, lcls, rcls);
+      if (c->err_code && c->first_bad_k >= 0 && c->first_bad_k < m) c->first_bad_k = sel[g0 + c->first_bad_k];
+      if (rc == SKKR_OK && !c->err_code) rc = run_tau2d(c, 0, m, icls);
+      c->force_fp64 = false;
+    }
+    std::swap(c->G, Gc);
+    std::swap(c->sspo, Sc);
+    std::swap(c->wk, Wc);
+    if (rc != SKKR_OK) return rc;
+    if (c->err_code) return SKKR_OK;
+    launch_ksum(c->tauk.as<zd>(), m, E, T.as<zd>(), 0, st);
+    launch_axpy_flat(c->S.as<zd>(), T.as<zd>(), E, 1.0, st);
+    for (int i = 0; i < m; i++)
+      CK(cudaMemcpyAsync(c->sspo.as<zd>() + (size_t)sel[g0 + i] * sk, Sc.as<zd>() + (size_t)i * sk,
+                         sk * sizeof(zd), cudaMemcpyDeviceToDevice, st));
+    c->k_fp64 += m;
+  }
+  return SKKR_OK;
+}
+
+extern "C" int skkr_gpu_set_mixed_policy(skkr_ctx *c, double dec_fp64_im, double near_im, int slices_near,
+                                         double dominant_frac) {
+  if (!c || dec_fp64_im < 0.0 || near_im < 0.0 || (slices_near != 0 && (slices_near < 3 || slices_near > 8)) ||
+      dominant_frac < 0.0)
+    return SKKR_ERR_ARG;
+  c->dec_fp64_im = dec_fp64_im;
+  c->near_im = near_im;
+  c->slices_near = slices_near;
+  c->dominant_frac = dominant_frac;
+  return SKKR_OK;
+}
+
 extern "C" int skkr_gpu_set_reduce(skkr_ctx *c, skkr_reduce_fn fn, void *user) {
   if (!c) return SKKR_ERR_ARG;
   c->red_fn = fn;
@@ -1073,11 +1188,17 @@ extern "C" int skkr_gpu_run(skkr_ctx *c, skkr_status *status) {
   c->err_code = 0;
   c->first_bad_k = -1;
   c->max_resid = 0.0;
+  c->k_fp64 = 0;
+  CKR(c->knorm.ensure((size_t)nk * sizeof(double)));
   if (c->sz.precision == SKKR_MIXED && !c->mw) {
     c->mw = mixed_create();
     if (!c->mw) return SKKR_ERR_NOMEM;
   }
-  if (c->mw) CKR(mixed_resid_reset(c->mw, st));
+  if (c->mw) {
+    CKR(mixed_resid_reset(c->mw, st));
+    // near the real axis the products also run on the exact-level tile
+    mixed_set_precise(c->mw, c->slices_near > 0 && std::fabs(c->ce.y) < c->near_im);
+  }
   plan_pack(c);
   CKR(c->jobs.ensure(c->jobs_h.size() * sizeof(PackJob)));
   CK(cudaMemcpyAsync(c->jobs.p, c->jobs_h.data(), c->jobs_h.size() * sizeof(PackJob),
@@ -1136,7 +1257,11 @@ extern "C" int skkr_gpu_run(skkr_ctx *c, skkr_status *status) {
       if (c->err_code) break;
       CKR(run_tau2d(c, k0, nkc, icls));
       launch_ksum(c->tauk.as<zd>(), nkc, (long long)ncls * ni * lk2, c->S.as<zd>(), k0 > 0, st);
+      if (c->sz.precision == SKKR_MIXED && c->dominant_frac > 0.0)
+        launch_knorm(c->tauk.as<zd>(), nkc, (long long)ncls * ni * lk2, c->knorm.as<double>() + k0, st);
     }
+    if (!c->err_code && c->sz.precision == SKKR_MIXED && c->dominant_frac > 0.0)
+      CKR(redo_dominant_k(c, itcpa, lcls, rcls, icls));
     if (c->err_code) {
       if (c->red_fn) reduce_tauc(c, true);  // tell the other ranks before returning
       break;
@@ -1177,7 +1302,8 @@ extern "C" int skkr_gpu_run(skkr_ctx *c, skkr_status *status) {
     if (!(concpa && cpacon)) break;
   }
   trace_point("after CPA loop");
-  if (c->mw) CKR(mixed_resid_read(c->mw, &c->max_resid, st));
+  c->inv_fallbacks = 0;
+  if (c->mw) CKR(mixed_resid_read(c->mw, &c->max_resid, &c->inv_fallbacks, st));
   if (c->mw && c->err_code == 0) {
     int f = mixed_error_flag(c->mw);
     if (f != 0) {
@@ -1202,6 +1328,8 @@ extern "C" int skkr_gpu_run(skkr_ctx *c, skkr_status *status) {
     status->gpu_launches = g_skkr_launches - l0;
     status->max_refine_resid = c->max_resid;
     status->run_ms = run_ms;
+    status->inv_fallbacks = c->inv_fallbacks;
+    status->k_fp64 = c->k_fp64;
   }
   return c->err_code;
 }
@@ -1643,7 +1771,7 @@ extern "C" int skkr_gpu_zinv_batch(int precision, int n, int batch, double *a, i
     double r = 0.0;
     int rc = mixed_resid_reset(w, 0);
     if (!rc) rc = mixed_zinv(w, Am, Am, n, batch, 1, nullptr, newton, 7, true, 0);
-    if (!rc) rc = mixed_resid_read(w, &r, 0);
+    if (!rc) rc = mixed_resid_read(w, &r, nullptr, 0);
     if (rc == SKKR_OK && cudaDeviceSynchronize() != cudaSuccess) rc = SKKR_ERR_CUDA;
     if (rc == SKKR_OK && mixed_error_flag(w) != 0) rc = SKKR_ERR_CUDA;
     mixed_destroy(w);

@@ -45,6 +45,9 @@ void launch_dec_state(const double *err, int *act, int *stat, int *iters, int ni
 void launch_extract_tau(const MatRef &W, int lk, int nl, int layer0, const double *wk,
                         double wscale, zd *out, long long out_sk, long long out_sc, int nk,
                         int nc, int ehsplit, cudaStream_t st);
+// per-k norms of k-resolved contributions tk[k][E] -> out[k]; S[e] += sign x[e]
+void launch_knorm(const zd *tk, int nk, long long E, double *out, cudaStream_t st);
+void launch_axpy_flat(zd *S, const zd *x, long long E, double sign, cudaStream_t st);
 // deterministic k-sum (warp-shuffle): S[e] (+)= sum_k tk[k*E + e]
 void launch_ksum(const zd *tk, int nk, long long E, zd *S, int accumulate, cudaStream_t st);
 // sum over g of T[layer][g] -> out[layer]
@@ -67,6 +70,9 @@ int mixed_error_flag(MixedWork *w);
 constexpr int MIXED_SLOTS = 6;
 int mixed_split(MixedWork *w, int side, int slot, int S, const MatRef &M, int n, int K, int nk, int nc,
                 const int *act, cudaStream_t st);
+// products of 6+ slices on 64-column tiles with 7 TMEM accumulators (levels
+// 0..5 exact): rounding below FP64's, for ill-conditioned energies
+void mixed_set_precise(MixedWork *w, bool on);
 int mixed_gemm_staged(MixedWork *w, int mode, int S, int sa, int sb, const MatRef &C, const MatRef &D,
                       const MatRef &E, int n, int K, int nk, int nc, const int *act, cudaStream_t st);
 // C (op) A[:, 0:K] B[0:K, :] for n x K by K x n blocks (A, B already offset
@@ -78,7 +84,8 @@ int mixed_zgemm(MixedWork *w, int mode, int S, const MatRef &A, const MatRef &B,
                 const MatRef &D, const MatRef &E, int n, int nk, int nc, const int *act, cudaStream_t st);
 int mixed_zinv(MixedWork *w, const MatRef &A, const MatRef &X, int n, int nk, int nc, const int *act,
                int newton, int sres, bool track_resid, cudaStream_t st);
-// running maximum of the final Newton residual norms (device scalar): reset
-// asynchronously, read with a stream synchronisation
+// running maximum of the accepted Newton residual norms and the count of
+// inverses redone in FP64 (device scalars): reset asynchronously, read with a
+// stream synchronisation
 int mixed_resid_reset(MixedWork *w, cudaStream_t st);
-int mixed_resid_read(MixedWork *w, double *out, cudaStream_t st);
+int mixed_resid_read(MixedWork *w, double *out, long long *fallbacks, cudaStream_t st);

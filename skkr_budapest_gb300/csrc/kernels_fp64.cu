@@ -568,6 +568,43 @@ void launch_ksum(const zd *tk, int nk, long long E, zd *S, int accumulate, cudaS
   SKKR_LAUNCHED();
 }
 
+// per-k Frobenius norm of the k-resolved contributions tk[k][E]
+__global__ void k_knorm(const zd *__restrict__ tk, long long E, double *__restrict__ out) {
+  const zd *t = tk + (long long)blockIdx.x * E;
+  double s = 0.0;
+  for (long long e = threadIdx.x; e < E; e += blockDim.x) s += t[e].x * t[e].x + t[e].y * t[e].y;
+  __shared__ double red[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    s = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (threadIdx.x == 0) out[blockIdx.x] = sqrt(s);
+  }
+}
+
+void launch_knorm(const zd *tk, int nk, long long E, double *out, cudaStream_t st) {
+  if (nk <= 0 || E <= 0) return;
+  k_knorm<<<nk, 256, 0, st>>>(tk, E, out);
+  SKKR_LAUNCHED();
+}
+
+// S[e] += sign * x[e]
+__global__ void k_axpy_flat(zd *__restrict__ S, const zd *__restrict__ x, long long E, double sign) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < E; e += (long long)gridDim.x * blockDim.x)
+    S[e] = make_double2(S[e].x + sign * x[e].x, S[e].y + sign * x[e].y);
+}
+
+void launch_axpy_flat(zd *S, const zd *x, long long E, double sign, cudaStream_t st) {
+  if (E <= 0) return;
+  const long long nb = (E + 255) / 256;
+  k_axpy_flat<<<(unsigned)(nb < 1024 ? nb : 1024), 256, 0, st>>>(S, x, E, sign);
+  SKKR_LAUNCHED();
+}
+
 __global__ void k_gsum(const zd *T, int ng, int lk, int nl, zd *out) {
   const int tot = nl * lk * lk;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += gridDim.x * blockDim.x) {

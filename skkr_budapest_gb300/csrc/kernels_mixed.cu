@@ -384,25 +384,32 @@ __device__ __forceinline__ double fix_to_double(long long a, int e) {
 // accumulator of product (p, q), 0-based slices: its level p+q; levels >= 4
 // share the last accumulator (they sit 2^-32 and further below the leading
 // level, so the truncation of the shared sum is far below the slice error)
-__host__ __device__ constexpr int level_of(int p, int q) { return p + q < NACC ? p + q : NACC - 1; }
+template <int NA>
+__host__ __device__ constexpr int level_of(int p, int q) { return p + q < NA ? p + q : NA - 1; }
 // accumulators in use for S slices (levels 0 .. S-1)
-__host__ __device__ constexpr int nlevels(int S) { return S < NACC ? S : NACC; }
+template <int NA>
+__host__ __device__ constexpr int nlevels(int S) { return S < NA ? S : NA; }
 
-template <int S>
+// TN: N tile (TMEM columns per accumulator); NA: TMEM accumulators, one per
+// level p+q = 0..NA-2 and a shared tail for the deeper levels (NA * TN <= 512).
+// (96, 5) is the default tile; (64, 7) keeps levels 0..5 exact and pushes the
+// truncation of the shared tail below 2^-60 of the leading level.
+template <int S, int TN, int NA>
 __global__ void __launch_bounds__(256, 1) k_ozaki(const __grid_constant__ CUtensorMap tmA,
                                                   const __grid_constant__ CUtensorMap tmB, OzArgs g) {
+  static_assert(NA * TN <= 512 && TN % 32 == 0, "accumulators must fit the 512 TMEM columns");
   const int item = blockIdx.y;
   if (g.act && !g.act[item]) return;
   const int mt = blockIdx.x / g.ntiles, nt = blockIdx.x % g.ntiles;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
-  // NSTAGE stages, each: S A tiles (MT x KB) then S B tiles (NT x KB), 1024-byte aligned
+  // NSTAGE stages, each: S A tiles (MT x KB) then S B tiles (TN x KB), 1024-byte aligned
   unsigned char *tiles = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  constexpr uint32_t A_BYTES = MT * KB * 2, B_BYTES = NT * KB * 2;
+  constexpr uint32_t A_BYTES = MT * KB * 2, B_BYTES = TN * KB * 2;
   constexpr uint32_t STAGE_BYTES = S * (A_BYTES + B_BYTES);
   __shared__ __align__(8) uint64_t bar_full[NSTAGE], bar_empty[NSTAGE], bar_acc;
   __shared__ uint32_t tmem_base;
   __shared__ volatile int failed, issued_kb, consumed_kb;
-  __shared__ int col_exp[NT / 2];  // column scale exponents of this tile's complex columns
+  __shared__ int col_exp[TN / 2];  // column scale exponents of this tile's complex columns
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
   if (warp == 0) {
@@ -410,8 +417,8 @@ __global__ void __launch_bounds__(256, 1) k_ozaki(const __grid_constant__ CUtens
     tmem_relinquish();
   }
   if (threadIdx.x >= 64) {  // warps 2-7: column scales of the tile (read by the epilogue)
-    for (int t = threadIdx.x - 64; t < NT / 2; t += blockDim.x - 64) {
-      const int j = (nt * NT) / 2 + t;
+    for (int t = threadIdx.x - 64; t < TN / 2; t += blockDim.x - 64) {
+      const int j = (nt * TN) / 2 + t;
       col_exp[t] = j < g.n ? g.tau[(long long)item * g.n + j] : 0;
     }
   }
@@ -431,7 +438,7 @@ __global__ void __launch_bounds__(256, 1) k_ozaki(const __grid_constant__ CUtens
   __syncthreads();
   tc_fence_after();
   const uint32_t tbase = tmem_base;
-  constexpr uint32_t IDESC = idesc_bf16(MT, NT);
+  constexpr uint32_t IDESC = idesc_bf16(MT, TN);
   const int nkb = g.kblocks;
 
   if (warp == 0 && lane == 0) {
@@ -448,13 +455,15 @@ __global__ void __launch_bounds__(256, 1) k_ozaki(const __grid_constant__ CUtens
       for (int sl = 0; sl < S; sl++) {
         const int z = (item * S + sl) * nkb + kb;
         tma_load_3d(sA + sl * A_BYTES, &tmA, 0, mt * MT, z, &bar_full[st]);
-        tma_load_3d(sB + sl * B_BYTES, &tmB, 0, nt * NT, z, &bar_full[st]);
+        tma_load_3d(sB + sl * B_BYTES, &tmB, 0, nt * TN, z, &bar_full[st]);
       }
       issued_kb = kb;
     }
   } else if (warp == 1 && lane == 0) {
     // MMA issuer
-    bool first[NACC] = {true, true, true, true, true};
+    bool first[NA];
+#pragma unroll
+    for (int l = 0; l < NA; l++) first[l] = true;
     for (int kb = 0; kb < nkb; kb++) {
       const int st = kb % NSTAGE;
       if (failed || !mbar_wait(&bar_full[st], (kb / NSTAGE) & 1)) {
@@ -468,10 +477,10 @@ __global__ void __launch_bounds__(256, 1) k_ozaki(const __grid_constant__ CUtens
 #pragma unroll
         for (int q = 0; q < S; q++) {
           if (p + q > S - 1) continue;  // keep p+q <= S+1 in 1-based slices
-          const int lv = level_of(p, q);
+          const int lv = level_of<NA>(p, q);
 #pragma unroll
           for (int k = 0; k < KB / 16; k++) {
-            umma_bf16(tbase + lv * NT, sdesc_sw64(a0 + p * A_BYTES + 32 * k),
+            umma_bf16(tbase + lv * TN, sdesc_sw64(a0 + p * A_BYTES + 32 * k),
                       sdesc_sw64(b0 + q * B_BYTES + 32 * k), IDESC, first[lv] ? 0u : 1u);
             first[lv] = false;
           }
@@ -509,17 +518,17 @@ __global__ void __launch_bounds__(256, 1) k_ozaki(const __grid_constant__ CUtens
     double *pc = (double *)mat_ptr(g.C, kk, cc);
     double *pd = (double *)mat_ptr(g.D, kk, cc);
     double *pe = (double *)mat_ptr(g.E, kk, cc);
-    constexpr int NL = nlevels(S);
+    constexpr int NL = nlevels<NA>(S);
 #pragma unroll 1
-    for (int c0 = half * (NT / 2); c0 < (half + 1) * (NT / 2); c0 += 16) {
-      uint32_t v[NACC][16];
+    for (int c0 = half * (TN / 2); c0 < (half + 1) * (TN / 2); c0 += 16) {
+      uint32_t v[NA][16];
 #pragma unroll
-      for (int l = 0; l < NL; l++) tmem_ld16(lane_addr + l * NT + c0, v[l]);
+      for (int l = 0; l < NL; l++) tmem_ld16(lane_addr + l * TN + c0, v[l]);
       tmem_ld_wait();
       if (row >= g.n) continue;
 #pragma unroll
       for (int t = 0; t < 16; t += 2) {  // accumulator columns 2j, 2j+1 = Re, Im of column j
-        const int j = (nt * NT + c0 + t) >> 1;
+        const int j = (nt * TN + c0 + t) >> 1;
         if (j < g.n) {
           long long ar = 0, ai = 0;
 #pragma unroll
@@ -754,8 +763,8 @@ int make_map(CUtensorMap *m, void *base, int rows, long long depth, int boxrows)
 
 // at least 120 KB so that only one CTA (and one 512-column TMEM allocation)
 // is resident per SM
-size_t oz_smem_bytes(int S) {
-  size_t b = (size_t)NSTAGE * S * (MT * KB * 2 + NT * KB * 2) + 1024;
+size_t oz_smem_bytes(int S, int TN) {
+  size_t b = (size_t)NSTAGE * S * (MT * KB * 2 + TN * KB * 2) + 1024;
   return b < 120 * 1024 ? 120 * 1024 : b;
 }
 
@@ -771,6 +780,7 @@ struct Stage {
   int *scale = nullptr;    // row (A) / column (B) scale exponents
   size_t scap = 0;
   int n = -1, K = -1;      // padding layout
+  int tn = 0;              // N tile the B layout is padded to
   int S = 0, DB = 0;
   long long items = 0;
 };
@@ -782,9 +792,19 @@ struct MixedWork {
   double *rnorm = nullptr;
   size_t rn_cap = 0;
   int *err = nullptr;
-  unsigned long long *dmax = nullptr;  // running max of Newton residual norms (double bits)
-  int smem_set[16] = {0};
+  unsigned long long *dmax = nullptr;  // running max of accepted Newton residual norms (double bits)
+  unsigned long long *nfb = nullptr;   // inverses redone in FP64 (residual above the limit)
+  int *flag = nullptr;                 // per-item FP64 fallback mask
+  size_t flag_cap = 0;
+  int smem_set[32] = {0};
+  bool precise = false;    // (64, 7) tile: exact levels 0..5 (mixed_set_precise)
 };
+
+void mixed_set_precise(MixedWork *w, bool on) { w->precise = on; }
+
+// the (64, 7) tile serves products of 6 slices and more (the low-slice
+// Newton corrections keep the default tile); split and multiply agree on it
+static bool use_precise(const MixedWork *w, int S) { return w->precise && S >= 6; }
 
 static int grow(void **p, size_t *cap, size_t bytes, bool zero) {
   if (bytes <= *cap) return 0;
@@ -800,28 +820,36 @@ static int grow(void **p, size_t *cap, size_t bytes, bool zero) {
 MixedWork *mixed_create() {
   MixedWork *w = new MixedWork();
   if (cudaMalloc(&w->err, sizeof(int)) != cudaSuccess ||
-      cudaMalloc(&w->dmax, sizeof(unsigned long long)) != cudaSuccess) {
+      cudaMalloc(&w->dmax, sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMalloc(&w->nfb, sizeof(unsigned long long)) != cudaSuccess) {
     if (w->err) cudaFree(w->err);
+    if (w->dmax) cudaFree(w->dmax);
     delete w;
     return nullptr;
   }
   cudaMemset(w->err, 0, sizeof(int));
   cudaMemset(w->dmax, 0, sizeof(unsigned long long));
+  cudaMemset(w->nfb, 0, sizeof(unsigned long long));
   return w;
 }
 
 int mixed_resid_reset(MixedWork *w, cudaStream_t st) {
-  return cudaMemsetAsync(w->dmax, 0, sizeof(unsigned long long), st) == cudaSuccess ? 0 : SKKR_ERR_CUDA;
+  return (cudaMemsetAsync(w->dmax, 0, sizeof(unsigned long long), st) == cudaSuccess &&
+          cudaMemsetAsync(w->nfb, 0, sizeof(unsigned long long), st) == cudaSuccess)
+             ? 0
+             : SKKR_ERR_CUDA;
 }
 
-int mixed_resid_read(MixedWork *w, double *out, cudaStream_t st) {
-  unsigned long long h = 0;
-  if (cudaMemcpyAsync(&h, w->dmax, sizeof(h), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+int mixed_resid_read(MixedWork *w, double *out, long long *fallbacks, cudaStream_t st) {
+  unsigned long long h[2] = {0, 0};
+  if (cudaMemcpyAsync(&h[0], w->dmax, sizeof(h[0]), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaMemcpyAsync(&h[1], w->nfb, sizeof(h[1]), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
       cudaStreamSynchronize(st) != cudaSuccess)
     return SKKR_ERR_CUDA;
   double v;
-  memcpy(&v, &h, sizeof(v));
+  memcpy(&v, &h[0], sizeof(v));
   *out = v;
+  if (fallbacks) *fallbacks = (long long)h[1];
   return 0;
 }
 
@@ -832,7 +860,7 @@ void mixed_destroy(MixedWork *w) {
     for (void *p : q)
       if (p) cudaFree(p);
   }
-  void *ps[] = {w->acopy, w->rbuf, w->rnorm, w->err, w->dmax};
+  void *ps[] = {w->acopy, w->rbuf, w->rnorm, w->err, w->dmax, w->nfb, w->flag};
   for (void *p : ps)
     if (p) cudaFree(p);
   delete w;
@@ -844,12 +872,12 @@ int mixed_error_flag(MixedWork *w) {
   return h;
 }
 
-// dims of the staged real problem for complex n x K times K x n
-static void oz_dims(int n, int K, int *Mp, int *Np, int *Kp, int *mtiles, int *ntiles, int *kblocks) {
+// dims of the staged real problem for complex n x K times K x n, N tile tn
+static void oz_dims(int n, int K, int tn, int *Mp, int *Np, int *Kp, int *mtiles, int *ntiles, int *kblocks) {
   *mtiles = (n + MT - 1) / MT;
   *Mp = *mtiles * MT;
-  *ntiles = (2 * n + NT - 1) / NT;
-  *Np = *ntiles * NT;
+  *ntiles = (2 * n + tn - 1) / tn;
+  *Np = *ntiles * tn;
   *kblocks = (2 * K + KB - 1) / KB;
   *Kp = *kblocks * KB;
 }
@@ -866,7 +894,8 @@ template <int S, int DB>
 static int split_s(MixedWork *w, int side, int slot, const MatRef &M, int n, int K, int nk, int nc,
                    const int *act, cudaStream_t st) {
   int Mp, Np, Kp, mtiles, ntiles, kblocks;
-  oz_dims(n, K, &Mp, &Np, &Kp, &mtiles, &ntiles, &kblocks);
+  const int tn = use_precise(w, S) ? 64 : NT;
+  oz_dims(n, K, tn, &Mp, &Np, &Kp, &mtiles, &ntiles, &kblocks);
   const long long items = (long long)nk * nc;
   Stage &sg = side == 0 ? w->A[slot] : w->B[slot];
   const int rows = side == 0 ? Mp : Np;
@@ -874,13 +903,14 @@ static int split_s(MixedWork *w, int side, int slot, const MatRef &M, int n, int
   if ((rc = grow(&sg.p, &sg.cap, (size_t)items * S * rows * Kp * 2, true))) return rc;
   if ((rc = grow((void **)&sg.scale, &sg.scap, (size_t)items * (side == 0 ? Mp : n) * sizeof(int), false)))
     return rc;
-  if (sg.n != n || sg.K != K) {
+  if (sg.n != n || sg.K != K || (side == 1 && sg.tn != tn)) {
     // padding (rows beyond the operand, columns >= 2K of every slice region)
     // must be zero; a new layout clears what an earlier one wrote there
     if (cudaMemsetAsync(sg.p, 0, sg.cap, st) != cudaSuccess) return SKKR_ERR_CUDA;
     sg.n = n;
     sg.K = K;
   }
+  sg.tn = side == 1 ? tn : 0;
   const long long active_s = act ? skkr_active_items(items) : items;
   // split traffic: FP64 operand read + S bf16 slices of the real embedding written
   const double split_bytes = (double)active_s * n * K * (16.0 + S * 2.0 * 2.0);
@@ -901,26 +931,27 @@ static int split_s(MixedWork *w, int side, int slot, const MatRef &M, int n, int
   return 0;
 }
 
-template <int S>
+template <int S, int TN, int NA>
 static int gemm_s(MixedWork *w, int mode, int sa, int sb, const MatRef &C, const MatRef &D, const MatRef &E,
                   int n, int K, int nk, int nc, const int *act, cudaStream_t st) {
   if (get_encoder()) return SKKR_ERR_CUDA;
   int Mp, Np, Kp, mtiles, ntiles, kblocks;
-  oz_dims(n, K, &Mp, &Np, &Kp, &mtiles, &ntiles, &kblocks);
+  oz_dims(n, K, TN, &Mp, &Np, &Kp, &mtiles, &ntiles, &kblocks);
   const long long items = (long long)nk * nc;
   const Stage &A = w->A[sa], &B = w->B[sb];
   if (A.S != S || B.S != S || A.DB != B.DB || A.n != n || B.n != n || A.K != K || B.K != K ||
-      A.items != items || B.items != items)
+      A.items != items || B.items != items || B.tn != TN)
     return SKKR_ERR_ARG;  // the slots do not hold splits of this product's operands
   CUtensorMap ma, mb;
-  if (make_map(&ma, A.p, Mp, items * S * kblocks, MT) || make_map(&mb, B.p, Np, items * S * kblocks, NT))
+  if (make_map(&ma, A.p, Mp, items * S * kblocks, MT) || make_map(&mb, B.p, Np, items * S * kblocks, TN))
     return SKKR_ERR_CUDA;
-  const size_t smem = oz_smem_bytes(S);
-  if (!w->smem_set[S]) {
-    if (cudaFuncSetAttribute(k_ozaki<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+  const size_t smem = oz_smem_bytes(S, TN);
+  const int sk = S + (TN == NT ? 0 : 16);
+  if (!w->smem_set[sk]) {
+    if (cudaFuncSetAttribute(k_ozaki<S, TN, NA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
         cudaSuccess)
       return SKKR_ERR_CUDA;
-    w->smem_set[S] = 1;
+    w->smem_set[sk] = 1;
   }
   OzArgs g;
   g.n = n;
@@ -941,7 +972,7 @@ static int gemm_s(MixedWork *w, int mode, int sa, int sb, const MatRef &C, const
   const long long active = act ? skkr_active_items(items) : items;
   // algorithmic BF16 tensor work: S(S+1)/2 real products of n x 2K x 2n per item
   kstat_begin(KS_OZAKI, (double)(S * (S + 1) / 2) * 8.0 * n * (double)n * K * (double)active, st);
-  k_ozaki<S><<<grid, 256, smem, st>>>(ma, mb, g);
+  k_ozaki<S, TN, NA><<<grid, 256, smem, st>>>(ma, mb, g);
   kstat_end(st);
   SKKR_LAUNCHED();
   return 0;
@@ -980,13 +1011,21 @@ int mixed_gemm_staged(MixedWork *w, int mode, int S, int sa, int sb, const MatRe
   if (sa < 0 || sa >= MIXED_SLOTS || sb < 0 || sb >= MIXED_SLOTS) return SKKR_ERR_ARG;
   int Se, DB;
   oz_digits(S, K, &Se, &DB);
+  if (use_precise(w, Se)) {
+    switch (Se) {  // 64-column tiles, levels 0..5 in their own accumulators
+      case 6: return gemm_s<6, 64, 7>(w, mode, sa, sb, C, D, E, n, K, nk, nc, act, st);
+      case 7: return gemm_s<7, 64, 7>(w, mode, sa, sb, C, D, E, n, K, nk, nc, act, st);
+      case 8: return gemm_s<8, 64, 7>(w, mode, sa, sb, C, D, E, n, K, nk, nc, act, st);
+      default: return SKKR_ERR_ARG;
+    }
+  }
   switch (Se) {
-    case 3: return gemm_s<3>(w, mode, sa, sb, C, D, E, n, K, nk, nc, act, st);
-    case 4: return gemm_s<4>(w, mode, sa, sb, C, D, E, n, K, nk, nc, act, st);
-    case 5: return gemm_s<5>(w, mode, sa, sb, C, D, E, n, K, nk, nc, act, st);
-    case 6: return gemm_s<6>(w, mode, sa, sb, C, D, E, n, K, nk, nc, act, st);
-    case 7: return gemm_s<7>(w, mode, sa, sb, C, D, E, n, K, nk, nc, act, st);
-    case 8: return gemm_s<8>(w, mode, sa, sb, C, D, E, n, K, nk, nc, act, st);
+    case 3: return gemm_s<3, NT, NACC>(w, mode, sa, sb, C, D, E, n, K, nk, nc, act, st);
+    case 4: return gemm_s<4, NT, NACC>(w, mode, sa, sb, C, D, E, n, K, nk, nc, act, st);
+    case 5: return gemm_s<5, NT, NACC>(w, mode, sa, sb, C, D, E, n, K, nk, nc, act, st);
+    case 6: return gemm_s<6, NT, NACC>(w, mode, sa, sb, C, D, E, n, K, nk, nc, act, st);
+    case 7: return gemm_s<7, NT, NACC>(w, mode, sa, sb, C, D, E, n, K, nk, nc, act, st);
+    case 8: return gemm_s<8, NT, NACC>(w, mode, sa, sb, C, D, E, n, K, nk, nc, act, st);
     default: return SKKR_ERR_ARG;
   }
 }
@@ -1005,30 +1044,21 @@ int mixed_zgemm(MixedWork *w, int mode, int S, const MatRef &A, const MatRef &B,
   return mixed_zgemm_k(w, mode, S, A, B, C, D, E, n, n, nk, nc, act, st);
 }
 
-// Frobenius norm of every item's residual folded into a running maximum
+// Newton residual check per item: an item whose last residual norm
+// |I - A X|_F is above `limit` (or not finite) is marked for an FP64
+// Gauss-Jordan redo; the others fold their norm into the running maximum
 // (non-negative doubles order like their bit patterns: integer atomicMax)
-__global__ void k_fnorm_max(MatRef A, int n, int nc, const int *__restrict__ act,
-                            unsigned long long *dmax) {
-  const int item = blockIdx.x;
-  const int kk = item / nc, cc = item % nc;
-  if (act && !act[item]) return;
-  const zd *a = mat_ptr(A, kk, cc);
-  double s = 0.0;
-  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
-    zd v = a[(e % n) + (long long)(e / n) * A.ld];
-    s += v.x * v.x + v.y * v.y;
-  }
-  __shared__ double red[32];
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    s = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-    if (threadIdx.x == 0) atomicMax(dmax, (unsigned long long)__double_as_longlong(sqrt(s)));
-  }
+__global__ void k_newton_check(const double *__restrict__ rn, const int *__restrict__ act, int items,
+                               double limit, int *__restrict__ flag, unsigned long long *dmax,
+                               unsigned long long *nfb) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= items) return;
+  const int a = act ? act[i] : 1;
+  const double r = rn[i];
+  const int f = a && !(r <= limit);
+  flag[i] = f;
+  if (f) atomicAdd(nfb, 1ull);
+  else if (a) atomicMax(dmax, (unsigned long long)__double_as_longlong(r));
 }
 
 // X = A^-1: FP32 Gauss-Jordan, then `newton` steps X += X (I - A X) with the
@@ -1036,12 +1066,14 @@ __global__ void k_fnorm_max(MatRef A, int n, int nc, const int *__restrict__ act
 // alias A.
 int mixed_zinv(MixedWork *w, const MatRef &A, const MatRef &X, int n, int nk, int nc, const int *act,
                int newton, int sres, bool track_resid, cudaStream_t st) {
-  if (n < 1 || n > 128) return SKKR_ERR_ARG;
+  (void)track_resid;
+  if (n < 1 || n > 128 || newton < 1) return SKKR_ERR_ARG;
   const long long items = (long long)nk * nc, MB = (long long)n * n;
   int rc;
   if ((rc = grow((void **)&w->acopy, &w->ac_cap, (size_t)items * MB * sizeof(zd), false))) return rc;
   if ((rc = grow((void **)&w->rbuf, &w->rb_cap, (size_t)items * MB * sizeof(zd), false))) return rc;
   if ((rc = grow((void **)&w->rnorm, &w->rn_cap, (size_t)items * sizeof(double), false))) return rc;
+  if ((rc = grow((void **)&w->flag, &w->flag_cap, (size_t)items * sizeof(int), false))) return rc;
   MatRef Ac = mref(w->acopy, (long long)nc * MB, MB, n);
   MatRef R = mref(w->rbuf, (long long)nc * MB, MB, n);
   launch_zaxpby(Ac, A, nullptr, 0, nullptr, 0, n, nk, nc, act, st);
@@ -1057,14 +1089,20 @@ int mixed_zinv(MixedWork *w, const MatRef &A, const MatRef &X, int n, int nk, in
     // R = I - A X
     if ((rc = mixed_split(w, 1, 0, sres, X, n, n, nk, nc, act, st))) return rc;
     if ((rc = mixed_gemm_staged(w, 4, sres, 0, 0, R, R, R, n, n, nk, nc, act, st))) return rc;
-    if (track_resid && it == newton - 1) {
-      k_fnorm_max<<<(unsigned)items, 256, 0, st>>>(R, n, nc, act, w->dmax);
-      SKKR_LAUNCHED();
-    }
+    if (it == newton - 1) launch_fnorm(R, n, nk, nc, act, w->rnorm, st);
     // X = X + X R (slot 5: slot 0 keeps A)
     if ((rc = mixed_split(w, 0, 5, 3, X, n, n, nk, nc, act, st))) return rc;
     if ((rc = mixed_split(w, 1, 5, 3, R, n, n, nk, nc, act, st))) return rc;
     if ((rc = mixed_gemm_staged(w, 5, 3, 5, 5, X, X, X, n, n, nk, nc, act, st))) return rc;
   }
+  // An ill-conditioned A (cond ~ 1e7 and above) leaves the FP32 start outside
+  // Newton's basin: such items are inverted again in FP64 (copy A, column-
+  // pivoting Gauss-Jordan), masked so that the others are untouched.  The
+  // residual before the last correction bounds the final error by its square.
+  k_newton_check<<<(unsigned)((items + 255) / 256), 256, 0, st>>>(w->rnorm, act, (int)items, 1e-6, w->flag,
+                                                                   w->dmax, w->nfb);
+  SKKR_LAUNCHED();
+  launch_zaxpby(X, Ac, nullptr, 0, nullptr, 0, n, nk, nc, w->flag, st);
+  launch_zgj(X, n, nk, nc, w->flag, st);
   return 0;
 }

@@ -37,7 +37,8 @@ class RTable(C.Structure):
 class Status(C.Structure):
     _fields_ = [("code", I), ("ik", I), ("cpa_iterations", I), ("cpa_error", D),
                 ("max_dec_iters", I), ("dec_iters_total", C.c_longlong),
-                ("gpu_launches", C.c_longlong), ("max_refine_resid", D), ("run_ms", D)]
+                ("gpu_launches", C.c_longlong), ("max_refine_resid", D), ("run_ms", D),
+                ("inv_fallbacks", C.c_longlong), ("k_fp64", C.c_longlong)]
 
 
 class SkkrError(RuntimeError):
@@ -70,6 +71,7 @@ def lib():
         L.skkr_gpu_phystau.argtypes = [I, I, P, P, P, I]
         L.skkr_gpu_layer_dos.argtypes = [I, I, I, P, I, P, P, I, P, P]
         L.skkr_gpu_set_reduce.argtypes = [P, P, P]
+        L.skkr_gpu_set_mixed_policy.argtypes = [P, D, D, I, D]
         L.skkr_gpu_cpacoord_many.argtypes = [I, P, P, P]
         L.skkr_gpu_gjinv_batch.argtypes = [I, I, P, I]
         L.skkr_gpu_surfgf_batch.argtypes = [I, I, P, P, P, P, I, I, D, P, P]

@@ -524,9 +524,15 @@ class RTable:
 
 
 def build_rtable(st: Stacking, e_struct: complex, alpha: np.ndarray, lmax: int, nshell: int = 3,
-                 hole: bool = False) -> RTable:
+                 hole: bool = False, nshell_screen: int | None = None) -> RTable:
+    """Screened table of the first nshell neighbour shells; the screening
+    inversion runs on the larger cluster of nshell_screen shells (default:
+    the same) so that the kept couplings do not see the cluster boundary."""
+    big, nsb, _ = cluster(st, nshell_screen or nshell)
     vecs, ns, _ = cluster(st, nshell)
-    g = screened_realspace(e_struct, vecs, alpha, lmax, hole)
+    gbig = screened_realspace(e_struct, big, alpha, lmax, hole)
+    g = gbig[:len(vecs)]            # cluster() orders sites by distance: inner shells first
+    assert np.allclose(big[:len(vecs)], vecs)
     jmax = int(np.max(np.abs(ns)))
     starts, rv, gr, blk_of_j = [0], [], [], {}
     for j in range(-jmax, jmax + 1):

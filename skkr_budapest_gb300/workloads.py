@@ -93,6 +93,11 @@ class SystemSpec:
     conc_range: tuple = (0.1, 0.9)
     alloy_depth_range: tuple = (-1.2, -0.4)
     cpatol: float = 1.0e-10
+    # neighbour shells of the cluster the screening inversion runs on (the
+    # table keeps 3 shells): on the bare 3-shell cluster the boundary distorts
+    # the kept couplings enough that the lead decimation of the bcc stacking
+    # exceeds the 1e10 limit of surfgf.f at the contour points nearest the axis
+    screen_shells: int = 5
     # BdG (irel=2): energies relative to e_fermi, pairing delta on sc_layers
     # (interface layer indices) and on the leads flagged in sc_leads (L, R)
     e_fermi: float = 0.0
@@ -117,14 +122,20 @@ def plain_fcc(nset: int = 22) -> SystemSpec:
 REL_NSETS = [20] * 12 + [32] * 4 + [48] * 3 + [70] * 2 + [100, 125, 155]
 
 
-def rel_bcc(nsets=None) -> SystemSpec:
+# The measured relativistic workloads carry no j = l +- 1/2 splitting of the
+# well depths (so_split = 0): with the 0.03 Ry split the doubling iteration of
+# the synthetic lead exceeds the absolute 1e10 limit of surfgf.f at some k of
+# the dense meshes near the real axis (a transient that grows with the split;
+# the oracle reproduces it), and the reference stops there.  The (kappa,mu)
+# machinery is the same; the split path is tested on meshes where it converges.
+def rel_bcc(nsets=None, so_split: float = 0.0) -> SystemSpec:
     z = _contour(24, -0.5, 0.7, 10.0)
     return SystemSpec("rel_bcc", S.bcc001(6.0), 1, 3, 4, 3, z,
-                      list(REL_NSETS if nsets is None else nsets), seed=1)
+                      list(REL_NSETS if nsets is None else nsets), seed=1, so_split=so_split)
 
 
-def rel_bcc_cpa(nsets=None) -> SystemSpec:
-    s = rel_bcc(nsets)
+def rel_bcc_cpa(nsets=None, so_split: float = 0.0) -> SystemSpec:
+    s = rel_bcc(nsets, so_split)
     s.name = "rel_bcc_cpa"
     s.seed = 2
     s.alloy_layers = (4, 5, 6, 7)
@@ -137,10 +148,10 @@ def nonrel_pl2() -> SystemSpec:
                       [14] * 8 + [20] * 4 + [40] * 2 + [80, 126], seed=3)
 
 
-def rel_pl3_l2() -> SystemSpec:
+def rel_pl3_l2(so_split: float = 0.0) -> SystemSpec:
     z = _contour(20, -0.5, 0.7, 10.0)
     return SystemSpec("rel_pl3_l2", S.bcc001(6.0), 1, 2, 3, 3, z,
-                      [14] * 10 + [20] * 4 + [40] * 3 + [60, 90, 126], seed=4)
+                      [14] * 10 + [20] * 4 + [40] * 3 + [60, 90, 126], seed=4, so_split=so_split)
 
 
 def bdg_bcc(nsets=None, lmax: int = 3, pl: int = 4, ne: int = 64, im_e: float = 1.0e-4) -> SystemSpec:
@@ -154,7 +165,7 @@ def bdg_bcc(nsets=None, lmax: int = 3, pl: int = 4, ne: int = 64, im_e: float = 
     nintfc = pl * 3
     return SystemSpec("bdg_bcc", S.bcc001(6.0), 2, lmax, pl, 3, z,
                       list([6] * ne if nsets is None else nsets), seed=5, e_fermi=0.7, delta=delta,
-                      sc_layers=tuple(range(nintfc // 2)), sc_leads=(True, False))
+                      sc_layers=tuple(range(nintfc // 2)), sc_leads=(True, False), so_split=0.0)
 
 
 def system_layers(spec: SystemSpec):
@@ -180,7 +191,7 @@ def energy_problem(spec: SystemSpec, ie: int, nset: int | None = None, kmesh: st
     _, _, dnn = S.cluster(st, 1)
     rs = 0.7 * dnn
     alpha = S.alpha_sqwell(ce, spec.vscreen, rs, lmax)
-    rt = S.build_rtable(st, psq, alpha, lmax)
+    rt = S.build_rtable(st, psq, alpha, lmax, nshell_screen=spec.screen_shells)
     ninprc, nintfc = system_layers(spec)
     blkmap = S.blkmap_translation_invariant(rt, spec.nprc + 2, int(max(ninprc)))
 
@@ -245,8 +256,8 @@ def _bdg_problem(spec: SystemSpec, ie: int, nset, kmesh) -> EnergyProblem:
     rs = 0.7 * dnn
     alpha_e = S.alpha_sqwell(psq, spec.vscreen, rs, lmax)
     alpha_h = S.alpha_sqwell_hole(ef - ce, spec.vscreen, rs, lmax)
-    rt = S.build_rtable(st, psq, alpha_e, lmax)
-    rt_h = S.build_rtable(st, psqh, alpha_h, lmax, hole=True)
+    rt = S.build_rtable(st, psq, alpha_e, lmax, nshell_screen=spec.screen_shells)
+    rt_h = S.build_rtable(st, psqh, alpha_h, lmax, hole=True, nshell_screen=spec.screen_shells)
     ninprc, nintfc = system_layers(spec)
     blkmap = S.blkmap_translation_invariant(rt, spec.nprc + 2, int(max(ninprc)))
     rng = np.random.default_rng(spec.seed)

@@ -105,11 +105,12 @@ def test_full_bz_equals_symmetrised_ibz_on_gpu():
 
 
 def test_decimation_divergence_is_reported_not_trapped():
-    # the relativistic lmax=2 bcc stack has a k point at Im E ~ 0.013 Ry whose
-    # decimation error transiently exceeds 1e10 (surfgf.f:88-93)
-    spec = W.rel_bcc(nsets=[3] * 24)
+    # with the 0.03 Ry j-split wells, the relativistic lmax=2 bcc stack has a
+    # k point at Im E ~ 0.07 Ry whose decimation error transiently exceeds
+    # 1e10 (surfgf.f:88-93)
+    spec = W.rel_bcc(nsets=[3] * 24, so_split=0.03)
     spec.lmax = 2
-    ep = W.energy_problem(spec, 20)
+    ep = W.energy_problem(spec, 16)
     o = O.cpacoord(ep, nthreads=4)
     assert o["status"] == 2
     with pytest.raises(native.SkkrError) as ei:
@@ -160,3 +161,11 @@ def test_cpa_from_learned_start_converges_to_the_same_tau():
     assert a["status"] == 0 and b["status"] == 0
     assert b["cpa_error"] < ep.cpatol
     assert rel(b["tauc"], a["tauc"]) < 1e-7
+
+
+def test_cpacoord_relativistic_with_j_split():
+    """The j = l +- 1/2 split well depths (0.03 Ry) on a mesh where the lead
+    decimation converges: the (kappa,mu)-dependent t-matrix path."""
+    spec = W.rel_bcc(nsets=[3] * 24, so_split=0.03)
+    g, o = _compare(W.energy_problem(spec, 14))
+    assert g["cpa_iterations"] == 1
