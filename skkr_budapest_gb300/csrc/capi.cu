@@ -144,12 +144,18 @@ void skkr_after_launch(const char *file, int line) {
 namespace {
 
 // growable device buffer
+// The library stream is non-blocking, so cudaFree does not wait for its
+// queued kernels: a buffer is freed (to grow it, or on release) only after the
+// device is idle.  Growth is rare; steady state never frees.
 struct DBuf {
   void *p = nullptr;
   size_t cap = 0;
   int ensure(size_t bytes) {
     if (bytes <= cap) return SKKR_OK;
-    if (p) cudaFree(p);
+    if (p) {
+      cudaDeviceSynchronize();
+      cudaFree(p);
+    }
     p = nullptr;
     cap = 0;
     cudaError_t e = cudaMalloc(&p, bytes ? bytes : 16);
@@ -163,7 +169,10 @@ struct DBuf {
   template <class T>
   T *as() const { return (T *)p; }
   void release() {
-    if (p) cudaFree(p);
+    if (p) {
+      cudaDeviceSynchronize();
+      cudaFree(p);
+    }
     p = nullptr;
     cap = 0;
   }

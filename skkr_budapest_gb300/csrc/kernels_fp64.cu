@@ -86,6 +86,12 @@ cudaError_t pack_set_tables(int irel, int lmax) {
       if (!i2[k]) i2[k] = 1;
       i1[k]--;
       i2[k]--;
+      // a zero coefficient marks a spinor component outside the basis
+      // (|m| > l, e.g. l = lmax + 1 for the last kappa); its index would
+      // point past the lm block, so the term reads element 0 instead (it is
+      // multiplied by zero either way, as in the zero-padded reference copy)
+      if (u1[k] == 0.0) i1[k] = 0;
+      if (u2[k] == 0.0) i2[k] = 0;
     }
   }
   cudaError_t e = cudaMemcpyToSymbol(c_u1, u1, sizeof(u1));

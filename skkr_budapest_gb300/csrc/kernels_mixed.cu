@@ -806,13 +806,21 @@ void mixed_set_precise(MixedWork *w, bool on) { w->precise = on; }
 // Newton corrections keep the default tile); split and multiply agree on it
 static bool use_precise(const MixedWork *w, int S) { return w->precise && S >= 6; }
 
+// the callers' streams are non-blocking: free the old buffer only once the
+// device is idle (cudaFree does not wait for those streams)
 static int grow(void **p, size_t *cap, size_t bytes, bool zero) {
   if (bytes <= *cap) return 0;
-  if (*p) cudaFree(*p);
+  if (*p) {
+    cudaDeviceSynchronize();
+    cudaFree(*p);
+  }
   *p = nullptr;
   *cap = 0;
   if (cudaMalloc(p, bytes) != cudaSuccess) return SKKR_ERR_NOMEM;
-  if (zero && cudaMemset(*p, 0, bytes) != cudaSuccess) return SKKR_ERR_NOMEM;
+  // cudaMemset runs on the legacy default stream, which the non-blocking
+  // streams do not wait for: finish it before the buffer is used
+  if (zero && (cudaMemset(*p, 0, bytes) != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess))
+    return SKKR_ERR_NOMEM;
   *cap = bytes;
   return 0;
 }
@@ -830,6 +838,7 @@ MixedWork *mixed_create() {
   cudaMemset(w->err, 0, sizeof(int));
   cudaMemset(w->dmax, 0, sizeof(unsigned long long));
   cudaMemset(w->nfb, 0, sizeof(unsigned long long));
+  cudaDeviceSynchronize();  // default-stream memsets, before the non-blocking streams use the flags
   return w;
 }
 
@@ -855,6 +864,7 @@ int mixed_resid_read(MixedWork *w, double *out, long long *fallbacks, cudaStream
 
 void mixed_destroy(MixedWork *w) {
   if (!w) return;
+  cudaDeviceSynchronize();
   for (int i = 0; i < MIXED_SLOTS; i++) {
     void *q[] = {w->A[i].p, w->A[i].scale, w->B[i].p, w->B[i].scale};
     for (void *p : q)
