@@ -248,7 +248,7 @@ def timed_steps(ctx, order, slot_of, eps, args, flush, stats=False):
     torch.cuda.synchronize()
     if stats:
         N.kernel_stats_start()
-    t_dev, pts, launches, dec_iters, resid, fallbacks, kfp64 = 0.0, 0, 0, 0, 0.0, 0, 0
+    t_dev, pts, launches, dec_iters, resid, fallbacks, kfp64, refined = 0.0, 0, 0, 0, 0.0, 0, 0, 0
     w0 = time.perf_counter()
     for i in range(args.steps):
         ie = order[args.warmup + i]
@@ -261,12 +261,13 @@ def timed_steps(ctx, order, slot_of, eps, args, flush, stats=False):
         dec_iters += st.dec_iters_total
         resid = max(resid, st.max_refine_resid)
         fallbacks += st.inv_fallbacks
+        refined += st.inv_refined
         kfp64 += st.k_fp64
     torch.cuda.synchronize()
     wall = time.perf_counter() - w0
     ks = N.kernel_stats_stop() if stats else None
     return dict(t_dev=t_dev, pts=pts, launches=launches, dec_iters=dec_iters, wall=wall, ks=ks, resid=resid,
-                fallbacks=fallbacks, kfp64=kfp64)
+                fallbacks=fallbacks, kfp64=kfp64, refined=refined)
 
 
 def roofline(ks, precision):
@@ -384,6 +385,7 @@ def run_ours(args, rank, ws):
                        "l2": "256 MB buffer written between steps; per-step working set > 1 GB",
                        "wall_s": round(r["wall"], 3), "dec_iters": r["dec_iters"],
                        "max_newton_resid": r["resid"], "inverses_redone_in_fp64": r["fallbacks"],
+                       "inverses_with_further_newton_steps": r["refined"],
                        "k_points_redone_in_fp64": r["kfp64"]},
             "fp64_gpu": fp64,
             "roofline": roof, "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d // args.steps,

@@ -102,6 +102,8 @@ typedef struct {
   long long inv_fallbacks;    /* mixed precision: inverses whose residual stayed above 1e-6
                                  and were redone in FP64 */
   long long k_fp64;           /* mixed precision: k points redone in FP64 (dominant contributions) */
+  long long inv_refined;      /* mixed precision: inverses that took further Newton steps (residual
+                                 above 1e-6 after the standard steps, below 1/2) */
 } skkr_status;
 
 typedef struct skkr_ctx skkr_ctx;
@@ -118,7 +120,9 @@ int skkr_gpu_destroy(skkr_ctx *ctx);
  * exact-level tile when |Im E| < near_im (default: never; 3..8, 0 = off);
  * every k point whose contribution exceeds dominant_frac (default 1e-2) of
  * the norm of the k-summed tau is recomputed in FP64 (0 = off).  Inverses
- * whose Newton residual stays above 1e-6 are always redone in FP64. */
+ * whose Newton residual is above 1e-6 after the standard steps take up to
+ * four further steps while it stays below 1/2; those still above 1e-6 are
+ * always redone in FP64. */
 int skkr_gpu_set_mixed_policy(skkr_ctx *ctx, double dec_fp64_im, double near_im, int slices_near,
                               double dominant_frac);
 

@@ -164,6 +164,7 @@ class Context:
                    max_dec_iters=st.max_dec_iters, dec_iters_total=st.dec_iters_total,
                    gpu_launches=st.gpu_launches, ik=st.ik, run_ms=st.run_ms,
                    max_refine_resid=st.max_refine_resid, inv_fallbacks=st.inv_fallbacks, k_fp64=st.k_fp64,
+                   inv_refined=st.inv_refined,
                    h2d_bytes=sum(v.nbytes for v in a.values()) + rt.gR.nbytes + rt.rvec.nbytes,
                    d2h_bytes=sum(v.nbytes for v in out.values()))
         return res

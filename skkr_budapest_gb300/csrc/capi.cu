@@ -233,6 +233,7 @@ struct skkr_ctx {
   std::vector<double> red_buf;
   double max_resid = 0.0;    // largest accepted Newton residual seen in this run
   long long inv_fallbacks = 0;  // inverses redone in FP64 in this run
+  long long inv_refined = 0;    // inverses that took further Newton steps in this run
 };
 
 // Inputs and outputs of one staged energy.  A context keeps any number of
@@ -1312,7 +1313,8 @@ extern "C" int skkr_gpu_run(skkr_ctx *c, skkr_status *status) {
   }
   trace_point("after CPA loop");
   c->inv_fallbacks = 0;
-  if (c->mw) CKR(mixed_resid_read(c->mw, &c->max_resid, &c->inv_fallbacks, st));
+  c->inv_refined = 0;
+  if (c->mw) CKR(mixed_resid_read(c->mw, &c->max_resid, &c->inv_fallbacks, &c->inv_refined, st));
   if (c->mw && c->err_code == 0) {
     int f = mixed_error_flag(c->mw);
     if (f != 0) {
@@ -1338,6 +1340,7 @@ extern "C" int skkr_gpu_run(skkr_ctx *c, skkr_status *status) {
     status->max_refine_resid = c->max_resid;
     status->run_ms = run_ms;
     status->inv_fallbacks = c->inv_fallbacks;
+    status->inv_refined = c->inv_refined;
     status->k_fp64 = c->k_fp64;
   }
   return c->err_code;
@@ -1780,7 +1783,7 @@ extern "C" int skkr_gpu_zinv_batch(int precision, int n, int batch, double *a, i
     double r = 0.0;
     int rc = mixed_resid_reset(w, 0);
     if (!rc) rc = mixed_zinv(w, Am, Am, n, batch, 1, nullptr, newton, 7, true, 0);
-    if (!rc) rc = mixed_resid_read(w, &r, nullptr, 0);
+    if (!rc) rc = mixed_resid_read(w, &r, nullptr, nullptr, 0);
     if (rc == SKKR_OK && cudaDeviceSynchronize() != cudaSuccess) rc = SKKR_ERR_CUDA;
     if (rc == SKKR_OK && mixed_error_flag(w) != 0) rc = SKKR_ERR_CUDA;
     mixed_destroy(w);

@@ -68,6 +68,8 @@ int mixed_error_flag(MixedWork *w);
 // slot 0 is the one mixed_zgemm / mixed_zgemm_k / mixed_zinv use.  Splitting
 // once and multiplying several times reuses an operand's slices.
 constexpr int MIXED_SLOTS = 6;
+// further Newton steps (at most) for inverses left above the residual limit
+constexpr int NEWTON_EXTRA = 4;
 int mixed_split(MixedWork *w, int side, int slot, int S, const MatRef &M, int n, int K, int nk, int nc,
                 const int *act, cudaStream_t st);
 // products of 6+ slices on 64-column tiles with 7 TMEM accumulators (levels
@@ -85,7 +87,8 @@ int mixed_zgemm(MixedWork *w, int mode, int S, const MatRef &A, const MatRef &B,
 int mixed_zinv(MixedWork *w, const MatRef &A, const MatRef &X, int n, int nk, int nc, const int *act,
                int newton, int sres, bool track_resid, cudaStream_t st);
 // running maximum of the accepted Newton residual norms and the count of
-// inverses redone in FP64 (device scalars): reset asynchronously, read with a
+// inverses redone in FP64 (device scalars), and the count of inverses that
+// took further Newton steps (host): reset asynchronously, read with a
 // stream synchronisation
 int mixed_resid_reset(MixedWork *w, cudaStream_t st);
-int mixed_resid_read(MixedWork *w, double *out, long long *fallbacks, cudaStream_t st);
+int mixed_resid_read(MixedWork *w, double *out, long long *fallbacks, long long *refined, cudaStream_t st);

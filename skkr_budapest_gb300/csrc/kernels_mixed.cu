@@ -796,6 +796,10 @@ struct MixedWork {
   unsigned long long *nfb = nullptr;   // inverses redone in FP64 (residual above the limit)
   int *flag = nullptr;                 // per-item FP64 fallback mask
   size_t flag_cap = 0;
+  int *mark = nullptr;                 // per-item mask of the further Newton steps
+  size_t mark_cap = 0;
+  int *cnt = nullptr;                  // count of marked items (device scalar)
+  long long nref = 0;                  // inverses that took further Newton steps (host count)
   int smem_set[32] = {0};
   bool precise = false;    // (64, 7) tile: exact levels 0..5 (mixed_set_precise)
 };
@@ -829,9 +833,11 @@ MixedWork *mixed_create() {
   MixedWork *w = new MixedWork();
   if (cudaMalloc(&w->err, sizeof(int)) != cudaSuccess ||
       cudaMalloc(&w->dmax, sizeof(unsigned long long)) != cudaSuccess ||
-      cudaMalloc(&w->nfb, sizeof(unsigned long long)) != cudaSuccess) {
+      cudaMalloc(&w->nfb, sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMalloc(&w->cnt, sizeof(int)) != cudaSuccess) {
     if (w->err) cudaFree(w->err);
     if (w->dmax) cudaFree(w->dmax);
+    if (w->nfb) cudaFree(w->nfb);
     delete w;
     return nullptr;
   }
@@ -843,13 +849,15 @@ MixedWork *mixed_create() {
 }
 
 int mixed_resid_reset(MixedWork *w, cudaStream_t st) {
+  w->nref = 0;
   return (cudaMemsetAsync(w->dmax, 0, sizeof(unsigned long long), st) == cudaSuccess &&
           cudaMemsetAsync(w->nfb, 0, sizeof(unsigned long long), st) == cudaSuccess)
              ? 0
              : SKKR_ERR_CUDA;
 }
 
-int mixed_resid_read(MixedWork *w, double *out, long long *fallbacks, cudaStream_t st) {
+int mixed_resid_read(MixedWork *w, double *out, long long *fallbacks, long long *refined, cudaStream_t st) {
+  if (refined) *refined = w->nref;
   unsigned long long h[2] = {0, 0};
   if (cudaMemcpyAsync(&h[0], w->dmax, sizeof(h[0]), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
       cudaMemcpyAsync(&h[1], w->nfb, sizeof(h[1]), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
@@ -870,7 +878,7 @@ void mixed_destroy(MixedWork *w) {
     for (void *p : q)
       if (p) cudaFree(p);
   }
-  void *ps[] = {w->acopy, w->rbuf, w->rnorm, w->err, w->dmax, w->nfb, w->flag};
+  void *ps[] = {w->acopy, w->rbuf, w->rnorm, w->err, w->dmax, w->nfb, w->flag, w->mark, w->cnt};
   for (void *p : ps)
     if (p) cudaFree(p);
   delete w;
@@ -1071,6 +1079,19 @@ __global__ void k_newton_check(const double *__restrict__ rn, const int *__restr
   else if (a) atomicMax(dmax, (unsigned long long)__double_as_longlong(r));
 }
 
+// Items whose residual is above `limit` but below `basin` (Newton's
+// quadratic regime) are marked for a further step; `count` accumulates them
+__global__ void k_newton_select(const double *__restrict__ rn, const int *__restrict__ act, int items,
+                                double limit, double basin, int *__restrict__ mark, int *count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= items) return;
+  const int a = act ? act[i] : 1;
+  const double r = rn[i];
+  const int m = a && r > limit && r < basin;
+  mark[i] = m;
+  if (m) atomicAdd(count, 1);
+}
+
 // X = A^-1: FP32 Gauss-Jordan, then `newton` steps X += X (I - A X) with the
 // residual product at S = sres slices and the correction at S = 3.  X may
 // alias A.
@@ -1084,6 +1105,7 @@ int mixed_zinv(MixedWork *w, const MatRef &A, const MatRef &X, int n, int nk, in
   if ((rc = grow((void **)&w->rbuf, &w->rb_cap, (size_t)items * MB * sizeof(zd), false))) return rc;
   if ((rc = grow((void **)&w->rnorm, &w->rn_cap, (size_t)items * sizeof(double), false))) return rc;
   if ((rc = grow((void **)&w->flag, &w->flag_cap, (size_t)items * sizeof(int), false))) return rc;
+  if ((rc = grow((void **)&w->mark, &w->mark_cap, (size_t)items * sizeof(int), false))) return rc;
   MatRef Ac = mref(w->acopy, (long long)nc * MB, MB, n);
   MatRef R = mref(w->rbuf, (long long)nc * MB, MB, n);
   launch_zaxpby(Ac, A, nullptr, 0, nullptr, 0, n, nk, nc, act, st);
@@ -1104,6 +1126,33 @@ int mixed_zinv(MixedWork *w, const MatRef &A, const MatRef &X, int n, int nk, in
     if ((rc = mixed_split(w, 0, 5, 3, X, n, n, nk, nc, act, st))) return rc;
     if ((rc = mixed_split(w, 1, 5, 3, R, n, n, nk, nc, act, st))) return rc;
     if ((rc = mixed_gemm_staged(w, 5, 3, 5, 5, X, X, X, n, n, nk, nc, act, st))) return rc;
+  }
+  // Items above the limit but inside Newton's basin (|R| < 1/2) take up to
+  // NEWTON_EXTRA further steps with the correction at sres slices as well:
+  // the 3-slice correction leaves about cond(A) 2^-24 |R| in the next
+  // residual, which stalls ill-conditioned items.  The host reads the count
+  // of marked items once per step and stops when none is left.
+  const long long hint = skkr_active_items(-1);
+  for (int e = 0; e < NEWTON_EXTRA; e++) {
+    if (cudaMemsetAsync(w->cnt, 0, sizeof(int), st) != cudaSuccess) return SKKR_ERR_CUDA;
+    k_newton_select<<<(unsigned)((items + 255) / 256), 256, 0, st>>>(w->rnorm, act, (int)items, 1e-6, 0.5,
+                                                                    w->mark, w->cnt);
+    SKKR_LAUNCHED();
+    int marked = 0;
+    if (cudaMemcpyAsync(&marked, w->cnt, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      return SKKR_ERR_CUDA;
+    if (marked == 0) break;
+    if (e == 0) w->nref += marked;
+    const int *mk = w->mark;
+    skkr_set_active_items(marked);
+    if ((rc = mixed_split(w, 1, 0, sres, X, n, n, nk, nc, mk, st))) return rc;
+    if ((rc = mixed_gemm_staged(w, 4, sres, 0, 0, R, R, R, n, n, nk, nc, mk, st))) return rc;
+    launch_fnorm(R, n, nk, nc, mk, w->rnorm, st);
+    if ((rc = mixed_split(w, 0, 5, sres, X, n, n, nk, nc, mk, st))) return rc;
+    if ((rc = mixed_split(w, 1, 5, sres, R, n, n, nk, nc, mk, st))) return rc;
+    if ((rc = mixed_gemm_staged(w, 5, sres, 5, 5, X, X, X, n, n, nk, nc, mk, st))) return rc;
+    skkr_set_active_items(hint);
   }
   // An ill-conditioned A (cond ~ 1e7 and above) leaves the FP32 start outside
   // Newton's basin: such items are inverted again in FP64 (copy A, column-

@@ -38,7 +38,8 @@ class Status(C.Structure):
     _fields_ = [("code", I), ("ik", I), ("cpa_iterations", I), ("cpa_error", D),
                 ("max_dec_iters", I), ("dec_iters_total", C.c_longlong),
                 ("gpu_launches", C.c_longlong), ("max_refine_resid", D), ("run_ms", D),
-                ("inv_fallbacks", C.c_longlong), ("k_fp64", C.c_longlong)]
+                ("inv_fallbacks", C.c_longlong), ("k_fp64", C.c_longlong),
+                ("inv_refined", C.c_longlong)]
 
 
 class SkkrError(RuntimeError):
