@@ -116,8 +116,9 @@ int skkr_gpu_destroy(skkr_ctx *ctx);
 /* Split-precision policy near the real axis, where the lead and slab
  * matrices become ill-conditioned and rounding of the products is amplified
  * by their condition number: decimation runs in FP64 when |Im E| < dec_fp64_im
- * (default 1e-3 Ry); the products use slices_near BF16 slices on the
- * exact-level tile when |Im E| < near_im (default: never; 3..8, 0 = off);
+ * (default 2e-4 Ry); the products use slices_near BF16 slices on the
+ * exact-level tile when |Im E| < near_im (defaults 7 slices below 1e-3 Ry;
+ * 3..8, 0 = off);
  * every k point whose contribution exceeds dominant_frac (default 1e-2) of
  * the norm of the k-summed tau is recomputed in FP64 (0 = off).  Inverses
  * whose Newton residual is above 1e-6 after the standard steps take up to

@@ -48,7 +48,7 @@ class Context:
         return cls(ep.irel, ep.lmax, ep.nprc, ep.ninprc, len(ep.lg), ep.itermaxl, ep.itermaxr, ep.errmax,
                    ep.itcpam, ep.cpatol, precision, nk_chunk, slices)
 
-    def set_mixed_policy(self, dec_fp64_im=1e-3, near_im=0.0, slices_near=0, dominant_frac=1e-2):
+    def set_mixed_policy(self, dec_fp64_im=2e-4, near_im=1e-3, slices_near=7, dominant_frac=1e-2):
         """Precision near the real axis (skkr_gpu_set_mixed_policy): FP64
         decimation below |Im E| = dec_fp64_im, slices_near BF16 slices for the
         products below |Im E| = near_im, FP64 redo of every k point carrying

@@ -221,9 +221,9 @@ struct skkr_ctx {
   MixedWork *mw = nullptr;   // split-precision engine (precision == SKKR_MIXED)
   int slices = 6, slices_res = 7;  // BF16 slices of products / of Newton residuals
   // split-precision policy near the real axis (skkr_gpu_set_mixed_policy)
-  double dec_fp64_im = 1.0e-3;   // decimation in FP64 when |Im E| is below
-  double near_im = 0.0;          // products use slices_near when |Im E| is below
-  int slices_near = 0;
+  double dec_fp64_im = 2.0e-4;   // decimation in FP64 when |Im E| is below
+  double near_im = 1.0e-3;       // products use slices_near when |Im E| is below
+  int slices_near = 7;
   double dominant_frac = 1.0e-2; // k points carrying more of |sum_k tau_k| are redone in FP64
   bool force_fp64 = false;       // set while such a k point is redone
   DBuf knorm;                    // [nk] norms of the k-resolved tau contributions
@@ -685,7 +685,7 @@ static int eng_inv(skkr_ctx *c, bool mixed, const MatRef &A, const MatRef &X, bo
 
 static bool use_mixed(const skkr_ctx *c, bool decimation) {
   if (c->sz.precision != SKKR_MIXED || c->force_fp64) return false;
-  // decimation near the real axis stays in FP64 (default: within 1e-3 Ry)
+  // decimation near the real axis stays in FP64 (default: within 2e-4 Ry)
   if (decimation && std::fabs(c->ce.y) < c->dec_fp64_im) return false;
   return true;
 }

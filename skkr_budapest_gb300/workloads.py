@@ -117,7 +117,7 @@ def plain_fcc(nset: int = 22) -> SystemSpec:
 
 
 # per-energy IBZ subdivisions of the relativistic interface: 210 k far from the
-# real axis up to 12090 k at the contour point nearest E_F (Im E ~ 5e-3 Ry),
+# real axis up to 12090 k at the contour point nearest E_F (Im E = 5e-4 Ry),
 # grouped like the reference's KSETTAB/INTAB table
 REL_NSETS = [20] * 12 + [32] * 4 + [48] * 3 + [70] * 2 + [100, 125, 155]
 
