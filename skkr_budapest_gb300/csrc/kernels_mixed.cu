@@ -25,7 +25,8 @@
 // Staging layouts (bf16, K-major for both UMMA operands, tiled by k-block so
 // that one TMA box is one contiguous block):
 //   A'[item][s][kb][M'][32]   M' = 128 * mtiles, kb < kblocks = ceil(2n/32)
-//   B'[item][s][kb][N'][32]   N' = NT * ntiles (zero padded)
+//   B'[item][s][kb][N'][32]   N' = TN * ntiles (zero padded; TN = 96, or 64
+//                                 for the exact-level tile)
 // Tiles reach shared memory by TMA (3-D tensor maps, 64-byte swizzle).
 #include <cuda.h>
 #include <cuda_bf16.h>
@@ -46,6 +47,7 @@ constexpr int KB = 32;            // K per k-block (one 64-byte swizzle row of b
 constexpr int NSTAGE = 2;         // shared-memory pipeline stages
 constexpr int NACC = 5;           // TMEM accumulators: one per level p+q = 0..4
 constexpr long long WAIT_LIMIT = 1LL << 22;
+constexpr int OZ_THREADS = 384;   // 12 warps: producer and MMA lanes in warps 0-1, all 12 run the epilogue
 
 // ------------------------------------------------------------------ PTX helpers
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -334,6 +336,7 @@ __global__ void __launch_bounds__(256) k_split_b(MatRef B, int n, int K, int nc,
 struct OzArgs {
   int n, mtiles, ntiles, kblocks, nc, mode;
   int eoff;             // 32 + 2 (DB - 1): result = acc 2^(sigma_i + tau_j - eoff), acc in 2^-16 units
+  int db;               // digit bits DB
   const int *sigma;     // [item][M']  row scale exponents of A
   const int *tau;       // [item][n]   column scale exponents of B
   MatRef C, D, E;
@@ -344,6 +347,13 @@ struct OzArgs {
 // FP32 accumulator value -> int64 in units of 2^-16 (bit manipulation only).
 // Levels 0..3 hold exact multiples of 2^(16-DB l) >= 2^-8; the shared tail
 // level is truncated at 2^-16, about 2^-53 below the leading level.
+// exact level l <= 3 (its FP32 accumulator holds an integer N times
+// 2^(16 - DB l), |N| < 2^24) in the same 2^-16 units: N from one conversion,
+// then a shift (32 - DB l >= 0 for l <= 3); the result equals f2fix16(v)
+__device__ __forceinline__ long long level_fix16(float v, int l, int db) {
+  const int n = __float2int_rn(v * pow2f(db * l - 16));
+  return (long long)n << (32 - db * l);
+}
 __device__ __forceinline__ long long f2fix16(float v) {
   const int b = __float_as_int(v);
   const int ex = (b >> 23) & 0xFF;
@@ -393,9 +403,12 @@ __host__ __device__ constexpr int nlevels(int S) { return S < NA ? S : NA; }
 // TN: N tile (TMEM columns per accumulator); NA: TMEM accumulators, one per
 // level p+q = 0..NA-2 and a shared tail for the deeper levels (NA * TN <= 512).
 // (96, 5) is the default tile; (64, 7) keeps levels 0..5 exact and pushes the
-// truncation of the shared tail below 2^-60 of the leading level.
+// truncation of the shared tail below 2^-60 of the leading level.  Four
+// levels would not do: with the shared tail from level 3 on, the tensor
+// core's truncating FP32 addition leaves ~2^-47 of the leading level per
+// accumulation step in it (4e-12 over a 128-deep product instead of 7e-14).
 template <int S, int TN, int NA>
-__global__ void __launch_bounds__(256, 1) k_ozaki(const __grid_constant__ CUtensorMap tmA,
+__global__ void __launch_bounds__(OZ_THREADS, 1) k_ozaki(const __grid_constant__ CUtensorMap tmA,
                                                   const __grid_constant__ CUtensorMap tmB, OzArgs g) {
   static_assert(NA * TN <= 512 && TN % 32 == 0, "accumulators must fit the 512 TMEM columns");
   const int item = blockIdx.y;
@@ -416,7 +429,7 @@ __global__ void __launch_bounds__(256, 1) k_ozaki(const __grid_constant__ CUtens
     tmem_alloc(&tmem_base, 512);
     tmem_relinquish();
   }
-  if (threadIdx.x >= 64) {  // warps 2-7: column scales of the tile (read by the epilogue)
+  if (threadIdx.x >= 64) {  // warps 2-11: column scales of the tile (read by the epilogue)
     for (int t = threadIdx.x - 64; t < TN / 2; t += blockDim.x - 64) {
       const int j = (nt * TN) / 2 + t;
       col_exp[t] = j < g.n ? g.tau[(long long)item * g.n + j] : 0;
@@ -507,9 +520,9 @@ __global__ void __launch_bounds__(256, 1) k_ozaki(const __grid_constant__ CUtens
         mbar_wait(&bar_full[kb % NSTAGE], (kb / NSTAGE) & 1);
     }
   } else {
-    // epilogue, 8 warps: warp w reads TMEM lanes 32 (w % 4) .. +31 (rows of
-    // this M tile) and accumulator columns [48 (w / 4), +48)
-    const int quarter = warp & 3, half = warp >> 2;
+    // epilogue, 12 warps: warp w reads TMEM lanes 32 (w % 4) .. +31 (rows of
+    // this M tile) and the 16-column chunks part, part + 3, ... (part = w / 4)
+    const int quarter = warp & 3, part = warp >> 2;
     const int row = mt * MT + quarter * 32 + lane;
     const uint32_t lane_addr = tbase + ((uint32_t)(quarter * 32) << 16);
     const int kk = item / g.nc, cc = item % g.nc;
@@ -520,7 +533,7 @@ __global__ void __launch_bounds__(256, 1) k_ozaki(const __grid_constant__ CUtens
     double *pe = (double *)mat_ptr(g.E, kk, cc);
     constexpr int NL = nlevels<NA>(S);
 #pragma unroll 1
-    for (int c0 = half * (TN / 2); c0 < (half + 1) * (TN / 2); c0 += 16) {
+    for (int c0 = part * 16; c0 < TN; c0 += 3 * 16) {
       uint32_t v[NA][16];
 #pragma unroll
       for (int l = 0; l < NL; l++) tmem_ld16(lane_addr + l * TN + c0, v[l]);
@@ -533,8 +546,10 @@ __global__ void __launch_bounds__(256, 1) k_ozaki(const __grid_constant__ CUtens
           long long ar = 0, ai = 0;
 #pragma unroll
           for (int l = 0; l < NL; l++) {
-            ar += f2fix16(__uint_as_float(v[l][t]));
-            ai += f2fix16(__uint_as_float(v[l][t + 1]));
+            // exact levels by conversion and shift; the shared tail bitwise
+            const float vr = __uint_as_float(v[l][t]), vi = __uint_as_float(v[l][t + 1]);
+            ar += (l < NA - 1 && l <= 3) ? level_fix16(vr, l, g.db) : f2fix16(vr);
+            ai += (l < NA - 1 && l <= 3) ? level_fix16(vi, l, g.db) : f2fix16(vi);
           }
           const int e = erow + col_exp[(c0 + t) >> 1];
           const double2 val = make_double2(fix_to_double(ar, e), fix_to_double(ai, e));
@@ -569,44 +584,85 @@ __global__ void __launch_bounds__(256, 1) k_ozaki(const __grid_constant__ CUtens
 }
 
 // ------------------------------------------------------------------ FP32 GJ
-// Gauss-Jordan with column pivoting (main/gjinv.f) in complex FP32, the
-// matrix held in registers: TY*16 threads as a TY x 16 grid, thread (ty, tx)
-// owning rows ty + TY a (a < RA) and columns tx + 16 b (b < RB).  A step
-// stages the pivot column, the old column i and row i in shared memory (only
-// the owning threads write), then every thread updates its RA x RB block with
-// straight-line FMAs and selects (no per-element branches, so the compiler
-// interleaves the independent chains); the pivot of the next step (largest
-// |a(i+1, j)|^2, j > i, first index on ties) is reduced by the 16 threads
-// that own row i+1.  Two block barriers per step.  The result (written as
-// FP64) only seeds the Newton refinement.
-// Pivot of row `rowidx` (held by the 16 threads of one half warp): the
-// largest |a(rowidx, j)|^2 over jmin <= j < n, first index on ties.
+// Gauss-Jordan with column pivoting (main/gjinv.f: in row i the pivot is the
+// largest |a(i, j)| over the columns not yet used, first index on ties) in
+// complex FP32, the matrix held in registers: TY*16 threads as a TY x 16
+// grid, thread (ty, tx) owning rows ty + TY a (a < RA) and columns
+// tx + 16 b (b < RB); the 16 threads of one ty are one half warp.
+//
+// The pivot columns are not swapped into place: step i eliminates with the
+// pivot (i, kp) where it lies and records sigma(i) = kp, which is Gauss-Jordan
+// on A P (P the column permutation); the array then holds (A P)^-1 with its
+// columns stored at the positions of A P's, so A^-1(sigma(r), c) is found at
+// (r, sigma(c)) and the store permutes both indices.  With
+//   c_r = a(r,kp)/piv (r != i), c_i = -1/piv,   p_j = a(i,j) (j != kp), p_kp = 1
+// and row i and column kp masked to zero first, every element takes the same
+// update a(r,j) <- s(r,j) a(r,j) - c_r p_j (s = 0 on row i and column kp,
+// else 1): the rank-1 update, the scaled pivot row a(i,j)/piv, the pivot
+// column -a(r,kp)/piv and the pivot 1/piv, as packed FP32x2 multiply-adds.
+// a(r,kp) comes from the owner in the same half warp (a shuffle); the pivot
+// row and the next pivot index are staged in shared memory (double-buffered)
+// by the 16 threads that own row i+1 after their update: one block barrier
+// per step.  The result
+// (written as FP64) only seeds the Newton refinement.
+
+__device__ __forceinline__ unsigned long long pk2(float x, float y) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(x), "f"(y));
+  return r;
+}
+__device__ __forceinline__ float2 upk2(unsigned long long r) {
+  float2 v;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(v.x), "=f"(v.y) : "l"(r));
+  return v;
+}
+__device__ __forceinline__ unsigned long long fma2(unsigned long long a, unsigned long long b,
+                                                   unsigned long long c) {
+  unsigned long long d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+__device__ __forceinline__ unsigned long long mul2(unsigned long long a, unsigned long long b) {
+  unsigned long long d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+
+// Pivot of row `row` among the unused columns (the row's owners: one half
+// warp): the largest |a(row, j)|^2, first index on ties; the row is staged
+// into `rowbuf` on the way.  Every candidate NaN: the first unused column.
 template <int TY, int RA, int RB>
-__device__ __forceinline__ void gj_row_pivot(const float2 (&m)[RA][RB], int rowidx, int jmin, int n, int tx,
-                                             unsigned hmask, int *kp_out) {
-  const int iar = rowidx / TY;
+__device__ __forceinline__ void gj_search(const unsigned long long (&m)[RA][RB], int row, unsigned used, int tx,
+                                          unsigned hmask, float2 *rowbuf, int *kp_out) {
+  const int iar = row / TY;
   float best = -1.f;
-  int bj = 0x7FFFFFFF;
+  int bj = 0x7FFFFFFF, fu = 0x7FFFFFFF;
 #pragma unroll
   for (int ib = 0; ib < RB; ib++) {
-    float2 v = m[0][ib];
+    unsigned long long w = m[0][ib];
 #pragma unroll
-    for (int ia = 1; ia < RA; ia++) v = (ia == iar) ? m[ia][ib] : v;  // static indices keep m in registers
+    for (int ia = 1; ia < RA; ia++) w = (ia == iar) ? m[ia][ib] : w;  // static indices keep m in registers
+    const float2 v = upk2(w);
     const int j = tx + 16 * ib;
+    rowbuf[j] = v;
+    const bool free = !((used >> ib) & 1u);
     const float mm = v.x * v.x + v.y * v.y;
-    const bool ok = j >= jmin && j < n && (mm > best || (mm == best && j < bj));
+    const bool ok = free && (mm > best || (mm == best && j < bj));
     best = ok ? mm : best;
     bj = ok ? j : bj;
+    fu = (free && j < fu) ? j : fu;
   }
 #pragma unroll
   for (int o = 8; o > 0; o >>= 1) {
     const float ob = __shfl_xor_sync(hmask, best, o, 16);
     const int oj = __shfl_xor_sync(hmask, bj, o, 16);
+    const int of = __shfl_xor_sync(hmask, fu, o, 16);
     const bool take = ob > best || (ob == best && oj < bj);
     best = take ? ob : best;
     bj = take ? oj : bj;
+    fu = of < fu ? of : fu;
   }
-  if (bj >= n) bj = jmin;  // all candidates NaN: keep the index in range
+  if (bj == 0x7FFFFFFF) bj = fu;
   if (tx == 0) *kp_out = bj;
 }
 
@@ -616,12 +672,12 @@ __global__ void __launch_bounds__(TY * 16, 1) k_cgj32(MatRef A, MatRef X, int n,
   constexpr int NR = TY * RA, NCOL = 16 * RB;
   const int item = blockIdx.x, kk = item / nc, cc = item % nc;
   if (act && !act[item]) return;
-  __shared__ float2 pc[NR], oc[NR], rowi[NCOL];
-  __shared__ int ind[NR], dest[NR];
-  __shared__ int kp_next;
+  __shared__ float2 rowi[2][NCOL];
+  __shared__ int sig[NR], sinv[NCOL];
+  __shared__ int kpn[2];
   const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
   const zd *a = mat_ptr(A, kk, cc);
-  float2 m[RA][RB];
+  unsigned long long m[RA][RB];  // (re, im) pairs
 #pragma unroll
   for (int ia = 0; ia < RA; ia++)
 #pragma unroll
@@ -632,102 +688,75 @@ __global__ void __launch_bounds__(TY * 16, 1) k_cgj32(MatRef A, MatRef X, int n,
         const zd w = a[r + (long long)j * A.ld];
         v = make_float2((float)w.x, (float)w.y);
       }
-      m[ia][ib] = v;
+      m[ia][ib] = pk2(v.x, v.y);
     }
+  // columns j >= n never pivot
+  unsigned used = 0;
+#pragma unroll
+  for (int ib = 0; ib < RB; ib++)
+    if (tx + 16 * ib >= n) used |= 1u << ib;
   const unsigned hmask = (ty & 1) ? 0xFFFF0000u : 0x0000FFFFu;  // the 16 threads of this ty
-  if (ty == 0) gj_row_pivot<TY, RA, RB>(m, 0, 0, n, tx, hmask, &kp_next);
+
+  if (ty == 0) gj_search<TY, RA, RB>(m, 0, used, tx, hmask, rowi[0], &kpn[0]);
   __syncthreads();
   for (int i = 0; i < n; i++) {
-    const int kp = kp_next;
-    // stage: pivot column kp -> pc, old column i -> oc, row i -> rowi (owners
-    // only); select chains over static indices keep m in registers
-    if (tx == (kp & 15)) {
-      const int kb = kp >> 4;
-#pragma unroll
-      for (int ia = 0; ia < RA; ia++) {
-        float2 v = m[ia][0];
-#pragma unroll
-        for (int ib = 1; ib < RB; ib++) v = (ib == kb) ? m[ia][ib] : v;
-        pc[ty + TY * ia] = v;
-      }
+    const int kp = kpn[i & 1], kb = kp >> 4, kt = kp & 15;
+    if (tid == 0) {
+      sig[i] = kp;
+      sinv[kp] = i;
     }
-    if (tx == (i & 15)) {
-      const int ibi = i >> 4;
-#pragma unroll
-      for (int ia = 0; ia < RA; ia++) {
-        float2 v = m[ia][0];
-#pragma unroll
-        for (int ib = 1; ib < RB; ib++) v = (ib == ibi) ? m[ia][ib] : v;
-        oc[ty + TY * ia] = v;
-      }
-    }
-    if (ty == i % TY) {
-      const int iai = i / TY;
-#pragma unroll
-      for (int ib = 0; ib < RB; ib++) {
-        float2 v = m[0][ib];
-#pragma unroll
-        for (int ia = 1; ia < RA; ia++) v = (ia == iai) ? m[ia][ib] : v;
-        rowi[tx + 16 * ib] = v;
-      }
-    }
-    if (tid == 0) ind[i] = kp;
-    __syncthreads();
-    const float2 piv = pc[i];
-    const float den = piv.x * piv.x + piv.y * piv.y;
-    const float2 q = make_float2(piv.x / den, -piv.y / den);
-    const float2 rw_i = rowi[i], rw_kp = rowi[kp];
-    float2 cr[RA], ocr[RA], rj[RB];
+    if (tx == kt) used |= 1u << kb;
+    const float2 *ri = rowi[i & 1];
+    const float2 piv = ri[kp];
+    const float rden = __frcp_rn(piv.x * piv.x + piv.y * piv.y);
+    const float2 q = make_float2(piv.x * rden, -piv.y * rden);
+    // multipliers c_r as the pairs (-Re c, -Re c) and (Im c, Im c); row mask
+    unsigned long long ncx[RA], cy[RA];
+    float f[RA];
 #pragma unroll
     for (int ia = 0; ia < RA; ia++) {
-      const int r = ty + TY * ia;
-      const float2 v = pc[r];
-      cr[ia] = (r == i) ? q : make_float2(v.x * q.x - v.y * q.y, v.x * q.y + v.y * q.x);
-      ocr[ia] = oc[r];
+      unsigned long long w = m[ia][0];
+#pragma unroll
+      for (int ib = 1; ib < RB; ib++) w = (ib == kb) ? m[ia][ib] : w;
+      w = __shfl_sync(0xFFFFFFFFu, w, kt, 16);  // a(r, kp) from its owner in this half warp
+      const float2 v = upk2(w);
+      const bool isrow = ty + TY * ia == i;
+      const float2 cr = isrow ? make_float2(-q.x, -q.y)
+                              : make_float2(v.x * q.x - v.y * q.y, v.x * q.y + v.y * q.x);
+      ncx[ia] = pk2(-cr.x, -cr.x);
+      cy[ia] = pk2(cr.y, cr.y);
+      f[ia] = isrow ? 0.f : 1.f;
     }
+    // row i+1's owners reduce the next pivot after their update
+    const bool srch = i + 1 < n && ty == ((i + 1) % TY);
 #pragma unroll
     for (int ib = 0; ib < RB; ib++) {
       const int j = tx + 16 * ib;
-      const float2 w = rowi[j];
-      rj[ib] = (j == i) ? rw_kp : ((j == kp) ? rw_i : w);
-    }
+      const bool iscol = j == kp;
+      const float2 p = iscol ? make_float2(1.f, 0.f) : ri[j];
+      const float g = iscol ? 0.f : 1.f;
+      const unsigned long long pp = pk2(p.x, p.y), ps = pk2(p.y, -p.x);
 #pragma unroll
-    for (int ia = 0; ia < RA; ia++) {
-      const bool isrow = (ty + TY * ia) == i;
-#pragma unroll
-      for (int ib = 0; ib < RB; ib++) {
-        const int j = tx + 16 * ib;
-        float2 v = (j == kp) ? ocr[ia] : m[ia][ib];  // the old column i moves to kp
-        v = isrow ? make_float2(0.f, 0.f) : v;
-        v.x = fmaf(-cr[ia].x, rj[ib].x, v.x);
-        v.x = fmaf(cr[ia].y, rj[ib].y, v.x);
-        v.y = fmaf(-cr[ia].x, rj[ib].y, v.y);
-        v.y = fmaf(-cr[ia].y, rj[ib].x, v.y);
-        m[ia][ib] = (j == i) ? cr[ia] : v;
+      for (int ia = 0; ia < RA; ia++) {
+        const float sm = f[ia] * g;
+        const unsigned long long t = fma2(cy[ia], ps, mul2(ncx[ia], pp));
+        m[ia][ib] = fma2(m[ia][ib], pk2(sm, sm), t);
       }
     }
-    if (i + 1 < n && ty == ((i + 1) % TY)) gj_row_pivot<TY, RA, RB>(m, i + 1, i + 1, n, tx, hmask, &kp_next);
+    if (srch) gj_search<TY, RA, RB>(m, i + 1, used, tx, hmask, rowi[(i + 1) & 1], &kpn[(i + 1) & 1]);
     __syncthreads();
   }
-  // final row swaps of gjinv.f (i = n-1 .. 0: rows i <-> ind[i]) as one permutation
-  if (tid == 0) {
-    for (int r = 0; r < n; r++) dest[r] = r;  // dest[pos] = original row now at pos
-    for (int i2 = n - 1; i2 >= 0; i2--) {
-      const int j = ind[i2];
-      const int t = dest[i2];
-      dest[i2] = dest[j];
-      dest[j] = t;
-    }
-    for (int pos = 0; pos < n; pos++) ind[dest[pos]] = pos;  // ind[orig row] = final position
-  }
-  __syncthreads();
+  // storage (r, j) holds A^-1(sigma(r), sigma^-1(j))
   zd *x = mat_ptr(X, kk, cc);
 #pragma unroll
   for (int ia = 0; ia < RA; ia++)
 #pragma unroll
     for (int ib = 0; ib < RB; ib++) {
       const int r = ty + TY * ia, j = tx + 16 * ib;
-      if (r < n && j < n) x[ind[r] + (long long)j * X.ld] = make_double2((double)m[ia][ib].x, (double)m[ia][ib].y);
+      if (r < n && j < n) {
+        const float2 v = upk2(m[ia][ib]);
+        x[sig[r] + (long long)sinv[j] * X.ld] = make_double2((double)v.x, (double)v.y);
+      }
     }
 }
 
@@ -979,6 +1008,7 @@ static int gemm_s(MixedWork *w, int mode, int sa, int sb, const MatRef &C, const
   g.nc = nc;
   g.mode = mode;
   g.eoff = 32 + 2 * (A.DB - 1);
+  g.db = A.DB;
   g.sigma = A.scale;
   g.tau = B.scale;
   g.C = C;
@@ -986,11 +1016,11 @@ static int gemm_s(MixedWork *w, int mode, int sa, int sb, const MatRef &C, const
   g.E = E;
   g.act = act;
   g.err = w->err;
-  dim3 grid(mtiles * ntiles, items);
   const long long active = act ? skkr_active_items(items) : items;
   // algorithmic BF16 tensor work: S(S+1)/2 real products of n x 2K x 2n per item
   kstat_begin(KS_OZAKI, (double)(S * (S + 1) / 2) * 8.0 * n * (double)n * K * (double)active, st);
-  k_ozaki<S, TN, NA><<<grid, 256, smem, st>>>(ma, mb, g);
+  dim3 grid(mtiles * ntiles, items);
+  k_ozaki<S, TN, NA><<<grid, OZ_THREADS, smem, st>>>(ma, mb, g);
   kstat_end(st);
   SKKR_LAUNCHED();
   return 0;
