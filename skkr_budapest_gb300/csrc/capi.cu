@@ -677,7 +677,7 @@ static int eng_inv(skkr_ctx *c, bool mixed, const MatRef &A, const MatRef &X, bo
                    int nc, const int *act) {
   if (mixed && n <= 128)
     return mixed_zinv(c->mw, A, X, n, nk, nc, act, 2, std::min(8, std::max(c->slices_res, slices_for(c) + 1)),
-                      true, c->st);
+                      inplace, c->st);
   if (!inplace) launch_zaxpby(X, A, nullptr, 0, nullptr, 0, n, nk, nc, act, c->st);
   launch_zgj(X, n, nk, nc, act, c->st);
   return SKKR_OK;

@@ -85,7 +85,7 @@ int mixed_zgemm_k(MixedWork *w, int mode, int S, const MatRef &A, const MatRef &
 int mixed_zgemm(MixedWork *w, int mode, int S, const MatRef &A, const MatRef &B, const MatRef &C,
                 const MatRef &D, const MatRef &E, int n, int nk, int nc, const int *act, cudaStream_t st);
 int mixed_zinv(MixedWork *w, const MatRef &A, const MatRef &X, int n, int nk, int nc, const int *act,
-               int newton, int sres, bool track_resid, cudaStream_t st);
+               int newton, int sres, bool inplace, cudaStream_t st);
 // running maximum of the accepted Newton residual norms and the count of
 // inverses redone in FP64 (device scalars), and the count of inverses that
 // took further Newton steps (host): reset asynchronously, read with a

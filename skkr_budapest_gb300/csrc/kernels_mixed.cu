@@ -1123,22 +1123,23 @@ __global__ void k_newton_select(const double *__restrict__ rn, const int *__rest
 }
 
 // X = A^-1: FP32 Gauss-Jordan, then `newton` steps X += X (I - A X) with the
-// residual product at S = sres slices and the correction at S = 3.  X may
-// alias A.
+// residual product at S = sres slices and the correction at S = 3.  X may be
+// A itself (`inplace`); otherwise the two must not overlap.
 int mixed_zinv(MixedWork *w, const MatRef &A, const MatRef &X, int n, int nk, int nc, const int *act,
-               int newton, int sres, bool track_resid, cudaStream_t st) {
-  (void)track_resid;
+               int newton, int sres, bool inplace, cudaStream_t st) {
   if (n < 1 || n > 128 || newton < 1) return SKKR_ERR_ARG;
   const long long items = (long long)nk * nc, MB = (long long)n * n;
   int rc;
-  if ((rc = grow((void **)&w->acopy, &w->ac_cap, (size_t)items * MB * sizeof(zd), false))) return rc;
+  if (inplace && (rc = grow((void **)&w->acopy, &w->ac_cap, (size_t)items * MB * sizeof(zd), false))) return rc;
   if ((rc = grow((void **)&w->rbuf, &w->rb_cap, (size_t)items * MB * sizeof(zd), false))) return rc;
   if ((rc = grow((void **)&w->rnorm, &w->rn_cap, (size_t)items * sizeof(double), false))) return rc;
   if ((rc = grow((void **)&w->flag, &w->flag_cap, (size_t)items * sizeof(int), false))) return rc;
   if ((rc = grow((void **)&w->mark, &w->mark_cap, (size_t)items * sizeof(int), false))) return rc;
-  MatRef Ac = mref(w->acopy, (long long)nc * MB, MB, n);
+  // A itself serves the Gauss-Jordan start, the residuals and the FP64 redo
+  // unless X overwrites it (in place): then a copy does
+  const MatRef Ac = inplace ? mref(w->acopy, (long long)nc * MB, MB, n) : A;
   MatRef R = mref(w->rbuf, (long long)nc * MB, MB, n);
-  launch_zaxpby(Ac, A, nullptr, 0, nullptr, 0, n, nk, nc, act, st);
+  if (inplace) launch_zaxpby(Ac, A, nullptr, 0, nullptr, 0, n, nk, nc, act, st);
   kstat_begin(KS_GJ, 8.0 * n * (double)n * n * (double)(act ? skkr_active_items(items) : items), st);
   if (n <= 32) k_cgj32<16, 2, 2><<<(unsigned)items, 256, 0, st>>>(Ac, X, n, nc, act);
   else if (n <= 64) k_cgj32<16, 4, 4><<<(unsigned)items, 256, 0, st>>>(Ac, X, n, nc, act);
