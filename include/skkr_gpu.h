@@ -120,7 +120,8 @@ int skkr_gpu_destroy(skkr_ctx *ctx);
  * exact-level tile when |Im E| < near_im (defaults 7 slices below 1e-3 Ry;
  * 3..8, 0 = off);
  * every k point whose contribution exceeds dominant_frac (default 1e-2) of
- * the norm of the k-summed tau is recomputed in FP64 (0 = off).  Inverses
+ * the norm of the k-summed tau, and ten times the mean contribution of a k
+ * point (an isolated peak), is recomputed in FP64 (0 = off).  Inverses
  * whose Newton residual is above 1e-6 after the standard steps take up to
  * four further steps while it stays below 1/2; those still above 1e-6 are
  * always redone in FP64. */

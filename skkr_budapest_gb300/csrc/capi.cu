@@ -1079,13 +1079,16 @@ static int reduce_tauc(skkr_ctx *c, bool failed) {
 // Accuracy guard of the split-precision path: near the real axis a few k
 // points sit close to an interface resonance, carry much of |sum_k tau_k| and
 // see the product rounding amplified by their conditioning.  Every k whose
-// contribution exceeds dominant_frac of the k-summed norm is recomputed in
-// FP64 and its contribution swapped in the class sums: the selected k are
+// contribution exceeds dominant_frac of the k-summed norm and DOMINANT_PEAK
+// times the mean per-k norm is recomputed in FP64 and its contribution
+// swapped in the class sums: the selected k are
 // gathered into compact buffers (structure-constant blocks, cached surface
 // operators, weights) that stand in for the context's, their mixed
 // contribution is recomputed from the same cached state and subtracted, the
 // decimation and tau2d are redone in FP64 and added, and the FP64 surface
 // operators are scattered back for the later CPA iterations.
+constexpr double DOMINANT_PEAK = 10.0;  // a redone k point carries this many times the mean per-k norm
+
 static int redo_dominant_k(skkr_ctx *c, int itcpa, const std::vector<int> &lcls, const std::vector<int> &rcls,
                            const std::vector<int> &icls) {
   (void)itcpa;
@@ -1103,7 +1106,13 @@ static int redo_dominant_k(skkr_ctx *c, int itcpa, const std::vector<int> &lcls,
   CK(cudaStreamSynchronize(st));
   double s2 = 0.0;
   for (const zd &v : Sh) s2 += v.x * v.x + v.y * v.y;
-  const double lim = c->dominant_frac * std::sqrt(s2);
+  // an isolated peak of the integrand: above dominant_frac of the k-summed
+  // norm and above DOMINANT_PEAK times the mean per-k norm (on coarse meshes
+  // of smooth integrands the largest points stay within a few times the mean,
+  // and their split-precision rounding is not amplified)
+  double ksum = 0.0;
+  for (int k = 0; k < nk; k++) ksum += kn[k];
+  const double lim = std::max(c->dominant_frac * std::sqrt(s2), DOMINANT_PEAK * ksum / nk);
   std::vector<int> sel;
   for (int k = 0; k < nk; k++)
     if (kn[k] > lim) sel.push_back(k);

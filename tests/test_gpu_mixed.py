@@ -65,6 +65,37 @@ def test_mixed_inverse_refined_to_fp64(n):
     assert resid < 1e-5
 
 
+@pytest.mark.parametrize("cond", [1e3, 1e5, 1e6])
+def test_mixed_inverse_ill_conditioned(cond):
+    # singular values spread over `cond`: the FP32 start leaves |I - AX| up
+    # to ~cond 2^-24, so the larger conditions go through the further Newton
+    # steps (or the FP64 redo); the result is held to FP64 accuracy
+    n = 128
+    u, _ = np.linalg.qr(crand(n, n))
+    v, _ = np.linalg.qr(crand(n, n))
+    a = np.stack([u @ np.diag(np.logspace(0, -np.log10(cond), n)) @ v.conj().T for _ in range(2)])
+    a[1] = a[1].T
+    x, resid = native.zinv_batch(a, precision="mixed", newton=2)
+    # the floor is the residual product's rounding amplified by cond(A); two
+    # plain Newton steps from the FP32 start would stop near (cond 2^-24)^4
+    for i in range(2):
+        ref = np.linalg.inv(a[i])
+        assert rel(x[i], ref) < 2e-14 * cond, (cond, rel(x[i], ref))
+        assert np.abs(a[i] @ x[i] - np.eye(n)).max() < 1e-13 * cond
+    assert resid < 1e-5
+
+
+def test_mixed_inverse_nan_input_is_contained():
+    # a NaN item neither faults nor leaks into its batch neighbours
+    n = 64
+    a = crand(3, n, n) + 3 * np.eye(n)
+    a[1, 5, 7] = np.nan
+    x, _ = native.zinv_batch(a, precision="mixed", newton=2)
+    assert np.isnan(x[1]).any()
+    for i in (0, 2):
+        assert rel(x[i], np.linalg.inv(a[i])) < 1e-12
+
+
 def _compare_mixed(ep):
     g = api.cpacoord(ep, precision="mixed")
     o = O.cpacoord(ep, nthreads=8)
