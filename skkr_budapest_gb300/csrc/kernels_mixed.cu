@@ -114,24 +114,6 @@ __device__ __forceinline__ void tc_fence_before() {
 __device__ __forceinline__ void tc_fence_after() {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
-// 32 consecutive FP32 columns of this thread's TMEM lane
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
-  uint32_t r[32];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
-        "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
-        "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
-        "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr)
-      : "memory");
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
-}
-
 // 16 consecutive accumulator columns of this warp's 32 TMEM lanes, without
 // the wait (tmem_ld_wait after a batch of loads)
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t *r) {
@@ -363,16 +345,10 @@ __device__ __forceinline__ long long f2fix16(float v) {
   const long long m = sh >= 0 ? (mant << sh) : (sh > -31 ? (mant >> -sh) : 0);
   return b < 0 ? -m : m;
 }
-// x * 2^e for a normal double x by exponent addition (x == 0 stays 0)
-__device__ __forceinline__ double scale_pow2(double x, int e) {
-  if (x == 0.0) return 0.0;
-  return __longlong_as_double(__double_as_longlong(x) + ((long long)e << 52));
-}
-
 // round-to-nearest-even double of a * 2^e from integer operations only (the
 // FP64 pipe of this GPU is ~1/40 of the integer rate): normalise with a
 // leading-zero count, keep 53 bits, round on the dropped 11, add e to the
-// exponent.  Equal to scale_pow2(__ll2double_rn(a), e) for normal results.
+// exponent.  Equal to __ll2double_rn(a) * 2^e for normal results.
 __device__ __forceinline__ double fix_to_double(long long a, int e) {
   if (a == 0) return 0.0;
   const unsigned long long sign = a < 0 ? 0x8000000000000000ull : 0ull;
