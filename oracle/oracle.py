@@ -287,3 +287,66 @@ def cpacoord(ep, nthreads=1, tminv=None, reduce=None):
                 tminv=from_cm(ti), cpa_iterations=res.cpa_iterations, cpa_error=res.cpa_error,
                 sgf_status=res.sgf_status, max_dec_iters=res.max_dec_iters,
                 dec_iters_total=res.dec_iters_total)
+
+
+def tauij(ep, pairs, a1, a2, cvec, a0mat, tminv=None, nthreads=1):
+    """Off-diagonal k sums of one energy problem with fixed t^-1 (no CPA
+    update): for each pair (n1, n2, li, lj) the inter-site tau between layer
+    li in cell 0 and layer lj in cell n1 a1 + n2 a2, and back
+    (skkr_dbogo_bsf/rsp-scf/cpacoord_ksave.f:760-840 with tau2d_god.f);
+    a0mat[g] is the 2x2 in-plane rotation of group operation g, cvec[l] the
+    in-plane position of interface layer l.  Returns dict tau_ij, tau_ji
+    [pair,row,col], tauc [layer,row,col], status."""
+    keep = []
+
+    def arr(a, dt):
+        a = np.ascontiguousarray(a, dt)
+        keep.append(a)
+        return a
+
+    lk = ep.lkmax
+    blk = arr(ep.blkmap, np.int32)
+    bdg = ep.irel == 2
+    gmap = G2DMap(ep.lmax, (ep.lmax + 1) ** 2, blk.shape[0], blk.shape[1], (blk.shape[2] - 1) // 2,
+                  _ptr(blk), int(bdg), ep.rt.nblk, _zc(ep.fach if bdg else 0.0))
+    nin = arr(ep.ninprc, np.int32)
+    xk = arr(ep.xk, np.float64)
+    wk = arr(ep.wk, np.float64)
+    lg = arr(to_cm(ep.lg), np.complex128)
+    rg = arr(to_cm(ep.rg), np.complex128)
+    rs = arr(ep.rt.rstart, np.int32)
+    rv = arr(ep.rt.rvec, np.float64)
+    gR = arr(to_cm(np.concatenate([ep.rt.gR, ep.rt_h.gR]) if bdg else ep.rt.gR), np.complex128)
+    pr = Problem(ep.irel, ep.lmax, lk, ep.nprc, _ptr(nin), int(ep.bulkgeo), ep.nintfc,
+                 C.cast(C.pointer(gmap), C.c_void_p), len(xk), _ptr(xk), _ptr(wk), len(lg), _ptr(lg),
+                 _ptr(rg), ep.itermaxl, ep.itermaxr, ep.errmax, ep.itcpam, ep.cpatol, _zc(ep.fac),
+                 ep.rt.nblk, _ptr(rs), _ptr(rv), _ptr(gR))
+    tl = arr(to_cm(ep.tminvl), np.complex128)
+    tr = arr(to_cm(ep.tminvr), np.complex128)
+    ti = arr(to_cm(ep.tminv if tminv is None else tminv), np.complex128)
+    pa = arr(np.asarray(pairs, np.int32).reshape(-1, 4), np.int32)
+    npair = len(pa)
+    va1 = arr(a1, np.float64)
+    va2 = arr(a2, np.float64)
+    cv = arr(np.asarray(cvec, np.float64).reshape(-1, 2), np.float64)
+    am = arr(np.asarray(a0mat, np.float64).reshape(-1, 4), np.float64)
+    tij = np.zeros((max(npair, 1), lk, lk), np.complex128)
+    tji = np.zeros_like(tij)
+    tauc = np.zeros((ep.nintfc, lk, lk), np.complex128)
+    L = lib()
+    L.orc_tauij.restype = C.c_int
+    st = L.orc_tauij(C.cast(C.pointer(pr), C.c_void_p), _ptr(tl), _ptr(tr), _ptr(ti), npair, _ptr(pa),
+                     _ptr(va1), _ptr(va2), _ptr(cv), _ptr(am), _ptr(tij), _ptr(tji), _ptr(tauc), lk,
+                     nthreads)
+    return dict(status=st, tau_ij=from_cm(tij)[:npair], tau_ji=from_cm(tji)[:npair], tauc=from_cm(tauc))
+
+
+def tau2dgod_k(ep, ik, tminv=None):
+    """Full layer-pair tau of one k point (ngeff classes ignored: the first
+    group element only), for checks against a direct inverse."""
+    ep1 = ep.with_k(ep.xk[ik:ik + 1], np.array([1.0]))
+    ep1.lg, ep1.rg = ep.lg[:1], ep.rg[:1]
+    n = ep.nintfc
+    pairs = [(0, 0, a, b) for a in range(n) for b in range(n)]
+    r = tauij(ep1, pairs, [1.0, 0.0], [0.0, 1.0], np.zeros((n, 2)), [[1.0, 0.0, 0.0, 1.0]], tminv=tminv)
+    return r["tau_ij"].reshape(n, n, ep.lkmax, ep.lkmax)

@@ -463,6 +463,138 @@ void orc_tau2d(int irel, double wgeff, int bulkgeo, const int *ninprc,
 }
 
 /* ===================================================================== *
+ * skkr_dbogo_bsf/clu/tau2d_god.f:2-270  full Godfrin tau: every layer    *
+ * pair of the interface.  The forward and backward sweeps are tau2d.f's; *
+ * dd(p) = -(m00 - yy(p))^-1 m01 and cc(p) = -(tau00(p) - xx(p))^-1 m10   *
+ * are kept, and the PL-diagonal tau(p,p) is carried down the slab by      *
+ * tau(q,p) = cc(q) tau(q-1,p) (q > p) and up by tau(q,p) = dd(q)          *
+ * tau(q+1,p) (q < p).  tauij[(a*nintfc + b)*ld*ld] = wgeff tau_{a,b}     *
+ * (row layer a, column layer b).                                          *
+ * ===================================================================== */
+void orc_tau2dgod(int irel, double wgeff, int bulkgeo, const int *ninprc,
+                  int nprc, const orc_g2dmap *map, const zc *blocks,
+                  const zc *tminv, int lkmaxp, int lkmax, const zc *x,
+                  const zc *y, int mdimp, zc *tauij, int nintfc, zc fac) {
+  int mdim = mdimp;
+  size_t sz = (size_t)mdim * mdim, lsz = (size_t)lkmaxp * lkmaxp;
+  zc *xx = calloc(sz * nprc, sizeof(zc)), *yy = calloc(sz * nprc, sizeof(zc));
+  zc *tau00 = calloc(sz * nprc, sizeof(zc));
+  zc *cc = calloc(sz * nprc, sizeof(zc)), *dd = calloc(sz * nprc, sizeof(zc));
+  zc *m00 = calloc(sz, sizeof(zc)), *m01 = calloc(sz, sizeof(zc)), *m10 = calloc(sz, sizeof(zc));
+  zc *help = calloc(sz, sizeof(zc)), *help1 = calloc(sz, sizeof(zc));
+  int *nnprc = calloc(nprc, sizeof(int));
+  zc detl;
+  for (int ipl = 0, acc = 0; ipl < nprc; ipl++) {
+    nnprc[ipl] = acc;
+    acc += ninprc[ipl + 1];
+  }
+  int ndim = lkmax * ninprc[1];
+  for (int i = 0; i < ndim; i++)
+    for (int j = 0; j < ndim; j++) yy[IX(i, j, mdim)] = y[IX(i, j, mdimp)];
+  ndim = lkmax * ninprc[nprc];
+  for (int i = 0; i < ndim; i++)
+    for (int j = 0; j < ndim; j++) xx[IX(i, j, mdim) + sz * (nprc - 1)] = x[IX(i, j, mdimp)];
+
+  int ilay = 0;
+  for (int ipl = 1; ipl <= nprc; ipl++) {
+    int slot = bulkgeo ? 1 : ipl;
+    ndim = lkmax * ninprc[ipl];
+    orc_packer(ninprc[ipl], ninprc[ipl - 1], ninprc[ipl + 1], map, slot, blocks, m00, m10, m01,
+               lkmax, mdim, irel, fac);
+    for (int li = 0; li < ninprc[ipl]; li++) {
+      for (int k1 = 0; k1 < lkmax; k1++)
+        for (int k2 = 0; k2 < lkmax; k2++) {
+          int kk1 = li * lkmax + k1, kk2 = li * lkmax + k2;
+          m00[IX(kk1, kk2, mdim)] = tminv[IX(k1, k2, lkmaxp) + (size_t)ilay * lsz] + m00[IX(kk1, kk2, mdim)];
+        }
+      ilay++;
+    }
+    zc *t00 = tau00 + sz * (ipl - 1), *yyp = yy + sz * (ipl - 1);
+    for (int i = 0; i < ndim; i++)
+      for (int j = 0; j < ndim; j++) t00[IX(i, j, mdim)] = m00[IX(i, j, mdim)];
+    if (ipl > 1) {
+      int ndim0 = lkmax * ninprc[ipl - 1];
+      orc_doubmt2(m10, yyp, help, ndim, ndim0, ndim, mdim);
+      for (int i = 0; i < ndim; i++)
+        for (int j = 0; j < ndim; j++) yyp[IX(i, j, mdim)] = help[IX(i, j, mdim)];
+    }
+    if (ipl < nprc) {
+      int ndim1 = lkmax * ninprc[ipl + 1];
+      for (int i = 0; i < ndim; i++)
+        for (int j = 0; j < ndim; j++) m00[IX(i, j, mdim)] -= yyp[IX(i, j, mdim)];
+      orc_gjinv(m00, ndim, mdim, &detl);
+      orc_doubmt2(m00, m01, yy + sz * ipl, ndim, ndim, ndim1, mdim);
+      zc *ddp = dd + sz * (ipl - 1), *yn = yy + sz * ipl;   /* dd = -yy(ipl+1), tau2d_god.f:85-90 */
+      for (int i = 0; i < ndim1; i++)
+        for (int j = 0; j < ndim; j++) ddp[IX(j, i, mdim)] = -yn[IX(j, i, mdim)];
+    }
+  }
+  for (int ipl = nprc; ipl >= 1; ipl--) {
+    int slot = bulkgeo ? 1 : ipl;
+    ndim = lkmax * ninprc[ipl];
+    orc_packer(ninprc[ipl], ninprc[ipl - 1], ninprc[ipl + 1], map, slot, blocks, m00, m10, m01,
+               lkmax, mdim, irel, fac);
+    zc *xxp = xx + sz * (ipl - 1);
+    if (ipl < nprc) {
+      int ndim1 = lkmax * ninprc[ipl + 1];
+      orc_doubmt2(m01, xxp, m00, ndim, ndim1, ndim, mdim);
+      for (int i = 0; i < ndim; i++)
+        for (int j = 0; j < ndim; j++) xxp[IX(i, j, mdim)] = m00[IX(i, j, mdim)];
+    }
+    if (ipl > 1) {
+      int ndim0 = lkmax * ninprc[ipl - 1];
+      zc *t00 = tau00 + sz * (ipl - 1);
+      for (int i = 0; i < ndim; i++)
+        for (int j = 0; j < ndim; j++) m00[IX(i, j, mdim)] = t00[IX(i, j, mdim)] - xxp[IX(i, j, mdim)];
+      orc_gjinv(m00, ndim, mdim, &detl);
+      orc_doubmt2(m00, m10, xx + sz * (ipl - 2), ndim, ndim, ndim0, mdim);
+      zc *ccp = cc + sz * (ipl - 1), *xn = xx + sz * (ipl - 2);  /* cc = -xx(ipl-1), :108-113 */
+      for (int i = 0; i < ndim0; i++)
+        for (int j = 0; j < ndim; j++) ccp[IX(j, i, mdim)] = -xn[IX(j, i, mdim)];
+    }
+  }
+  for (int ip = 0; ip < nprc; ip++) {
+    ndim = lkmax * ninprc[ip + 1];
+    zc *t00 = tau00 + sz * ip, *xxp = xx + sz * ip, *yyp = yy + sz * ip;
+    for (int i = 0; i < ndim; i++)
+      for (int j = 0; j < ndim; j++)
+        t00[IX(i, j, mdim)] = t00[IX(i, j, mdim)] - xxp[IX(i, j, mdim)] - yyp[IX(i, j, mdim)];
+    orc_gjinv(t00, ndim, mdim, &detl);
+    /* PL block (q, ip) -> layer blocks (nnprc[q] + a, nnprc[ip] + b) */
+#define PUT_BLOCK(Q, HB)                                                                          \
+    for (int a = 0; a < ninprc[(Q) + 1]; a++)                                                     \
+      for (int b = 0; b < ninprc[ip + 1]; b++) {                                                  \
+        zc *tl = tauij + ((size_t)(nnprc[Q] + a) * nintfc + (nnprc[ip] + b)) * lsz;               \
+        for (int r = 0; r < lkmax; r++)                                                           \
+          for (int c2 = 0; c2 < lkmax; c2++)                                                      \
+            tl[IX(r, c2, lkmaxp)] = wgeff * (HB)[IX(a * lkmax + r, b * lkmax + c2, mdim)];        \
+      }
+    PUT_BLOCK(ip, t00)
+    for (int i = 0; i < ndim; i++)
+      for (int j = 0; j < ndim; j++) help[IX(i, j, mdim)] = t00[IX(i, j, mdim)];
+    for (int q = ip + 1; q < nprc; q++) {     /* down: tau(q,ip) = cc(q) tau(q-1,ip) */
+      int jdim = lkmax * ninprc[q + 1], jdim0 = lkmax * ninprc[q];
+      orc_doubmt2(cc + sz * q, help, help1, jdim, jdim0, ndim, mdim);
+      for (int i = 0; i < jdim; i++)
+        for (int j = 0; j < ndim; j++) help[IX(i, j, mdim)] = help1[IX(i, j, mdim)];
+      PUT_BLOCK(q, help)
+    }
+    for (int i = 0; i < ndim; i++)
+      for (int j = 0; j < ndim; j++) help[IX(i, j, mdim)] = t00[IX(i, j, mdim)];
+    for (int q = ip - 1; q >= 0; q--) {       /* up: tau(q,ip) = dd(q) tau(q+1,ip) */
+      int jdim = lkmax * ninprc[q + 1], jdim1 = lkmax * ninprc[q + 2];
+      orc_doubmt2(dd + sz * q, help, help1, jdim, jdim1, ndim, mdim);
+      for (int i = 0; i < jdim; i++)
+        for (int j = 0; j < ndim; j++) help[IX(i, j, mdim)] = help1[IX(i, j, mdim)];
+      PUT_BLOCK(q, help)
+    }
+#undef PUT_BLOCK
+  }
+  free(xx); free(yy); free(tau00); free(cc); free(dd); free(m00); free(m01); free(m10);
+  free(help); free(help1); free(nnprc);
+}
+
+/* ===================================================================== *
  * rsp-scf/fullcpa.f:2-155  ATA start, Ginatempo-Staunton CPA update      *
  * ===================================================================== */
 void orc_tata(double conc, int n, int ld, zc *mc, const zc *ma, const zc *mb) {
@@ -846,6 +978,129 @@ int orc_cpacoord(const orc_problem *p, const double *conc, const zc *tminvl,
   free(ttmpl); free(ttmpr); free(ttmp); free(ieqg); free(ieqgl); free(ieqgr);
   free(igordl); free(igordr); free(gcache); free(ysave); free(xsave); free(taupart);
   free(stat_thr); free(maxit_thr); free(totit_thr);
+  return status;
+}
+
+/* ===================================================================== *
+ * skkr_dbogo_bsf/rsp-scf/cpacoord_ksave.f:638-660, 760-840  off-diagonal *
+ * tau of the interface for cluster embedding: one k loop with the given   *
+ * t^-1 (no CPA update), tau2dgod per class, and for each pair (R = n1 a1 *
+ * + n2 a2, layers li, lj)                                                 *
+ *   tau_ij += w_k/ngeff e^{+i k.g(R+b)} [L_g tau^(g)(k) R_g]_{li,lj}      *
+ *   tau_ji += w_k/ngeff e^{-i k.g(R+b)} [L_g tau^(g)(k) R_g]_{lj,li}      *
+ * with b = c_li - c_lj and g(v) = a0mat(g) v.  This is the reference's    *
+ * e^{-i k.dcpar}, dcpar = -g(R) - g(b) + b, written for structure         *
+ * constants whose Bloch phases carry the full in-plane site vectors (the *
+ * real-space table form: tau_ab(k) here = e^{i k.(c_b - c_a)} tau_ab(k)  *
+ * of the lattice-vector phase convention).  tauc gets the layer-diagonal *
+ * k sum as orc_cpacoord forms it.  pairs[4 q] = (n1, n2, li, lj), layers  *
+ * 0-based; a0mat[4 g] = (a11, a12, a21, a22); cvec[2 l] in-plane          *
+ * positions of the interface layers.                                      *
+ * ===================================================================== */
+int orc_tauij(const orc_problem *p, const zc *tminvl, const zc *tminvr, const zc *tminv, int npair,
+              const int *pairs, const double *a1, const double *a2, const double *cvec,
+              const double *a0mat, zc *tau_ij, zc *tau_ji, zc *tauc, int ld, int nthreads) {
+  const int nprc = p->nprc, lkmax = p->lkmax, ngeff = p->ngeff, nk = p->nk;
+  const int nl = p->ninprc[0], nr = p->ninprc[nprc + 1], nintfc = p->nintfc;
+  int mdim = 0;
+  for (int i = 0; i <= nprc + 1; i++)
+    if (p->ninprc[i] * lkmax > mdim) mdim = p->ninprc[i] * lkmax;
+  const size_t sz = (size_t)ld * ld, msz = (size_t)mdim * mdim;
+  const size_t bsz = (size_t)p->map->lmmax * p->map->lmmax;
+  const size_t nfull = (size_t)nintfc * nintfc;
+  if (nthreads < 1) nthreads = 1;
+  cg_table_init();
+  zc *ttmpl = calloc(sz * nl * ngeff, sizeof(zc)), *ttmpr = calloc(sz * nr * ngeff, sizeof(zc));
+  zc *ttmp = calloc(sz * nintfc * ngeff, sizeof(zc));
+  int *ieqg = malloc(sizeof(int) * ngeff), *ieqgl = malloc(sizeof(int) * ngeff),
+      *ieqgr = malloc(sizeof(int) * ngeff), *igordl = malloc(sizeof(int) * ngeff),
+      *igordr = malloc(sizeof(int) * ngeff);
+  orc_sorttmat(lkmax, ld, nintfc, nl, nr, ngeff, p->rg, p->lg, tminvl, tminvr, tminv, ttmpl, ttmpr,
+               ttmp, ieqgl, ieqgr, ieqg, igordl, igordr);
+  const int nbk = p->irel == 2 ? 2 * p->nblk : p->nblk;
+  zc *part_ij = calloc(sz * npair * (size_t)nthreads, sizeof(zc));
+  zc *part_ji = calloc(sz * npair * (size_t)nthreads, sizeof(zc));
+  zc *part_c = calloc(sz * nintfc * (size_t)nthreads, sizeof(zc));
+  int *stat_thr = calloc(nthreads, sizeof(int));
+#pragma omp parallel num_threads(nthreads)
+  {
+    int tid = 0;
+#ifdef _OPENMP
+    tid = omp_get_thread_num();
+#endif
+    zc *blocks = calloc(bsz * nbk, sizeof(zc));
+    zc *xx = calloc(msz * ngeff, sizeof(zc)), *yy = calloc(msz * ngeff, sizeof(zc));
+    zc *tau1 = calloc(sz * nfull * ngeff, sizeof(zc)), *t2 = calloc(sz, sizeof(zc));
+    zc *pij = part_ij + sz * npair * tid, *pji = part_ji + sz * npair * tid, *pc = part_c + sz * nintfc * tid;
+    for (int ik = tid; ik < nk; ik += nthreads) {
+      const double kx = p->xk[2 * ik], ky = p->xk[2 * ik + 1];
+      orc_gk_from_rtable(p->nblk, p->rstart, p->rvec, p->gR, p->map->lmmax, kx, ky, blocks);
+      if (p->irel == 2)
+        orc_gk_from_rtable(p->nblk, p->rstart, p->rvec, p->gR + bsz * p->rstart[p->nblk], p->map->lmmax,
+                           kx, ky, blocks + bsz * p->nblk);
+      for (int ig = 0; ig < ngeff; ig++) {
+        int ige = ieqg[ig] - 1, igel = ieqgl[ig] - 1, iger = ieqgr[ig] - 1;
+        int it = 0, st;
+        if (igel == ig) {
+          st = orc_dugo('L', p->ninprc, nprc, p->map, blocks, 0, 1, ttmpl + sz * (size_t)igel * nl, ld,
+                        yy + msz * igel, mdim, lkmax, p->irel, p->fac, p->itermaxl, p->errmax, &it);
+          if (st && !stat_thr[tid]) stat_thr[tid] = st;
+        }
+        if (iger == ig) {
+          st = orc_dugo('R', p->ninprc, nprc, p->map, blocks, nprc + 1, 1, ttmpr + sz * (size_t)iger * nr,
+                        ld, xx + msz * iger, mdim, lkmax, p->irel, p->fac, p->itermaxr, p->errmax, &it);
+          if (st && !stat_thr[tid]) stat_thr[tid] = st;
+        }
+        if (ige == ig)
+          orc_tau2dgod(p->irel, p->wk[ik] / ngeff, p->bulkgeo, p->ninprc, nprc, p->map, blocks,
+                       ttmp + sz * (size_t)ig * nintfc, ld, lkmax, xx + msz * iger, yy + msz * igel, mdim,
+                       tau1 + sz * nfull * ig, nintfc, p->fac);
+        const zc *tg = tau1 + sz * nfull * ige;
+        for (int li = 0; li < nintfc; li++) {
+          memcpy(t2, tg + sz * ((size_t)li * nintfc + li), sz * sizeof(zc));
+          orc_tripmt(p->lg + sz * ig, t2, p->rg + sz * ig, lkmax, lkmax, ld);
+          zc *t = pc + sz * li;
+          for (int i = 0; i < lkmax; i++)
+            for (int j = 0; j < lkmax; j++) t[IX(i, j, ld)] += t2[IX(i, j, ld)];
+        }
+        const double *am = a0mat + 4 * ig;
+        for (int q = 0; q < npair; q++) {
+          const int n1 = pairs[4 * q], n2 = pairs[4 * q + 1], li = pairs[4 * q + 2], lj = pairs[4 * q + 3];
+          const double vx = n1 * a1[0] + n2 * a2[0] + cvec[2 * li] - cvec[2 * lj];
+          const double vy = n1 * a1[1] + n2 * a2[1] + cvec[2 * li + 1] - cvec[2 * lj + 1];
+          const double gx = am[0] * vx + am[1] * vy, gy = am[2] * vx + am[3] * vy;
+          const double ph = kx * gx + ky * gy;
+          const zc f = cos(ph) + I * sin(ph);
+          memcpy(t2, tg + sz * ((size_t)li * nintfc + lj), sz * sizeof(zc));
+          orc_tripmt(p->lg + sz * ig, t2, p->rg + sz * ig, lkmax, lkmax, ld);
+          zc *t = pij + sz * q;
+          for (int i = 0; i < lkmax; i++)
+            for (int j = 0; j < lkmax; j++) t[IX(i, j, ld)] += f * t2[IX(i, j, ld)];
+          memcpy(t2, tg + sz * ((size_t)lj * nintfc + li), sz * sizeof(zc));
+          orc_tripmt(p->lg + sz * ig, t2, p->rg + sz * ig, lkmax, lkmax, ld);
+          t = pji + sz * q;
+          for (int i = 0; i < lkmax; i++)
+            for (int j = 0; j < lkmax; j++) t[IX(i, j, ld)] += conj(f) * t2[IX(i, j, ld)];
+        }
+      }
+    }
+    free(blocks); free(xx); free(yy); free(tau1); free(t2);
+  }
+  czero(tau_ij, sz * npair);
+  czero(tau_ji, sz * npair);
+  czero(tauc, sz * nintfc);
+  for (int t = 0; t < nthreads; t++) {
+    for (size_t q = 0; q < sz * npair; q++) {
+      tau_ij[q] += part_ij[sz * npair * t + q];
+      tau_ji[q] += part_ji[sz * npair * t + q];
+    }
+    for (size_t q = 0; q < sz * nintfc; q++) tauc[q] += part_c[sz * nintfc * t + q];
+  }
+  int status = 0;
+  for (int t = 0; t < nthreads; t++)
+    if (stat_thr[t] && !status) status = stat_thr[t];
+  free(ttmpl); free(ttmpr); free(ttmp); free(ieqg); free(ieqgl); free(ieqgr); free(igordl); free(igordr);
+  free(part_ij); free(part_ji); free(part_c); free(stat_thr);
   return status;
 }
 

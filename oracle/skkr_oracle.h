@@ -164,6 +164,19 @@ int orc_cpacoord(const orc_problem *p, const double *conc, const zc *tminvl,
                  const zc *tminvb, zc *tauc, zc *taua, zc *taub, int ld,
                  orc_result *res, int nthreads);
 
+/* full Godfrin tau of one k (skkr_dbogo_bsf/clu/tau2d_god.f): tauij[(a*nintfc+b)]
+ * = wgeff tau_{a,b}, every interface layer pair; args as orc_tau2d */
+void orc_tau2dgod(int irel, double wgeff, int bulkgeo, const int *ninprc,
+                  int nprc, const orc_g2dmap *map, const zc *blocks,
+                  const zc *tminv, int lkmaxp, int lkmax, const zc *x,
+                  const zc *y, int mdimp, zc *tauij, int nintfc, zc fac);
+/* off-diagonal k sums for pairs (n1, n2, li, lj) with phases and group
+ * rotations (skkr_dbogo_bsf/rsp-scf/cpacoord_ksave.f:760-840), one k loop
+ * with fixed t^-1; see skkr_oracle.c */
+int orc_tauij(const orc_problem *p, const zc *tminvl, const zc *tminvr, const zc *tminv, int npair,
+              const int *pairs, const double *a1, const double *a2, const double *cvec,
+              const double *a0mat, zc *tau_ij, zc *tau_ji, zc *tauc, int ld, int nthreads);
+
 /* ---- generators: main/zmesh.f, main/legzero.f, main/speck2.f, main/kmesh2d.f,
  *      main/alphamat.f, main/csbf.f ----------------------------------- */
 void orc_legzero(int ng, double *xx, double *wx);
