@@ -128,6 +128,27 @@ int skkr_gpu_destroy(skkr_ctx *ctx);
 int skkr_gpu_set_mixed_policy(skkr_ctx *ctx, double dec_fp64_im, double near_im, int slices_near,
                               double dominant_frac);
 
+/* Off-diagonal tau of the interface for cluster embedding
+ * (skkr_dbogo_bsf/clu/tau2d_god.f with the pair sums of
+ * skkr_dbogo_bsf/rsp-scf/cpacoord_ksave.f:760-840): one k loop of the staged
+ * energy with its current t^-1 (no CPA update).  For pair q,
+ * pairs[4q..4q+3] = (n1, n2, li, lj) with 0-based interface layers, the
+ * results are the inter-site scattering path operators
+ *   tau_ij[q] = tau(layer li in cell 0, layer lj in cell n1 a1 + n2 a2)
+ *             = sum_k w_k/ngeff sum_g e^{+i k.g(v)} [L_g tau^(g)(k) R_g]_{li,lj}
+ *   tau_ji[q] = tau(layer lj in cell n1 a1 + n2 a2, layer li in cell 0)
+ * with v = n1 a1 + n2 a2 + c_li - c_lj, a1/a2 the in-plane lattice vectors,
+ * cvec[2 l] the in-plane position of interface layer l and a0mat[4 g] the
+ * row-major 2x2 in-plane matrix of group element g applied to v: the
+ * transpose (inverse) of the in-plane rotation whose D matrices are
+ * L_g = lg[g], R_g = rg[g] (the IBZ point k stands for a0mat[g]^T k of the
+ * full zone).  tau_ij / tau_ji are [npair][ld][ld] column-major; npair *
+ * ngeff <= 65535; non-relativistic and relativistic modes (BdG:
+ * SKKR_ERR_UNSUPPORTED).  The status carries the decimation counters. */
+int skkr_gpu_tauij(skkr_ctx *ctx, int npair, const int *pairs, const double *a1, const double *a2,
+                   const double *cvec, const double *a0mat, double *tau_ij, double *tau_ji, int ld,
+                   skkr_status *status);
+
 /* Host reduction for an energy whose k points are split over ranks (the
  * modulo(ik-1,nprocs) split of cpacoord_ksave.f:189 with the mpi_allreduce of
  * the k-summed tau at :406).  When set, every CPA iteration calls

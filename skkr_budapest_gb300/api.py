@@ -95,6 +95,29 @@ class Context:
                                     p(a["tb"]), self.lk)
         N._check(rc, "skkr_gpu_stage")
 
+    def tauij(self, ep, pairs, a1, a2, cvec, a0mat, tminv=None, check=True):
+        """Off-diagonal tau of the interface for cluster embedding
+        (skkr_gpu_tauij): stages ep (with tminv as the coherent t^-1) and
+        runs one k loop; pairs are (n1, n2, li, lj), 0-based layers.  Returns
+        tau_ij, tau_ji as (npair, lk, lk) arrays and the status."""
+        self.stage(ep, tminv)
+        pa = np.ascontiguousarray(np.asarray(pairs, np.int32).reshape(-1, 4))
+        npair, lk = len(pa), self.lk
+        va1 = np.ascontiguousarray(a1, np.float64)
+        va2 = np.ascontiguousarray(a2, np.float64)
+        cv = np.ascontiguousarray(np.asarray(cvec, np.float64).reshape(-1, 2))
+        am = np.ascontiguousarray(np.asarray(a0mat, np.float64).reshape(-1, 4))
+        oij = np.zeros((npair, lk, lk), np.complex128)
+        oji = np.zeros_like(oij)
+        st = N.Status()
+        p = N._p
+        rc = N.lib().skkr_gpu_tauij(self.h, npair, p(pa), p(va1), p(va2), p(cv), p(am), p(oij), p(oji), lk,
+                                    C.cast(C.pointer(st), C.c_void_p))
+        if check:
+            N._check(rc, "skkr_gpu_tauij")
+        return dict(status=rc, tau_ij=N.uncm(oij), tau_ji=N.uncm(oji), gpu_launches=st.gpu_launches,
+                    max_dec_iters=st.max_dec_iters)
+
     def run(self, check=True):
         st = N.Status()
         rc = N.lib().skkr_gpu_run(self.h, C.cast(C.pointer(st), C.c_void_p))

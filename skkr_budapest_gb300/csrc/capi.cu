@@ -941,6 +941,108 @@ static int run_tau2d(skkr_ctx *c, int k0, int nkc, const std::vector<int> &icls)
 }
 
 // ---------------------------------------------------------------------------
+// full Godfrin tau (skkr_dbogo_bsf/clu/tau2d_god.f) for k in [k0, k0+nkc),
+// items (k, class): the sweeps of run_tau2d, then every PL block carried
+// from the diagonal, tau(q,p) = cc(q) tau(q-1,p) below (cc(q) = -Xr(q-1)) and
+// tau(q,p) = dd(q) tau(q+1,p) above (dd(q) = -Yr(q+1)); the signs are applied
+// at the extraction into tauf[item][li][lj][lk^2] (weight wk/ngeff).
+static int run_tau2d_full(skkr_ctx *c, int k0, int nkc, const std::vector<int> &icls, zd *tauf) {
+  const int n = c->n, lk = c->lk, lk2 = lk * lk, pl = c->pl, nprc = c->nprc, ni = c->nintfc;
+  const int nc = (int)icls.size();
+  const long long MB = (long long)n * n;
+  const int nbuf = 5 * nprc + 1;
+  CKR(c->tauw.ensure((size_t)nkc * nc * nbuf * MB * sizeof(zd)));
+  cudaStream_t st = c->st;
+  zd *Wb = c->tauw.as<zd>();
+  auto buf = [&](int b) { return mref(Wb + (long long)b * MB, (long long)nc * nbuf * MB, nbuf * MB, n); };
+  auto T00 = [&](int p) { return buf(p); };
+  auto YY = [&](int p) { return buf(nprc + p); };
+  auto Yr = [&](int p) { return buf(2 * nprc + p); };
+  auto XX = [&](int p) { return buf(3 * nprc + p); };
+  auto Xr = [&](int p) { return buf(4 * nprc + p); };
+  MatRef Wm = buf(5 * nprc);
+  zd *poolk = c->pool.as<zd>();
+  const long long psk = (long long)c->nmat * MB;
+  int m00[SKKR_MAPN], m10[SKKR_MAPN], m01[SKKR_MAPN], ysl[SKKR_MAPN], xsl[SKKR_MAPN], tmap[SKKR_MAPN];
+  const int nlay = 2 * pl + ni;
+  for (int s = 0; s < nc; s++) {
+    int g = icls[s];
+    m00[s] = c->idx00;
+    m10[s] = c->idx10;
+    m01[s] = c->idx01;
+    ysl[s] = c->igordl[c->ieqgl[g] - 1] - 1;
+    xsl[s] = c->nls + c->igordr[c->ieqgr[g] - 1] - 1;
+    tmap[s] = g * nlay + 2 * pl;
+  }
+  MatRef M00 = mref_map(poolk, psk, MB, n, m00, nc);
+  MatRef M10 = mref_map(poolk, psk, MB, n, m10, nc);
+  MatRef M01 = mref_map(poolk, psk, MB, n, m01, nc);
+  zd *sbase = c->sspo.as<zd>() + (long long)k0 * c->nsl * MB;
+  MatRef Ys = mref_map(sbase, (long long)c->nsl * MB, MB, n, ysl, nc);
+  MatRef Xs = mref_map(sbase, (long long)c->nsl * MB, MB, n, xsl, nc);
+  const bool mx = use_mixed(c, false);
+  for (int p = 0; p < nprc; p++) {  // forward (tau2d_god.f:53-91)
+    int tm2[SKKR_MAPN];
+    for (int s = 0; s < nc; s++) tm2[s] = tmap[s] + p * pl;
+    MatRef Tt = mref_map(c->trot.as<zd>(), 0, lk2, lk, tm2, nc);
+    launch_add_tblocks(T00(p), M00, Tt, lk, pl, n, nkc, nc, nullptr, ehsplit(c), st);
+    if (p == 0)
+      launch_zaxpby(YY(0), Ys, nullptr, 0, nullptr, 0, n, nkc, nc, nullptr, st);
+    else
+      CKR(eng_gemm(c, mx, 0, M10, Yr(p), YY(p), YY(p), YY(p), n, nkc, nc, nullptr));
+    if (p < nprc - 1) {
+      MatRef yy = YY(p);
+      launch_zaxpby(Wm, T00(p), &yy, -1.0, nullptr, 0, n, nkc, nc, nullptr, st);
+      CKR(eng_inv(c, mx, Wm, Wm, true, n, nkc, nc, nullptr));
+      CKR(eng_gemm(c, mx, 0, Wm, M01, Yr(p + 1), Yr(p + 1), Yr(p + 1), n, nkc, nc, nullptr));
+    }
+  }
+  for (int p = nprc - 1; p >= 0; p--) {  // backward (:93-114)
+    if (p == nprc - 1)
+      launch_zaxpby(XX(p), Xs, nullptr, 0, nullptr, 0, n, nkc, nc, nullptr, st);
+    else
+      CKR(eng_gemm(c, mx, 0, M01, Xr(p), XX(p), XX(p), XX(p), n, nkc, nc, nullptr));
+    if (p > 0) {
+      MatRef xx = XX(p);
+      launch_zaxpby(Wm, T00(p), &xx, -1.0, nullptr, 0, n, nkc, nc, nullptr, st);
+      CKR(eng_inv(c, mx, Wm, Wm, true, n, nkc, nc, nullptr));
+      CKR(eng_gemm(c, mx, 0, Wm, M10, Xr(p - 1), Xr(p - 1), Xr(p - 1), n, nkc, nc, nullptr));
+    }
+  }
+  // PL-diagonal tau(p,p) in place of T00(p) (:115-119)
+  for (int p = 0; p < nprc; p++) {
+    MatRef t = T00(p), xx = XX(p), yy = YY(p);
+    launch_zaxpby(t, t, &xx, -1.0, &yy, -1.0, n, nkc, nc, nullptr, st);
+    CKR(eng_inv(c, mx, t, t, true, n, nkc, nc, nullptr));
+  }
+  // every PL block, carried from the diagonal (:151-205); YY(0) and XX(0)
+  // serve as the two work matrices
+  const double ws = 1.0 / c->ngeff;
+  const long long osk = (long long)nc * ni * ni * lk2, osc = (long long)ni * ni * lk2;
+  const double *wk = c->wk.as<double>() + k0;
+  for (int p = 0; p < nprc; p++) {
+    launch_extract_pairs(T00(p), lk, pl, p * pl, p * pl, ni, wk, ws, tauf, osk, osc, nkc, nc, ehsplit(c), st);
+    MatRef cur = T00(p);
+    for (int q = p + 1; q < nprc; q++) {  // below: tau(q,p) = -Xr(q-1) tau(q-1,p)
+      MatRef nxt = ((q - p) & 1) ? YY(0) : XX(0);
+      CKR(eng_gemm(c, mx, 0, Xr(q - 1), cur, nxt, nxt, nxt, n, nkc, nc, nullptr));
+      launch_extract_pairs(nxt, lk, pl, q * pl, p * pl, ni, wk, ((q - p) & 1) ? -ws : ws, tauf, osk, osc, nkc, nc,
+                           ehsplit(c), st);
+      cur = nxt;
+    }
+    cur = T00(p);
+    for (int q = p - 1; q >= 0; q--) {  // above: tau(q,p) = -Yr(q+1) tau(q+1,p)
+      MatRef nxt = ((p - q) & 1) ? YY(0) : XX(0);
+      CKR(eng_gemm(c, mx, 0, Yr(q + 1), cur, nxt, nxt, nxt, n, nkc, nc, nullptr));
+      launch_extract_pairs(nxt, lk, pl, q * pl, p * pl, ni, wk, ((p - q) & 1) ? -ws : ws, tauf, osk, osc, nkc, nc,
+                           ehsplit(c), st);
+      cur = nxt;
+    }
+  }
+  return SKKR_OK;
+}
+
+// ---------------------------------------------------------------------------
 // CPA update (rsp-scf/fullcpa.f cpacor/cpasol) on the device
 __global__ void k_cpa_norms(const zd *mc, const zd *tab, int lk2, double *out) {
   // out[l*4 + {0 ||ma-mc||^2, 1 ||ma||^2, 2 ||mb-mc||^2, 3 ||mb||^2}]
@@ -1170,6 +1272,147 @@ static int redo_dominant_k(skkr_ctx *c, int itcpa, const std::vector<int> &lcls,
     c->k_fp64 += m;
   }
   return SKKR_OK;
+}
+
+// Off-diagonal tau of the interface for cluster embedding
+// (skkr_dbogo_bsf/rsp-scf/cpacoord_ksave.f:638-660, 760-840): one k loop of
+// the staged energy with its current t^-1 -- G(k), decimation, the full
+// Godfrin tau per class, the phased pair sums per group element -- then the
+// group rotations L_g (.) R_g summed over g.
+extern "C" int skkr_gpu_tauij(skkr_ctx *c, int npair, const int *pairs, const double *a1, const double *a2,
+                              const double *cvec, const double *a0mat, double *tau_ij, double *tau_ji, int ld,
+                              skkr_status *status) {
+  if (!c || !c->staged || npair < 1 || (long long)npair * c->ngeff > 65535 || !pairs || !a1 || !a2 || !cvec || !a0mat || !tau_ij ||
+      !tau_ji || ld < c->lk)
+    return SKKR_ERR_ARG;
+  // BdG energies run through skkr_gpu_cpacoord_bdg, which stages the hole factors itself
+  if (c->sz.mode == SKKR_BDG) return SKKR_ERR_UNSUPPORTED;
+  const int n = c->n, lk = c->lk, lk2 = lk * lk, ni = c->nintfc, nk = c->nk, ng = c->ngeff;
+  for (int q = 0; q < npair; q++)
+    if (pairs[4 * q + 2] < 0 || pairs[4 * q + 2] >= ni || pairs[4 * q + 3] < 0 || pairs[4 * q + 3] >= ni)
+      return SKKR_ERR_ARG;
+  const long long l0 = g_skkr_launches;
+  const long long MB = (long long)n * n;
+  const size_t bs = (size_t)c->lmmax * c->lmmax;
+  cudaStream_t st = c->st;
+  c->max_dec = 0;
+  c->tot_dec = 0;
+  c->err_code = 0;
+  c->first_bad_k = -1;
+  if (c->sz.precision == SKKR_MIXED && !c->mw) {
+    c->mw = mixed_create();
+    if (!c->mw) return SKKR_ERR_NOMEM;
+  }
+  if (c->mw) {
+    CKR(mixed_resid_reset(c->mw, st));
+    mixed_set_precise(c->mw, c->slices_near > 0 && std::fabs(c->ce.y) < c->near_im);
+  }
+  plan_pack(c);
+  CKR(c->jobs.ensure(c->jobs_h.size() * sizeof(PackJob)));
+  CK(cudaMemcpyAsync(c->jobs.p, c->jobs_h.data(), c->jobs_h.size() * sizeof(PackJob), cudaMemcpyHostToDevice,
+                     st));
+  CKR(c->G.ensure((size_t)nk * c->nbk * bs * sizeof(zd)));
+  CKR(sorttmat_dev(c));
+  CKR(check_slot_quirk(c));
+  std::vector<int> lcls, rcls, icls;
+  lead_classes(c, lcls, rcls);
+  for (int g = 0; g < ng; g++)
+    if (c->ieqg[g] == g + 1) icls.push_back(g);
+  const int nc = (int)icls.size();
+  {
+    int nLs = 0, nRs = 0;
+    for (int g : lcls) nLs = std::max(nLs, c->igordl[g]);
+    for (int g : rcls) nRs = std::max(nRs, c->igordr[g]);
+    c->nls = nLs;
+    c->nsl = nLs + nRs;
+  }
+  // chunk: the run's per-k work plus the full tau of every class
+  int kc;
+  {
+    const int ncmax = 2 * ng;
+    double per_k = (double)MB * sizeof(zd) * (c->nmat + 9.0 * ncmax + (5.0 * c->nprc + 1) * ng) +
+                   (double)nc * ni * ni * lk2 * sizeof(zd);
+    if (c->sz.precision == SKKR_MIXED) {
+      const double Mp = 128.0 * ((n + 127) / 128), Np = 96.0 * ((2 * n + 95) / 96), Kp = 32.0 * ((2 * n + 31) / 32);
+      per_k += (double)ncmax * MIXED_SLOTS * c->slices_res * (Mp + Np) * Kp * 2.0;
+    }
+    kc = c->sz.nk_chunk > 0 ? c->sz.nk_chunk : (int)std::max(1.0, std::floor(32.0e9 / per_k));
+    kc = std::max(1, std::min(std::min(kc, 65535 / (2 * ng)), nk));
+  }
+  CKR(c->pool.ensure((size_t)kc * c->nmat * MB * sizeof(zd)));
+  CKR(c->sspo.ensure((size_t)nk * c->nsl * MB * sizeof(zd)));
+  launch_gk_ft(c->gR.as<zd>(), c->rvec.as<double>(), c->rstart.as<int>(), c->nbk, c->lmmax, c->xk.as<double>(), nk,
+               c->G.as<zd>(), st);
+  // pair data: class of each g, R + c_li - c_lj, a0mat
+  std::vector<int> cls(ng);
+  for (int g = 0; g < ng; g++)
+    cls[g] = (int)(std::find(icls.begin(), icls.end(), c->ieqg[g] - 1) - icls.begin());
+  std::vector<double> vecs(2 * (size_t)npair);
+  for (int q = 0; q < npair; q++) {
+    const int n1 = pairs[4 * q], n2 = pairs[4 * q + 1], li = pairs[4 * q + 2], lj = pairs[4 * q + 3];
+    vecs[2 * q] = n1 * a1[0] + n2 * a2[0] + cvec[2 * li] - cvec[2 * lj];
+    vecs[2 * q + 1] = n1 * a1[1] + n2 * a2[1] + cvec[2 * li + 1] - cvec[2 * lj + 1];
+  }
+  DBuf tauf, acc, misc, rot;
+  struct Release {
+    DBuf *b[4];
+    ~Release() {
+      for (DBuf *x : b) x->release();
+    }
+  } release_on_return{{&tauf, &acc, &misc, &rot}};
+  const size_t accn = (size_t)npair * ng * lk2;
+  CKR(tauf.ensure((size_t)kc * nc * ni * ni * lk2 * sizeof(zd)));
+  CKR(acc.ensure(2 * accn * sizeof(zd)));
+  CKR(rot.ensure(4 * accn * sizeof(zd)));
+  const size_t moff_vec = ((size_t)ng + 4 * npair) * sizeof(int);
+  const size_t moff_a0 = moff_vec + 2 * (size_t)npair * sizeof(double);
+  CKR(misc.ensure(moff_a0 + 4 * (size_t)ng * sizeof(double)));
+  char *mb = misc.as<char>();
+  CK(cudaMemcpyAsync(mb, cls.data(), ng * sizeof(int), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(mb + ng * sizeof(int), pairs, 4 * (size_t)npair * sizeof(int), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(mb + moff_vec, vecs.data(), vecs.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(mb + moff_a0, a0mat, 4 * (size_t)ng * sizeof(double), cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(acc.p, 0, 2 * accn * sizeof(zd), st));
+  CK(cudaStreamSynchronize(st));  // the host vectors above are temporaries
+  zd *acc_ij = acc.as<zd>(), *acc_ji = acc_ij + accn;
+  for (int k0 = 0; k0 < nk; k0 += kc) {
+    const int nkc = std::min(kc, nk - k0);
+    launch_pack(c->G.as<zd>() + (size_t)k0 * c->nbk * bs, c->nblk, c->nbk, c->blkmap_d.as<int>(), c->mi, c->jmax,
+                c->jobs.as<PackJob>(), c->nmat, lk, c->lmmax, c->sz.mode, c->fac, c->fach, nkc, c->pool.as<zd>(),
+                c->nmat, n, ehsplit(c), st);
+    CKR(run_decimation(c, k0, nkc, lcls, rcls));
+    if (c->err_code) break;
+    CKR(run_tau2d_full(c, k0, nkc, icls, tauf.as<zd>()));
+    launch_pair_sum(tauf.as<zd>(), nkc, nc, ni, lk, (const int *)mb, ng, npair, (const int *)(mb + ng * sizeof(int)),
+                    (const double *)(mb + moff_vec), (const double *)(mb + moff_a0), c->xk.as<double>() + 2 * k0,
+                    acc_ij, acc_ji, st);
+  }
+  if (!c->err_code) {
+    // tau_ij[q] = sum_g L_g acc[q][g] R_g, likewise tau_ji
+    zd *T1 = rot.as<zd>(), *T2 = T1 + 2 * accn;
+    MatRef Lm = mref(c->lg.as<zd>(), 0, lk2, lk), Rm = mref(c->rg.as<zd>(), 0, lk2, lk);
+    for (int side = 0; side < 2; side++) {
+      MatRef Am = mref((side ? acc_ji : acc_ij), (long long)ng * lk2, lk2, lk);
+      MatRef T1m = mref(T1 + side * accn, (long long)ng * lk2, lk2, lk);
+      MatRef T2m = mref(T2 + side * accn, (long long)ng * lk2, lk2, lk);
+      launch_zgemm(0, Lm, Am, T1m, T1m, T1m, lk, lk, lk, npair, ng, nullptr, st);
+      launch_zgemm(0, T1m, Rm, T2m, T2m, T2m, lk, lk, lk, npair, ng, nullptr, st);
+      launch_gsum(T2 + side * accn, ng, lk, npair, T1 + side * accn, st);
+    }
+    CKR(get_mats(tau_ij, T1, npair, lk, ld, st));
+    CKR(get_mats(tau_ji, T1 + accn, npair, lk, ld, st));
+  }
+  CK(cudaStreamSynchronize(st));
+  CK(cudaGetLastError());
+  if (status) {
+    *status = skkr_status{};
+    status->code = c->err_code;
+    status->ik = c->first_bad_k;
+    status->max_dec_iters = c->max_dec;
+    status->dec_iters_total = c->tot_dec;
+    status->gpu_launches = g_skkr_launches - l0;
+  }
+  return c->err_code;
 }
 
 extern "C" int skkr_gpu_set_mixed_policy(skkr_ctx *c, double dec_fp64_im, double near_im, int slices_near,

@@ -52,6 +52,13 @@ void launch_axpy_flat(zd *S, const zd *x, long long E, double sign, cudaStream_t
 void launch_ksum(const zd *tk, int nk, long long E, zd *S, int accumulate, cudaStream_t st);
 // sum over g of T[layer][g] -> out[layer]
 void launch_gsum(const zd *T, int ng, int lk, int nl, zd *out, cudaStream_t st);
+// layer-pair blocks of one PL block of the full tau, and the phased pair k sums
+void launch_extract_pairs(const MatRef &W, int lk, int nl, int rowlay0, int collay0, int nintfc,
+                          const double *wk, double wscale, zd *out, long long out_sk, long long out_sc,
+                          int nk, int nc, int ehsplit, cudaStream_t st);
+void launch_pair_sum(const zd *tauf, int nkc, int nc, int nintfc, int lk, const int *cls_of_g, int ngeff,
+                     int npair, const int *pairs, const double *vecs, const double *a0mat, const double *xk,
+                     zd *acc_ij, zd *acc_ji, cudaStream_t st);
 // CPA helpers
 void launch_layer_dos(int rel, int nd, int nl, int nlay, const zd *tau, int ld, const zd *F,
                       const zd *G, double fac, zd *zmom, zd *zdos_l, cudaStream_t st);

@@ -545,6 +545,89 @@ void launch_extract_tau(const MatRef &W, int lk, int nl, int layer0, const doubl
   SKKR_LAUNCHED();
 }
 
+// One principal-layer block (rows: PL of `rowlay0`, columns: PL of
+// `collay0`) of the full Godfrin tau into its layer-pair blocks
+// (skkr_dbogo_bsf/clu/tau2d_god.f:152-205): out[item][rowlay0 + a][collay0 + b]
+// = wk wscale W(layer a rows, layer b columns), nl layers per PL, nintfc
+// interface layers.
+__global__ void k_extract_pairs(MatRef W, int lk, int nl, int rowlay0, int collay0, int nintfc,
+                                const double *wk, double wscale, zd *out, long long out_sk,
+                                long long out_sc, int nc, int ehsplit) {
+  const int item = blockIdx.y;
+  const int kk = item / nc, cc = item % nc;
+  const zd *w = mat_ptr(W, kk, cc);
+  const double wg = wk[kk] * wscale;
+  const int lk2 = lk * lk, tot = nl * nl * lk2;
+  zd *o = out + (long long)kk * out_sk + (long long)cc * out_sc;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += gridDim.x * blockDim.x) {
+    const int ab = e / lk2, rem = e % lk2;
+    const int a = ab / nl, b = ab % nl;
+    const int r = rem % lk, c = rem / lk;
+    const zd v = w[pl_row(a, r, lk, nl, ehsplit) + (long long)pl_row(b, c, lk, nl, ehsplit) * W.ld];
+    o[((long long)(rowlay0 + a) * nintfc + (collay0 + b)) * lk2 + rem] = zscale(wg, v);
+  }
+}
+
+void launch_extract_pairs(const MatRef &W, int lk, int nl, int rowlay0, int collay0, int nintfc,
+                          const double *wk, double wscale, zd *out, long long out_sk, long long out_sc,
+                          int nk, int nc, int ehsplit, cudaStream_t st) {
+  if (nk <= 0 || nc <= 0) return;
+  int per = (nl * nl * lk * lk + 255) / 256;
+  dim3 grid(per < 16 ? per : 16, nk * nc);
+  k_extract_pairs<<<grid, 256, 0, st>>>(W, lk, nl, rowlay0, collay0, nintfc, wk, wscale, out, out_sk, out_sc,
+                                        nc, ehsplit);
+  SKKR_LAUNCHED();
+}
+
+// Phased k sums of the pair blocks (skkr_dbogo_bsf/rsp-scf/cpacoord_ksave.f:
+// 818-840) for the k points of one chunk, before the group rotation:
+//   acc_ij[q][g] += sum_k e^{+i k.g v_q} tau^(class g)_{li,lj}(k)
+//   acc_ji[q][g] += sum_k e^{-i k.g v_q} tau^(class g)_{lj,li}(k)
+// v_q = R_q + c_li - c_lj, g(v) = a0mat[g] v (row-major 2x2).  One thread
+// per matrix element of one (pair, g); the k loop runs in order.
+__global__ void k_pair_sum(const zd *__restrict__ tauf, int nkc, int nc, int nintfc, int lk2,
+                           const int *__restrict__ cls_of_g, int ngeff, const int *__restrict__ pairs,
+                           const double *__restrict__ vecs, const double *__restrict__ a0mat,
+                           const double *__restrict__ xk, zd *acc_ij, zd *acc_ji) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  const int q = blockIdx.y, g = blockIdx.z;
+  if (e >= lk2) return;
+  const int li = pairs[4 * q + 2], lj = pairs[4 * q + 3];
+  const double vx = vecs[2 * q], vy = vecs[2 * q + 1];
+  const double *am = a0mat + 4 * g;
+  const double gx = am[0] * vx + am[1] * vy, gy = am[2] * vx + am[3] * vy;
+  const int cl = cls_of_g[g];
+  const long long blk = (long long)nintfc * nintfc * lk2;
+  const zd *tij = tauf + (long long)cl * blk + ((long long)li * nintfc + lj) * lk2 + e;
+  const zd *tji = tauf + (long long)cl * blk + ((long long)lj * nintfc + li) * lk2 + e;
+  const long long sk = (long long)nc * blk;
+  double sr = 0, si = 0, tr = 0, ti = 0;
+  for (int k = 0; k < nkc; k++) {
+    double sn, cs;
+    sincos(xk[2 * k] * gx + xk[2 * k + 1] * gy, &sn, &cs);
+    const zd a = tij[k * sk], b = tji[k * sk];
+    sr += cs * a.x - sn * a.y;
+    si += cs * a.y + sn * a.x;
+    tr += cs * b.x + sn * b.y;
+    ti += cs * b.y - sn * b.x;
+  }
+  zd *oij = acc_ij + ((long long)q * ngeff + g) * lk2 + e;
+  zd *oji = acc_ji + ((long long)q * ngeff + g) * lk2 + e;
+  *oij = make_double2(oij->x + sr, oij->y + si);
+  *oji = make_double2(oji->x + tr, oji->y + ti);
+}
+
+void launch_pair_sum(const zd *tauf, int nkc, int nc, int nintfc, int lk, const int *cls_of_g, int ngeff,
+                     int npair, const int *pairs, const double *vecs, const double *a0mat, const double *xk,
+                     zd *acc_ij, zd *acc_ji, cudaStream_t st) {
+  if (nkc <= 0 || npair <= 0) return;
+  const int lk2 = lk * lk;
+  dim3 grid((lk2 + 127) / 128, npair, ngeff);
+  k_pair_sum<<<grid, 128, 0, st>>>(tauf, nkc, nc, nintfc, lk2, cls_of_g, ngeff, pairs, vecs, a0mat, xk, acc_ij,
+                                   acc_ji);
+  SKKR_LAUNCHED();
+}
+
 // k-sum: block (32 elements) x (32 k-slices); coalesced loads over elements,
 // then a shared-memory transpose and a warp-shuffle reduction over slices.
 // The summation tree is fixed, so the result is bitwise reproducible.

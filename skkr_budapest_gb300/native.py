@@ -82,6 +82,7 @@ def lib():
         L.skkr_gpu_run_slot.argtypes = [P, I, P]
         L.skkr_gpu_fetch_slot.argtypes = [P, I, P, P, P, P, I]
         L.skkr_gpu_kernel_stats.argtypes = [I, P]
+        L.skkr_gpu_tauij.argtypes = [P, I, P, P, P, P, P, P, P, I, P]
         _lib = L
     return _lib
 
