@@ -57,8 +57,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", action="store_true",
                     help="only the device loop of the timed steps (for ncu captures); prints a short line")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3"],
-                    help="c3: one energy of each of three systems per step through skkr_gpu_cpacoord_many")
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "tauij"],
+                    help="c3: one energy of each of three systems per step through skkr_gpu_cpacoord_many; "
+                         "tauij: the off-diagonal tau of the interface (skkr_gpu_tauij) per step")
     return ap.parse_args()
 
 
@@ -446,10 +447,65 @@ def run_c3(args):
                                  "timing": "host wall clock around whole calls (host buffers)"}}), flush=True)
 
 
+def run_tauij(args):
+    """Off-diagonal tau of the relativistic PL4 lmax=3 interface for cluster
+    embedding: per step one contour energy through skkr_gpu_tauij (G(k),
+    decimation, full Godfrin tau, phased pair sums over all 144 layer pairs
+    at R = 0 and the 4 nearest in-plane cells), split precision against FP64,
+    host buffers in and out."""
+    import torch
+    from skkr_budapest_gb300 import api, synth as S
+    from skkr_budapest_gb300 import workloads as W
+    spec = W.rel_bcc()
+    plan = [12, 16, 14, 19, 13]
+    eps = {ie: W.energy_problem(spec, ie) for ie in plan}
+    ep0 = eps[plan[0]]
+    n, a2d, l0 = ep0.nintfc, spec.stacking.a2d, int(ep0.ninprc[0])
+    cvec = np.array([[0.5 * ((l0 + l) % 2) * a2d] * 2 for l in range(n)])
+    pairs = [(0, 0, a, b) for a in range(n) for b in range(n)]
+    pairs += [(d1, d2, a, a) for (d1, d2) in ((1, 0), (0, 1), (-1, 0), (0, -1)) for a in range(n)]
+    a0mat = [o[:2, :2].T.ravel() for o in S.c4v_ops()]
+    out = {}
+    res = {}
+    for prec in ("mixed", "fp64"):
+        ctx = api.Context.for_problem(ep0, prec)
+        order = [plan[i % len(plan)] for i in range(args.warmup + args.steps)]
+        for ie in order[:args.warmup]:
+            ctx.tauij(eps[ie], pairs, [a2d, 0.0], [0.0, a2d], cvec, a0mat)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        pts = 0
+        for ie in order[args.warmup:]:
+            res[(prec, ie)] = ctx.tauij(eps[ie], pairs, [a2d, 0.0], [0.0, a2d], cvec, a0mat)
+            pts += eps[ie].nk
+        torch.cuda.synchronize()
+        out[prec] = (pts, time.perf_counter() - t0)
+        ctx.close()
+    err = 0.0
+    for ie in set(order[args.warmup:]):
+        a, b = res[("mixed", ie)], res[("fp64", ie)]
+        scale = np.abs(b["tau_ij"]).max()
+        err = max(err, float(np.abs(a["tau_ij"] - b["tau_ij"]).max() / scale),
+                  float(np.abs(a["tau_ji"] - b["tau_ji"]).max() / scale))
+    v = out["mixed"][0] / out["mixed"][1]
+    v64 = out["fp64"][0] / out["fp64"][1]
+    print(json.dumps({"metric": "(E,k) points/s of the off-diagonal interface tau (skkr_gpu_tauij)",
+                      "value": v, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+                      "ms_per_step": 1e3 * out["mixed"][1] / args.steps, "higher_is_better": True,
+                      "dtype": "c128 via BF16x6 slices + FP64 refinement", "data": "synthetic",
+                      "fp64_value": v64, "speedup": v / v64,
+                      "max_abs_err_vs_fp64_rel_to_largest_block": err,
+                      "config": {"workload": WORKLOAD, "pairs": len(pairs), "energies": order[args.warmup:],
+                                 "timing": "host wall clock around whole calls (host buffers)"}}), flush=True)
+
+
 def main():
     args = parse()
     if args.workload == "c3":
         run_c3(args)
+        return
+    if args.workload == "tauij":
+        run_tauij(args)
         return
     rank, ws = dist_init(args.gpus)
     if args.impl == "reference":
