@@ -307,10 +307,18 @@ __global__ void __launch_bounds__(256) k_split_b(MatRef B, int n, int K, int nc,
     float dr[S], di[S];
     slice_digits<S, DB>(v.x, es, dr);
     slice_digits<S, DB>(v.y, es, di);
-    store_digits<S, DB>(dr, 1.0f, 16, base + tiled(2 * j, k, Np), sstride);
-    store_digits<S, DB>(di, -1.0f, 16, base + tiled(2 * j, K + k, Np), sstride);
-    store_digits<S, DB>(di, 1.0f, 16, base + tiled(2 * j + 1, k, Np), sstride);
-    store_digits<S, DB>(dr, 1.0f, 16, base + tiled(2 * j + 1, K + k, Np), sstride);
+    // each digit is converted once and stored twice; -Im is the sign bit flipped
+    __nv_bfloat16 *o0 = base + tiled(2 * j, k, Np), *o1 = base + tiled(2 * j, K + k, Np);
+    __nv_bfloat16 *o2 = base + tiled(2 * j + 1, k, Np), *o3 = base + tiled(2 * j + 1, K + k, Np);
+#pragma unroll
+    for (int p = 0; p < S; p++) {
+      const float sc = pow2f(16 - DB * p);
+      const __nv_bfloat16 br = __float2bfloat16_rn(dr[p] * sc), bi = __float2bfloat16_rn(di[p] * sc);
+      o0[p * sstride] = br;
+      o1[p * sstride] = __hneg(bi);
+      o2[p * sstride] = bi;
+      o3[p * sstride] = br;
+    }
   }
 }
 
