@@ -50,3 +50,24 @@ def test_no_cpu_fallback_when_library_missing(monkeypatch, tmp_path):
     import pytest
     with pytest.raises(RuntimeError):
         native.lib()
+
+
+def test_argument_checks_before_any_device_call():
+    # invalid arguments are refused with SKKR_ERR_ARG before CUDA is touched,
+    # so these run without a GPU
+    import __graft_entry__
+    __graft_entry__.build()
+    lib = ctypes.CDLL(native.LIB_PATH)
+    ARG = -1
+    P, I, D = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+    lib.skkr_gpu_tauij.argtypes = [P, I, P, P, P, P, P, P, P, I, P]
+    assert lib.skkr_gpu_tauij(None, 1, None, None, None, None, None, None, None, 32, None) == ARG
+    lib.skkr_gpu_set_mixed_policy.argtypes = [P, D, D, I, D]
+    assert lib.skkr_gpu_set_mixed_policy(None, 1e-3, 0.0, 0, 1e-2) == ARG
+    s = native.Sizes()
+    s.mode, s.lmax, s.nprc, s.ngeff = 7, 3, 3, 1
+    out = ctypes.c_void_p()
+    lib.skkr_gpu_create.argtypes = [P, P]
+    assert lib.skkr_gpu_create(ctypes.cast(ctypes.pointer(s), P), ctypes.cast(ctypes.pointer(out), P)) == ARG
+    s.mode, s.precision = 1, 5          # unknown precision
+    assert lib.skkr_gpu_create(ctypes.cast(ctypes.pointer(s), P), ctypes.cast(ctypes.pointer(out), P)) == ARG
