@@ -453,9 +453,21 @@ def bcc001(a: float) -> Stacking:
     return Stacking(a, a / 2.0, "bcc(001)")
 
 
+_CLUSTERS = {}
+
+
 def cluster(st: Stacking, nshell: int = 3):
     """Sites within the first nshell neighbour shells of the origin (with it).
-    Returns (vectors (N,3), layer offsets (N,), nn distance)."""
+    Returns (vectors (N,3), layer offsets (N,), nn distance).  The geometry
+    does not depend on the energy: it is computed once per stacking."""
+    key = (st.a2d, st.dz, nshell)
+    if key not in _CLUSTERS:
+        _CLUSTERS[key] = _cluster(st, nshell)
+    v, n, d = _CLUSTERS[key]
+    return v.copy(), n.copy(), d
+
+
+def _cluster(st: Stacking, nshell: int):
     vs, ns = [], []
     rng = range(-6, 7)
     for n in range(-6, 7):

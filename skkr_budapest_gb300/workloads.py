@@ -173,6 +173,53 @@ def system_layers(spec: SystemSpec):
     return ninprc, spec.pl * spec.nprc
 
 
+def screened_table(spec: SystemSpec, ie: int):
+    """G_scr(R) of contour point ie (non-BdG): the screened real-space table
+    the GPU path Fourier-transforms per k, built on the host."""
+    ce = complex(spec.energies[ie])
+    psq = ce + ce * ce / (S.C_LIGHT * S.C_LIGHT) if spec.irel else ce
+    _, _, dnn = S.cluster(spec.stacking, 1)
+    alpha = S.alpha_sqwell(ce, spec.vscreen, 0.7 * dnn, spec.lmax)
+    return S.build_rtable(spec.stacking, psq, alpha, spec.lmax, nshell_screen=spec.screen_shells)
+
+
+def _table_seconds(job):
+    import time
+    spec, ie = job
+    t = time.perf_counter()
+    screened_table(spec, ie)
+    return time.perf_counter() - t
+
+
+def table_build_seconds(spec: SystemSpec, energies, workers: int) -> float:
+    """Wall time to build the screened tables of `energies` on `workers` host
+    processes (spawned: the caller may already hold a CUDA context)."""
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    import os
+    import time
+    if workers <= 1:
+        t = time.perf_counter()
+        for ie in energies:
+            screened_table(spec, ie)
+        return time.perf_counter() - t
+    keep = {k: os.environ.get(k) for k in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS")}
+    for k in keep:
+        os.environ[k] = "1"   # one BLAS thread per worker process
+    try:
+        with cf.ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn")) as ex:
+            list(ex.map(_table_seconds, [(spec, energies[0])] * workers))   # start-up outside the timing
+            t = time.perf_counter()
+            list(ex.map(_table_seconds, [(spec, ie) for ie in energies]))
+            return time.perf_counter() - t
+    finally:
+        for k, v in keep.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+
+
 def energy_problem(spec: SystemSpec, ie: int, nset: int | None = None, kmesh: str = "ibz") -> EnergyProblem:
     """Build the inputs of contour point ie of a system (seeded, deterministic)."""
     if spec.irel == 2:
@@ -189,9 +236,8 @@ def energy_problem(spec: SystemSpec, ie: int, nset: int | None = None, kmesh: st
     fac = psq / ce
     st = spec.stacking
     _, _, dnn = S.cluster(st, 1)
-    rs = 0.7 * dnn
-    alpha = S.alpha_sqwell(ce, spec.vscreen, rs, lmax)
-    rt = S.build_rtable(st, psq, alpha, lmax, nshell_screen=spec.screen_shells)
+    alpha = S.alpha_sqwell(ce, spec.vscreen, 0.7 * dnn, lmax)
+    rt = screened_table(spec, ie)
     ninprc, nintfc = system_layers(spec)
     blkmap = S.blkmap_translation_invariant(rt, spec.nprc + 2, int(max(ninprc)))
 
