@@ -143,7 +143,7 @@ def free_g0(e: complex, rvecs: np.ndarray, lmax: int) -> np.ndarray:
     ph = (1j) ** ((-lv[:, None, None] + lv[None, :, None] - lv2[None, None, :]) % 4)
     coef = -4 * math.pi * 1j * kap * c * ph    # (LM, LM, LM2)
     hy = h[lv2, :].T * yr                      # (N, LM2)
-    return np.einsum("abc,nc->nab", coef, hy)
+    return np.tensordot(hy, coef, axes=([1], [2]))   # (N, LM, LM), one BLAS product
 
 
 # --------------------------------------------------------------------------
@@ -510,15 +510,16 @@ def screened_realspace(e_struct: complex, vecs: np.ndarray, alpha: np.ndarray, l
     big = np.zeros((nsite * lmmax, nsite * lmmax), complex)
     pair_n, pair_m = np.nonzero(~np.eye(nsite, dtype=bool))
     g = free_g0(e_struct, vecs[pair_n] - vecs[pair_m], lmax)
-    for idx, (n, m) in enumerate(zip(pair_n, pair_m)):
-        big[n * lmmax:(n + 1) * lmmax, m * lmmax:(m + 1) * lmmax] = g[idx]
+    big.reshape(nsite, lmmax, nsite, lmmax)[pair_n, :, pair_m, :] = g
     if hole:
         tm = np.kron(np.eye(nsite), lm_conj_matrix(lmax))
         big = -tm @ big.conj().T @ tm
-    # (1 - G0 alpha) X = G0, alpha diagonal per site
+    # (1 - G0 alpha) X = G0, alpha diagonal per site; only the central rows of
+    # X are kept, so the rows of (1 - G0 alpha)^-1 come from lmmax solves of the
+    # transposed system
     amat = np.eye(nsite * lmmax, dtype=complex) - big * np.tile(al, nsite)[None, :]
-    x = np.linalg.solve(amat, big)
-    row = x[:lmmax, :].reshape(lmmax, nsite, lmmax).transpose(1, 0, 2)
+    rinv = np.linalg.solve(amat.T, np.eye(nsite * lmmax, lmmax, dtype=complex)).T   # (lmmax, N)
+    row = (rinv @ big).reshape(lmmax, nsite, lmmax).transpose(1, 0, 2)
     # G_scr(0 -> R_n) couples site 0 (row) to site n (column): G_{0n}
     return np.ascontiguousarray(row)
 
