@@ -267,6 +267,16 @@ int skkr_gpu_kernel_stats(int enable, double *out);
 int skkr_gpu_phystau(int mode, int lmax, double *tau, const double *tinv,
                      const double *alpha, int ld);
 
+/* Screened -> physical tau of one off-diagonal block tau_ij on the device
+ * (cluster/rsp-lay/phystau2.f:2-60, skkr_dbogo_bsf/clu/phystau2.f:2-75, in
+ * the form the cpacoord of skkr_dbogo_bsf applies to tau_ij and tau_ji
+ * before writing them for the cluster code, rsp-scf/cpacoord_ksave.f:976-988,
+ * idiag = 0): tau := (1 + alpha1 tinv1) tau (1 + tinv2 alpha2), alpha1 /
+ * tinv1 of the row layer i, alpha2 / tinv2 of the column layer j; alpha as
+ * for skkr_gpu_phystau. */
+int skkr_gpu_phystau2(int mode, int lmax, double *tau, const double *tinv1, const double *alpha1,
+                      const double *tinv2, const double *alpha2, int ld);
+
 /* Layer DOS of nlay layers from their physical site-diagonal tau (replaces
  * the lambda = 0 moment of nrsp-scf/moment.f:47-110 with locquant.f:86-126,
  * and rsp-scf/moment.f:60-140 with locquant.f:197-232):

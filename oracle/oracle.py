@@ -79,6 +79,7 @@ def _setup(L):
     L.orc_dugo.restype = I
     L.orc_tata.argtypes = [D, I, I, P, P, P]
     L.orc_phystau.argtypes = [P, P, P, P, I, I, I, I]
+    L.orc_phystau2.argtypes = [P, P, P, P, P, I, I, I, I]
     L.orc_cpacoord.argtypes = [P, P, P, P, P, P, P, P, P, P, I, P, I]
     L.orc_cpacoord.restype = I
     L.orc_gk_from_rtable.argtypes = [I, P, P, P, I, D, D, P]
@@ -149,6 +150,20 @@ def phystau(tau, tinv, alpha, lmax, irel):
     ti = to_cm(tinv)
     al = np.asarray(alpha, np.complex128).copy()
     lib().orc_phystau(_ptr(t), _ptr(ti), _ptr(ti), _ptr(al), lmax, irel, n, 1)
+    return from_cm(t)
+
+
+def phystau2(tau, tinv1, alpha1, tinv2, alpha2, lmax, irel, idiag=0):
+    """orc_phystau2: the pair block tau_ij screened -> physical with layer i's
+    (tinv1, alpha1) on the rows and layer j's (tinv2, alpha2) on the columns;
+    idiag=0 is the form cpacoord_ksave.f:982-988 applies to tau_ij / tau_ji."""
+    n = tau.shape[0]
+    t = to_cm(tau)
+    t1 = to_cm(tinv1)
+    t2 = to_cm(tinv2)
+    a1 = np.asarray(alpha1, np.complex128).copy()
+    a2 = np.asarray(alpha2, np.complex128).copy()
+    lib().orc_phystau2(_ptr(t), _ptr(t1), _ptr(a1), _ptr(t2), _ptr(a2), lmax, irel, n, int(idiag))
     return from_cm(t)
 
 

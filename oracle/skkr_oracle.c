@@ -703,10 +703,14 @@ void orc_cpacor(const double *conc, zc *mc, const zc *ma, const zc *mb,
   (*itcpa)++;
 }
 
-/* rsp-scf/phystau.f:2-61 (irel=1, ldex over kappa-mu) and
- * nrsp-scf/phystau.f (irel=0, l over lm).  alpha[l], l = 0..lmax. */
-void orc_phystau(zc *tau, const zc *tinv1, const zc *tinv2, const zc *alpha,
-                 int lmax, int irel, int ld, int idiag) {
+/* cluster/rsp-lay/phystau2.f:2-60 and skkr_dbogo_bsf/clu/phystau2.f:2-75:
+ * the block tau_ij between layers i and j, screened -> physical:
+ *   tau := (1 + alpha1 tinv1) tau (1 + tinv2 alpha2)  [- (alpha1 + alpha1 tinv1 alpha2) if idiag],
+ * alpha1 / tinv1 those of layer i (rows), alpha2 / tinv2 of layer j (columns).
+ * The same l index tables as rsp-scf/phystau.f:2-61 (irel=1, ldex over
+ * kappa-mu), nrsp-scf/phystau.f (irel=0, l over lm).  alpha[l], l = 0..lmax. */
+void orc_phystau2(zc *tau, const zc *tinv1, const zc *alpha1, const zc *tinv2,
+                  const zc *alpha2, int lmax, int irel, int ld, int idiag) {
   int lmmax = (lmax + 1) * (lmax + 1);
   int nd = irel == 2 ? 4 * lmmax : irel ? 2 * lmmax : lmmax;
   size_t sz = (size_t)ld * ld;
@@ -727,9 +731,9 @@ void orc_phystau(zc *tau, const zc *tinv1, const zc *tinv2, const zc *alpha,
       for (int m = -l; m <= l; m++) ldex[k++] = l;
   }
   for (int a = 0; a < nd; a++) {
-    zc al = alpha[ldex[a]];
+    zc al = alpha1[ldex[a]];
     for (int b = 0; b < nd; b++) {
-      zc alp = alpha[ldex[b]];
+      zc alp = alpha2[ldex[b]];
       lmat[IX(a, b, ld)] = al * tinv1[IX(a, b, ld)];
       rmat[IX(a, b, ld)] = tinv2[IX(a, b, ld)] * alp;
       cmat[IX(a, b, ld)] = al * tinv1[IX(a, b, ld)] * alp;
@@ -743,6 +747,12 @@ void orc_phystau(zc *tau, const zc *tinv1, const zc *tinv2, const zc *alpha,
     for (int a = 0; a < nd; a++)
       for (int b = 0; b < nd; b++) tau[IX(a, b, ld)] -= cmat[IX(a, b, ld)];
   free(lmat); free(rmat); free(cmat); free(ldex);
+}
+
+/* rsp-scf/phystau.f:2-61, nrsp-scf/phystau.f: one screening set on both sides */
+void orc_phystau(zc *tau, const zc *tinv1, const zc *tinv2, const zc *alpha,
+                 int lmax, int irel, int ld, int idiag) {
+  orc_phystau2(tau, tinv1, alpha, tinv2, alpha, lmax, irel, ld, idiag);
 }
 
 /* ===================================================================== *

@@ -90,6 +90,10 @@ void orc_cpacor(const double *conc, zc *mc, const zc *ma, const zc *mb,
                 int *concpa, double *error);
 void orc_phystau(zc *tau, const zc *tinv1, const zc *tinv2, const zc *alpha,
                  int lmax, int irel, int ld, int idiag);
+/* pair blocks (cluster/rsp-lay/phystau2.f, skkr_dbogo_bsf/clu/phystau2.f):
+ * alpha1 / tinv1 of the row layer, alpha2 / tinv2 of the column layer */
+void orc_phystau2(zc *tau, const zc *tinv1, const zc *alpha1, const zc *tinv2,
+                  const zc *alpha2, int lmax, int irel, int ld, int idiag);
 
 /* ---- layer DOS: nrsp-scf/moment.f:47-110 + locquant.f:86-126 (lm),
  *      rsp-scf/moment.f:60-140 + locquant.f:197-232 (kappa,mu) ----------

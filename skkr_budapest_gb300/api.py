@@ -304,3 +304,32 @@ def layer_dos(ep, tau, which="a", para=False):
     phys = np.array([N.phystau(tau[li], tinv[li], ep.alpha[li], ep.lmax, ep.irel) for li in range(ep.nintfc)])
     F, G = S.layer_dos_inputs(ep, which)
     return N.layer_dos(phys, F, G, ep.lmax, ep.irel, para)
+
+
+def host_tau(ep, tminv, tauc, tij, pairs):
+    """The physical tau that the BdG layer code hands to the cluster code
+    (skkr_dbogo_bsf/rsp-scf/cpacoord_ksave.f:976-1016), on the device: every
+    pair block of `tij` (Context.tauij: k-summed, screened) through phystau2
+    with layer li's screening on the rows and layer lj's on the columns
+    (tau_ji the other way round, idiag = 0), every layer of the k-summed
+    coherent `tauc` (Context.cpacoord) through phystau.  `tminv` is the
+    coherent t^-1 both were computed with; pairs are (n1, n2, li, lj),
+    0-based layers.  Returns tau_ij, tau_ji (npair, lk, lk), tau_ii
+    (nintfc, lk, lk)."""
+    pa = np.asarray(pairs, np.int64).reshape(-1, 4)
+    lmax, irel, al = ep.lmax, ep.irel, ep.alpha
+    tau_ij = np.array([N.phystau2(tij["tau_ij"][q], tminv[li], al[li], tminv[lj], al[lj], lmax, irel)
+                       for q, (_, _, li, lj) in enumerate(pa)]).reshape(len(pa), ep.lkmax, ep.lkmax)
+    tau_ji = np.array([N.phystau2(tij["tau_ji"][q], tminv[lj], al[lj], tminv[li], al[li], lmax, irel)
+                       for q, (_, _, li, lj) in enumerate(pa)]).reshape(len(pa), ep.lkmax, ep.lkmax)
+    tau_ii = np.array([N.phystau(tauc[li], tminv[li], al[li], lmax, irel) for li in range(ep.nintfc)])
+    return dict(tau_ij=tau_ij, tau_ji=tau_ji, tau_ii=tau_ii)
+
+
+def write_host_tau(taupath, ie, ep, tminv, tauc, tij, pairs):
+    """tauhout after cpacoord: host_tau, then the .tau file of energy index ie
+    (the reference's 1-based contour index, part of the file name) with the
+    number of k points of ep.  Returns the file name."""
+    from . import tauh
+    h = host_tau(ep, tminv, tauc, tij, pairs)
+    return tauh.write_tauh(taupath, ie, ep.ce, ep.nk, pairs, h["tau_ij"], h["tau_ji"], h["tau_ii"])

@@ -1915,24 +1915,35 @@ __global__ void k_phys_mats(const zd *tinv, const zd *alpha, const int *lof, int
   }
 }
 
-extern "C" int skkr_gpu_phystau(int mode, int lmax, double *tau, const double *tinv,
-                                const double *alpha, int ld) {
-  if (!tau || !tinv || !alpha || lmax < 0 || lmax > 3) return SKKR_ERR_ARG;
+// basis size, number of screening constants and the l of every basis index
+// of phystau.f / phystau2.f (ldex over kappa-mu: 2 entries for l = 0, 4l+2
+// for l > 0; BdG: the hole half indexes alpha_h, stored after alpha_e)
+static int phys_basis(int mode, int lmax, int ld, int *nd, int *nal, std::vector<int> &lof) {
+  if (lmax < 0 || lmax > 3) return SKKR_ERR_ARG;
   if (mode != SKKR_NONREL && mode != SKKR_REL && mode != SKKR_BDG) return SKKR_ERR_ARG;
-  const int lmmax = (lmax + 1) * (lmax + 1),
-            nd = mode == SKKR_BDG ? 4 * lmmax : mode == SKKR_REL ? 2 * lmmax : lmmax;
-  const int nal = mode == SKKR_BDG ? 2 * (lmax + 1) : lmax + 1;  // BdG: alpha_e then alpha_h
-  if (ld < nd) return SKKR_ERR_ARG;
-  std::vector<int> lof(nd);
+  const int lmmax = (lmax + 1) * (lmax + 1);
+  *nd = mode == SKKR_BDG ? 4 * lmmax : mode == SKKR_REL ? 2 * lmmax : lmmax;
+  *nal = mode == SKKR_BDG ? 2 * (lmax + 1) : lmax + 1;  // BdG: alpha_e then alpha_h
+  if (ld < *nd) return SKKR_ERR_ARG;
+  lof.assign(*nd, 0);
   if (mode != SKKR_NONREL) {
-    int k = 0;  // ldex of rsp-scf/phystau.f: 2 entries for l=0, 4l+2 for l>0
+    int k = 0;
     for (int l = 0; k < 2 * lmmax; l++)
       for (int q = 0; q < (l == 0 ? 2 : 4 * l + 2) && k < 2 * lmmax; q++) lof[k++] = l;
-    for (int q = 2 * lmmax; q < nd; q++) lof[q] = lof[q - 2 * lmmax] + lmax + 1;
+    for (int q = 2 * lmmax; q < *nd; q++) lof[q] = lof[q - 2 * lmmax] + lmax + 1;
   } else {
     for (int l = 0, k = 0; l <= lmax; l++)
       for (int m = -l; m <= l; m++) lof[k++] = l;
   }
+  return SKKR_OK;
+}
+
+extern "C" int skkr_gpu_phystau(int mode, int lmax, double *tau, const double *tinv,
+                                const double *alpha, int ld) {
+  if (!tau || !tinv || !alpha) return SKKR_ERR_ARG;
+  int nd, nal;
+  std::vector<int> lof;
+  CKR(phys_basis(mode, lmax, ld, &nd, &nal, lof));
   const long long MB = (long long)nd * nd;
   Scoped s;
   zd *T, *Ti, *Al, *Lm, *Rm, *Cm, *H;
@@ -1958,6 +1969,49 @@ extern "C" int skkr_gpu_phystau(int mode, int lmax, double *tau, const double *t
                mref(T, 0, 0, nd), nd, nd, nd, 1, 1, nullptr, 0);
   MatRef Tm = mref(T, 0, 0, nd), Cmm = mref(Cm, 0, 0, nd);
   launch_zaxpby(Tm, Tm, &Cmm, -1.0, nullptr, 0, nd, 1, 1, nullptr, 0);
+  CK(cudaDeviceSynchronize());
+  CK(cudaGetLastError());
+  return download_mats(tau, T, 1, nd, ld);
+}
+
+extern "C" int skkr_gpu_phystau2(int mode, int lmax, double *tau, const double *tinv1,
+                                 const double *alpha1, const double *tinv2, const double *alpha2,
+                                 int ld) {
+  if (!tau || !tinv1 || !alpha1 || !tinv2 || !alpha2) return SKKR_ERR_ARG;
+  int nd, nal;
+  std::vector<int> lof;
+  CKR(phys_basis(mode, lmax, ld, &nd, &nal, lof));
+  const long long MB = (long long)nd * nd;
+  Scoped s;
+  zd *T, *Ti1, *Ti2, *Al1, *Al2, *Lm, *Rm, *Sc, *Cm, *H;
+  int *Lo;
+  CKR(s.alloc(&T, MB));
+  CKR(s.alloc(&Ti1, MB));
+  CKR(s.alloc(&Ti2, MB));
+  CKR(s.alloc(&Al1, nal));
+  CKR(s.alloc(&Al2, nal));
+  CKR(s.alloc(&Lm, MB));
+  CKR(s.alloc(&Rm, MB));
+  CKR(s.alloc(&Sc, MB));
+  CKR(s.alloc(&Cm, MB));
+  CKR(s.alloc(&H, MB));
+  CKR(s.alloc(&Lo, nd));
+  CKR(upload_mats(T, tau, 1, nd, ld));
+  CKR(upload_mats(Ti1, tinv1, 1, nd, ld));
+  CKR(upload_mats(Ti2, tinv2, 1, nd, ld));
+  CK(cudaMemcpy(Al1, alpha1, nal * sizeof(zd), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(Al2, alpha2, nal * sizeof(zd), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(Lo, lof.data(), nd * sizeof(int), cudaMemcpyHostToDevice));
+  // lmat = 1 + alpha1 tinv1 from the row layer, rmat = 1 + tinv2 alpha2 from
+  // the column layer (the other two outputs of each launch are scratch)
+  k_phys_mats<<<4, 256>>>(Ti1, Al1, Lo, nd, Lm, Sc, Cm);
+  SKKR_LAUNCHED();
+  k_phys_mats<<<4, 256>>>(Ti2, Al2, Lo, nd, Sc, Rm, Cm);
+  SKKR_LAUNCHED();
+  launch_zgemm(0, mref(Lm, 0, 0, nd), mref(T, 0, 0, nd), mref(H, 0, 0, nd), mref(H, 0, 0, nd),
+               mref(H, 0, 0, nd), nd, nd, nd, 1, 1, nullptr, 0);
+  launch_zgemm(0, mref(H, 0, 0, nd), mref(Rm, 0, 0, nd), mref(T, 0, 0, nd), mref(T, 0, 0, nd),
+               mref(T, 0, 0, nd), nd, nd, nd, 1, 1, nullptr, 0);
   CK(cudaDeviceSynchronize());
   CK(cudaGetLastError());
   return download_mats(tau, T, 1, nd, ld);

@@ -70,6 +70,7 @@ def lib():
         L.skkr_gpu_cpacoord_bdg.argtypes = [P, D, D, D, D, D, D, P, I, P, P, P, P, P, P, P, P, P, P, P, P, P,
                                             I, P]
         L.skkr_gpu_phystau.argtypes = [I, I, P, P, P, I]
+        L.skkr_gpu_phystau2.argtypes = [I, I, P, P, P, P, P, I]
         L.skkr_gpu_layer_dos.argtypes = [I, I, I, P, I, P, P, I, P, P]
         L.skkr_gpu_set_reduce.argtypes = [P, P, P]
         L.skkr_gpu_set_mixed_policy.argtypes = [P, D, D, I, D]
@@ -166,6 +167,20 @@ def phystau(tau, tinv, alpha, lmax, irel):
     ti = cm(tinv)
     al = np.ascontiguousarray(alpha, np.complex128)
     _check(lib().skkr_gpu_phystau(irel, lmax, _p(t), _p(ti), _p(al), t.shape[-1]), "skkr_gpu_phystau")
+    return uncm(t)
+
+
+def phystau2(tau, tinv1, alpha1, tinv2, alpha2, lmax, irel):
+    """Pair block tau_ij screened -> physical on the device (skkr_gpu_phystau2):
+    (1 + alpha1 tinv1) tau (1 + tinv2 alpha2), layer i's screening on the rows
+    and layer j's on the columns."""
+    t = cm(tau)
+    t1 = cm(tinv1)
+    t2 = cm(tinv2)
+    a1 = np.ascontiguousarray(alpha1, np.complex128)
+    a2 = np.ascontiguousarray(alpha2, np.complex128)
+    _check(lib().skkr_gpu_phystau2(irel, lmax, _p(t), _p(t1), _p(a1), _p(t2), _p(a2), t.shape[-1]),
+           "skkr_gpu_phystau2")
     return uncm(t)
 
 

@@ -60,3 +60,51 @@ def test_tauij_rejects_bad_pairs():
             ctx.tauij(ep, [(0, 0, 0, ep.nintfc)], a1, a2, cvec, a0mat)
     finally:
         ctx.close()
+
+
+@pytest.mark.parametrize("irel,lmax", [(0, 2), (1, 3), (2, 2)])
+def test_phystau2_matches_oracle(irel, lmax):
+    # pair block screened -> physical (phystau2.f, idiag = 0), two layers'
+    # screening on the two sides
+    rng = np.random.default_rng(17 + irel)
+    lm = (lmax + 1) ** 2
+    nd = lm if irel == 0 else 2 * lm if irel == 1 else 4 * lm
+    nal = lmax + 1 if irel < 2 else 2 * (lmax + 1)
+    c = lambda *s: rng.normal(size=s) + 1j * rng.normal(size=s)
+    tau, t1, t2, a1, a2 = c(nd, nd), c(nd, nd), c(nd, nd), 0.3 * c(nal), 0.3 * c(nal)
+    g = native.phystau2(tau, t1, a1, t2, a2, lmax, irel)
+    o = O.phystau2(tau, t1, a1, t2, a2, lmax, irel)
+    assert np.linalg.norm(g - o) < 1e-12 * np.linalg.norm(o)
+
+
+def test_host_tau_file_matches_oracle(tmp_path):
+    # cpacoord, then the pair sums with its coherent t^-1, then the physical
+    # tau of every pair and layer into the .tau file the cluster code reads
+    # (skkr_dbogo_bsf/rsp-scf/cpacoord_ksave.f:949-1036); read back and
+    # compared with the oracle's chain
+    from skkr_budapest_gb300 import tauh
+    ep, pairs, a1, a2, cvec, a0mat = _case("plain")
+    ctx = api.Context.for_problem(ep, "fp64")
+    try:
+        r = ctx.cpacoord(ep)
+    finally:
+        ctx.close()
+    ctx = api.Context.for_problem(ep, "fp64")
+    try:
+        t = ctx.tauij(ep, pairs, a1, a2, cvec, a0mat, tminv=r["tminv"])
+    finally:
+        ctx.close()
+    path = api.write_host_tau(str(tmp_path / "host"), 5, ep, r["tminv"], r["tauc"], t, pairs)
+    assert path.endswith("host0005.tau")
+    f = tauh.read_tauh(str(tmp_path / "host"), 5, ep.ce, pairs, ep.nintfc, ep.lkmax)
+    assert f["nk"] == ep.nk
+    o = O.tauij(ep, pairs, a1, a2, cvec, a0mat, tminv=r["tminv"], nthreads=8)
+    tm, al = r["tminv"], ep.alpha
+    for q, (_, _, i, j) in enumerate(pairs):
+        w_ij = O.phystau2(o["tau_ij"][q], tm[i], al[i], tm[j], al[j], ep.lmax, ep.irel)
+        w_ji = O.phystau2(o["tau_ji"][q], tm[j], al[j], tm[i], al[i], ep.lmax, ep.irel)
+        assert np.linalg.norm(f["tau_ij"][q] - w_ij) < 1e-10 * np.linalg.norm(w_ij), pairs[q]
+        assert np.linalg.norm(f["tau_ji"][q] - w_ji) < 1e-10 * np.linalg.norm(w_ji), pairs[q]
+    for li in range(ep.nintfc):
+        w = O.phystau(r["tauc"][li], tm[li], al[li], ep.lmax, ep.irel)
+        assert np.linalg.norm(f["tau_ii"][li] - w) < 1e-12 * np.linalg.norm(w), li

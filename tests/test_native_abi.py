@@ -62,6 +62,15 @@ def test_argument_checks_before_any_device_call():
     P, I, D = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
     lib.skkr_gpu_tauij.argtypes = [P, I, P, P, P, P, P, P, P, I, P]
     assert lib.skkr_gpu_tauij(None, 1, None, None, None, None, None, None, None, 32, None) == ARG
+    import numpy as np
+    buf = np.zeros(2 * 64 * 64)
+    al = np.zeros(16)
+    bp = buf.ctypes.data
+    lib.skkr_gpu_phystau2.argtypes = [I, I, P, P, P, P, P, I]
+    assert lib.skkr_gpu_phystau2(1, 3, bp, bp, al.ctypes.data, None, al.ctypes.data, 32) == ARG
+    assert lib.skkr_gpu_phystau2(5, 3, bp, bp, al.ctypes.data, bp, al.ctypes.data, 32) == ARG    # mode
+    assert lib.skkr_gpu_phystau2(1, 4, bp, bp, al.ctypes.data, bp, al.ctypes.data, 64) == ARG    # lmax
+    assert lib.skkr_gpu_phystau2(1, 3, bp, bp, al.ctypes.data, bp, al.ctypes.data, 31) == ARG    # ld < 32
     lib.skkr_gpu_set_mixed_policy.argtypes = [P, D, D, I, D]
     assert lib.skkr_gpu_set_mixed_policy(None, 1e-3, 0.0, 0, 1e-2) == ARG
     s = native.Sizes()
