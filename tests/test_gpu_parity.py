@@ -169,3 +169,19 @@ def test_cpacoord_relativistic_with_j_split():
     spec = W.rel_bcc(nsets=[3] * 24, so_split=0.03)
     g, o = _compare(W.energy_problem(spec, 14))
     assert g["cpa_iterations"] == 1
+
+
+def test_empty_k_list_is_refused_and_the_context_stays_usable():
+    import dataclasses
+    ep = W.energy_problem(W.plain_fcc(nset=4), 4)
+    empty = dataclasses.replace(ep, xk=np.zeros((0, 2)), wk=np.zeros(0))
+    ctx = api.Context.for_problem(ep)
+    try:
+        with pytest.raises(native.SkkrError) as ei:
+            ctx.cpacoord(empty)
+        assert ei.value.code == -1
+        g = ctx.cpacoord(ep)
+    finally:
+        ctx.close()
+    assert g["status"] == 0
+    assert rel(g["tauc"], api.cpacoord(ep)["tauc"]) < 1e-13

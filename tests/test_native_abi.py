@@ -80,3 +80,32 @@ def test_argument_checks_before_any_device_call():
     assert lib.skkr_gpu_create(ctypes.cast(ctypes.pointer(s), P), ctypes.cast(ctypes.pointer(out), P)) == ARG
     s.mode, s.precision = 1, 5          # unknown precision
     assert lib.skkr_gpu_create(ctypes.cast(ctypes.pointer(s), P), ctypes.cast(ctypes.pointer(out), P)) == ARG
+
+
+def test_size_limits_at_creation():
+    # the checks of skkr_gpu_create that run before any CUDA call: principal
+    # layers above the 256-row kernels, non-uniform principal layers, slice
+    # counts outside 3..8, more than 8 group elements, no interface PL
+    import __graft_entry__
+    __graft_entry__.build()
+    lib = ctypes.CDLL(native.LIB_PATH)
+    P = ctypes.c_void_p
+    lib.skkr_gpu_create.argtypes = [P, P]
+    ARG, UNSUPPORTED = -1, -5
+
+    def create(mode=1, lmax=3, nprc=3, pl=4, ngeff=8, slices=0, ninprc=None):
+        s = native.Sizes()
+        s.mode, s.lmax, s.nprc, s.ngeff, s.precision, s.slices = mode, lmax, nprc, ngeff, 0, slices
+        for i, v in enumerate(ninprc or [pl] * (nprc + 2)):
+            s.ninprc[i] = v
+        out = ctypes.c_void_p()
+        return lib.skkr_gpu_create(ctypes.cast(ctypes.pointer(s), P), ctypes.cast(ctypes.pointer(out), P))
+
+    assert create(mode=2, lmax=3, pl=5) == UNSUPPORTED        # BdG lmax 3: 5 x 64 = 320 rows
+    assert create(mode=1, lmax=3, pl=9) == UNSUPPORTED        # relativistic: 9 x 32 = 288 rows
+    assert create(ninprc=[4, 4, 2, 4, 4]) == UNSUPPORTED      # non-uniform principal layers
+    assert create(slices=2) == ARG
+    assert create(slices=9) == ARG
+    assert create(ngeff=9) == ARG
+    assert create(nprc=0, ninprc=[4, 4]) == ARG
+    assert create(nprc=17, ninprc=[4] * 18) == ARG
