@@ -1,0 +1,133 @@
+"""The oracle's restatement of the reference's k-space structure constants
+(oracle/kambe.py: main/kamstr.f with incgamma / ilkam / delkam / blm /
+gauntcalc, and the slab screening of main/scrstr.f), CPU:
+
+* the Kambe sums do not depend on the Ewald splitting parameter (the identity
+  the split rests on), at a near-axis and at a complex energy, for the
+  zero, in-plane and out-of-plane separations kamstr distinguishes;
+* at Im E = 0.6 Ry, where the plain lattice sum converges, they equal it:
+  D_L = -i kappa (-1)^l sum_R e^{-ik.R} h_l(kappa|R+s|) Y*_L(R+s), to rounding
+  out of plane and to the reference's own in-plane shift s_z = 1.1e-4 in plane;
+* blm is the Gaunt integral of three Condon-Shortley harmonics, and kamstr's
+  alm(k, s) is the sum of the free-space constants of the real-space tables at
+  -k (the orientation the slab and table comparison uses);
+* the Fourier transform of the real-space screened table approaches the
+  reference's k-space slab screening as the table keeps more shells, for a
+  barrier that localises the screened constants."""
+import math
+
+import numpy as np
+import pytest
+
+import kambe as K
+from skkr_budapest_gb300 import synth as S
+from skkr_budapest_gb300 import workloads as W
+
+A2D = 4.808326112068523
+LAT = K.Lattice2D([A2D, 0.0], [0.0, A2D])
+K0 = (0.21, 0.07)
+
+
+def _hankel(lmax, x):
+    # h_l^(1) by upward recursion (stable for the outgoing wave); x (N,)
+    x = np.asarray(x, complex)
+    h = np.zeros((lmax + 1,) + x.shape, complex)
+    hm1 = np.exp(1j * x) / x
+    h[0] = -1j * np.exp(1j * x) / x
+    if lmax >= 1:
+        h[1] = h[0] / x - hm1
+    for l in range(1, lmax):
+        h[l + 1] = (2 * l + 1) / x * h[l] - h[l - 1]
+    return h
+
+
+SEPS = [(0.0, 0.0, 0.0), (1.2, 0.7, 3.4), (0.5 * A2D, 0.5 * A2D, 0.0), (0.4, -1.1, -6.8)]
+
+
+@pytest.mark.parametrize("e", [0.3 + 0.01j, 0.4 + 0.6j, -0.45 + 0.06j])
+@pytest.mark.parametrize("sep", SEPS)
+def test_kambe_sums_do_not_depend_on_the_ewald_parameter(e, sep):
+    d1 = K.kambe_dlm(e, *K0, sep, 4, LAT, factor=1.0)
+    d2 = K.kambe_dlm(e, *K0, sep, 4, LAT, factor=0.55)
+    assert np.abs(d1 - d2).max() < 1e-12 * np.abs(d1).max()
+
+
+@pytest.mark.parametrize("sep", SEPS)
+def test_kambe_sums_equal_the_plain_lattice_sum(sep):
+    e, lmax2 = 0.4 + 0.6j, 4
+    kap = np.sqrt(e)
+    d = K.kambe_dlm(e, *K0, sep, lmax2, LAT)
+    rv = LAT.rvecs(160.0, centre=(-sep[0], -sep[1]))         # |h_l| ~ exp(-0.40 r): below 1e-27 there
+    r = np.c_[rv + np.asarray(sep[:2]), np.full(len(rv), sep[2])]
+    rr = np.linalg.norm(r, axis=1)
+    keep = rr > 1e-8
+    rv, r, rr = rv[keep], r[keep], rr[keep]
+    h = _hankel(lmax2, kap * rr)                             # (lmax2+1, N)
+    y = S.ylm(lmax2, r)                                      # the generator's Y_lm, (N, LM)
+    lv = np.array([l for l in range(lmax2 + 1) for _ in range(-l, l + 1)])
+    ph = np.exp(-1j * (rv @ np.asarray(K0)))
+    bf = (ph[:, None] * h[lv].T * np.conj(y)).sum(0) * (-1j * kap) * (-1.0) ** lv
+    in_plane = sep[2] == 0.0 and any(sep[:2])
+    # in plane: kamstr moves the pair to s_z = 1.1e-4 (kamstr.f:136-140), a
+    # first-order change of the odd-(l+m) sums of 4e-5 of the largest at lmax2 = 4
+    assert np.abs(d - bf).max() < (1e-4 if in_plane else 1e-12) * np.abs(bf).max()
+
+
+def test_blm_is_the_gaunt_integral_of_condon_shortley_harmonics():
+    xg, wg = np.polynomial.legendre.leggauss(12)
+    pts = [(ct, w, 2 * math.pi * p / 24) for ct, w in zip(xg, wg) for p in range(24)]
+    ys = [K.ylmc((math.sqrt(1 - ct * ct) * math.cos(ph), math.sqrt(1 - ct * ct) * math.sin(ph), ct), 4)
+          for ct, _, ph in pts]
+    ws = np.array([w * 2 * math.pi / 24 for _, w, _ in pts])
+    Y = np.array(ys)
+    idx = [(l, m) for l in range(5) for m in range(-l, l + 1)]
+    for (l1, m1) in idx[:9]:
+        for (l2, m2) in idx[:9]:
+            for (l3, m3) in idx:
+                q = np.sum(ws * Y[:, l1 * (l1 + 1) + m1] * Y[:, l2 * (l2 + 1) + m2] * Y[:, l3 * (l3 + 1) + m3])
+                assert abs(K.blm(l1, m1, l2, m2, l3, m3) - q) < 1e-12, (l1, m1, l2, m2, l3, m3)
+
+
+@pytest.mark.parametrize("sep", SEPS[:3])
+def test_reference_alm_is_the_table_convention_sum_at_minus_k(sep):
+    # kamstr's Gaunt table (blm, gauntcalc) against the free-space constants of
+    # the real-space tables: alm(k, s) = sum_R e^{-ik.R} G0(R + s)
+    e, lmax = 0.4 + 0.6j, 2
+    a = K.kamstr(e, *K0, lmax, sep, LAT)
+    b = K.lattice_g(e, -K0[0], -K0[1], lmax, sep, LAT)
+    assert np.abs(a - b).max() < 1e-13 * np.abs(b).max()
+    # and at this energy the same as the direct sum of the generator's G0
+    rv = LAT.rvecs(60.0, centre=(-sep[0], -sep[1]))
+    r = np.c_[rv + np.asarray(sep[:2]), np.full(len(rv), sep[2])]
+    keep = np.linalg.norm(r, axis=1) > 1e-8
+    g = S.free_g0(e, r[keep], lmax)
+    direct = np.tensordot(np.exp(-1j * (rv[keep] @ np.asarray(K0))), g, axes=([0], [0]))
+    in_plane = sep[2] == 0.0 and any(sep[:2])                 # the s_z = 1.1e-4 shift again
+    assert np.abs(a - direct).max() < (1e-4 if in_plane else 1e-6) * np.abs(direct).max()
+
+
+def test_table_transform_approaches_the_slab_screening():
+    spec = W.plain_fcc(nset=4)
+    st = spec.stacking
+    _, _, dnn = S.cluster(st, 1)
+    ce = complex(spec.energies[8])
+    al = S.alpha_sqwell(ce, 4.0, 0.5 * dnn, spec.lmax)    # a barrier that localises
+    kx, ky = 0.31, 0.12
+    nl = 8
+    pos = np.array([st.site(n, 0, 0) for n in range(nl)])
+    gs = K.screened_slab(ce, kx, ky, spec.lmax, pos, [al] * nl, LAT)
+    a = nl // 2
+    ref = [gs[a, a + dl] for dl in range(3)]
+    scale = np.linalg.norm(ref[0])
+    err = {}
+    for keep in (3, 5, 9):
+        big, _, _ = S.cluster(st, 11)
+        vecs, ns, _ = S.cluster(st, keep)
+        gt = S.screened_realspace(ce, big, al, spec.lmax)[:len(vecs)]
+        e = 0.0
+        for dl in range(3):
+            sel = ns == dl
+            t = np.tensordot(np.exp(1j * (vecs[sel][:, 0] * kx + vecs[sel][:, 1] * ky)), gt[sel], axes=([0], [0]))
+            e = max(e, np.linalg.norm(t - ref[dl]) / scale)
+        err[keep] = e
+    assert err[3] < 3e-2 and err[5] < 1e-3 and err[9] < 1e-4, err
