@@ -23,12 +23,18 @@ the reference's formulation:
                                + the s = 0 correction (formula 55), then
                                alm = sum_L gau D_L
 
-The reference switches to a direct plane-wave sum (main/directg.f) for layer
-pairs with |s_z| |b|_min >= 5 (main/gstore.f:158-166); both evaluate the same
-lattice sum, and this module uses the Kambe sums for every pair.  Lattice
-vectors are taken within fixed cut-offs (`gcut`, `rcut`) instead of the
-shell-by-shell stopping rule of kamstr.f (1e-10 absolute change), which only
-decides where a converged sum is truncated."""
+  sphrm     main/sphrm.f       Y_lm of complex angles (evanescent waves)
+  directg   main/directg.f:2   the plane-wave form of the same lattice sum,
+                               which gstore.f:158-166 uses for layer pairs
+                               with |s_z| |b|_min >= 5
+  gstore_block                 that choice between kamstr and directg
+  screened_slab                gstore.f:146-185 + scrstr.f: the slab of layers
+                               and its screening in k space
+
+Lattice vectors are taken within fixed cut-offs (`gcut`, `rcut`) instead of
+the shell-by-shell stopping rules of kamstr.f (1e-10 absolute change) and
+directg.f (1e-12 relative), which only decide where a converged sum is
+truncated."""
 from __future__ import annotations
 
 import math
@@ -403,18 +409,29 @@ def lattice_g(e: complex, kx: float, ky: float, lmax: int, sep, lat: Lattice2D, 
     return 4 * math.pi * np.tensordot(_gaunt_ours(lmax) * ph, p, axes=([2], [0]))
 
 
-def screened_slab(e: complex, kx: float, ky: float, lmax: int, pos, alpha, lat: Lattice2D, **cut) -> np.ndarray:
+def gstore_block(e: complex, kx: float, ky: float, lmax: int, sep, lat: Lattice2D) -> np.ndarray:
+    """alm(k, sep) the way main/gstore.f:146-170 evaluates block (a, b) of
+    gtotal for sep = c_a - c_b: the plane-wave sum of directg.f when
+    |s_z| |b|_min >= 5 (its gp for s_z > 0, its gm of -sep otherwise), else
+    the Kambe sums of kamstr.f."""
+    s = np.asarray(sep, float)
+    if abs(s[2]) * lat.bmin >= 5.0:
+        if s[2] > 0:
+            return directg(e, kx, ky, lmax, s, lat)[0]
+        return directg(e, kx, ky, lmax, -s, lat)[1]
+    return kamstr(e, kx, ky, lmax, s, lat)
+
+
+def screened_slab(e: complex, kx: float, ky: float, lmax: int, pos, alpha, lat: Lattice2D) -> np.ndarray:
     """main/gstore.f:146-185 + main/scrstr.f:2-138: the layer-pair constants of
     a slab of layers at positions pos (nl, 3), screened as
     G' = G (1 - alpha G)^-1 with alpha[a, l] per layer and l.
 
-    Block (a, b) is the Bloch sum over the sites R_b = pos_b + R of layer b of
-    G0(pos_a - R_b) (the orientation G_nm = G0(R_n - R_m) of the real-space
-    screened tables) with the phase e^{ik.(R_b - pos_a)} of the full in-plane
-    site vectors, i.e. e^{ik.(pos_b - pos_a)} alm(k, pos_a - pos_b) with alm the
-    sum kamstr.f evaluates for block (a, b) of gtotal (gstore.f:146-170): the
-    reference's blocks differ only by that in-plane phase.  Returns
-    (nl, nl, lmmax, lmmax)."""
+    Block (a, b) is gstore's alm(k, pos_a - pos_b) times the in-plane phase
+    e^{ik.(pos_b - pos_a)}: the Bloch sum over the sites R_b = pos_b + R of
+    layer b of G0(pos_a - R_b) with the phase e^{ik.(R_b - pos_a)} of the full
+    site vectors, the orientation (G_nm = G0(R_n - R_m)) and phase convention
+    of the real-space screened tables.  Returns (nl, nl, lmmax, lmmax)."""
     pos = np.asarray(pos, float)
     nl, lm = len(pos), (lmax + 1) ** 2
     lv = np.array([l for l in range(lmax + 1) for _ in range(-l, l + 1)])
@@ -424,9 +441,90 @@ def screened_slab(e: complex, kx: float, ky: float, lmax: int, pos, alpha, lat: 
         for b in range(nl):
             s = tuple(np.round(pos[a] - pos[b], 10))
             if s not in cache:
-                cache[s] = lattice_g(e, -kx, -ky, lmax, s, lat, **cut)
+                cache[s] = gstore_block(e, kx, ky, lmax, s, lat)
             ph = np.exp(1j * (kx * (pos[b][0] - pos[a][0]) + ky * (pos[b][1] - pos[a][1])))
             g[a * lm:(a + 1) * lm, b * lm:(b + 1) * lm] = ph * cache[s]
     al = np.concatenate([np.asarray(alpha[a], complex)[lv] for a in range(nl)])
     gs = g @ np.linalg.inv(np.eye(nl * lm) - al[:, None] * g)
     return gs.reshape(nl, lm, nl, lm).transpose(0, 2, 1, 3)
+
+
+def sphrm(ct: complex, st: complex, cf: complex, lmax: int) -> np.ndarray:
+    """main/sphrm.f: Y_lm for the complex angles (cos, sin, e^{i phi}) of an
+    evanescent wave vector, by the explicit m = l, l-1 forms and the
+    recurrence in l; index l(l+1)+m."""
+    y = np.zeros((lmax + 1) ** 2 + 1, complex)      # 1-based as in the Fortran
+    y[1] = math.sqrt(0.25 / math.pi)
+    if lmax == 0:
+        return y[1:]
+    a = b = asg = 1.0
+    sf = sa = 1.0 + 0j
+    lp = 1
+    for l in range(1, lmax + 1):
+        fl = float(l)
+        a = 0.5 * a * fl * (2.0 * fl - 1.0)
+        b = fl * b
+        asg = -asg
+        lm = lp + 1
+        lp = lp + l + l + 1
+        sf = sf * cf
+        fac = math.sqrt((2.0 * fl + 1.0) * a / (4.0 * math.pi * b * b)) * sa
+        y[lm] = fac * st / sf
+        y[lp] = asg * fac * st * sf
+        fac = math.sqrt(2.0 * fl) * fac * ct
+        y[lm + 1] = fac * cf / sf
+        y[lp - 1] = -asg * fac * sf / cf
+        sa = sa * st
+    if lmax == 1:
+        return y[1:]
+    for m in range(2, lmax + 1):
+        mm = m + m - 4
+        fm = float(m - 2)
+        a = math.sqrt(1.0 / (fm + fm + 3.0))
+        ln = m * m - 1
+        lm = ln - m - m + 2
+        for l in range(m, lmax + 1):
+            fl = float(l)
+            b = math.sqrt((fl + fm) * (fl - fm) / ((fl + fl + 1.0) * (fl + fl - 1.0)))
+            lp = ln + l + l
+            y[lp] = (ct * y[ln] - a * y[lm]) / b
+            y[lp - mm] = (ct * y[ln - mm] - a * y[lm - mm]) / b
+            a = b
+            lm = ln
+            ln = lp
+    return y[1:]
+
+
+def directg(e: complex, kx: float, ky: float, lmax: int, sep, lat: Lattice2D, gcut: float = 30.0):
+    """main/directg.f:2-151: the plane-wave form of the layer-pair sums that
+    gstore.f:158-166 uses when |s_z| |b|_min >= 5 (s_z > 0).  Returns
+    (gp, gm): gp is block (j, i) and gm block (i, j) of gtotal for
+    sep = c_j - c_i, i.e. alm(k, sep) and alm(k, -sep) of kamstr."""
+    lmx2 = (lmax + 1) ** 2
+    kappa2 = complex(e)
+    kappa = np.sqrt(kappa2)
+    f1 = 8.0 * math.pi * math.pi / lat.area
+    gp = np.zeros((lmx2, lmx2), complex)
+    gm = np.zeros((lmx2, lmx2), complex)
+    s1, s2, s3 = (float(t) for t in sep)
+    lv = np.array([l for l in range(lmax + 1) for _ in range(-l, l + 1)])
+    mv = np.array([m for l in range(lmax + 1) for m in range(-l, l + 1)])
+    neg = np.array([l * (l + 1) - m for l in range(lmax + 1) for m in range(-l, l + 1)])
+    sl, il, sm = (-1.0) ** lv, (1j) ** lv, (-1.0) ** mv
+    for g in lat.gvecs(gcut, centre=(-kx, -ky)):
+        gkx, gky = g[0] + kx, g[1] + ky
+        gk2 = gkx * gkx + gky * gky
+        gk = math.sqrt(gk2)
+        gkz = np.sqrt(kappa2 - gk2)
+        phi = (gkx + 1j * gky) / gk if gk > 1e-6 else 1.0 + 0j
+        y = sphrm(gkz / kappa, gk / kappa, phi, lmax)
+        ylm1 = sl * il * y
+        ylm2 = il * sm * y[neg]
+        ylm3 = il * sm * y
+        ylm4 = sl * il * y[neg]
+        fp = np.exp(1j * (gkx * s1 + gky * s2 + gkz * s3)) * f1 / gkz
+        fm = np.exp(1j * (-gkx * s1 - gky * s2 + gkz * s3)) * f1 / gkz
+        # gp(lmj, lmi) += ylm1(lmi) fp ylm2(lmj) (-i)
+        gp += -1j * fp * np.outer(ylm2, ylm1)
+        gm += -1j * fm * np.outer(ylm4, ylm3)
+    return gp, gm

@@ -11,6 +11,7 @@ gauntcalc, and the slab screening of main/scrstr.f), CPU:
 * blm is the Gaunt integral of three Condon-Shortley harmonics, and kamstr's
   alm(k, s) is the sum of the free-space constants of the real-space tables at
   -k (the orientation the slab and table comparison uses);
+* the plane-wave sums of directg.f equal the Kambe sums for distant layers;
 * the Fourier transform of the real-space screened table approaches the
   reference's k-space slab screening as the table keeps more shells, for a
   barrier that localises the screened constants."""
@@ -104,6 +105,18 @@ def test_reference_alm_is_the_table_convention_sum_at_minus_k(sep):
     direct = np.tensordot(np.exp(-1j * (rv[keep] @ np.asarray(K0))), g, axes=([0], [0]))
     in_plane = sep[2] == 0.0 and any(sep[:2])                 # the s_z = 1.1e-4 shift again
     assert np.abs(a - direct).max() < (1e-4 if in_plane else 1e-6) * np.abs(direct).max()
+
+
+@pytest.mark.parametrize("e", [0.4 + 0.6j, 0.3 + 0.01j, -0.45 + 0.06j])
+@pytest.mark.parametrize("sep", [(0.5 * A2D, 0.5 * A2D, 6.8), (0.3, -0.8, 10.2), (0.0, 0.0, 13.6)])
+def test_directg_equals_kamstr_for_distant_layers(e, sep):
+    # the two forms gstore.f chooses between: plane waves (directg.f) and the
+    # Ewald split (kamstr.f), independent formulas for the same lattice sum
+    gp, gm = K.directg(e, *K0, 2, sep, LAT)
+    a = K.kamstr(e, *K0, 2, sep, LAT)
+    b = K.kamstr(e, *K0, 2, tuple(-x for x in sep), LAT)
+    assert np.abs(gp - a).max() < 1e-13 * np.abs(a).max()
+    assert np.abs(gm - b).max() < 1e-13 * np.abs(b).max()
 
 
 def test_table_transform_approaches_the_slab_screening():
