@@ -15,7 +15,8 @@ the reference's formulation:
   incgamma  main/incgamma.f:7  Gamma(1/2 - n, z) by downward recursion from erfc
   ilkam     main/ilkam.f:5     the real-space Ewald integrals I_l
   delkam    main/delkam.f:5    the Delta_n integrals of the out-of-plane case
-  ylmc      main/ylmc.f        complex Y_lm, Condon-Shortley phase
+  ylmc      main/ylmc.f        complex Y_lm, Condon-Shortley phase, from its
+                               power-series table of d^m P_l / dx^m
   blm       main/blm.f         Gaunt integral of three Y_lm
   gauntcalc main/gauntcalc.f:2 the coupling table of kamstr
   kamstr    main/kamstr.f:20   D_L = reciprocal part (formulas 35 / 50 of the
@@ -131,14 +132,37 @@ def delkam(n: int, x: complex, zz: complex) -> np.ndarray:
     return delta[:n + 1]
 
 
-def _legendre_derivs(lmax: int, x: float) -> np.ndarray:
-    """d^m P_l / dx^m at x, [l, m] (the b(l,m,k) polynomial sums of ylmc.f)."""
-    out = np.zeros((lmax + 1, lmax + 1))
-    for l in range(lmax + 1):
-        c = np.polynomial.legendre.Legendre.basis(l).convert(kind=np.polynomial.Polynomial)
+_YLM_B: dict = {}
+
+
+def _ylm_table(lmax: int) -> np.ndarray:
+    """b[l, m, k] of main/ylmc.f: the power-series coefficients of
+    d^m P_l / dx^m, from the coefficients a[l, n] of P_l (its recursion
+    a(l,n) = (2l-1)/l a(l-1,n-1) - (l-1)/l a(l-2,n)) and n!/(n-m)!."""
+    if lmax in _YLM_B:
+        return _YLM_B[lmax]
+    L = max(lmax, 2)
+    a = np.zeros((L + 1, L + 1))
+    a[0, 0], a[1, 1], a[2, 0], a[2, 2] = 1.0, 1.0, -0.5, 1.5
+    for l in range(3, L + 1):
+        fa1, fa2 = (2 * l - 1) / l, -(l - 1) / l
+        a[l, 0] = fa2 * a[l - 2, 0]
+        for n in range(1, l - 1):
+            a[l, n] = fa1 * a[l - 1, n - 1] + fa2 * a[l - 2, n]
+        a[l, l - 1] = fa1 * a[l - 1, l - 2]
+        a[l, l] = fa1 * a[l - 1, l - 1]
+    f = np.zeros((L + 1, L + 1))
+    for n in range(L + 1):
+        f[n, 0] = 1.0
+        for m in range(n):
+            f[n, m + 1] = f[n, m] * (n - m)
+    b = np.zeros((L + 1, L + 1, L + 1))
+    for l in range(L + 1):
         for m in range(l + 1):
-            out[l, m] = c.deriv(m)(x) if m else c(x)
-    return out
+            for k in range(l - m + 1):
+                b[l, m, k] = a[l, k + m] * f[k + m, m]
+    _YLM_B[lmax] = b
+    return b
 
 
 def ylmc(v, lmax: int) -> np.ndarray:
@@ -152,13 +176,15 @@ def ylmc(v, lmax: int) -> np.ndarray:
         d = math.sqrt(x * x + y * y)
         ephi = 1.0 + 0j if d < 1e-6 else (x + CI * y) / d
     px = math.sqrt(max(1.0 - cth * cth, 0.0)) + 1e-30
-    dp = _legendre_derivs(lmax, cth)
+    b = _ylm_table(lmax)
+    p = cth ** np.arange(lmax + 1)
     out = np.zeros((lmax + 1) ** 2, complex)
     for l in range(lmax + 1):
         for m in range(-l, l + 1):
             mb = abs(m)
             cf = math.sqrt((2 * l + 1) * _fac(l - mb) / (4 * math.pi * _fac(l + mb))) * CI ** (m + mb)
-            out[l * (l + 1) + m] = cf * px ** mb * dp[l, mb] * ephi ** m
+            t = float(b[l, mb, :l + 1] @ p[:l + 1])
+            out[l * (l + 1) + m] = cf * px ** mb * t * ephi ** m
     return out
 
 
@@ -528,3 +554,16 @@ def directg(e: complex, kx: float, ky: float, lmax: int, sep, lat: Lattice2D, gc
         gp += -1j * fp * np.outer(ylm2, ylm1)
         gm += -1j * fm * np.outer(ylm4, ylm3)
     return gp, gm
+
+
+def slab_table_blocks(e: complex, kx: float, ky: float, lmax: int, pos, alpha, lat: Lattice2D, blk_of_j: dict,
+                      centre: int) -> np.ndarray:
+    """The reference's G_scr(k) in the block layout of the real-space tables:
+    block blk_of_j[j] = screened slab block (centre, centre + j), the layer
+    offsets -jmax..jmax that gstore.f:236-282 keeps of gtotal as g2d."""
+    gs = screened_slab(e, kx, ky, lmax, pos, alpha, lat)
+    lm = (lmax + 1) ** 2
+    out = np.zeros((len(blk_of_j), lm, lm), complex)
+    for j, b in blk_of_j.items():
+        out[b] = gs[centre, centre + j]
+    return out

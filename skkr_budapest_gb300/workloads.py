@@ -89,6 +89,7 @@ class SystemSpec:
     radius: float = 2.5
     so_split: float = 0.03
     vscreen: float = 2.0
+    rscreen: float = 0.7      # radius of the screening spheres in units of the NN distance
     alloy_layers: tuple = ()
     conc_range: tuple = (0.1, 0.9)
     alloy_depth_range: tuple = (-1.2, -0.4)
@@ -179,7 +180,7 @@ def screened_table(spec: SystemSpec, ie: int):
     ce = complex(spec.energies[ie])
     psq = ce + ce * ce / (S.C_LIGHT * S.C_LIGHT) if spec.irel else ce
     _, _, dnn = S.cluster(spec.stacking, 1)
-    alpha = S.alpha_sqwell(ce, spec.vscreen, 0.7 * dnn, spec.lmax)
+    alpha = S.alpha_sqwell(ce, spec.vscreen, spec.rscreen * dnn, spec.lmax)
     return S.build_rtable(spec.stacking, psq, alpha, spec.lmax, nshell_screen=spec.screen_shells)
 
 
@@ -236,7 +237,7 @@ def energy_problem(spec: SystemSpec, ie: int, nset: int | None = None, kmesh: st
     fac = psq / ce
     st = spec.stacking
     _, _, dnn = S.cluster(st, 1)
-    alpha = S.alpha_sqwell(ce, spec.vscreen, 0.7 * dnn, lmax)
+    alpha = S.alpha_sqwell(ce, spec.vscreen, spec.rscreen * dnn, lmax)
     rt = screened_table(spec, ie)
     ninprc, nintfc = system_layers(spec)
     blkmap = S.blkmap_translation_invariant(rt, spec.nprc + 2, int(max(ninprc)))
@@ -299,7 +300,7 @@ def _bdg_problem(spec: SystemSpec, ie: int, nset, kmesh) -> EnergyProblem:
     lk = 4 * (lmax + 1) ** 2
     st = spec.stacking
     _, _, dnn = S.cluster(st, 1)
-    rs = 0.7 * dnn
+    rs = spec.rscreen * dnn
     alpha_e = S.alpha_sqwell(psq, spec.vscreen, rs, lmax)
     alpha_h = S.alpha_sqwell_hole(ef - ce, spec.vscreen, rs, lmax)
     rt = S.build_rtable(st, psq, alpha_e, lmax, nshell_screen=spec.screen_shells)

@@ -14,7 +14,10 @@ gauntcalc, and the slab screening of main/scrstr.f), CPU:
 * the plane-wave sums of directg.f equal the Kambe sums for distant layers;
 * the Fourier transform of the real-space screened table approaches the
   reference's k-space slab screening as the table keeps more shells, for a
-  barrier that localises the screened constants."""
+  barrier that localises the screened constants;
+* carried through the oracle's k loop, the reference's G(k) gives a k-summed
+  tau 2.6e-2 from the 3-shell table's at that barrier, and with the
+  configured barrier it sends the lead decimation past surfgf's limit."""
 import math
 
 import numpy as np
@@ -144,3 +147,62 @@ def test_table_transform_approaches_the_slab_screening():
             e = max(e, np.linalg.norm(t - ref[dl]) / scale)
         err[keep] = e
     assert err[3] < 3e-2 and err[5] < 1e-3 and err[9] < 1e-4, err
+
+
+def _per_k_tau(ep, blocks_of_k):
+    # the oracle's k loop one k point at a time, on a table with one entry per
+    # block at R = 0 holding that k's blocks; summed with the k weights (the
+    # systems here have no alloy layer, so the CPA loop makes one pass)
+    import dataclasses
+    import oracle as O
+    tau, status = 0, []
+    for ik in range(ep.nk):
+        rt = ep.rt
+        fake = S.RTable(rt.lmax, rt.nblk, np.arange(rt.nblk + 1, dtype=np.int32), np.zeros((rt.nblk, 2)),
+                        np.ascontiguousarray(blocks_of_k(ik)), rt.jmax, rt.blk_of_j)
+        r = O.cpacoord(dataclasses.replace(ep, xk=ep.xk[ik:ik + 1], wk=ep.wk[ik:ik + 1], rt=fake))
+        status.append(r["status"])
+        if r["status"] == 0:
+            tau = tau + r["tauc"]
+    return tau, status
+
+
+def test_tau_with_the_reference_form_of_g():
+    import oracle as O
+    spec = W.plain_fcc(nset=4)
+    spec.vscreen, spec.rscreen = 4.0, 0.5            # a barrier that localises
+    st = spec.stacking
+    ep = W.energy_problem(spec, 8)
+    assert all(c == 1.0 for c in ep.conc)
+    ref = O.cpacoord(ep, nthreads=4)
+    # the per-k route reproduces the oracle's own k loop
+    same, st_same = _per_k_tau(ep, lambda ik: S.gk_blocks(ep.rt, ep.xk[ik]))
+    assert all(s == 0 for s in st_same)
+    assert np.linalg.norm(same - ref["tauc"]) < 1e-12 * np.linalg.norm(ref["tauc"])
+    nl = 8
+    pos = np.array([st.site(n, 0, 0) for n in range(nl)])
+    kam, st_k = _per_k_tau(ep, lambda ik: K.slab_table_blocks(ep.psq, ep.xk[ik][0], ep.xk[ik][1], ep.lmax, pos,
+                                                              [ep.alpha[0]] * nl, LAT, ep.rt.blk_of_j, nl // 2))
+    assert all(s == 0 for s in st_k)
+    # the 3-shell table against the reference's G(k): 2.6e-2 at this energy
+    d = np.linalg.norm(kam - ref["tauc"]) / np.linalg.norm(kam)
+    assert 1e-3 < d < 5e-2, d
+
+
+def test_configured_screening_breaks_the_reference_form():
+    # with 2 Ry in spheres of 0.7 d_NN the screened constants do not decay
+    # within the principal layer; cut to the layer offsets gstore.f keeps, the
+    # reference's G(k) sends the lead decimation past the 1e10 limit of
+    # surfgf.f (status 2: the reference stops), while the table form is fine
+    import dataclasses
+    import oracle as O
+    spec = W.plain_fcc(nset=4)
+    st = spec.stacking
+    ep = W.energy_problem(spec, 8)
+    assert O.cpacoord(ep, nthreads=4)["status"] == 0
+    nl = 8
+    pos = np.array([st.site(n, 0, 0) for n in range(nl)])
+    ep1 = dataclasses.replace(ep, xk=ep.xk[:1], wk=ep.wk[:1])
+    _, status = _per_k_tau(ep1, lambda ik: K.slab_table_blocks(ep.psq, ep.xk[0][0], ep.xk[0][1], ep.lmax, pos,
+                                                               [ep.alpha[0]] * nl, LAT, ep.rt.blk_of_j, nl // 2))
+    assert status == [2]
