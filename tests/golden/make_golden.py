@@ -1,6 +1,8 @@
 """Extract the reference's own known answers for the contour and k-mesh
-generators from its sample run sample/02-layer-scf (input_rsp.in,
-input_geo.in and the run log Nb8_110.prn) into sample02_contour.json.
+generators, and the 2D lattice of the Kambe sums (unit-cell area, real and
+reciprocal cell vectors as routine VECTOR2D prints them), from its sample run
+sample/02-layer-scf (input_rsp.in, input_geo.in and the run log
+Nb8_110.prn) into sample02_contour.json.
 
 Run here, where the reference tree is mounted:
     python tests/golden/make_golden.py /root/reference
@@ -44,6 +46,13 @@ for line in prn:
     m = pat.search(line)
     if m:
         pts.append([int(m.group(1)), float(m.group(2)), float(m.group(3)), int(m.group(4))])
+for i, line in enumerate(prn):
+    if "unit cell area:" in line and "area2d" not in out:
+        out["area2d"] = float(line.split()[-1])
+    if "real lattice unit cell in 2D:" in line and "a_vectors" not in out:
+        out["a_vectors"] = [[float(v) for v in prn[i + j].split()] for j in (2, 3)]
+    if "reciprocal lattice unit cell in 2D:" in line and "b_vectors" not in out:
+        out["b_vectors"] = [[float(v) for v in prn[i + j].split()] for j in (2, 3)]
 n = out["nepanel"]
 out["energies"] = [[p[1], p[2]] for p in pts[:n]]
 out["nk"] = [p[3] for p in pts[:n]]

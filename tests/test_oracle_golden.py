@@ -1,5 +1,6 @@
 """The oracle's generators against the reference's own sample run
-(sample/02-layer-scf: contour energies and k-mesh sizes printed in its log)."""
+(sample/02-layer-scf: contour energies, k-mesh sizes and the 2D lattice cell
+printed in its log)."""
 import json
 import os
 
@@ -54,3 +55,17 @@ def test_alpha_package_equals_oracle():
         a0 = O.alpha_sqwell(e, 2.0, 3.2, 3)
         a1 = S.alpha_sqwell(e, 2.0, 3.2, 3)
         assert np.allclose(a0, a1, rtol=1e-12, atol=1e-14)
+
+
+def test_kambe_lattice_matches_sample_log():
+    # routine VECTOR2D of the sample run prints the 2D cell of the bcc(110)
+    # slab (centered rectangular, i2dlat = 2): a2 = (a/2, beta a/2), the
+    # unit-cell area and the reciprocal cell the Kambe sums run over (10
+    # decimals in the log)
+    import kambe as K
+    a1, a2 = (np.array(v) for v in G["a_vectors"])
+    assert np.allclose(a2, [a1[0] / 2, G["beta"] * a1[0] / 2], atol=1e-9)
+    lat = K.Lattice2D(a1, a2)
+    assert abs(lat.area - G["area2d"]) < 1e-7
+    b1, b2 = (np.array(v) for v in G["b_vectors"])
+    assert np.allclose(lat.b1, b1, atol=1e-9) and np.allclose(lat.b2, b2, atol=1e-9)
