@@ -277,6 +277,30 @@ int skkr_gpu_phystau(int mode, int lmax, double *tau, const double *tinv,
 int skkr_gpu_phystau2(int mode, int lmax, double *tau, const double *tinv1, const double *alpha1,
                       const double *tinv2, const double *alpha2, int ld);
 
+/* Learned CPA warm start: a dense MLP with tanh hidden layers and a linear
+ * output layer, FP64 on the device (forward, backward and AdamW are this
+ * library's own kernels).  nlayer layers (1..8) of sizes dims[0..nlayer]
+ * (1..4096); params packs W_0 [dims0][dims1] (row-major), b_0 [dims1],
+ * W_1, b_1, ...; x [n][dims0], y [n][dims_last], row-major.  rows[r] = 1
+ * puts row r in the training loss, 0 holds it out (rows NULL: all rows
+ * train).  The loss is the mean squared error over the training rows and
+ * all outputs. */
+int skkr_gpu_mlp_forward(int nlayer, const int *dims, const double *params, int n, const double *x, double *y);
+/* loss and its gradient w.r.t. params (packed like params) */
+int skkr_gpu_mlp_grad(int nlayer, const int *dims, const double *params, int n, const double *x,
+                      const double *y, const unsigned char *rows, double *loss, double *grad);
+/* Full-batch AdamW (beta 0.9 / 0.999, eps 1e-8, decoupled weight decay) for
+ * `epochs` steps from params; train_loss[ep] is the training loss before
+ * step ep, params receives the final parameters.  With held-out rows and
+ * eval_every > 0 the held-out loss is evaluated after the steps ep with
+ * ep % eval_every == 0 and after the last one; best_params receives the
+ * parameters of the lowest held-out loss and best = {that loss, the training
+ * loss of its epoch}.  Without them best = {NaN, last training loss} and
+ * best_params the final parameters (either may be NULL). */
+int skkr_gpu_mlp_train(int nlayer, const int *dims, double *params, int n, const double *x, const double *y,
+                       const unsigned char *rows, int epochs, double lr, double weight_decay, int eval_every,
+                       double *train_loss, double *best, double *best_params);
+
 /* Layer DOS of nlay layers from their physical site-diagonal tau (replaces
  * the lambda = 0 moment of nrsp-scf/moment.f:47-110 with locquant.f:86-126,
  * and rsp-scf/moment.f:60-140 with locquant.f:197-232):

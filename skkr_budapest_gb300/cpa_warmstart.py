@@ -83,8 +83,11 @@ class Model:
         self.lmax = int(z["lmax"])
         self.cont = bool(z["cont"]) if "cont" in z else False
 
-    def predict(self, x: np.ndarray) -> np.ndarray:
+    def predict(self, x: np.ndarray, device: str = "cpu") -> np.ndarray:
         h = (np.atleast_2d(x) - self.xmean) / self.xstd
+        if device == "gpu":
+            from . import native as N
+            return N.mlp_forward(self.layers, h) * self.ystd + self.ymean
         for i, (w, b) in enumerate(self.layers):
             h = h @ w + b
             if i < len(self.layers) - 1:
@@ -175,19 +178,29 @@ def _dataset(data: str, cont: bool, itcpam: int = 50):
 
 
 def train(data: str, out: str, hidden: int = 64, epochs: int = 3000, seed: int = 0, val_frac: float = 0.1,
-          cont: bool = False, weight_decay: float = 1e-4):
+          cont: bool = False, weight_decay: float = 1e-4, device: str = "cpu"):
     """Full-batch AdamW on the mean squared error of the targets (one global
-    target scale), torch on the CPU; the last val_frac of the seeds is held
-    out and the epoch with the lowest held-out error is kept."""
-    import torch
+    target scale); the last val_frac of the seeds is held out and the epoch
+    with the lowest held-out error is kept.  device "gpu": this library's
+    forward, backward and AdamW kernels (skkr_gpu_mlp_train) from a seeded
+    uniform(-1/sqrt(fan_in), 1/sqrt(fan_in)) start; "cpu": torch."""
     x, y, sd, lmax = _dataset(data, cont)
     seeds = np.unique(sd)
     nval = max(1, int(len(seeds) * val_frac))
     val = np.isin(sd, seeds[-nval:])
     xm, xsd = x[~val].mean(0), x[~val].std(0) + 1e-12
     ym, ysd = np.zeros(y.shape[1]), np.full(y.shape[1], y[~val].std() + 1e-12)
-    torch.manual_seed(seed)
     dims = [x.shape[1], hidden, hidden, y.shape[1]]
+    if device == "gpu":
+        from . import native as N
+        rng = np.random.default_rng(seed)
+        init = [(rng.uniform(-1, 1, (a, b)) / np.sqrt(a), rng.uniform(-1, 1, b) / np.sqrt(a))
+                for a, b in zip(dims[:-1], dims[1:])]
+        _, wts, _, (vl, tl) = N.mlp_train(init, (x - xm) / xsd, (y - ym) / ysd, (~val).astype(np.uint8),
+                                          epochs, 2e-3, weight_decay, eval_every=20)
+        return _save_model(out, wts, xm, xsd, ym, ysd, lmax, cont, tl, vl, y, val)
+    import torch
+    torch.manual_seed(seed)
     lins = [torch.nn.Linear(a, b, dtype=torch.float64) for a, b in zip(dims[:-1], dims[1:])]
     params = [p for l in lins for p in l.parameters()]
     opt = torch.optim.AdamW(params, lr=2e-3, weight_decay=weight_decay)
@@ -214,12 +227,17 @@ def train(data: str, out: str, hidden: int = 64, epochs: int = 3000, seed: int =
             if vl < best[0]:
                 best = (vl, loss.item(), [(l.weight.detach().clone(), l.bias.detach().clone()) for l in lins])
     vl, tl, wts = best
-    save = {"nlayers": len(lins), "xmean": xm, "xstd": xsd, "ymean": ym, "ystd": ysd, "lmax": lmax,
+    wts = [(w.numpy().T.copy(), b.numpy().copy()) for w, b in wts]
+    return _save_model(out, wts, xm, xsd, ym, ysd, lmax, cont, tl, vl, y, val)
+
+
+def _save_model(out, wts, xm, xsd, ym, ysd, lmax, cont, tl, vl, y, val):
+    save = {"nlayers": len(wts), "xmean": xm, "xstd": xsd, "ymean": ym, "ystd": ysd, "lmax": lmax,
             "cont": int(cont), "train_mse": tl * ysd[0] ** 2, "val_mse": vl * ysd[0] ** 2,
             "val_mse_ata": float((y[val] ** 2).mean())}
     for i, (w, b) in enumerate(wts):
-        save["w%d" % i] = w.numpy().T.copy()
-        save["b%d" % i] = b.numpy().copy()
+        save["w%d" % i] = np.asarray(w, np.float64)
+        save["b%d" % i] = np.asarray(b, np.float64)
     os.makedirs(os.path.dirname(os.path.abspath(out)), exist_ok=True)
     np.savez(out, **save)
     return save["train_mse"], save["val_mse"], save["val_mse_ata"]
@@ -269,6 +287,7 @@ def main():
     t.add_argument("--out", default=DEFAULT_MODEL)
     t.add_argument("--epochs", type=int, default=3000)
     t.add_argument("--cont", action="store_true")
+    t.add_argument("--device", choices=("cpu", "gpu"), default="cpu")
     r = sub.add_parser("report")
     r.add_argument("--models", default=DEFAULT_MODEL)
     r.add_argument("--seeds", default="9001,9002,9003")
@@ -280,7 +299,7 @@ def main():
         print("samples:", n)
     elif a.cmd == "train":
         print("mse train / held out / held out of the ATA start: %.3e / %.3e / %.3e" % train(
-            a.data, a.out, epochs=a.epochs, cont=a.cont))
+            a.data, a.out, epochs=a.epochs, cont=a.cont, device=a.device))
     else:
         paths = a.models.split(",")
         rows = report(paths, [int(s) for s in a.seeds.split(",")], [int(e) for e in a.energies.split(",")],

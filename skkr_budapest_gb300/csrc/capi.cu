@@ -2102,3 +2102,184 @@ extern "C" int skkr_gpu_zinv_batch(int precision, int n, int batch, double *a, i
   CK(cudaGetLastError());
   return download_mats(a, A, batch, n, ld);
 }
+
+// ---- learned CPA warm start: the MLP on the device ----------------------
+namespace {
+constexpr int MLP_MAX_LAYERS = 8, MLP_MAX_DIM = 4096;
+
+struct MlpRun {
+  int nl = 0, n = 0, dmax = 0;
+  std::vector<int> d;
+  std::vector<long long> off;  // W_i at off[i], b_i at off[i] + d[i] d[i+1]
+  long long np = 0;
+  Scoped s;
+  double *P = nullptr, *X = nullptr, *Y = nullptr, *buf0 = nullptr, *buf1 = nullptr, *rows = nullptr;
+  double *scal = nullptr;  // [0] train loss, [1] held-out loss
+  std::vector<double *> A;  // A[0] = X, A[i+1] = output of layer i
+  unsigned char *sel = nullptr;
+};
+
+int mlp_sizes(int nlayer, const int *dims, int n, MlpRun &m) {
+  if (nlayer < 1 || nlayer > MLP_MAX_LAYERS || !dims || n < 1) return SKKR_ERR_ARG;
+  m.nl = nlayer;
+  m.n = n;
+  m.d.assign(dims, dims + nlayer + 1);
+  m.off.resize(nlayer);
+  m.np = 0;
+  m.dmax = 0;
+  for (int i = 0; i <= nlayer; i++) {
+    if (m.d[i] < 1 || m.d[i] > MLP_MAX_DIM) return SKKR_ERR_ARG;
+    m.dmax = std::max(m.dmax, m.d[i]);
+  }
+  for (int i = 0; i < nlayer; i++) {
+    m.off[i] = m.np;
+    m.np += (long long)m.d[i] * m.d[i + 1] + m.d[i + 1];
+  }
+  long long act = 0;
+  for (int i = 0; i <= nlayer; i++) act += (long long)n * m.d[i];
+  if ((act + 2LL * n * m.dmax) * 8 > (16LL << 30)) return SKKR_ERR_ARG;  // activations within 16 GB
+  return SKKR_OK;
+}
+
+// device buffers; x [n][d0], y [n][d_last] (may be null), rows [n] (may be null)
+int mlp_alloc(MlpRun &m, const double *params, const double *x, const double *y, const unsigned char *rows) {
+  const int n = m.n;
+  CKR(m.s.alloc(&m.P, m.np));
+  m.A.assign(m.nl + 1, nullptr);
+  for (int i = 0; i <= m.nl; i++) CKR(m.s.alloc(&m.A[i], (size_t)n * m.d[i]));
+  m.X = m.A[0];
+  CKR(m.s.alloc(&m.buf0, (size_t)n * m.dmax));
+  CKR(m.s.alloc(&m.buf1, (size_t)n * m.dmax));
+  CKR(m.s.alloc(&m.rows, n));
+  CKR(m.s.alloc(&m.scal, 2));
+  CK(cudaMemcpy(m.P, params, m.np * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(m.X, x, (size_t)n * m.d[0] * sizeof(double), cudaMemcpyHostToDevice));
+  if (y) {
+    CKR(m.s.alloc(&m.Y, (size_t)n * m.d[m.nl]));
+    CK(cudaMemcpy(m.Y, y, (size_t)n * m.d[m.nl] * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  if (rows) {
+    CKR(m.s.alloc(&m.sel, n));
+    CK(cudaMemcpy(m.sel, rows, n, cudaMemcpyHostToDevice));
+  }
+  return SKKR_OK;
+}
+
+void mlp_forward(MlpRun &m, cudaStream_t st) {
+  for (int i = 0; i < m.nl; i++)
+    mlp_launch_dense(m.A[i], m.n, m.d[i], m.P + m.off[i], m.P + m.off[i] + (long long)m.d[i] * m.d[i + 1],
+                     m.d[i + 1], i < m.nl - 1, m.A[i + 1], st);
+}
+
+// gradient of the loss whose output gradient the loss kernel left in buf0
+void mlp_backward(MlpRun &m, double *G, cudaStream_t st) {
+  double *cur = m.buf0, *nxt = m.buf1;
+  for (int i = m.nl - 1; i >= 0; i--) {
+    if (i < m.nl - 1) mlp_launch_tanh_back(m.A[i + 1], cur, (long long)m.n * m.d[i + 1], st);
+    mlp_launch_wgrad(m.A[i], cur, m.n, m.d[i], m.d[i + 1], G + m.off[i], st);
+    if (i > 0) {
+      mlp_launch_hgrad(cur, m.P + m.off[i], m.n, m.d[i], m.d[i + 1], nxt, st);
+      std::swap(cur, nxt);
+    }
+  }
+}
+
+int mlp_count(const unsigned char *rows, int n, int want) {
+  if (!rows) return want ? n : 0;
+  int c = 0;
+  for (int r = 0; r < n; r++) c += rows[r] == want;
+  return c;
+}
+}  // namespace
+
+extern "C" int skkr_gpu_mlp_forward(int nlayer, const int *dims, const double *params, int n, const double *x,
+                                    double *y) {
+  if (!params || !x || !y) return SKKR_ERR_ARG;
+  MlpRun m;
+  CKR(mlp_sizes(nlayer, dims, n, m));
+  CKR(mlp_alloc(m, params, x, nullptr, nullptr));
+  mlp_forward(m, 0);
+  CK(cudaDeviceSynchronize());
+  CK(cudaGetLastError());
+  CK(cudaMemcpy(y, m.A[m.nl], (size_t)n * m.d[m.nl] * sizeof(double), cudaMemcpyDeviceToHost));
+  return SKKR_OK;
+}
+
+extern "C" int skkr_gpu_mlp_grad(int nlayer, const int *dims, const double *params, int n, const double *x,
+                                 const double *y, const unsigned char *rows, double *loss, double *grad) {
+  if (!params || !x || !y || !loss || !grad) return SKKR_ERR_ARG;
+  MlpRun m;
+  CKR(mlp_sizes(nlayer, dims, n, m));
+  const int nsel = mlp_count(rows, n, 1);
+  if (nsel < 1) return SKKR_ERR_ARG;
+  CKR(mlp_alloc(m, params, x, y, rows));
+  double *G;
+  CKR(m.s.alloc(&G, m.np));
+  const int dout = m.d[m.nl];
+  mlp_forward(m, 0);
+  mlp_launch_loss(m.A[m.nl], m.Y, m.sel, 1, n, dout, 1.0 / ((double)nsel * dout), m.buf0, m.rows, m.scal, 0);
+  mlp_backward(m, G, 0);
+  CK(cudaDeviceSynchronize());
+  CK(cudaGetLastError());
+  CK(cudaMemcpy(loss, m.scal, sizeof(double), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(grad, G, m.np * sizeof(double), cudaMemcpyDeviceToHost));
+  return SKKR_OK;
+}
+
+extern "C" int skkr_gpu_mlp_train(int nlayer, const int *dims, double *params, int n, const double *x,
+                                  const double *y, const unsigned char *rows, int epochs, double lr,
+                                  double weight_decay, int eval_every, double *train_loss, double *best,
+                                  double *best_params) {
+  if (!params || !x || !y || !train_loss || epochs < 1 || !(lr > 0.0) || weight_decay < 0.0) return SKKR_ERR_ARG;
+  MlpRun m;
+  CKR(mlp_sizes(nlayer, dims, n, m));
+  const int ntr = mlp_count(rows, n, 1), nval = mlp_count(rows, n, 0);
+  if (ntr < 1) return SKKR_ERR_ARG;
+  const bool eval = eval_every > 0 && nval > 0 && best && best_params;
+  CKR(mlp_alloc(m, params, x, y, rows));
+  double *G, *Mo, *Vo, *losses, *bestd = nullptr, *Pbest = nullptr;
+  CKR(m.s.alloc(&G, m.np));
+  CKR(m.s.alloc(&Mo, m.np));
+  CKR(m.s.alloc(&Vo, m.np));
+  CKR(m.s.alloc(&losses, epochs));
+  CK(cudaMemset(Mo, 0, m.np * sizeof(double)));
+  CK(cudaMemset(Vo, 0, m.np * sizeof(double)));
+  if (eval) {
+    CKR(m.s.alloc(&bestd, 2));
+    CKR(m.s.alloc(&Pbest, m.np));
+    const double init[2] = {HUGE_VAL, HUGE_VAL};
+    CK(cudaMemcpy(bestd, init, sizeof(init), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(Pbest, m.P, m.np * sizeof(double), cudaMemcpyDeviceToDevice));
+  }
+  const int dout = m.d[m.nl];
+  const double b1 = 0.9, b2 = 0.999, eps = 1e-8;  // the AdamW defaults the host training uses
+  for (int ep = 0; ep < epochs; ep++) {
+    mlp_forward(m, 0);
+    mlp_launch_loss(m.A[m.nl], m.Y, m.sel, 1, n, dout, 1.0 / ((double)ntr * dout), m.buf0, m.rows, losses + ep, 0);
+    mlp_backward(m, G, 0);
+    const double t = ep + 1.0;
+    const double bc1 = 1.0 - std::pow(b1, t), bc2 = 1.0 - std::pow(b2, t);
+    mlp_launch_adamw(m.P, G, Mo, Vo, m.np, lr, weight_decay, b1, b2, eps, lr / bc1, std::sqrt(bc2), 0);
+    if (eval && (ep % eval_every == 0 || ep == epochs - 1)) {
+      mlp_forward(m, 0);
+      mlp_launch_loss(m.A[m.nl], m.Y, m.sel, 0, n, dout, 1.0 / ((double)nval * dout), nullptr, m.rows,
+                      m.scal + 1, 0);
+      mlp_launch_keep_best(m.scal + 1, losses + ep, bestd, m.P, Pbest, m.np, 0);
+    }
+  }
+  CK(cudaDeviceSynchronize());
+  CK(cudaGetLastError());
+  CK(cudaMemcpy(train_loss, losses, epochs * sizeof(double), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(params, m.P, m.np * sizeof(double), cudaMemcpyDeviceToHost));
+  if (eval) {
+    CK(cudaMemcpy(best, bestd, 2 * sizeof(double), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(best_params, Pbest, m.np * sizeof(double), cudaMemcpyDeviceToHost));
+  } else {
+    if (best) {
+      best[0] = NAN;
+      best[1] = train_loss[epochs - 1];
+    }
+    if (best_params) std::memcpy(best_params, params, m.np * sizeof(double));
+  }
+  return SKKR_OK;
+}

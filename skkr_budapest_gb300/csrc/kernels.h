@@ -99,3 +99,19 @@ int mixed_zinv(MixedWork *w, const MatRef &A, const MatRef &X, int n, int nk, in
 // stream synchronisation
 int mixed_resid_reset(MixedWork *w, cudaStream_t st);
 int mixed_resid_read(MixedWork *w, double *out, long long *fallbacks, long long *refined, cudaStream_t st);
+
+// dense tanh MLP of the learned CPA warm start (kernels_mlp.cu), FP64,
+// row-major H[n][d], W[din][dout]
+void mlp_launch_dense(const double *H, int n, int din, const double *W, const double *b, int dout, int act,
+                      double *A, cudaStream_t st);
+// rowsum, dY (may be null) and out[0] = scale * sum of squared errors over
+// the rows with sel[r] == want (sel null: all rows); dY = scale * 2 (Yh - Y)
+void mlp_launch_loss(const double *Yh, const double *Y, const unsigned char *sel, int want, int n, int dout,
+                     double scale, double *dY, double *rowsum, double *out, cudaStream_t st);
+void mlp_launch_tanh_back(const double *A, double *G, long long m, cudaStream_t st);
+void mlp_launch_wgrad(const double *H, const double *dZ, int n, int din, int dout, double *g, cudaStream_t st);
+void mlp_launch_hgrad(const double *dZ, const double *W, int n, int din, int dout, double *dH, cudaStream_t st);
+void mlp_launch_adamw(double *p, const double *g, double *m, double *v, long long np, double lr, double wd,
+                      double b1, double b2, double eps, double step_size, double bc2_sqrt, cudaStream_t st);
+void mlp_launch_keep_best(const double *val, const double *train, double *best, const double *p, double *pbest,
+                          long long np, cudaStream_t st);

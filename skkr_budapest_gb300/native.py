@@ -71,6 +71,9 @@ def lib():
                                             I, P]
         L.skkr_gpu_phystau.argtypes = [I, I, P, P, P, I]
         L.skkr_gpu_phystau2.argtypes = [I, I, P, P, P, P, P, I]
+        L.skkr_gpu_mlp_forward.argtypes = [I, P, P, I, P, P]
+        L.skkr_gpu_mlp_grad.argtypes = [I, P, P, I, P, P, P, P, P]
+        L.skkr_gpu_mlp_train.argtypes = [I, P, P, I, P, P, P, I, D, D, I, P, P, P]
         L.skkr_gpu_layer_dos.argtypes = [I, I, I, P, I, P, P, I, P, P]
         L.skkr_gpu_set_reduce.argtypes = [P, P, P]
         L.skkr_gpu_set_mixed_policy.argtypes = [P, D, D, I, D]
@@ -182,6 +185,67 @@ def phystau2(tau, tinv1, alpha1, tinv2, alpha2, lmax, irel):
     _check(lib().skkr_gpu_phystau2(irel, lmax, _p(t), _p(t1), _p(a1), _p(t2), _p(a2), t.shape[-1]),
            "skkr_gpu_phystau2")
     return uncm(t)
+
+
+def _mlp_args(layers):
+    """dims (int32) and packed params (W_0, b_0, W_1, ...) of [(W, b), ...]."""
+    dims = [layers[0][0].shape[0]] + [w.shape[1] for w, _ in layers]
+    for (w, b), din, dout in zip(layers, dims[:-1], dims[1:]):
+        if w.shape != (din, dout) or b.shape != (dout,):
+            raise ValueError("layer shapes do not chain")
+    params = np.concatenate([np.concatenate([np.ascontiguousarray(w, np.float64).ravel(),
+                                             np.ascontiguousarray(b, np.float64)]) for w, b in layers])
+    return np.array(dims, np.int32), params
+
+
+def _mlp_unpack(dims, params):
+    out, o = [], 0
+    for din, dout in zip(dims[:-1], dims[1:]):
+        w = params[o:o + din * dout].reshape(din, dout).copy()
+        o += din * dout
+        out.append((w, params[o:o + dout].copy()))
+        o += dout
+    return out
+
+
+def mlp_forward(layers, x):
+    """Device forward of the warm-start MLP (skkr_gpu_mlp_forward)."""
+    dims, params = _mlp_args(layers)
+    x = np.ascontiguousarray(x, np.float64)
+    y = np.zeros((len(x), dims[-1]))
+    _check(lib().skkr_gpu_mlp_forward(len(layers), _p(dims), _p(params), len(x), _p(x), _p(y)),
+           "skkr_gpu_mlp_forward")
+    return y
+
+
+def mlp_grad(layers, x, y, rows=None):
+    """Device loss and gradient [(dW, db), ...] (skkr_gpu_mlp_grad)."""
+    dims, params = _mlp_args(layers)
+    x = np.ascontiguousarray(x, np.float64)
+    y = np.ascontiguousarray(y, np.float64)
+    r = None if rows is None else np.ascontiguousarray(rows, np.uint8)
+    loss = np.zeros(1)
+    grad = np.zeros_like(params)
+    _check(lib().skkr_gpu_mlp_grad(len(layers), _p(dims), _p(params), len(x), _p(x), _p(y),
+                                   None if r is None else _p(r), _p(loss), _p(grad)), "skkr_gpu_mlp_grad")
+    return float(loss[0]), _mlp_unpack(dims, grad)
+
+
+def mlp_train(layers, x, y, rows, epochs, lr, weight_decay, eval_every=20):
+    """Device full-batch AdamW training (skkr_gpu_mlp_train).  Returns
+    (final layers, best layers, per-epoch training loss, (best held-out
+    loss, training loss of that epoch))."""
+    dims, params = _mlp_args(layers)
+    x = np.ascontiguousarray(x, np.float64)
+    y = np.ascontiguousarray(y, np.float64)
+    r = None if rows is None else np.ascontiguousarray(rows, np.uint8)
+    tl = np.zeros(int(epochs))
+    best = np.zeros(2)
+    bp = np.zeros_like(params)
+    _check(lib().skkr_gpu_mlp_train(len(layers), _p(dims), _p(params), len(x), _p(x), _p(y),
+                                    None if r is None else _p(r), int(epochs), float(lr), float(weight_decay),
+                                    int(eval_every), _p(tl), _p(best), _p(bp)), "skkr_gpu_mlp_train")
+    return _mlp_unpack(dims, params), _mlp_unpack(dims, bp), tl, (float(best[0]), float(best[1]))
 
 
 REDUCE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.POINTER(C.c_double), C.c_longlong)

@@ -39,3 +39,19 @@ def test_ata_has_zero_target():
     groups = CW.kappa_groups(ep.lmax)
     li = [l for l in range(ep.nintfc) if 1e-6 < ep.conc[l] < 1 - 1e-6][0]
     assert np.abs(CW.layer_target(ep, li, ep.tminv[li], groups)).max() < 1e-12
+
+
+def test_host_training_writes_a_model(tmp_path):
+    pytest.importorskip("torch")
+    rng = np.random.default_rng(7)
+    n = 240
+    x = rng.normal(size=(n, 11))
+    y = 0.3 * np.tanh(x[:, :6] @ rng.normal(size=(6, 6)))
+    meta = np.c_[np.repeat(np.arange(12), n // 12), np.zeros(n), np.zeros(n), np.ones(n)]
+    data = tmp_path / "d.npz"
+    np.savez(data, x=x, y=y, meta=meta, lmax=1)
+    out = tmp_path / "m.npz"
+    tr, vl, ata = CW.train(str(data), str(out), hidden=16, epochs=200)
+    assert np.isfinite(tr) and vl < ata
+    model = CW.Model(str(out))
+    assert model.predict(x[:3]).shape == (3, 6)

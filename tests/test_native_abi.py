@@ -109,3 +109,31 @@ def test_size_limits_at_creation():
     assert create(ngeff=9) == ARG
     assert create(nprc=0, ninprc=[4, 4]) == ARG
     assert create(nprc=17, ninprc=[4] * 18) == ARG
+
+
+def test_mlp_argument_checks_before_any_device_call():
+    import numpy as np
+    import __graft_entry__
+    __graft_entry__.build()
+    lib = ctypes.CDLL(native.LIB_PATH)
+    P, I, D = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+    ARG = -1
+    lib.skkr_gpu_mlp_forward.argtypes = [I, P, P, I, P, P]
+    lib.skkr_gpu_mlp_grad.argtypes = [I, P, P, I, P, P, P, P, P]
+    lib.skkr_gpu_mlp_train.argtypes = [I, P, P, I, P, P, P, I, D, D, I, P, P, P]
+    dims = np.array([3, 4, 2], np.int32)
+    bad = np.array([3, 0, 2], np.int32)
+    big = np.array([3, 5000, 2], np.int32)
+    buf = np.zeros(64)
+    d, b, g = dims.ctypes.data, buf.ctypes.data, bad.ctypes.data
+    assert lib.skkr_gpu_mlp_forward(0, d, b, 4, b, b) == ARG          # no layer
+    assert lib.skkr_gpu_mlp_forward(9, d, b, 4, b, b) == ARG          # more than 8
+    assert lib.skkr_gpu_mlp_forward(2, g, b, 4, b, b) == ARG          # a zero width
+    assert lib.skkr_gpu_mlp_forward(2, big.ctypes.data, b, 4, b, b) == ARG
+    assert lib.skkr_gpu_mlp_forward(2, d, b, 0, b, b) == ARG          # no row
+    assert lib.skkr_gpu_mlp_forward(2, d, None, 4, b, b) == ARG
+    held = np.zeros(4, np.uint8)                                      # every row held out
+    assert lib.skkr_gpu_mlp_grad(2, d, b, 4, b, b, held.ctypes.data, b, b) == ARG
+    assert lib.skkr_gpu_mlp_train(2, d, b, 4, b, b, None, 0, 1e-3, 0.0, 20, b, b, b) == ARG   # no epoch
+    assert lib.skkr_gpu_mlp_train(2, d, b, 4, b, b, None, 5, 0.0, 0.0, 20, b, b, b) == ARG   # lr 0
+    assert lib.skkr_gpu_mlp_train(2, d, b, 4, b, b, None, 5, 1e-3, -1.0, 20, b, b, b) == ARG  # wd < 0
