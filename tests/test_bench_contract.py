@@ -35,3 +35,12 @@ def test_reference_arm_line():
         assert key in line, key
     assert line["value"] > 0 and line["e2e"]["value"] == line["value"]
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["cpu_baseline"]["kind"] == "port"
+
+
+def test_reference_arm_of_the_off_diagonal_tau():
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--workload", "tauij",
+                        "--steps", "1", "--warmup", "1"], capture_output=True, text=True, cwd=ROOT, timeout=900)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["metric"].startswith("(E,k) points/s of the off-diagonal")
+    assert line["value"] > 0 and line["cpu_baseline"]["kind"] == "port" and "192 pairs" in line["config"]["workload"]
