@@ -419,16 +419,63 @@ def run_ours(args, rank, ws):
         print(json.dumps(line), flush=True)
 
 
+C3_METRIC = "(E,k) points/s of three interface systems in one call"
+C3_WORKLOAD = "c3: rel_bcc lmax3 PL4 + nonrel fcc lmax2 PL2 + rel bcc lmax2 PL3"
+
+
+def _c3_setup():
+    from skkr_budapest_gb300 import workloads as W
+    specs = [W.rel_bcc(), W.nonrel_pl2(), W.rel_pl3_l2()]
+    plan = [[12, 16, 4, 14, 8], [12, 14, 6, 10, 3], [14, 17, 8, 12, 4]]
+    return plan, [[W.energy_problem(sp, ie) for ie in pl] for sp, pl in zip(specs, plan)]
+
+
+def run_c3_reference(args):
+    """Reference arm of the three-system workload: the oracle's CPA and k loop
+    of every system on all host threads, a bounded sample of k points per
+    energy and system."""
+    nth = os.cpu_count() or 1
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    plan, eps = _c3_setup()
+    per_step = nth
+
+    def step(i):
+        pts = 0
+        for e in eps:
+            ep = e[i % len(e)]
+            sub = ep.with_k(ep.xk[:per_step], ep.wk[:per_step] / ep.wk[:per_step].sum())
+            if O.cpacoord(sub, nthreads=nth)["status"] != 0:
+                raise RuntimeError("oracle failed")
+            pts += len(sub.xk)
+        return pts
+
+    for i in range(args.warmup):
+        step(i)
+    t0 = time.perf_counter()
+    pts = sum(step(i) for i in range(args.warmup, args.warmup + args.steps))
+    dt = time.perf_counter() - t0
+    v = pts / dt
+    print(json.dumps({"impl": "reference", "metric": C3_METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+                      "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+                      "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+                      "data": "synthetic (seeded)",
+                      "config": {"workload": C3_WORKLOAD, "energies": plan,
+                                 "step": "%d k points of one energy of each system (CPU)" % per_step},
+                      "cpu_baseline": {"value": v, "unit": UNIT, "cores": nth, "kind": "port",
+                                       "sample": "%d k points per system and step, %d steps" % (per_step,
+                                                                                              args.steps)},
+                      "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}),
+          flush=True)
+
+
 def run_c3(args):
     """Three interfaces in one call per step (relativistic PL4 lmax=3,
     non-relativistic PL2 lmax=2, relativistic PL3 lmax=2), host buffers in and
     out, against the same calls made one after the other."""
     import torch
     from skkr_budapest_gb300 import api
-    from skkr_budapest_gb300 import workloads as W
-    specs = [W.rel_bcc(), W.nonrel_pl2(), W.rel_pl3_l2()]
-    plan = [[12, 16, 4, 14, 8], [12, 14, 6, 10, 3], [14, 17, 8, 12, 4]]
-    eps = [[W.energy_problem(sp, ie) for ie in pl] for sp, pl in zip(specs, plan)]
+    plan, eps = _c3_setup()
     ctxs = [api.Context.for_problem(e[0], args.precision) for e in eps]
     nsteps = args.warmup + args.steps
 
@@ -454,12 +501,12 @@ def run_c3(args):
         c.close()
     v = out[True][0] / out[True][1]
     seq = out[False][0] / out[False][1]
-    print(json.dumps({"metric": "(E,k) points/s of three interface systems in one call", "value": v,
+    print(json.dumps({"metric": C3_METRIC, "value": v,
                       "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
                       "ms_per_step": 1e3 * out[True][1] / args.steps, "higher_is_better": True,
                       "dtype": "c128 via BF16x6 slices" if args.precision == "mixed" else "c128",
                       "data": "synthetic", "sequential_value": seq, "concurrency_gain": v / seq,
-                      "config": {"workload": "c3: rel_bcc lmax3 PL4 + nonrel fcc lmax2 PL2 + rel bcc lmax2 PL3",
+                      "config": {"workload": C3_WORKLOAD,
                                  "precision": args.precision, "energies": plan,
                                  "timing": "host wall clock around whole calls (host buffers)"}}), flush=True)
 
@@ -565,7 +612,10 @@ def run_tauij(args):
 def main():
     args = parse()
     if args.workload == "c3":
-        run_c3(args)
+        if args.impl == "reference":
+            run_c3_reference(args)
+        else:
+            run_c3(args)
         return
     if args.workload == "tauij":
         if args.impl == "reference":

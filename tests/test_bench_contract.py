@@ -44,3 +44,12 @@ def test_reference_arm_of_the_off_diagonal_tau():
     line = json.loads(r.stdout.strip().splitlines()[-1])
     assert line["impl"] == "reference" and line["metric"].startswith("(E,k) points/s of the off-diagonal")
     assert line["value"] > 0 and line["cpu_baseline"]["kind"] == "port" and "192 pairs" in line["config"]["workload"]
+
+
+def test_reference_arm_of_the_three_systems():
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--workload", "c3",
+                        "--steps", "1", "--warmup", "1"], capture_output=True, text=True, cwd=ROOT, timeout=900)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["metric"].startswith("(E,k) points/s of three interface")
+    assert line["value"] > 0 and line["config"]["workload"].startswith("c3:")
