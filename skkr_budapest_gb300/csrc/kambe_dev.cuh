@@ -1,0 +1,270 @@
+// Kambe's Ewald split of the 2D lattice sums of outgoing spherical waves,
+// for host and device code: D_L(k, s), L = (l, m) up to l = lmax2, for one
+// k point and one layer-pair separation s, in the form the reference
+// evaluates per k (main/kamstr.f:72-355):
+//   reciprocal part over g (incgamma.f, delkam.f; formula 35 for s_z != 0,
+//   formula 50 for s = 0), real-space part over R (ilkam.f, complex Y_lm of
+//   ylmc.f; formula 47), and the s = 0 correction (formula 55);
+// in-plane pairs (s != 0, s_z = 0) are moved to s_z = 1.1e-4 as kamstr.f
+// does.  The caller passes superset lists of g and R; terms with
+// |g + k| > gcut or an in-plane |R + s| > rcut are skipped, so the same lists
+// serve every k point and separation.  Index of (l, m): l(l+1) + m.
+#pragma once
+#include "faddeeva.cuh"
+
+#define SKKR_KAMBE_L2 6   // lmax2 = 2 lmax, lmax <= 3
+
+SKKR_HD inline fcplx fscal(double s, fcplx a) { return fc(s * a.re, s * a.im); }
+SKKR_HD inline fcplx fneg(fcplx a) { return fc(-a.re, -a.im); }
+SKKR_HD inline fcplx fconj(fcplx a) { return fc(a.re, -a.im); }
+// principal square root
+SKKR_HD inline fcplx fsqrtc(fcplx z) {
+  const double r = hypot(z.re, z.im);
+  if (r == 0.0) return fc(0.0, 0.0);
+  if (z.re >= 0.0) {
+    const double t = sqrt(0.5 * (r + z.re));
+    return fc(t, z.im / (2.0 * t));
+  }
+  const double t = sqrt(0.5 * (r - z.re));
+  return fc(fabs(z.im) / (2.0 * t), copysign(t, z.im));
+}
+// z^n, n of either sign
+SKKR_HD inline fcplx fpowi(fcplx z, int n) {
+  fcplx r = fc(1.0, 0.0);
+  for (int i = 0; i < (n < 0 ? -n : n); i++) r = fmulc(r, z);
+  return n < 0 ? fdivc(fc(1.0, 0.0), r) : r;
+}
+SKKR_HD inline fcplx fipow(int n) {  // i^n
+  const int q = ((n % 4) + 4) % 4;
+  return q == 0 ? fc(1, 0) : q == 1 ? fc(0, 1) : q == 2 ? fc(-1, 0) : fc(0, -1);
+}
+
+// Gamma(1/2 - i, z), i = 0..n (incgamma.f)
+SKKR_HD inline void kambe_incgamma(int n, fcplx z, fcplx *gam) {
+  const fcplx ex = fexpc(fneg(z));
+  const fcplx sz = fsqrtc(z);
+  const fcplx a = fc(-sz.im, sz.re);  // i sqrt(z)
+  fcplx s = fscal(1.7724538509055160273, fmulc(ex, faddeeva(a)));
+  gam[0] = s;
+  double b = -0.5;
+  fcplx zb = sz;
+  for (int i = 1; i <= n; i++) {
+    zb = fdivc(zb, z);
+    s = fscal(1.0 / b, fsub(s, fmulc(zb, ex)));
+    gam[i] = s;
+    b -= 1.0;
+  }
+}
+
+// real-space integrals delta(0..l) at distance t (ilkam.f)
+SKKR_HD inline void kambe_ilkam(int l, fcplx alpha, double t, fcplx kappa, fcplx *delta) {
+  const fcplx z = fscal(t, kappa);
+  const fcplx sx = fsqrtc(alpha);
+  fcplx b = fdivc(fc(2.0, 0.0), z);
+  const double dc = 0.88622692545275801365;  // sqrt(pi) / 2
+  const fcplx a = fdivc(fscal(0.5, z), sx);
+  const fcplx ex = fexpc(fsub(alpha, fmulc(a, a)));
+  const fcplx ia = fc(-a.im, a.re);
+  const fcplx wp = faddeeva(fadd(sx, ia)), wm = faddeeva(fsub(ia, sx));
+  const fcplx c = fscal(dc, ex);
+  fcplx dl = fmulc(fmulc(fadd(wp, wm), c), b);
+  const fcplx dd = fmulc(fsub(wp, wm), c);
+  fcplx delm1 = fc(dd.im, -dd.re);  // / i
+  delta[0] = dl;
+  b = fmulc(b, b);
+  fcplx cx = sx;
+  double d = 0.5;
+  for (int i = 1; i <= l; i++) {
+    cx = fdivc(cx, alpha);
+    const fcplx del2 = fmulc(fadd(fsub(fscal(d, dl), delm1), fmulc(cx, ex)), b);
+    delta[i] = del2;
+    delm1 = dl;
+    dl = del2;
+    d += 1.0;
+  }
+}
+
+// delta(0..n) of the out-of-plane reciprocal term (delkam.f), n >= 1
+SKKR_HD inline void kambe_delkam(int n, fcplx x, fcplx zz, fcplx *delta) {
+  const fcplx z = fsqrtc(zz);
+  const fcplx sx = fsqrtc(x);
+  const double dc = 0.88622692545275801365;
+  fcplx b = fdivc(fc(2.0, 0.0), z);
+  const fcplx a = fdivc(fscal(0.5, z), sx);
+  const fcplx ex = fexpc(fsub(fmulc(a, a), x));
+  const fcplx isx = fc(-sx.im, sx.re);
+  const fcplx wm = faddeeva(fsub(isx, a)), wp = faddeeva(fadd(a, isx));
+  const fcplx c = fscal(dc, ex);
+  delta[0] = fmulc(fadd(wm, wp), c);
+  const fcplx t = fmulc(fmulc(fsub(wm, wp), c), b);
+  delta[1] = fc(-t.im, t.re);  // * i
+  fcplx fcx = sx;
+  b = fmulc(b, b);
+  double d = 0.5;
+  for (int i = 0; i < n - 1; i++) {
+    fcx = fdivc(fcx, x);
+    delta[i + 2] = fmulc(b, fadd(fsub(fneg(fscal(d, delta[i + 1])), delta[i]), fmulc(ex, fcx)));
+    d += 1.0;
+  }
+}
+
+SKKR_HD inline double kambe_fac(int n) {
+  double f = 1.0;
+  for (int i = 2; i <= n; i++) f *= (double)i;
+  return f;
+}
+
+// complex Y_lm(v), Condon-Shortley phase, l <= lmax2 (ylmc.f: the power
+// series of d^m P_l / dx^m from the recursion of the Legendre coefficients)
+SKKR_HD inline void kambe_ylm(double x, double y, double z, int lmax2, fcplx *out) {
+  double a[SKKR_KAMBE_L2 + 1][SKKR_KAMBE_L2 + 1];
+  for (int l = 0; l <= SKKR_KAMBE_L2; l++)
+    for (int n = 0; n <= SKKR_KAMBE_L2; n++) a[l][n] = 0.0;
+  a[0][0] = 1.0;
+  if (SKKR_KAMBE_L2 >= 1) a[1][1] = 1.0;
+  if (SKKR_KAMBE_L2 >= 2) {
+    a[2][0] = -0.5;
+    a[2][2] = 1.5;
+  }
+  for (int l = 3; l <= lmax2; l++) {
+    const double fa1 = (2.0 * l - 1.0) / l, fa2 = -(l - 1.0) / l;
+    a[l][0] = fa2 * a[l - 2][0];
+    for (int n = 1; n < l - 1; n++) a[l][n] = fa1 * a[l - 1][n - 1] + fa2 * a[l - 2][n];
+    a[l][l - 1] = fa1 * a[l - 1][l - 2];
+    a[l][l] = fa1 * a[l - 1][l - 1];
+  }
+  const double r = sqrt(x * x + y * y + z * z);
+  double cth = 0.0;
+  fcplx ephi = fc(1.0, 0.0);
+  if (r >= 1e-16) {
+    cth = z / r;
+    const double d = sqrt(x * x + y * y);
+    if (d >= 1e-6) ephi = fc(x / d, y / d);
+  }
+  const double px = sqrt(fmax(1.0 - cth * cth, 0.0)) + 1e-30;
+  for (int l = 0; l <= lmax2; l++)
+    for (int m = -l; m <= l; m++) {
+      const int mb = m < 0 ? -m : m;
+      // t = sum_k a(l, k + mb) (k + mb)! / k! cth^k
+      double t = 0.0, p = 1.0;
+      for (int k = 0; k <= l - mb; k++) {
+        t += a[l][k + mb] * (kambe_fac(k + mb) / kambe_fac(k)) * p;
+        p *= cth;
+      }
+      const double nrm = sqrt((2.0 * l + 1.0) * kambe_fac(l - mb) / (12.566370614359172954 * kambe_fac(l + mb)));
+      const fcplx cf = fscal(nrm, fipow(m + mb));
+      out[l * (l + 1) + m] = fmulc(fscal(pow(px, mb) * t, cf), fpowi(ephi, m));
+    }
+}
+
+// D_L(k, s) into out[(lmax2+1)^2] (kamstr.f dlm1 + dlm2)
+SKKR_HD inline void kambe_dlm(fcplx e, double kx, double ky, double sx, double sy, double sz, int lmax2,
+                              const double *gvec, int ng, const double *rvec, int nr, double area,
+                              double factor, double gcut, double rcut, fcplx *out) {
+  const int lmmx = (lmax2 + 1) * (lmax2 + 1);
+  const fcplx kappa = fsqrtc(e);
+  const fcplx cs1 = fdivc(fc(-1.0 / area, 0.0), kappa);
+  const fcplx cs2 = fscal(-0.28209479177387814347, kappa);  // -kappa / (2 sqrt(pi))
+  const fcplx alpha = fscal(factor * area / 12.566370614359172954, e);
+  const fcplx w = fdivc(fscal(2.0, alpha), e);
+  double flm[(SKKR_KAMBE_L2 + 1) * (SKKR_KAMBE_L2 + 1)];
+  for (int l = 0; l <= lmax2; l++)
+    for (int m = 0; m <= l; m++) {
+      const double v = pow(2.0, -l) * sqrt((2.0 * l + 1.0) * kambe_fac(l + m) * kambe_fac(l - m));
+      flm[l * (l + 1) + m] = v;
+      flm[l * (l + 1) - m] = v;
+    }
+  for (int i = 0; i < lmmx; i++) out[i] = fc(0.0, 0.0);
+  double s = sqrt(sx * sx + sy * sy + sz * sz);
+  const double ctol = 1e-4;
+  if (s < ctol) {
+    // formula 55: d003 = -kappa (e^alpha c - i) / (2 sqrt(pi)),
+    // c = i (e^-alpha - w(sqrt alpha)) - 1 / (sqrt(pi) sqrt(alpha))
+    const fcplx a = fsqrtc(alpha);
+    const fcplx t = fsub(fexpc(fneg(alpha)), faddeeva(a));
+    const fcplx c = fsub(fc(-t.im, t.re), fdivc(fc(0.56418958354775628695, 0.0), a));
+    const fcplx u = fsub(fmulc(fexpc(alpha), c), fc(0.0, 1.0));
+    out[0] = fadd(out[0], fscal(-0.28209479177387814347, fmulc(kappa, u)));
+  }
+  if (s > ctol && fabs(sz) < ctol) {
+    sz = 1.1 * ctol;
+    s = sqrt(sx * sx + sy * sy + sz * sz);
+  }
+  const bool f35 = s > ctol && fabs(sz) > ctol;
+  fcplx cs[SKKR_KAMBE_L2 + 1];
+  cs[0] = fc(1.0, 0.0);
+  for (int l = 1; l <= lmax2; l++) cs[l] = fmulc(cs[l - 1], fscal(sz, kappa));
+  fcplx gam[SKKR_KAMBE_L2 + 1], dl[SKKR_KAMBE_L2 + 2], cp[SKKR_KAMBE_L2 + 1], cm[SKKR_KAMBE_L2 + 1];
+  const fcplx xrot = fexpc(fc(0.0, -3.14159265358979323846));  // exp(-i pi) of kamstr.f
+  for (int ig = 0; ig < ng; ig++) {
+    const double gkx = gvec[2 * ig] + kx, gky = gvec[2 * ig + 1] + ky;
+    const double km2 = gkx * gkx + gky * gky, km = sqrt(km2);
+    if (km > gcut) continue;
+    const fcplx kp = fsqrtc(fsub(e, fc(km2, 0.0)));
+    const fcplx ex2 = km > 1e-10 ? fc(gkx / km, gky / km) : fc(1.0, 0.0);
+    const fcplx xc = fscal(0.5, fmulc(fmulc(xrot, fsub(e, fc(km * km, 0.0))), w));
+    kambe_incgamma(lmax2, xc, gam);
+    const fcplx rp = fdivc(kp, kappa), rm = fdivc(fc(km, 0.0), kappa);
+    for (int l = 0; l <= lmax2; l++) {
+      cp[l] = fpowi(rp, 2 * l - 1);
+      cm[l] = fpowi(rm, l);
+    }
+    if (f35) {
+      kambe_delkam(lmax2, xc, fmulc(fscal(sz, kp), fscal(sz, kp)), dl);
+      const fcplx ex1 = fmulc(fexpc(fc(0.0, gkx * sx + gky * sy)), cs1);
+      for (int l = 0; l <= lmax2; l++)
+        for (int m = -l; m <= l; m++) {
+          const int mm = m < 0 ? -m : m, ipar = (l - mm) % 2;
+          const fcplx ex = fmulc(fpowi(ex2, -m), ex1);
+          fcplx csum = fc(0.0, 0.0);
+          for (int n = 0; n <= l - mm; n++) {
+            fcplx b = fc(0.0, 0.0);
+            const int kmax = 2 * n < l - mm ? 2 * n : l - mm;
+            for (int k = n + (n + ipar) % 2; k <= kmax; k += 2) {
+              const int i = 2 * n - k, j = l - k;
+              const fcplx cc = fscal(1.0 / (kambe_fac(i) * kambe_fac(k - n)), fmulc(cs[i], cm[j]));
+              b = fadd(b, fscal(1.0 / (kambe_fac((l - mm - k) / 2) * kambe_fac((l + mm - k) / 2)), cc));
+            }
+            csum = fadd(csum, fmulc(fmulc(cp[n], dl[n]), b));
+          }
+          const int lm = l * (l + 1) + m;
+          out[lm] = fadd(out[lm], fmulc(fscal(flm[lm], fmulc(ex, csum)), fipow(1 - m)));
+        }
+    } else {
+      for (int l = 0; l <= lmax2; l++)
+        for (int m = -l; m <= l; m++) {
+          const int mm = m < 0 ? -m : m;
+          if ((l - mm) % 2) continue;
+          const fcplx ex = fmulc(fpowi(ex2, -m), cs1);
+          fcplx csum = fc(0.0, 0.0);
+          for (int n = 0; n <= (l - mm) / 2; n++) {
+            const fcplx t = fmulc(fmulc(cp[n], cm[l - 2 * n]), gam[n]);
+            csum = fadd(csum, fscal(1.0 / (kambe_fac(n) * kambe_fac((l - mm - 2 * n) / 2) *
+                                           kambe_fac((l + mm - 2 * n) / 2)), t));
+          }
+          const int lm = l * (l + 1) + m;
+          out[lm] = fadd(out[lm], fmulc(fscal(flm[lm], fmulc(ex, csum)), fipow(1 - m)));
+        }
+    }
+  }
+  fcplx ylm[(SKKR_KAMBE_L2 + 1) * (SKKR_KAMBE_L2 + 1)], intil[SKKR_KAMBE_L2 + 1];
+  for (int ir = 0; ir < nr; ir++) {
+    const double rx = rvec[2 * ir], ry = rvec[2 * ir + 1];
+    const double vx = rx + sx, vy = ry + sy, vz = sz;
+    const double rs = sqrt(vx * vx + vy * vy + vz * vz);
+    if (rs < 1e-5 || sqrt(vx * vx + vy * vy) > rcut) continue;
+    const fcplx ex1 = fexpc(fc(0.0, -(rx * kx + ry * ky)));
+    kambe_ylm(vx, vy, vz, lmax2, ylm);
+    kambe_ilkam(lmax2, alpha, rs, kappa, intil);
+    const fcplx a = fscal(-0.5 * rs, kappa);
+    fcplx b = fdivc(fmulc(ex1, cs2), a);
+    for (int l = 0; l <= lmax2; l++) {
+      b = fmulc(b, a);
+      const fcplx c = fmulc(intil[l], b);
+      for (int m = -l; m <= l; m++) {
+        const int lm = l * (l + 1) + m;
+        out[lm] = fadd(out[lm], fmulc(c, fconj(ylm[lm])));
+      }
+    }
+  }
+}

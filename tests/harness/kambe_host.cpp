@@ -1,0 +1,14 @@
+// Host build of the device Kambe lattice sums, for their CPU test: the same
+// header the device code includes, compiled by g++.
+#include "../../skkr_budapest_gb300/csrc/kambe_dev.cuh"
+
+extern "C" void kambe_eval(double er, double ei, double kx, double ky, double sx, double sy, double sz, int lmax2,
+                           const double *gvec, int ng, const double *rvec, int nr, double area, double factor,
+                           double gcut, double rcut, double *out) {
+  fcplx d[(SKKR_KAMBE_L2 + 1) * (SKKR_KAMBE_L2 + 1)];
+  kambe_dlm(fc(er, ei), kx, ky, sx, sy, sz, lmax2, gvec, ng, rvec, nr, area, factor, gcut, rcut, d);
+  for (int i = 0; i < (lmax2 + 1) * (lmax2 + 1); i++) {
+    out[2 * i] = d[i].re;
+    out[2 * i + 1] = d[i].im;
+  }
+}

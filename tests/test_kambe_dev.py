@@ -1,0 +1,52 @@
+"""The Kambe lattice sums written for the device
+(skkr_budapest_gb300/csrc/kambe_dev.cuh), compiled for the host from the
+same header, against the oracle's restatement of main/kamstr.f
+(oracle/kambe.py) on the same lattice vectors (CPU)."""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import kambe as K
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+A2D = 4.808326112068523
+LAT = K.Lattice2D([A2D, 0.0], [0.0, A2D])
+GCUT, RCUT = 12.0, 40.0
+
+
+@pytest.fixture(scope="module")
+def lib(tmp_path_factory):
+    so = str(tmp_path_factory.mktemp("kam") / "libkam.so")
+    subprocess.run(["g++", "-O2", "-shared", "-fPIC", "-o", so,
+                    os.path.join(ROOT, "tests", "harness", "kambe_host.cpp")], check=True)
+    L = ctypes.CDLL(so)
+    D, I, P = ctypes.c_double, ctypes.c_int, ctypes.c_void_p
+    L.kambe_eval.argtypes = [D, D, D, D, D, D, D, I, P, I, P, I, D, D, D, D, P]
+    return L
+
+
+def _dev(lib, e, k, sep, lmax2):
+    g = np.ascontiguousarray(LAT.gvecs(GCUT + 2.0))
+    r = np.ascontiguousarray(LAT.rvecs(RCUT + 15.0))
+    out = np.zeros(2 * (lmax2 + 1) ** 2)
+    lib.kambe_eval(e.real, e.imag, k[0], k[1], *sep, lmax2, g.ctypes.data, len(g), r.ctypes.data, len(r),
+                   LAT.area, 1.0, GCUT, RCUT, out.ctypes.data)
+    return out[0::2] + 1j * out[1::2]
+
+
+@pytest.mark.parametrize("e", [0.3 + 0.01j, 0.4 + 0.6j, -0.45 + 0.06j, 0.7 + 1e-4j])
+@pytest.mark.parametrize("sep", [(0.0, 0.0, 0.0), (1.2, 0.7, 3.4), (0.5 * A2D, 0.5 * A2D, 0.0), (0.4, -1.1, -6.8)])
+@pytest.mark.parametrize("lmax2", [4, 6])
+def test_device_form_equals_the_oracle(lib, e, sep, lmax2):
+    k = (0.21, 0.07)
+    d = _dev(lib, e, k, sep, lmax2)
+    ref = K.kambe_dlm(e, *k, sep, lmax2, LAT, gcut=GCUT, rcut=RCUT)
+    # in plane kamstr shifts the pair to s_z = 1.1e-4, and delkam's upward
+    # recursion multiplies by (2 / (k_z s_z))^2 per step: at lmax2 = 6 the two
+    # builds' rounding then differs by up to 1.5e-10, while both sit 8e-5
+    # from the unshifted lattice sum (the method's own error there)
+    in_plane = sep[2] == 0.0 and any(sep[:2])
+    assert np.abs(d - ref).max() < (1e-9 if in_plane else 1e-12) * np.abs(ref).max()
