@@ -301,6 +301,18 @@ int skkr_gpu_mlp_train(int nlayer, const int *dims, double *params, int n, const
                        const unsigned char *rows, int epochs, double lr, double weight_decay, int eval_every,
                        double *train_loss, double *best, double *best_params);
 
+/* The reference's k-space structure constants (main/kamstr.f:20-392): the
+ * Kambe lattice sums D_L(k, s) of outgoing spherical waves over a 2D lattice,
+ * L = (l, m) up to l = lmax2 (0..6), index l(l+1)+m, for nitem items of one
+ * energy e (k point kxy[2 item], layer-pair separation sep[3 item], a.u.).
+ * gvec [ng][2] / rvec [nr][2]: reciprocal and direct lattice vectors (any
+ * superset: terms with |g + k| > gcut or an in-plane |R + s| > rcut are
+ * skipped); area the cell area; factor the Ewald parameter (eta of the
+ * input, 1 in the reference's samples).  out [nitem][(lmax2+1)^2] complex. */
+int skkr_gpu_kambe_dlm(int nitem, double e_re, double e_im, const double *kxy, const double *sep, int lmax2,
+                       const double *gvec, int ng, const double *rvec, int nr, double area, double factor,
+                       double gcut, double rcut, double *out);
+
 /* Layer DOS of nlay layers from their physical site-diagonal tau (replaces
  * the lambda = 0 moment of nrsp-scf/moment.f:47-110 with locquant.f:86-126,
  * and rsp-scf/moment.f:60-140 with locquant.f:197-232):

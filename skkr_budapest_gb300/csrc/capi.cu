@@ -2283,3 +2283,30 @@ extern "C" int skkr_gpu_mlp_train(int nlayer, const int *dims, double *params, i
   }
   return SKKR_OK;
 }
+
+// ---- the reference's k-space structure constants: Kambe lattice sums ----
+extern "C" int skkr_gpu_kambe_dlm(int nitem, double e_re, double e_im, const double *kxy, const double *sep,
+                                  int lmax2, const double *gvec, int ng, const double *rvec, int nr, double area,
+                                  double factor, double gcut, double rcut, double *out) {
+  if (nitem < 1 || !kxy || !sep || !gvec || !rvec || !out || ng < 1 || nr < 1) return SKKR_ERR_ARG;
+  if (lmax2 < 0 || lmax2 > 6 || !(area > 0.0) || !(factor > 0.0) || !(gcut > 0.0) || !(rcut > 0.0))
+    return SKKR_ERR_ARG;
+  if (e_re == 0.0 && e_im == 0.0) return SKKR_ERR_ARG;
+  const int lmmx = (lmax2 + 1) * (lmax2 + 1);
+  Scoped s;
+  double *K, *S, *G, *R, *O;
+  CKR(s.alloc(&K, 2 * (size_t)nitem));
+  CKR(s.alloc(&S, 3 * (size_t)nitem));
+  CKR(s.alloc(&G, 2 * (size_t)ng));
+  CKR(s.alloc(&R, 2 * (size_t)nr));
+  CKR(s.alloc(&O, 2 * (size_t)nitem * lmmx));
+  CK(cudaMemcpy(K, kxy, 2 * (size_t)nitem * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(S, sep, 3 * (size_t)nitem * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(G, gvec, 2 * (size_t)ng * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(R, rvec, 2 * (size_t)nr * sizeof(double), cudaMemcpyHostToDevice));
+  launch_kambe_dlm(nitem, e_re, e_im, K, S, lmax2, G, ng, R, nr, area, factor, gcut, rcut, O, 0);
+  CK(cudaDeviceSynchronize());
+  CK(cudaGetLastError());
+  CK(cudaMemcpy(out, O, 2 * (size_t)nitem * lmmx * sizeof(double), cudaMemcpyDeviceToHost));
+  return SKKR_OK;
+}

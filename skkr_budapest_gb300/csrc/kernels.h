@@ -115,3 +115,8 @@ void mlp_launch_adamw(double *p, const double *g, double *m, double *v, long lon
                       double b1, double b2, double eps, double step_size, double bc2_sqrt, cudaStream_t st);
 void mlp_launch_keep_best(const double *val, const double *train, double *best, const double *p, double *pbest,
                           long long np, cudaStream_t st);
+
+// Kambe lattice sums D_L(k, s) (kernels_kambe.cu): out[item][(lmax2+1)^2] complex
+void launch_kambe_dlm(int nitem, double er, double ei, const double *kxy, const double *sep, int lmax2,
+                      const double *gvec, int ng, const double *rvec, int nr, double area, double factor,
+                      double gcut, double rcut, double *out, cudaStream_t st);

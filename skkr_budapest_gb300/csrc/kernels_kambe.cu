@@ -1,0 +1,37 @@
+// The reference's k-space structure constants on the device, first form:
+// the Kambe lattice sums D_L(k, s) of kambe_dev.cuh, one thread per
+// (k point, layer-pair separation) item running the whole sum.
+#include "common.cuh"
+#include "kernels.h"
+#include "kambe_dev.cuh"
+
+namespace {
+
+__global__ void k_kambe_dlm(int nitem, double er, double ei, const double *__restrict__ kxy,
+                            const double *__restrict__ sep, int lmax2, const double *__restrict__ gvec, int ng,
+                            const double *__restrict__ rvec, int nr, double area, double factor, double gcut,
+                            double rcut, double *__restrict__ out) {
+  const int lmmx = (lmax2 + 1) * (lmax2 + 1);
+  for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < nitem; it += gridDim.x * blockDim.x) {
+    fcplx d[(SKKR_KAMBE_L2 + 1) * (SKKR_KAMBE_L2 + 1)];
+    kambe_dlm(fc(er, ei), kxy[2 * it], kxy[2 * it + 1], sep[3 * it], sep[3 * it + 1], sep[3 * it + 2], lmax2,
+              gvec, ng, rvec, nr, area, factor, gcut, rcut, d);
+    double *o = out + (long long)it * 2 * lmmx;
+    for (int i = 0; i < lmmx; i++) {
+      o[2 * i] = d[i].re;
+      o[2 * i + 1] = d[i].im;
+    }
+  }
+}
+
+}  // namespace
+
+void launch_kambe_dlm(int nitem, double er, double ei, const double *kxy, const double *sep, int lmax2,
+                      const double *gvec, int ng, const double *rvec, int nr, double area, double factor,
+                      double gcut, double rcut, double *out, cudaStream_t st) {
+  const int threads = 64;
+  const int blocks = (nitem + threads - 1) / threads;
+  k_kambe_dlm<<<blocks, threads, 0, st>>>(nitem, er, ei, kxy, sep, lmax2, gvec, ng, rvec, nr, area, factor, gcut,
+                                          rcut, out);
+  SKKR_LAUNCHED();
+}

@@ -74,6 +74,7 @@ def lib():
         L.skkr_gpu_mlp_forward.argtypes = [I, P, P, I, P, P]
         L.skkr_gpu_mlp_grad.argtypes = [I, P, P, I, P, P, P, P, P]
         L.skkr_gpu_mlp_train.argtypes = [I, P, P, I, P, P, P, I, D, D, I, P, P, P]
+        L.skkr_gpu_kambe_dlm.argtypes = [I, D, D, P, P, I, P, I, P, I, D, D, D, D, P]
         L.skkr_gpu_layer_dos.argtypes = [I, I, I, P, I, P, P, I, P, P]
         L.skkr_gpu_set_reduce.argtypes = [P, P, P]
         L.skkr_gpu_set_mixed_policy.argtypes = [P, D, D, I, D]
@@ -246,6 +247,21 @@ def mlp_train(layers, x, y, rows, epochs, lr, weight_decay, eval_every=20):
                                     None if r is None else _p(r), int(epochs), float(lr), float(weight_decay),
                                     int(eval_every), _p(tl), _p(best), _p(bp)), "skkr_gpu_mlp_train")
     return _mlp_unpack(dims, params), _mlp_unpack(dims, bp), tl, (float(best[0]), float(best[1]))
+
+
+def kambe_dlm(e, kxy, sep, lmax2, gvec, rvec, area, factor=1.0, gcut=12.0, rcut=40.0):
+    """Device Kambe lattice sums D_L(k, s) of one energy for items (kxy[i],
+    sep[i]) (skkr_gpu_kambe_dlm); returns (nitem, (lmax2+1)^2) complex."""
+    kxy = np.ascontiguousarray(kxy, np.float64).reshape(-1, 2)
+    sep = np.ascontiguousarray(sep, np.float64).reshape(-1, 3)
+    g = np.ascontiguousarray(gvec, np.float64).reshape(-1, 2)
+    r = np.ascontiguousarray(rvec, np.float64).reshape(-1, 2)
+    out = np.zeros((len(kxy), 2 * (lmax2 + 1) ** 2))
+    e = complex(e)
+    _check(lib().skkr_gpu_kambe_dlm(len(kxy), e.real, e.imag, _p(kxy), _p(sep), lmax2, _p(g), len(g), _p(r), len(r),
+                                    float(area), float(factor), float(gcut), float(rcut), _p(out)),
+           "skkr_gpu_kambe_dlm")
+    return out[:, 0::2] + 1j * out[:, 1::2]
 
 
 REDUCE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.POINTER(C.c_double), C.c_longlong)

@@ -137,3 +137,19 @@ def test_mlp_argument_checks_before_any_device_call():
     assert lib.skkr_gpu_mlp_train(2, d, b, 4, b, b, None, 0, 1e-3, 0.0, 20, b, b, b) == ARG   # no epoch
     assert lib.skkr_gpu_mlp_train(2, d, b, 4, b, b, None, 5, 0.0, 0.0, 20, b, b, b) == ARG   # lr 0
     assert lib.skkr_gpu_mlp_train(2, d, b, 4, b, b, None, 5, 1e-3, -1.0, 20, b, b, b) == ARG  # wd < 0
+
+
+def test_kambe_argument_checks_before_any_device_call():
+    import numpy as np
+    import __graft_entry__
+    __graft_entry__.build()
+    lib = ctypes.CDLL(native.LIB_PATH)
+    D, I, P = ctypes.c_double, ctypes.c_int, ctypes.c_void_p
+    lib.skkr_gpu_kambe_dlm.argtypes = [I, D, D, P, P, I, P, I, P, I, D, D, D, D, P]
+    b = np.zeros(64).ctypes.data
+    ok = (0.5, 0.01, b, b, 4, b, 3, b, 3, 23.1, 1.0, 12.0, 40.0, b)
+    assert lib.skkr_gpu_kambe_dlm(0, *ok) == -1                                     # no item
+    assert lib.skkr_gpu_kambe_dlm(1, 0.5, 0.01, b, b, 7, b, 3, b, 3, 23.1, 1.0, 12.0, 40.0, b) == -1   # lmax2
+    assert lib.skkr_gpu_kambe_dlm(1, 0.5, 0.01, b, b, 4, b, 3, b, 3, 0.0, 1.0, 12.0, 40.0, b) == -1    # area
+    assert lib.skkr_gpu_kambe_dlm(1, 0.0, 0.0, b, b, 4, b, 3, b, 3, 23.1, 1.0, 12.0, 40.0, b) == -1    # E = 0
+    assert lib.skkr_gpu_kambe_dlm(1, 0.5, 0.01, None, b, 4, b, 3, b, 3, 23.1, 1.0, 12.0, 40.0, b) == -1
