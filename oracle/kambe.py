@@ -417,6 +417,22 @@ def _gaunt_ours(lmax: int) -> np.ndarray:
     return out
 
 
+def alm_coef(lmax: int) -> np.ndarray:
+    """coef[L, L', q] with alm(k, s) = sum_q coef[L, L', q] D_q(k, s): the
+    mapping of lattice_g folded into one tensor (4 pi <Y_L Y*_L' Y_L''>
+    i^(l'-l-l'') (-1)^(l''+m'') at q = (l'', -m''))."""
+    l2 = 2 * lmax
+    lv = np.array([l for l in range(lmax + 1) for _ in range(-l, l + 1)])
+    lv2 = np.array([l for l in range(l2 + 1) for _ in range(-l, l + 1)])
+    mv2 = np.array([m for l in range(l2 + 1) for m in range(-l, l + 1)])
+    neg = np.array([l * (l + 1) - m for l in range(l2 + 1) for m in range(-l, l + 1)])
+    ph = (1j) ** ((-lv[:, None, None] + lv[None, :, None] - lv2[None, None, :]) % 4)
+    t = 4 * math.pi * _gaunt_ours(lmax) * ph * ((-1.0) ** (mv2 + lv2))[None, None, :]
+    out = np.zeros_like(t)
+    out[:, :, neg] = t
+    return out
+
+
 def lattice_g(e: complex, kx: float, ky: float, lmax: int, sep, lat: Lattice2D, **cut) -> np.ndarray:
     """sum_R e^{ik.R} G0_{LL'}(R + sep) with the free-space constants
     G0_{LL'}(r) = -4 pi i kappa sum_L'' <Y_L Y*_L' Y_L''> i^(l'-l-l'') h_l''(kappa r) Y_L''(r)

@@ -268,3 +268,19 @@ SKKR_HD inline void kambe_dlm(fcplx e, double kx, double ky, double sx, double s
     }
   }
 }
+
+// alm(k, s)[L][L'] = sum_L'' coef[L][L'][L''] D_L''(k, s), the layer-pair
+// structure constants kamstr.f forms from its lattice sums (in this library's
+// harmonics: coef = 4 pi <Y_L Y*_L' Y_L''> i^(l'-l-l'') with D taken at
+// (l'', -m'') and signed (-1)^(l''+m''), prepared by the host).  coef is
+// [lmmax][lmmax][lmmx2] complex (re, im interleaved); out [lmmax][lmmax].
+SKKR_HD inline void kambe_alm(const fcplx *d, int lmax, const double *coef, fcplx *out) {
+  const int lm = (lmax + 1) * (lmax + 1), lm2 = (2 * lmax + 1) * (2 * lmax + 1);
+  for (int a = 0; a < lm; a++)
+    for (int b = 0; b < lm; b++) {
+      fcplx s = fc(0.0, 0.0);
+      const double *c = coef + 2 * ((long long)(a * lm + b) * lm2);
+      for (int q = 0; q < lm2; q++) s = fadd(s, fmulc(fc(c[2 * q], c[2 * q + 1]), d[q]));
+      out[a * lm + b] = s;
+    }
+}

@@ -12,3 +12,15 @@ extern "C" void kambe_eval(double er, double ei, double kx, double ky, double sx
     out[2 * i + 1] = d[i].im;
   }
 }
+
+extern "C" void kambe_alm_eval(double er, double ei, double kx, double ky, double sx, double sy, double sz,
+                               int lmax, const double *gvec, int ng, const double *rvec, int nr, double area,
+                               double gcut, double rcut, const double *coef, double *out) {
+  fcplx d[(SKKR_KAMBE_L2 + 1) * (SKKR_KAMBE_L2 + 1)], g[256];
+  kambe_dlm(fc(er, ei), kx, ky, sx, sy, sz, 2 * lmax, gvec, ng, rvec, nr, area, 1.0, gcut, rcut, d);
+  kambe_alm(d, lmax, coef, g);
+  for (int i = 0; i < (lmax + 1) * (lmax + 1) * (lmax + 1) * (lmax + 1); i++) {
+    out[2 * i] = g[i].re;
+    out[2 * i + 1] = g[i].im;
+  }
+}

@@ -50,3 +50,22 @@ def test_device_form_equals_the_oracle(lib, e, sep, lmax2):
     # from the unshifted lattice sum (the method's own error there)
     in_plane = sep[2] == 0.0 and any(sep[:2])
     assert np.abs(d - ref).max() < (1e-9 if in_plane else 1e-12) * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("e", [0.3 + 0.01j, 0.4 + 0.6j])
+@pytest.mark.parametrize("sep", [(0.0, 0.0, 0.0), (1.2, 0.7, 3.4), (0.4, -1.1, -6.8)])
+@pytest.mark.parametrize("lmax", [2, 3])
+def test_device_blocks_equal_kamstr(lib, e, sep, lmax):
+    D, I, P = ctypes.c_double, ctypes.c_int, ctypes.c_void_p
+    lib.kambe_alm_eval.argtypes = [D, D, D, D, D, D, D, I, P, I, P, I, D, D, D, P, P]
+    g = np.ascontiguousarray(LAT.gvecs(GCUT + 2.0))
+    r = np.ascontiguousarray(LAT.rvecs(RCUT + 15.0))
+    coef = np.ascontiguousarray(K.alm_coef(lmax).view(np.float64))
+    lm = (lmax + 1) ** 2
+    out = np.zeros(2 * lm * lm)
+    k = (0.21, 0.07)
+    lib.kambe_alm_eval(e.real, e.imag, *k, *sep, lmax, g.ctypes.data, len(g), r.ctypes.data, len(r), LAT.area,
+                       GCUT, RCUT, coef.ctypes.data, out.ctypes.data)
+    got = (out[0::2] + 1j * out[1::2]).reshape(lm, lm)
+    ref = K.kamstr(e, *k, lmax, sep, LAT, gcut=GCUT, rcut=RCUT)
+    assert np.abs(got - ref).max() < 1e-12 * np.abs(ref).max()
