@@ -333,3 +333,40 @@ def write_host_tau(taupath, ie, ep, tminv, tauc, tij, pairs):
     from . import tauh
     h = host_tau(ep, tminv, tauc, tij, pairs)
     return tauh.write_tauh(taupath, ie, ep.ce, ep.nk, pairs, h["tau_ij"], h["tau_ji"], h["tau_ii"])
+
+
+def bloch_spectral(ep, kpts, which="a", para=False):
+    """Bloch spectral function of the interface layers at the k points kpts
+    ((nk, 2), a.u.), for layers without an alloy (rsp-scf/bsf.f with the
+    coherent tau of those layers, skkr_dbogo_bsf/rsp-scf/bsf.f:236-240):
+        A_l(k, E) = -1/pi Im sum_{L in l} F_L tau_LL(k),
+    tau(k) the physical site-diagonal tau of that one k point (no point-group
+    average), F the single-site radial integrals of the layer DOS; the
+    k-independent single-site term of the DOS is not part of it.  Each k
+    point is a one-point k loop of cpacoord with the identity alone, then
+    phystau and the layer-DOS kernel with G = 0, all on the device.  Returns
+    (A_l [nk, nintfc, lmax+1], A_L [nk, nintfc, lk]).  The CPA form (the A0
+    and A1 terms of bsf.f for alloy layers) needs the radial integrals across
+    the two species and is not built."""
+    import dataclasses
+    from . import synth as S
+    if any(1e-6 < c < 1 - 1e-6 for c in ep.conc):
+        raise ValueError("bloch_spectral: alloy layers need the CPA form of bsf.f (not built)")
+    one = dataclasses.replace(ep, lg=ep.lg[:1], rg=ep.rg[:1])
+    F, _ = S.layer_dos_inputs(ep, which)
+    zero = np.zeros_like(F)
+    kpts = np.asarray(kpts, float).reshape(-1, 2)
+    al = np.zeros((len(kpts), ep.nintfc, ep.lmax + 1))
+    aL = np.zeros((len(kpts), ep.nintfc, ep.lkmax))
+    ctx = Context.for_problem(one)
+    try:
+        for i, k in enumerate(kpts):
+            r = ctx.cpacoord(one.with_k(k[None, :], np.ones(1)))
+            tm = r["tminv"]
+            phys = np.array([N.phystau(r["tauc"][li], tm[li], ep.alpha[li], ep.lmax, ep.irel)
+                             for li in range(ep.nintfc)])
+            zm, zl = N.layer_dos(phys, F, zero, ep.lmax, ep.irel, para)
+            al[i], aL[i] = zl.imag, zm.imag
+    finally:
+        ctx.close()
+    return al, aL
