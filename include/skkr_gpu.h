@@ -312,6 +312,11 @@ int skkr_gpu_mlp_train(int nlayer, const int *dims, double *params, int n, const
 int skkr_gpu_kambe_dlm(int nitem, double e_re, double e_im, const double *kxy, const double *sep, int lmax2,
                        const double *gvec, int ng, const double *rvec, int nr, double area, double factor,
                        double gcut, double rcut, double *out);
+/* The coefficients that turn those sums into the layer-pair structure
+ * constants, alm[L][L'] = sum_q coef[L][L'][q] D_q (kamstr.f:355-390 in this
+ * library's harmonics), for lmax 0..3: coef [lmmax][lmmax][(2 lmax+1)^2]
+ * complex.  Host only: no device call. */
+int skkr_gpu_kambe_coef(int lmax, double *out);
 
 /* Layer DOS of nlay layers from their physical site-diagonal tau (replaces
  * the lambda = 0 moment of nrsp-scf/moment.f:47-110 with locquant.f:86-126,

@@ -20,6 +20,7 @@
 
 #include "../../include/skkr_gpu.h"
 #include "kernels.h"
+#include "kambe_dev.cuh"
 
 thread_local long long g_skkr_launches = 0;
 static thread_local std::string g_last_error;
@@ -2308,5 +2309,66 @@ extern "C" int skkr_gpu_kambe_dlm(int nitem, double e_re, double e_im, const dou
   CK(cudaDeviceSynchronize());
   CK(cudaGetLastError());
   CK(cudaMemcpy(out, O, 2 * (size_t)nitem * lmmx * sizeof(double), cudaMemcpyDeviceToHost));
+  return SKKR_OK;
+}
+
+// coefficient tensor of the block contraction kambe_alm (host only, no
+// device call): coef[L][L'][q] = 4 pi <Y_L Y*_L' Y_q'> i^(l'-l-l_q')
+// (-1)^(l_q'+m_q') at q = (l_q', -m_q'), the Gaunt integrals of the complex
+// harmonics by Gauss-Legendre x uniform-phi quadrature (exact at these
+// degrees), entries below 1e-13 set to zero
+extern "C" int skkr_gpu_kambe_coef(int lmax, double *out) {
+  if (lmax < 0 || lmax > 3 || !out) return SKKR_ERR_ARG;
+  const int lm = (lmax + 1) * (lmax + 1), l2 = 2 * lmax, lm2 = (l2 + 1) * (l2 + 1);
+  const int nq = (4 * lmax + l2) / 2 + 2, nph = 4 * lmax + l2 + 2;
+  // Gauss-Legendre nodes and weights by Newton's method on P_nq
+  std::vector<double> xg(nq), wg(nq);
+  for (int i = 0; i < nq; i++) {
+    double x = std::cos(M_PI * (i + 0.75) / (nq + 0.5)), dp = 1.0;
+    for (int it = 0; it < 100; it++) {
+      double p0 = 1.0, p1 = x;
+      for (int n = 2; n <= nq; n++) {
+        const double p2 = ((2.0 * n - 1.0) * x * p1 - (n - 1.0) * p0) / n;
+        p0 = p1;
+        p1 = p2;
+      }
+      dp = nq * (x * p1 - p0) / (x * x - 1.0);
+      const double dx = p1 / dp;
+      x -= dx;
+      if (std::fabs(dx) < 1e-16) break;
+    }
+    xg[i] = x;
+    wg[i] = 2.0 / ((1.0 - x * x) * dp * dp);
+  }
+  std::vector<fcplx> C((size_t)lm * lm * lm2, fc(0.0, 0.0)), y(lm2);
+  for (int i = 0; i < nq; i++) {
+    const double ct = xg[i], st = std::sqrt(std::max(0.0, 1.0 - ct * ct));
+    for (int p = 0; p < nph; p++) {
+      const double phi = 2.0 * M_PI * p / nph, w = wg[i] * 2.0 * M_PI / nph;
+      kambe_ylm(st * std::cos(phi), st * std::sin(phi), ct, l2, y.data());
+      for (int a = 0; a < lm; a++)
+        for (int b = 0; b < lm; b++) {
+          const fcplx ab = fmulc(y[a], fconj(y[b]));
+          for (int q = 0; q < lm2; q++) {
+            fcplx &c = C[((size_t)a * lm + b) * lm2 + q];
+            c = fadd(c, fscal(w, fmulc(ab, y[q])));
+          }
+        }
+    }
+  }
+  auto lof = [](int i) { int l = 0; while ((l + 1) * (l + 1) <= i) l++; return l; };
+  for (int a = 0; a < lm; a++)
+    for (int b = 0; b < lm; b++)
+      for (int q = 0; q < lm2; q++) {
+        fcplx c = C[((size_t)a * lm + b) * lm2 + q];
+        if (std::fabs(c.re) < 1e-13) c.re = 0.0;
+        if (std::fabs(c.im) < 1e-13) c.im = 0.0;
+        const int la = lof(a), lb = lof(b), lq = lof(q), mq = q - lq * (lq + 1);
+        const fcplx t = fscal(4.0 * M_PI * (((lq + mq) % 2 + 2) % 2 ? -1.0 : 1.0), fmulc(c, fipow(lb - la - lq)));
+        const int qn = lq * (lq + 1) - mq;
+        double *o = out + 2 * (((size_t)a * lm + b) * lm2 + qn);
+        o[0] = t.re;
+        o[1] = t.im;
+      }
   return SKKR_OK;
 }

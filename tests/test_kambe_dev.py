@@ -69,3 +69,17 @@ def test_device_blocks_equal_kamstr(lib, e, sep, lmax):
     got = (out[0::2] + 1j * out[1::2]).reshape(lm, lm)
     ref = K.kamstr(e, *k, lmax, sep, LAT, gcut=GCUT, rcut=RCUT)
     assert np.abs(got - ref).max() < 1e-12 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("lmax", [0, 1, 2, 3])
+def test_library_coefficient_table_equals_the_oracle(lmax):
+    # skkr_gpu_kambe_coef is host code (no device call), so it runs here
+    from skkr_budapest_gb300 import native
+    L = ctypes.CDLL(native.LIB_PATH)
+    L.skkr_gpu_kambe_coef.argtypes = [ctypes.c_int, ctypes.c_void_p]
+    lm, lm2 = (lmax + 1) ** 2, (2 * lmax + 1) ** 2
+    out = np.zeros(2 * lm * lm * lm2)
+    assert L.skkr_gpu_kambe_coef(lmax, out.ctypes.data) == 0
+    got = (out[0::2] + 1j * out[1::2]).reshape(lm, lm, lm2)
+    assert np.abs(got - K.alm_coef(lmax)).max() < 1e-13
+    assert L.skkr_gpu_kambe_coef(4, out.ctypes.data) == -1
