@@ -317,6 +317,13 @@ int skkr_gpu_kambe_dlm(int nitem, double e_re, double e_im, const double *kxy, c
  * library's harmonics), for lmax 0..3: coef [lmmax][lmmax][(2 lmax+1)^2]
  * complex.  Host only: no device call. */
 int skkr_gpu_kambe_coef(int lmax, double *out);
+/* The layer-pair structure constants alm(k, s) [lmmax][lmmax] of nitem items
+ * (kamstr.f's output; the arguments as for skkr_gpu_kambe_dlm with lmax
+ * 0..3 in place of lmax2): the lattice sums and their contraction on the
+ * device, one thread per item.  out [nitem][lmmax][lmmax] complex, row L. */
+int skkr_gpu_kambe_alm(int nitem, double e_re, double e_im, const double *kxy, const double *sep, int lmax,
+                       const double *gvec, int ng, const double *rvec, int nr, double area, double factor,
+                       double gcut, double rcut, double *out);
 
 /* Layer DOS of nlay layers from their physical site-diagonal tau (replaces
  * the lambda = 0 moment of nrsp-scf/moment.f:47-110 with locquant.f:86-126,

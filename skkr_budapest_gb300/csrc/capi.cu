@@ -2372,3 +2372,34 @@ extern "C" int skkr_gpu_kambe_coef(int lmax, double *out) {
       }
   return SKKR_OK;
 }
+
+extern "C" int skkr_gpu_kambe_alm(int nitem, double e_re, double e_im, const double *kxy, const double *sep,
+                                  int lmax, const double *gvec, int ng, const double *rvec, int nr, double area,
+                                  double factor, double gcut, double rcut, double *out) {
+  if (nitem < 1 || !kxy || !sep || !gvec || !rvec || !out || ng < 1 || nr < 1) return SKKR_ERR_ARG;
+  if (lmax < 0 || lmax > 3 || !(area > 0.0) || !(factor > 0.0) || !(gcut > 0.0) || !(rcut > 0.0))
+    return SKKR_ERR_ARG;
+  if (e_re == 0.0 && e_im == 0.0) return SKKR_ERR_ARG;
+  const int lm = (lmax + 1) * (lmax + 1), lm2 = (2 * lmax + 1) * (2 * lmax + 1);
+  std::vector<double> coef(2 * (size_t)lm * lm * lm2);
+  CKR(skkr_gpu_kambe_coef(lmax, coef.data()));
+  Scoped s;
+  double *K, *S, *G, *R, *Cf, *O;
+  CKR(s.alloc(&K, 2 * (size_t)nitem));
+  CKR(s.alloc(&S, 3 * (size_t)nitem));
+  CKR(s.alloc(&G, 2 * (size_t)ng));
+  CKR(s.alloc(&R, 2 * (size_t)nr));
+  CKR(s.alloc(&Cf, coef.size()));
+  CKR(s.alloc(&O, 2 * (size_t)nitem * lm * lm));
+  CK(cudaMemcpy(K, kxy, 2 * (size_t)nitem * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(S, sep, 3 * (size_t)nitem * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(G, gvec, 2 * (size_t)ng * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(R, rvec, 2 * (size_t)nr * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(Cf, coef.data(), coef.size() * sizeof(double), cudaMemcpyHostToDevice));
+  launch_kambe_alm(nitem, e_re, e_im, K, S, lmax, G, ng, R, nr, area, factor, gcut, rcut, Cf, O, 0);
+  CK(cudaDeviceSynchronize());
+  CK(cudaGetLastError());
+  CK(cudaMemcpy(out, O, 2 * (size_t)nitem * lm * lm * sizeof(double), cudaMemcpyDeviceToHost));
+  return SKKR_OK;
+}
+

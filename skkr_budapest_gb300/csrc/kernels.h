@@ -120,3 +120,8 @@ void mlp_launch_keep_best(const double *val, const double *train, double *best, 
 void launch_kambe_dlm(int nitem, double er, double ei, const double *kxy, const double *sep, int lmax2,
                       const double *gvec, int ng, const double *rvec, int nr, double area, double factor,
                       double gcut, double rcut, double *out, cudaStream_t st);
+// layer-pair blocks alm(k, s) (kernels_kambe.cu): out[item][lmmax][lmmax]
+// complex, coef from skkr_gpu_kambe_coef
+void launch_kambe_alm(int nitem, double er, double ei, const double *kxy, const double *sep, int lmax,
+                      const double *gvec, int ng, const double *rvec, int nr, double area, double factor,
+                      double gcut, double rcut, const double *coef, double *out, cudaStream_t st);

@@ -24,7 +24,31 @@ __global__ void k_kambe_dlm(int nitem, double er, double ei, const double *__res
   }
 }
 
+// the layer-pair blocks alm(k, s) = sum_q coef[L][L'][q] D_q(k, s) of each item
+__global__ void k_kambe_alm(int nitem, double er, double ei, const double *__restrict__ kxy,
+                            const double *__restrict__ sep, int lmax, const double *__restrict__ gvec, int ng,
+                            const double *__restrict__ rvec, int nr, double area, double factor, double gcut,
+                            double rcut, const double *__restrict__ coef, double *__restrict__ out) {
+  const int lm = (lmax + 1) * (lmax + 1);
+  for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < nitem; it += gridDim.x * blockDim.x) {
+    fcplx d[(SKKR_KAMBE_L2 + 1) * (SKKR_KAMBE_L2 + 1)];
+    kambe_dlm(fc(er, ei), kxy[2 * it], kxy[2 * it + 1], sep[3 * it], sep[3 * it + 1], sep[3 * it + 2], 2 * lmax,
+              gvec, ng, rvec, nr, area, factor, gcut, rcut, d);
+    kambe_alm(d, lmax, coef, reinterpret_cast<fcplx *>(out + (long long)it * 2 * lm * lm));
+  }
+}
+
 }  // namespace
+
+void launch_kambe_alm(int nitem, double er, double ei, const double *kxy, const double *sep, int lmax,
+                      const double *gvec, int ng, const double *rvec, int nr, double area, double factor,
+                      double gcut, double rcut, const double *coef, double *out, cudaStream_t st) {
+  const int threads = 64;
+  const int blocks = (nitem + threads - 1) / threads;
+  k_kambe_alm<<<blocks, threads, 0, st>>>(nitem, er, ei, kxy, sep, lmax, gvec, ng, rvec, nr, area, factor, gcut,
+                                          rcut, coef, out);
+  SKKR_LAUNCHED();
+}
 
 void launch_kambe_dlm(int nitem, double er, double ei, const double *kxy, const double *sep, int lmax2,
                       const double *gvec, int ng, const double *rvec, int nr, double area, double factor,

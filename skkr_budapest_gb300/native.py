@@ -75,6 +75,7 @@ def lib():
         L.skkr_gpu_mlp_grad.argtypes = [I, P, P, I, P, P, P, P, P]
         L.skkr_gpu_mlp_train.argtypes = [I, P, P, I, P, P, P, I, D, D, I, P, P, P]
         L.skkr_gpu_kambe_dlm.argtypes = [I, D, D, P, P, I, P, I, P, I, D, D, D, D, P]
+        L.skkr_gpu_kambe_alm.argtypes = [I, D, D, P, P, I, P, I, P, I, D, D, D, D, P]
         L.skkr_gpu_layer_dos.argtypes = [I, I, I, P, I, P, P, I, P, P]
         L.skkr_gpu_set_reduce.argtypes = [P, P, P]
         L.skkr_gpu_set_mixed_policy.argtypes = [P, D, D, I, D]
@@ -262,6 +263,22 @@ def kambe_dlm(e, kxy, sep, lmax2, gvec, rvec, area, factor=1.0, gcut=12.0, rcut=
                                     float(area), float(factor), float(gcut), float(rcut), _p(out)),
            "skkr_gpu_kambe_dlm")
     return out[:, 0::2] + 1j * out[:, 1::2]
+
+
+def kambe_alm(e, kxy, sep, lmax, gvec, rvec, area, factor=1.0, gcut=12.0, rcut=40.0):
+    """Device layer-pair structure constants alm(k, s) of one energy for items
+    (kxy[i], sep[i]) (skkr_gpu_kambe_alm); returns (nitem, lmmax, lmmax)."""
+    kxy = np.ascontiguousarray(kxy, np.float64).reshape(-1, 2)
+    sep = np.ascontiguousarray(sep, np.float64).reshape(-1, 3)
+    g = np.ascontiguousarray(gvec, np.float64).reshape(-1, 2)
+    r = np.ascontiguousarray(rvec, np.float64).reshape(-1, 2)
+    lm = (lmax + 1) ** 2
+    out = np.zeros((len(kxy), 2 * lm * lm))
+    e = complex(e)
+    _check(lib().skkr_gpu_kambe_alm(len(kxy), e.real, e.imag, _p(kxy), _p(sep), lmax, _p(g), len(g), _p(r), len(r),
+                                    float(area), float(factor), float(gcut), float(rcut), _p(out)),
+           "skkr_gpu_kambe_alm")
+    return (out[:, 0::2] + 1j * out[:, 1::2]).reshape(len(kxy), lm, lm)
 
 
 REDUCE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.POINTER(C.c_double), C.c_longlong)

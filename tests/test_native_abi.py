@@ -153,3 +153,16 @@ def test_kambe_argument_checks_before_any_device_call():
     assert lib.skkr_gpu_kambe_dlm(1, 0.5, 0.01, b, b, 4, b, 3, b, 3, 0.0, 1.0, 12.0, 40.0, b) == -1    # area
     assert lib.skkr_gpu_kambe_dlm(1, 0.0, 0.0, b, b, 4, b, 3, b, 3, 23.1, 1.0, 12.0, 40.0, b) == -1    # E = 0
     assert lib.skkr_gpu_kambe_dlm(1, 0.5, 0.01, None, b, 4, b, 3, b, 3, 23.1, 1.0, 12.0, 40.0, b) == -1
+
+
+def test_kambe_blocks_argument_checks_before_any_device_call():
+    import numpy as np
+    import __graft_entry__
+    __graft_entry__.build()
+    lib = ctypes.CDLL(native.LIB_PATH)
+    D, I, P = ctypes.c_double, ctypes.c_int, ctypes.c_void_p
+    lib.skkr_gpu_kambe_alm.argtypes = [I, D, D, P, P, I, P, I, P, I, D, D, D, D, P]
+    b = np.zeros(64).ctypes.data
+    assert lib.skkr_gpu_kambe_alm(1, 0.5, 0.01, b, b, 4, b, 3, b, 3, 23.1, 1.0, 12.0, 40.0, b) == -1   # lmax 4
+    assert lib.skkr_gpu_kambe_alm(0, 0.5, 0.01, b, b, 2, b, 3, b, 3, 23.1, 1.0, 12.0, 40.0, b) == -1   # no item
+    assert lib.skkr_gpu_kambe_alm(1, 0.5, 0.01, b, b, 2, b, 0, b, 3, 23.1, 1.0, 12.0, 40.0, b) == -1   # no g

@@ -31,3 +31,16 @@ def test_device_kambe_sums_match_the_oracle(e, lmax2):
         # parts from the oracle by 7e-10 there, against the shift's own 8e-5
         in_plane = s[2] == 0.0 and any(s[:2])
         assert np.abs(d[i] - ref).max() < (1e-8 if in_plane else 1e-12) * np.abs(ref).max(), (k, s)
+
+
+@pytest.mark.parametrize("e", [0.3 + 0.01j, 0.7 + 1e-4j])
+@pytest.mark.parametrize("lmax", [2, 3])
+def test_device_layer_pair_blocks_match_kamstr(e, lmax):
+    items = [(k, s) for k in KS[:2] for s in SEPS]
+    g = LAT.gvecs(14.0)
+    r = LAT.rvecs(55.0)
+    a = native.kambe_alm(e, [k for k, _ in items], [s for _, s in items], lmax, g, r, LAT.area)
+    for i, (k, s) in enumerate(items):
+        ref = K.kamstr(e, *k, lmax, s, LAT, gcut=12.0, rcut=40.0)
+        in_plane = s[2] == 0.0 and any(s[:2])
+        assert np.abs(a[i] - ref).max() < (1e-8 if in_plane else 1e-12) * np.abs(ref).max(), (k, s)
