@@ -1,8 +1,9 @@
-"""The reference's k-space structure constants on the device
-(skkr_gpu_kambe_dlm: the Kambe lattice sums of main/kamstr.f, one thread per
-(k point, separation) item) against the oracle's restatement on the same
-lattice vectors, at energies down to Im E = 1e-4 Ry and for the zero,
-in-plane and out-of-plane separations of the layer pairs."""
+"""The reference's k-space structure constants on the device, one thread per
+(k point, separation) item: the Kambe lattice sums of main/kamstr.f
+(skkr_gpu_kambe_dlm) against the oracle's restatement on the same lattice
+vectors, and the layer-pair blocks they contract to (skkr_gpu_kambe_alm)
+against the oracle's kamstr, at energies down to Im E = 1e-4 Ry and for the
+zero, in-plane and out-of-plane separations of the layer pairs."""
 import numpy as np
 import pytest
 
