@@ -324,6 +324,17 @@ int skkr_gpu_kambe_coef(int lmax, double *out);
 int skkr_gpu_kambe_alm(int nitem, double e_re, double e_im, const double *kxy, const double *sep, int lmax,
                        const double *gvec, int ng, const double *rvec, int nr, double area, double factor,
                        double gcut, double rcut, double *out);
+/* The reference's screened G_scr(k) (main/gstore.f:146-282 with
+ * main/scrstr.f:2-138) on the device: for each of nk k points the layer-pair
+ * blocks of a slab of nl layers at pos [nl][3] (block (a, b) with the
+ * in-plane phase e^{ik.(pos_b - pos_a)}, the orientation of the real-space
+ * tables), G' = G (1 - alpha G)^-1 with alpha [nl][lmax+1] complex, and the
+ * blocks (centre, centre + j) for j = -jmax..jmax into
+ * out [nk][2 jmax + 1][lmmax][lmmax] complex.  nl (lmax+1)^2 <= 256. */
+int skkr_gpu_kambe_screened(int nk, double e_re, double e_im, const double *kxy, int nl, const double *pos,
+                            const double *alpha, int lmax, const double *gvec, int ng, const double *rvec, int nr,
+                            double area, double factor, double gcut, double rcut, int centre, int jmax,
+                            double *out);
 
 /* Layer DOS of nlay layers from their physical site-diagonal tau (replaces
  * the lambda = 0 moment of nrsp-scf/moment.f:47-110 with locquant.f:86-126,

@@ -2403,3 +2403,65 @@ extern "C" int skkr_gpu_kambe_alm(int nitem, double e_re, double e_im, const dou
   return SKKR_OK;
 }
 
+
+// The reference's screened G_scr(k) on the device (gstore.f + scrstr.f): the
+// layer-pair blocks of a slab of nl layers at pos [nl][3] for each k point,
+// G' = G (1 - alpha G)^-1 per k (Gauss-Jordan and GEMM batched over k), and
+// the blocks (centre, centre + j), j = -jmax..jmax, into
+// out [nk][2 jmax + 1][lmmax][lmmax] complex (row L).  alpha [nl][lmax+1]
+// complex per layer and l; the lattice arguments as for skkr_gpu_kambe_alm.
+extern "C" int skkr_gpu_kambe_screened(int nk, double e_re, double e_im, const double *kxy, int nl,
+                                       const double *pos, const double *alpha, int lmax, const double *gvec,
+                                       int ng, const double *rvec, int nr, double area, double factor,
+                                       double gcut, double rcut, int centre, int jmax, double *out) {
+  if (nk < 1 || nl < 1 || !kxy || !pos || !alpha || !gvec || !rvec || !out || ng < 1 || nr < 1) return SKKR_ERR_ARG;
+  if (lmax < 0 || lmax > 3 || !(area > 0.0) || !(factor > 0.0) || !(gcut > 0.0) || !(rcut > 0.0)) return SKKR_ERR_ARG;
+  if (e_re == 0.0 && e_im == 0.0) return SKKR_ERR_ARG;
+  const int lm = (lmax + 1) * (lmax + 1), lm2 = (2 * lmax + 1) * (2 * lmax + 1), N = nl * lm;
+  if (N > 256 || jmax < 0 || centre - jmax < 0 || centre + jmax >= nl) return SKKR_ERR_ARG;
+  const long long items = (long long)nk * nl * nl, NN = (long long)N * N;
+  std::vector<double> ik(2 * items), is(3 * items), coef(2 * (size_t)lm * lm * lm2);
+  for (int k = 0; k < nk; k++)
+    for (int a = 0; a < nl; a++)
+      for (int b = 0; b < nl; b++) {
+        const long long it = ((long long)k * nl + a) * nl + b;
+        ik[2 * it] = kxy[2 * k];
+        ik[2 * it + 1] = kxy[2 * k + 1];
+        for (int c = 0; c < 3; c++) is[3 * it + c] = pos[3 * a + c] - pos[3 * b + c];
+      }
+  CKR(skkr_gpu_kambe_coef(lmax, coef.data()));
+  Scoped s;
+  double *IK, *IS, *G, *R, *Cf, *KX, *PS;
+  zd *ALM, *AL, *Gs, *A, *X, *O;
+  CKR(s.alloc(&IK, ik.size()));
+  CKR(s.alloc(&IS, is.size()));
+  CKR(s.alloc(&G, 2 * (size_t)ng));
+  CKR(s.alloc(&R, 2 * (size_t)nr));
+  CKR(s.alloc(&Cf, coef.size()));
+  CKR(s.alloc(&KX, 2 * (size_t)nk));
+  CKR(s.alloc(&PS, 3 * (size_t)nl));
+  CKR(s.alloc(&ALM, (size_t)items * lm * lm));
+  CKR(s.alloc(&AL, (size_t)nl * (lmax + 1)));
+  CKR(s.alloc(&Gs, (size_t)nk * NN));
+  CKR(s.alloc(&A, (size_t)nk * NN));
+  CKR(s.alloc(&X, (size_t)nk * NN));
+  CKR(s.alloc(&O, (size_t)nk * (2 * jmax + 1) * lm * lm));
+  CK(cudaMemcpy(IK, ik.data(), ik.size() * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(IS, is.data(), is.size() * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(G, gvec, 2 * (size_t)ng * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(R, rvec, 2 * (size_t)nr * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(Cf, coef.data(), coef.size() * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(KX, kxy, 2 * (size_t)nk * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(PS, pos, 3 * (size_t)nl * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(AL, alpha, (size_t)nl * (lmax + 1) * sizeof(zd), cudaMemcpyHostToDevice));
+  launch_kambe_alm((int)items, e_re, e_im, IK, IS, lmax, G, ng, R, nr, area, factor, gcut, rcut, Cf, (double *)ALM, 0);
+  launch_slab_assemble(nk, nl, lm, ALM, KX, PS, AL, lmax + 1, Gs, A, 0);
+  launch_zgj(mref(A, NN, 0, N), N, nk, 1, nullptr, 0);
+  launch_zgemm(0, mref(Gs, NN, 0, N), mref(A, NN, 0, N), mref(X, NN, 0, N), mref(X, NN, 0, N), mref(X, NN, 0, N), N,
+               N, N, nk, 1, nullptr, 0);
+  launch_slab_extract(nk, nl, lm, centre, jmax, X, O, 0);
+  CK(cudaDeviceSynchronize());
+  CK(cudaGetLastError());
+  CK(cudaMemcpy(out, O, (size_t)nk * (2 * jmax + 1) * lm * lm * sizeof(zd), cudaMemcpyDeviceToHost));
+  return SKKR_OK;
+}

@@ -125,3 +125,10 @@ void launch_kambe_dlm(int nitem, double er, double ei, const double *kxy, const 
 void launch_kambe_alm(int nitem, double er, double ei, const double *kxy, const double *sep, int lmax,
                       const double *gvec, int ng, const double *rvec, int nr, double area, double factor,
                       double gcut, double rcut, const double *coef, double *out, cudaStream_t st);
+// slab screening of the reference's k-space form (kernels_kambe.cu):
+// G and A = 1 - alpha G per k from the layer-pair blocks, and the central
+// layer offsets of X = G A^-1
+void launch_slab_assemble(int nk, int nl, int lm, const zd *alm, const double *kxy, const double *pos,
+                          const zd *alpha, int nal, zd *G, zd *A, cudaStream_t st);
+void launch_slab_extract(int nk, int nl, int lm, int centre, int jmax, const zd *X, zd *out, cudaStream_t st);
+

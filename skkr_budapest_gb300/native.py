@@ -76,6 +76,7 @@ def lib():
         L.skkr_gpu_mlp_train.argtypes = [I, P, P, I, P, P, P, I, D, D, I, P, P, P]
         L.skkr_gpu_kambe_dlm.argtypes = [I, D, D, P, P, I, P, I, P, I, D, D, D, D, P]
         L.skkr_gpu_kambe_alm.argtypes = [I, D, D, P, P, I, P, I, P, I, D, D, D, D, P]
+        L.skkr_gpu_kambe_screened.argtypes = [I, D, D, P, I, P, P, I, P, I, P, I, D, D, D, D, I, I, P]
         L.skkr_gpu_layer_dos.argtypes = [I, I, I, P, I, P, P, I, P, P]
         L.skkr_gpu_set_reduce.argtypes = [P, P, P]
         L.skkr_gpu_set_mixed_policy.argtypes = [P, D, D, I, D]
@@ -279,6 +280,23 @@ def kambe_alm(e, kxy, sep, lmax, gvec, rvec, area, factor=1.0, gcut=12.0, rcut=4
                                     float(area), float(factor), float(gcut), float(rcut), _p(out)),
            "skkr_gpu_kambe_alm")
     return (out[:, 0::2] + 1j * out[:, 1::2]).reshape(len(kxy), lm, lm)
+
+
+def kambe_screened(e, kxy, pos, alpha, lmax, gvec, rvec, area, centre, jmax, factor=1.0, gcut=12.0, rcut=40.0):
+    """Device screened G_scr(k) of the reference's slab form
+    (skkr_gpu_kambe_screened); returns (nk, 2 jmax + 1, lmmax, lmmax)."""
+    kxy = np.ascontiguousarray(kxy, np.float64).reshape(-1, 2)
+    pos = np.ascontiguousarray(pos, np.float64).reshape(-1, 3)
+    al = np.ascontiguousarray(alpha, np.complex128).reshape(len(pos), lmax + 1)
+    g = np.ascontiguousarray(gvec, np.float64).reshape(-1, 2)
+    r = np.ascontiguousarray(rvec, np.float64).reshape(-1, 2)
+    lm = (lmax + 1) ** 2
+    out = np.zeros((len(kxy), 2 * jmax + 1, lm, lm), np.complex128)
+    e = complex(e)
+    _check(lib().skkr_gpu_kambe_screened(len(kxy), e.real, e.imag, _p(kxy), len(pos), _p(pos), _p(al), lmax, _p(g),
+                                         len(g), _p(r), len(r), float(area), float(factor), float(gcut), float(rcut),
+                                         int(centre), int(jmax), _p(out)), "skkr_gpu_kambe_screened")
+    return out
 
 
 REDUCE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.POINTER(C.c_double), C.c_longlong)

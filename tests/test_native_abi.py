@@ -166,3 +166,17 @@ def test_kambe_blocks_argument_checks_before_any_device_call():
     assert lib.skkr_gpu_kambe_alm(1, 0.5, 0.01, b, b, 4, b, 3, b, 3, 23.1, 1.0, 12.0, 40.0, b) == -1   # lmax 4
     assert lib.skkr_gpu_kambe_alm(0, 0.5, 0.01, b, b, 2, b, 3, b, 3, 23.1, 1.0, 12.0, 40.0, b) == -1   # no item
     assert lib.skkr_gpu_kambe_alm(1, 0.5, 0.01, b, b, 2, b, 0, b, 3, 23.1, 1.0, 12.0, 40.0, b) == -1   # no g
+
+
+def test_kambe_screened_argument_checks_before_any_device_call():
+    import numpy as np
+    import __graft_entry__
+    __graft_entry__.build()
+    lib = ctypes.CDLL(native.LIB_PATH)
+    D, I, P = ctypes.c_double, ctypes.c_int, ctypes.c_void_p
+    lib.skkr_gpu_kambe_screened.argtypes = [I, D, D, P, I, P, P, I, P, I, P, I, D, D, D, D, I, I, P]
+    b = np.zeros(256).ctypes.data
+    # 17 layers of lmax 3 exceed the 256-row inverse; the centre must leave jmax layers on each side
+    assert lib.skkr_gpu_kambe_screened(1, 0.5, 0.01, b, 17, b, b, 3, b, 3, b, 3, 23.1, 1.0, 12.0, 40.0, 8, 2, b) == -1
+    assert lib.skkr_gpu_kambe_screened(1, 0.5, 0.01, b, 8, b, b, 2, b, 3, b, 3, 23.1, 1.0, 12.0, 40.0, 1, 2, b) == -1
+    assert lib.skkr_gpu_kambe_screened(1, 0.5, 0.01, b, 8, b, b, 2, b, 3, b, 3, 23.1, 1.0, 12.0, 40.0, 6, 2, b) == -1
