@@ -284,3 +284,41 @@ SKKR_HD inline void kambe_alm(const fcplx *d, int lmax, const double *coef, fcpl
       out[a * lm + b] = s;
     }
 }
+
+// element e of the slab matrices of one batch (column-major N x N per k,
+// N = nl lm): G[(a,L),(b,L')] = e^{ik.(pos_b - pos_a)} alm[k][a][b][L][L'],
+// A = 1 - alpha[a][l(L)] G; alm, alpha, G, A complex (re, im interleaved)
+SKKR_HD inline void kambe_slab_elem(long long e, int nl, int lm, const double *alm, const double *kxy,
+                                    const double *pos, const double *alpha, int nal, double *G, double *A) {
+  const int N = nl * lm;
+  const long long NN = (long long)N * N;
+  const int k = (int)(e / NN);
+  const long long rem = e - (long long)k * NN;
+  const int col = (int)(rem / N), row = (int)(rem - (long long)col * N);
+  const int a = row / lm, L = row - a * lm, b = col / lm, Lp = col - b * lm;
+  int l = 0;
+  while ((l + 1) * (l + 1) <= L) l++;
+  const long long iv = ((((long long)k * nl + a) * nl + b) * lm + L) * lm + Lp;
+  const double ph = kxy[2 * k] * (pos[3 * b] - pos[3 * a]) + kxy[2 * k + 1] * (pos[3 * b + 1] - pos[3 * a + 1]);
+  const fcplx g = fmulc(fc(alm[2 * iv], alm[2 * iv + 1]), fc(cos(ph), sin(ph)));
+  const fcplx al = fc(alpha[2 * (a * nal + l)], alpha[2 * (a * nal + l) + 1]);
+  fcplx m = fneg(fmulc(al, g));
+  if (row == col) m.re += 1.0;
+  G[2 * e] = g.re;
+  G[2 * e + 1] = g.im;
+  A[2 * e] = m.re;
+  A[2 * e + 1] = m.im;
+}
+
+// element e of out[k][j][L][L'] = X[k][(centre, L), (centre + j - jmax, L')]
+SKKR_HD inline void kambe_slab_extract_elem(long long e, int nl, int lm, int centre, int jmax, const double *X,
+                                            double *out) {
+  const int N = nl * lm, nj = 2 * jmax + 1;
+  const int Lp = (int)(e % lm), L = (int)((e / lm) % lm), j = (int)((e / ((long long)lm * lm)) % nj);
+  const int k = (int)(e / ((long long)lm * lm * nj));
+  const int row = centre * lm + L, col = (centre + j - jmax) * lm + Lp;
+  const long long ix = (long long)k * N * N + row + (long long)col * N;
+  out[2 * e] = X[2 * ix];
+  out[2 * e + 1] = X[2 * ix + 1];
+}
+

@@ -40,46 +40,24 @@ __global__ void k_kambe_alm(int nitem, double er, double ei, const double *__res
   }
 }
 
-// the slab of nl layers per k point, column-major N x N (N = nl lm):
-// G[(a,L),(b,L')] = e^{ik.(pos_b - pos_a)} alm[k][a][b][L][L'] and
-// A = 1 - alpha G (alpha of row layer a and l(L))
+// the slab of nl layers per k point and its 1 - alpha G (kambe_slab_elem)
 __global__ void k_slab_assemble(int nk, int nl, int lm, const zd *__restrict__ alm, const double *__restrict__ kxy,
                                 const double *__restrict__ pos, const zd *__restrict__ alpha, int nal,
                                 zd *__restrict__ G, zd *__restrict__ A) {
-  const int N = nl * lm;
-  const long long NN = (long long)N * N, tot = (long long)nk * NN;
+  const long long tot = (long long)nk * nl * lm * nl * lm;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < tot;
-       e += (long long)gridDim.x * blockDim.x) {
-    const int k = (int)(e / NN);
-    const long long rem = e - (long long)k * NN;
-    const int col = (int)(rem / N), row = (int)(rem - (long long)col * N);
-    const int a = row / lm, L = row - a * lm, b = col / lm, Lp = col - b * lm;
-    int l = 0;
-    while ((l + 1) * (l + 1) <= L) l++;
-    const zd v = alm[((((long long)k * nl + a) * nl + b) * lm + L) * lm + Lp];
-    const double ph = kxy[2 * k] * (pos[3 * b] - pos[3 * a]) + kxy[2 * k + 1] * (pos[3 * b + 1] - pos[3 * a + 1]);
-    double sn, cs;
-    sincos(ph, &sn, &cs);
-    const zd g = zmul(v, zmk(cs, sn));
-    G[e] = g;
-    zd m = zscale(-1.0, zmul(alpha[a * nal + l], g));
-    if (row == col) m.x += 1.0;
-    A[e] = m;
-  }
+       e += (long long)gridDim.x * blockDim.x)
+    kambe_slab_elem(e, nl, lm, (const double *)alm, kxy, pos, (const double *)alpha, nal, (double *)G,
+                    (double *)A);
 }
 
-// out[k][j][L][L'] = X[k][(centre, L), (centre + j - jmax, L')]
+// the central layer offsets (kambe_slab_extract_elem)
 __global__ void k_slab_extract(int nk, int nl, int lm, int centre, int jmax, const zd *__restrict__ X,
                                zd *__restrict__ out) {
-  const int N = nl * lm, nj = 2 * jmax + 1;
-  const long long tot = (long long)nk * nj * lm * lm;
+  const long long tot = (long long)nk * (2 * jmax + 1) * lm * lm;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < tot;
-       e += (long long)gridDim.x * blockDim.x) {
-    const int Lp = (int)(e % lm), L = (int)((e / lm) % lm), j = (int)((e / ((long long)lm * lm)) % nj);
-    const int k = (int)(e / ((long long)lm * lm * nj));
-    const int row = centre * lm + L, col = (centre + j - jmax) * lm + Lp;
-    out[e] = X[(long long)k * N * N + row + (long long)col * N];
-  }
+       e += (long long)gridDim.x * blockDim.x)
+    kambe_slab_extract_elem(e, nl, lm, centre, jmax, (const double *)X, (double *)out);
 }
 
 }  // namespace

@@ -24,3 +24,14 @@ extern "C" void kambe_alm_eval(double er, double ei, double kx, double ky, doubl
     out[2 * i + 1] = g[i].im;
   }
 }
+
+extern "C" void slab_assemble_eval(int nk, int nl, int lm, const double *alm, const double *kxy, const double *pos,
+                                   const double *alpha, int nal, double *G, double *A) {
+  const long long tot = (long long)nk * nl * lm * nl * lm;
+  for (long long e = 0; e < tot; e++) kambe_slab_elem(e, nl, lm, alm, kxy, pos, alpha, nal, G, A);
+}
+
+extern "C" void slab_extract_eval(int nk, int nl, int lm, int centre, int jmax, const double *X, double *out) {
+  const long long tot = (long long)nk * (2 * jmax + 1) * lm * lm;
+  for (long long e = 0; e < tot; e++) kambe_slab_extract_elem(e, nl, lm, centre, jmax, X, out);
+}

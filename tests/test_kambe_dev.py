@@ -83,3 +83,58 @@ def test_library_coefficient_table_equals_the_oracle(lmax):
     got = (out[0::2] + 1j * out[1::2]).reshape(lm, lm, lm2)
     assert np.abs(got - K.alm_coef(lmax)).max() < 1e-13
     assert L.skkr_gpu_kambe_coef(4, out.ctypes.data) == -1
+
+
+def test_slab_chain_of_the_device_entry_point(lib):
+    # the element functions of k_slab_assemble / k_slab_extract (the same
+    # header) with the host-built blocks; numpy stands in for the batched
+    # Gauss-Jordan and GEMM the entry point runs between them
+    from skkr_budapest_gb300 import native
+    from skkr_budapest_gb300 import synth as S
+    from skkr_budapest_gb300 import workloads as W
+    D, I, P = ctypes.c_double, ctypes.c_int, ctypes.c_void_p
+    lib.kambe_alm_eval.argtypes = [D, D, D, D, D, D, D, I, P, I, P, I, D, D, D, P, P]
+    lib.slab_assemble_eval.argtypes = [I, I, I, P, P, P, P, I, P, P]
+    lib.slab_extract_eval.argtypes = [I, I, I, I, I, P, P]
+    spec = W.plain_fcc(nset=4)
+    st = spec.stacking
+    lat = K.Lattice2D([st.a2d, 0.0], [0.0, st.a2d])
+    _, _, dnn = S.cluster(st, 1)
+    ce = complex(spec.energies[8])
+    lmax = spec.lmax
+    al = S.alpha_sqwell(ce, 4.0, 0.5 * dnn, lmax)
+    nl, centre, jmax = 6, 3, 2
+    lm, lm2 = (lmax + 1) ** 2, (2 * lmax + 1) ** 2
+    pos = np.ascontiguousarray([st.site(n, 0, 0) for n in range(nl)], np.float64)
+    kpts = np.ascontiguousarray([(0.31, 0.12), (0.5, 0.2)], np.float64)
+    Lb = ctypes.CDLL(native.LIB_PATH)
+    Lb.skkr_gpu_kambe_coef.argtypes = [I, P]
+    coef = np.zeros(2 * lm * lm * lm2)
+    Lb.skkr_gpu_kambe_coef(lmax, coef.ctypes.data)
+    g = np.ascontiguousarray(lat.gvecs(14.0))
+    r = np.ascontiguousarray(lat.rvecs(55.0))
+    alm = np.zeros((len(kpts), nl, nl, lm, lm), complex)
+    for ik, k in enumerate(kpts):
+        for a in range(nl):
+            for b in range(nl):
+                out = np.zeros(2 * lm * lm)
+                s = pos[a] - pos[b]
+                lib.kambe_alm_eval(ce.real, ce.imag, k[0], k[1], *s, lmax, g.ctypes.data, len(g), r.ctypes.data,
+                                   len(r), lat.area, 12.0, 40.0, coef.ctypes.data, out.ctypes.data)
+                alm[ik, a, b] = (out[0::2] + 1j * out[1::2]).reshape(lm, lm)
+    alm = np.ascontiguousarray(alm)
+    alpha = np.ascontiguousarray(np.array([al] * nl, complex))
+    N = nl * lm
+    G = np.zeros((len(kpts), N, N), complex)
+    A = np.zeros_like(G)
+    lib.slab_assemble_eval(len(kpts), nl, lm, alm.ctypes.data, kpts.ctypes.data, pos.ctypes.data,
+                           alpha.ctypes.data, lmax + 1, G.ctypes.data, A.ctypes.data)
+    # the buffers are column-major per k: transpose to (row, col)
+    G, A = G.transpose(0, 2, 1), A.transpose(0, 2, 1)
+    X = np.ascontiguousarray(np.array([Gk @ np.linalg.inv(Ak) for Gk, Ak in zip(G, A)]).transpose(0, 2, 1))
+    out = np.zeros((len(kpts), 2 * jmax + 1, lm, lm), complex)
+    lib.slab_extract_eval(len(kpts), nl, lm, centre, jmax, X.ctypes.data, out.ctypes.data)
+    for ik, k in enumerate(kpts):
+        gs = K.screened_slab(ce, k[0], k[1], lmax, pos, [al] * nl, lat)
+        ref = np.array([gs[centre, centre + j] for j in range(-jmax, jmax + 1)])
+        assert np.abs(out[ik] - ref).max() < 1e-10 * np.abs(ref).max()
