@@ -5,6 +5,7 @@
 // reduction runs in a fixed order, so results do not depend on scheduling.
 #include "common.cuh"
 #include "kernels.h"
+#include "mlp_dev.cuh"
 
 namespace {
 
@@ -22,14 +23,8 @@ __global__ void k_mlp_dense(const double *__restrict__ H, int n, int din, const 
                             const double *__restrict__ b, int dout, int act, double *__restrict__ A) {
   const long long m = (long long)n * dout;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < m;
-       e += (long long)gridDim.x * blockDim.x) {
-    const long long r = e / dout;
-    const int j = (int)(e - r * dout);
-    const double *h = H + r * din;
-    double s = b[j];
-    for (int i = 0; i < din; i++) s = fma(h[i], W[(long long)i * dout + j], s);
-    A[e] = act ? tanh(s) : s;
-  }
+       e += (long long)gridDim.x * blockDim.x)
+    mlp_dense_elem(e, H, din, W, b, dout, act, A);
 }
 
 // per row: squared error over the outputs for the rows the selection keeps
@@ -37,17 +32,8 @@ __global__ void k_mlp_dense(const double *__restrict__ H, int n, int din, const 
 __global__ void k_mlp_loss_rows(const double *__restrict__ Yh, const double *__restrict__ Y,
                                 const unsigned char *__restrict__ sel, int want, int n, int dout, double scale,
                                 double *__restrict__ dY, double *__restrict__ rowsum) {
-  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
-    const bool on = sel ? (sel[r] == want) : true;
-    double s = 0.0;
-    for (int j = 0; j < dout; j++) {
-      const long long e = (long long)r * dout + j;
-      const double d = Yh[e] - Y[e];
-      s = fma(d, d, s);
-      if (dY) dY[e] = on ? scale * 2.0 * d : 0.0;
-    }
-    rowsum[r] = on ? s : 0.0;
-  }
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x)
+    mlp_loss_row(r, Yh, Y, sel, want, dout, scale, dY, rowsum);
 }
 
 // out[0] = scale * sum v[0..n): one block, each thread a strided subset in
@@ -68,10 +54,8 @@ __global__ void k_mlp_sum(const double *__restrict__ v, int n, double scale, dou
 // G *= 1 - A^2 (tanh layer)
 __global__ void k_mlp_tanh_back(const double *__restrict__ A, double *__restrict__ G, long long m) {
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < m;
-       e += (long long)gridDim.x * blockDim.x) {
-    const double a = A[e];
-    G[e] *= 1.0 - a * a;
-  }
+       e += (long long)gridDim.x * blockDim.x)
+    mlp_tanh_back_elem(e, A, G);
 }
 
 // g[p][j] = sum_r H[r][p] dZ[r][j] for p < din (dW), g[din][j] = sum_r dZ[r][j]
@@ -80,16 +64,8 @@ __global__ void k_mlp_wgrad(const double *__restrict__ H, const double *__restri
                             int dout, double *__restrict__ g) {
   const long long m = (long long)(din + 1) * dout;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < m;
-       e += (long long)gridDim.x * blockDim.x) {
-    const int p = (int)(e / dout), j = (int)(e - (long long)p * dout);
-    double s = 0.0;
-    if (p < din) {
-      for (int r = 0; r < n; r++) s = fma(H[(long long)r * din + p], dZ[(long long)r * dout + j], s);
-    } else {
-      for (int r = 0; r < n; r++) s += dZ[(long long)r * dout + j];
-    }
-    g[e] = s;
-  }
+       e += (long long)gridDim.x * blockDim.x)
+    mlp_wgrad_elem(e, H, dZ, n, din, dout, g);
 }
 
 // dH[r][p] = sum_j dZ[r][j] W[p][j]
@@ -97,15 +73,8 @@ __global__ void k_mlp_hgrad(const double *__restrict__ dZ, const double *__restr
                             int dout, double *__restrict__ dH) {
   const long long m = (long long)n * din;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < m;
-       e += (long long)gridDim.x * blockDim.x) {
-    const long long r = e / din;
-    const int p = (int)(e - r * din);
-    const double *dz = dZ + r * dout;
-    const double *w = W + (long long)p * dout;
-    double s = 0.0;
-    for (int j = 0; j < dout; j++) s = fma(dz[j], w[j], s);
-    dH[e] = s;
-  }
+       e += (long long)gridDim.x * blockDim.x)
+    mlp_hgrad_elem(e, dZ, W, din, dout, dH);
 }
 
 // one AdamW step (decoupled weight decay, bias-corrected moments):
@@ -115,15 +84,8 @@ __global__ void k_mlp_adamw(double *__restrict__ p, const double *__restrict__ g
                             double *__restrict__ v, long long np, double lr, double wd, double b1, double b2,
                             double eps, double step_size, double bc2_sqrt) {
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < np;
-       e += (long long)gridDim.x * blockDim.x) {
-    const double ge = g[e];
-    double pe = p[e] * (1.0 - lr * wd);
-    double me = m[e] + (1.0 - b1) * (ge - m[e]);
-    double ve = v[e] * b2 + (1.0 - b2) * ge * ge;
-    m[e] = me;
-    v[e] = ve;
-    p[e] = pe + (-step_size) * (me / (sqrt(ve) / bc2_sqrt + eps));
-  }
+       e += (long long)gridDim.x * blockDim.x)
+    mlp_adamw_elem(e, p, g, m, v, lr, wd, b1, b2, eps, step_size, bc2_sqrt);
 }
 
 // keep the parameters of the lowest held-out loss: one block; the decision

@@ -86,3 +86,42 @@ def test_train_keeps_the_best_held_out_epoch():
             vals[ep] = M.loss_grad(cur, x, y, held)[0]
     assert abs(bv - min(vals.values())) < 1e-15
     assert np.array_equal(final[0][0], cur[0][0])
+
+
+def test_device_element_logic_on_the_host(tmp_path):
+    # mlp_dev.cuh (the bodies of the device kernels) compiled for the host and
+    # driven like skkr_gpu_mlp_grad: the loss and packed gradient equal the
+    # reference's, and one AdamW step equals the reference's step
+    import ctypes
+    import os
+    import subprocess
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    so = str(tmp_path / "libmlp.so")
+    subprocess.run(["g++", "-O2", "-shared", "-fPIC", "-o", so, os.path.join(root, "tests", "harness", "mlp_host.cpp")],
+                   check=True)
+    L = ctypes.CDLL(so)
+    P, I, D = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+    L.mlp_grad_eval.argtypes = [I, P, P, I, P, P, P, P, P]
+    L.mlp_adamw_eval.argtypes = [ctypes.c_longlong, P, P, P, P, D, D, D, D]
+    rng = np.random.default_rng(8)
+    dims = [19, 32, 32, 14]
+    layers = _net(rng, dims)
+    x, y = rng.normal(size=(90, 19)), rng.normal(size=(90, 14))
+    rows = (rng.random(90) < 0.8).astype(np.uint8)
+    d = np.array(dims, np.int32)
+    params = np.concatenate([np.concatenate([w.ravel(), b]) for w, b in layers])
+    grad = np.zeros_like(params)
+    loss = np.zeros(1)
+    L.mlp_grad_eval(3, d.ctypes.data, params.ctypes.data, 90, x.ctypes.data, y.ctypes.data, rows.ctypes.data,
+                    loss.ctypes.data, grad.ctypes.data)
+    lr_, gr = M.loss_grad(layers, x, y, rows)
+    ref = np.concatenate([np.concatenate([gw.ravel(), gb]) for gw, gb in gr])
+    assert abs(loss[0] - lr_) < 1e-14 * lr_
+    assert np.abs(grad - ref).max() < 1e-13 * np.abs(ref).max()
+    m, v, p = np.zeros_like(params), np.zeros_like(params), params.copy()
+    bc1, bc2 = 1 - 0.9, 1 - 0.999
+    L.mlp_adamw_eval(len(p), p.ctypes.data, grad.ctypes.data, m.ctypes.data, v.ctypes.data, 2e-3, 1e-4, 2e-3 / bc1,
+                     np.sqrt(bc2))
+    step = M.AdamW(layers, 2e-3, 1e-4).step(layers, gr)
+    refp = np.concatenate([np.concatenate([w.ravel(), b]) for w, b in step])
+    assert np.abs(p - refp).max() < 1e-13 * np.abs(refp).max()
