@@ -104,6 +104,11 @@ typedef struct {
   long long k_fp64;           /* mixed precision: k points redone in FP64 (dominant contributions) */
   long long inv_refined;      /* mixed precision: inverses that took further Newton steps (residual
                                  above 1e-6 after the standard steps, below 1/2) */
+  double alg_flops;           /* FP64-equivalent algorithmic work of the call in the reference's
+                                 operation count, U = 8 n_PL^3 real FLOP per block operation:
+                                 (9 it + 3) U per lead decimation of `it` iterations (surfgf.f,
+                                 dugo.f) and (7 nprc - 6) U per tau2d item (tau2d.f) on every
+                                 CPA iteration; the precision guards' FP64 redos are not counted */
 } skkr_status;
 
 typedef struct skkr_ctx skkr_ctx;
@@ -254,10 +259,13 @@ int skkr_gpu_fetch_slot(skkr_ctx *ctx, int slot, double *tminv, double *tauc,
                         double *taua, double *taub, int ld);
 
 /* Per-kernel-class timing with CUDA events (process wide).  enable=1 resets
- * and starts; enable=0 stops and writes out[cls*3 + {launches, total ms,
- * algorithmic work}] for cls = 0 FP64 complex GEMM (FLOP), 1 Gauss-Jordan
- * inverse (FP64-equivalent FLOP), 2 G(k) transform (bytes written), 3 other,
- * 4 sliced complex GEMM on the tensor cores (BF16 FLOP). */
+ * and starts; enable=0 stops and writes out[cls*4 + {launches, total ms,
+ * work, FP64-equivalent algorithmic work}] (5 x 4 doubles) for cls = 0 FP64
+ * complex GEMM (FLOP), 1 Gauss-Jordan inverse (8 n^3 FLOP per inverse), 2 G(k)
+ * transform (bytes written), 3 other (bytes), 4 sliced complex GEMM on the
+ * tensor cores (work: BF16 FLOP of every slice pair; FP64-equivalent: 8 n^2 K
+ * per complex product).  The events add a gap around every launch: time
+ * throughput with the statistics off. */
 int skkr_gpu_kernel_stats(int enable, double *out);
 
 /* Screened -> physical tau of one layer on the device
@@ -368,10 +376,14 @@ int skkr_gpu_surfgf_batch(int n, int batch, const double *ml, const double *m0,
  * of SKKR_NOALLOC_SCRATCH_BYTES (32 MiB, held by every GPU that loads the
  * library until the process exits).  A request needing more than
  * batch * (8 * n * n * 16 + 20) + 64 > SKKR_NOALLOC_SCRATCH_BYTES bytes is
- * rejected with SKKR_ERR_NOMEM before anything runs.  The first call on each
- * device looks up the array's device address (cudaGetSymbolAddress); make
- * that first call before any stream capture.  All calls share the one array:
- * calls that overlap on the GPU (several streams or host threads) race. */
+ * rejected with SKKR_ERR_NOMEM, and batch > 65535 with SKKR_ERR_ARG, before
+ * anything runs.  The first call on each device looks up the array's device
+ * address (cudaGetSymbolAddress); make that first call before any stream
+ * capture.  After every decimation iteration the call reads the number of
+ * items still iterating from the device, synchronizing `stream`, and it
+ * returns after a final synchronization, with x, iters and stat written.
+ * All calls share the one array: calls that overlap on the GPU (several
+ * streams or host threads) race. */
 #define SKKR_NOALLOC_SCRATCH_BYTES (32u << 20)
 int skkr_gpu_surfgf_batch_noalloc(int n, int batch, const double *ml,
                                   const double *m0, const double *mr,

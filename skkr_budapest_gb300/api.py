@@ -187,7 +187,7 @@ class Context:
                    max_dec_iters=st.max_dec_iters, dec_iters_total=st.dec_iters_total,
                    gpu_launches=st.gpu_launches, ik=st.ik, run_ms=st.run_ms,
                    max_refine_resid=st.max_refine_resid, inv_fallbacks=st.inv_fallbacks, k_fp64=st.k_fp64,
-                   inv_refined=st.inv_refined,
+                   inv_refined=st.inv_refined, alg_flops=st.alg_flops,
                    h2d_bytes=sum(v.nbytes for v in a.values()) + rt.gR.nbytes + rt.rvec.nbytes,
                    d2h_bytes=sum(v.nbytes for v in out.values()))
         return res
@@ -273,7 +273,7 @@ def cpacoord_many(eps, precision="fp64", check=True, slices=0, contexts=None):
             r["tminv"] = N.uncm(a["ti"])
             r.update(status=st.code, cpa_iterations=st.cpa_iterations, cpa_error=st.cpa_error,
                      max_dec_iters=st.max_dec_iters, dec_iters_total=st.dec_iters_total,
-                     gpu_launches=st.gpu_launches, run_ms=st.run_ms)
+                     gpu_launches=st.gpu_launches, run_ms=st.run_ms, alg_flops=st.alg_flops)
             res.append(r)
         return res
     finally:

@@ -52,7 +52,7 @@ struct KStats {
   std::vector<cudaEvent_t> ev;
   size_t used = 0;
   std::vector<int> cls;
-  std::vector<double> work;
+  std::vector<double> work, work2;
   std::vector<char> done;   // end event recorded
 };
 KStats g_ks;
@@ -63,7 +63,7 @@ thread_local long long g_ks_open = -1;
 void skkr_set_active_items(long long n) { g_active_hint = n; }
 long long skkr_active_items(long long all) { return g_active_hint >= 0 ? g_active_hint : all; }
 
-void kstat_begin(int cls, double work, cudaStream_t st) {
+void kstat_begin2(int cls, double work, double work2, cudaStream_t st) {
   if (!g_ks.on) return;
   std::lock_guard<std::mutex> lk(g_ks.mu);
   if (!g_ks.on) return;
@@ -78,9 +78,12 @@ void kstat_begin(int cls, double work, cudaStream_t st) {
   cudaEventRecord(g_ks.ev[g_ks.used], st);
   g_ks.cls.push_back(cls);
   g_ks.work.push_back(work);
+  g_ks.work2.push_back(work2);
   g_ks.done.push_back(0);
   g_ks.used += 2;
 }
+
+void kstat_begin(int cls, double work, cudaStream_t st) { kstat_begin2(cls, work, work, st); }
 
 void kstat_end(cudaStream_t st) {
   if (g_ks_open < 0) return;
@@ -92,8 +95,9 @@ void kstat_end(cudaStream_t st) {
   g_ks_open = -1;
 }
 
-// enable=1: reset and start; enable=0: stop and report out[cls*3 + {0 launches,
-// 1 total ms, 2 total algorithmic work}] for the KS_NCLS classes.
+// enable=1: reset and start; enable=0: stop and report out[cls*4 + {0 launches,
+// 1 total ms, 2 total work, 3 total FP64-equivalent algorithmic work}] for the
+// KS_NCLS classes.
 extern "C" int skkr_gpu_kernel_stats(int enable, double *out) {
   std::lock_guard<std::mutex> lk(g_ks.mu);
   if (enable) {
@@ -101,21 +105,23 @@ extern "C" int skkr_gpu_kernel_stats(int enable, double *out) {
     g_ks.used = 0;
     g_ks.cls.clear();
     g_ks.work.clear();
+    g_ks.work2.clear();
     g_ks.done.clear();
     return SKKR_OK;
   }
   g_ks.on = 0;
   CK(cudaDeviceSynchronize());
   if (out)
-    for (int i = 0; i < KS_NCLS * 3; i++) out[i] = 0.0;
+    for (int i = 0; i < KS_NCLS * 4; i++) out[i] = 0.0;
   for (size_t i = 0; i < g_ks.cls.size() && 2 * i + 1 < g_ks.used; i++) {
     if (!g_ks.done[i]) continue;
     float ms = 0.f;
     CK(cudaEventElapsedTime(&ms, g_ks.ev[2 * i], g_ks.ev[2 * i + 1]));
     if (out) {
-      out[g_ks.cls[i] * 3 + 0] += 1.0;
-      out[g_ks.cls[i] * 3 + 1] += ms;
-      out[g_ks.cls[i] * 3 + 2] += g_ks.work[i];
+      out[g_ks.cls[i] * 4 + 0] += 1.0;
+      out[g_ks.cls[i] * 4 + 1] += ms;
+      out[g_ks.cls[i] * 4 + 2] += g_ks.work[i];
+      out[g_ks.cls[i] * 4 + 3] += g_ks.work2[i];
     }
   }
   return SKKR_OK;
@@ -235,6 +241,7 @@ struct skkr_ctx {
   double max_resid = 0.0;    // largest accepted Newton residual seen in this run
   long long inv_fallbacks = 0;  // inverses redone in FP64 in this run
   long long inv_refined = 0;    // inverses that took further Newton steps in this run
+  double alg_units = 0.0;       // reference block operations (8 n^3 FLOP each) of this run
 };
 
 // Inputs and outputs of one staged energy.  A context keeps any number of
@@ -1452,6 +1459,7 @@ extern "C" int skkr_gpu_run(skkr_ctx *c, skkr_status *status) {
   c->first_bad_k = -1;
   c->max_resid = 0.0;
   c->k_fp64 = 0;
+  c->alg_units = 0.0;
   CKR(c->knorm.ensure((size_t)nk * sizeof(double)));
   if (c->sz.precision == SKKR_MIXED && !c->mw) {
     c->mw = mixed_create();
@@ -1516,9 +1524,16 @@ extern "C" int skkr_gpu_run(skkr_ctx *c, skkr_status *status) {
       launch_pack(c->G.as<zd>() + (size_t)k0 * c->nbk * bs, c->nblk, c->nbk, c->blkmap_d.as<int>(),
                   c->mi, c->jmax, c->jobs.as<PackJob>(), c->nmat, lk, c->lmmax, c->sz.mode, c->fac,
                   c->fach, nkc, c->pool.as<zd>(), c->nmat, n, ehsplit(c), st);
-      if (itcpa == 1) CKR(run_decimation(c, k0, nkc, lcls, rcls));
+      if (itcpa == 1) {
+        const long long d0 = c->tot_dec;
+        CKR(run_decimation(c, k0, nkc, lcls, rcls));
+        // surfgf.f: 1 inverse + 4 triple products per iteration; dugo.f: the
+        // final inverse and tripmt2
+        c->alg_units += 9.0 * (double)(c->tot_dec - d0) + 3.0 * nkc * (double)(lcls.size() + rcls.size());
+      }
       if (c->err_code) break;
       CKR(run_tau2d(c, k0, nkc, icls));
+      c->alg_units += (7.0 * c->nprc - 6.0) * nkc * (double)ncls;  // tau2d.f per item
       launch_ksum(c->tauk.as<zd>(), nkc, (long long)ncls * ni * lk2, c->S.as<zd>(), k0 > 0, st);
       if (c->sz.precision == SKKR_MIXED && c->dominant_frac > 0.0)
         launch_knorm(c->tauk.as<zd>(), nkc, (long long)ncls * ni * lk2, c->knorm.as<double>() + k0, st);
@@ -1595,6 +1610,7 @@ extern "C" int skkr_gpu_run(skkr_ctx *c, skkr_status *status) {
     status->inv_fallbacks = c->inv_fallbacks;
     status->inv_refined = c->inv_refined;
     status->k_fp64 = c->k_fp64;
+    status->alg_flops = c->alg_units * 8.0 * (double)n * n * n;
   }
   return c->err_code;
 }

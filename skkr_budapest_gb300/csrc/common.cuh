@@ -81,6 +81,9 @@ void skkr_after_launch(const char *file, int line);
 // active items the host announced through skkr_set_active_items (-1: all).
 enum { KS_GEMM = 0, KS_GJ = 1, KS_GKFT = 2, KS_OTHER = 3, KS_OZAKI = 4, KS_NCLS = 5 };
 void kstat_begin(int cls, double work, cudaStream_t st);
+// work2: the FP64-equivalent algorithmic count of the launch where it differs
+// from `work` (a sliced product: one complex product, 8 n^2 K FLOP per item)
+void kstat_begin2(int cls, double work, double work2, cudaStream_t st);
 void kstat_end(cudaStream_t st);
 long long skkr_active_items(long long all);
 void skkr_set_active_items(long long n);

@@ -1002,7 +1002,9 @@ static int gemm_s(MixedWork *w, int mode, int sa, int sb, const MatRef &C, const
   g.err = w->err;
   const long long active = act ? skkr_active_items(items) : items;
   // algorithmic BF16 tensor work: S(S+1)/2 real products of n x 2K x 2n per item
-  kstat_begin(KS_OZAKI, (double)(S * (S + 1) / 2) * 8.0 * n * (double)n * K * (double)active, st);
+  // FP64-equivalent: one complex n x K by K x n product per item
+  kstat_begin2(KS_OZAKI, (double)(S * (S + 1) / 2) * 8.0 * n * (double)n * K * (double)active,
+               8.0 * n * (double)n * K * (double)active, st);
   dim3 grid(mtiles * ntiles, items);
   k_ozaki<S, TN, NA><<<grid, OZ_THREADS, smem, st>>>(ma, mb, g);
   kstat_end(st);

@@ -8,28 +8,31 @@
 // outputs; the work matrices this routine needs live in one file-scope
 // device array of fixed size (SKKR_NOALLOC_SCRATCH_BYTES), which every GPU
 // that loads the library holds until the process exits.
+#include <atomic>
+
 #include "../../include/skkr_gpu.h"
 #include "kernels.h"
 
 static __device__ __align__(256) unsigned char g_sgf_scratch[SKKR_NOALLOC_SCRATCH_BYTES];
 
-// Device address of g_sgf_scratch per device ordinal.  In host code the name
-// g_sgf_scratch is only a host-side stand-in, never a device pointer.
-static void *g_scratch_addr[128];
-static int g_scratch_ready[128];
+// Device address of g_sgf_scratch per device ordinal, looked up by the first
+// call on that device (with the device current) and kept.  In host code the
+// name g_sgf_scratch is only a host-side stand-in, never a device pointer.
+// Calls may come from several host threads: the cached address is atomic
+// (two threads that both find it empty look up the same value).
+static std::atomic<void *> g_scratch_addr[128];
 
 static int scratch_address(void **out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess || dev < 0 || dev >= 128) return SKKR_ERR_CUDA;
-  if (!g_scratch_ready[dev]) {
-    void *p = nullptr;
+  void *p = g_scratch_addr[dev].load(std::memory_order_acquire);
+  if (!p) {
     e = cudaGetSymbolAddress(&p, g_sgf_scratch);
     if (e != cudaSuccess || !p) return SKKR_ERR_CUDA;
-    g_scratch_addr[dev] = p;
-    g_scratch_ready[dev] = 1;
+    g_scratch_addr[dev].store(p, std::memory_order_release);
   }
-  *out = g_scratch_addr[dev];
+  *out = p;
   return SKKR_OK;
 }
 
@@ -66,7 +69,8 @@ __global__ void k_noalloc_count(const int *act, int nb, int *count) {
 extern "C" int skkr_gpu_surfgf_batch_noalloc(int n, int batch, const double *ml, const double *m0,
                                              const double *mr, double *x, int ld, int itermax,
                                              double errmax, int *iters, int *stat, void *stream) {
-  if (n < 1 || n > 256 || batch < 1 || !ml || !m0 || !mr || !x || ld < n || itermax < 1)
+  // the batched kernels put the item index in grid.y (at most 65535)
+  if (n < 1 || n > 256 || batch < 1 || batch > 65535 || !ml || !m0 || !mr || !x || ld < n || itermax < 1)
     return SKKR_ERR_ARG;
   const size_t MB = (size_t)n * n;
   // scratch: 8 work matrices per item, then err[batch], act/stat/iters[batch], count
@@ -114,7 +118,9 @@ extern "C" int skkr_gpu_surfgf_batch_noalloc(int n, int batch, const double *ml,
     NA_CK(cudaStreamSynchronize(st));
     active = h;
     skkr_set_active_items(active);
-    if (h == 0 || iter > itermax + 1) break;
+    // k_dec_state retires every item once iter > itermax, so the count
+    // reaches zero by iteration itermax + 1 at the latest
+    if (h == 0) break;
   }
   skkr_set_active_items(-1);
   launch_zgj(X, n, batch, 1, nullptr, st);

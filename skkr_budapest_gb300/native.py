@@ -39,7 +39,7 @@ class Status(C.Structure):
                 ("max_dec_iters", I), ("dec_iters_total", C.c_longlong),
                 ("gpu_launches", C.c_longlong), ("max_refine_resid", D), ("run_ms", D),
                 ("inv_fallbacks", C.c_longlong), ("k_fp64", C.c_longlong),
-                ("inv_refined", C.c_longlong)]
+                ("inv_refined", C.c_longlong), ("alg_flops", D)]
 
 
 class SkkrError(RuntimeError):
@@ -337,9 +337,10 @@ def kernel_stats_start():
 
 
 def kernel_stats_stop():
-    out = np.zeros(3 * len(KSTAT_CLASSES))
+    out = np.zeros(4 * len(KSTAT_CLASSES))
     _check(lib().skkr_gpu_kernel_stats(0, _p(out)), "skkr_gpu_kernel_stats")
-    return {name: dict(launches=int(out[3 * i]), ms=float(out[3 * i + 1]), work=float(out[3 * i + 2]))
+    return {name: dict(launches=int(out[4 * i]), ms=float(out[4 * i + 1]), work=float(out[4 * i + 2]),
+                       work_fp64eq=float(out[4 * i + 3]))
             for i, name in enumerate(KSTAT_CLASSES)}
 
 

@@ -4,8 +4,8 @@ reciprocal cell vectors as routine VECTOR2D prints them), from its sample run
 sample/02-layer-scf (input_rsp.in, input_geo.in and the run log
 Nb8_110.prn) into sample02_contour.json.
 
-Run here, where the reference tree is mounted:
-    python tests/golden/make_golden.py /root/reference
+Run where a checkout of the reference tree exists, passing its root:
+    python tests/golden/make_golden.py <path to the reference checkout>
 The JSON it writes is committed; the tests only read the JSON.
 """
 import json
@@ -13,7 +13,9 @@ import os
 import re
 import sys
 
-ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if len(sys.argv) != 2:
+    sys.exit("usage: make_golden.py <path to the reference checkout>")
+ref = sys.argv[1]
 d = os.path.join(ref, "sample", "02-layer-scf")
 rsp = open(os.path.join(d, "input_rsp.in")).read().splitlines()
 geo = open(os.path.join(d, "input_geo.in")).read().splitlines()
