@@ -133,6 +133,16 @@ int skkr_gpu_destroy(skkr_ctx *ctx);
 int skkr_gpu_set_mixed_policy(skkr_ctx *ctx, double dec_fp64_im, double near_im, int slices_near,
                               double dominant_frac);
 
+/* Decimation loop as a CUDA graph (default on): after the first iteration,
+ * the remaining iterations of every k chunk run as one graph launch whose
+ * WHILE node repeats the iteration body until no (k, lead) item is left,
+ * with the convergence test, the iteration count and the split-precision
+ * inverse's further Newton steps (IF nodes) decided on the device.  on = 0
+ * runs every iteration from the host (one stream synchronisation per
+ * iteration); results are identical.  While per-kernel statistics are on
+ * (skkr_gpu_kernel_stats) the host loop is used. */
+int skkr_gpu_set_graphs(skkr_ctx *ctx, int on);
+
 /* Off-diagonal tau of the interface for cluster embedding
  * (skkr_dbogo_bsf/clu/tau2d_god.f with the pair sums of
  * skkr_dbogo_bsf/rsp-scf/cpacoord_ksave.f:760-840): one k loop of the staged

@@ -56,6 +56,11 @@ class Context:
         N._check(N.lib().skkr_gpu_set_mixed_policy(self.h, dec_fp64_im, near_im, slices_near, dominant_frac),
                  "skkr_gpu_set_mixed_policy")
 
+    def set_graphs(self, on=True):
+        """Decimation loop as one CUDA graph launch per k chunk (the default)
+        or one host-driven iteration at a time (skkr_gpu_set_graphs)."""
+        N._check(N.lib().skkr_gpu_set_graphs(self.h, 1 if on else 0), "skkr_gpu_set_graphs")
+
     def set_reduce(self, fn):
         """Make this context one rank of a k-split energy: fn(buf) must sum
         the float64 host buffer over the ranks in place (an allreduce) and is
@@ -165,6 +170,8 @@ class Context:
 
     # -- one call, host buffers in and out (the drop-in form) ---------------
     def cpacoord(self, ep, tminv=None, check=True):
+        """One energy through the reference-facing call skkr_gpu_cpacoord
+        (BdG: skkr_gpu_cpacoord_bdg) with host buffers in and out."""
         rt, a = self._host_inputs(ep, tminv)
         n, lk = self.nintfc, self.lk
         out = {k: np.zeros((n, lk, lk), np.complex128) for k in ("tauc", "taua", "taub")}

@@ -23,6 +23,7 @@
 #include "kambe_dev.cuh"
 
 thread_local long long g_skkr_launches = 0;
+thread_local long long g_skkr_if_captured = 0;
 static thread_local std::string g_last_error;
 
 #define CK(x)                                                                          \
@@ -84,6 +85,10 @@ void kstat_begin2(int cls, double work, double work2, cudaStream_t st) {
 }
 
 void kstat_begin(int cls, double work, cudaStream_t st) { kstat_begin2(cls, work, work, st); }
+
+// per-launch events and the per-launch synchronisation check record every
+// launch from the host: the decimation then runs without graphs
+static bool launches_observed() { return g_ks.on || g_sync_check == 1; }
 
 void kstat_end(cudaStream_t st) {
   if (g_ks_open < 0) return;
@@ -242,6 +247,10 @@ struct skkr_ctx {
   long long inv_fallbacks = 0;  // inverses redone in FP64 in this run
   long long inv_refined = 0;    // inverses that took further Newton steps in this run
   double alg_units = 0.0;       // reference block operations (8 n^3 FLOP each) of this run
+  bool graphs = true;           // decimation loop as a CUDA graph WHILE node (skkr_gpu_set_graphs)
+  DBuf decctl;                  // [0] iteration, [1] items left, [2] half-bodies run (captured loop)
+  long long graph_kernels = 0;  // kernels run inside graphs in this run
+  long long graph_launches = 0; // graph launches in this run
 };
 
 // Inputs and outputs of one staged energy.  A context keeps any number of
@@ -341,7 +350,7 @@ extern "C" int skkr_gpu_destroy(skkr_ctx *c) {
   DBuf *all[] = {&c->gR, &c->rvec, &c->rstart, &c->blkmap_d, &c->xk, &c->wk, &c->lg, &c->rg,
                  &c->conc, &c->tcat, &c->tab, &c->trot, &c->trtmp, &c->pnorm, &c->G, &c->sspo,
                  &c->pool, &c->jobs, &c->dec, &c->decf, &c->deci, &c->tauw, &c->tauk, &c->S,
-                 &c->T1, &c->T2, &c->tauc, &c->cpa, &c->cpan, &c->cpaact};
+                 &c->T1, &c->T2, &c->tauc, &c->cpa, &c->cpan, &c->cpaact, &c->decctl, &c->knorm};
   for (DBuf *b : all) b->release();
   if (c->mw) mixed_destroy(c->mw);
   for (SlotStore *sl : c->slots) {
@@ -700,6 +709,72 @@ static bool use_mixed(const skkr_ctx *c, bool decimation) {
 
 
 // ---------------------------------------------------------------------------
+// The decimation iterations from `first` on as one CUDA graph: a WHILE node
+// (condition 1 at launch) whose body is two iterations, each followed by
+// k_dec_advance (iteration number + 1, loop condition from the count of
+// items left).  The body is captured on the context stream into the node's
+// graph; the mixed inverse inside it adds IF nodes for its further Newton
+// steps.  Kernels run inside the graph are counted from device counters.
+template <class Iterate>
+static int decimation_graph(skkr_ctx *c, int first, int itermax, Iterate &iterate) {
+  cudaStream_t st = c->st;
+  CKR(c->decctl.ensure(4 * sizeof(int)));
+  int *ctl = c->decctl.as<int>();
+  const int init[4] = {first, 0, 0, 0};
+  CK(cudaMemcpyAsync(ctl, init, sizeof(init), cudaMemcpyHostToDevice, st));
+  long long if0 = 0;
+  if (c->mw) if0 = mixed_graph_kernels(c->mw, st);  // also completes the copy above
+  else CK(cudaStreamSynchronize(st));
+  cudaGraph_t G = nullptr;
+  cudaGraphExec_t X = nullptr;
+  CK(cudaGraphCreate(&G, 0));
+  struct Done {
+    cudaGraph_t &g;
+    cudaGraphExec_t &x;
+    ~Done() {
+      if (x) cudaGraphExecDestroy(x);
+      if (g) cudaGraphDestroy(g);
+    }
+  } done{G, X};
+  cudaGraphConditionalHandle h;
+  CK(cudaGraphConditionalHandleCreate(&h, G, 1, cudaGraphCondAssignDefault));
+  cudaGraphNodeParams p = {};
+  p.type = cudaGraphNodeTypeConditional;
+  p.conditional.handle = h;
+  p.conditional.type = cudaGraphCondTypeWhile;
+  p.conditional.size = 1;
+  cudaGraphNode_t node;
+  CK(cudaGraphAddNode(&node, G, nullptr, nullptr, 0, &p));
+  cudaGraph_t body = p.conditional.phGraph_out[0];
+  const long long l0 = g_skkr_launches, i0 = g_skkr_if_captured;
+  CK(cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+  const int *errflag = c->mw ? mixed_error_ptr(c->mw) : nullptr;
+  int rc = SKKR_OK;
+  for (int half = 0; half < 2 && rc == SKKR_OK; half++) {
+    rc = iterate(((first + half) & 1) != 0, 0, ctl, ctl + 1);
+    if (rc == SKKR_OK) launch_dec_advance(ctl, ctl + 1, itermax, errflag, h, ctl + 2, st);
+  }
+  cudaGraph_t cap = nullptr;
+  const cudaError_t ec = cudaStreamEndCapture(st, &cap);
+  // kernels captured into the body (outside the IF bodies), per half
+  const long long per_half = (g_skkr_launches - l0) / 2;
+  g_skkr_launches = l0;
+  g_skkr_if_captured = i0;
+  if (rc != SKKR_OK) return rc;
+  CK(ec);
+  CK(cudaGraphInstantiate(&X, G, 0));
+  CK(cudaGraphLaunch(X, st));
+  int halves = 0;
+  CK(cudaMemcpyAsync(&halves, ctl + 2, sizeof(int), cudaMemcpyDeviceToHost, st));
+  long long if1 = 0;
+  if (c->mw) if1 = mixed_graph_kernels(c->mw, st);
+  else CK(cudaStreamSynchronize(st));
+  c->graph_launches += 1;
+  c->graph_kernels += per_half * halves + (if1 - if0);
+  return SKKR_OK;
+}
+
+// ---------------------------------------------------------------------------
 // decimation (main/dugo.f + main/surfgf.f) for the k points [k0, k0+nkc)
 // items (k, s): s < nLc left-lead classes, then right-lead classes.
 static int run_decimation(skkr_ctx *c, int k0, int nkc, const std::vector<int> &lcls,
@@ -757,11 +832,12 @@ static int run_decimation(skkr_ctx *c, int k0, int nkc, const std::vector<int> &
   }
   const int itermax = std::max(c->sz.itermaxl, c->sz.itermaxr);
   const bool mx = use_mixed(c, true);
-  int iter = 1;
-  skkr_set_active_items(nit);
-  for (;; iter++) {
-    MatRef &ac = (iter & 1) ? a0 : a1, &an = (iter & 1) ? a1 : a0;
-    MatRef &bc = (iter & 1) ? b0 : b1, &bn = (iter & 1) ? b1 : b0;
+  // one iteration (surfgf.f:47-96); the parity picks the alfa / beta buffers
+  // read and written; iter_dev: the iteration number lives on the device (the
+  // captured loop), else `iter` from the host
+  auto iterate = [&](bool odd, int iter, const int *iter_dev, int *nact_dev) -> int {
+    MatRef &ac = odd ? a0 : a1, &an = odd ? a1 : a0;
+    MatRef &bc = odd ? b0 : b1, &bn = odd ? b1 : b0;
     CKR(eng_inv(c, mx, eps, y1, false, n, nkc, nc, act));              // y1 = eps^-1
     if (mx && !ehsplit(c)) {
       // split-precision engine: each operand split once (B slots 1-3: y1,
@@ -791,20 +867,34 @@ static int run_decimation(skkr_ctx *c, int k0, int nkc, const std::vector<int> &
     }
     launch_fnorm(an, n, nkc, nc, act, err, st);
     // the two leads may carry different caps (itermaxl / itermaxr)
-    launch_dec_state(err, act, stat, iters, nit, iter, itermax, c->sz.errmax, st);
-    int any = 0;
+    if (iter_dev)
+      launch_dec_state_dev(err, act, stat, iters, nit, iter_dev, itermax, c->sz.errmax, nact_dev, st);
+    else
+      launch_dec_state(err, act, stat, iters, nit, iter, itermax, c->sz.errmax, st);
+    return SKKR_OK;
+  };
+  skkr_set_active_items(nit);
+  // The first iteration runs eagerly (it sizes every work buffer); the rest
+  // is one CUDA graph whose WHILE node repeats a body of two iterations (odd
+  // and even buffers) until no item is left, with the iteration number, the
+  // count of items left and the loop condition on the device: no host
+  // round trip per iteration.  Observed launches (per-kernel statistics, the
+  // synchronisation check) keep the host loop.
+  for (int iter = 1;; iter++) {
+    CKR(iterate(iter & 1, iter, nullptr, nullptr));
+    long long cnt = 0;
     {
       std::vector<int> h(nit);
       CK(cudaMemcpyAsync(h.data(), act, nit * sizeof(int), cudaMemcpyDeviceToHost, st));
       CK(cudaStreamSynchronize(st));
-      long long cnt = 0;
-      for (int v : h) {
-        any |= v;
-        cnt += v;
-      }
+      for (int v : h) cnt += v;
       skkr_set_active_items(cnt);
     }
-    if (!any || iter > itermax + 1) break;
+    if (cnt == 0 || iter > itermax + 1) break;
+    if (c->graphs && !launches_observed()) {
+      CKR(decimation_graph(c, iter + 1, itermax, iterate));
+      break;
+    }
   }
   skkr_set_active_items(-1);
   // statuses
@@ -1435,6 +1525,12 @@ extern "C" int skkr_gpu_set_mixed_policy(skkr_ctx *c, double dec_fp64_im, double
   return SKKR_OK;
 }
 
+extern "C" int skkr_gpu_set_graphs(skkr_ctx *c, int on) {
+  if (!c) return SKKR_ERR_ARG;
+  c->graphs = on != 0;
+  return SKKR_OK;
+}
+
 extern "C" int skkr_gpu_set_reduce(skkr_ctx *c, skkr_reduce_fn fn, void *user) {
   if (!c) return SKKR_ERR_ARG;
   c->red_fn = fn;
@@ -1460,6 +1556,8 @@ extern "C" int skkr_gpu_run(skkr_ctx *c, skkr_status *status) {
   c->max_resid = 0.0;
   c->k_fp64 = 0;
   c->alg_units = 0.0;
+  c->graph_kernels = 0;
+  c->graph_launches = 0;
   CKR(c->knorm.ensure((size_t)nk * sizeof(double)));
   if (c->sz.precision == SKKR_MIXED && !c->mw) {
     c->mw = mixed_create();
@@ -1604,7 +1702,8 @@ extern "C" int skkr_gpu_run(skkr_ctx *c, skkr_status *status) {
     status->cpa_error = cpaerr;
     status->max_dec_iters = c->max_dec;
     status->dec_iters_total = c->tot_dec;
-    status->gpu_launches = g_skkr_launches - l0;
+    // host-issued launches plus the kernels run inside graphs
+    status->gpu_launches = g_skkr_launches - l0 + c->graph_kernels;
     status->max_refine_resid = c->max_resid;
     status->run_ms = run_ms;
     status->inv_fallbacks = c->inv_fallbacks;

@@ -72,6 +72,9 @@ inline MatRef mref_map(zd *base, long long sk, long long sc, int ld, const int *
 // the environment every launch is followed by a device synchronisation and
 // the first failing launch site is recorded (diagnostics only).
 extern thread_local long long g_skkr_launches;  // launches made by this host thread
+// kernels captured into the IF bodies of conditional graph nodes by this
+// thread (counted when they run, from device counters)
+extern thread_local long long g_skkr_if_captured;
 void skkr_after_launch(const char *file, int line);
 #define SKKR_LAUNCHED() skkr_after_launch(__FILE__, __LINE__)
 

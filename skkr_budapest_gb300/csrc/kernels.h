@@ -41,6 +41,13 @@ void launch_fnorm(const MatRef &a, int n, int nk, int nc, const int *act, double
 // decimation state update (surfgf.f:81-96)
 void launch_dec_state(const double *err, int *act, int *stat, int *iters, int nitems, int iter,
                       int itermax, double errmax, cudaStream_t st);
+// the same with the iteration number on the device and the count of items
+// left iterating added to *nactive; then the loop step of a captured WHILE
+// node: iteration number + 1, *nactive cleared, condition set
+void launch_dec_state_dev(const double *err, int *act, int *stat, int *iters, int nitems, const int *iter_p,
+                          int itermax, double errmax, int *nactive, cudaStream_t st);
+void launch_dec_advance(int *iter_p, int *nactive, int itermax, const int *errflag, cudaGraphConditionalHandle cond,
+                        int *runs, cudaStream_t st);
 // tau(k) diagonal-block extraction: out[k][c][layer] = (wk[k]*wscale) * W(layer block)
 void launch_extract_tau(const MatRef &W, int lk, int nl, int layer0, const double *wk,
                         double wscale, zd *out, long long out_sk, long long out_sc, int nk,
@@ -70,6 +77,17 @@ struct MixedWork;
 MixedWork *mixed_create();
 void mixed_destroy(MixedWork *w);
 int mixed_error_flag(MixedWork *w);
+int *mixed_error_ptr(MixedWork *w);   // device flag set by an expired tensor-core wait
+// kernels run so far by the IF bodies of captured further Newton steps
+// (device count since mixed_resid_reset; synchronizes st)
+long long mixed_graph_kernels(MixedWork *w, cudaStream_t st);
+// conditional graph nodes inside a stream capture (kernels_mixed.cu): a
+// handle on the graph being captured, then an IF / WHILE node after the
+// stream's current work whose body is captured on `side` until cond_end
+int cond_handle(cudaStream_t st, cudaGraphConditionalHandle *h);
+int cond_begin(cudaStream_t st, cudaStream_t side, cudaGraphConditionalHandle h, int type);
+int cond_end(cudaStream_t side);
+bool stream_capturing(cudaStream_t st);
 // modes as launch_zgemm plus 4: C = I - A*B, 5: C = C + A*B; S = slices (3..7)
 // Split operands live in MIXED_SLOTS staging slots per side (0: A, 1: B);
 // slot 0 is the one mixed_zgemm / mixed_zgemm_k / mixed_zinv use.  Splitting

@@ -518,6 +518,66 @@ void launch_dec_state(const double *err, int *act, int *stat, int *iters, int ni
   SKKR_LAUNCHED();
 }
 
+// The same update with the iteration number read from the device (*iter_p,
+// the iteration just completed), counting the items left iterating in
+// *nactive: the form a captured graph replays
+__global__ void k_dec_state_dev(const double *err, int *act, int *stat, int *iters, int nitems,
+                                const int *iter_p, int itermax, double errmax, int *nactive) {
+  const int it = blockIdx.x * blockDim.x + threadIdx.x;
+  const int iter = *iter_p;
+  int keep = 0;
+  if (it < nitems && act[it]) {
+    const double e = err[it];
+    keep = 1;
+    if (e < errmax || iter > itermax) {
+      act[it] = 0;
+      iters[it] = iter;
+      stat[it] = (iter > itermax) ? -3 : 0;
+      keep = 0;
+    } else if (e > 1.0e10) {
+      act[it] = 0;
+      iters[it] = iter;
+      stat[it] = -4;
+      keep = 0;
+    } else if (!(e == e)) {
+      act[it] = 0;
+      iters[it] = iter;
+      stat[it] = -7;
+      keep = 0;
+    }
+  }
+  keep = __syncthreads_count(keep);
+  if (threadIdx.x == 0 && keep) atomicAdd(nactive, keep);
+}
+
+void launch_dec_state_dev(const double *err, int *act, int *stat, int *iters, int nitems, const int *iter_p,
+                          int itermax, double errmax, int *nactive, cudaStream_t st) {
+  if (nitems <= 0) return;
+  k_dec_state_dev<<<(nitems + 255) / 256, 256, 0, st>>>(err, act, stat, iters, nitems, iter_p, itermax, errmax,
+                                                         nactive);
+  SKKR_LAUNCHED();
+}
+
+// After one decimation iteration of a captured loop: advance the iteration
+// number, clear the active count, count the iteration (*runs) and set the
+// loop condition (items left, within itermax, no tensor-core wait expired).  Every item retires by
+// iteration itermax + 1, so the loop ends.
+__global__ void k_dec_advance(int *iter_p, int *nactive, int itermax, const int *errflag,
+                              cudaGraphConditionalHandle cond, int *runs) {
+  const int it = *iter_p, na = *nactive;
+  *iter_p = it + 1;
+  *nactive = 0;
+  *runs += 1;
+  const bool go = na > 0 && it <= itermax && (errflag == nullptr || *errflag == 0);
+  cudaGraphSetConditional(cond, go ? 1u : 0u);
+}
+
+void launch_dec_advance(int *iter_p, int *nactive, int itermax, const int *errflag, cudaGraphConditionalHandle cond,
+                        int *runs, cudaStream_t st) {
+  k_dec_advance<<<1, 1, 0, st>>>(iter_p, nactive, itermax, errflag, cond, runs);
+  SKKR_LAUNCHED();
+}
+
 // tau2d.f:137-147: tau(l,lp,ilay) = wgeff * tau00(il0+l, il0+lp)
 __global__ void k_extract_tau(MatRef W, int lk, int nl, int layer0, const double *wk, double wscale,
                               zd *out, long long out_sk, long long out_sc, int nc, int ehsplit) {

@@ -812,7 +812,9 @@ struct MixedWork {
   int *mark = nullptr;                 // per-item mask of the further Newton steps
   size_t mark_cap = 0;
   int *cnt = nullptr;                  // count of marked items (device scalar)
-  long long nref = 0;                  // inverses that took further Newton steps (host count)
+  unsigned long long *nref = nullptr;  // [0] inverses that took further Newton steps, [1] kernels run by the
+                                       // IF bodies of captured further steps (device counts)
+  cudaStream_t side = nullptr;         // captures the bodies of conditional graph nodes
   int smem_set[32] = {0};
   bool precise = false;    // (64, 7) tile: exact levels 0..5 (mixed_set_precise)
 };
@@ -847,40 +849,54 @@ MixedWork *mixed_create() {
   if (cudaMalloc(&w->err, sizeof(int)) != cudaSuccess ||
       cudaMalloc(&w->dmax, sizeof(unsigned long long)) != cudaSuccess ||
       cudaMalloc(&w->nfb, sizeof(unsigned long long)) != cudaSuccess ||
-      cudaMalloc(&w->cnt, sizeof(int)) != cudaSuccess) {
-    if (w->err) cudaFree(w->err);
-    if (w->dmax) cudaFree(w->dmax);
-    if (w->nfb) cudaFree(w->nfb);
+      cudaMalloc(&w->cnt, sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&w->nref, 2 * sizeof(unsigned long long)) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&w->side, cudaStreamNonBlocking) != cudaSuccess) {
+    void *ps[] = {w->err, w->dmax, w->nfb, w->cnt, w->nref};
+    for (void *p : ps)
+      if (p) cudaFree(p);
     delete w;
     return nullptr;
   }
   cudaMemset(w->err, 0, sizeof(int));
   cudaMemset(w->dmax, 0, sizeof(unsigned long long));
   cudaMemset(w->nfb, 0, sizeof(unsigned long long));
+  cudaMemset(w->nref, 0, 2 * sizeof(unsigned long long));
   cudaDeviceSynchronize();  // default-stream memsets, before the non-blocking streams use the flags
   return w;
 }
 
 int mixed_resid_reset(MixedWork *w, cudaStream_t st) {
-  w->nref = 0;
   return (cudaMemsetAsync(w->dmax, 0, sizeof(unsigned long long), st) == cudaSuccess &&
-          cudaMemsetAsync(w->nfb, 0, sizeof(unsigned long long), st) == cudaSuccess)
+          cudaMemsetAsync(w->nfb, 0, sizeof(unsigned long long), st) == cudaSuccess &&
+          cudaMemsetAsync(w->nref, 0, 2 * sizeof(unsigned long long), st) == cudaSuccess)
              ? 0
              : SKKR_ERR_CUDA;
 }
 
 int mixed_resid_read(MixedWork *w, double *out, long long *fallbacks, long long *refined, cudaStream_t st) {
-  if (refined) *refined = w->nref;
-  unsigned long long h[2] = {0, 0};
+  unsigned long long h[3] = {0, 0, 0};
   if (cudaMemcpyAsync(&h[0], w->dmax, sizeof(h[0]), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
       cudaMemcpyAsync(&h[1], w->nfb, sizeof(h[1]), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaMemcpyAsync(&h[2], w->nref, sizeof(h[2]), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
       cudaStreamSynchronize(st) != cudaSuccess)
     return SKKR_ERR_CUDA;
   double v;
   memcpy(&v, &h[0], sizeof(v));
   *out = v;
   if (fallbacks) *fallbacks = (long long)h[1];
+  if (refined) *refined = (long long)h[2];
   return 0;
+}
+
+int *mixed_error_ptr(MixedWork *w) { return w->err; }
+
+long long mixed_graph_kernels(MixedWork *w, cudaStream_t st) {
+  unsigned long long h = 0;
+  if (cudaMemcpyAsync(&h, w->nref + 1, sizeof(h), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return 0;
+  return (long long)h;
 }
 
 void mixed_destroy(MixedWork *w) {
@@ -891,9 +907,10 @@ void mixed_destroy(MixedWork *w) {
     for (void *p : q)
       if (p) cudaFree(p);
   }
-  void *ps[] = {w->acopy, w->rbuf, w->rnorm, w->err, w->dmax, w->nfb, w->flag, w->mark, w->cnt};
+  void *ps[] = {w->acopy, w->rbuf, w->rnorm, w->err, w->dmax, w->nfb, w->flag, w->mark, w->cnt, w->nref};
   for (void *p : ps)
     if (p) cudaFree(p);
+  if (w->side) cudaStreamDestroy(w->side);
   delete w;
 }
 
@@ -1096,16 +1113,85 @@ __global__ void k_newton_check(const double *__restrict__ rn, const int *__restr
 }
 
 // Items whose residual is above `limit` but below `basin` (Newton's
-// quadratic regime) are marked for a further step; `count` accumulates them
-__global__ void k_newton_select(const double *__restrict__ rn, const int *__restrict__ act, int items,
-                                double limit, double basin, int *__restrict__ mark, int *count) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= items) return;
-  const int a = act ? act[i] : 1;
-  const double r = rn[i];
-  const int m = a && r > limit && r < basin;
-  mark[i] = m;
-  if (m) atomicAdd(count, 1);
+// quadratic regime) are marked for a further step.  One block: the count of
+// marked items goes to *count (eager runs read it on the host), is added to
+// *nref on the first further step, and, inside a captured graph, decides the
+// IF node of the step (cudaGraphSetConditional).
+__global__ void __launch_bounds__(1024) k_newton_select(const double *__restrict__ rn, const int *__restrict__ act,
+                                                        int items, double limit, double basin, int *__restrict__ mark,
+                                                        int *count, unsigned long long *nref, int first,
+                                                        cudaGraphConditionalHandle cond, int use_cond,
+                                                        int body_kernels) {
+  __shared__ int part[32];
+  int v = 0;
+  for (int i = threadIdx.x; i < items; i += blockDim.x) {
+    const int a = act ? act[i] : 1;
+    const double r = rn[i];
+    const int m = a && r > limit && r < basin;
+    mark[i] = m;
+    v += m;
+  }
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int t = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += part[w];
+    *count = t;
+    if (first && t) nref[0] += (unsigned long long)t;
+    if (use_cond) {
+      cudaGraphSetConditional(cond, t > 0 ? 1u : 0u);
+      if (t > 0) nref[1] += (unsigned long long)body_kernels;
+    }
+  }
+}
+
+// Inside a stream capture: an IF node whose condition a kernel captured
+// before it sets, with its body captured on `side`.  cond_handle creates the
+// handle on the graph being captured (the setter needs it as an argument);
+// cond_if_begin appends the node after the stream's current dependencies and
+// starts the capture of its body; cond_if_end closes that capture.
+int cond_handle(cudaStream_t st, cudaGraphConditionalHandle *h) {
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t g;
+  if (cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, nullptr, nullptr, nullptr) != cudaSuccess ||
+      cs != cudaStreamCaptureStatusActive)
+    return SKKR_ERR_CUDA;
+  return cudaGraphConditionalHandleCreate(h, g, 0, 0) == cudaSuccess ? 0 : SKKR_ERR_CUDA;
+}
+
+int cond_begin(cudaStream_t st, cudaStream_t side, cudaGraphConditionalHandle h, int type) {
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t g;
+  const cudaGraphNode_t *deps = nullptr;
+  const cudaGraphEdgeData *ed = nullptr;
+  size_t nd = 0;
+  if (cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, &ed, &nd) != cudaSuccess ||
+      cs != cudaStreamCaptureStatusActive)
+    return SKKR_ERR_CUDA;
+  cudaGraphNodeParams p = {};
+  p.type = cudaGraphNodeTypeConditional;
+  p.conditional.handle = h;
+  p.conditional.type = (cudaGraphConditionalNodeType)type;
+  p.conditional.size = 1;
+  cudaGraphNode_t node;
+  if (cudaGraphAddNode(&node, g, deps, ed, nd, &p) != cudaSuccess) return SKKR_ERR_CUDA;
+  if (cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies) != cudaSuccess)
+    return SKKR_ERR_CUDA;
+  return cudaStreamBeginCaptureToGraph(side, p.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                       cudaStreamCaptureModeRelaxed) == cudaSuccess
+             ? 0
+             : SKKR_ERR_CUDA;
+}
+
+int cond_end(cudaStream_t side) {
+  cudaGraph_t body = nullptr;
+  return cudaStreamEndCapture(side, &body) == cudaSuccess ? 0 : SKKR_ERR_CUDA;
+}
+
+bool stream_capturing(cudaStream_t st) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  return cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusActive;
 }
 
 // X = A^-1: FP32 Gauss-Jordan, then `newton` steps X += X (I - A X) with the
@@ -1147,28 +1233,50 @@ int mixed_zinv(MixedWork *w, const MatRef &A, const MatRef &X, int n, int nk, in
   // Items above the limit but inside Newton's basin (|R| < 1/2) take up to
   // NEWTON_EXTRA further steps with the correction at sres slices as well:
   // the 3-slice correction leaves about cond(A) 2^-24 |R| in the next
-  // residual, which stalls ill-conditioned items.  The host reads the count
-  // of marked items once per step and stops when none is left.
+  // residual, which stalls ill-conditioned items.  Each step runs only if an
+  // item is marked: inside a captured graph an IF node decides on the
+  // device; run eagerly, the host reads the count.
+  const bool cap = stream_capturing(st);
   const long long hint = skkr_active_items(-1);
   for (int e = 0; e < NEWTON_EXTRA; e++) {
-    if (cudaMemsetAsync(w->cnt, 0, sizeof(int), st) != cudaSuccess) return SKKR_ERR_CUDA;
-    k_newton_select<<<(unsigned)((items + 255) / 256), 256, 0, st>>>(w->rnorm, act, (int)items, 1e-6, 0.5,
-                                                                    w->mark, w->cnt);
+    cudaGraphConditionalHandle h = 0;
+    if (cap && (rc = cond_handle(st, &h))) return rc;
+    // the IF body below launches 6 kernels (3 splits, 2 sliced products, 1 norm)
+    k_newton_select<<<1, 1024, 0, st>>>(w->rnorm, act, (int)items, 1e-6, 0.5, w->mark, w->cnt, w->nref, e == 0,
+                                        h, cap ? 1 : 0, 6);
     SKKR_LAUNCHED();
-    int marked = 0;
-    if (cudaMemcpyAsync(&marked, w->cnt, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-        cudaStreamSynchronize(st) != cudaSuccess)
-      return SKKR_ERR_CUDA;
-    if (marked == 0) break;
-    if (e == 0) w->nref += marked;
+    const long long l_body = g_skkr_launches;
+    cudaStream_t sx = st;
+    if (cap) {
+      if ((rc = cond_begin(st, w->side, h, cudaGraphCondTypeIf))) return rc;
+      sx = w->side;
+    } else {
+      int marked = 0;
+      if (cudaMemcpyAsync(&marked, w->cnt, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+          cudaStreamSynchronize(st) != cudaSuccess)
+        return SKKR_ERR_CUDA;
+      if (marked == 0) break;
+      skkr_set_active_items(marked);
+    }
     const int *mk = w->mark;
-    skkr_set_active_items(marked);
-    if ((rc = mixed_split(w, 1, 0, sres, X, n, n, nk, nc, mk, st))) return rc;
-    if ((rc = mixed_gemm_staged(w, 4, sres, 0, 0, R, R, R, n, n, nk, nc, mk, st))) return rc;
-    launch_fnorm(R, n, nk, nc, mk, w->rnorm, st);
-    if ((rc = mixed_split(w, 0, 5, sres, X, n, n, nk, nc, mk, st))) return rc;
-    if ((rc = mixed_split(w, 1, 5, sres, R, n, n, nk, nc, mk, st))) return rc;
-    if ((rc = mixed_gemm_staged(w, 5, sres, 5, 5, X, X, X, n, n, nk, nc, mk, st))) return rc;
+    auto step = [&]() -> int {
+      int r;
+      if ((r = mixed_split(w, 1, 0, sres, X, n, n, nk, nc, mk, sx))) return r;
+      if ((r = mixed_gemm_staged(w, 4, sres, 0, 0, R, R, R, n, n, nk, nc, mk, sx))) return r;
+      launch_fnorm(R, n, nk, nc, mk, w->rnorm, sx);
+      if ((r = mixed_split(w, 0, 5, sres, X, n, n, nk, nc, mk, sx))) return r;
+      if ((r = mixed_split(w, 1, 5, sres, R, n, n, nk, nc, mk, sx))) return r;
+      return mixed_gemm_staged(w, 5, sres, 5, 5, X, X, X, n, n, nk, nc, mk, sx);
+    };
+    rc = step();
+    if (cap) {  // close the body's capture whatever happened inside it
+      const int rc2 = cond_end(w->side);
+      if (!rc) rc = rc2;
+      // the body's kernels are counted when they run (nref[1]), not here
+      g_skkr_launches = l_body;
+      g_skkr_if_captured += 6;
+    }
+    if (rc) return rc;
     skkr_set_active_items(hint);
   }
   // An ill-conditioned A (cond ~ 1e7 and above) leaves the FP32 start outside

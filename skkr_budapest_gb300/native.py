@@ -80,6 +80,7 @@ def lib():
         L.skkr_gpu_layer_dos.argtypes = [I, I, I, P, I, P, P, I, P, P]
         L.skkr_gpu_set_reduce.argtypes = [P, P, P]
         L.skkr_gpu_set_mixed_policy.argtypes = [P, D, D, I, D]
+        L.skkr_gpu_set_graphs.argtypes = [P, I]
         L.skkr_gpu_cpacoord_many.argtypes = [I, P, P, P]
         L.skkr_gpu_gjinv_batch.argtypes = [I, I, P, I]
         L.skkr_gpu_surfgf_batch.argtypes = [I, I, P, P, P, P, I, I, D, P, P]

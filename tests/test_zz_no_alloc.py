@@ -78,7 +78,7 @@ def test_noalloc_padded_leading_dimension_on_a_caller_stream():
     non-default stream, against the allocating entry point and the oracle."""
     import torch
     s = torch.cuda.Stream()
-    for call, (seed, b, n) in enumerate([(5, 3, 18), (6, 2, 29)]):
+    for call, (seed, b, n) in enumerate([(3, 3, 18), (10, 3, 29)]):
         ml, m0, mr = _inputs(seed, b, n)
         rc, x, it, st = _noalloc(ml, m0, mr, ld=n + 3, stream=s)
         assert rc == 0, (call, rc)
