@@ -3,7 +3,8 @@
 Workload: the relativistic (kappa,mu) bcc(001) interface, lmax=3 (32x32 per
 site), 4 layers per principal layer (128x128 blocks), 12 interface layers,
 24 semicircle-contour energies with uneven adaptive IBZ meshes of 210..12090
-k points (seeded synthetic inputs, see skkr_budapest_gb300/workloads.py).
+k points, square wells with j = l +- 1/2 split depths (seeded synthetic
+inputs, see skkr_budapest_gb300/workloads.py).
 
 One step = one contour energy, all of its k points carried through the CPA
 pass: G_scr(k) transform, L and R decimation, tau2d, k-sum with point-group
@@ -57,8 +58,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", action="store_true",
                     help="only the device loop of the timed steps (for ncu captures); prints a short line")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "tauij"],
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "tauij"],
                     help="c3: one energy of each of three systems per step through skkr_gpu_cpacoord_many; "
+                         "c4: CPA alloy interfaces from the ATA and from the learned start; "
                          "tauij: the off-diagonal tau of the interface (skkr_gpu_tauij) per step")
     return ap.parse_args()
 
@@ -245,7 +247,7 @@ def run_reference(args, rank, ws):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
             "data": "synthetic (seeded)",
             "config": {"workload": WORKLOAD, "step": "one contour energy of the cycle, strided k sample (CPU)",
-                       "so_split": 0.0, "alloy_layers": 0, "l2": "host run"},
+                       "so_split": spec.so_split, "alloy_layers": 0, "l2": "host run"},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": nth, "kind": "port", "sample": sample,
                              "single_core": {"value": v1, "unit": UNIT, "cores": 1,
                                              "sample": "2 strided k points of each of 3 steps, %.1f s" % t1}},
@@ -432,8 +434,8 @@ def run_ours(args, rank, ws):
                        "step": "one contour energy, all k, full CPA pass",
                        "step_energies": order[args.warmup:], "points": r["pts"],
                        "so_split": spec.so_split, "alloy_layers": len(spec.alloy_layers),
-                       "deviation": "C2 asks for j = l +- 1/2 split well depths; this workload has none "
-                                    "(so_split 0) and no alloy layers",
+                       "screening": "%.1f Ry in spheres of %.4f d_NN (the reference's bcc sample: "
+                                    "Wigner-Seitz spheres)" % (spec.vscreen, spec.rscreen),
                        "launches_per_energy": r["launches"] / max(1, args.steps),
                        "l2": "256 MB buffer written between steps; per-step working set > 1 GB",
                        "wall_s": round(r["wall"], 3), "dec_iters": r["dec_iters"],
@@ -541,6 +543,89 @@ def run_c3(args):
                       "config": {"workload": C3_WORKLOAD,
                                  "precision": args.precision, "energies": plan,
                                  "timing": "host wall clock around whole calls (host buffers)"}}), flush=True)
+
+
+C4_METRIC = "(E,k) points/s of CPA alloy interfaces converged to cpatol 1e-10"
+C4_WORKLOAD = ("c4: relativistic bcc(001) PL4 lmax=3 interface with 4 alloy layers A_c B_(1-c), c ~ U[0.1, 0.9], "
+               "depths ~ U[-1.2, -0.4] Ry drawn per step (held-out draws), contour energies cycled, IBZ mesh of "
+               "the surrogate's family")
+
+
+def _c4_steps(nsteps, seed=9001):
+    from skkr_budapest_gb300 import cpa_warmstart as CW
+    model = CW.Model()
+    fam = model.family()
+    rng = np.random.default_rng(seed)
+    eps = [fam.problem(fam.energies[i % len(fam.energies)], fam.draw(rng)) for i in range(nsteps)]
+    return model, fam, eps
+
+
+def run_c4_reference(args):
+    """Reference arm of the alloy workload: the oracle's CPA loop on all host
+    threads, one k point per thread spread over each step's mesh."""
+    nth = os.cpu_count() or 1
+    _, _, eps = _c4_steps(args.warmup + args.steps)
+    _oracle_rate(eps[:args.warmup], nth, nth)
+    v, pts, dt = _oracle_rate(eps[args.warmup:], nth, nth)
+    print(json.dumps({"impl": "reference", "metric": C4_METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+                      "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+                      "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+                      "data": "synthetic (seeded)",
+                      "config": {"workload": C4_WORKLOAD, "start": "ATA (tata)",
+                                 "step": "one alloy stack at one energy, strided k sample (CPU)"},
+                      "cpu_baseline": {"value": v, "unit": UNIT, "cores": nth, "kind": "port",
+                                       "sample": "%d k points per step, %d steps" % (nth, args.steps)},
+                      "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}),
+          flush=True)
+
+
+def run_c4(args):
+    """Alloy interfaces converged to cpatol 1e-10 through the reference-facing
+    call with host buffers: the FP64 path and the split-precision path from
+    the ATA start, and the split-precision path from the learned start (the
+    surrogate's inference and the start's assembly inside the timed region).
+    value = the last; the CPA iterations of each are reported."""
+    import torch
+    from skkr_budapest_gb300 import api, cpa_warmstart as CW
+    model, fam, eps = _c4_steps(args.warmup + args.steps)
+    out = {}
+    for name, prec, learned in (("fp64", "fp64", False), ("mixed", "mixed", False), ("mixed_mlp", "mixed", True)):
+        ctx = api.Context.for_problem(eps[0], prec)
+        for ep in eps[:args.warmup]:
+            ctx.cpacoord(ep, tminv=CW.warm_start(ep, model, fam) if learned else None)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        pts, its, dev, res, h2d, d2h = 0, 0, 0.0, [], 0, 0
+        for ep in eps[args.warmup:]:
+            r = ctx.cpacoord(ep, tminv=CW.warm_start(ep, model, fam) if learned else None)
+            pts += ep.nk
+            its += r["cpa_iterations"]
+            dev += r["run_ms"]
+            h2d += r["h2d_bytes"]
+            d2h += r["d2h_bytes"]
+            res.append(r["tauc"])
+        torch.cuda.synchronize()
+        out[name] = dict(wall=time.perf_counter() - t0, pts=pts, its=its, dev=dev, tau=res, h2d=h2d, d2h=d2h)
+        ctx.close()
+    ref = out["fp64"]["tau"]
+    err = {k: max(float(np.linalg.norm(a - b) / np.linalg.norm(b)) for a, b in zip(out[k]["tau"], ref))
+           for k in ("mixed", "mixed_mlp")}
+    rate = {k: v["pts"] / v["wall"] for k, v in out.items()}
+    line = {"metric": C4_METRIC, "value": rate["mixed_mlp"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * out["mixed_mlp"]["wall"] / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "c128 via BF16 slices + FP64 refinement; surrogate BF16 weights, FP32 accumulation",
+            "data": "synthetic (seeded, held-out alloy draws)",
+            "config": {"workload": C4_WORKLOAD, "nset": fam.nset, "k_points_per_step": eps[0].nk,
+                       "so_split": fam.so_split, "cpatol": eps[0].cpatol,
+                       "timing": "host wall clock around whole calls (host buffers), surrogate included"},
+            "paths": {k: {"value": rate[k], "cpa_iterations": out[k]["its"], "device_ms": round(out[k]["dev"], 1),
+                          "max_rel_err_tau_vs_fp64": err.get(k)} for k in out},
+            "speedup_vs_fp64": rate["mixed_mlp"] / rate["fp64"],
+            "cpa_iterations_learned_vs_ata": out["mixed_mlp"]["its"] / max(1, out["mixed"]["its"]),
+            "e2e": {"value": rate["mixed_mlp"], "unit": UNIT, "h2d_bytes_per_step": out["mixed_mlp"]["h2d"] // args.steps,
+                    "d2h_bytes_per_step": out["mixed_mlp"]["d2h"] // args.steps}}
+    print(json.dumps(line), flush=True)
 
 
 TAUIJ_METRIC = "(E,k) points/s of the off-diagonal interface tau (skkr_gpu_tauij)"
@@ -654,6 +739,12 @@ def main():
             run_tauij_reference(args)
         else:
             run_tauij(args)
+        return
+    if args.workload == "c4":
+        if args.impl == "reference":
+            run_c4_reference(args)
+        else:
+            run_c4(args)
         return
     rank, ws = dist_init(args.gpus)
     if args.impl == "reference":

@@ -319,6 +319,19 @@ int skkr_gpu_mlp_train(int nlayer, const int *dims, double *params, int n, const
                        const unsigned char *rows, int epochs, double lr, double weight_decay, int eval_every,
                        double *train_loss, double *best, double *best_params);
 
+/* The same network in the precision of the C4 warm-start surrogate: FP32
+ * master parameters (packed like params above), whose weights the products
+ * read as BF16 (round to nearest even) with FP32 activations and FP32
+ * accumulation; the gradient is that of the BF16-weight network, applied to
+ * the FP32 masters by AdamW (beta 0.9 / 0.999, eps 1e-8), after which the
+ * BF16 copies are refreshed.  Arguments and outputs as for the FP64 forms. */
+int skkr_gpu_mlp16_forward(int nlayer, const int *dims, const float *params, int n, const float *x, float *y);
+int skkr_gpu_mlp16_grad(int nlayer, const int *dims, const float *params, int n, const float *x, const float *y,
+                        const unsigned char *rows, float *loss, float *grad);
+int skkr_gpu_mlp16_train(int nlayer, const int *dims, float *params, int n, const float *x, const float *y,
+                         const unsigned char *rows, int epochs, float lr, float weight_decay, int eval_every,
+                         float *train_loss, float *best, float *best_params);
+
 /* The reference's k-space structure constants (main/kamstr.f:20-392): the
  * Kambe lattice sums D_L(k, s) of outgoing spherical waves over a 2D lattice,
  * L = (l, m) up to l = lmax2 (0..6), index l(l+1)+m, for nitem items of one

@@ -87,3 +87,33 @@ def train(layers, x, y, rows, epochs, lr, weight_decay, eval_every=20):
             if vl < best[0]:
                 best, bestp = (vl, loss), layers
     return layers, bestp, np.array(losses), best
+
+
+def bf16_round(a):
+    """Round to the nearest BF16 value (ties to even) of the FP32 value of
+    each entry, returned as float64: the weights the BF16 network multiplies
+    with.  Bit form: the FP32 pattern plus 0x7FFF plus the lowest kept bit,
+    cut to the upper 16 bits (finite inputs)."""
+    f = np.ascontiguousarray(a, np.float32)
+    u = f.view(np.uint32).astype(np.uint64)
+    r = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return r.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+def layers16(layers):
+    """The BF16-weight network of FP32 master layers: weights rounded, biases
+    kept in FP32."""
+    return [(bf16_round(w), np.asarray(np.float32(b), np.float64)) for w, b in layers]
+
+
+def forward16(layers, x):
+    """Activations of the BF16-weight network (FP64 arithmetic on the rounded
+    weights; the device runs the same products in FP32)."""
+    return forward(layers16(layers), np.asarray(np.float32(x), np.float64))
+
+
+def loss_grad16(layers, x, y, rows=None):
+    """Loss and gradient of the BF16-weight network with respect to its
+    weights, which the device applies to the FP32 masters."""
+    return loss_grad(layers16(layers), np.asarray(np.float32(x), np.float64),
+                     np.asarray(np.float32(y), np.float64), rows)

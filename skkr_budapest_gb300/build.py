@@ -11,7 +11,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "_lib", "libskkr_gpu.so")
-SOURCES = ["kernels_fp64.cu", "kernels_mixed.cu", "kernels_mlp.cu", "kernels_kambe.cu", "capi.cu", "noalloc.cu"]
+SOURCES = ["kernels_fp64.cu", "kernels_mixed.cu", "kernels_mlp.cu", "kernels_mlp16.cu", "kernels_kambe.cu", "capi.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-I" + os.path.join(ROOT, "include")]

@@ -1,32 +1,46 @@
-"""Learned warm start of the CPA loop.
+"""Learned warm start of the CPA loop (the C4 surrogate).
 
 The CPA iteration of rsp-scf/fullcpa.f (cpacor/cpasol) starts from the
 coherent inverse t-matrix m_c it is given: the ATA average (tata,
 fullcpa.f:2-23) or an effective t-matrix read back from a previous run
-(main/tcpaio.f:193-276).  Here a small MLP maps the single-site data of one
-alloy layer at one energy to its converged m_c; the CPA iteration itself is
-unchanged (same update, same error3 test, same tolerance), only its starting
-point moves, so the converged result is the same up to the CPA tolerance.
+(main/tcpaio.f:193-276).  Here a network trained on converged CPA solutions
+of the method itself predicts m_c; the CPA iteration is unchanged (same
+update, same error3 test, same tolerance), only its starting point moves, so
+the converged result is the same up to the CPA tolerance.
 
-Features of (alloy layer, energy), from the (kappa,mu)-diagonal screened
-inverse t-matrices of the two species (one value per kappa):
-    Re E, Im E, c, Re/Im m_A(kappa), Re/Im m_B(kappa)
-Target, per kappa: (m_c(kappa) - m_ATA(kappa)) / |m_A(kappa) - m_B(kappa)|
-(Re, Im), with m_c(kappa) the mu-average of the converged diagonal.  The
-warm start is m_ATA + diag(prediction), off-diagonal elements from ATA (zero
-for these diagonal species).  The "continuation" variant also reads the
-converged target of the same layer at the previous contour energy (a proxy
-for the lattice environment, which the single-site features cannot see).
+The system family (C4): the relativistic bcc(001) PL4 lmax=3 interface of
+the benchmarked workload with 4 alloy layers A_c B_(1-c); every other layer
+and the leads are fixed, each alloy layer draws c ~ U[0.1, 0.9] and square-
+well depths of A and B ~ U[-1.2, -0.4] Ry.  The coherent t-matrix of one
+alloy layer depends on the whole alloy stack, so the inputs of one sample
+(one alloy layer at one energy) are
 
-    python -m skkr_budapest_gb300.cpa_warmstart gen   --out data.npz     (GPU)
-    python -m skkr_budapest_gb300.cpa_warmstart train --data data.npz --out model.npz
-    python -m skkr_budapest_gb300.cpa_warmstart report --model model.npz    (GPU)
+    Re E, Im E, the layer's position (one-hot over the 4 alloy layers),
+    then for the layer itself and the other alloy layers in stack order:
+    c, Re/Im of the kappa-diagonal of m_A and of m_B
+
+(E, c and the diagonals of t_A / t_B, the C4 inputs, for the whole stack).
+The output is the correction of the converged m_c to the ATA start on the
+elements the point group leaves free (the matrices with R_g m L_g = m for
+all g; 256 of the 32 x 32 elements at lmax=3), divided by the layer's mean
+|m_A - m_B| over kappa.  The warm start is m_ATA + the prediction projected
+onto those invariant matrices.
+
+The network is 3 tanh hidden layers of 256 with BF16 weights and FP32
+accumulation, trained and evaluated by this library's own kernels
+(skkr_gpu_mlp16_*: forward, backward, AdamW on FP32 masters).
+
+    python -m skkr_budapest_gb300.cpa_warmstart gen   --out data.npz   (GPU)
+    python -m skkr_budapest_gb300.cpa_warmstart train --data data.npz  (GPU)
+    python -m skkr_budapest_gb300.cpa_warmstart report                 (GPU)
 """
 from __future__ import annotations
 
 import argparse
+import copy
 import os
 import time
+from dataclasses import dataclass, field
 
 import numpy as np
 
@@ -34,7 +48,59 @@ from . import synth as S
 from . import workloads as W
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-DEFAULT_MODEL = os.path.join(HERE, "data", "cpa_mlp_bcc_lmax3.npz")
+DEFAULT_MODEL = os.path.join(HERE, "data", "cpa_surrogate_c4.npz")
+HIDDEN = (256, 256, 256)
+
+
+@dataclass
+class Family:
+    """The C4 alloy interface family: host system fixed, alloy stack drawn."""
+    nset: int = 6                      # IBZ subdivision of the k mesh of every energy
+    host_seed: int = 2                 # leads and non-alloy layers (rel_bcc_cpa's seed)
+    so_split: float = 0.03             # j = l +- 1/2 split of the well depths, as the C2 interface
+    lmax: int = 3
+    alloy_layers: tuple = (4, 5, 6, 7)
+    conc_range: tuple = (0.1, 0.9)
+    depth_range: tuple = (-1.2, -0.4)
+    energies: tuple = tuple(range(24))
+    _base: dict = field(default_factory=dict, repr=False)
+
+    def spec(self):
+        s = W.rel_bcc_cpa(so_split=self.so_split)
+        s.seed = self.host_seed
+        s.lmax = self.lmax
+        s.nsets = [self.nset] * len(s.energies)
+        return s
+
+    def base(self, ie: int):
+        """The EnergyProblem of contour energy ie with the host's own alloy
+        draw (its table and leads are what every configuration shares)."""
+        if ie not in self._base:
+            self._base[ie] = W.energy_problem(self.spec(), ie)
+        return self._base[ie]
+
+    def draw(self, rng):
+        na = len(self.alloy_layers)
+        return (rng.uniform(*self.conc_range, na), rng.uniform(*self.depth_range, na),
+                rng.uniform(*self.depth_range, na))
+
+    def problem(self, ie: int, cfg):
+        """Energy ie with the alloy stack cfg = (c, depth_A, depth_B): species
+        t^-1 of the drawn wells, ATA start (tata) on the alloy layers."""
+        b = self.base(ie)
+        ep = copy.copy(b)
+        conc, da, db = cfg
+        ep.conc = b.conc.copy()
+        ep.tminva, ep.tminvb, ep.tminv = b.tminva.copy(), b.tminvb.copy(), b.tminv.copy()
+        alpha = b.alpha[0]
+        for j, li in enumerate(self.alloy_layers):
+            ta = S.screened_tinv_rel(b.ce, b.psq, da[j], b.meta["radius"], self.so_split, alpha, self.lmax)
+            tb = S.screened_tinv_rel(b.ce, b.psq, db[j], b.meta["radius"], self.so_split, alpha, self.lmax)
+            ep.conc[li] = conc[j]
+            ep.tminva[li], ep.tminvb[li] = ta, tb
+            ep.tminv[li] = W.ata(conc[j], ta, tb)
+        ep.meta = dict(b.meta, cfg=cfg)
+        return ep
 
 
 def kappa_groups(lmax: int):
@@ -47,228 +113,217 @@ def kappa_groups(lmax: int):
     return [np.nonzero(kv == k)[0] for k in kappas]
 
 
-def _kdiag(m: np.ndarray, groups) -> np.ndarray:
+def _kdiag(m, groups):
     d = np.diag(m)
     return np.array([d[g].mean() for g in groups])
 
 
-def layer_features(ep, li: int, groups) -> np.ndarray:
-    ma = _kdiag(ep.tminva[li], groups)
-    mb = _kdiag(ep.tminvb[li], groups)
-    return np.concatenate([[ep.ce.real, ep.ce.imag, ep.conc[li]], ma.real, ma.imag, mb.real, mb.imag])
+def invariant_projector(ep):
+    """P(m) = (1/ng) sum_g R_g m L_g: the point-group average under which the
+    k-summed tau and hence the converged m_c are invariant."""
+    lg, rg = np.asarray(ep.lg), np.asarray(ep.rg)
+    return lambda m: np.einsum("gij,jk,gkl->il", rg, m, lg) / len(lg)
 
 
-def _ata_kdiag(ep, li, groups):
-    ma = _kdiag(ep.tminva[li], groups)
-    mb = _kdiag(ep.tminvb[li], groups)
-    c = ep.conc[li]
-    ata = ma * mb / (c * mb + (1.0 - c) * ma)   # tata for diagonal species
-    return ata, np.abs(ma - mb) + 1e-30
+def free_elements(ep):
+    """Mask of the matrix elements that invariant matrices can carry."""
+    P = invariant_projector(ep)
+    n = ep.lkmax
+    rng = np.random.default_rng(0)
+    acc = np.zeros((n, n))
+    for _ in range(3):
+        acc += np.abs(P(rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n))))
+    return acc > 1e-9 * acc.max()
 
 
-def layer_target(ep, li: int, mc: np.ndarray, groups) -> np.ndarray:
-    ata, scale = _ata_kdiag(ep, li, groups)
-    r = (_kdiag(mc, groups) - ata) / scale
-    return np.concatenate([r.real, r.imag])
+def stack_features(ep, fam: Family):
+    """One input row per alloy layer (see the module docstring)."""
+    groups = kappa_groups(fam.lmax)
+    al = list(fam.alloy_layers)
+    per = {}
+    for li in al:
+        ma, mb = _kdiag(ep.tminva[li], groups), _kdiag(ep.tminvb[li], groups)
+        per[li] = np.concatenate([[ep.conc[li]], ma.real, ma.imag, mb.real, mb.imag])
+    rows = []
+    for j, li in enumerate(al):
+        onehot = np.zeros(len(al))
+        onehot[j] = 1.0
+        order = [li] + [x for x in al if x != li]
+        rows.append(np.concatenate([[ep.ce.real, ep.ce.imag], onehot] + [per[x] for x in order]))
+    return np.array(rows)
+
+
+def _scale(ep, li, groups):
+    return np.abs(_kdiag(ep.tminva[li], groups) - _kdiag(ep.tminvb[li], groups)).mean() + 1e-30
+
+
+def stack_targets(ep, mc, fam: Family, mask):
+    """(m_c - m_ATA) on the free elements, Re then Im, over the layer's scale."""
+    groups = kappa_groups(fam.lmax)
+    out = []
+    for li in fam.alloy_layers:
+        d = (mc[li] - ep.tminv[li])[mask] / _scale(ep, li, groups)
+        out.append(np.concatenate([d.real, d.imag]))
+    return np.array(out)
+
+
+def bf16_round(a):
+    """Nearest BF16 value (ties to even) of the FP32 value of each entry."""
+    f = np.ascontiguousarray(a, np.float32)
+    u = f.view(np.uint32).astype(np.uint64)
+    r = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return r.astype(np.uint32).view(np.float32)
 
 
 class Model:
-    """Inference of the trained MLP (tanh hidden layers) in numpy."""
+    """The trained surrogate: FP32 master layers, input and output
+    normalisation, the free-element mask."""
 
     def __init__(self, path: str = DEFAULT_MODEL):
         z = np.load(path)
-        self.layers = [(z["w%d" % i], z["b%d" % i]) for i in range(int(z["nlayers"]))]
+        self.layers = [(z["w%d" % i].astype(np.float32), z["b%d" % i].astype(np.float32))
+                       for i in range(int(z["nlayers"]))]
         self.xmean, self.xstd = z["xmean"], z["xstd"]
         self.ymean, self.ystd = z["ymean"], z["ystd"]
-        self.lmax = int(z["lmax"])
-        self.cont = bool(z["cont"]) if "cont" in z else False
+        self.mask = z["mask"].astype(bool)
+        self.nset = int(z["nset"])
+        self.so_split = float(z["so_split"])
+        self.info = {k: z[k] for k in z.files if k.startswith(("train_", "val_", "n_"))}
 
-    def predict(self, x: np.ndarray, device: str = "cpu") -> np.ndarray:
-        h = (np.atleast_2d(x) - self.xmean) / self.xstd
+    def predict(self, x, device: str = "gpu"):
+        """Normalised outputs -> targets.  device "gpu": the library's BF16
+        forward kernel; "host": the same network in numpy (rounded weights,
+        FP32 arithmetic), for machines without a GPU."""
+        h = np.float32((np.atleast_2d(x) - self.xmean) / self.xstd)
         if device == "gpu":
             from . import native as N
-            return N.mlp_forward(self.layers, h) * self.ystd + self.ymean
-        for i, (w, b) in enumerate(self.layers):
-            h = h @ w + b
-            if i < len(self.layers) - 1:
-                h = np.tanh(h)
-        return h * self.ystd + self.ymean
+            y = N.mlp16_forward(self.layers, h)
+        else:
+            y = h
+            for i, (w, b) in enumerate(self.layers):
+                y = np.float32(y @ bf16_round(w) + b)
+                if i < len(self.layers) - 1:
+                    y = np.tanh(y)
+        return y * self.ystd + self.ymean
+
+    def family(self):
+        return Family(nset=self.nset, so_split=self.so_split)
 
 
-def warm_start(ep, model: Model, prev=None) -> np.ndarray:
-    """Starting coherent t^-1 for every interface layer: the MLP estimate on
-    alloy layers (conc strictly between 0 and 1), the given one elsewhere.
-    prev = (EnergyProblem, converged tminv) of the previous contour energy,
-    read by a continuation model (zeros without it)."""
-    groups = kappa_groups(ep.lmax)
+def warm_start(ep, model: Model, fam: Family | None = None, device: str = "gpu"):
+    """Starting coherent t^-1: m_ATA + the projected prediction on the alloy
+    layers of the family, the given start elsewhere."""
+    fam = fam or model.family()
+    groups = kappa_groups(fam.lmax)
+    pred = model.predict(stack_features(ep, fam), device)
+    P = invariant_projector(ep)
     tm = np.array(ep.tminv, copy=True)
-    alloy = [li for li in range(ep.nintfc) if 1e-6 < ep.conc[li] < 1.0 - 1e-6]
-    if not alloy:
-        return tm
-    feats = []
-    for li in alloy:
-        f = layer_features(ep, li, groups)
-        if model.cont:
-            pt = (layer_target(prev[0], li, prev[1][li], groups) if prev is not None
-                  else np.zeros(2 * len(groups)))
-            f = np.concatenate([f, pt])
-        feats.append(f)
-    pred = model.predict(np.array(feats))
-    ng = len(groups)
-    for row, li in zip(pred, alloy):
-        ata, scale = _ata_kdiag(ep, li, groups)
-        mk = ata + (row[:ng] + 1j * row[ng:]) * scale
-        m = np.zeros_like(tm[li])
-        for g, v in zip(groups, mk):
-            m[g, g] = v
-        tm[li] = m
+    nm = int(model.mask.sum())
+    for row, li in zip(pred, fam.alloy_layers):
+        d = np.zeros_like(tm[li])
+        d[model.mask] = (row[:nm] + 1j * row[nm:]) * _scale(ep, li, groups)
+        tm[li] = ep.tminv[li] + P(d)
     return tm
 
 
-def _spec(seed: int, lmax: int = 3):
-    # the committed models were trained on the j-split (0.03 Ry) inputs
-    spec = W.rel_bcc_cpa(nsets=[4] * 24, so_split=0.03)
-    spec.seed = seed
-    spec.lmax = lmax
-    return spec
-
-
-def generate(out: str, seeds, nset: int, lmax: int = 3, max_seconds: float = 1e9, precision="fp64"):
-    """Converged CPA solutions of seeded C4 variants (4 alloy layers each) on
-    nset meshes, all 24 contour energies: (features, targets) per alloy layer."""
+def generate(out: str, nsolve: int, fam: Family, seed: int = 1000, precision: str = "mixed", nctx: int = 8,
+             max_seconds: float = 1e9):
+    """Converged CPA solutions of nsolve drawn alloy stacks, energies cycled
+    over the contour, nctx systems per call (skkr_gpu_cpacoord_many).  Saves
+    x [rows, 122], y [rows, 2 nfree], solve id, energy, CPA iterations."""
     from . import api
-    groups = kappa_groups(lmax)
+    rng = np.random.default_rng(seed)
+    mask = free_elements(fam.base(fam.energies[0]))
+    ctxs = [api.Context.for_problem(fam.base(fam.energies[0]), precision) for _ in range(nctx)]
     xs, ys, meta = [], [], []
     t0 = time.time()
-    ctx = None
-    for seed in seeds:
-        spec = _spec(seed, lmax)
-        for ie in range(len(spec.energies)):
-            ep = W.energy_problem(spec, ie, nset=nset)
-            if ctx is None:
-                ctx = api.Context.for_problem(ep, precision)
-            r = ctx.cpacoord(ep, check=False)
-            if r["status"] != 0:
-                continue
-            for li in spec.alloy_layers:
-                xs.append(layer_features(ep, li, groups))
-                ys.append(layer_target(ep, li, r["tminv"][li], groups))
-                meta.append((seed, ie, li, r["cpa_iterations"]))
-        print("seed %d: %d samples, %.1f s" % (seed, len(xs), time.time() - t0), flush=True)
-        if time.time() - t0 > max_seconds:
-            break
-    ctx.close()
-    np.savez(out, x=np.array(xs), y=np.array(ys), meta=np.array(meta), lmax=lmax, nset=nset)
-    return len(xs)
+    s = 0
+    try:
+        while s < nsolve and time.time() - t0 < max_seconds:
+            group = []
+            for _ in range(min(nctx, nsolve - s)):
+                ie = fam.energies[s % len(fam.energies)]
+                group.append((s, ie, fam.problem(ie, fam.draw(rng))))
+                s += 1
+            res = api.cpacoord_many([g[2] for g in group], contexts=ctxs[:len(group)], check=False)
+            for (sid, ie, ep), r in zip(group, res):
+                if r["status"] != 0 or r["cpa_error"] > ep.cpatol:
+                    continue
+                xs.append(stack_features(ep, fam))
+                ys.append(stack_targets(ep, r["tminv"], fam, mask))
+                meta += [(sid, ie, li, r["cpa_iterations"]) for li in fam.alloy_layers]
+            if s % (50 * nctx) < nctx:
+                print("%d solves, %d rows, %.1f s" % (s, 4 * len(xs), time.time() - t0), flush=True)
+    finally:
+        for c in ctxs:
+            c.close()
+    np.savez(out, x=np.concatenate(xs).astype(np.float32), y=np.concatenate(ys).astype(np.float32),
+             meta=np.array(meta, np.int32), mask=mask, nset=fam.nset, so_split=fam.so_split,
+             seconds=time.time() - t0)
+    return len(meta)
 
 
-def _dataset(data: str, cont: bool, itcpam: int = 50):
-    """(x, y, seed) of the converged samples; cont appends the previous
-    energy's target of the same (seed, layer) (samples without one dropped)."""
+def train(data: str, out: str, epochs: int = 4000, lr: float = 1e-3, weight_decay: float = 0.0, seed: int = 0,
+          val_frac: float = 0.1, eval_every: int = 25):
+    """Full-batch AdamW of the BF16-weight network on the device
+    (skkr_gpu_mlp16_train), last val_frac of the solves held out, the epoch
+    with the lowest held-out error kept.  Returns (train mse, held-out mse,
+    held-out mse of the ATA start), all in units of the normalised targets."""
+    from . import native as N
     z = np.load(data)
-    x, y, meta = z["x"], z["y"], z["meta"]
-    ok = meta[:, 3] < itcpam                      # CPA converged within its cap
-    if cont:
-        key = {(int(a), int(b), int(c)): i for i, (a, b, c, _) in enumerate(meta)}
-        prev = np.array([key.get((int(a), int(b) - 1, int(c)), -1) for a, b, c, _ in meta])
-        ok &= prev >= 0
-        ok &= meta[np.maximum(prev, 0), 3] < itcpam
-        x = np.c_[x, y[np.maximum(prev, 0)]]
-    return x[ok], y[ok], meta[ok, 0], int(z["lmax"])
-
-
-def train(data: str, out: str, hidden: int = 64, epochs: int = 3000, seed: int = 0, val_frac: float = 0.1,
-          cont: bool = False, weight_decay: float = 1e-4, device: str = "cpu"):
-    """Full-batch AdamW on the mean squared error of the targets (one global
-    target scale); the last val_frac of the seeds is held out and the epoch
-    with the lowest held-out error is kept.  device "gpu": this library's
-    forward, backward and AdamW kernels (skkr_gpu_mlp_train) from a seeded
-    uniform(-1/sqrt(fan_in), 1/sqrt(fan_in)) start; "cpu": torch."""
-    x, y, sd, lmax = _dataset(data, cont)
-    seeds = np.unique(sd)
-    nval = max(1, int(len(seeds) * val_frac))
-    val = np.isin(sd, seeds[-nval:])
+    x, y, meta = z["x"].astype(np.float64), z["y"].astype(np.float64), z["meta"]
+    sid = meta[:, 0]
+    solves = np.unique(sid)
+    nval = max(1, int(len(solves) * val_frac))
+    val = np.isin(sid, solves[-nval:])
     xm, xsd = x[~val].mean(0), x[~val].std(0) + 1e-12
-    ym, ysd = np.zeros(y.shape[1]), np.full(y.shape[1], y[~val].std() + 1e-12)
-    dims = [x.shape[1], hidden, hidden, y.shape[1]]
-    if device == "gpu":
-        from . import native as N
-        rng = np.random.default_rng(seed)
-        init = [(rng.uniform(-1, 1, (a, b)) / np.sqrt(a), rng.uniform(-1, 1, b) / np.sqrt(a))
-                for a, b in zip(dims[:-1], dims[1:])]
-        _, wts, _, (vl, tl) = N.mlp_train(init, (x - xm) / xsd, (y - ym) / ysd, (~val).astype(np.uint8),
-                                          epochs, 2e-3, weight_decay, eval_every=20)
-        return _save_model(out, wts, xm, xsd, ym, ysd, lmax, cont, tl, vl, y, val)
-    import torch
-    torch.manual_seed(seed)
-    lins = [torch.nn.Linear(a, b, dtype=torch.float64) for a, b in zip(dims[:-1], dims[1:])]
-    params = [p for l in lins for p in l.parameters()]
-    opt = torch.optim.AdamW(params, lr=2e-3, weight_decay=weight_decay)
-
-    def fwd(t):
-        for i, l in enumerate(lins):
-            t = l(t)
-            if i < len(lins) - 1:
-                t = torch.tanh(t)
-        return t
-
-    xt = torch.tensor((x - xm) / xsd)
-    yt = torch.tensor((y - ym) / ysd)
-    tr = torch.tensor(~val)
-    best = (float("inf"), None, None)
-    for ep_ in range(epochs):
-        opt.zero_grad()
-        loss = ((fwd(xt[tr]) - yt[tr]) ** 2).mean()
-        loss.backward()
-        opt.step()
-        if ep_ % 20 == 0 or ep_ == epochs - 1:
-            with torch.no_grad():
-                vl = ((fwd(xt[~tr]) - yt[~tr]) ** 2).mean().item()
-            if vl < best[0]:
-                best = (vl, loss.item(), [(l.weight.detach().clone(), l.bias.detach().clone()) for l in lins])
-    vl, tl, wts = best
-    wts = [(w.numpy().T.copy(), b.numpy().copy()) for w, b in wts]
-    return _save_model(out, wts, xm, xsd, ym, ysd, lmax, cont, tl, vl, y, val)
-
-
-def _save_model(out, wts, xm, xsd, ym, ysd, lmax, cont, tl, vl, y, val):
-    save = {"nlayers": len(wts), "xmean": xm, "xstd": xsd, "ymean": ym, "ystd": ysd, "lmax": lmax,
-            "cont": int(cont), "train_mse": tl * ysd[0] ** 2, "val_mse": vl * ysd[0] ** 2,
-            "val_mse_ata": float((y[val] ** 2).mean())}
-    for i, (w, b) in enumerate(wts):
-        save["w%d" % i] = np.asarray(w, np.float64)
-        save["b%d" % i] = np.asarray(b, np.float64)
+    ym, ysd = y[~val].mean(0), y[~val].std(0) + 1e-12
+    dims = [x.shape[1], *HIDDEN, y.shape[1]]
+    rng = np.random.default_rng(seed)
+    init = [(np.float32(rng.uniform(-1, 1, (a, b)) / np.sqrt(a)), np.zeros(b, np.float32))
+            for a, b in zip(dims[:-1], dims[1:])]
+    _, best, tl, (vl, trl) = N.mlp16_train(init, (x - xm) / xsd, (y - ym) / ysd, (~val).astype(np.uint8),
+                                           epochs, lr, weight_decay, eval_every=eval_every)
+    # errors in target units (what the warm start is off by), and the ATA start's
+    pred = N.mlp16_forward(best, np.float32((x - xm) / xsd)) * ysd + ym
+    mse_val = float(((pred[val] - y[val]) ** 2).mean())
+    mse_tr = float(((pred[~val] - y[~val]) ** 2).mean())
+    mse_ata = float((y[val] ** 2).mean())
+    save = {"nlayers": len(best), "xmean": xm, "xstd": xsd, "ymean": ym, "ystd": ysd, "mask": z["mask"],
+            "nset": int(z["nset"]), "so_split": float(z["so_split"]), "train_mse": mse_tr, "val_mse": mse_val,
+            "val_mse_ata": mse_ata, "train_epochs": epochs, "train_loss_curve": tl[::max(1, epochs // 200)],
+            "n_rows": len(x), "n_solves": len(solves)}
+    for i, (w, b) in enumerate(best):
+        save["w%d" % i] = np.asarray(w, np.float32)
+        save["b%d" % i] = np.asarray(b, np.float32)
     os.makedirs(os.path.dirname(os.path.abspath(out)), exist_ok=True)
     np.savez(out, **save)
-    return save["train_mse"], save["val_mse"], save["val_mse_ata"]
+    return mse_tr, mse_val, mse_ata
 
 
-def report(model_paths, seeds, energies, nset: int, lmax: int = 3, precision="fp64"):
-    """CPA iterations, final error3 and device time from the ATA start and
-    from each learned start on held-out configurations, energies in contour
-    order (a continuation model reads its own previous converged result),
-    and the agreement of the converged tau with the ATA-started run."""
+def report(model_path: str, nsolve: int, seed: int = 9001, precision: str = "mixed"):
+    """Held-out alloy stacks (a seed the training never drew), energies cycled
+    over the contour: CPA iterations, final error3 and device time from the
+    ATA start and from the learned start, and the agreement of the converged
+    tau.  Returns the per-solve rows."""
     from . import api
-    models = [Model(p) for p in model_paths]
+    model = Model(model_path)
+    fam = model.family()
+    rng = np.random.default_rng(seed)
+    ctx = api.Context.for_problem(fam.base(fam.energies[0]), precision)
     rows = []
-    for seed in seeds:
-        spec = _spec(seed, lmax)
-        prev = [None] * len(models)
-        ctx = None
-        for ie in energies:
-            ep = W.energy_problem(spec, ie, nset=nset)
-            if ctx is None:
-                ctx = api.Context.for_problem(ep, precision)
+    try:
+        for s in range(nsolve):
+            ie = fam.energies[s % len(fam.energies)]
+            ep = fam.problem(ie, fam.draw(rng))
             a = ctx.cpacoord(ep, check=False)
-            row = dict(seed=seed, ie=ie, nk=ep.nk, runs=[("ATA", a["cpa_iterations"], a["cpa_error"], a["run_ms"], 0.0,
-                                                            a["status"])])
-            for i, (mp, model) in enumerate(zip(model_paths, models)):
-                b = ctx.cpacoord(ep, tminv=warm_start(ep, model, prev[i]), check=False)
-                d = np.linalg.norm(b["tauc"] - a["tauc"]) / np.linalg.norm(a["tauc"])
-                row["runs"].append((os.path.basename(mp), b["cpa_iterations"], b["cpa_error"], b["run_ms"], d,
-                                    b["status"]))
-                prev[i] = (ep, b["tminv"]) if b["status"] == 0 else None
-            rows.append(row)
+            ws = warm_start(ep, model, fam)
+            b = ctx.cpacoord(ep, tminv=ws, check=False)
+            d = float(np.linalg.norm(b["tauc"] - a["tauc"]) / np.linalg.norm(a["tauc"]))
+            rows.append(dict(ie=ie, nk=ep.nk, it_ata=a["cpa_iterations"], it_mlp=b["cpa_iterations"],
+                             err_ata=a["cpa_error"], err_mlp=b["cpa_error"], ms_ata=a["run_ms"], ms_mlp=b["run_ms"],
+                             st=(a["status"], b["status"]), dtau=d))
+    finally:
         ctx.close()
     return rows
 
@@ -278,49 +333,37 @@ def main():
     sub = ap.add_subparsers(dest="cmd", required=True)
     g = sub.add_parser("gen")
     g.add_argument("--out", required=True)
-    g.add_argument("--seeds", type=int, default=200)
-    g.add_argument("--seed0", type=int, default=1000)
-    g.add_argument("--nset", type=int, default=4)
-    g.add_argument("--max-seconds", type=float, default=600.0)
+    g.add_argument("--solves", type=int, default=5000)
+    g.add_argument("--nset", type=int, default=6)
+    g.add_argument("--so-split", type=float, default=0.03)
+    g.add_argument("--max-seconds", type=float, default=1200.0)
     t = sub.add_parser("train")
     t.add_argument("--data", required=True)
     t.add_argument("--out", default=DEFAULT_MODEL)
-    t.add_argument("--epochs", type=int, default=3000)
-    t.add_argument("--cont", action="store_true")
-    t.add_argument("--device", choices=("cpu", "gpu"), default="cpu")
+    t.add_argument("--epochs", type=int, default=4000)
+    t.add_argument("--lr", type=float, default=1e-3)
     r = sub.add_parser("report")
-    r.add_argument("--models", default=DEFAULT_MODEL)
-    r.add_argument("--seeds", default="9001,9002,9003")
-    r.add_argument("--energies", default="0,2,4,6,8,10,12,14,16")
-    r.add_argument("--nset", type=int, default=20)
+    r.add_argument("--model", default=DEFAULT_MODEL)
+    r.add_argument("--solves", type=int, default=48)
     a = ap.parse_args()
     if a.cmd == "gen":
-        n = generate(a.out, range(a.seed0, a.seed0 + a.seeds), a.nset, max_seconds=a.max_seconds)
-        print("samples:", n)
+        n = generate(a.out, a.solves, Family(nset=a.nset, so_split=a.so_split), max_seconds=a.max_seconds)
+        print("rows:", n)
     elif a.cmd == "train":
-        print("mse train / held out / held out of the ATA start: %.3e / %.3e / %.3e" % train(
-            a.data, a.out, epochs=a.epochs, cont=a.cont, device=a.device))
+        print("mse train / held out / held out of the ATA start: %.3e / %.3e / %.3e"
+              % train(a.data, a.out, epochs=a.epochs, lr=a.lr))
     else:
-        paths = a.models.split(",")
-        rows = report(paths, [int(s) for s in a.seeds.split(",")], [int(e) for e in a.energies.split(",")],
-                      a.nset)
-        names = [r[0] for r in rows[0]["runs"]]
-        print("| seed | E | nk | " + " | ".join("CPA it. %s | error3 %s | ms %s" % (n, n, n) for n in names)
-              + " | max rel diff tau |")
-        print("|---|---|---|" + "---|---|---|" * len(names) + "---|")
-        tot = np.zeros(len(names))
-        ms = np.zeros(len(names))
+        rows = report(a.model, a.solves)
+        ita = sum(r["it_ata"] for r in rows)
+        itm = sum(r["it_mlp"] for r in rows)
+        print("| E | nk | CPA it. ATA | CPA it. MLP | error3 ATA | error3 MLP | ms ATA | ms MLP | rel diff tau |")
+        print("|---|---|---|---|---|---|---|---|---|")
         for x in rows:
-            cells = []
-            for k, (n, it, er, t, d, st) in enumerate(x["runs"]):
-                cells.append("%d | %.1e | %.1f" % (it, er, t))
-                tot[k] += it
-                ms[k] += t
-            print("| %d | %d | %d | %s | %.1e |" % (x["seed"], x["ie"], x["nk"], " | ".join(cells),
-                                                   max(r[4] for r in x["runs"])))
-        print()
-        for n, it, t in zip(names, tot, ms):
-            print("%s: %d CPA iterations (%.1f%% of ATA), %.1f ms device time" % (n, it, 100 * it / tot[0], t))
+            print("| %d | %d | %d | %d | %.1e | %.1e | %.1f | %.1f | %.1e |" % (
+                x["ie"], x["nk"], x["it_ata"], x["it_mlp"], x["err_ata"], x["err_mlp"], x["ms_ata"], x["ms_mlp"],
+                x["dtau"]))
+        print("\ntotal CPA iterations: ATA %d, MLP %d (%.1f %%); device time ATA %.1f ms, MLP %.1f ms"
+              % (ita, itm, 100.0 * itm / ita, sum(r["ms_ata"] for r in rows), sum(r["ms_mlp"] for r in rows)))
 
 
 if __name__ == "__main__":

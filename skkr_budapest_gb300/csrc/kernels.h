@@ -134,6 +134,26 @@ void mlp_launch_adamw(double *p, const double *g, double *m, double *v, long lon
 void mlp_launch_keep_best(const double *val, const double *train, double *best, const double *p, double *pbest,
                           long long np, cudaStream_t st);
 
+// the warm-start network with BF16 weights and FP32 activations
+// (kernels_mlp16.cu): Z = act(H W16 + b), dH = dZ W16^T, the packed W-then-b
+// gradient with its row sum split into nsplit ordered ranges (part:
+// [nsplit][din][dout] scratch), loss, tanh', AdamW on the FP32 masters with
+// their BF16 copies refreshed
+struct __nv_bfloat16;
+void mlp16_dense(const float *H, int n, int din, const __nv_bfloat16 *W16, const float *b, int dout, int act, float *Z,
+                 cudaStream_t st);
+void mlp16_hgrad(const float *dZ, int n, int din, int dout, const __nv_bfloat16 *W16, float *dH, cudaStream_t st);
+void mlp16_wgrad(const float *H, const float *dZ, int n, int din, int dout, float *g, float *part, int nsplit,
+                 cudaStream_t st);
+void mlp16_loss(const float *Yh, const float *Y, const unsigned char *sel, int want, int n, int dout, float scale,
+                float *dY, float *rowsum, float *out, cudaStream_t st);
+void mlp16_tanh_back(const float *A, float *G, long long m, cudaStream_t st);
+void mlp16_adamw(float *p, const float *g, float *m, float *v, __nv_bfloat16 *p16, long long np, float lr, float wd,
+                 float b1, float b2, float eps, float step_size, float bc2_sqrt, cudaStream_t st);
+void mlp16_to_bf16(const float *p, __nv_bfloat16 *q, long long np, cudaStream_t st);
+void mlp16_keep_best(const float *val, const float *train, float *best, const float *p, float *pbest, long long np,
+                     cudaStream_t st);
+
 // Kambe lattice sums D_L(k, s) (kernels_kambe.cu): out[item][(lmax2+1)^2] complex
 void launch_kambe_dlm(int nitem, double er, double ei, const double *kxy, const double *sep, int lmax2,
                       const double *gvec, int ng, const double *rvec, int nr, double area, double factor,

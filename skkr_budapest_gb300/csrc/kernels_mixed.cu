@@ -32,6 +32,7 @@
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -948,6 +949,9 @@ static int split_s(MixedWork *w, int side, int slot, const MatRef &M, int n, int
   Stage &sg = side == 0 ? w->A[slot] : w->B[slot];
   const int rows = side == 0 ? Mp : Np;
   int rc;
+  // a buffer cannot be reallocated inside a captured graph: the eager run
+  // before any capture sizes every slot (mixed_zinv reserves its further steps')
+  if ((size_t)items * S * rows * Kp * 2 > sg.cap && stream_capturing(st)) return SKKR_ERR_CUDA;
   if ((rc = grow(&sg.p, &sg.cap, (size_t)items * S * rows * Kp * 2, true))) return rc;
   if ((rc = grow((void **)&sg.scale, &sg.scap, (size_t)items * (side == 0 ? Mp : n) * sizeof(int), false)))
     return rc;
@@ -1207,6 +1211,21 @@ int mixed_zinv(MixedWork *w, const MatRef &A, const MatRef &X, int n, int nk, in
   if ((rc = grow((void **)&w->rnorm, &w->rn_cap, (size_t)items * sizeof(double), false))) return rc;
   if ((rc = grow((void **)&w->flag, &w->flag_cap, (size_t)items * sizeof(int), false))) return rc;
   if ((rc = grow((void **)&w->mark, &w->mark_cap, (size_t)items * sizeof(int), false))) return rc;
+  // the further Newton steps split X and R into slot 5 at sres slices (the
+  // standard correction uses 3): reserve that size, for either B tile, while
+  // not capturing, so that a captured step never has to grow the slot
+  if (!stream_capturing(st)) {
+    int Se, DB, Mp, Np, Kp, mt, ntl, kbl;
+    oz_digits(sres, n, &Se, &DB);
+    size_t bb = 0, ba = 0;
+    for (int tn : {NT, 64}) {
+      oz_dims(n, n, tn, &Mp, &Np, &Kp, &mt, &ntl, &kbl);
+      ba = (size_t)items * Se * Mp * Kp * 2;
+      bb = std::max(bb, (size_t)items * Se * Np * Kp * 2);
+    }
+    if ((rc = grow(&w->A[5].p, &w->A[5].cap, ba, true))) return rc;
+    if ((rc = grow(&w->B[5].p, &w->B[5].cap, bb, true))) return rc;
+  }
   // A itself serves the Gauss-Jordan start, the residuals and the FP64 redo
   // unless X overwrites it (in place): then a copy does
   const MatRef Ac = inplace ? mref(w->acopy, (long long)nc * MB, MB, n) : A;

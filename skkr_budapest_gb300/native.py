@@ -252,6 +252,63 @@ def mlp_train(layers, x, y, rows, epochs, lr, weight_decay, eval_every=20):
     return _mlp_unpack(dims, params), _mlp_unpack(dims, bp), tl, (float(best[0]), float(best[1]))
 
 
+def _mlp16_args(layers):
+    dims, params = _mlp_args(layers)
+    return dims, params.astype(np.float32)
+
+
+def _mlp16_lib():
+    L = lib()
+    F = C.c_float
+    L.skkr_gpu_mlp16_forward.argtypes = [I, P, P, I, P, P]
+    L.skkr_gpu_mlp16_grad.argtypes = [I, P, P, I, P, P, P, P, P]
+    L.skkr_gpu_mlp16_train.argtypes = [I, P, P, I, P, P, P, I, F, F, I, P, P, P]
+    return L
+
+
+def mlp16_forward(layers, x):
+    """Device forward of the BF16-weight network (skkr_gpu_mlp16_forward):
+    FP32 master layers in, FP32 outputs."""
+    dims, params = _mlp16_args(layers)
+    x = np.ascontiguousarray(x, np.float32)
+    y = np.zeros((len(x), dims[-1]), np.float32)
+    _check(_mlp16_lib().skkr_gpu_mlp16_forward(len(layers), _p(dims), _p(params), len(x), _p(x), _p(y)),
+           "skkr_gpu_mlp16_forward")
+    return y
+
+
+def mlp16_grad(layers, x, y, rows=None):
+    """Device loss and gradient [(dW, db), ...] of the BF16-weight network
+    (skkr_gpu_mlp16_grad)."""
+    dims, params = _mlp16_args(layers)
+    x = np.ascontiguousarray(x, np.float32)
+    y = np.ascontiguousarray(y, np.float32)
+    r = None if rows is None else np.ascontiguousarray(rows, np.uint8)
+    loss = np.zeros(1, np.float32)
+    grad = np.zeros_like(params)
+    _check(_mlp16_lib().skkr_gpu_mlp16_grad(len(layers), _p(dims), _p(params), len(x), _p(x), _p(y),
+                                            None if r is None else _p(r), _p(loss), _p(grad)),
+           "skkr_gpu_mlp16_grad")
+    return float(loss[0]), _mlp_unpack(dims, grad)
+
+
+def mlp16_train(layers, x, y, rows, epochs, lr, weight_decay, eval_every=20):
+    """Device training of the BF16-weight network (skkr_gpu_mlp16_train);
+    returns as mlp_train, FP32 master layers."""
+    dims, params = _mlp16_args(layers)
+    x = np.ascontiguousarray(x, np.float32)
+    y = np.ascontiguousarray(y, np.float32)
+    r = None if rows is None else np.ascontiguousarray(rows, np.uint8)
+    tl = np.zeros(int(epochs), np.float32)
+    best = np.zeros(2, np.float32)
+    bp = np.zeros_like(params)
+    _check(_mlp16_lib().skkr_gpu_mlp16_train(len(layers), _p(dims), _p(params), len(x), _p(x), _p(y),
+                                             None if r is None else _p(r), int(epochs), float(lr),
+                                             float(weight_decay), int(eval_every), _p(tl), _p(best), _p(bp)),
+           "skkr_gpu_mlp16_train")
+    return _mlp_unpack(dims, params), _mlp_unpack(dims, bp), tl, (float(best[0]), float(best[1]))
+
+
 def kambe_dlm(e, kxy, sep, lmax2, gvec, rvec, area, factor=1.0, gcut=12.0, rcut=40.0):
     """Device Kambe lattice sums D_L(k, s) of one energy for items (kxy[i],
     sep[i]) (skkr_gpu_kambe_dlm); returns (nitem, (lmax2+1)^2) complex."""

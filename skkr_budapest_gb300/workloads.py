@@ -8,7 +8,8 @@ square-well t-matrices and real-space screened structure constants.
   plain_fcc   fcc(001) a=6.8, non-relativistic lmax=2 (9/site), PL2, 6-layer
               interface, 16 energies -0.5..0.7 Ry, 253 k per energy.
   rel_bcc     bcc(001) a=6.0, relativistic lmax=3 (32/site), PL4, 12-layer
-              interface, 24 energies, 210..12090 k per energy (uneven).
+              interface, 24 energies, 210..12090 k per energy (uneven),
+              j = l +- 1/2 split wells, screening of the reference's bcc sample.
   rel_bcc_cpa rel_bcc with 4 alloy layers A_c B_(1-c).
   nonrel_pl2 / rel_pl3_l2   the two extra systems of the batched run.
 """
@@ -123,19 +124,27 @@ def plain_fcc(nset: int = 22) -> SystemSpec:
 REL_NSETS = [20] * 12 + [32] * 4 + [48] * 3 + [70] * 2 + [100, 125, 155]
 
 
-# The measured relativistic workloads carry no j = l +- 1/2 splitting of the
-# well depths (so_split = 0): with the 0.03 Ry split the doubling iteration of
-# the synthetic lead exceeds the absolute 1e10 limit of surfgf.f at some k of
-# the dense meshes near the real axis (a transient that grows with the split;
-# the oracle reproduces it), and the reference stops there.  The (kappa,mu)
-# machinery is the same; the split path is tested on meshes where it converges.
-def rel_bcc(nsets=None, so_split: float = 0.0) -> SystemSpec:
+# Screening of the bcc(001) workloads: the reference's own bcc layer sample
+# (sample/02-layer-scf: ISCREEN 1, VSCREEN 3.0 Ry, screening spheres of the
+# Wigner-Seitz radius, sws = 3.0709 a.u. of its Nb) -- 3 Ry in spheres of the
+# bcc Wigner-Seitz radius, r_WS / d_NN = (3 / (8 pi))^(1/3) / (sqrt(3) / 2).
+# With it the three-shell screened table is localised and the lead
+# decimation of the j = l +- 1/2 split wells stays below surfgf.f's 1e10
+# limit on every contour energy and mesh; the 2 Ry / 0.7 d_NN barrier of the
+# fcc configuration does neither for the split bcc lead.
+WS_BCC = (3.0 / (8.0 * math.pi)) ** (1.0 / 3.0) / (math.sqrt(3.0) / 2.0)
+
+
+def rel_bcc(nsets=None, so_split: float = 0.03, vscreen: float = 3.0, rscreen: float = WS_BCC) -> SystemSpec:
+    """The relativistic PL4 lmax=3 interface: j = l +- 1/2 split wells
+    (0.03 Ry <l.s>), the reference sample's bcc screening."""
     z = _contour(24, -0.5, 0.7, 10.0)
     return SystemSpec("rel_bcc", S.bcc001(6.0), 1, 3, 4, 3, z,
-                      list(REL_NSETS if nsets is None else nsets), seed=1, so_split=so_split)
+                      list(REL_NSETS if nsets is None else nsets), seed=1, so_split=so_split, vscreen=vscreen,
+                      rscreen=rscreen)
 
 
-def rel_bcc_cpa(nsets=None, so_split: float = 0.0) -> SystemSpec:
+def rel_bcc_cpa(nsets=None, so_split: float = 0.03) -> SystemSpec:
     s = rel_bcc(nsets, so_split)
     s.name = "rel_bcc_cpa"
     s.seed = 2
@@ -149,10 +158,11 @@ def nonrel_pl2() -> SystemSpec:
                       [14] * 8 + [20] * 4 + [40] * 2 + [80, 126], seed=3)
 
 
-def rel_pl3_l2(so_split: float = 0.0) -> SystemSpec:
+def rel_pl3_l2(so_split: float = 0.03) -> SystemSpec:
     z = _contour(20, -0.5, 0.7, 10.0)
     return SystemSpec("rel_pl3_l2", S.bcc001(6.0), 1, 2, 3, 3, z,
-                      [14] * 10 + [20] * 4 + [40] * 3 + [60, 90, 126], seed=4, so_split=so_split)
+                      [14] * 10 + [20] * 4 + [40] * 3 + [60, 90, 126], seed=4, so_split=so_split, vscreen=3.0,
+                      rscreen=WS_BCC)
 
 
 def bdg_bcc(nsets=None, lmax: int = 3, pl: int = 4, ne: int = 64, im_e: float = 1.0e-4) -> SystemSpec:

@@ -1,57 +1,74 @@
-"""Learned CPA warm start: the committed models load, their features have the
-trained shape, and the start they give is a finite kappa-diagonal matrix on
-alloy layers only (the CPA loop itself is unchanged)."""
-import os
-
+"""Learned CPA warm start (CPU): the C4 family's inputs and targets, the
+symmetry of the start, and a model file's host inference.  The ATA start has
+a zero target; the free elements are those the point-group average keeps;
+the start of any model is invariant under that average and equals ATA off
+the alloy layers."""
 import numpy as np
-import pytest
 
 from skkr_budapest_gb300 import cpa_warmstart as CW
-from skkr_budapest_gb300 import workloads as W
-
-HERE = os.path.dirname(CW.__file__)
 
 
-@pytest.mark.parametrize("name", ["cpa_mlp_bcc_lmax3.npz", "cpa_mlp_bcc_lmax3_cont.npz"])
-def test_model_start_is_diagonal_on_alloy_layers(name):
-    model = CW.Model(os.path.join(HERE, "data", name))
-    ep = W.energy_problem(CW._spec(9001), 6, nset=2)
-    groups = CW.kappa_groups(ep.lmax)
-    nf = 3 + 4 * len(groups) + (2 * len(groups) if model.cont else 0)
-    assert model.xmean.shape == (nf,)
-    tm = CW.warm_start(ep, model)
-    alloy = [li for li in range(ep.nintfc) if 1e-6 < ep.conc[li] < 1 - 1e-6]
-    assert alloy
+def _family():
+    return CW.Family(nset=2)
+
+
+def _model(tmp_path, fam, ep, scale=0.0):
+    mask = CW.free_elements(ep)
+    x = CW.stack_features(ep, fam)
+    dims = [x.shape[1], 8, 8, 8, 2 * int(mask.sum())]
+    rng = np.random.default_rng(3)
+    save = {"nlayers": 4, "xmean": x.mean(0), "xstd": np.ones(x.shape[1]), "ymean": np.zeros(dims[-1]),
+            "ystd": np.full(dims[-1], 1e-2), "mask": mask, "nset": fam.nset, "so_split": fam.so_split}
+    for i, (a, b) in enumerate(zip(dims[:-1], dims[1:])):
+        save["w%d" % i] = np.float32(rng.normal(size=(a, b)) * scale)
+        save["b%d" % i] = np.zeros(b, np.float32)
+    p = tmp_path / "m.npz"
+    np.savez(p, **save)
+    return CW.Model(str(p))
+
+
+def test_features_and_targets_of_the_alloy_stack():
+    fam = _family()
+    rng = np.random.default_rng(0)
+    ep = fam.problem(10, fam.draw(rng))
+    x = CW.stack_features(ep, fam)
+    assert x.shape == (4, 2 + 4 + 4 * 29)
+    # the target layer comes first after E and the one-hot position
+    assert np.allclose(x[:, 2:6], np.eye(4))
+    assert np.allclose(x[:, 6], ep.conc[list(fam.alloy_layers)])
+    mask = CW.free_elements(ep)
+    assert mask.sum() == 256
+    # the ATA start (what the problem carries) has a zero target
+    assert np.abs(CW.stack_targets(ep, ep.tminv, fam, mask)).max() == 0.0
+
+
+def test_ata_start_is_invariant_and_zero_model_gives_it(tmp_path):
+    fam = _family()
+    ep = fam.problem(5, fam.draw(np.random.default_rng(1)))
+    P = CW.invariant_projector(ep)
+    for li in fam.alloy_layers:
+        assert np.abs(P(ep.tminv[li]) - ep.tminv[li]).max() < 1e-12 * np.abs(ep.tminv[li]).max()
+    m0 = _model(tmp_path, fam, ep, scale=0.0)
+    ws = CW.warm_start(ep, m0, fam, device="host")
+    assert np.array_equal(ws, ep.tminv)
+
+
+def test_start_of_a_model_is_symmetric_and_local_to_the_alloy(tmp_path):
+    fam = _family()
+    ep = fam.problem(7, fam.draw(np.random.default_rng(2)))
+    m = _model(tmp_path, fam, ep, scale=0.3)
+    ws = CW.warm_start(ep, m, fam, device="host")
+    P = CW.invariant_projector(ep)
     for li in range(ep.nintfc):
-        if li in alloy:
-            assert np.all(np.isfinite(tm[li]))
-            assert np.abs(tm[li] - np.diag(np.diag(tm[li]))).max() == 0.0
-            # a correction of the ATA start, small relative to |m_A - m_B|
-            ata, scale = CW._ata_kdiag(ep, li, groups)
-            corr = (CW._kdiag(tm[li], groups) - ata) / scale
-            assert np.abs(corr).max() < 0.5
+        if li in fam.alloy_layers:
+            assert np.all(np.isfinite(ws[li]))
+            assert not np.array_equal(ws[li], ep.tminv[li])
+            assert np.abs(P(ws[li]) - ws[li]).max() < 1e-10 * np.abs(ws[li]).max()
         else:
-            assert np.array_equal(tm[li], ep.tminv[li])
+            assert np.array_equal(ws[li], ep.tminv[li])
 
 
-def test_ata_has_zero_target():
-    ep = W.energy_problem(CW._spec(9002), 3, nset=2)
-    groups = CW.kappa_groups(ep.lmax)
-    li = [l for l in range(ep.nintfc) if 1e-6 < ep.conc[l] < 1 - 1e-6][0]
-    assert np.abs(CW.layer_target(ep, li, ep.tminv[li], groups)).max() < 1e-12
-
-
-def test_host_training_writes_a_model(tmp_path):
-    pytest.importorskip("torch")
-    rng = np.random.default_rng(7)
-    n = 240
-    x = rng.normal(size=(n, 11))
-    y = 0.3 * np.tanh(x[:, :6] @ rng.normal(size=(6, 6)))
-    meta = np.c_[np.repeat(np.arange(12), n // 12), np.zeros(n), np.zeros(n), np.ones(n)]
-    data = tmp_path / "d.npz"
-    np.savez(data, x=x, y=y, meta=meta, lmax=1)
-    out = tmp_path / "m.npz"
-    tr, vl, ata = CW.train(str(data), str(out), hidden=16, epochs=200)
-    assert np.isfinite(tr) and vl < ata
-    model = CW.Model(str(out))
-    assert model.predict(x[:3]).shape == (3, 6)
+def test_bf16_rounding_ties_to_even():
+    v = np.float32([1.0 + 2.0 ** -8, 1.0 + 3 * 2.0 ** -9, -2.5, 1.0 + 2.0 ** -7 + 2.0 ** -8])
+    r = CW.bf16_round(v)
+    assert list(r) == [1.0, np.float32(1.0 + 2.0 ** -7), -2.5, np.float32(1.0 + 2.0 ** -6)]

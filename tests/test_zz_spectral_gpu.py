@@ -20,7 +20,7 @@ def test_bsf_on_the_device_matches_the_oracle():
 
 
 def test_bsf_refuses_alloy_layers():
-    from skkr_budapest_gb300 import api, cpa_warmstart as CW
-    ep = W.energy_problem(CW._spec(9001), 6, nset=2)
+    from skkr_budapest_gb300 import api
+    ep = W.energy_problem(W.rel_bcc_cpa(nsets=[2] * 24), 6)
     with pytest.raises(ValueError):
         api.bloch_spectral(ep, [(0.1, 0.1)])
