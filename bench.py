@@ -55,6 +55,10 @@ def parse():
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--no-fp64-compare", action="store_true")
     ap.add_argument("--energies", default="", help="comma list overriding the step energies")
+    ap.add_argument("--split", default="energies", choices=["energies", "k"],
+                    help="N > 1: each rank its own contour energies (weak scaling), or every energy's k points "
+                         "split round-robin over the ranks with one in-place NCCL allreduce of the k-summed tau "
+                         "per CPA iteration (strong scaling)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", action="store_true",
                     help="only the device loop of the timed steps (for ncu captures); prints a short line")
@@ -266,6 +270,7 @@ def timed_steps(ctx, order, slot_of, eps, args, flush, stats=False):
     if stats:
         N.kernel_stats_start()
     t_dev, pts, launches, dec_iters, resid, fallbacks, kfp64, refined, alg = 0.0, 0, 0, 0, 0.0, 0, 0, 0, 0.0
+    host_ops = 0
     w0 = time.perf_counter()
     for i in range(args.steps):
         ie = order[args.warmup + i]
@@ -281,11 +286,12 @@ def timed_steps(ctx, order, slot_of, eps, args, flush, stats=False):
         refined += st.inv_refined
         kfp64 += st.k_fp64
         alg += st.alg_flops
+        host_ops += st.gpu_launches - st.graph_kernels + st.graph_launches
     torch.cuda.synchronize()
     wall = time.perf_counter() - w0
     ks = N.kernel_stats_stop() if stats else None
     return dict(t_dev=t_dev, pts=pts, launches=launches, dec_iters=dec_iters, wall=wall, ks=ks, resid=resid,
-                fallbacks=fallbacks, kfp64=kfp64, refined=refined, alg=alg)
+                fallbacks=fallbacks, kfp64=kfp64, refined=refined, alg=alg, host_ops=host_ops)
 
 
 def roofline(ks, precision, alg_flops, t_dev_ms):
@@ -347,15 +353,26 @@ def run_ours(args, rank, ws):
     energies = [int(x) for x in args.energies.split(",")] if args.energies else STEP_ENERGIES
     spec = W.rel_bcc()
     nsteps = args.steps + args.warmup
-    # rank r starts its energy cycle at offset r (weak scaling: every rank its own energies)
-    order = [energies[(rank + i) % len(energies)] for i in range(nsteps)]
+    split_k = args.split == "k" and ws > 1
+    # energy split: rank r starts its energy cycle at offset r (weak scaling,
+    # every rank its own energies); k split: every rank every energy, its own
+    # k points (the reference's modulo(ik-1, nprocs) split), strong scaling
+    order = [energies[((0 if split_k else rank) + i) % len(energies)] for i in range(nsteps)]
     eps = {ie: W.energy_problem(spec, ie) for ie in set(order)}
-    ctx = api.Context.for_problem(eps[order[0]], precision=args.precision)
+    mine = {ie: api.ksplit_problem(ep, rank, ws) for ie, ep in eps.items()} if split_k else eps
+
+    def context(precision):
+        c = api.Context.for_problem(eps[order[0]], precision=precision)
+        if split_k:
+            c.set_reduce_device(api.torch_allreduce_device())
+        return c
+
+    ctx = context(args.precision)
     slot_of = {}
     for ie in order:
         if ie not in slot_of:
             slot_of[ie] = len(slot_of)
-            ctx.stage_slot(slot_of[ie], eps[ie])
+            ctx.stage_slot(slot_of[ie], mine[ie])
     flush = torch.empty(256 * 2 ** 20 // 4, dtype=torch.float32, device="cuda")  # > L2 (129 MB)
     barrier(ws)
     clocks = Clocks()
@@ -369,16 +386,17 @@ def run_ours(args, rank, ws):
         return
     barrier(ws)
     t_max = max_over_ranks(r["t_dev"], ws)
-    pts_all = sum_over_ranks(r["pts"], ws)
+    # k split: the ranks share each energy's points, counted once
+    pts_all = r["pts"] if split_k else sum_over_ranks(r["pts"], ws)
     value = pts_all / (t_max * 1e-3)
 
     # the same steps through the plain FP64 GPU path: the metric's denominator,
     # and the error of the k-summed tau against it
     fp64 = None
     if args.precision == "mixed" and not args.no_fp64_compare:
-        cref = api.Context.for_problem(eps[order[0]], precision="fp64")
+        cref = context("fp64")
         for ie, sl in slot_of.items():
-            cref.stage_slot(sl, eps[ie])
+            cref.stage_slot(sl, mine[ie])
         r64 = timed_steps(cref, order, slot_of, eps, args, flush)
         errs = []
         for ie, sl in slot_of.items():
@@ -398,7 +416,7 @@ def run_ours(args, rank, ws):
     h2d = d2h = 0
     for i in range(args.steps):
         ie = order[args.warmup + i]
-        rr = ctx.cpacoord(eps[ie])
+        rr = ctx.cpacoord(mine[ie])
         h2d += rr["h2d_bytes"]
         d2h += rr["d2h_bytes"]
     torch.cuda.synchronize()
@@ -427,16 +445,19 @@ def run_ours(args, rank, ws):
     roof = roofline(rs["ks"], args.precision, r["alg"], r["t_dev"])
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None,
+            "scaling": "strong" if split_k else "weak", "vs_baseline": None,
             "dtype": "c128" if args.precision == "fp64" else "c128 via BF16x6 slices + FP64 refinement",
             "data": "synthetic (seeded square wells, real-space screened structure constants)",
             "config": {"workload": WORKLOAD, "precision": args.precision,
                        "step": "one contour energy, all k, full CPA pass",
+                       "parallelism": ("k split over %d ranks, NCCL allreduce per CPA iteration" % ws) if split_k
+                       else "energies over %d ranks" % ws,
                        "step_energies": order[args.warmup:], "points": r["pts"],
                        "so_split": spec.so_split, "alloy_layers": len(spec.alloy_layers),
                        "screening": "%.1f Ry in spheres of %.4f d_NN (the reference's bcc sample: "
                                     "Wigner-Seitz spheres)" % (spec.vscreen, spec.rscreen),
                        "launches_per_energy": r["launches"] / max(1, args.steps),
+                       "host_launch_ops_per_energy": r["host_ops"] / max(1, args.steps),
                        "l2": "256 MB buffer written between steps; per-step working set > 1 GB",
                        "wall_s": round(r["wall"], 3), "dec_iters": r["dec_iters"],
                        "max_newton_resid": r["resid"], "inverses_redone_in_fp64": r["fallbacks"],

@@ -109,6 +109,10 @@ typedef struct {
                                  (9 it + 3) U per lead decimation of `it` iterations (surfgf.f,
                                  dugo.f) and (7 nprc - 6) U per tau2d item (tau2d.f) on every
                                  CPA iteration; the precision guards' FP64 redos are not counted */
+  long long graph_launches;   /* CUDA graph launches of the call (the captured decimation loops) */
+  long long graph_kernels;    /* kernels those graphs ran (counted on the device; included in
+                                 gpu_launches, which minus these plus graph_launches gives the
+                                 launch operations the host issued) */
 } skkr_status;
 
 typedef struct skkr_ctx skkr_ctx;
@@ -178,6 +182,20 @@ int skkr_gpu_tauij(skkr_ctx *ctx, int npair, const int *pairs, const double *a1,
  * the other ranks then return SKKR_ERR_PEER.  fn = NULL switches it off. */
 typedef int (*skkr_reduce_fn)(void *user, double *buf, long long n);
 int skkr_gpu_set_reduce(skkr_ctx *ctx, skkr_reduce_fn fn, void *user);
+
+/* The same reduction on the device, for a collective library that works on
+ * device memory (an NCCL allreduce): every CPA iteration the context calls
+ *   fn(user, buf, n, stream)   with buf a DEVICE pointer to the n doubles laid
+ *                              out as for skkr_gpu_set_reduce (k-summed tau,
+ *                              then the failure flag),
+ * after queueing the writes of buf on `stream` (the context's cudaStream_t).
+ * fn must leave the element-wise sum over all ranks in buf, ordered on that
+ * stream (for NCCL: the allreduce enqueued on it, in place), and return 0;
+ * buf stays valid until the context is destroyed.  Replaces the host copies
+ * of skkr_gpu_set_reduce by one device-to-device copy each way and the read
+ * of the flag; when both are set this one is used.  fn = NULL switches it off. */
+typedef int (*skkr_reduce_dev_fn)(void *user, double *buf, long long n, void *stream);
+int skkr_gpu_set_reduce_device(skkr_ctx *ctx, skkr_reduce_dev_fn fn, void *user);
 
 /* One energy: the CPA loop around the k loop, k-sum with point-group
  * rotation and the CPA update (cpacoord_ksave.f:139-419).
@@ -361,11 +379,39 @@ int skkr_gpu_kambe_alm(int nitem, double e_re, double e_im, const double *kxy, c
  * in-plane phase e^{ik.(pos_b - pos_a)}, the orientation of the real-space
  * tables), G' = G (1 - alpha G)^-1 with alpha [nl][lmax+1] complex, and the
  * blocks (centre, centre + j) for j = -jmax..jmax into
- * out [nk][2 jmax + 1][lmmax][lmmax] complex.  nl (lmax+1)^2 <= 256. */
+ * out [nk][2 jmax + 1][lmmax][lmmax] complex.  nl (lmax+1)^2 <= 512.  The
+ * lattice sums run once per distinct layer separation of the slab, one
+ * thread block per (k, separation) item. */
 int skkr_gpu_kambe_screened(int nk, double e_re, double e_im, const double *kxy, int nl, const double *pos,
                             const double *alpha, int lmax, const double *gvec, int ng, const double *rvec, int nr,
                             double area, double factor, double gcut, double rcut, int centre, int jmax,
                             double *out);
+
+/* The reference's own k-space structure constants in place of the table
+ * transform, for the energy staged last by skkr_gpu_stage (not the slot
+ * API): per k point the Kambe lattice sums of every distinct layer
+ * separation of a slab of nl layers (main/kamstr.f:20-392, gstore.f:146-282),
+ * the slab screening G' = G (1 - alpha G)^-1 (main/scrstr.f:2-138,
+ * main/scrinv.f:2-63; nl (lmax+1)^2 <= 512) and, as the blocks of the staged
+ * table's layer offsets j, the slab blocks (centre, centre + j).  The staged
+ * block map must send an offset to one block from every layer and slot (a
+ * stacking of equivalent layers).  Packing, decimation, tau2d, the k-sum and
+ * the CPA update are unchanged.  kf = NULL, or a new skkr_gpu_stage, returns
+ * to the table transform.  Not for SKKR_BDG contexts. */
+typedef struct {
+  double e_re, e_im;          /* energy of the lattice sums (kappa^2; psq in the relativistic code) */
+  int nl;                     /* layers of the screening slab */
+  const double *pos;          /* [nl][3] layer positions (a.u.), in the table's orientation */
+  const double *alpha;        /* [nl][lmax+1] complex screening constants */
+  int centre;                 /* slab layer whose blocks are kept (centre +- jmax inside the slab) */
+  const double *gvec;         /* [ng][2] reciprocal lattice vectors (a superset: |g + k| > gcut skipped) */
+  int ng;
+  const double *rvec;         /* [nr][2] direct lattice vectors (in-plane |R + s| > rcut skipped) */
+  int nr;
+  double area, factor;        /* 2D cell area; Ewald parameter (1 in the reference's samples) */
+  double gcut, rcut;
+} skkr_kambe_form;
+int skkr_gpu_stage_kambe(skkr_ctx *ctx, const skkr_kambe_form *kf);
 
 /* Layer DOS of nlay layers from their physical site-diagonal tau (replaces
  * the lambda = 0 moment of nrsp-scf/moment.f:47-110 with locquant.f:86-126,
@@ -380,7 +426,7 @@ int skkr_gpu_layer_dos(int mode, int lmax, int nlay, const double *tau, int ld, 
                        const double *G, int para, double *zmom, double *zdos_l);
 
 /* Lower-level batched kernels, exported for tests. */
-/* In-place inverses of `batch` n x n matrices (main/gjinv.f:2-59, column pivoting). */
+/* In-place inverses of `batch` n x n matrices, n <= 512 (main/gjinv.f:2-59, column pivoting). */
 int skkr_gpu_gjinv_batch(int n, int batch, double *a, int ld);
 /* Decimation of `batch` (ml, m0, mr) triples -> x = (m0 - ...)^-1 (main/surfgf.f:2-108).
  * iters[b] receives the iteration count, stat[b] 0 / SKKR_ERR_SGF_*. */

@@ -69,6 +69,14 @@ class Context:
         N._check(N.lib().skkr_gpu_set_reduce(self.h, C.cast(self._reduce_cb, C.c_void_p) if fn else None, None),
                  "skkr_gpu_set_reduce")
 
+    def set_reduce_device(self, fn):
+        """The same with the sum done on the device (skkr_gpu_set_reduce_device):
+        fn(ptr, n, stream) must sum the n doubles at device address ptr over
+        the ranks in place, ordered on the CUDA stream `stream`."""
+        self._reduce_dev_cb = N.reduce_device_callback(fn) if fn is not None else None
+        N._check(N.lib().skkr_gpu_set_reduce_device(self.h, C.cast(self._reduce_dev_cb, C.c_void_p) if fn else None,
+                                                    None), "skkr_gpu_set_reduce_device")
+
     def close(self):
         if self.h:
             N.lib().skkr_gpu_destroy(self.h)
@@ -99,6 +107,23 @@ class Context:
                                     p(a["conc"]), p(a["tl"]), p(a["tr"]), p(a["ti"]), p(a["ta"]),
                                     p(a["tb"]), self.lk)
         N._check(rc, "skkr_gpu_stage")
+
+    def cpacoord_kambe(self, ep, form, tminv=None, check=True):
+        """One energy with the reference's k-space G_scr(k) (the Kambe sums and
+        slab screening of kspace.kambe_form) in place of the table transform:
+        stage, skkr_gpu_stage_kambe, run, fetch."""
+        self.stage(ep, tminv)
+        al = np.ascontiguousarray(form["alpha"], np.complex128)
+        keep = (form["pos"], al, form["gvec"], form["rvec"])
+        kf = N.KambeForm(form["e"].real, form["e"].imag, int(form["nl"]), N._p(keep[0]), N._p(al),
+                         int(form["centre"]), N._p(keep[2]), len(keep[2]), N._p(keep[3]), len(keep[3]),
+                         float(form["area"]), float(form["factor"]), float(form["gcut"]), float(form["rcut"]))
+        N._check(N.lib().skkr_gpu_stage_kambe(self.h, C.cast(C.pointer(kf), C.c_void_p)), "skkr_gpu_stage_kambe")
+        st = self.run(check=check)
+        out = self.fetch() if st.code == 0 else {}
+        out.update(status=st.code, cpa_iterations=st.cpa_iterations, max_dec_iters=st.max_dec_iters,
+                   run_ms=st.run_ms, gpu_launches=st.gpu_launches)
+        return out
 
     def tauij(self, ep, pairs, a1, a2, cvec, a0mat, tminv=None, check=True):
         """Off-diagonal tau of the interface for cluster embedding
@@ -233,15 +258,42 @@ def torch_allreduce(group=None):
     return fn
 
 
-def cpacoord_ksplit(ep, rank, world, allreduce, precision="fp64", slices=0, check=True):
+class _DeviceDoubles:
+    """A view of n doubles at a device address, for torch.as_tensor."""
+
+    def __init__(self, ptr, n):
+        self.__cuda_array_interface__ = {"shape": (int(n),), "typestr": "<f8", "data": (int(ptr), False),
+                                         "version": 2}
+
+
+def torch_allreduce_device(group=None):
+    """fn(ptr, n, stream) for Context.set_reduce_device: an in-place
+    torch.distributed allreduce (NCCL) of the library's device buffer,
+    ordered on the library's stream (no host copy)."""
+    import torch
+    import torch.distributed as dist
+
+    def fn(ptr, n, stream):
+        t = torch.as_tensor(_DeviceDoubles(ptr, n), device="cuda")
+        s = torch.cuda.ExternalStream(stream) if stream else torch.cuda.current_stream()
+        with torch.cuda.stream(s):
+            dist.all_reduce(t, group=group)
+    return fn
+
+
+def cpacoord_ksplit(ep, rank, world, allreduce, precision="fp64", slices=0, check=True, device_reduce=False):
     """One rank of an energy whose k points are split over `world` ranks:
     the library runs this rank's k points and calls `allreduce` on the
     k-summed tau before every CPA update, so every rank returns the full
-    result."""
+    result.  device_reduce: `allreduce` is a device hook (fn(ptr, n, stream),
+    e.g. torch_allreduce_device) instead of a host one."""
     epl = ksplit_problem(ep, rank, world)
     ctx = Context.for_problem(epl, precision, slices=slices)
     try:
-        ctx.set_reduce(allreduce)
+        if device_reduce:
+            ctx.set_reduce_device(allreduce)
+        else:
+            ctx.set_reduce(allreduce)
         return ctx.cpacoord(epl, check=check)
     finally:
         ctx.close()

@@ -227,7 +227,7 @@ def warm_start(ep, model: Model, fam: Family | None = None, device: str = "gpu")
 
 
 def generate(out: str, nsolve: int, fam: Family, seed: int = 1000, precision: str = "mixed", nctx: int = 8,
-             max_seconds: float = 1e9):
+             max_seconds: float = 1e9, graphs: bool = True, progress: int = 50):
     """Converged CPA solutions of nsolve drawn alloy stacks, energies cycled
     over the contour, nctx systems per call (skkr_gpu_cpacoord_many).  Saves
     x [rows, 122], y [rows, 2 nfree], solve id, energy, CPA iterations."""
@@ -235,6 +235,8 @@ def generate(out: str, nsolve: int, fam: Family, seed: int = 1000, precision: st
     rng = np.random.default_rng(seed)
     mask = free_elements(fam.base(fam.energies[0]))
     ctxs = [api.Context.for_problem(fam.base(fam.energies[0]), precision) for _ in range(nctx)]
+    for c in ctxs:
+        c.set_graphs(graphs)
     xs, ys, meta = [], [], []
     t0 = time.time()
     s = 0
@@ -252,7 +254,7 @@ def generate(out: str, nsolve: int, fam: Family, seed: int = 1000, precision: st
                 xs.append(stack_features(ep, fam))
                 ys.append(stack_targets(ep, r["tminv"], fam, mask))
                 meta += [(sid, ie, li, r["cpa_iterations"]) for li in fam.alloy_layers]
-            if s % (50 * nctx) < nctx:
+            if s % (progress * nctx) < nctx:
                 print("%d solves, %d rows, %.1f s" % (s, 4 * len(xs), time.time() - t0), flush=True)
     finally:
         for c in ctxs:
@@ -337,6 +339,9 @@ def main():
     g.add_argument("--nset", type=int, default=6)
     g.add_argument("--so-split", type=float, default=0.03)
     g.add_argument("--max-seconds", type=float, default=1200.0)
+    g.add_argument("--nctx", type=int, default=8)
+    g.add_argument("--no-graphs", action="store_true")
+    g.add_argument("--progress", type=int, default=50)
     t = sub.add_parser("train")
     t.add_argument("--data", required=True)
     t.add_argument("--out", default=DEFAULT_MODEL)
@@ -347,7 +352,8 @@ def main():
     r.add_argument("--solves", type=int, default=48)
     a = ap.parse_args()
     if a.cmd == "gen":
-        n = generate(a.out, a.solves, Family(nset=a.nset, so_split=a.so_split), max_seconds=a.max_seconds)
+        n = generate(a.out, a.solves, Family(nset=a.nset, so_split=a.so_split), max_seconds=a.max_seconds,
+                     nctx=a.nctx, graphs=not a.no_graphs, progress=a.progress)
         print("rows:", n)
     elif a.cmd == "train":
         print("mse train / held out / held out of the ATA start: %.3e / %.3e / %.3e"

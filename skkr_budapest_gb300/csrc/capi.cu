@@ -190,7 +190,113 @@ struct DBuf {
   }
 };
 
+// The reference's screened structure constants G_scr(k) (main/gstore.f:146-282
+// with main/scrstr.f:2-138, main/scrinv.f) on the device for batches of k
+// points: the Kambe lattice sums once per distinct layer separation of the
+// slab (kamstr.f), the slab G and 1 - alpha G through the pair map, the
+// batched Gauss-Jordan inverse (N = nl (lmax+1)^2 <= 512) and the product
+// X = G (1 - alpha G)^-1.  setup() takes the lattice and slab once, screen()
+// runs one batch of k points whose coordinates are already on the device.
+struct KambeDev {
+  int lmax = 0, lm = 0, nl = 0, N = 0, nsep = 0, ng = 0, nr = 0, centre = 0, jmax = 0;
+  double er = 0, ei = 0, area = 0, factor = 1, gcut = 0, rcut = 0;
+  DBuf gvec, rvec, coef, pos, alpha, seps, pmap, ik, is, alm, Gs, A, X;
+
+  void release() {
+    DBuf *all[] = {&gvec, &rvec, &coef, &pos, &alpha, &seps, &pmap, &ik, &is, &alm, &Gs, &A, &X};
+    for (DBuf *b : all) b->release();
+  }
+  size_t per_k() const {
+    return (size_t)nsep * lm * lm * sizeof(zd) + 3 * (size_t)N * N * sizeof(zd) + (size_t)nsep * 5 * sizeof(double);
+  }
+  int setup(double e_re, double e_im, int lmax_, int nl_, const double *pos_h, const double *alpha_h, int centre_,
+            int jmax_, const double *gvec_h, int ng_, const double *rvec_h, int nr_, double area_, double factor_,
+            double gcut_, double rcut_, cudaStream_t st);
+  int screen(const double *xk, int m, cudaStream_t st);
+};
+
 }  // namespace
+
+int KambeDev::setup(double e_re, double e_im, int lmax_, int nl_, const double *pos_h, const double *alpha_h,
+                    int centre_, int jmax_, const double *gvec_h, int ng_, const double *rvec_h, int nr_, double area_,
+                    double factor_, double gcut_, double rcut_, cudaStream_t st) {
+  if (nl_ < 1 || !pos_h || !alpha_h || !gvec_h || !rvec_h || ng_ < 1 || nr_ < 1) return SKKR_ERR_ARG;
+  if (lmax_ < 0 || lmax_ > 3 || !(area_ > 0.0) || !(factor_ > 0.0) || !(gcut_ > 0.0) || !(rcut_ > 0.0))
+    return SKKR_ERR_ARG;
+  if (e_re == 0.0 && e_im == 0.0) return SKKR_ERR_ARG;
+  lmax = lmax_;
+  lm = (lmax + 1) * (lmax + 1);
+  nl = nl_;
+  N = nl * lm;
+  if (N > 512 || jmax_ < 0 || centre_ - jmax_ < 0 || centre_ + jmax_ >= nl) return SKKR_ERR_ARG;
+  er = e_re;
+  ei = e_im;
+  centre = centre_;
+  jmax = jmax_;
+  ng = ng_;
+  nr = nr_;
+  area = area_;
+  factor = factor_;
+  gcut = gcut_;
+  rcut = rcut_;
+  // distinct separations pos_a - pos_b (to 1e-9 a.u.) and the pair map
+  std::vector<double> sv;
+  std::vector<int> pm((size_t)nl * nl);
+  for (int a = 0; a < nl; a++)
+    for (int b = 0; b < nl; b++) {
+      double d[3];
+      for (int c = 0; c < 3; c++) d[c] = pos_h[3 * a + c] - pos_h[3 * b + c];
+      int f = -1;
+      for (size_t q = 0; q < sv.size() / 3 && f < 0; q++)
+        if (std::fabs(sv[3 * q] - d[0]) < 1e-9 && std::fabs(sv[3 * q + 1] - d[1]) < 1e-9 &&
+            std::fabs(sv[3 * q + 2] - d[2]) < 1e-9)
+          f = (int)q;
+      if (f < 0) {
+        f = (int)(sv.size() / 3);
+        sv.insert(sv.end(), d, d + 3);
+      }
+      pm[(size_t)a * nl + b] = f;
+    }
+  nsep = (int)(sv.size() / 3);
+  const int lm2 = (2 * lmax + 1) * (2 * lmax + 1);
+  std::vector<double> cf(2 * (size_t)lm * lm * lm2);
+  CKR(skkr_gpu_kambe_coef(lmax, cf.data()));
+  CKR(gvec.ensure(2 * (size_t)ng * sizeof(double)));
+  CKR(rvec.ensure(2 * (size_t)nr * sizeof(double)));
+  CKR(coef.ensure(cf.size() * sizeof(double)));
+  CKR(pos.ensure(3 * (size_t)nl * sizeof(double)));
+  CKR(alpha.ensure((size_t)nl * (lmax + 1) * sizeof(zd)));
+  CKR(seps.ensure(sv.size() * sizeof(double)));
+  CKR(pmap.ensure(pm.size() * sizeof(int)));
+  CK(cudaMemcpyAsync(gvec.p, gvec_h, 2 * (size_t)ng * sizeof(double), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(rvec.p, rvec_h, 2 * (size_t)nr * sizeof(double), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(coef.p, cf.data(), cf.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(pos.p, pos_h, 3 * (size_t)nl * sizeof(double), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(alpha.p, alpha_h, (size_t)nl * (lmax + 1) * sizeof(zd), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(seps.p, sv.data(), sv.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(pmap.p, pm.data(), pm.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+  CK(cudaStreamSynchronize(st));  // cf, sv, pm are host temporaries
+  return SKKR_OK;
+}
+
+int KambeDev::screen(const double *xk, int m, cudaStream_t st) {
+  const long long items = (long long)m * nsep, NN = (long long)N * N;
+  CKR(ik.ensure((size_t)items * 2 * sizeof(double)));
+  CKR(is.ensure((size_t)items * 3 * sizeof(double)));
+  CKR(alm.ensure((size_t)items * lm * lm * sizeof(zd)));
+  CKR(Gs.ensure((size_t)m * NN * sizeof(zd)));
+  CKR(A.ensure((size_t)m * NN * sizeof(zd)));
+  CKR(X.ensure((size_t)m * NN * sizeof(zd)));
+  launch_kambe_items(m, nsep, xk, seps.as<double>(), ik.as<double>(), is.as<double>(), st);
+  launch_kambe_alm((int)items, er, ei, ik.as<double>(), is.as<double>(), lmax, gvec.as<double>(), ng,
+                   rvec.as<double>(), nr, area, factor, gcut, rcut, coef.as<double>(), alm.as<double>(), st);
+  launch_slab_assemble(m, nl, lm, alm.as<zd>(), pmap.as<int>(), nsep, xk, pos.as<double>(), alpha.as<zd>(), lmax + 1,
+                       Gs.as<zd>(), A.as<zd>(), st);
+  launch_zgj(mref(A.as<zd>(), NN, 0, N), N, m, 1, nullptr, st);
+  MatRef x = mref(X.as<zd>(), NN, 0, N);
+  launch_zgemm(0, mref(Gs.as<zd>(), NN, 0, N), mref(A.as<zd>(), NN, 0, N), x, x, x, N, N, N, m, 1, nullptr, st);
+  return SKKR_OK;
+}
 
 struct skkr_ctx {
   skkr_sizes sz;
@@ -242,6 +348,9 @@ struct skkr_ctx {
   long long k_fp64 = 0;          // k points redone in FP64 in this run
   skkr_reduce_fn red_fn = nullptr;  // host allreduce of tauc for a k-split energy
   void *red_user = nullptr;
+  skkr_reduce_dev_fn red_dev_fn = nullptr;  // the same on a device buffer (NCCL)
+  void *red_dev_user = nullptr;
+  DBuf redd;                                // [2 nz + 1] doubles handed to red_dev_fn
   std::vector<double> red_buf;
   double max_resid = 0.0;    // largest accepted Newton residual seen in this run
   long long inv_fallbacks = 0;  // inverses redone in FP64 in this run
@@ -251,6 +360,11 @@ struct skkr_ctx {
   DBuf decctl;                  // [0] iteration, [1] items left, [2] half-bodies run (captured loop)
   long long graph_kernels = 0;  // kernels run inside graphs in this run
   long long graph_launches = 0; // graph launches in this run
+  // the reference's k-space G_scr(k) in place of the table transform for the
+  // energy staged last (skkr_gpu_stage_kambe)
+  bool kambe_on = false;
+  KambeDev kd;
+  DBuf kblk;                    // [2 jmax + 1] cache block of each layer offset, or -1
 };
 
 // Inputs and outputs of one staged energy.  A context keeps any number of
@@ -350,8 +464,11 @@ extern "C" int skkr_gpu_destroy(skkr_ctx *c) {
   DBuf *all[] = {&c->gR, &c->rvec, &c->rstart, &c->blkmap_d, &c->xk, &c->wk, &c->lg, &c->rg,
                  &c->conc, &c->tcat, &c->tab, &c->trot, &c->trtmp, &c->pnorm, &c->G, &c->sspo,
                  &c->pool, &c->jobs, &c->dec, &c->decf, &c->deci, &c->tauw, &c->tauk, &c->S,
-                 &c->T1, &c->T2, &c->tauc, &c->cpa, &c->cpan, &c->cpaact, &c->decctl, &c->knorm};
+                 &c->T1, &c->T2, &c->tauc, &c->cpa, &c->cpan, &c->cpaact, &c->decctl, &c->knorm,
+                 &c->redd};
   for (DBuf *b : all) b->release();
+  c->kd.release();
+  c->kblk.release();
   if (c->mw) mixed_destroy(c->mw);
   for (SlotStore *sl : c->slots) {
     DBuf *sb[] = {&sl->gR, &sl->rvec, &sl->rstart, &sl->blkmap_d, &sl->xk, &sl->wk, &sl->lg,
@@ -415,6 +532,7 @@ extern "C" int skkr_gpu_stage(skkr_ctx *c, double ce_re, double ce_im, double fa
   c->ce = zmk(ce_re, ce_im);
   c->fac = zmk(fac_re, fac_im);
   c->nk = nk;
+  c->kambe_on = false;  // a new energy starts from its table
   c->nblk = rt->nblk;
   const bool bdg = c->sz.mode == SKKR_BDG;
   c->nbk = bdg ? 2 * rt->nblk : rt->nblk;
@@ -1257,6 +1375,31 @@ static int cpa_step(skkr_ctx *c, int *itcpa, int *cpacon, int *concpa, double *e
 // host hook (cpacoord_ksave.f:406).  `failed` ranks send the flag only.
 static int reduce_tauc(skkr_ctx *c, bool failed) {
   const size_t nz = (size_t)c->nintfc * c->lk * c->lk;
+  if (c->red_dev_fn) {
+    // device form: tauc and the flag into one device buffer, the hook sums it
+    // in place on the context stream, the sum goes back into tauc
+    CKR(c->redd.ensure((2 * nz + 1) * sizeof(double)));
+    double *b = c->redd.as<double>();
+    if (failed) CK(cudaMemsetAsync(b, 0, 2 * nz * sizeof(double), c->st));
+    else CK(cudaMemcpyAsync(b, c->tauc.p, nz * sizeof(zd), cudaMemcpyDeviceToDevice, c->st));
+    const double flag = failed ? 1.0 : 0.0;
+    CK(cudaMemcpyAsync(b + 2 * nz, &flag, sizeof(double), cudaMemcpyHostToDevice, c->st));
+    CK(cudaStreamSynchronize(c->st));  // `flag` is a host temporary
+    if (c->red_dev_fn(c->red_dev_user, b, (long long)(2 * nz + 1), (void *)c->st) != 0) {
+      g_last_error = "reduction hook returned an error";
+      return SKKR_ERR_PEER;
+    }
+    if (failed) return SKKR_OK;
+    double sum_flag = 0.0;
+    CK(cudaMemcpyAsync(&sum_flag, b + 2 * nz, sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    if (sum_flag != 0.0) {
+      g_last_error = "another rank of the k-split energy failed";
+      return SKKR_ERR_PEER;
+    }
+    CK(cudaMemcpyAsync(c->tauc.p, b, nz * sizeof(zd), cudaMemcpyDeviceToDevice, c->st));
+    return SKKR_OK;
+  }
   c->red_buf.assign(2 * nz + 1, 0.0);
   if (!failed) {
     CK(cudaMemcpyAsync(c->red_buf.data(), c->tauc.p, nz * sizeof(zd), cudaMemcpyDeviceToHost, c->st));
@@ -1531,10 +1674,66 @@ extern "C" int skkr_gpu_set_graphs(skkr_ctx *c, int on) {
   return SKKR_OK;
 }
 
+extern "C" int skkr_gpu_set_reduce_device(skkr_ctx *c, skkr_reduce_dev_fn fn, void *user) {
+  if (!c) return SKKR_ERR_ARG;
+  c->red_dev_fn = fn;
+  c->red_dev_user = user;
+  return SKKR_OK;
+}
+
 extern "C" int skkr_gpu_set_reduce(skkr_ctx *c, skkr_reduce_fn fn, void *user) {
   if (!c) return SKKR_ERR_ARG;
   c->red_fn = fn;
   c->red_user = user;
+  return SKKR_OK;
+}
+
+// G_scr(k) of every k point of the staged energy from the reference's
+// k-space form, written into the structure-constant cache in batches of k
+// points sized to a few GB of scratch
+static int kambe_gk(skkr_ctx *c) {
+  KambeDev &K = c->kd;
+  const size_t bs = (size_t)c->lmmax * c->lmmax;
+  int m = (int)std::max<size_t>(1, (size_t)8e9 / K.per_k());
+  m = std::min(std::min(m, 65535), c->nk);
+  for (int k0 = 0; k0 < c->nk; k0 += m) {
+    const int mm = std::min(m, c->nk - k0);
+    CKR(K.screen(c->xk.as<double>() + 2 * (size_t)k0, mm, c->st));
+    launch_slab_cache(mm, K.nl, K.lm, K.centre, K.jmax, c->kblk.as<int>(), c->nbk, K.X.as<zd>(),
+                      c->G.as<zd>() + (size_t)k0 * c->nbk * bs, c->st);
+  }
+  return SKKR_OK;
+}
+
+extern "C" int skkr_gpu_stage_kambe(skkr_ctx *c, const skkr_kambe_form *kf) {
+  if (!c || !c->staged) return SKKR_ERR_ARG;
+  if (!kf) {
+    c->kambe_on = false;
+    return SKKR_OK;
+  }
+  if (c->sz.mode == SKKR_BDG) return SKKR_ERR_UNSUPPORTED;
+  // offset j of the staged block map -> block; every (slot, layer) must map
+  // an offset to one block and a block to one offset (equivalent layers)
+  const int nj = 2 * c->jmax + 1, rowlen = c->mi * nj;
+  std::vector<int> blk(nj, -1);
+  for (int sl = 0; sl < c->nslot; sl++)
+    for (int i = 0; i < c->mi; i++)
+      for (int j = 0; j < nj; j++) {
+        const int b = c->blkmap[(size_t)sl * rowlen + i * nj + j];
+        if (b < 0) continue;
+        if (blk[j] >= 0 && blk[j] != b) return SKKR_ERR_UNSUPPORTED;
+        blk[j] = b;
+      }
+  for (int j = 0; j < nj; j++)
+    for (int j2 = 0; j2 < j; j2++)
+      if (blk[j] >= 0 && blk[j] == blk[j2]) return SKKR_ERR_UNSUPPORTED;
+  int rc = c->kd.setup(kf->e_re, kf->e_im, c->sz.lmax, kf->nl, kf->pos, kf->alpha, kf->centre, c->jmax, kf->gvec,
+                       kf->ng, kf->rvec, kf->nr, kf->area, kf->factor, kf->gcut, kf->rcut, c->st);
+  if (rc != SKKR_OK) return rc;
+  CKR(c->kblk.ensure(nj * sizeof(int)));
+  CK(cudaMemcpyAsync(c->kblk.p, blk.data(), nj * sizeof(int), cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  c->kambe_on = true;
   return SKKR_OK;
 }
 
@@ -1613,8 +1812,12 @@ extern "C" int skkr_gpu_run(skkr_ctx *c, skkr_status *status) {
       c->nls = nLs;
       c->nsl = nLs + nRs;
       CKR(c->sspo.ensure((size_t)nk * c->nsl * MB * sizeof(zd)));
-      launch_gk_ft(c->gR.as<zd>(), c->rvec.as<double>(), c->rstart.as<int>(), c->nbk, c->lmmax,
-                   c->xk.as<double>(), nk, c->G.as<zd>(), st);
+      if (c->kambe_on) {
+        CKR(kambe_gk(c));
+      } else {
+        launch_gk_ft(c->gR.as<zd>(), c->rvec.as<double>(), c->rstart.as<int>(), c->nbk, c->lmmax,
+                     c->xk.as<double>(), nk, c->G.as<zd>(), st);
+      }
     }
     CKR(c->S.ensure((size_t)ncls * ni * lk2 * sizeof(zd)));
     for (int k0 = 0; k0 < nk; k0 += c->kc) {
@@ -1639,7 +1842,7 @@ extern "C" int skkr_gpu_run(skkr_ctx *c, skkr_status *status) {
     if (!c->err_code && c->sz.precision == SKKR_MIXED && c->dominant_frac > 0.0)
       CKR(redo_dominant_k(c, itcpa, lcls, rcls, icls));
     if (c->err_code) {
-      if (c->red_fn) reduce_tauc(c, true);  // tell the other ranks before returning
+      if (c->red_fn || c->red_dev_fn) reduce_tauc(c, true);  // tell the other ranks before returning
       break;
     }
     // rotation of the class sums: tauc = sum_g L_g S[class(g)] R_g   (cpacoord_ksave.f:382-391)
@@ -1661,7 +1864,7 @@ extern "C" int skkr_gpu_run(skkr_ctx *c, skkr_status *status) {
       launch_zgemm(0, T1m, Rm, T2m, T2m, T2m, lk, lk, lk, ni, c->ngeff, nullptr, st);
       launch_gsum(c->T2.as<zd>(), c->ngeff, lk, ni, c->tauc.as<zd>(), st);
     }
-    if (c->red_fn) {
+    if (c->red_fn || c->red_dev_fn) {
       int rrc = reduce_tauc(c, false);
       if (rrc != SKKR_OK) {
         c->err_code = rrc;
@@ -1710,6 +1913,8 @@ extern "C" int skkr_gpu_run(skkr_ctx *c, skkr_status *status) {
     status->inv_refined = c->inv_refined;
     status->k_fp64 = c->k_fp64;
     status->alg_flops = c->alg_units * 8.0 * (double)n * n * n;
+    status->graph_launches = c->graph_launches;
+    status->graph_kernels = c->graph_kernels;
   }
   return c->err_code;
 }
@@ -1834,7 +2039,10 @@ extern "C" int skkr_gpu_run_slot(skkr_ctx *c, int slot, skkr_status *status) {
   SlotStore *s = get_slot(c, slot, false);
   if (!s || !s->staged) return SKKR_ERR_ARG;
   swap_slot(c, *s);
+  const bool kon = c->kambe_on;  // the k-space form belongs to the energy of skkr_gpu_stage
+  c->kambe_on = false;
   int rc = skkr_gpu_run(c, status);
+  c->kambe_on = kon;
   swap_slot(c, *s);
   return rc;
 }
@@ -1900,7 +2108,7 @@ int download_mats(double *dst, const zd *src, int count, int n, int ld) {
 }  // namespace
 
 extern "C" int skkr_gpu_gjinv_batch(int n, int batch, double *a, int ld) {
-  if (n < 1 || n > 256 || batch < 1 || !a || ld < n) return SKKR_ERR_ARG;
+  if (n < 1 || n > 512 || batch < 1 || !a || ld < n) return SKKR_ERR_ARG;
   Scoped s;
   zd *d;
   CKR(s.alloc(&d, (size_t)batch * n * n));
@@ -2529,54 +2737,31 @@ extern "C" int skkr_gpu_kambe_screened(int nk, double e_re, double e_im, const d
                                        const double *pos, const double *alpha, int lmax, const double *gvec,
                                        int ng, const double *rvec, int nr, double area, double factor,
                                        double gcut, double rcut, int centre, int jmax, double *out) {
-  if (nk < 1 || nl < 1 || !kxy || !pos || !alpha || !gvec || !rvec || !out || ng < 1 || nr < 1) return SKKR_ERR_ARG;
-  if (lmax < 0 || lmax > 3 || !(area > 0.0) || !(factor > 0.0) || !(gcut > 0.0) || !(rcut > 0.0)) return SKKR_ERR_ARG;
-  if (e_re == 0.0 && e_im == 0.0) return SKKR_ERR_ARG;
-  const int lm = (lmax + 1) * (lmax + 1), lm2 = (2 * lmax + 1) * (2 * lmax + 1), N = nl * lm;
-  if (N > 256 || jmax < 0 || centre - jmax < 0 || centre + jmax >= nl) return SKKR_ERR_ARG;
-  const long long items = (long long)nk * nl * nl, NN = (long long)N * N;
-  std::vector<double> ik(2 * items), is(3 * items), coef(2 * (size_t)lm * lm * lm2);
-  for (int k = 0; k < nk; k++)
-    for (int a = 0; a < nl; a++)
-      for (int b = 0; b < nl; b++) {
-        const long long it = ((long long)k * nl + a) * nl + b;
-        ik[2 * it] = kxy[2 * k];
-        ik[2 * it + 1] = kxy[2 * k + 1];
-        for (int c = 0; c < 3; c++) is[3 * it + c] = pos[3 * a + c] - pos[3 * b + c];
-      }
-  CKR(skkr_gpu_kambe_coef(lmax, coef.data()));
-  Scoped s;
-  double *IK, *IS, *G, *R, *Cf, *KX, *PS;
-  zd *ALM, *AL, *Gs, *A, *X, *O;
-  CKR(s.alloc(&IK, ik.size()));
-  CKR(s.alloc(&IS, is.size()));
-  CKR(s.alloc(&G, 2 * (size_t)ng));
-  CKR(s.alloc(&R, 2 * (size_t)nr));
-  CKR(s.alloc(&Cf, coef.size()));
-  CKR(s.alloc(&KX, 2 * (size_t)nk));
-  CKR(s.alloc(&PS, 3 * (size_t)nl));
-  CKR(s.alloc(&ALM, (size_t)items * lm * lm));
-  CKR(s.alloc(&AL, (size_t)nl * (lmax + 1)));
-  CKR(s.alloc(&Gs, (size_t)nk * NN));
-  CKR(s.alloc(&A, (size_t)nk * NN));
-  CKR(s.alloc(&X, (size_t)nk * NN));
-  CKR(s.alloc(&O, (size_t)nk * (2 * jmax + 1) * lm * lm));
-  CK(cudaMemcpy(IK, ik.data(), ik.size() * sizeof(double), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(IS, is.data(), is.size() * sizeof(double), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(G, gvec, 2 * (size_t)ng * sizeof(double), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(R, rvec, 2 * (size_t)nr * sizeof(double), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(Cf, coef.data(), coef.size() * sizeof(double), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(KX, kxy, 2 * (size_t)nk * sizeof(double), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(PS, pos, 3 * (size_t)nl * sizeof(double), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(AL, alpha, (size_t)nl * (lmax + 1) * sizeof(zd), cudaMemcpyHostToDevice));
-  launch_kambe_alm((int)items, e_re, e_im, IK, IS, lmax, G, ng, R, nr, area, factor, gcut, rcut, Cf, (double *)ALM, 0);
-  launch_slab_assemble(nk, nl, lm, ALM, KX, PS, AL, lmax + 1, Gs, A, 0);
-  launch_zgj(mref(A, NN, 0, N), N, nk, 1, nullptr, 0);
-  launch_zgemm(0, mref(Gs, NN, 0, N), mref(A, NN, 0, N), mref(X, NN, 0, N), mref(X, NN, 0, N), mref(X, NN, 0, N), N,
-               N, N, nk, 1, nullptr, 0);
-  launch_slab_extract(nk, nl, lm, centre, jmax, X, O, 0);
+  if (nk < 1 || !kxy || !out) return SKKR_ERR_ARG;
+  struct Own {
+    KambeDev k;
+    DBuf kx, o;
+    ~Own() {
+      k.release();
+      kx.release();
+      o.release();
+    }
+  } w;
+  KambeDev &K = w.k;
+  CKR(K.setup(e_re, e_im, lmax, nl, pos, alpha, centre, jmax, gvec, ng, rvec, nr, area, factor, gcut, rcut, 0));
+  const int nj = 2 * jmax + 1;
+  const size_t blocks = (size_t)nj * K.lm * K.lm;
+  const int m = std::min(std::min((int)std::max<size_t>(1, (size_t)4e9 / K.per_k()), 65535), nk);
+  CKR(w.kx.ensure(2 * (size_t)nk * sizeof(double)));
+  CKR(w.o.ensure((size_t)nk * blocks * sizeof(zd)));
+  CK(cudaMemcpy(w.kx.p, kxy, 2 * (size_t)nk * sizeof(double), cudaMemcpyHostToDevice));
+  for (int k0 = 0; k0 < nk; k0 += m) {
+    const int mm = std::min(m, nk - k0);
+    CKR(K.screen(w.kx.as<double>() + 2 * (size_t)k0, mm, 0));
+    launch_slab_extract(mm, nl, K.lm, centre, jmax, K.X.as<zd>(), w.o.as<zd>() + (size_t)k0 * blocks, 0);
+  }
   CK(cudaDeviceSynchronize());
   CK(cudaGetLastError());
-  CK(cudaMemcpy(out, O, (size_t)nk * (2 * jmax + 1) * lm * lm * sizeof(zd), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(out, w.o.p, (size_t)nk * blocks * sizeof(zd), cudaMemcpyDeviceToHost));
   return SKKR_OK;
 }

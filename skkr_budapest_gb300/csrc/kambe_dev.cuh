@@ -157,116 +157,153 @@ SKKR_HD inline void kambe_ylm(double x, double y, double z, int lmax2, fcplx *ou
     }
 }
 
-// D_L(k, s) into out[(lmax2+1)^2] (kamstr.f dlm1 + dlm2)
-SKKR_HD inline void kambe_dlm(fcplx e, double kx, double ky, double sx, double sy, double sz, int lmax2,
-                              const double *gvec, int ng, const double *rvec, int nr, double area,
-                              double factor, double gcut, double rcut, fcplx *out) {
-  const int lmmx = (lmax2 + 1) * (lmax2 + 1);
-  const fcplx kappa = fsqrtc(e);
-  const fcplx cs1 = fdivc(fc(-1.0 / area, 0.0), kappa);
-  const fcplx cs2 = fscal(-0.28209479177387814347, kappa);  // -kappa / (2 sqrt(pi))
-  const fcplx alpha = fscal(factor * area / 12.566370614359172954, e);
-  const fcplx w = fdivc(fscal(2.0, alpha), e);
+// Per-(k, s) constants of the sums (kamstr.f:72-140): kappa, the prefactors
+// of the two parts, the Ewald alpha, the flm normalisation, the in-plane
+// shift of in-plane pairs, and (sz kappa)^l of the out-of-plane form.
+struct KambeSetup {
+  fcplx e, kappa, cs1, cs2, alpha, w, xrot;
+  double kx, ky, sx, sy, sz, s;
+  int lmax2;
+  bool f35;
   double flm[(SKKR_KAMBE_L2 + 1) * (SKKR_KAMBE_L2 + 1)];
+  fcplx cs[SKKR_KAMBE_L2 + 1];
+};
+
+SKKR_HD inline void kambe_setup(fcplx e, double kx, double ky, double sx, double sy, double sz, int lmax2,
+                                double area, double factor, KambeSetup &K) {
+  K.e = e;
+  K.kx = kx;
+  K.ky = ky;
+  K.lmax2 = lmax2;
+  K.kappa = fsqrtc(e);
+  K.cs1 = fdivc(fc(-1.0 / area, 0.0), K.kappa);
+  K.cs2 = fscal(-0.28209479177387814347, K.kappa);  // -kappa / (2 sqrt(pi))
+  K.alpha = fscal(factor * area / 12.566370614359172954, e);
+  K.w = fdivc(fscal(2.0, K.alpha), e);
   for (int l = 0; l <= lmax2; l++)
     for (int m = 0; m <= l; m++) {
       const double v = pow(2.0, -l) * sqrt((2.0 * l + 1.0) * kambe_fac(l + m) * kambe_fac(l - m));
-      flm[l * (l + 1) + m] = v;
-      flm[l * (l + 1) - m] = v;
+      K.flm[l * (l + 1) + m] = v;
+      K.flm[l * (l + 1) - m] = v;
     }
-  for (int i = 0; i < lmmx; i++) out[i] = fc(0.0, 0.0);
   double s = sqrt(sx * sx + sy * sy + sz * sz);
   const double ctol = 1e-4;
-  if (s < ctol) {
-    // formula 55: d003 = -kappa (e^alpha c - i) / (2 sqrt(pi)),
-    // c = i (e^-alpha - w(sqrt alpha)) - 1 / (sqrt(pi) sqrt(alpha))
-    const fcplx a = fsqrtc(alpha);
-    const fcplx t = fsub(fexpc(fneg(alpha)), faddeeva(a));
-    const fcplx c = fsub(fc(-t.im, t.re), fdivc(fc(0.56418958354775628695, 0.0), a));
-    const fcplx u = fsub(fmulc(fexpc(alpha), c), fc(0.0, 1.0));
-    out[0] = fadd(out[0], fscal(-0.28209479177387814347, fmulc(kappa, u)));
-  }
+  K.s = s;  // before the in-plane shift: s < ctol selects formula 55
   if (s > ctol && fabs(sz) < ctol) {
     sz = 1.1 * ctol;
     s = sqrt(sx * sx + sy * sy + sz * sz);
   }
-  const bool f35 = s > ctol && fabs(sz) > ctol;
-  fcplx cs[SKKR_KAMBE_L2 + 1];
-  cs[0] = fc(1.0, 0.0);
-  for (int l = 1; l <= lmax2; l++) cs[l] = fmulc(cs[l - 1], fscal(sz, kappa));
+  K.sx = sx;
+  K.sy = sy;
+  K.sz = sz;
+  K.f35 = s > ctol && fabs(sz) > ctol;
+  K.cs[0] = fc(1.0, 0.0);
+  for (int l = 1; l <= lmax2; l++) K.cs[l] = fmulc(K.cs[l - 1], fscal(sz, K.kappa));
+  K.xrot = fexpc(fc(0.0, -3.14159265358979323846));  // exp(-i pi) of kamstr.f
+}
+
+// formula 55 (s = 0): d003 = -kappa (e^alpha c - i) / (2 sqrt(pi)),
+// c = i (e^-alpha - w(sqrt alpha)) - 1 / (sqrt(pi) sqrt(alpha))
+SKKR_HD inline void kambe_self_term(const KambeSetup &K, fcplx *out) {
+  if (K.s >= 1e-4) return;
+  const fcplx a = fsqrtc(K.alpha);
+  const fcplx t = fsub(fexpc(fneg(K.alpha)), faddeeva(a));
+  const fcplx c = fsub(fc(-t.im, t.re), fdivc(fc(0.56418958354775628695, 0.0), a));
+  const fcplx u = fsub(fmulc(fexpc(K.alpha), c), fc(0.0, 1.0));
+  out[0] = fadd(out[0], fscal(-0.28209479177387814347, fmulc(K.kappa, u)));
+}
+
+// the reciprocal-space term of one g (formula 35 out of plane, 50 in plane)
+SKKR_HD inline void kambe_gterm(const KambeSetup &K, double gx, double gy, double gcut, fcplx *out) {
+  const int lmax2 = K.lmax2;
+  const double gkx = gx + K.kx, gky = gy + K.ky;
+  const double km2 = gkx * gkx + gky * gky, km = sqrt(km2);
+  if (km > gcut) return;
   fcplx gam[SKKR_KAMBE_L2 + 1], dl[SKKR_KAMBE_L2 + 2], cp[SKKR_KAMBE_L2 + 1], cm[SKKR_KAMBE_L2 + 1];
-  const fcplx xrot = fexpc(fc(0.0, -3.14159265358979323846));  // exp(-i pi) of kamstr.f
-  for (int ig = 0; ig < ng; ig++) {
-    const double gkx = gvec[2 * ig] + kx, gky = gvec[2 * ig + 1] + ky;
-    const double km2 = gkx * gkx + gky * gky, km = sqrt(km2);
-    if (km > gcut) continue;
-    const fcplx kp = fsqrtc(fsub(e, fc(km2, 0.0)));
-    const fcplx ex2 = km > 1e-10 ? fc(gkx / km, gky / km) : fc(1.0, 0.0);
-    const fcplx xc = fscal(0.5, fmulc(fmulc(xrot, fsub(e, fc(km * km, 0.0))), w));
-    kambe_incgamma(lmax2, xc, gam);
-    const fcplx rp = fdivc(kp, kappa), rm = fdivc(fc(km, 0.0), kappa);
-    for (int l = 0; l <= lmax2; l++) {
-      cp[l] = fpowi(rp, 2 * l - 1);
-      cm[l] = fpowi(rm, l);
-    }
-    if (f35) {
-      kambe_delkam(lmax2, xc, fmulc(fscal(sz, kp), fscal(sz, kp)), dl);
-      const fcplx ex1 = fmulc(fexpc(fc(0.0, gkx * sx + gky * sy)), cs1);
-      for (int l = 0; l <= lmax2; l++)
-        for (int m = -l; m <= l; m++) {
-          const int mm = m < 0 ? -m : m, ipar = (l - mm) % 2;
-          const fcplx ex = fmulc(fpowi(ex2, -m), ex1);
-          fcplx csum = fc(0.0, 0.0);
-          for (int n = 0; n <= l - mm; n++) {
-            fcplx b = fc(0.0, 0.0);
-            const int kmax = 2 * n < l - mm ? 2 * n : l - mm;
-            for (int k = n + (n + ipar) % 2; k <= kmax; k += 2) {
-              const int i = 2 * n - k, j = l - k;
-              const fcplx cc = fscal(1.0 / (kambe_fac(i) * kambe_fac(k - n)), fmulc(cs[i], cm[j]));
-              b = fadd(b, fscal(1.0 / (kambe_fac((l - mm - k) / 2) * kambe_fac((l + mm - k) / 2)), cc));
-            }
-            csum = fadd(csum, fmulc(fmulc(cp[n], dl[n]), b));
-          }
-          const int lm = l * (l + 1) + m;
-          out[lm] = fadd(out[lm], fmulc(fscal(flm[lm], fmulc(ex, csum)), fipow(1 - m)));
-        }
-    } else {
-      for (int l = 0; l <= lmax2; l++)
-        for (int m = -l; m <= l; m++) {
-          const int mm = m < 0 ? -m : m;
-          if ((l - mm) % 2) continue;
-          const fcplx ex = fmulc(fpowi(ex2, -m), cs1);
-          fcplx csum = fc(0.0, 0.0);
-          for (int n = 0; n <= (l - mm) / 2; n++) {
-            const fcplx t = fmulc(fmulc(cp[n], cm[l - 2 * n]), gam[n]);
-            csum = fadd(csum, fscal(1.0 / (kambe_fac(n) * kambe_fac((l - mm - 2 * n) / 2) *
-                                           kambe_fac((l + mm - 2 * n) / 2)), t));
-          }
-          const int lm = l * (l + 1) + m;
-          out[lm] = fadd(out[lm], fmulc(fscal(flm[lm], fmulc(ex, csum)), fipow(1 - m)));
-        }
-    }
+  const fcplx e = K.e, kappa = K.kappa;
+  const fcplx kp = fsqrtc(fsub(e, fc(km2, 0.0)));
+  const fcplx ex2 = km > 1e-10 ? fc(gkx / km, gky / km) : fc(1.0, 0.0);
+  const fcplx xc = fscal(0.5, fmulc(fmulc(K.xrot, fsub(e, fc(km * km, 0.0))), K.w));
+  kambe_incgamma(lmax2, xc, gam);
+  const fcplx rp = fdivc(kp, kappa), rm = fdivc(fc(km, 0.0), kappa);
+  for (int l = 0; l <= lmax2; l++) {
+    cp[l] = fpowi(rp, 2 * l - 1);
+    cm[l] = fpowi(rm, l);
   }
-  fcplx ylm[(SKKR_KAMBE_L2 + 1) * (SKKR_KAMBE_L2 + 1)], intil[SKKR_KAMBE_L2 + 1];
-  for (int ir = 0; ir < nr; ir++) {
-    const double rx = rvec[2 * ir], ry = rvec[2 * ir + 1];
-    const double vx = rx + sx, vy = ry + sy, vz = sz;
-    const double rs = sqrt(vx * vx + vy * vy + vz * vz);
-    if (rs < 1e-5 || sqrt(vx * vx + vy * vy) > rcut) continue;
-    const fcplx ex1 = fexpc(fc(0.0, -(rx * kx + ry * ky)));
-    kambe_ylm(vx, vy, vz, lmax2, ylm);
-    kambe_ilkam(lmax2, alpha, rs, kappa, intil);
-    const fcplx a = fscal(-0.5 * rs, kappa);
-    fcplx b = fdivc(fmulc(ex1, cs2), a);
-    for (int l = 0; l <= lmax2; l++) {
-      b = fmulc(b, a);
-      const fcplx c = fmulc(intil[l], b);
+  if (K.f35) {
+    const double sz = K.sz;
+    kambe_delkam(lmax2, xc, fmulc(fscal(sz, kp), fscal(sz, kp)), dl);
+    const fcplx ex1 = fmulc(fexpc(fc(0.0, gkx * K.sx + gky * K.sy)), K.cs1);
+    for (int l = 0; l <= lmax2; l++)
       for (int m = -l; m <= l; m++) {
+        const int mm = m < 0 ? -m : m, ipar = (l - mm) % 2;
+        const fcplx ex = fmulc(fpowi(ex2, -m), ex1);
+        fcplx csum = fc(0.0, 0.0);
+        for (int n = 0; n <= l - mm; n++) {
+          fcplx b = fc(0.0, 0.0);
+          const int kmax = 2 * n < l - mm ? 2 * n : l - mm;
+          for (int k = n + (n + ipar) % 2; k <= kmax; k += 2) {
+            const int i = 2 * n - k, j = l - k;
+            const fcplx cc = fscal(1.0 / (kambe_fac(i) * kambe_fac(k - n)), fmulc(K.cs[i], cm[j]));
+            b = fadd(b, fscal(1.0 / (kambe_fac((l - mm - k) / 2) * kambe_fac((l + mm - k) / 2)), cc));
+          }
+          csum = fadd(csum, fmulc(fmulc(cp[n], dl[n]), b));
+        }
         const int lm = l * (l + 1) + m;
-        out[lm] = fadd(out[lm], fmulc(c, fconj(ylm[lm])));
+        out[lm] = fadd(out[lm], fmulc(fscal(K.flm[lm], fmulc(ex, csum)), fipow(1 - m)));
       }
+  } else {
+    for (int l = 0; l <= lmax2; l++)
+      for (int m = -l; m <= l; m++) {
+        const int mm = m < 0 ? -m : m;
+        if ((l - mm) % 2) continue;
+        const fcplx ex = fmulc(fpowi(ex2, -m), K.cs1);
+        fcplx csum = fc(0.0, 0.0);
+        for (int n = 0; n <= (l - mm) / 2; n++) {
+          const fcplx t = fmulc(fmulc(cp[n], cm[l - 2 * n]), gam[n]);
+          csum = fadd(csum, fscal(1.0 / (kambe_fac(n) * kambe_fac((l - mm - 2 * n) / 2) *
+                                         kambe_fac((l + mm - 2 * n) / 2)), t));
+        }
+        const int lm = l * (l + 1) + m;
+        out[lm] = fadd(out[lm], fmulc(fscal(K.flm[lm], fmulc(ex, csum)), fipow(1 - m)));
+      }
+  }
+}
+
+// the real-space term of one R (formula 47)
+SKKR_HD inline void kambe_rterm(const KambeSetup &K, double rx, double ry, double rcut, fcplx *out) {
+  const int lmax2 = K.lmax2;
+  const double vx = rx + K.sx, vy = ry + K.sy, vz = K.sz;
+  const double rs = sqrt(vx * vx + vy * vy + vz * vz);
+  if (rs < 1e-5 || sqrt(vx * vx + vy * vy) > rcut) return;
+  fcplx ylm[(SKKR_KAMBE_L2 + 1) * (SKKR_KAMBE_L2 + 1)], intil[SKKR_KAMBE_L2 + 1];
+  const fcplx ex1 = fexpc(fc(0.0, -(rx * K.kx + ry * K.ky)));
+  kambe_ylm(vx, vy, vz, lmax2, ylm);
+  kambe_ilkam(lmax2, K.alpha, rs, K.kappa, intil);
+  const fcplx a = fscal(-0.5 * rs, K.kappa);
+  fcplx b = fdivc(fmulc(ex1, K.cs2), a);
+  for (int l = 0; l <= lmax2; l++) {
+    b = fmulc(b, a);
+    const fcplx c = fmulc(intil[l], b);
+    for (int m = -l; m <= l; m++) {
+      const int lm = l * (l + 1) + m;
+      out[lm] = fadd(out[lm], fmulc(c, fconj(ylm[lm])));
     }
   }
+}
+
+// D_L(k, s) into out[(lmax2+1)^2] (kamstr.f dlm1 + dlm2): the self term,
+// then the g terms and the R terms in list order
+SKKR_HD inline void kambe_dlm(fcplx e, double kx, double ky, double sx, double sy, double sz, int lmax2,
+                              const double *gvec, int ng, const double *rvec, int nr, double area,
+                              double factor, double gcut, double rcut, fcplx *out) {
+  const int lmmx = (lmax2 + 1) * (lmax2 + 1);
+  KambeSetup K;
+  kambe_setup(e, kx, ky, sx, sy, sz, lmax2, area, factor, K);
+  for (int i = 0; i < lmmx; i++) out[i] = fc(0.0, 0.0);
+  kambe_self_term(K, out);
+  for (int ig = 0; ig < ng; ig++) kambe_gterm(K, gvec[2 * ig], gvec[2 * ig + 1], gcut, out);
+  for (int ir = 0; ir < nr; ir++) kambe_rterm(K, rvec[2 * ir], rvec[2 * ir + 1], rcut, out);
 }
 
 // alm(k, s)[L][L'] = sum_L'' coef[L][L'][L''] D_L''(k, s), the layer-pair
@@ -286,10 +323,11 @@ SKKR_HD inline void kambe_alm(const fcplx *d, int lmax, const double *coef, fcpl
 }
 
 // element e of the slab matrices of one batch (column-major N x N per k,
-// N = nl lm): G[(a,L),(b,L')] = e^{ik.(pos_b - pos_a)} alm[k][a][b][L][L'],
+// N = nl lm): G[(a,L),(b,L')] = e^{ik.(pos_b - pos_a)} alm_ab[L][L'],
 // A = 1 - alpha[a][l(L)] G; alm, alpha, G, A complex (re, im interleaved)
-SKKR_HD inline void kambe_slab_elem(long long e, int nl, int lm, const double *alm, const double *kxy,
-                                    const double *pos, const double *alpha, int nal, double *G, double *A) {
+SKKR_HD inline void kambe_slab_elem(long long e, int nl, int lm, const double *alm, const int *pmap, int nsep,
+                                    const double *kxy, const double *pos, const double *alpha, int nal, double *G,
+                                    double *A) {
   const int N = nl * lm;
   const long long NN = (long long)N * N;
   const int k = (int)(e / NN);
@@ -298,7 +336,8 @@ SKKR_HD inline void kambe_slab_elem(long long e, int nl, int lm, const double *a
   const int a = row / lm, L = row - a * lm, b = col / lm, Lp = col - b * lm;
   int l = 0;
   while ((l + 1) * (l + 1) <= L) l++;
-  const long long iv = ((((long long)k * nl + a) * nl + b) * lm + L) * lm + Lp;
+  // the pair's lattice sums: alm[k][pmap[a][b]] (its separation among nsep)
+  const long long iv = (((long long)k * nsep + pmap[a * nl + b]) * lm + L) * lm + Lp;
   const double ph = kxy[2 * k] * (pos[3 * b] - pos[3 * a]) + kxy[2 * k + 1] * (pos[3 * b + 1] - pos[3 * a + 1]);
   const fcplx g = fmulc(fc(alm[2 * iv], alm[2 * iv + 1]), fc(cos(ph), sin(ph)));
   const fcplx al = fc(alpha[2 * (a * nal + l)], alpha[2 * (a * nal + l) + 1]);
@@ -308,6 +347,23 @@ SKKR_HD inline void kambe_slab_elem(long long e, int nl, int lm, const double *a
   G[2 * e + 1] = g.im;
   A[2 * e] = m.re;
   A[2 * e + 1] = m.im;
+}
+
+// element e (k, j, L', L) of the structure-constant cache: block blk[j] of
+// k, column-major lm x lm, = X[k][(centre, L), (centre + j - jmax, L')];
+// offsets with blk[j] < 0 are not written
+SKKR_HD inline void kambe_slab_cache_elem(long long e, int nl, int lm, int centre, int jmax, const int *blk, int nbk,
+                                          const double *X, double *Gc) {
+  const int N = nl * lm, nj = 2 * jmax + 1;
+  const int L = (int)(e % lm), Lp = (int)((e / lm) % lm), j = (int)((e / ((long long)lm * lm)) % nj);
+  const int k = (int)(e / ((long long)lm * lm * nj));
+  const int b = blk[j];
+  if (b < 0) return;
+  const int row = centre * lm + L, col = (centre + j - jmax) * lm + Lp;
+  const long long ix = (long long)k * N * N + row + (long long)col * N;
+  const long long o = ((long long)k * nbk + b) * lm * lm + L + (long long)Lp * lm;
+  Gc[2 * o] = X[2 * ix];
+  Gc[2 * o + 1] = X[2 * ix + 1];
 }
 
 // element e of out[k][j][L][L'] = X[k][(centre, L), (centre + j - jmax, L')]

@@ -25,7 +25,7 @@ void launch_zgemm(int mode, const MatRef &A, const MatRef &B, const MatRef &C, c
                   const MatRef &E, int m, int n, int kdim, int nk, int nc, const int *act,
                   cudaStream_t st);
 
-// in-place Gauss-Jordan inverses (gjinv.f), one CTA per item
+// in-place Gauss-Jordan inverses (gjinv.f), one CTA per item, n <= 512
 void launch_zgj(const MatRef &A, int n, int nk, int nc, const int *act, cudaStream_t st);
 
 // elementwise: out = a + s1*b + s2*d over n x n (b/d may be null)
@@ -166,7 +166,14 @@ void launch_kambe_alm(int nitem, double er, double ei, const double *kxy, const 
 // slab screening of the reference's k-space form (kernels_kambe.cu):
 // G and A = 1 - alpha G per k from the layer-pair blocks, and the central
 // layer offsets of X = G A^-1
-void launch_slab_assemble(int nk, int nl, int lm, const zd *alm, const double *kxy, const double *pos,
-                          const zd *alpha, int nal, zd *G, zd *A, cudaStream_t st);
+void launch_slab_assemble(int nk, int nl, int lm, const zd *alm, const int *pmap, int nsep, const double *kxy,
+                          const double *pos, const zd *alpha, int nal, zd *G, zd *A, cudaStream_t st);
 void launch_slab_extract(int nk, int nl, int lm, int centre, int jmax, const zd *X, zd *out, cudaStream_t st);
+// the central offsets straight into the structure-constant cache: block
+// blk[j] of each k (column-major lm x lm, nbk blocks per k)
+void launch_slab_cache(int nk, int nl, int lm, int centre, int jmax, const int *blk, int nbk, const zd *X, zd *Gc,
+                       cudaStream_t st);
+// the (k, separation) items of the lattice sums: xk[it / nsep], seps[it % nsep]
+void launch_kambe_items(int nk, int nsep, const double *xk, const double *seps, double *ik, double *is,
+                        cudaStream_t st);
 

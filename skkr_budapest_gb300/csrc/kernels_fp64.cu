@@ -305,9 +305,9 @@ __global__ void __launch_bounds__(512) k_zgj(MatRef A, int n, int nc, const int 
   if (act && !act[item]) return;
   zd *a = mat_ptr(A, kk, cc);
   const int ld = A.ld;
-  __shared__ int ind[256];
-  __shared__ zd coli[256];
-  __shared__ zd rowi[256];
+  __shared__ int ind[512];    // n <= 512
+  __shared__ zd coli[512];
+  __shared__ zd rowi[512];
   __shared__ double rv[32];
   __shared__ int ri[32];
   const int tid = threadIdx.x, nth = blockDim.x;

@@ -39,7 +39,13 @@ class Status(C.Structure):
                 ("max_dec_iters", I), ("dec_iters_total", C.c_longlong),
                 ("gpu_launches", C.c_longlong), ("max_refine_resid", D), ("run_ms", D),
                 ("inv_fallbacks", C.c_longlong), ("k_fp64", C.c_longlong),
-                ("inv_refined", C.c_longlong), ("alg_flops", D)]
+                ("inv_refined", C.c_longlong), ("alg_flops", D), ("graph_launches", C.c_longlong),
+                ("graph_kernels", C.c_longlong)]
+
+
+class KambeForm(C.Structure):
+    _fields_ = [("e_re", D), ("e_im", D), ("nl", I), ("pos", P), ("alpha", P), ("centre", I), ("gvec", P),
+                ("ng", I), ("rvec", P), ("nr", I), ("area", D), ("factor", D), ("gcut", D), ("rcut", D)]
 
 
 class SkkrError(RuntimeError):
@@ -79,8 +85,10 @@ def lib():
         L.skkr_gpu_kambe_screened.argtypes = [I, D, D, P, I, P, P, I, P, I, P, I, D, D, D, D, I, I, P]
         L.skkr_gpu_layer_dos.argtypes = [I, I, I, P, I, P, P, I, P, P]
         L.skkr_gpu_set_reduce.argtypes = [P, P, P]
+        L.skkr_gpu_set_reduce_device.argtypes = [P, P, P]
         L.skkr_gpu_set_mixed_policy.argtypes = [P, D, D, I, D]
         L.skkr_gpu_set_graphs.argtypes = [P, I]
+        L.skkr_gpu_stage_kambe.argtypes = [P, P]
         L.skkr_gpu_cpacoord_many.argtypes = [I, P, P, P]
         L.skkr_gpu_gjinv_batch.argtypes = [I, I, P, I]
         L.skkr_gpu_surfgf_batch.argtypes = [I, I, P, P, P, P, I, I, D, P, P]
@@ -358,6 +366,22 @@ def kambe_screened(e, kxy, pos, alpha, lmax, gvec, rvec, area, centre, jmax, fac
 
 
 REDUCE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.POINTER(C.c_double), C.c_longlong)
+
+
+REDUCE_DEV_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_longlong, C.c_void_p)
+
+
+def reduce_device_callback(fn):
+    """skkr_reduce_dev_fn around fn(ptr, n, stream): ptr the device address
+    of n doubles, stream the library's cudaStream_t (as an int); an exception
+    is reported to the library as a failed reduction."""
+    def cb(_user, buf, n, stream):
+        try:
+            fn(int(buf), int(n), int(stream or 0))
+            return 0
+        except Exception:  # noqa: BLE001
+            return 1
+    return REDUCE_DEV_FN(cb)
 
 
 def reduce_callback(fn):

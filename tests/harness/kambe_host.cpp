@@ -25,10 +25,17 @@ extern "C" void kambe_alm_eval(double er, double ei, double kx, double ky, doubl
   }
 }
 
-extern "C" void slab_assemble_eval(int nk, int nl, int lm, const double *alm, const double *kxy, const double *pos,
-                                   const double *alpha, int nal, double *G, double *A) {
+extern "C" void slab_assemble_eval(int nk, int nl, int lm, const double *alm, const int *pmap, int nsep,
+                                   const double *kxy, const double *pos, const double *alpha, int nal, double *G,
+                                   double *A) {
   const long long tot = (long long)nk * nl * lm * nl * lm;
-  for (long long e = 0; e < tot; e++) kambe_slab_elem(e, nl, lm, alm, kxy, pos, alpha, nal, G, A);
+  for (long long e = 0; e < tot; e++) kambe_slab_elem(e, nl, lm, alm, pmap, nsep, kxy, pos, alpha, nal, G, A);
+}
+
+extern "C" void slab_cache_eval(int nk, int nl, int lm, int centre, int jmax, const int *blk, int nbk, const double *X,
+                                double *Gc) {
+  const long long tot = (long long)nk * (2 * jmax + 1) * lm * lm;
+  for (long long e = 0; e < tot; e++) kambe_slab_cache_elem(e, nl, lm, centre, jmax, blk, nbk, X, Gc);
 }
 
 extern "C" void slab_extract_eval(int nk, int nl, int lm, int centre, int jmax, const double *X, double *out) {

@@ -17,7 +17,7 @@ def rel(a, b):
     return np.linalg.norm(a - b) / np.linalg.norm(b)
 
 
-@pytest.mark.parametrize("n", [1, 9, 18, 54, 128, 256])
+@pytest.mark.parametrize("n", [1, 9, 18, 54, 128, 256, 448])
 def test_gjinv_batch(n):
     a = rng.normal(size=(3, n, n)) + 1j * rng.normal(size=(3, n, n)) + 2 * np.eye(n)
     g = native.gjinv_batch(a)

@@ -21,7 +21,9 @@ def _run(ctx, slot):
 
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
 def test_slots_equal_fresh_contexts(precision):
-    spec = W.rel_bcc()
+    # unsplit wells under the 2 Ry / 0.7 d_NN barrier: these energies carry
+    # isolated peaks of the k integrand, so the FP64 redo path runs
+    spec = W.rel_bcc(so_split=0.0, vscreen=2.0, rscreen=0.7)
     order = [0, 12, 16, 4]
     eps = {ie: W.energy_problem(spec, ie) for ie in order}
     ctx = api.Context.for_problem(eps[order[0]], precision)

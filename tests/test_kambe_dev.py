@@ -94,8 +94,9 @@ def test_slab_chain_of_the_device_entry_point(lib):
     from skkr_budapest_gb300 import workloads as W
     D, I, P = ctypes.c_double, ctypes.c_int, ctypes.c_void_p
     lib.kambe_alm_eval.argtypes = [D, D, D, D, D, D, D, I, P, I, P, I, D, D, D, P, P]
-    lib.slab_assemble_eval.argtypes = [I, I, I, P, P, P, P, I, P, P]
+    lib.slab_assemble_eval.argtypes = [I, I, I, P, P, I, P, P, P, I, P, P]
     lib.slab_extract_eval.argtypes = [I, I, I, I, I, P, P]
+    lib.slab_cache_eval.argtypes = [I, I, I, I, I, P, I, P, P]
     spec = W.plain_fcc(nset=4)
     st = spec.stacking
     lat = K.Lattice2D([st.a2d, 0.0], [0.0, st.a2d])
@@ -113,27 +114,47 @@ def test_slab_chain_of_the_device_entry_point(lib):
     Lb.skkr_gpu_kambe_coef(lmax, coef.ctypes.data)
     g = np.ascontiguousarray(lat.gvecs(14.0))
     r = np.ascontiguousarray(lat.rvecs(55.0))
-    alm = np.zeros((len(kpts), nl, nl, lm, lm), complex)
+    # the lattice sums once per distinct separation, the pairs through a map
+    # (this stacking's sites alternate by half a lattice vector: 15
+    # separations for 6 layers instead of 36 pairs)
+    seps, pmap = [], np.zeros((nl, nl), np.int32)
+    for a in range(nl):
+        for b in range(nl):
+            sv = tuple(np.round(pos[a] - pos[b], 9))
+            if sv not in seps:
+                seps.append(sv)
+            pmap[a, b] = seps.index(sv)
+    assert len(seps) == 15
+    alm = np.zeros((len(kpts), len(seps), lm, lm), complex)
     for ik, k in enumerate(kpts):
-        for a in range(nl):
-            for b in range(nl):
-                out = np.zeros(2 * lm * lm)
-                s = pos[a] - pos[b]
-                lib.kambe_alm_eval(ce.real, ce.imag, k[0], k[1], *s, lmax, g.ctypes.data, len(g), r.ctypes.data,
-                                   len(r), lat.area, 12.0, 40.0, coef.ctypes.data, out.ctypes.data)
-                alm[ik, a, b] = (out[0::2] + 1j * out[1::2]).reshape(lm, lm)
+        for q, sv in enumerate(seps):
+            out = np.zeros(2 * lm * lm)
+            lib.kambe_alm_eval(ce.real, ce.imag, k[0], k[1], *sv, lmax, g.ctypes.data, len(g), r.ctypes.data,
+                               len(r), lat.area, 12.0, 40.0, coef.ctypes.data, out.ctypes.data)
+            alm[ik, q] = (out[0::2] + 1j * out[1::2]).reshape(lm, lm)
     alm = np.ascontiguousarray(alm)
     alpha = np.ascontiguousarray(np.array([al] * nl, complex))
     N = nl * lm
     G = np.zeros((len(kpts), N, N), complex)
     A = np.zeros_like(G)
-    lib.slab_assemble_eval(len(kpts), nl, lm, alm.ctypes.data, kpts.ctypes.data, pos.ctypes.data,
-                           alpha.ctypes.data, lmax + 1, G.ctypes.data, A.ctypes.data)
+    lib.slab_assemble_eval(len(kpts), nl, lm, alm.ctypes.data, np.ascontiguousarray(pmap).ctypes.data, len(seps),
+                           kpts.ctypes.data, pos.ctypes.data, alpha.ctypes.data, lmax + 1, G.ctypes.data,
+                           A.ctypes.data)
     # the buffers are column-major per k: transpose to (row, col)
     G, A = G.transpose(0, 2, 1), A.transpose(0, 2, 1)
     X = np.ascontiguousarray(np.array([Gk @ np.linalg.inv(Ak) for Gk, Ak in zip(G, A)]).transpose(0, 2, 1))
     out = np.zeros((len(kpts), 2 * jmax + 1, lm, lm), complex)
     lib.slab_extract_eval(len(kpts), nl, lm, centre, jmax, X.ctypes.data, out.ctypes.data)
+    # the same blocks written into a structure-constant cache of 7 blocks per
+    # k (column-major), offset j at block blk[j], offset +2 left out
+    blk = np.array([4, 0, 6, 2, -1], np.int32)
+    cache = np.zeros((len(kpts), 7, lm, lm), complex)
+    lib.slab_cache_eval(len(kpts), nl, lm, centre, jmax, blk.ctypes.data, 7, X.ctypes.data, cache.ctypes.data)
+    for ik in range(len(kpts)):
+        for j in range(2 * jmax + 1):
+            if blk[j] >= 0:
+                assert np.array_equal(cache[ik, blk[j]].T, out[ik, j])
+        assert not cache[ik, [1, 3, 5]].any()
     for ik, k in enumerate(kpts):
         gs = K.screened_slab(ce, k[0], k[1], lmax, pos, [al] * nl, lat)
         ref = np.array([gs[centre, centre + j] for j in range(-jmax, jmax + 1)])

@@ -176,7 +176,7 @@ def test_kambe_screened_argument_checks_before_any_device_call():
     D, I, P = ctypes.c_double, ctypes.c_int, ctypes.c_void_p
     lib.skkr_gpu_kambe_screened.argtypes = [I, D, D, P, I, P, P, I, P, I, P, I, D, D, D, D, I, I, P]
     b = np.zeros(256).ctypes.data
-    # 17 layers of lmax 3 exceed the 256-row inverse; the centre must leave jmax layers on each side
-    assert lib.skkr_gpu_kambe_screened(1, 0.5, 0.01, b, 17, b, b, 3, b, 3, b, 3, 23.1, 1.0, 12.0, 40.0, 8, 2, b) == -1
+    # 33 layers of lmax 3 exceed the 512-row inverse; the centre must leave jmax layers on each side
+    assert lib.skkr_gpu_kambe_screened(1, 0.5, 0.01, b, 33, b, b, 3, b, 3, b, 3, 23.1, 1.0, 12.0, 40.0, 8, 2, b) == -1
     assert lib.skkr_gpu_kambe_screened(1, 0.5, 0.01, b, 8, b, b, 2, b, 3, b, 3, 23.1, 1.0, 12.0, 40.0, 1, 2, b) == -1
     assert lib.skkr_gpu_kambe_screened(1, 0.5, 0.01, b, 8, b, b, 2, b, 3, b, 3, 23.1, 1.0, 12.0, 40.0, 6, 2, b) == -1
