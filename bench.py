@@ -62,9 +62,17 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", action="store_true",
                     help="only the device loop of the timed steps (for ncu captures); prints a short line")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "tauij"],
+    ap.add_argument("--slab", type=int, default=12, help="gk workload: layers of the screening slab")
+    ap.add_argument("--slices", type=int, default=0, help="BF16 slices per product operand (0: the library's 6)")
+    ap.add_argument("--newton", type=int, default=2, help="standard Newton steps of the split-precision inverse")
+    ap.add_argument("--fp64-ref", default="", help="file of the FP64 pass (tau per energy, timing): written when "
+                                                   "absent, read instead of rerunning the FP64 pass when present")
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5", "gk", "tauij"],
                     help="c3: one energy of each of three systems per step through skkr_gpu_cpacoord_many; "
                          "c4: CPA alloy interfaces from the ATA and from the learned start; "
+                         "c5: the BdG interface (n_PL = 256, Im E = 1e-4 Ry), FP64 and split precision; "
+                         "gk: the C2 path on the reference's k-space G_scr(k) (Kambe sums + slab screening) "
+                         "beside the table transform; "
                          "tauij: the off-diagonal tau of the interface (skkr_gpu_tauij) per step")
     return ap.parse_args()
 
@@ -362,7 +370,9 @@ def run_ours(args, rank, ws):
     mine = {ie: api.ksplit_problem(ep, rank, ws) for ie, ep in eps.items()} if split_k else eps
 
     def context(precision):
-        c = api.Context.for_problem(eps[order[0]], precision=precision)
+        c = api.Context.for_problem(eps[order[0]], precision=precision, slices=args.slices)
+        if precision == "mixed":
+            c.set_newton(args.newton)
         if split_k:
             c.set_reduce_device(api.torch_allreduce_device())
         return c
@@ -394,17 +404,25 @@ def run_ours(args, rank, ws):
     # and the error of the k-summed tau against it
     fp64 = None
     if args.precision == "mixed" and not args.no_fp64_compare:
-        cref = context("fp64")
-        for ie, sl in slot_of.items():
-            cref.stage_slot(sl, mine[ie])
-        r64 = timed_steps(cref, order, slot_of, eps, args, flush)
+        timed = order[args.warmup:]
+        if args.fp64_ref and os.path.exists(args.fp64_ref):
+            z = np.load(args.fp64_ref)
+            ref_tau = {int(ie): z["tau_%d" % ie] for ie in set(timed)}
+            r64 = {"t_dev": float(z["t_dev"])}
+        else:
+            cref = context("fp64")
+            for ie, sl in slot_of.items():
+                cref.stage_slot(sl, mine[ie])
+            r64 = timed_steps(cref, order, slot_of, eps, args, flush)
+            ref_tau = {ie: cref.fetch_slot(slot_of[ie])["tauc"] for ie in set(timed)}
+            cref.close()
+            if args.fp64_ref:
+                np.savez(args.fp64_ref, t_dev=r64["t_dev"], **{"tau_%d" % ie: v for ie, v in ref_tau.items()})
         errs = []
-        for ie, sl in slot_of.items():
-            if ie in order[args.warmup:]:
-                a = ctx.fetch_slot(sl)["tauc"]
-                b = cref.fetch_slot(sl)["tauc"]
-                errs.append(float(np.linalg.norm(a - b) / np.linalg.norm(b)))
-        cref.close()
+        for ie in set(timed):
+            a = ctx.fetch_slot(slot_of[ie])["tauc"]
+            b = ref_tau[ie]
+            errs.append(float(np.linalg.norm(a - b) / np.linalg.norm(b)))
         t64 = max_over_ranks(r64["t_dev"], ws)
         v64 = pts_all / (t64 * 1e-3)
         fp64 = {"value": v64, "unit": UNIT, "ms_per_step": t64 / args.steps, "speedup": value / v64,
@@ -446,10 +464,12 @@ def run_ours(args, rank, ws):
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
             "scaling": "strong" if split_k else "weak", "vs_baseline": None,
-            "dtype": "c128" if args.precision == "fp64" else "c128 via BF16x6 slices + FP64 refinement",
+            "dtype": "c128" if args.precision == "fp64" else
+            "c128 via BF16x%d slices + FP64 refinement" % (args.slices or 6),
             "data": "synthetic (seeded square wells, real-space screened structure constants)",
             "config": {"workload": WORKLOAD, "precision": args.precision,
                        "step": "one contour energy, all k, full CPA pass",
+                       "slices": args.slices or 6, "newton_steps": args.newton,
                        "parallelism": ("k split over %d ranks, NCCL allreduce per CPA iteration" % ws) if split_k
                        else "energies over %d ranks" % ws,
                        "step_energies": order[args.warmup:], "points": r["pts"],
@@ -649,6 +669,141 @@ def run_c4(args):
     print(json.dumps(line), flush=True)
 
 
+C5_METRIC = "(E,k) points/s of the BdG interface (anomalous block within 1e-9 of FP64)"
+C5_ENERGIES = [8, 24, 40, 56]
+C5_NSET = 12
+
+
+def _c5_problems():
+    from skkr_budapest_gb300 import workloads as W
+    spec = W.bdg_bcc()
+    return spec, {ie: W.energy_problem(spec, ie, nset=C5_NSET) for ie in C5_ENERGIES}
+
+
+def run_c5(args):
+    """The Bogoliubov-de Gennes interface of config C5 (electron + hole
+    (kappa,mu) blocks, lmax=3, PL4: n_PL = 256, 12 layers, Im E = 1e-4 Ry)
+    on a bounded sample: 4 of its 64 energies, 78-point IBZ meshes.  FP64 and
+    split precision (near the axis the decimation stays FP64 by policy, tau2d
+    runs split), through skkr_gpu_cpacoord_bdg with host buffers; the error
+    of the k-summed tau and of its electron-hole block against FP64."""
+    import torch
+    from skkr_budapest_gb300 import api
+    spec, eps = _c5_problems()
+    order = [C5_ENERGIES[i % len(C5_ENERGIES)] for i in range(args.warmup + args.steps)]
+    out, tau = {}, {}
+    for prec in ("fp64", "mixed"):
+        ctx = api.Context.for_problem(eps[order[0]], prec)
+        for ie in order[:args.warmup]:
+            ctx.cpacoord(eps[ie])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        pts, dev = 0, 0.0
+        for ie in order[args.warmup:]:
+            r = ctx.cpacoord(eps[ie])
+            pts += eps[ie].nk
+            dev += r["run_ms"]
+            tau[(prec, ie)] = r["tauc"]
+        torch.cuda.synchronize()
+        out[prec] = dict(wall=time.perf_counter() - t0, pts=pts, dev=dev)
+        ctx.close()
+    km = eps[order[0]].lkmax // 2
+    err = err_eh = 0.0
+    for ie in set(order[args.warmup:]):
+        a, b = tau[("mixed", ie)], tau[("fp64", ie)]
+        err = max(err, float(np.linalg.norm(a - b) / np.linalg.norm(b)))
+        e, f = a[:, :km, km:], b[:, :km, km:]
+        err_eh = max(err_eh, float(np.linalg.norm(e - f) / np.linalg.norm(f)))
+    rate = {k: v["pts"] / (v["dev"] * 1e-3) for k, v in out.items()}
+    print(json.dumps({"metric": C5_METRIC, "value": rate["mixed"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+                      "warmup": args.warmup, "ms_per_step": out["mixed"]["dev"] / args.steps,
+                      "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                      "dtype": "c128 via BF16 slices (electron and hole K halves) + FP64 refinement",
+                      "data": "synthetic (seeded)",
+                      "config": {"workload": "c5: BdG bcc(001) lmax=3 PL4 (n_PL = 256), 12 layers, delta = 1e-3 Ry, "
+                                             "Im E = 1e-4 Ry, energies %s of 64, %d k each" %
+                                             (C5_ENERGIES, eps[order[0]].nk),
+                                 "sample": "4 of the 64 energies on 78-point meshes (40000 k per energy would take "
+                                           "about half an hour per energy with the FP64 decimation near the axis)"},
+                      "fp64_value": rate["fp64"], "speedup": rate["mixed"] / rate["fp64"],
+                      "max_rel_err_tau_vs_fp64": err, "max_rel_err_anomalous_block_vs_fp64": err_eh,
+                      "e2e": {"value": out["mixed"]["pts"] / out["mixed"]["wall"], "unit": UNIT,
+                              "h2d_bytes_per_step": None, "d2h_bytes_per_step": None}}), flush=True)
+
+
+def run_c5_reference(args):
+    """Reference arm of the BdG workload: the oracle's CPA and k loop on all
+    host threads, one k point per thread spread over each energy's mesh."""
+    nth = os.cpu_count() or 1
+    _, eps = _c5_problems()
+    order = [C5_ENERGIES[i % len(C5_ENERGIES)] for i in range(args.warmup + args.steps)]
+    _oracle_rate([eps[ie] for ie in order[:args.warmup]], nth, nth)
+    v, pts, dt = _oracle_rate([eps[ie] for ie in order[args.warmup:]], nth, nth)
+    print(json.dumps({"impl": "reference", "metric": C5_METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+                      "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+                      "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+                      "data": "synthetic (seeded)",
+                      "config": {"workload": "c5 (see the GPU arm)", "step": "strided k sample of one energy (CPU)"},
+                      "cpu_baseline": {"value": v, "unit": UNIT, "cores": nth, "kind": "port",
+                                       "sample": "%d k points per step, %d steps" % (nth, args.steps)},
+                      "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}),
+          flush=True)
+
+
+GK_METRIC = "(E,k) points/s of the C2 path with the reference's k-space G_scr(k)"
+
+
+def run_gk(args):
+    """The relativistic PL4 lmax=3 interface with G_scr(k) from the
+    reference's own form (Kambe lattice sums of the slab's distinct layer
+    separations, slab screening, skkr_gpu_stage_kambe) against the same
+    energies on the table transform: (E,k)/s of each, the time of the G(k)
+    build, and the relative difference of the k-summed tau between the two
+    formulations (the truncation of the three-shell table, not an error)."""
+    import torch
+    from skkr_budapest_gb300 import api, kspace
+    from skkr_budapest_gb300 import workloads as W
+    spec = W.rel_bcc()
+    plan = [4, 8, 12, 16, 18]
+    order = [plan[i % len(plan)] for i in range(args.warmup + args.steps)]
+    eps = {ie: W.energy_problem(spec, ie) for ie in set(order)}
+    forms = {ie: kspace.kambe_form(ep, spec, nl=args.slab) for ie, ep in eps.items()}
+    out, tau = {}, {}
+    for name in ("table", "kambe"):
+        ctx = api.Context.for_problem(eps[order[0]], args.precision)
+        run = (lambda ie: ctx.cpacoord_kambe(eps[ie], forms[ie])) if name == "kambe" else \
+            (lambda ie: ctx.cpacoord(eps[ie]))
+        for ie in order[:args.warmup]:
+            run(ie)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        pts, dev = 0, 0.0
+        for ie in order[args.warmup:]:
+            r = run(ie)
+            pts += eps[ie].nk
+            dev += r["run_ms"]
+            tau[(name, ie)] = r["tauc"]
+        torch.cuda.synchronize()
+        out[name] = dict(wall=time.perf_counter() - t0, pts=pts, dev=dev)
+        ctx.close()
+    diff = max(float(np.linalg.norm(tau[("kambe", ie)] - tau[("table", ie)]) / np.linalg.norm(tau[("kambe", ie)]))
+               for ie in set(order[args.warmup:]))
+    rate = {k: v["pts"] / (v["dev"] * 1e-3) for k, v in out.items()}
+    print(json.dumps({"metric": GK_METRIC, "value": rate["kambe"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+                      "warmup": args.warmup, "ms_per_step": out["kambe"]["dev"] / args.steps,
+                      "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                      "dtype": "c128" if args.precision == "fp64" else "c128 via BF16 slices + FP64 refinement",
+                      "data": "synthetic (seeded)",
+                      "config": {"workload": "rel_bcc001_lmax3_pl4 energies %s, full meshes" % plan,
+                                 "slab_layers": args.slab, "slab_rows": args.slab * 16,
+                                 "screening": "%.1f Ry, %.4f d_NN" % (spec.vscreen, spec.rscreen),
+                                 "precision": args.precision},
+                      "table_value": rate["table"], "kambe_over_table_time": out["kambe"]["dev"] / out["table"]["dev"],
+                      "max_rel_diff_tau_kambe_vs_table": diff,
+                      "e2e": {"value": out["kambe"]["pts"] / out["kambe"]["wall"], "unit": UNIT,
+                              "h2d_bytes_per_step": None, "d2h_bytes_per_step": None}}), flush=True)
+
+
 TAUIJ_METRIC = "(E,k) points/s of the off-diagonal interface tau (skkr_gpu_tauij)"
 TAUIJ_WORKLOAD = ("off-diagonal tau of the relativistic bcc(001) PL4 lmax=3 interface: 144 layer pairs at R = 0 "
                   "and the 4 nearest in-plane cells of every layer (192 pairs), contour energies 12 16 14 19 13")
@@ -766,6 +921,20 @@ def main():
             run_c4_reference(args)
         else:
             run_c4(args)
+        return
+    if args.workload == "c5":
+        if args.impl == "reference":
+            run_c5_reference(args)
+        else:
+            run_c5(args)
+        return
+    if args.workload == "gk":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "metric": GK_METRIC,
+                              "unavailable": "the reference's Kambe G(k) has no CPU arm here: the oracle restates it "
+                                             "in numpy per k point (test infrastructure, minutes per k)"}))
+        else:
+            run_gk(args)
         return
     rank, ws = dist_init(args.gpus)
     if args.impl == "reference":

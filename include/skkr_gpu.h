@@ -137,6 +137,22 @@ int skkr_gpu_destroy(skkr_ctx *ctx);
 int skkr_gpu_set_mixed_policy(skkr_ctx *ctx, double dec_fp64_im, double near_im, int slices_near,
                               double dominant_frac);
 
+/* Standard Newton steps X += X (I - A X) after the FP32 Gauss-Jordan start of
+ * every split-precision inverse (1..3, default 2).  The acceptance test is
+ * unchanged: the residual before the last correction must be below 1e-6 (or
+ * the further steps and the FP64 redo take over), so one step suits inputs
+ * whose FP32 start is already that close. */
+int skkr_gpu_set_newton(skkr_ctx *ctx, int steps);
+
+/* Autotuner of the split-precision inverse's FP32 Gauss-Jordan: each size
+ * class (n <= 32, 64, 128) has 2-3 thread layouts that give the same inverse
+ * bit for bit; the first batch of each (class, batch size) times them once
+ * and later calls use the fastest (process wide).  report (may be NULL)
+ * receives the choices so far, e.g. "n<=128 >=4 waves: 64x2x8; ".
+ * force > 0 makes every class use its layout force - 1 (tests); force = 0
+ * with report NULL forgets the choices and tunes afresh. */
+int skkr_gpu_autotune(int force, char *report, int len);
+
 /* Decimation loop as a CUDA graph (default on): after the first iteration,
  * the remaining iterations of every k chunk run as one graph launch whose
  * WHILE node repeats the iteration body until no (k, lead) item is left,
@@ -144,7 +160,10 @@ int skkr_gpu_set_mixed_policy(skkr_ctx *ctx, double dec_fp64_im, double near_im,
  * inverse's further Newton steps (IF nodes) decided on the device.  on = 0
  * runs every iteration from the host (one stream synchronisation per
  * iteration); results are identical.  While per-kernel statistics are on
- * (skkr_gpu_kernel_stats) the host loop is used. */
+ * (skkr_gpu_kernel_stats), and inside skkr_gpu_cpacoord_many (contexts driven
+ * from several host threads at once), the host loop is used; callers that
+ * drive contexts from their own threads concurrently should switch graphs
+ * off the same way. */
 int skkr_gpu_set_graphs(skkr_ctx *ctx, int on);
 
 /* Off-diagonal tau of the interface for cluster embedding

@@ -56,6 +56,10 @@ class Context:
         N._check(N.lib().skkr_gpu_set_mixed_policy(self.h, dec_fp64_im, near_im, slices_near, dominant_frac),
                  "skkr_gpu_set_mixed_policy")
 
+    def set_newton(self, steps=2):
+        """Standard Newton steps of the split-precision inverse (skkr_gpu_set_newton)."""
+        N._check(N.lib().skkr_gpu_set_newton(self.h, int(steps)), "skkr_gpu_set_newton")
+
     def set_graphs(self, on=True):
         """Decimation loop as one CUDA graph launch per k chunk (the default)
         or one host-driven iteration at a time (skkr_gpu_set_graphs)."""

@@ -62,7 +62,9 @@ class Family:
     alloy_layers: tuple = (4, 5, 6, 7)
     conc_range: tuple = (0.1, 0.9)
     depth_range: tuple = (-1.2, -0.4)
-    energies: tuple = tuple(range(24))
+    # the contour energies with Im E >= 0.013 Ry: nearer the axis a mesh this
+    # coarse leaves the CPA iteration itself stalling above 1e-10 (from any start)
+    energies: tuple = tuple(range(21))
     _base: dict = field(default_factory=dict, repr=False)
 
     def spec(self):
@@ -265,12 +267,15 @@ def generate(out: str, nsolve: int, fam: Family, seed: int = 1000, precision: st
     return len(meta)
 
 
-def train(data: str, out: str, epochs: int = 4000, lr: float = 1e-3, weight_decay: float = 0.0, seed: int = 0,
-          val_frac: float = 0.1, eval_every: int = 25):
+def train(data: str, out: str, schedule=((4000, 1e-3), (4000, 3e-4), (4000, 1e-4)), weight_decay: float = 0.0,
+          seed: int = 0, val_frac: float = 0.1, eval_every: int = 25, norm: str = "global"):
     """Full-batch AdamW of the BF16-weight network on the device
-    (skkr_gpu_mlp16_train), last val_frac of the solves held out, the epoch
-    with the lowest held-out error kept.  Returns (train mse, held-out mse,
-    held-out mse of the ATA start), all in units of the normalised targets."""
+    (skkr_gpu_mlp16_train) in phases of (epochs, learning rate), each phase
+    restarting from the previous phase's best held-out parameters; the last
+    val_frac of the solves is held out.  norm "global": one output scale (the
+    loss is the mean squared error of the correction itself); "column": every
+    output standardised.  Returns (train mse, held-out mse, held-out mse of the
+    ATA start), in units of the targets."""
     from . import native as N
     z = np.load(data)
     x, y, meta = z["x"].astype(np.float64), z["y"].astype(np.float64), z["meta"]
@@ -279,23 +284,30 @@ def train(data: str, out: str, epochs: int = 4000, lr: float = 1e-3, weight_deca
     nval = max(1, int(len(solves) * val_frac))
     val = np.isin(sid, solves[-nval:])
     xm, xsd = x[~val].mean(0), x[~val].std(0) + 1e-12
-    ym, ysd = y[~val].mean(0), y[~val].std(0) + 1e-12
+    if norm == "global":
+        ym, ysd = np.zeros(y.shape[1]), np.full(y.shape[1], y[~val].std() + 1e-12)
+    else:
+        ym, ysd = y[~val].mean(0), y[~val].std(0) + 1e-12
     dims = [x.shape[1], *HIDDEN, y.shape[1]]
     rng = np.random.default_rng(seed)
-    init = [(np.float32(rng.uniform(-1, 1, (a, b)) / np.sqrt(a)), np.zeros(b, np.float32))
-            for a, b in zip(dims[:-1], dims[1:])]
-    _, best, tl, (vl, trl) = N.mlp16_train(init, (x - xm) / xsd, (y - ym) / ysd, (~val).astype(np.uint8),
-                                           epochs, lr, weight_decay, eval_every=eval_every)
+    layers = [(np.float32(rng.uniform(-1, 1, (a, b)) / np.sqrt(a)), np.zeros(b, np.float32))
+              for a, b in zip(dims[:-1], dims[1:])]
+    xs, ys, rows = (x - xm) / xsd, (y - ym) / ysd, (~val).astype(np.uint8)
+    curve, t0 = [], time.time()
+    for epochs, lr in schedule:
+        _, layers, tl, _ = N.mlp16_train(layers, xs, ys, rows, epochs, lr, weight_decay, eval_every=eval_every)
+        curve.append(tl[::max(1, epochs // 100)])
     # errors in target units (what the warm start is off by), and the ATA start's
-    pred = N.mlp16_forward(best, np.float32((x - xm) / xsd)) * ysd + ym
+    pred = N.mlp16_forward(layers, np.float32(xs)) * ysd + ym
     mse_val = float(((pred[val] - y[val]) ** 2).mean())
     mse_tr = float(((pred[~val] - y[~val]) ** 2).mean())
     mse_ata = float((y[val] ** 2).mean())
-    save = {"nlayers": len(best), "xmean": xm, "xstd": xsd, "ymean": ym, "ystd": ysd, "mask": z["mask"],
+    save = {"nlayers": len(layers), "xmean": xm, "xstd": xsd, "ymean": ym, "ystd": ysd, "mask": z["mask"],
             "nset": int(z["nset"]), "so_split": float(z["so_split"]), "train_mse": mse_tr, "val_mse": mse_val,
-            "val_mse_ata": mse_ata, "train_epochs": epochs, "train_loss_curve": tl[::max(1, epochs // 200)],
-            "n_rows": len(x), "n_solves": len(solves)}
-    for i, (w, b) in enumerate(best):
+            "val_mse_ata": mse_ata, "train_schedule": np.array(schedule, float),
+            "train_loss_curve": np.concatenate(curve), "train_seconds": time.time() - t0, "n_rows": len(x),
+            "n_solves": len(solves), "train_norm": norm}
+    for i, (w, b) in enumerate(layers):
         save["w%d" % i] = np.asarray(w, np.float32)
         save["b%d" % i] = np.asarray(b, np.float32)
     os.makedirs(os.path.dirname(os.path.abspath(out)), exist_ok=True)
@@ -345,8 +357,8 @@ def main():
     t = sub.add_parser("train")
     t.add_argument("--data", required=True)
     t.add_argument("--out", default=DEFAULT_MODEL)
-    t.add_argument("--epochs", type=int, default=4000)
-    t.add_argument("--lr", type=float, default=1e-3)
+    t.add_argument("--schedule", default="4000:1e-3,4000:3e-4,4000:1e-4", help="epochs:lr phases")
+    t.add_argument("--norm", choices=("global", "column"), default="global")
     r = sub.add_parser("report")
     r.add_argument("--model", default=DEFAULT_MODEL)
     r.add_argument("--solves", type=int, default=48)
@@ -356,8 +368,9 @@ def main():
                      nctx=a.nctx, graphs=not a.no_graphs, progress=a.progress)
         print("rows:", n)
     elif a.cmd == "train":
+        sched = [(int(p.split(":")[0]), float(p.split(":")[1])) for p in a.schedule.split(",")]
         print("mse train / held out / held out of the ATA start: %.3e / %.3e / %.3e"
-              % train(a.data, a.out, epochs=a.epochs, lr=a.lr))
+              % train(a.data, a.out, schedule=sched, norm=a.norm))
     else:
         rows = report(a.model, a.solves)
         ita = sum(r["it_ata"] for r in rows)

@@ -42,6 +42,11 @@ static thread_local std::string g_last_error;
 
 extern "C" const char *skkr_gpu_last_error(void) { return g_last_error.c_str(); }
 
+std::recursive_mutex &skkr_device_mutex() {
+  static std::recursive_mutex m;
+  return m;
+}
+
 static int g_sync_check = -1;
 // ---- per-kernel-class event timing --------------------------------------
 namespace {
@@ -164,6 +169,7 @@ struct DBuf {
   size_t cap = 0;
   int ensure(size_t bytes) {
     if (bytes <= cap) return SKKR_OK;
+    std::lock_guard<std::recursive_mutex> lk(skkr_device_mutex());
     if (p) {
       cudaDeviceSynchronize();
       cudaFree(p);
@@ -182,6 +188,7 @@ struct DBuf {
   T *as() const { return (T *)p; }
   void release() {
     if (p) {
+      std::lock_guard<std::recursive_mutex> lk(skkr_device_mutex());
       cudaDeviceSynchronize();
       cudaFree(p);
     }
@@ -357,6 +364,7 @@ struct skkr_ctx {
   long long inv_refined = 0;    // inverses that took further Newton steps in this run
   double alg_units = 0.0;       // reference block operations (8 n^3 FLOP each) of this run
   bool graphs = true;           // decimation loop as a CUDA graph WHILE node (skkr_gpu_set_graphs)
+  int newton = 2;               // standard Newton steps of the split-precision inverse (skkr_gpu_set_newton)
   DBuf decctl;                  // [0] iteration, [1] items left, [2] half-bodies run (captured loop)
   long long graph_kernels = 0;  // kernels run inside graphs in this run
   long long graph_launches = 0; // graph launches in this run
@@ -811,8 +819,8 @@ static int eng_gemm(skkr_ctx *c, bool mixed, int mode, const MatRef &A, const Ma
 static int eng_inv(skkr_ctx *c, bool mixed, const MatRef &A, const MatRef &X, bool inplace, int n, int nk,
                    int nc, const int *act) {
   if (mixed && n <= 128)
-    return mixed_zinv(c->mw, A, X, n, nk, nc, act, 2, std::min(8, std::max(c->slices_res, slices_for(c) + 1)),
-                      inplace, c->st);
+    return mixed_zinv(c->mw, A, X, n, nk, nc, act, c->newton,
+                      std::min(8, std::max(c->slices_res, slices_for(c) + 1)), inplace, c->st);
   if (!inplace) launch_zaxpby(X, A, nullptr, 0, nullptr, 0, n, nk, nc, act, c->st);
   launch_zgj(X, n, nk, nc, act, c->st);
   return SKKR_OK;
@@ -836,6 +844,9 @@ static bool use_mixed(const skkr_ctx *c, bool decimation) {
 template <class Iterate>
 static int decimation_graph(skkr_ctx *c, int first, int itermax, Iterate &iterate) {
   cudaStream_t st = c->st;
+  // capture, instantiation and launch never overlap a device-synchronising
+  // allocation of another host thread
+  std::lock_guard<std::recursive_mutex> lk(skkr_device_mutex());
   CKR(c->decctl.ensure(4 * sizeof(int)));
   int *ctl = c->decctl.as<int>();
   const int init[4] = {first, 0, 0, 0};
@@ -1668,6 +1679,22 @@ extern "C" int skkr_gpu_set_mixed_policy(skkr_ctx *c, double dec_fp64_im, double
   return SKKR_OK;
 }
 
+extern "C" int skkr_gpu_autotune(int force, char *report, int len) {
+  if (force < 0 || force > 3) return SKKR_ERR_ARG;
+  if (force > 0 || (!report && force == 0)) gj_tune_force(force);
+  if (report && len > 0) {
+    const std::string r = gj_tune_report();
+    std::snprintf(report, (size_t)len, "%s", r.c_str());
+  }
+  return SKKR_OK;
+}
+
+extern "C" int skkr_gpu_set_newton(skkr_ctx *c, int steps) {
+  if (!c || steps < 1 || steps > 3) return SKKR_ERR_ARG;
+  c->newton = steps;
+  return SKKR_OK;
+}
+
 extern "C" int skkr_gpu_set_graphs(skkr_ctx *c, int on) {
   if (!c) return SKKR_ERR_ARG;
   c->graphs = on != 0;
@@ -1976,6 +2003,14 @@ extern "C" int skkr_gpu_cpacoord_many(int n, skkr_ctx *const *ctx, const skkr_en
       if (ctx[f] == ctx[e]) return SKKR_ERR_ARG;
   }
   std::vector<int> rc(n, SKKR_OK);
+  // the contexts run concurrently from their own host threads: their
+  // decimation loops run from the host (graph capture from several threads
+  // at once is left out), the other threads' launches fill the GPU meanwhile
+  std::vector<bool> graphs(n);
+  for (int e = 0; e < n; e++) {
+    graphs[e] = ctx[e]->graphs;
+    ctx[e]->graphs = false;
+  }
   auto one = [&](int e) {
     skkr_ctx *c = ctx[e];
     const skkr_energy_args &a = args[e];
@@ -1997,6 +2032,7 @@ extern "C" int skkr_gpu_cpacoord_many(int n, skkr_ctx *const *ctx, const skkr_en
   for (int e = 1; e < n; e++) th.emplace_back(one, e);
   one(0);
   for (auto &t : th) t.join();
+  for (int e = 0; e < n; e++) ctx[e]->graphs = graphs[e];
   for (int e = 0; e < n; e++)
     if (rc[e] != SKKR_OK) return rc[e];
   return SKKR_OK;

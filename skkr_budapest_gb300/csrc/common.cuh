@@ -68,6 +68,13 @@ inline MatRef mref_map(zd *base, long long sk, long long sc, int ld, const int *
   return r;
 }
 
+// One process-wide lock between CUDA graph capture and the calls that may
+// synchronise the device (cudaMalloc / cudaFree / cudaDeviceSynchronize of a
+// growing work buffer): a capture on one host thread never overlaps such a
+// call on another.  Recursive: a capture that sizes a buffer takes it again.
+#include <mutex>
+std::recursive_mutex &skkr_device_mutex();
+
 // kernel launch bookkeeping (defined in capi.cu).  With SKKR_SYNC_CHECK=1 in
 // the environment every launch is followed by a device synchronisation and
 // the first failing launch site is recorded (diagnostics only).

@@ -78,6 +78,11 @@ MixedWork *mixed_create();
 void mixed_destroy(MixedWork *w);
 int mixed_error_flag(MixedWork *w);
 int *mixed_error_ptr(MixedWork *w);   // device flag set by an expired tensor-core wait
+// autotuned FP32 Gauss-Jordan layouts: force layout v - 1 for every size
+// class (v > 0), or tune afresh (v = 0); the layouts chosen so far
+int gj_tune_force(int v);
+#include <string>
+std::string gj_tune_report();
 // kernels run so far by the IF bodies of captured further Newton steps
 // (device count since mixed_resid_reset; synchronizes st)
 long long mixed_graph_kernels(MixedWork *w, cudaStream_t st);

@@ -34,6 +34,9 @@
 
 #include <algorithm>
 #include <cmath>
+#include <map>
+#include <mutex>
+#include <string>
 #include <cstring>
 #include <vector>
 
@@ -830,6 +833,7 @@ static bool use_precise(const MixedWork *w, int S) { return w->precise && S >= 6
 // device is idle (cudaFree does not wait for those streams)
 static int grow(void **p, size_t *cap, size_t bytes, bool zero) {
   if (bytes <= *cap) return 0;
+  std::lock_guard<std::recursive_mutex> lk(skkr_device_mutex());
   if (*p) {
     cudaDeviceSynchronize();
     cudaFree(*p);
@@ -846,6 +850,7 @@ static int grow(void **p, size_t *cap, size_t bytes, bool zero) {
 }
 
 MixedWork *mixed_create() {
+  std::lock_guard<std::recursive_mutex> lk(skkr_device_mutex());
   MixedWork *w = new MixedWork();
   if (cudaMalloc(&w->err, sizeof(int)) != cudaSuccess ||
       cudaMalloc(&w->dmax, sizeof(unsigned long long)) != cudaSuccess ||
@@ -902,6 +907,7 @@ long long mixed_graph_kernels(MixedWork *w, cudaStream_t st) {
 
 void mixed_destroy(MixedWork *w) {
   if (!w) return;
+  std::lock_guard<std::recursive_mutex> lk(skkr_device_mutex());
   cudaDeviceSynchronize();
   for (int i = 0; i < MIXED_SLOTS; i++) {
     void *q[] = {w->A[i].p, w->A[i].scale, w->B[i].p, w->B[i].scale};
@@ -1198,6 +1204,96 @@ bool stream_capturing(cudaStream_t st) {
   return cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusActive;
 }
 
+// ---------------------------------------------------------------------------
+// Autotuned thread layout of the FP32 Gauss-Jordan.  A size class fixes the
+// columns per thread (16 RB >= n); the rows split over TY x RA threads.  Every
+// layout gives the same inverse bit for bit (each element takes the same
+// sequence of updates, the pivot search is deterministic), so the first
+// batch of each (size class, batch size) key times the layouts once on the
+// real operands and later calls use the fastest.  A capture in progress
+// before a key is tuned takes the first layout.
+using GjLaunch = void (*)(const MatRef &, const MatRef &, int, int, const int *, unsigned, cudaStream_t);
+
+template <int TY, int RA, int RB>
+static void gj_launch(const MatRef &A, const MatRef &X, int n, int nc, const int *act, unsigned items,
+                      cudaStream_t st) {
+  k_cgj32<TY, RA, RB><<<items, TY * 16, 0, st>>>(A, X, n, nc, act);
+}
+
+struct GjClass {
+  int nmax;
+  int nv;
+  GjLaunch f[3];
+  const char *name[3];
+};
+
+static const GjClass GJ_CLASSES[3] = {
+    {32, 3, {gj_launch<16, 2, 2>, gj_launch<32, 1, 2>, gj_launch<8, 4, 2>}, {"16x2x2", "32x1x2", "8x4x2"}},
+    {64, 3, {gj_launch<16, 4, 4>, gj_launch<32, 2, 4>, gj_launch<64, 1, 4>}, {"16x4x4", "32x2x4", "64x1x4"}},
+    {128, 2, {gj_launch<32, 4, 8>, gj_launch<64, 2, 8>, nullptr}, {"32x4x8", "64x2x8", ""}},
+};
+
+namespace {
+std::mutex g_tune_mu;
+std::map<std::pair<int, int>, int> g_tuned;  // (class, batch bucket) -> layout
+int g_tune_force = 0;                         // > 0: always layout g_tune_force - 1 (tests)
+}  // namespace
+
+static GjLaunch gj_choose(int n, long long items, const MatRef &A, const MatRef &X, int nc, const int *act,
+                          cudaStream_t st) {
+  const int cls = n <= 32 ? 0 : n <= 64 ? 1 : 2;
+  const GjClass &C = GJ_CLASSES[cls];
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  if (g_tune_force > 0) return C.f[std::min(g_tune_force - 1, C.nv - 1)];
+  // batches below one wave, below four waves, and larger
+  const int bucket = items < 152 ? 0 : items < 608 ? 1 : 2;
+  auto it = g_tuned.find({cls, bucket});
+  if (it != g_tuned.end()) return C.f[it->second];
+  if (stream_capturing(st)) return C.f[0];
+  cudaEvent_t e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess) return C.f[0];
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return C.f[0];
+  }
+  int best = 0;
+  float tbest = 1e30f;
+  for (int v = 0; v < C.nv; v++) {
+    C.f[v](A, X, n, nc, act, (unsigned)items, st);  // warm (module load, caches)
+    cudaEventRecord(e0, st);
+    C.f[v](A, X, n, nc, act, (unsigned)items, st);
+    cudaEventRecord(e1, st);
+    float ms = 1e30f;
+    if (cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess &&
+        ms < tbest) {
+      tbest = ms;
+      best = v;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  g_tuned[{cls, bucket}] = best;
+  return C.f[best];
+}
+
+int gj_tune_force(int v) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune_force = v;
+  if (v == 0) g_tuned.clear();
+  return 0;
+}
+
+std::string gj_tune_report() {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  std::string r;
+  static const char *bn[3] = {"<1 wave", "<4 waves", ">=4 waves"};
+  for (auto &kv : g_tuned) {
+    const GjClass &C = GJ_CLASSES[kv.first.first];
+    r += "n<=" + std::to_string(C.nmax) + " " + bn[kv.first.second] + ": " + C.name[kv.second] + "; ";
+  }
+  return r;
+}
+
 // X = A^-1: FP32 Gauss-Jordan, then `newton` steps X += X (I - A X) with the
 // residual product at S = sres slices and the correction at S = 3.  X may be
 // A itself (`inplace`); otherwise the two must not overlap.
@@ -1231,10 +1327,9 @@ int mixed_zinv(MixedWork *w, const MatRef &A, const MatRef &X, int n, int nk, in
   const MatRef Ac = inplace ? mref(w->acopy, (long long)nc * MB, MB, n) : A;
   MatRef R = mref(w->rbuf, (long long)nc * MB, MB, n);
   if (inplace) launch_zaxpby(Ac, A, nullptr, 0, nullptr, 0, n, nk, nc, act, st);
+  const GjLaunch gj = gj_choose(n, items, Ac, X, nc, act, st);
   kstat_begin(KS_GJ, 8.0 * n * (double)n * n * (double)(act ? skkr_active_items(items) : items), st);
-  if (n <= 32) k_cgj32<16, 2, 2><<<(unsigned)items, 256, 0, st>>>(Ac, X, n, nc, act);
-  else if (n <= 64) k_cgj32<16, 4, 4><<<(unsigned)items, 256, 0, st>>>(Ac, X, n, nc, act);
-  else k_cgj32<32, 4, 8><<<(unsigned)items, 512, 0, st>>>(Ac, X, n, nc, act);
+  gj(Ac, X, n, nc, act, (unsigned)items, st);
   kstat_end(st);
   SKKR_LAUNCHED();
   // A is split once (A slot 0) for the residuals of every Newton step

@@ -88,6 +88,7 @@ def lib():
         L.skkr_gpu_set_reduce_device.argtypes = [P, P, P]
         L.skkr_gpu_set_mixed_policy.argtypes = [P, D, D, I, D]
         L.skkr_gpu_set_graphs.argtypes = [P, I]
+        L.skkr_gpu_set_newton.argtypes = [P, I]
         L.skkr_gpu_stage_kambe.argtypes = [P, P]
         L.skkr_gpu_cpacoord_many.argtypes = [I, P, P, P]
         L.skkr_gpu_gjinv_batch.argtypes = [I, I, P, I]
@@ -436,6 +437,17 @@ def zgemm_batch(a, b, precision="fp64", slices=5):
     _check(L.skkr_gpu_zgemm_batch({"fp64": FP64, "mixed": MIXED}[precision], slices, n, nb, _p(A), _p(B),
                                   _p(Cm), n), "skkr_gpu_zgemm_batch")
     return uncm(Cm)
+
+
+def autotune(force=None, report=False):
+    """The Gauss-Jordan autotuner (skkr_gpu_autotune): force a layout (1..3),
+    reset (0), and/or return the choices made so far."""
+    L = lib()
+    L.skkr_gpu_autotune.argtypes = [I, P, I]
+    buf = C.create_string_buffer(512) if report else None
+    _check(L.skkr_gpu_autotune(0 if force is None else int(force), buf, 512 if report else 0),
+           "skkr_gpu_autotune")
+    return buf.value.decode() if report else None
 
 
 def zinv_batch(a, precision="fp64", newton=2):

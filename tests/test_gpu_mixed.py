@@ -120,3 +120,23 @@ def test_mixed_cpacoord_cpa_alloy():
     spec.lmax = 2
     g, o = _compare_mixed(W.energy_problem(spec, 14))
     assert g["cpa_iterations"] > 1
+
+
+@pytest.mark.parametrize("n", [20, 54, 100])
+def test_gauss_jordan_layouts_are_bit_identical(n):
+    """The autotuner's thread layouts of the FP32 Gauss-Jordan give the same
+    inverse bit for bit, so the choice it makes cannot change a result."""
+    rng = np.random.default_rng(n)
+    a = rng.normal(size=(40, n, n)) + 1j * rng.normal(size=(40, n, n)) + 3 * np.eye(n)
+    outs = []
+    try:
+        for force in (1, 2, 3):
+            native.autotune(force)
+            outs.append(native.zinv_batch(a, "mixed")[0])
+    finally:
+        native.autotune(0)
+    for o in outs[1:]:
+        assert np.array_equal(o, outs[0])
+    tuned = native.zinv_batch(a, "mixed")[0]
+    assert np.array_equal(tuned, outs[0])
+    assert "n<=" in native.autotune(report=True)
