@@ -268,6 +268,14 @@ typedef struct {
   int ld;
 } skkr_energy_args;
 
+/* A list of energies of one system in one call (the contour loop of
+ * rsp-scf/skkr.f:389-486 around its cpacoord call at :439): energy e runs
+ * args[e] as skkr_gpu_cpacoord would (SKKR_BDG contexts: as
+ * skkr_gpu_cpacoord_bdg), in order on the context's stream, each with its
+ * decimation graphs; st[e] (st may be NULL) receives its status.  Every
+ * energy runs even after one fails; returns the first nonzero code. */
+int skkr_gpu_contour(skkr_ctx *ctx, int ne, const skkr_energy_args *args, skkr_status *st);
+
 /* Several systems in one call (e.g. interfaces of different lmax / PL size):
  * energy args[e] runs on context ctx[e] (n distinct contexts, each of its
  * own system) concurrently, each context on its own stream driven by its own

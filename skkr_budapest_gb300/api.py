@@ -345,6 +345,44 @@ def cpacoord_many(eps, precision="fp64", check=True, slices=0, contexts=None):
                 c.close()
 
 
+def contour(eps, precision="fp64", check=True, slices=0, context=None):
+    """Several energies of one system in one call (skkr_gpu_contour), in
+    order on one context.  Returns the per-energy results of
+    Context.cpacoord."""
+    own = context is None
+    ctx = Context.for_problem(eps[0], precision, slices=slices) if own else context
+    try:
+        keep, outs, args = [], [], (N.EnergyArgs * len(eps))()
+        p = N._p
+        for i, ep in enumerate(eps):
+            rt, a = ctx._host_inputs(ep, None)
+            n, lk = ctx.nintfc, ctx.lk
+            out = {k: np.zeros((n, lk, lk), np.complex128) for k in ("tauc", "taua", "taub")}
+            keep.append((rt, a))
+            outs.append(out)
+            fach = complex(ep.fach) if ep.irel == 2 else 0j
+            args[i] = N.EnergyArgs(ep.ce.real, ep.ce.imag, ep.fac.real, ep.fac.imag, fach.real, fach.imag,
+                                   rt.ptr(), len(a["xk"]), p(a["xk"]), p(a["wk"]), p(a["lg"]), p(a["rg"]),
+                                   p(a["conc"]), p(a["tl"]), p(a["tr"]), p(a["ti"]), p(a["ta"]), p(a["tb"]),
+                                   p(out["tauc"]), p(out["taua"]), p(out["taub"]), lk)
+        sts = (N.Status * len(eps))()
+        rc = N.lib().skkr_gpu_contour(ctx.h, len(eps), C.cast(args, C.c_void_p), C.cast(sts, C.c_void_p))
+        if check:
+            N._check(rc, "skkr_gpu_contour")
+        res = []
+        for (rt, a), out, st in zip(keep, outs, sts):
+            r = {k: N.uncm(v) for k, v in out.items()}
+            r["tminv"] = N.uncm(a["ti"])
+            r.update(status=st.code, cpa_iterations=st.cpa_iterations, cpa_error=st.cpa_error,
+                     max_dec_iters=st.max_dec_iters, dec_iters_total=st.dec_iters_total,
+                     gpu_launches=st.gpu_launches, run_ms=st.run_ms, alg_flops=st.alg_flops)
+            res.append(r)
+        return res
+    finally:
+        if own:
+            ctx.close()
+
+
 def cpacoord(ep, precision="fp64", tminv=None, check=True, slices=0):
     """One energy through the GPU path (creates a context for the call)."""
     ctx = Context.for_problem(ep, precision, slices=slices)

@@ -1991,6 +1991,32 @@ extern "C" int skkr_gpu_cpacoord_bdg(skkr_ctx *c, double ce_re, double ce_im, do
                            tminvr, tminv, tminva, tminvb, tauc, taua, taub, ld, status);
 }
 
+// A list of energies of one system in one call (the contour loop of
+// rsp-scf/skkr.f:389-486 around cpacoord, :439): energy e runs args[e] as
+// skkr_gpu_cpacoord would (BdG contexts: skkr_gpu_cpacoord_bdg), one after
+// the other on the context's stream, each with its decimation graphs; st[e]
+// receives its status.  Every energy runs even after one fails; the first
+// nonzero code is returned.
+extern "C" int skkr_gpu_contour(skkr_ctx *c, int ne, const skkr_energy_args *args, skkr_status *st) {
+  if (!c || ne < 1 || !args) return SKKR_ERR_ARG;
+  int first = SKKR_OK;
+  for (int e = 0; e < ne; e++) {
+    const skkr_energy_args &a = args[e];
+    skkr_status *s = st ? st + e : nullptr;
+    int rc;
+    if (c->sz.mode == SKKR_BDG)
+      rc = skkr_gpu_cpacoord_bdg(c, a.ce_re, a.ce_im, a.fac_re, a.fac_im, a.fach_re, a.fach_im, a.rt, a.nk, a.xk,
+                                 a.wk, a.lg, a.rg, a.conc, a.tminvl, a.tminvr, a.tminv, a.tminva, a.tminvb, a.tauc,
+                                 a.taua, a.taub, a.ld, s);
+    else
+      rc = skkr_gpu_cpacoord(c, a.ce_re, a.ce_im, a.fac_re, a.fac_im, a.rt, a.nk, a.xk, a.wk, a.lg, a.rg, a.conc,
+                             a.tminvl, a.tminvr, a.tminv, a.tminva, a.tminvb, a.tauc, a.taua, a.taub, a.ld, s);
+    if (s && rc != SKKR_OK) s->code = rc;
+    if (rc != SKKR_OK && first == SKKR_OK) first = rc;
+  }
+  return first;
+}
+
 // Several systems at once: context e runs args[e] on its own stream from its
 // own host thread, so the kernels of a small system fill the SMs a large one
 // leaves idle.  The contexts must be distinct.

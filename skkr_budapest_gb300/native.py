@@ -91,6 +91,7 @@ def lib():
         L.skkr_gpu_set_newton.argtypes = [P, I]
         L.skkr_gpu_stage_kambe.argtypes = [P, P]
         L.skkr_gpu_cpacoord_many.argtypes = [I, P, P, P]
+        L.skkr_gpu_contour.argtypes = [P, I, P, P]
         L.skkr_gpu_gjinv_batch.argtypes = [I, I, P, I]
         L.skkr_gpu_surfgf_batch.argtypes = [I, I, P, P, P, P, I, I, D, P, P]
         L.skkr_gpu_gk.argtypes = [P, I, I, P, P]

@@ -2,7 +2,8 @@
 PL4 lmax=3 interface, the non-relativistic PL2 lmax=2 interface and the
 relativistic PL3 lmax=2 interface run concurrently (one context, stream and
 host thread each) and give the results of the single calls; with kernel-class
-timing on at the same time."""
+timing on at the same time.  Several energies of one system in one call
+(skkr_gpu_contour) equal their single calls."""
 import numpy as np
 import pytest
 
@@ -41,3 +42,15 @@ def test_many_rejects_repeated_context():
             api.cpacoord_many(eps, contexts=[ctx, ctx])
     finally:
         ctx.close()
+
+
+def test_contour_call_equals_single_calls():
+    """skkr_gpu_contour: several energies of one system in one call, each
+    equal to its own skkr_gpu_cpacoord call."""
+    spec = W.rel_bcc(nsets=[3] * 24)
+    eps = [W.energy_problem(spec, ie) for ie in (2, 14, 20)]
+    many = api.contour(eps, precision="mixed")
+    for ep, r in zip(eps, many):
+        one = api.cpacoord(ep, precision="mixed")
+        assert r["status"] == one["status"] == 0
+        assert np.array_equal(r["tauc"], one["tauc"])
