@@ -133,7 +133,9 @@ int skkr_gpu_destroy(skkr_ctx *ctx);
  * point (an isolated peak), is recomputed in FP64 (0 = off).  Inverses
  * whose Newton residual is above 1e-6 after the standard steps take up to
  * four further steps while it stays below 1/2; those still above 1e-6 are
- * always redone in FP64. */
+ * always redone in FP64.  An energy whose decimation runs in FP64 on blocks
+ * above 128 rows (the split inverse's limit) runs wholly in FP64: splitting
+ * the tau2d products alone does not repay the splits and the peak redo. */
 int skkr_gpu_set_mixed_policy(skkr_ctx *ctx, double dec_fp64_im, double near_im, int slices_near,
                               double dominant_frac);
 
@@ -376,6 +378,14 @@ int skkr_gpu_mlp16_grad(int nlayer, const int *dims, const float *params, int n,
 int skkr_gpu_mlp16_train(int nlayer, const int *dims, float *params, int n, const float *x, const float *y,
                          const unsigned char *rows, int epochs, float lr, float weight_decay, int eval_every,
                          float *train_loss, float *best, float *best_params);
+/* The same network kept on the device for repeated inference (the warm start
+ * of one energy runs it on a few rows): load uploads the parameters once and
+ * sizes the buffers for up to maxrows rows; infer runs n <= maxrows rows on
+ * the handle's own stream and returns when y is written; free releases it. */
+typedef struct skkr_mlp16 skkr_mlp16;
+int skkr_gpu_mlp16_load(int nlayer, const int *dims, const float *params, int maxrows, skkr_mlp16 **net);
+int skkr_gpu_mlp16_infer(skkr_mlp16 *net, int n, const float *x, float *y);
+int skkr_gpu_mlp16_free(skkr_mlp16 *net);
 
 /* The reference's k-space structure constants (main/kamstr.f:20-392): the
  * Kambe lattice sums D_L(k, s) of outgoing spherical waves over a 2D lattice,

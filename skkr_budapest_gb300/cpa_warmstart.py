@@ -124,7 +124,7 @@ def invariant_projector(ep):
     """P(m) = (1/ng) sum_g R_g m L_g: the point-group average under which the
     k-summed tau and hence the converged m_c are invariant."""
     lg, rg = np.asarray(ep.lg), np.asarray(ep.rg)
-    return lambda m: np.einsum("gij,jk,gkl->il", rg, m, lg) / len(lg)
+    return lambda m: (rg @ m @ lg).mean(axis=0)
 
 
 def free_elements(ep):
@@ -199,7 +199,9 @@ class Model:
         h = np.float32((np.atleast_2d(x) - self.xmean) / self.xstd)
         if device == "gpu":
             from . import native as N
-            y = N.mlp16_forward(self.layers, h)
+            if getattr(self, "_net", None) is None or len(h) > self._net.maxrows:
+                self._net = N.Mlp16Net(self.layers, max(64, len(h)))
+            y = self._net(h)
         else:
             y = h
             for i, (w, b) in enumerate(self.layers):

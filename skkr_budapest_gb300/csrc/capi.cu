@@ -829,7 +829,13 @@ static int eng_inv(skkr_ctx *c, bool mixed, const MatRef &A, const MatRef &X, bo
 static bool use_mixed(const skkr_ctx *c, bool decimation) {
   if (c->sz.precision != SKKR_MIXED || c->force_fp64) return false;
   // decimation near the real axis stays in FP64 (default: within 2e-4 Ry)
-  if (decimation && std::fabs(c->ce.y) < c->dec_fp64_im) return false;
+  const bool dec_fp64 = std::fabs(c->ce.y) < c->dec_fp64_im;
+  if (decimation && dec_fp64) return false;
+  // with the decimation in FP64 and blocks above the split inverse's 128
+  // rows, only the tau2d products would be split: the splitting and the FP64
+  // redo of the integrand's peaks cost more than they save (BdG n_PL = 256 at
+  // Im E = 1e-4 Ry ran at 0.74 of the FP64 rate), so the energy runs in FP64
+  if (dec_fp64 && c->n > 128) return false;
   return true;
 }
 
@@ -1863,10 +1869,10 @@ extern "C" int skkr_gpu_run(skkr_ctx *c, skkr_status *status) {
       CKR(run_tau2d(c, k0, nkc, icls));
       c->alg_units += (7.0 * c->nprc - 6.0) * nkc * (double)ncls;  // tau2d.f per item
       launch_ksum(c->tauk.as<zd>(), nkc, (long long)ncls * ni * lk2, c->S.as<zd>(), k0 > 0, st);
-      if (c->sz.precision == SKKR_MIXED && c->dominant_frac > 0.0)
+      if (use_mixed(c, false) && c->dominant_frac > 0.0)
         launch_knorm(c->tauk.as<zd>(), nkc, (long long)ncls * ni * lk2, c->knorm.as<double>() + k0, st);
     }
-    if (!c->err_code && c->sz.precision == SKKR_MIXED && c->dominant_frac > 0.0)
+    if (!c->err_code && use_mixed(c, false) && c->dominant_frac > 0.0)
       CKR(redo_dominant_k(c, itcpa, lcls, rcls, icls));
     if (c->err_code) {
       if (c->red_fn || c->red_dev_fn) reduce_tauc(c, true);  // tell the other ranks before returning

@@ -461,3 +461,54 @@ extern "C" int skkr_gpu_mlp16_train(int nlayer, const int *dims, float *params, 
   }
   return SKKR_OK;
 }
+
+// ---- a network kept on the device for repeated inference ------------------
+// (the warm start runs it on a few rows per energy: the parameters are
+// uploaded once, inference is two small copies and one launch per layer)
+struct skkr_mlp16 {
+  M16 m;
+  int maxrows = 0;
+  cudaStream_t st = nullptr;
+};
+
+extern "C" int skkr_gpu_mlp16_load(int nlayer, const int *dims, const float *params, int maxrows, skkr_mlp16 **out) {
+  if (!params || !out || maxrows < 1) return SKKR_ERR_ARG;
+  skkr_mlp16 *h = new skkr_mlp16();
+  int rc = m16_sizes(nlayer, dims, maxrows, h->m);
+  if (rc == SKKR_OK) {
+    std::vector<float> zero((size_t)maxrows * h->m.d[0], 0.f);
+    rc = m16_alloc(h->m, params, zero.data(), nullptr, nullptr);
+  }
+  if (rc == SKKR_OK && cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess) rc = SKKR_ERR_CUDA;
+  if (rc == SKKR_OK && cudaDeviceSynchronize() != cudaSuccess) rc = SKKR_ERR_CUDA;
+  if (rc != SKKR_OK) {
+    if (h->st) cudaStreamDestroy(h->st);
+    delete h;
+    return rc;
+  }
+  h->maxrows = maxrows;
+  *out = h;
+  return SKKR_OK;
+}
+
+extern "C" int skkr_gpu_mlp16_infer(skkr_mlp16 *h, int n, const float *x, float *y) {
+  if (!h || !x || !y || n < 1 || n > h->maxrows) return SKKR_ERR_ARG;
+  M16 &m = h->m;
+  const int n0 = m.n;
+  m.n = n;  // the first n rows of the buffers sized for maxrows
+  M_CK(cudaMemcpyAsync(m.A[0], x, (size_t)n * m.d[0] * sizeof(float), cudaMemcpyHostToDevice, h->st));
+  m16_forward(m, h->st);
+  M_CK(cudaMemcpyAsync(y, m.A[m.nl], (size_t)n * m.d[m.nl] * sizeof(float), cudaMemcpyDeviceToHost, h->st));
+  m.n = n0;
+  M_CK(cudaStreamSynchronize(h->st));
+  M_CK(cudaGetLastError());
+  return SKKR_OK;
+}
+
+extern "C" int skkr_gpu_mlp16_free(skkr_mlp16 *h) {
+  if (!h) return SKKR_OK;
+  cudaStreamSynchronize(h->st);
+  cudaStreamDestroy(h->st);
+  delete h;  // M16 frees its device buffers
+  return SKKR_OK;
+}

@@ -276,6 +276,41 @@ def _mlp16_lib():
     return L
 
 
+class Mlp16Net:
+    """A BF16-weight network kept on the device for repeated inference
+    (skkr_gpu_mlp16_load / infer / free)."""
+
+    def __init__(self, layers, maxrows=64):
+        L = _mlp16_lib()
+        L.skkr_gpu_mlp16_load.argtypes = [I, P, P, I, P]
+        L.skkr_gpu_mlp16_infer.argtypes = [P, I, P, P]
+        L.skkr_gpu_mlp16_free.argtypes = [P]
+        self.dims, params = _mlp16_args(layers)
+        self.maxrows = int(maxrows)
+        h = C.c_void_p()
+        _check(L.skkr_gpu_mlp16_load(len(layers), _p(self.dims), _p(params), self.maxrows,
+                                     C.cast(C.pointer(h), C.c_void_p)), "skkr_gpu_mlp16_load")
+        self.h = h
+        self.L = L
+
+    def __call__(self, x):
+        x = np.ascontiguousarray(x, np.float32)
+        y = np.zeros((len(x), self.dims[-1]), np.float32)
+        _check(self.L.skkr_gpu_mlp16_infer(self.h, len(x), _p(x), _p(y)), "skkr_gpu_mlp16_infer")
+        return y
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.skkr_gpu_mlp16_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def mlp16_forward(layers, x):
     """Device forward of the BF16-weight network (skkr_gpu_mlp16_forward):
     FP32 master layers in, FP32 outputs."""

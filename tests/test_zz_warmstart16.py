@@ -64,3 +64,19 @@ def test_training_lowers_the_loss_like_the_reference():
         [(np.float64(w), np.float64(b)) for w, b in layers], g)
     for (w, b), (rw, rb) in zip(f1, ref):
         assert np.abs(w - rw).max() < 1e-5 and np.abs(b - rb).max() < 1e-5
+
+
+def test_device_resident_network_equals_the_one_call_forward():
+    """skkr_gpu_mlp16_load / infer: parameters uploaded once, then row blocks
+    of any size up to the handle's limit, equal to the one-call forward."""
+    rng = np.random.default_rng(6)
+    layers = _net([30, 64, 64, 10], 3)
+    net = N.Mlp16Net(layers, maxrows=16)
+    try:
+        for n in (1, 4, 16):
+            x = np.float32(rng.normal(size=(n, 30)))
+            assert np.array_equal(net(x), N.mlp16_forward(layers, x))
+        with pytest.raises(N.SkkrError):
+            net(np.zeros((17, 30), np.float32))
+    finally:
+        net.close()
