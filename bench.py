@@ -465,6 +465,7 @@ def run_ours(args, rank, ws):
     # kernel shares: the same steps again with per-launch events (not timed)
     rs = timed_steps(ctx, order, slot_of, eps, args, flush, stats=True)
     roof = roofline(rs["ks"], args.precision, r["alg"], r["t_dev"])
+    roof["gj_layouts"] = N.autotune(report=True)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
             "scaling": "strong" if split_k else "weak", "vs_baseline": None,
@@ -665,7 +666,11 @@ def run_c4(args):
                        "so_split": fam.so_split, "cpatol": eps[0].cpatol,
                        "timing": "host wall clock around whole calls (host buffers), surrogate included"},
             "paths": {k: {"value": rate[k], "cpa_iterations": out[k]["its"], "device_ms": round(out[k]["dev"], 1),
-                          "max_rel_err_tau_vs_fp64": err.get(k)} for k in out},
+                          # the learned start converges to cpatol from another
+                          # point: its difference from the ATA-started FP64 run
+                          # is the spread of converged solutions, not rounding
+                          ("max_rel_diff_tau_vs_fp64_from_ata" if k == "mixed_mlp" else
+                           "max_rel_err_tau_vs_fp64"): err.get(k)} for k in out},
             "speedup_vs_fp64": rate["mixed_mlp"] / rate["fp64"],
             "cpa_iterations_learned_vs_ata": out["mixed_mlp"]["its"] / max(1, out["mixed"]["its"]),
             "e2e": {"value": rate["mixed_mlp"], "unit": UNIT, "h2d_bytes_per_step": out["mixed_mlp"]["h2d"] // args.steps,

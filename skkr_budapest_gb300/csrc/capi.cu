@@ -1810,9 +1810,10 @@ extern "C" int skkr_gpu_run(skkr_ctx *c, skkr_status *status) {
     const int ncmax = 2 * c->ngeff;
     double per_k = (double)MB * sizeof(zd) * (c->nmat + 9.0 * ncmax + (5.0 * c->nprc + 1) * c->ngeff) +
                    (double)c->ngeff * ni * lk2 * sizeof(zd);
-    if (c->sz.precision == SKKR_MIXED) {
+    if (use_mixed(c, false)) {
       // BF16 slice staging: up to MIXED_SLOTS operands per side, S slices of
-      // the padded real embedding (A: 128-row tiles, B: 96-row tiles, K: 2n)
+      // the padded real embedding (A: 128-row tiles, B: 96-row tiles, K: 2n);
+      // an energy that runs wholly in FP64 stages nothing
       const double Mp = 128.0 * ((n + 127) / 128), Np = 96.0 * ((2 * n + 95) / 96),
                    Kp = 32.0 * ((2 * n + 31) / 32);
       per_k += (double)ncmax * MIXED_SLOTS * c->slices_res * (Mp + Np) * Kp * 2.0;
