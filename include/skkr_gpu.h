@@ -462,6 +462,30 @@ int skkr_gpu_stage_kambe(skkr_ctx *ctx, const skkr_kambe_form *kf);
 int skkr_gpu_layer_dos(int mode, int lmax, int nlay, const double *tau, int ld, const double *F,
                        const double *G, int para, double *zmom, double *zdos_l);
 
+/* Bloch spectral function of nlay (<= 16) interface layers at nk k points
+ * (replaces skkr_dbogo_bsf/rsp-scf/bsf.f:2-437 with gf.f:1-103 at reg =
+ * .true., pairing.f and moment.f at lambda = 0; the non-BdG modes keep its
+ * bsfe).  All taus are physical, nd x nd column-major (nd of phystau's
+ * mode): tauk [nk][nlay] the coherent tau of each k point, tauc / taua /
+ * taub [nlay] the k-integrated coherent and component taus of the CPA
+ * (bsf.f's tau_kint, taua_kint, taub_kint).  A layer with 1 - conc > 1e-6
+ * takes the CPA form: A0 = sum_a c_a R_aa tau_a and A1 = sum_ab c_a c_b
+ * R_ab D_a (tau(k) - tau_c) D~_b, D_a = tau_a tau_c^-1, D~_b = tau_c^-1 tau_b
+ * (species a = A, B with weights conc, 1 - conc); other layers R_AA tau(k).
+ * R are the radial overlaps of the right solution of species a with the
+ * left solution of species b: F [nlay][a][b][nd] on the basis diagonal
+ * (BdG: electron then hole half) and, for BdG, Feh [nlay][a][b][nde][nde]
+ * (column-major, nde = nd / 2) on the electron-hole block, contracted with
+ * the four pairing operators pair [4][nde][nde] (singlet, T0, T-up,
+ * T-down of pairing.f).  out [nk][nlay][6] = -1/pi Im of: the electron
+ * diagonal sum (bsfe), the hole diagonal sum (bsfh), tr(P_x G_eh) for the
+ * four operators (bsfeh, bsfhe, bsfteh, bsfthe); zero where a mode has no
+ * such part; doubled for para != 0 in the lm basis.  Feh / pair may be
+ * NULL outside BdG. */
+int skkr_gpu_bsf(int mode, int lmax, int nk, int nlay, const double *conc, const double *tauk,
+                 const double *tauc, const double *taua, const double *taub, const double *F,
+                 const double *Feh, const double *pair, int para, double *out);
+
 /* Lower-level batched kernels, exported for tests. */
 /* In-place inverses of `batch` n x n matrices, n <= 512 (main/gjinv.f:2-59, column pivoting). */
 int skkr_gpu_gjinv_batch(int n, int batch, double *a, int ld);

@@ -392,6 +392,59 @@ def cpacoord(ep, precision="fp64", tminv=None, check=True, slices=0):
         ctx.close()
 
 
+BSF_NAMES = ("bsfe", "bsfh", "bsfeh", "bsfhe", "bsfteh", "bsfthe")
+
+
+def bsf(ep, kpts, cpa=None, para=False, precision="fp64"):
+    """Bloch spectral function of the interface layers at the k points kpts
+    ((nk, 2), a.u.), CPA and BdG forms included, as the BdG code's spectral
+    mode does (skkr_dbogo_bsf/rsp-scf/skkr.f:688-712 and 1076-1090: the
+    converged CPA of the energy is read back by tcpa_in, cpacoord runs per k
+    point without CPA iterations, then bsf.f).  `cpa` is the result of
+    Context.cpacoord for ep over its own k mesh (run here when None): its
+    coherent t^-1 m_c and k-integrated tau_c, tau_A, tau_B.  Each k point is a
+    one-point k loop with the identity alone on m_c for every layer (no alloy,
+    so no CPA iteration); every tau goes through phystau on the device
+    (tau_c, tau(k) with m_c; tau_A, tau_B with their species' t^-1); then
+    skkr_gpu_bsf with the radial overlaps of the model's wells
+    (synth.bsf_radial) and, for BdG, the pairing operators
+    (synth.pairing_kmy).  Returns {name: [nk, nintfc]} for bsfe and, for BdG,
+    bsfh, bsfeh, bsfhe, bsfteh, bsfthe (bsf.f's output names)."""
+    import dataclasses
+    from . import synth as S
+    if cpa is None:
+        cpa = cpacoord(ep, precision)
+    mc = np.asarray(cpa["tminv"])
+    layers = range(ep.nintfc)
+
+    def phys(tau, tinv):
+        return np.array([N.phystau(tau[li], tinv[li], ep.alpha[li], ep.lmax, ep.irel) for li in layers])
+
+    tc = phys(cpa["tauc"], mc)
+    ta = phys(cpa["taua"], ep.tminva)
+    tb = phys(cpa["taub"], ep.tminvb)
+    one = dataclasses.replace(ep, lg=ep.lg[:1], rg=ep.rg[:1], conc=np.ones(ep.nintfc), tminv=mc.copy(),
+                              tminva=mc.copy(), tminvb=mc.copy())
+    kpts = np.asarray(kpts, float).reshape(-1, 2)
+    nd = ep.lkmax
+    tk = np.zeros((len(kpts), ep.nintfc, nd, nd), complex)
+    ctx = Context.for_problem(one, precision)
+    try:
+        for i, k in enumerate(kpts):
+            r = ctx.cpacoord(one.with_k(k[None, :], np.ones(1)))
+            tk[i] = phys(r["tauc"], mc)
+    finally:
+        ctx.close()
+    F, Feh = S.bsf_radial(ep)
+    pair = None
+    if ep.irel == 2:
+        P = S.pairing_kmy(ep.lmax)
+        pair = np.array([P[name] for name in ("singlet", "t0", "tup", "tdown")])
+    out = N.bsf(ep.irel, ep.lmax, ep.conc, tk, tc, ta, tb, F, Feh, pair, para)
+    names = BSF_NAMES if ep.irel == 2 else BSF_NAMES[:1]
+    return {name: out[:, :, i] for i, name in enumerate(names)}
+
+
 def layer_dos(ep, tau, which="a", para=False):
     """Layer DOS of the interface layers of one energy, as locquant.f does
     after cpacoord: screened -> physical tau (phystau) per layer, then
@@ -446,13 +499,12 @@ def bloch_spectral(ep, kpts, which="a", para=False):
     k-independent single-site term of the DOS is not part of it.  Each k
     point is a one-point k loop of cpacoord with the identity alone, then
     phystau and the layer-DOS kernel with G = 0, all on the device.  Returns
-    (A_l [nk, nintfc, lmax+1], A_L [nk, nintfc, lk]).  The CPA form (the A0
-    and A1 terms of bsf.f for alloy layers) needs the radial integrals across
-    the two species and is not built."""
+    (A_l [nk, nintfc, lmax+1], A_L [nk, nintfc, lk]).  Alloy layers need
+    the CPA form of bsf.f (its A0 and A1 terms): `bsf` below."""
     import dataclasses
     from . import synth as S
     if any(1e-6 < c < 1 - 1e-6 for c in ep.conc):
-        raise ValueError("bloch_spectral: alloy layers need the CPA form of bsf.f (not built)")
+        raise ValueError("bloch_spectral: alloy layers need the CPA form of bsf.f (api.bsf)")
     one = dataclasses.replace(ep, lg=ep.lg[:1], rg=ep.rg[:1])
     F, _ = S.layer_dos_inputs(ep, which)
     zero = np.zeros_like(F)

@@ -2438,6 +2438,100 @@ extern "C" int skkr_gpu_layer_dos(int mode, int lmax, int nlay, const double *ta
 }
 
 // ---------------------------------------------------------------------------
+// Bloch spectral function (skkr_dbogo_bsf/rsp-scf/bsf.f:2-437 with gf.f,
+// pairing.f and moment.f at lambda = 0) of nlay layers at nk k points.  Per
+// CPA layer (1 - conc > 1e-6): tau_c^-1, D_a = tau_a tau_c^-1 and
+// D~_a = tau_c^-1 tau_a once; per k point tau(k) - tau_c and the four
+// D_a (tau(k) - tau_c) D~_b; then k_bsf_reduce.  Layers without CPA use
+// tau(k) itself.  Chunks of k points keep the work buffers bounded.
+extern "C" int skkr_gpu_bsf(int mode, int lmax, int nk, int nlay, const double *conc, const double *tauk,
+                            const double *tauc, const double *taua, const double *taub, const double *F,
+                            const double *Feh, const double *pair, int para, double *out) {
+  if (!conc || !tauk || !tauc || !taua || !taub || !F || !out || nk < 1 || nlay < 1 || nlay > SKKR_MAPN)
+    return SKKR_ERR_ARG;
+  int nd, nal;
+  std::vector<int> lof;
+  CKR(phys_basis(mode, lmax, 0x7fffffff, &nd, &nal, lof));
+  const int bdg = mode == SKKR_BDG, nde = bdg ? nd / 2 : nd;
+  if (bdg && (!Feh || !pair)) return SKKR_ERR_ARG;
+  const long long MB = (long long)nd * nd, NE2 = (long long)nde * nde;
+  double fac = -1.0 / 3.14159265358979323846;
+  if (para && mode == SKKR_NONREL) fac *= 2.0;
+  std::vector<int> cpa(nlay);
+  for (int l = 0; l < nlay; l++) cpa[l] = (1.0 - conc[l]) > 1.0e-6;
+  // k points per chunk: grid.y of the batched kernels holds kc * nlay, and the
+  // seven per-k matrices of a chunk stay within 2 GB
+  const long long per_k = 7LL * nlay * MB * (long long)sizeof(zd);
+  const int kc = (int)std::max(1LL, std::min<long long>({(long long)nk, 65535LL / nlay, (2LL << 30) / per_k}));
+  Scoped s;
+  zd *TC, *TA, *TB, *TCI, *D4, *Fd, *Fe = nullptr, *Pd = nullptr, *DEL, *T2, *M4;
+  double *Cd, *Od;
+  int *Cp, *Ak;
+  CKR(s.alloc(&TC, nlay * MB));
+  CKR(s.alloc(&TA, nlay * MB));
+  CKR(s.alloc(&TB, nlay * MB));
+  CKR(s.alloc(&TCI, nlay * MB));
+  CKR(s.alloc(&D4, 4 * nlay * MB));  // D_A, D_B, D~_A, D~_B
+  CKR(s.alloc(&Fd, 4LL * nlay * nd));
+  CKR(s.alloc(&DEL, (long long)kc * nlay * MB));
+  CKR(s.alloc(&T2, 2LL * kc * nlay * MB));
+  CKR(s.alloc(&M4, 4LL * kc * nlay * MB));
+  CKR(s.alloc(&Cd, nlay));
+  CKR(s.alloc(&Od, (long long)kc * nlay * 6));
+  CKR(s.alloc(&Cp, nlay));
+  CKR(s.alloc(&Ak, (long long)kc * nlay));
+  CKR(upload_mats(TC, tauc, nlay, nd, nd));
+  CKR(upload_mats(TA, taua, nlay, nd, nd));
+  CKR(upload_mats(TB, taub, nlay, nd, nd));
+  CK(cudaMemcpy(Fd, F, 4LL * nlay * nd * sizeof(zd), cudaMemcpyHostToDevice));
+  if (bdg) {
+    CKR(s.alloc(&Fe, 4LL * nlay * NE2));
+    CKR(s.alloc(&Pd, 4 * NE2));
+    CK(cudaMemcpy(Fe, Feh, 4LL * nlay * NE2 * sizeof(zd), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(Pd, pair, 4 * NE2 * sizeof(zd), cudaMemcpyHostToDevice));
+  }
+  CK(cudaMemcpy(Cd, conc, nlay * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(Cp, cpa.data(), nlay * sizeof(int), cudaMemcpyHostToDevice));
+  {
+    std::vector<int> ak((size_t)kc * nlay);
+    for (size_t q = 0; q < ak.size(); q++) ak[q] = cpa[q % nlay];
+    CK(cudaMemcpy(Ak, ak.data(), ak.size() * sizeof(int), cudaMemcpyHostToDevice));
+  }
+  // per layer (items k = 0, c = layer): tau_c^-1 and the four D matrices
+  auto lay = [&](zd *b) { return mref(b, 0, MB, nd); };
+  launch_zaxpby(lay(TCI), lay(TC), nullptr, 0, nullptr, 0, nd, 1, nlay, Cp, 0);
+  launch_zgj(lay(TCI), nd, 1, nlay, Cp, 0);
+  zd *DA = D4, *DB = D4 + nlay * MB, *DAp = D4 + 2 * nlay * MB, *DBp = D4 + 3 * nlay * MB;
+  launch_zgemm(0, lay(TA), lay(TCI), lay(DA), lay(DA), lay(DA), nd, nd, nd, 1, nlay, Cp, 0);
+  launch_zgemm(0, lay(TB), lay(TCI), lay(DB), lay(DB), lay(DB), nd, nd, nd, 1, nlay, Cp, 0);
+  launch_zgemm(0, lay(TCI), lay(TA), lay(DAp), lay(DAp), lay(DAp), nd, nd, nd, 1, nlay, Cp, 0);
+  launch_zgemm(0, lay(TCI), lay(TB), lay(DBp), lay(DBp), lay(DBp), nd, nd, nd, 1, nlay, Cp, 0);
+  const long long msec = (long long)kc * nlay * MB;
+  for (int k0 = 0; k0 < nk; k0 += kc) {
+    const int m = std::min(kc, nk - k0);
+    // items (k, layer) of this chunk
+    auto per = [&](zd *b) { return mref(b, nlay * MB, MB, nd); };
+    CKR(upload_mats(DEL, tauk + (size_t)k0 * nlay * MB * 2, m * nlay, nd, nd));
+    MatRef tc = lay(TC);
+    launch_zaxpby(per(DEL), per(DEL), &tc, -1.0, nullptr, 0, nd, m, nlay, Ak, 0);
+    zd *TAk = T2, *TBk = T2 + msec;
+    launch_zgemm(0, lay(DA), per(DEL), per(TAk), per(TAk), per(TAk), nd, nd, nd, m, nlay, Ak, 0);
+    launch_zgemm(0, lay(DB), per(DEL), per(TBk), per(TBk), per(TBk), nd, nd, nd, m, nlay, Ak, 0);
+    for (int a = 0; a < 2; a++)
+      for (int b = 0; b < 2; b++) {
+        zd *Mab = M4 + (a * 2 + b) * msec;
+        launch_zgemm(0, per(a ? TBk : TAk), lay(b ? DBp : DAp), per(Mab), per(Mab), per(Mab), nd, nd, nd, m,
+                     nlay, Ak, 0);
+      }
+    launch_bsf_reduce(nd, nde, bdg, nlay, m * nlay, Cd, Cp, DEL, M4, msec, TA, TB, Fd, Fe, Pd, fac, Od, 0);
+    CK(cudaDeviceSynchronize());
+    CK(cudaGetLastError());
+    CK(cudaMemcpy(out + (size_t)k0 * nlay * 6, Od, (size_t)m * nlay * 6 * sizeof(double), cudaMemcpyDeviceToHost));
+  }
+  return SKKR_OK;
+}
+
+// ---------------------------------------------------------------------------
 // batched complex products and inverses on host arrays (tests, benchmarks)
 extern "C" int skkr_gpu_zgemm_batch(int precision, int slices, int n, int batch, const double *a,
                                     const double *b, double *cmat, int ld) {

@@ -69,6 +69,10 @@ void launch_pair_sum(const zd *tauf, int nkc, int nc, int nintfc, int lk, const 
 // CPA helpers
 void launch_layer_dos(int rel, int nd, int nl, int nlay, const zd *tau, int ld, const zd *F,
                       const zd *G, double fac, zd *zmom, zd *zdos_l, cudaStream_t st);
+// Bloch spectral function sums of (k, layer) items (k_bsf_reduce)
+void launch_bsf_reduce(int nd, int nde, int bdg, int nlay, int nitems, const double *conc, const int *cpa,
+                       const zd *del, const zd *M, long long msec, const zd *ta, const zd *tb, const zd *F,
+                       const zd *Feh, const zd *P, double fac, double *out, cudaStream_t st);
 void launch_cpa_mix(const zd *X, const double *conc, const int *act, int lk, int nl, zd *xc,
                     cudaStream_t st);
 

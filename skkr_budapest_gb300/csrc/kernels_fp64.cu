@@ -820,3 +820,74 @@ void launch_layer_dos(int rel, int nd, int nl, int nlay, const zd *tau, int ld, 
   k_layer_dos<<<nlay, 128, 0, st>>>(rel, nd, nl, tau, ld, F, G, fac, zmom, zdos_l);
   SKKR_LAUNCHED();
 }
+
+// ---------------------------------------------------------------------------
+// Bloch spectral function (skkr_dbogo_bsf/rsp-scf/bsf.f:251-418 after its
+// products): one CTA per (k, layer) item.  With diagonal radial solutions
+// gf.f's ggrmat(j, i) is R_ab(j, i) X(j, i); the moments at lambda = 0 read its
+// diagonal (electron and hole halves) and its electron-hole block through the
+// four pairing operators.  CPA layers: sum_ab c_a c_b R_ab M_ab (M_ab =
+// D_a (tau(k) - tau_c) D~_b, section a*2+b of M) plus sum_a c_a R_aa tau_a;
+// other layers: R_AA (tau(k)).  Six sums in a fixed order per item:
+// bsfe, bsfh, then Im tr(P_x G_eh) for x = singlet, T0, T-up, T-down.
+__global__ void __launch_bounds__(256) k_bsf_reduce(int nd, int nde, int bdg, int nlay, const double *conc,
+                                                    const int *__restrict__ cpa, const zd *__restrict__ del,
+                                                    const zd *__restrict__ M, long long msec,
+                                                    const zd *__restrict__ ta, const zd *__restrict__ tb,
+                                                    const zd *__restrict__ F, const zd *__restrict__ Feh,
+                                                    const zd *__restrict__ P, double fac, double *out) {
+  const int item = blockIdx.x, l = item % nlay;
+  const long long MB = (long long)nd * nd, NE2 = (long long)nde * nde;
+  const bool cp = cpa[l] != 0;
+  const double cab[2] = {conc[l], 1.0 - conc[l]};
+  const zd *Fl = F + (long long)l * 4 * nd;
+  const zd *Fe = bdg ? Feh + (long long)l * 4 * NE2 : nullptr;
+  double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  // element e of the matrices of this item, each term weighted by its radial
+  // overlap R[a*2+b] (stride rs between the four species pairs)
+  auto g_at = [&](long long e, const zd *R, long long rs) -> zd {
+    zd g = make_double2(0.0, 0.0);
+    if (cp) {
+      for (int a = 0; a < 2; a++)
+        for (int b = 0; b < 2; b++) {
+          const zd m = M[(a * 2 + b) * msec + (long long)item * MB + e];
+          zfma(g, zscale(cab[a] * cab[b], R[(a * 2 + b) * rs]), m);
+        }
+      for (int a = 0; a < 2; a++) {
+        const zd t = (a ? tb : ta)[(long long)l * MB + e];
+        zfma(g, zscale(cab[a], R[(a * 2 + a) * rs]), t);
+      }
+    } else {
+      zfma(g, R[0], del[(long long)item * MB + e]);
+    }
+    return g;
+  };
+  for (int i = threadIdx.x; i < nd; i += blockDim.x) {
+    const zd g = g_at(i + (long long)i * nd, Fl + i, nd);
+    acc[(bdg && i >= nde) ? 1 : 0] += g.y;
+  }
+  if (bdg)
+    for (long long idx = threadIdx.x; idx < NE2; idx += blockDim.x) {
+      const int j = (int)(idx % nde), i = (int)(idx / nde);
+      // G_eh(j, i) is element (j, nde + i); P_x(i, j) multiplies it in tr(P_x G_eh)
+      const zd g = g_at(j + (long long)(nde + i) * nd, Fe + j + (long long)i * nde, NE2);
+      for (int x = 0; x < 4; x++) acc[2 + x] += zmul(P[x * NE2 + i + (long long)j * nde], g).y;
+    }
+  __shared__ double red[6][256];
+  for (int q = 0; q < 6; q++) red[q][threadIdx.x] = acc[q];
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s)
+      for (int q = 0; q < 6; q++) red[q][threadIdx.x] += red[q][threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x < 6) out[(long long)item * 6 + threadIdx.x] = fac * red[threadIdx.x][0];
+}
+
+void launch_bsf_reduce(int nd, int nde, int bdg, int nlay, int nitems, const double *conc, const int *cpa,
+                       const zd *del, const zd *M, long long msec, const zd *ta, const zd *tb, const zd *F,
+                       const zd *Feh, const zd *P, double fac, double *out, cudaStream_t st) {
+  if (nitems <= 0) return;
+  k_bsf_reduce<<<nitems, 256, 0, st>>>(nd, nde, bdg, nlay, conc, cpa, del, M, msec, ta, tb, F, Feh, P, fac, out);
+  SKKR_LAUNCHED();
+}

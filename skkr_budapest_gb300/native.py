@@ -84,6 +84,7 @@ def lib():
         L.skkr_gpu_kambe_alm.argtypes = [I, D, D, P, P, I, P, I, P, I, D, D, D, D, P]
         L.skkr_gpu_kambe_screened.argtypes = [I, D, D, P, I, P, P, I, P, I, P, I, D, D, D, D, I, I, P]
         L.skkr_gpu_layer_dos.argtypes = [I, I, I, P, I, P, P, I, P, P]
+        L.skkr_gpu_bsf.argtypes = [I, I, I, I, P, P, P, P, P, P, P, P, I, P]
         L.skkr_gpu_set_reduce.argtypes = [P, P, P]
         L.skkr_gpu_set_reduce_device.argtypes = [P, P, P]
         L.skkr_gpu_set_mixed_policy.argtypes = [P, D, D, I, D]
@@ -446,6 +447,27 @@ def layer_dos(tau, F, G, lmax, irel, para=False):
     _check(lib().skkr_gpu_layer_dos(irel, lmax, nlay, _p(t), nd, _p(f), _p(g), int(bool(para)), _p(zm), _p(zl)),
            "skkr_gpu_layer_dos")
     return zm, zl
+
+
+def bsf(mode, lmax, conc, tauk, tauc, taua, taub, F, Feh=None, pair=None, para=False):
+    """Bloch spectral function on the device (skkr_gpu_bsf): tauk [nk, nlay,
+    nd, nd] physical coherent tau of each k point, tauc / taua / taub [nlay,
+    nd, nd] the k-integrated CPA taus, F [nlay, 2, 2, nd], for BdG Feh [nlay,
+    2, 2, nde, nde] and pair [4, nde, nde] (singlet, T0, T-up, T-down), all
+    [row, col].  Returns [nk, nlay, 6]: bsfe, bsfh, bsfeh, bsfhe, bsfteh,
+    bsfthe (-1/pi Im of the sums)."""
+    tk = np.asarray(tauk, np.complex128)
+    nk, nlay, nd = tk.shape[0], tk.shape[1], tk.shape[-1]
+    args = [cm(tk), cm(tauc), cm(taua), cm(taub)]
+    f = np.ascontiguousarray(F, np.complex128).reshape(nlay, 2, 2, nd)
+    fe = None if Feh is None else cm(np.asarray(Feh, np.complex128))
+    pr = None if pair is None else cm(np.asarray(pair, np.complex128))
+    out = np.zeros((nk, nlay, 6))
+    c = np.ascontiguousarray(conc, np.float64)
+    _check(lib().skkr_gpu_bsf(mode, lmax, nk, nlay, _p(c), *[_p(x) for x in args], _p(f),
+                              None if fe is None else _p(fe), None if pr is None else _p(pr),
+                              int(bool(para)), _p(out)), "skkr_gpu_bsf")
+    return out
 
 
 KSTAT_CLASSES = ("zgemm", "gjinv", "gk_ft", "other", "ozaki")

@@ -415,6 +415,158 @@ def sqwell_fg(p2: complex, vwell: float, radius: float, l: int):
     return complex(a * a * ijj), complex(a * (b * ijj + c * ijn))
 
 
+def sqwell_regular(p2: complex, vwell: float, radius: float, l: int):
+    """(a, q) of the regular solution inside the well in sqwell_fg's
+    normalisation: Z_l(r) = a j_l(q r) for r < R."""
+    ck = kappa_of(p2)
+    q = kappa_of(complex(p2) - vwell)
+    tand = _tan_delta(ck, q, radius, l)[l]
+    react = -tand / ck
+    t = react / (1.0 + 1j * ck * react)
+    _, jk0, _, _, nk0, _ = _bessel_l_pm(l, ck * radius)
+    j0 = _bessel_l_pm(l, q * radius)[1]
+    return complex((jk0 / t - 1j * ck * (jk0 + 1j * nk0)) / j0), complex(q)
+
+
+_GL_NODES = 48
+
+
+def radial_overlap(za, zb, radius: float, l: int, conj_b: bool = False) -> complex:
+    """int_0^R Z_a(r) Z_b(r) r^2 dr of two regular solutions (a, q) of
+    sqwell_regular (conj_b: the complex conjugate of Z_b, a hole solution),
+    by 48-node Gauss-Legendre quadrature over the sphere: the integrand is
+    entire in r, and the upward Bessel recurrence's error near r = 0 meets a
+    partner that vanishes like r^l there."""
+    x, w = np.polynomial.legendre.leggauss(_GL_NODES)
+    r = 0.5 * radius * (x + 1.0)
+    wr = 0.5 * radius * w
+    fa = za[0] * sph_bessel(l, za[1] * r)[0][l]
+    fb = zb[0] * sph_bessel(l, zb[1] * r)[0][l]
+    if conj_b:
+        fb = np.conj(fb)
+    return complex(np.sum(wr * r * r * fa * fb))
+
+
+def _species_depths(ep, li):
+    """Well depths of species A and B of interface layer li (BdG systems have
+    one species per layer)."""
+    m = ep.meta
+    if "depth_a" in m:
+        return float(m["depth_a"][li]), float(m["depth_b"][li])
+    d = float(m["depth_int"][li])
+    return d, d
+
+
+def bsf_radial(ep):
+    """Radial overlaps of the regular solutions that the Bloch spectral
+    function of bsf.f contracts with tau (gf.f's Z^R tau Z^L with the
+    diagonal, spherical solutions of the square wells of this model):
+
+    F[li, a, b, i] = int Z^a_i Z^b_i r^2 dr, a and b over species A, B (the
+    right solution of species a, the left of species b), i the basis index:
+    lm (non-relativistic), (kappa,mu) of the j-split well (relativistic,
+    momentum psq, large component), or for BdG the electron block (psq) then
+    the hole block (hole solutions: the conjugates of the electron ones at
+    the hole momentum psqh, the pairing living in t^-1).
+
+    Feh[li, a, b, j, i] (BdG only, else None) = int Z^{e,a}_j Z^{h,b}_i r^2 dr
+    for electron index j and hole index i of the same l, zero otherwise: the
+    electron-hole block that the anomalous components contract."""
+    lmax = ep.lmax
+    radius, so = ep.meta["radius"], ep.meta.get("so_split", 0.0)
+    bdg = ep.irel == 2
+    nde = ep.lkmax // 2 if bdg else ep.lkmax
+    if ep.irel:
+        lv, kv = kmy_l_kappa(lmax)
+    else:
+        lv, kv = lm_l(nde), None
+    lv = np.asarray(lv)[:nde]
+    F = np.zeros((ep.nintfc, 2, 2, ep.lkmax), complex)
+    Feh = np.zeros((ep.nintfc, 2, 2, nde, nde), complex) if bdg else None
+    psqh = ep.meta.get("psqh")
+
+    def wells(depth):
+        zs, zh = [], []
+        for i in range(nde):
+            l = int(lv[i])
+            v = depth
+            if kv is not None:
+                kap = int(kv[i])
+                v += so * (0.5 * l if kap < 0 else -0.5 * (l + 1))
+            zs.append((l, sqwell_regular(ep.psq, v, radius, l)))
+            if bdg:
+                zh.append((l, sqwell_regular(psqh, v, radius, l)))
+        return zs, zh
+
+    for li in range(ep.nintfc):
+        sp = [wells(d) for d in _species_depths(ep, li)]
+        for a in range(2):
+            for b in range(2):
+                ea, ha = sp[a]
+                eb, hb = sp[b]
+                cache = {}
+                for i in range(nde):
+                    l = ea[i][0]
+                    key = (l, ea[i][1], eb[i][1])
+                    if key not in cache:
+                        cache[key] = radial_overlap(ea[i][1], eb[i][1], radius, l)
+                    F[li, a, b, i] = cache[key]
+                    if bdg:
+                        # both hole solutions conjugated: the conjugate overlap
+                        F[li, a, b, nde + i] = np.conj(radial_overlap(ha[i][1], hb[i][1], radius, l))
+                if bdg:
+                    for j in range(nde):
+                        for i in range(nde):
+                            if ea[j][0] == ha[i][0]:
+                                key = ("eh", ea[j][0], ea[j][1], hb[i][1])
+                                if key not in cache:
+                                    cache[key] = radial_overlap(ea[j][1], hb[i][1], radius, ea[j][0], conj_b=True)
+                                Feh[li, a, b, j, i] = cache[key]
+    return F, Feh
+
+
+def _lms_pairs(lmax: int):
+    """(lm, lm', m) of the lm pairs with l = l' and m = -m' (main/pairing.f's
+    selection), lm in the order l = 0..lmax, m = -l..l."""
+    out = []
+    lm = 0
+    for l in range(lmax + 1):
+        for m in range(-l, l + 1):
+            out.append((lm, lm - 2 * m, m))
+            lm += 1
+    return out
+
+
+def pairing_kmy(lmax: int) -> dict:
+    """The four pairing operators of rsp-scf/pairing.f in the (kappa,mu)
+    basis: singlet (i sigma_y), triplet with unequal spins (T0), and the
+    equal-spin triplets (up, down), each built in the (l, m, s)
+    representation on l = l', m = -m' and taken to (kappa,mu) with the
+    Clebsch-Gordan matrix as rsp-scf/matlms.f matkmy does (U^T X U, no
+    conjugation; spin index 1 of the reference pairs with u1)."""
+    lmmax = (lmax + 1) ** 2
+    U = clebsch_u(lmax)
+    out = {}
+    for name in ("singlet", "t0", "tup", "tdown"):
+        X = np.zeros((2 * lmmax, 2 * lmmax), complex)
+        for lm, lmp, m in _lms_pairs(lmax):
+            sm, smp = (-1.0) ** m, (-1.0) ** (-m)
+            if name == "singlet":
+                X[lm, lmmax + lmp] = 0.5 * sm
+                X[lmmax + lm, lmp] = -0.5 * sm
+            elif name == "t0":
+                X[lm, lmmax + lmp] = 0.5 * smp
+                X[lmmax + lm, lmp] = 0.5 * smp
+            elif name == "tup":
+                X[lm, lmp] = 0.5 * smp
+                X[lmmax + lm, lmmax + lmp] = -0.5 * smp
+            else:
+                X[lm, lmp] = -0.5j * smp
+                X[lmmax + lm, lmmax + lmp] = -0.5j * smp
+        out[name] = U.T @ X @ U
+    return out
+
+
 def layer_dos_inputs(ep, which: str = "a"):
     """Per-basis-index F, G (nintfc, lk) of the interface layers of an
     EnergyProblem for species `which` ('a' or 'b'): lm-resolved F_l, G_l
