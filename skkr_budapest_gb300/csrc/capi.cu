@@ -207,10 +207,11 @@ struct DBuf {
 struct KambeDev {
   int lmax = 0, lm = 0, nl = 0, N = 0, nsep = 0, ng = 0, nr = 0, centre = 0, jmax = 0;
   double er = 0, ei = 0, area = 0, factor = 1, gcut = 0, rcut = 0;
-  DBuf gvec, rvec, coef, pos, alpha, seps, pmap, ik, is, alm, Gs, A, X;
+  int nfar = 0;
+  DBuf gvec, rvec, coef, pos, alpha, seps, pmap, far, ik, is, alm, Gs, A, X;
 
   void release() {
-    DBuf *all[] = {&gvec, &rvec, &coef, &pos, &alpha, &seps, &pmap, &ik, &is, &alm, &Gs, &A, &X};
+    DBuf *all[] = {&gvec, &rvec, &coef, &pos, &alpha, &seps, &pmap, &far, &ik, &is, &alm, &Gs, &A, &X};
     for (DBuf *b : all) b->release();
   }
   size_t per_k() const {
@@ -265,6 +266,19 @@ int KambeDev::setup(double e_re, double e_im, int lmax_, int nl_, const double *
       pm[(size_t)a * nl + b] = f;
     }
   nsep = (int)(sv.size() / 3);
+  // gstore.f:158-166: pairs with |s_z| |b|_min >= 5 take the plane-wave form
+  // of directg.f; |b|_min is the shortest nonzero vector of the g list
+  double bmin = 0.0;
+  for (int q = 0; q < ng_; q++) {
+    const double b = std::hypot(gvec_h[2 * q], gvec_h[2 * q + 1]);
+    if (b > 1e-9 && (bmin == 0.0 || b < bmin)) bmin = b;
+  }
+  std::vector<int> fr(nsep);
+  nfar = 0;
+  for (int q = 0; q < nsep; q++) {
+    fr[q] = std::fabs(sv[3 * q + 2]) * bmin >= 5.0;
+    nfar += fr[q];
+  }
   const int lm2 = (2 * lmax + 1) * (2 * lmax + 1);
   std::vector<double> cf(2 * (size_t)lm * lm * lm2);
   CKR(skkr_gpu_kambe_coef(lmax, cf.data()));
@@ -275,6 +289,8 @@ int KambeDev::setup(double e_re, double e_im, int lmax_, int nl_, const double *
   CKR(alpha.ensure((size_t)nl * (lmax + 1) * sizeof(zd)));
   CKR(seps.ensure(sv.size() * sizeof(double)));
   CKR(pmap.ensure(pm.size() * sizeof(int)));
+  CKR(far.ensure(fr.size() * sizeof(int)));
+  CK(cudaMemcpyAsync(far.p, fr.data(), fr.size() * sizeof(int), cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(gvec.p, gvec_h, 2 * (size_t)ng * sizeof(double), cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(rvec.p, rvec_h, 2 * (size_t)nr * sizeof(double), cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(coef.p, cf.data(), cf.size() * sizeof(double), cudaMemcpyHostToDevice, st));
@@ -282,7 +298,7 @@ int KambeDev::setup(double e_re, double e_im, int lmax_, int nl_, const double *
   CK(cudaMemcpyAsync(alpha.p, alpha_h, (size_t)nl * (lmax + 1) * sizeof(zd), cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(seps.p, sv.data(), sv.size() * sizeof(double), cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(pmap.p, pm.data(), pm.size() * sizeof(int), cudaMemcpyHostToDevice, st));
-  CK(cudaStreamSynchronize(st));  // cf, sv, pm are host temporaries
+  CK(cudaStreamSynchronize(st));  // cf, sv, pm, fr are host temporaries
   return SKKR_OK;
 }
 
@@ -296,7 +312,11 @@ int KambeDev::screen(const double *xk, int m, cudaStream_t st) {
   CKR(X.ensure((size_t)m * NN * sizeof(zd)));
   launch_kambe_items(m, nsep, xk, seps.as<double>(), ik.as<double>(), is.as<double>(), st);
   launch_kambe_alm((int)items, er, ei, ik.as<double>(), is.as<double>(), lmax, gvec.as<double>(), ng,
-                   rvec.as<double>(), nr, area, factor, gcut, rcut, coef.as<double>(), alm.as<double>(), st);
+                   rvec.as<double>(), nr, area, factor, gcut, rcut, coef.as<double>(), far.as<int>(), nsep,
+                   alm.as<double>(), st);
+  if (nfar > 0)
+    launch_directg((int)items, er, ei, ik.as<double>(), is.as<double>(), lmax, gvec.as<double>(), ng, area,
+                   far.as<int>(), nsep, alm.as<double>(), st);
   launch_slab_assemble(m, nl, lm, alm.as<zd>(), pmap.as<int>(), nsep, xk, pos.as<double>(), alpha.as<zd>(), lmax + 1,
                        Gs.as<zd>(), A.as<zd>(), st);
   launch_zgj(mref(A.as<zd>(), NN, 0, N), N, m, 1, nullptr, st);
@@ -2882,7 +2902,7 @@ extern "C" int skkr_gpu_kambe_alm(int nitem, double e_re, double e_im, const dou
   CK(cudaMemcpy(G, gvec, 2 * (size_t)ng * sizeof(double), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(R, rvec, 2 * (size_t)nr * sizeof(double), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(Cf, coef.data(), coef.size() * sizeof(double), cudaMemcpyHostToDevice));
-  launch_kambe_alm(nitem, e_re, e_im, K, S, lmax, G, ng, R, nr, area, factor, gcut, rcut, Cf, O, 0);
+  launch_kambe_alm(nitem, e_re, e_im, K, S, lmax, G, ng, R, nr, area, factor, gcut, rcut, Cf, nullptr, 1, O, 0);
   CK(cudaDeviceSynchronize());
   CK(cudaGetLastError());
   CK(cudaMemcpy(out, O, 2 * (size_t)nitem * lm * lm * sizeof(double), cudaMemcpyDeviceToHost));

@@ -322,6 +322,108 @@ SKKR_HD inline void kambe_alm(const fcplx *d, int lmax, const double *coef, fcpl
     }
 }
 
+// ---------------------------------------------------------------------------
+// The plane-wave form of the same layer-pair blocks, which gstore.f uses for
+// layers far apart (|s_z| |b|_min >= 5; main/directg.f:2-151):
+//   alm(k, s)[L][L'] = -i (8 pi^2 / A) sum_g e^{i (k+g).s_par + i K_z |s_z|} / K_z
+//                      Yl_L(g) Yr_L'(g),   K_z = sqrt(kappa^2 - |k+g|^2),
+// the harmonics taken at the complex direction (K_z, |k+g|, phi) / kappa
+// (sphrm.f).  s_z > 0 gives directg's gp block of s, s_z < 0 its gm block of
+// -s; they differ in which of Y_lm and Y_l,-m carries the sign (-1)^l and
+// which the sign (-1)^m.
+#define SKKR_DG_LM 16  // (lmax + 1)^2 for lmax <= 3
+
+// Y_lm of the complex angles (cos, sin, e^{i phi}), l <= lmax, index
+// l(l+1)+m: the m = l and m = l - 1 forms, then the recurrence in l (sphrm.f)
+SKKR_HD inline void directg_sphrm(fcplx ct, fcplx st, fcplx cf, int lmax, fcplx *yo) {
+  fcplx y[SKKR_DG_LM + 1];  // 1-based, as the recurrences index it
+  for (int i = 0; i <= SKKR_DG_LM; i++) y[i] = fc(0.0, 0.0);
+  const double pi = 3.14159265358979323846;
+  y[1] = fc(sqrt(0.25 / pi), 0.0);
+  double a = 1.0, b = 1.0, asg = 1.0;
+  fcplx sf = fc(1.0, 0.0), sa = fc(1.0, 0.0);
+  int lp = 1;
+  for (int l = 1; l <= lmax; l++) {
+    const double fl = l;
+    a = 0.5 * a * fl * (2.0 * fl - 1.0);
+    b = fl * b;
+    asg = -asg;
+    const int lm = lp + 1;
+    lp = lp + l + l + 1;
+    sf = fmulc(sf, cf);
+    fcplx fac = fscal(sqrt((2.0 * fl + 1.0) * a / (4.0 * pi * b * b)), sa);
+    y[lm] = fdivc(fmulc(fac, st), sf);
+    y[lp] = fscal(asg, fmulc(fmulc(fac, st), sf));
+    fac = fscal(sqrt(2.0 * fl), fmulc(fac, ct));
+    y[lm + 1] = fdivc(fmulc(fac, cf), sf);
+    y[lp - 1] = fscal(-asg, fdivc(fmulc(fac, sf), cf));
+    sa = fmulc(sa, st);
+  }
+  for (int m = 2; m <= lmax; m++) {
+    const int mm = m + m - 4;
+    const double fm = m - 2;
+    double aa = sqrt(1.0 / (fm + fm + 3.0));
+    int ln = m * m - 1, lm = ln - m - m + 2;
+    for (int l = m; l <= lmax; l++) {
+      const double fl = l;
+      const double bb = sqrt((fl + fm) * (fl - fm) / ((fl + fl + 1.0) * (fl + fl - 1.0)));
+      const int lq = ln + l + l;
+      y[lq] = fscal(1.0 / bb, fsub(fmulc(ct, y[ln]), fscal(aa, y[lm])));
+      y[lq - mm] = fscal(1.0 / bb, fsub(fmulc(ct, y[ln - mm]), fscal(aa, y[lm - mm])));
+      aa = bb;
+      lm = ln;
+      ln = lq;
+    }
+  }
+  for (int i = 0; i < (lmax + 1) * (lmax + 1); i++) yo[i] = y[i + 1];
+}
+
+// the g term of the plane-wave form: its scalar factor and the left / right
+// harmonic vectors (yl over L, yr over L'); f1 = 8 pi^2 / A
+SKKR_HD inline void directg_gterm(fcplx kappa2, fcplx kappa, double kx, double ky, double sx, double sy, double sz,
+                                  int lmax, double gx, double gy, double f1, fcplx *fac, fcplx *yl, fcplx *yr) {
+  const double gkx = gx + kx, gky = gy + ky, gk2 = gkx * gkx + gky * gky, gk = sqrt(gk2);
+  const fcplx gkz = fsqrtc(fsub(kappa2, fc(gk2, 0.0)));
+  const fcplx phi = gk > 1e-6 ? fc(gkx / gk, gky / gk) : fc(1.0, 0.0);
+  fcplx y[SKKR_DG_LM];
+  directg_sphrm(fdivc(gkz, kappa), fdivc(fc(gk, 0.0), kappa), phi, lmax, y);
+  const double az = fabs(sz);
+  // e^{i (gkx sx + gky sy + K_z |s_z|)}
+  const fcplx ph = fexpc(fc(-gkz.im * az, gkx * sx + gky * sy + gkz.re * az));
+  *fac = fdivc(fmulc(fc(0.0, -f1), ph), gkz);
+  for (int l = 0; l <= lmax; l++)
+    for (int m = -l; m <= l; m++) {
+      const int L = l * (l + 1) + m, Ln = l * (l + 1) - m;
+      const fcplx il = fipow(l);
+      const double sl = (l & 1) ? -1.0 : 1.0, sm = (m & 1) ? -1.0 : 1.0;
+      if (sz > 0.0) {
+        yr[L] = fscal(sl, fmulc(il, y[L]));
+        yl[L] = fscal(sm, fmulc(il, y[Ln]));
+      } else {
+        yr[L] = fscal(sm, fmulc(il, y[L]));
+        yl[L] = fscal(sl, fmulc(il, y[Ln]));
+      }
+    }
+}
+
+// the whole block, one thread (host check of the device kernel's terms):
+// out [lm][lm], g terms summed in list order
+SKKR_HD inline void directg_alm(fcplx e, double kx, double ky, double sx, double sy, double sz, int lmax,
+                                const double *gvec, int ng, double area, fcplx *out) {
+  const int lm = (lmax + 1) * (lmax + 1);
+  const fcplx kappa = fsqrtc(e);
+  const double f1 = 8.0 * 3.14159265358979323846 * 3.14159265358979323846 / area;
+  for (int i = 0; i < lm * lm; i++) out[i] = fc(0.0, 0.0);
+  for (int ig = 0; ig < ng; ig++) {
+    fcplx fac, yl[SKKR_DG_LM], yr[SKKR_DG_LM];
+    directg_gterm(e, kappa, kx, ky, sx, sy, sz, lmax, gvec[2 * ig], gvec[2 * ig + 1], f1, &fac, yl, yr);
+    for (int a = 0; a < lm; a++) {
+      const fcplx fa = fmulc(fac, yl[a]);
+      for (int b = 0; b < lm; b++) out[a * lm + b] = fadd(out[a * lm + b], fmulc(fa, yr[b]));
+    }
+  }
+}
+
 // element e of the slab matrices of one batch (column-major N x N per k,
 // N = nl lm): G[(a,L),(b,L')] = e^{ik.(pos_b - pos_a)} alm_ab[L][L'],
 // A = 1 - alpha[a][l(L)] G; alm, alpha, G, A complex (re, im interleaved)

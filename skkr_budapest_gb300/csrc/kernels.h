@@ -168,10 +168,17 @@ void launch_kambe_dlm(int nitem, double er, double ei, const double *kxy, const 
                       const double *gvec, int ng, const double *rvec, int nr, double area, double factor,
                       double gcut, double rcut, double *out, cudaStream_t st);
 // layer-pair blocks alm(k, s) (kernels_kambe.cu): out[item][lmmax][lmmax]
-// complex, coef from skkr_gpu_kambe_coef
+// complex, coef from skkr_gpu_kambe_coef; items with far[item % nsep] != 0
+// are left to launch_directg (far may be null: every item here)
 void launch_kambe_alm(int nitem, double er, double ei, const double *kxy, const double *sep, int lmax,
                       const double *gvec, int ng, const double *rvec, int nr, double area, double factor,
-                      double gcut, double rcut, const double *coef, double *out, cudaStream_t st);
+                      double gcut, double rcut, const double *coef, const int *far, int nsep, double *out,
+                      cudaStream_t st);
+// the plane-wave form (directg.f) of the blocks of the items with
+// far[item % nsep] != 0, same layout
+void launch_directg(int nitem, double er, double ei, const double *kxy, const double *sep, int lmax,
+                    const double *gvec, int ng, double area, const int *far, int nsep, double *out,
+                    cudaStream_t st);
 // slab screening of the reference's k-space form (kernels_kambe.cu):
 // G and A = 1 - alpha G per k from the layer-pair blocks, and the central
 // layer offsets of X = G A^-1

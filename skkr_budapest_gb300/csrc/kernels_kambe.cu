@@ -80,7 +80,10 @@ __global__ void __launch_bounds__(KB_THREADS) k_kambe_alm_cta(double er, double 
                                                               const double *__restrict__ rvec, int nr, double area,
                                                               double factor, double gcut, double rcut,
                                                               const double *__restrict__ coef,
+                                                              const int *__restrict__ far, int nsep,
                                                               double *__restrict__ out) {
+  // pairs far apart take the plane-wave form (k_directg_cta)
+  if (far && far[blockIdx.x % nsep]) return;
   __shared__ fcplx d[(SKKR_KAMBE_L2 + 1) * (SKKR_KAMBE_L2 + 1)];
   kambe_block_sums(er, ei, kxy, sep, 2 * lmax, gvec, ng, rvec, nr, area, factor, gcut, rcut, d);
   const int lm = (lmax + 1) * (lmax + 1), lm2 = (2 * lmax + 1) * (2 * lmax + 1);
@@ -90,6 +93,43 @@ __global__ void __launch_bounds__(KB_THREADS) k_kambe_alm_cta(double er, double 
     const double *c = coef + 2 * ((long long)e * lm2);
     for (int q = 0; q < lm2; q++) s = fadd(s, fmulc(fc(c[2 * q], c[2 * q + 1]), d[q]));
     o[e] = s;
+  }
+}
+
+// the plane-wave form of the blocks of items whose separation is far (far[item
+// % nsep] != 0; directg.f): one block per item, one thread per (L, L').  Tiles
+// of DG_TILE g vectors: the first threads form the terms (factor and the two
+// harmonic vectors) in shared memory, then every thread adds the tile's
+// terms to its element in g order.
+constexpr int DG_TILE = 64;
+__global__ void __launch_bounds__(256) k_directg_cta(double er, double ei, const double *__restrict__ kxy,
+                                                    const double *__restrict__ sep, int lmax,
+                                                    const double *__restrict__ gvec, int ng, double area,
+                                                    const int *__restrict__ far, int nsep,
+                                                    double *__restrict__ out) {
+  const int it = blockIdx.x, t = threadIdx.x;
+  if (!far[it % nsep]) return;
+  __shared__ fcplx fs[DG_TILE], yl[DG_TILE][SKKR_DG_LM], yr[DG_TILE][SKKR_DG_LM];
+  const int lm = (lmax + 1) * (lmax + 1), L = t / lm, Lp = t % lm;
+  const fcplx e = fc(er, ei), kappa = fsqrtc(e);
+  const double f1 = 8.0 * 3.14159265358979323846 * 3.14159265358979323846 / area;
+  const double kx = kxy[2 * it], ky = kxy[2 * it + 1];
+  const double sx = sep[3 * it], sy = sep[3 * it + 1], sz = sep[3 * it + 2];
+  fcplx acc = fc(0.0, 0.0);
+  for (int g0 = 0; g0 < ng; g0 += DG_TILE) {
+    const int nt = min(DG_TILE, ng - g0);
+    for (int q = t; q < nt; q += blockDim.x)
+      directg_gterm(e, kappa, kx, ky, sx, sy, sz, lmax, gvec[2 * (g0 + q)], gvec[2 * (g0 + q) + 1], f1, &fs[q],
+                    yl[q], yr[q]);
+    __syncthreads();
+    if (t < lm * lm)
+      for (int q = 0; q < nt; q++) acc = fadd(acc, fmulc(fmulc(fs[q], yl[q][L]), yr[q][Lp]));
+    __syncthreads();
+  }
+  if (t < lm * lm) {
+    double *o = out + 2 * ((long long)it * lm * lm + t);
+    o[0] = acc.re;
+    o[1] = acc.im;
   }
 }
 
@@ -172,10 +212,20 @@ void launch_kambe_items(int nk, int nsep, const double *xk, const double *seps, 
 // one block per item (grid.x holds up to 2^31 - 1 items)
 void launch_kambe_alm(int nitem, double er, double ei, const double *kxy, const double *sep, int lmax,
                       const double *gvec, int ng, const double *rvec, int nr, double area, double factor,
-                      double gcut, double rcut, const double *coef, double *out, cudaStream_t st) {
+                      double gcut, double rcut, const double *coef, const int *far, int nsep, double *out,
+                      cudaStream_t st) {
   if (nitem <= 0) return;
   k_kambe_alm_cta<<<nitem, KB_THREADS, 0, st>>>(er, ei, kxy, sep, lmax, gvec, ng, rvec, nr, area, factor, gcut, rcut,
-                                                coef, out);
+                                                coef, far, nsep, out);
+  SKKR_LAUNCHED();
+}
+
+// one block per item; items whose separation is not far return at once
+void launch_directg(int nitem, double er, double ei, const double *kxy, const double *sep, int lmax,
+                    const double *gvec, int ng, double area, const int *far, int nsep, double *out,
+                    cudaStream_t st) {
+  if (nitem <= 0) return;
+  k_directg_cta<<<nitem, 256, 0, st>>>(er, ei, kxy, sep, lmax, gvec, ng, area, far, nsep, out);
   SKKR_LAUNCHED();
 }
 

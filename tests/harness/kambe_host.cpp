@@ -42,3 +42,13 @@ extern "C" void slab_extract_eval(int nk, int nl, int lm, int centre, int jmax, 
   const long long tot = (long long)nk * (2 * jmax + 1) * lm * lm;
   for (long long e = 0; e < tot; e++) kambe_slab_extract_elem(e, nl, lm, centre, jmax, X, out);
 }
+
+extern "C" void directg_eval(double er, double ei, double kx, double ky, double sx, double sy, double sz, int lmax,
+                             const double *gvec, int ng, double area, double *out) {
+  fcplx g[256];
+  directg_alm(fc(er, ei), kx, ky, sx, sy, sz, lmax, gvec, ng, area, g);
+  for (int i = 0; i < (lmax + 1) * (lmax + 1) * (lmax + 1) * (lmax + 1); i++) {
+    out[2 * i] = g[i].re;
+    out[2 * i + 1] = g[i].im;
+  }
+}

@@ -159,3 +159,28 @@ def test_slab_chain_of_the_device_entry_point(lib):
         gs = K.screened_slab(ce, k[0], k[1], lmax, pos, [al] * nl, lat)
         ref = np.array([gs[centre, centre + j] for j in range(-jmax, jmax + 1)])
         assert np.abs(out[ik] - ref).max() < 1e-10 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("e", [0.4 + 0.6j, 0.3 + 0.01j, -0.45 + 0.06j, 0.7 + 1e-4j])
+@pytest.mark.parametrize("sep", [(0.5 * A2D, 0.5 * A2D, 6.8), (0.3, -0.8, 10.2), (0.0, 0.0, -13.6),
+                                 (0.5 * A2D, 0.5 * A2D, -6.8)])
+@pytest.mark.parametrize("lmax", [2, 3])
+def test_device_plane_wave_form_equals_directg(lib, e, sep, lmax):
+    """The plane-wave form of the device (directg_alm, the terms of its
+    kernel) against the oracle's directg: gp for s_z > 0, gm of -s for
+    s_z < 0, on the g vectors within 14 a.u.^-1 of the origin (the oracle
+    takes |k + g| <= 30; the rest is below e^{-14 |s_z|})."""
+    D, I, P = ctypes.c_double, ctypes.c_int, ctypes.c_void_p
+    lib.directg_eval.argtypes = [D, D, D, D, D, D, D, I, P, I, D, P]
+    g = np.ascontiguousarray(LAT.gvecs(14.0))
+    lm = (lmax + 1) ** 2
+    out = np.zeros(2 * lm * lm)
+    k = (0.21, 0.07)
+    lib.directg_eval(e.real, e.imag, *k, *sep, lmax, g.ctypes.data, len(g), LAT.area, out.ctypes.data)
+    got = (out[0::2] + 1j * out[1::2]).reshape(lm, lm)
+    s = np.asarray(sep)
+    ref = K.directg(e, *k, lmax, s, LAT)[0] if s[2] > 0 else K.directg(e, *k, lmax, -s, LAT)[1]
+    assert np.abs(got - ref).max() < 1e-12 * np.abs(ref).max()
+    # and gstore's choice for this pair is the plane-wave form
+    assert abs(s[2]) * LAT.bmin >= 5.0
+    assert np.abs(got - K.gstore_block(e, *k, lmax, s, LAT)).max() < 1e-12 * np.abs(ref).max()
