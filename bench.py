@@ -67,8 +67,10 @@ def parse():
     ap.add_argument("--newton", type=int, default=2, help="standard Newton steps of the split-precision inverse")
     ap.add_argument("--fp64-ref", default="", help="file of the FP64 pass (tau per energy, timing): written when "
                                                    "absent, read instead of rerunning the FP64 pass when present")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5", "gk", "tauij"],
-                    help="c3: one energy of each of three systems per step through skkr_gpu_cpacoord_many; "
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5", "gk", "tauij"],
+                    help="c1: the plain non-relativistic interface, the whole contour per step, FP64 and split "
+                         "precision; "
+                         "c3: one energy of each of three systems per step through skkr_gpu_cpacoord_many; "
                          "c4: CPA alloy interfaces from the ATA and from the learned start; "
                          "c5: the BdG interface (n_PL = 256, Im E = 1e-4 Ry), FP64 and split precision; "
                          "gk: the C2 path on the reference's k-space G_scr(k) (Kambe sums + slab screening) "
@@ -678,6 +680,88 @@ def run_c4(args):
     print(json.dumps(line), flush=True)
 
 
+C1_METRIC = "(E,k) points/s of the plain non-relativistic interface (k-summed tau within 1e-9 of FP64)"
+C1_WORKLOAD = ("c1: fcc(001) a = 6.8, lmax = 2, PL2 (n_PL = 18), 6-layer interface between identical bulks, "
+               "16 contour energies, 253-point IBZ meshes (nset 22), all energies and k points every step")
+
+
+def _c1_problems():
+    from skkr_budapest_gb300 import workloads as W
+    spec = W.plain_fcc()
+    return [W.energy_problem(spec, ie) for ie in range(len(spec.energies))]
+
+
+def run_c1(args):
+    """The plain non-relativistic interface (the reference's own CPU-sized
+    case): one step = the whole 16-energy contour with full meshes through
+    skkr_gpu_cpacoord with host buffers, FP64 and split precision; the error
+    of the k-summed tau of the split path against FP64."""
+    import torch
+    from skkr_budapest_gb300 import api
+    eps = _c1_problems()
+    out, tau = {}, {}
+    for prec in ("fp64", "mixed"):
+        ctx = api.Context.for_problem(eps[0], prec)
+        for _ in range(args.warmup):
+            for ep in eps:
+                ctx.cpacoord(ep)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        pts, dev = 0, 0.0
+        for _ in range(args.steps):
+            for ie, ep in enumerate(eps):
+                r = ctx.cpacoord(ep)
+                pts += ep.nk
+                dev += r["run_ms"]
+                tau[(prec, ie)] = r["tauc"]
+        torch.cuda.synchronize()
+        out[prec] = dict(wall=time.perf_counter() - t0, pts=pts, dev=dev)
+        ctx.close()
+    err = max(float(np.linalg.norm(tau[("mixed", ie)] - tau[("fp64", ie)]) / np.linalg.norm(tau[("fp64", ie)]))
+              for ie in range(len(eps)))
+    rate = {k: v["pts"] / (v["dev"] * 1e-3) for k, v in out.items()}
+    print(json.dumps({"metric": C1_METRIC, "value": rate["mixed"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+                      "warmup": args.warmup, "ms_per_step": out["mixed"]["dev"] / args.steps,
+                      "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                      "dtype": "c128 via BF16x6 slices + FP64 refinement", "data": "synthetic (seeded)",
+                      "config": {"workload": C1_WORKLOAD, "points_per_step": out["mixed"]["pts"] // args.steps},
+                      "fp64_value": rate["fp64"], "speedup": rate["mixed"] / rate["fp64"],
+                      "max_rel_err_tau_vs_fp64": err,
+                      "e2e": {"value": out["mixed"]["pts"] / out["mixed"]["wall"], "unit": UNIT,
+                              "fp64_value": out["fp64"]["pts"] / out["fp64"]["wall"],
+                              "h2d_bytes_per_step": None, "d2h_bytes_per_step": None}}), flush=True)
+
+
+def run_c1_reference(args):
+    """Reference arm of the plain interface: the oracle's CPA and k loop over
+    the whole contour with full meshes (no sample: the case runs on a CPU in
+    seconds), all host threads."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    nth = os.cpu_count() or 1
+    eps = _c1_problems()
+    for _ in range(args.warmup):
+        for ep in eps:
+            O.cpacoord(ep, nthreads=nth)
+    t0 = time.perf_counter()
+    pts = 0
+    for _ in range(args.steps):
+        for ep in eps:
+            if O.cpacoord(ep, nthreads=nth)["status"] != 0:
+                raise RuntimeError("oracle failed on the c1 workload")
+            pts += ep.nk
+    dt = time.perf_counter() - t0
+    v = pts / dt
+    print(json.dumps({"impl": "reference", "metric": C1_METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+                      "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+                      "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+                      "data": "synthetic (seeded)", "config": {"workload": C1_WORKLOAD},
+                      "cpu_baseline": {"value": v, "unit": UNIT, "cores": nth, "kind": "port",
+                                       "sample": "the whole workload, %d steps" % args.steps},
+                      "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}),
+          flush=True)
+
+
 C5_METRIC = "(E,k) points/s of the BdG interface (anomalous block within 1e-9 of FP64)"
 C5_ENERGIES = [8, 24, 40, 56]
 C5_NSET = 12
@@ -917,6 +1001,12 @@ def run_tauij(args):
 
 def main():
     args = parse()
+    if args.workload == "c1":
+        if args.impl == "reference":
+            run_c1_reference(args)
+        else:
+            run_c1(args)
+        return
     if args.workload == "c3":
         if args.impl == "reference":
             run_c3_reference(args)
