@@ -48,8 +48,13 @@ struct MatRef {
   int map[SKKR_MAPN];
 };
 
+// (the map entry by static selects: a dynamic index into a kernel
+// parameter's array would copy the whole MatRef to the thread's stack)
 __device__ inline zd *mat_ptr(const MatRef &m, int k, int c) {
-  return m.base + (long long)k * m.sk + (long long)m.map[c] * m.sc;
+  int mc = 0;
+#pragma unroll
+  for (int i = 0; i < SKKR_MAPN; i++) mc = i == c ? m.map[i] : mc;
+  return m.base + (long long)k * m.sk + (long long)mc * m.sc;
 }
 
 // host-side constructors

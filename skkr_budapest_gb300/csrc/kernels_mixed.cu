@@ -188,7 +188,7 @@ __device__ __forceinline__ float pow2f(int e) { return __int_as_float((127 + e) 
 // above, so that every FP32 level accumulator (at most 4 (p,q) pairs of
 // |d d| <= 2^(2DB-2) over K terms) stays an exact integer below 2^24.
 template <int S, int DB>
-__device__ __forceinline__ void slice_digits(double x, int es, float *dig) {
+__device__ __forceinline__ void slice_digits(double x, int es, int *dig) {
   static_assert(DB * S <= 62, "digits must fit the 62-bit fixed-point value");
   const long long Y = fix_round(x, (DB - 1) + DB * (S - 1) - es);
   const unsigned long long u = (unsigned long long)(Y < 0 ? -Y : Y);
@@ -200,32 +200,61 @@ __device__ __forceinline__ void slice_digits(double x, int es, float *dig) {
     int d = (int)((u >> (DB * q)) & ((1ull << DB) - 1)) + carry;
     carry = d > HALF;
     d -= carry << DB;
-    dig[S - 1 - q] = (float)(neg ? -d : d);
+    dig[S - 1 - q] = neg ? -d : d;
   }
 }
 
-template <int S, int DB>
-__device__ __forceinline__ void store_digits(const float *dig, float sign, int wshift, __nv_bfloat16 *dst,
-                                             long long sstride) {
-#pragma unroll
-  for (int p = 0; p < S; p++) dst[p * sstride] = __float2bfloat16_rn(sign * dig[p] * pow2f(wshift - DB * p));
+// float bits of d 2^k for an integer digit |d| <= 128, from one integer add
+// and one FMA: (1.5 2^23 + d) 2^k - 1.5 2^23 2^k is exact, and with at most
+// eight significant bits the value is a bf16 held in the upper half of the
+// float (zero digits give +0).  s = 2^k, off = -1.5 2^23 2^k.
+__device__ __forceinline__ uint32_t digit_bits(int d, float s, float off) {
+  return __float_as_uint(fmaf(__int_as_float(0x4B400000 + d), s, off));
 }
-
-template <int S, int DB>
-__device__ __forceinline__ void slice_store(double x, int es, int wshift, __nv_bfloat16 *dst,
-                                            long long sstride) {
-  float dig[S];
-  slice_digits<S, DB>(x, es, dig);
-  store_digits<S, DB>(dig, 1.0f, wshift, dst, sstride);
-}
+// the bf16 halves of two such floats as one word, a in the low half
+__device__ __forceinline__ uint32_t pack_bf16(uint32_t a, uint32_t b) { return __byte_perm(a, b, 0x7632); }
 
 // element (row r, K index kk) of one slice region in the k-block tiled layout
 __device__ __forceinline__ long long tiled(int r, int kk, int rows) {
   return ((long long)(kk >> 5) * rows + r) * 32 + (kk & 31);
 }
 
+// the slice words of four consecutive K indices of one row: w[p] holds the
+// bf16 values of digits dg[0..3][p] scaled by 2^(wshift - DB p)
+template <int S, int DB>
+__device__ __forceinline__ void pack4(const int (&dg)[4][S], int wshift, uint2 (&w)[S]) {
+#pragma unroll
+  for (int p = 0; p < S; p++) {
+    const float sc = pow2f(wshift - DB * p), off = -12582912.0f * sc;
+    w[p].x = pack_bf16(digit_bits(dg[0][p], sc, off), digit_bits(dg[1][p], sc, off));
+    w[p].y = pack_bf16(digit_bits(dg[2][p], sc, off), digit_bits(dg[3][p], sc, off));
+  }
+}
+// the S words at dst + p sstride, sign bits flipped by `flip` (0 or 0x80008000)
+template <int S>
+__device__ __forceinline__ void store_words(const uint2 (&w)[S], uint32_t flip, __nv_bfloat16 *dst,
+                                            long long sstride) {
+#pragma unroll
+  for (int p = 0; p < S; p++)
+    *reinterpret_cast<uint2 *>(dst + p * sstride) = make_uint2(w[p].x ^ flip, w[p].y ^ flip);
+}
+// one element, slices p = 0..S-1 (the shapes pack4 does not cover)
+template <int S, int DB>
+__device__ __forceinline__ void store1(const int (&dg)[S], int wshift, uint16_t flip, __nv_bfloat16 *dst,
+                                       long long sstride) {
+#pragma unroll
+  for (int p = 0; p < S; p++) {
+    const float sc = pow2f(wshift - DB * p);
+    const uint16_t h = (uint16_t)(digit_bits(dg[p], sc, -12582912.0f * sc) >> 16) ^ flip;
+    *reinterpret_cast<uint16_t *>(dst + p * sstride) = h;
+  }
+}
+
 // A' = [Re A, Im A] (n x 2K) from the n x K complex A; rows scaled by their
-// max over these K columns
+// max over these K columns.  32 rows per block: the row maxima, then 32 x 32
+// tiles transposed through shared memory, each thread taking four
+// consecutive columns of one row (8-byte stores of every slice) when K is a
+// multiple of four, one element otherwise.
 template <int S, int DB>
 __global__ void __launch_bounds__(256) k_split_a(MatRef A, int n, int K, int nc, const int *__restrict__ act,
                                                  __nv_bfloat16 *__restrict__ out, int Mp, int Kp,
@@ -258,19 +287,43 @@ __global__ void __launch_bounds__(256) k_split_a(MatRef A, int n, int K, int nc,
   __syncthreads();
   const long long sstride = (long long)Mp * Kp;
   __nv_bfloat16 *base = out + (long long)item * S * sstride;
+  const bool vec = (K & 3) == 0;
   for (int c0 = 0; c0 < K; c0 += 32) {
     for (int q = w; q < 32; q += 8) {
       int col = c0 + q;
       T[lane][q] = (row < n && col < K) ? a[row + (long long)col * A.ld] : make_double2(0.0, 0.0);
     }
     __syncthreads();
-    for (int q = w; q < 32; q += 8) {
-      const int r = r0 + q, col = c0 + lane;
+    if (vec) {
+      // thread t: row r0 + t / 8, columns c0 + 4 (t % 8) .. +3
+      const int q = threadIdx.x >> 3, c4 = (threadIdx.x & 7) * 4, r = r0 + q, col = c0 + c4;
       if (r < n && col < K) {
         const int es = sc[q];
-        zd v = T[q][lane];
-        slice_store<S, DB>(v.x, es, 0, base + tiled(r, col, Mp), sstride);
-        slice_store<S, DB>(v.y, es, 0, base + tiled(r, K + col, Mp), sstride);
+        int dr[4][S], di[4][S];
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+          const zd v = T[q][c4 + e];
+          slice_digits<S, DB>(v.x, es, dr[e]);
+          slice_digits<S, DB>(v.y, es, di[e]);
+        }
+        uint2 wr[S], wi[S];
+        pack4<S, DB>(dr, 0, wr);
+        pack4<S, DB>(di, 0, wi);
+        store_words<S>(wr, 0u, base + tiled(r, col, Mp), sstride);
+        store_words<S>(wi, 0u, base + tiled(r, K + col, Mp), sstride);
+      }
+    } else {
+      for (int q = w; q < 32; q += 8) {
+        const int r = r0 + q, col = c0 + lane;
+        if (r < n && col < K) {
+          const int es = sc[q];
+          const zd v = T[q][lane];
+          int dr[S], di[S];
+          slice_digits<S, DB>(v.x, es, dr);
+          slice_digits<S, DB>(v.y, es, di);
+          store1<S, DB>(dr, 0, 0, base + tiled(r, col, Mp), sstride);
+          store1<S, DB>(di, 0, 0, base + tiled(r, K + col, Mp), sstride);
+        }
       }
     }
     __syncthreads();
@@ -280,7 +333,10 @@ __global__ void __launch_bounds__(256) k_split_a(MatRef A, int n, int K, int nc,
 // B'^T from the K x n complex B: one warp per column j; rows 2j and 2j+1 of
 // B'^T are [Re B(:,j), -Im B(:,j)] and [Im B(:,j), Re B(:,j)] (columns scaled
 // by their max over these K rows), so that the real and imaginary parts of an
-// output element land in adjacent accumulator columns of one thread
+// output element land in adjacent accumulator columns of one thread.  Each
+// lane takes four consecutive rows k (8-byte stores) when K is a multiple of
+// four, one row otherwise; each digit is formed once and stored twice, -Im
+// with its sign bit flipped.
 template <int S, int DB>
 __global__ void __launch_bounds__(256) k_split_b(MatRef B, int n, int K, int nc, const int *__restrict__ act,
                                                  __nv_bfloat16 *__restrict__ out, int Np, int Kp,
@@ -306,22 +362,33 @@ __global__ void __launch_bounds__(256) k_split_b(MatRef B, int n, int K, int nc,
   if (lane == 0) tau[(long long)item * n + j] = es;
   const long long sstride = (long long)Np * Kp;
   __nv_bfloat16 *base = out + (long long)item * S * sstride;
-  for (int k = lane; k < K; k += 32) {
-    zd v = b[k];
-    float dr[S], di[S];
-    slice_digits<S, DB>(v.x, es, dr);
-    slice_digits<S, DB>(v.y, es, di);
-    // each digit is converted once and stored twice; -Im is the sign bit flipped
-    __nv_bfloat16 *o0 = base + tiled(2 * j, k, Np), *o1 = base + tiled(2 * j, K + k, Np);
-    __nv_bfloat16 *o2 = base + tiled(2 * j + 1, k, Np), *o3 = base + tiled(2 * j + 1, K + k, Np);
+  if ((K & 3) == 0) {
+    for (int k = 4 * lane; k < K; k += 128) {
+      int dr[4][S], di[4][S];
 #pragma unroll
-    for (int p = 0; p < S; p++) {
-      const float sc = pow2f(16 - DB * p);
-      const __nv_bfloat16 br = __float2bfloat16_rn(dr[p] * sc), bi = __float2bfloat16_rn(di[p] * sc);
-      o0[p * sstride] = br;
-      o1[p * sstride] = __hneg(bi);
-      o2[p * sstride] = bi;
-      o3[p * sstride] = br;
+      for (int e = 0; e < 4; e++) {
+        const zd v = b[k + e];
+        slice_digits<S, DB>(v.x, es, dr[e]);
+        slice_digits<S, DB>(v.y, es, di[e]);
+      }
+      uint2 wr[S], wi[S];
+      pack4<S, DB>(dr, 16, wr);
+      pack4<S, DB>(di, 16, wi);
+      store_words<S>(wr, 0u, base + tiled(2 * j, k, Np), sstride);
+      store_words<S>(wi, 0x80008000u, base + tiled(2 * j, K + k, Np), sstride);
+      store_words<S>(wi, 0u, base + tiled(2 * j + 1, k, Np), sstride);
+      store_words<S>(wr, 0u, base + tiled(2 * j + 1, K + k, Np), sstride);
+    }
+  } else {
+    for (int k = lane; k < K; k += 32) {
+      const zd v = b[k];
+      int dr[S], di[S];
+      slice_digits<S, DB>(v.x, es, dr);
+      slice_digits<S, DB>(v.y, es, di);
+      store1<S, DB>(dr, 16, 0, base + tiled(2 * j, k, Np), sstride);
+      store1<S, DB>(di, 16, 0x8000, base + tiled(2 * j, K + k, Np), sstride);
+      store1<S, DB>(di, 16, 0, base + tiled(2 * j + 1, k, Np), sstride);
+      store1<S, DB>(dr, 16, 0, base + tiled(2 * j + 1, K + k, Np), sstride);
     }
   }
 }
@@ -520,11 +587,26 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_ozaki(const __grid_constant__
     double *pd = (double *)mat_ptr(g.D, kk, cc);
     double *pe = (double *)mat_ptr(g.E, kk, cc);
     constexpr int NL = nlevels<NA>(S);
+    // modes that read the old C (1, 5) or D (2, 3) load the chunk's eight
+    // elements of it first, so that the loads are in flight together
+    const bool rd_c = g.mode == 1 || g.mode == 5, rd_d = g.mode == 2 || g.mode == 3;
+    const double2 *src = (const double2 *)(rd_c ? pc : pd);
+    const long long sld = rd_c ? g.C.ld : g.D.ld;
 #pragma unroll 1
     for (int c0 = part * 16; c0 < TN; c0 += 3 * 16) {
       uint32_t v[NA][16];
 #pragma unroll
       for (int l = 0; l < NL; l++) tmem_ld16(lane_addr + l * TN + c0, v[l]);
+      // (the seven-accumulator tile has no registers to spare for it)
+      constexpr bool PF = NA <= 5;
+      double2 old[PF ? 8 : 1];
+      if (PF && row < g.n && (rd_c || rd_d)) {
+#pragma unroll
+        for (int t = 0; t < 16; t += 2) {
+          const int j = (nt * TN + c0 + t) >> 1;
+          if (j < g.n) old[PF ? t >> 1 : 0] = src[row + (long long)j * sld];
+        }
+      }
       tmem_ld_wait();
       if (row >= g.n) continue;
 #pragma unroll
@@ -542,24 +624,29 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_ozaki(const __grid_constant__
           const int e = erow + col_exp[(c0 + t) >> 1];
           const double2 val = make_double2(fix_to_double(ar, e), fix_to_double(ai, e));
           double2 *oc = (double2 *)pc + row + (long long)j * g.C.ld;
+          double2 *od = (double2 *)pd + row + (long long)j * g.D.ld;
+          const int q = t >> 1;
+          double2 o = make_double2(0.0, 0.0);  // the old C or D of this element
+          if constexpr (PF) {
+            o = old[q];
+          } else {
+            if (g.mode == 1 || g.mode == 5) o = *oc;
+            if (g.mode == 2 || g.mode == 3) o = *od;
+          }
           if (g.mode == 0) {
             *oc = val;
           } else if (g.mode == 1) {
-            const double2 o = *oc;
             *oc = make_double2(o.x - val.x, o.y - val.y);
           } else if (g.mode == 2) {
-            double2 *od = (double2 *)pd + row + (long long)j * g.D.ld;
             double2 *oe = (double2 *)pe + row + (long long)j * g.E.ld;
-            const double2 d = *od, x = *oe;
-            *od = make_double2(d.x - val.x, d.y - val.y);
+            const double2 x = *oe;
+            *od = make_double2(o.x - val.x, o.y - val.y);
             *oe = make_double2(x.x - val.x, x.y - val.y);
           } else if (g.mode == 3) {
-            const double2 d = ((const double2 *)pd)[row + (long long)j * g.D.ld];
-            *oc = make_double2(d.x - val.x, d.y - val.y);
+            *oc = make_double2(o.x - val.x, o.y - val.y);
           } else if (g.mode == 4) {
             *oc = make_double2((row == j ? 1.0 : 0.0) - val.x, -val.y);
           } else {
-            const double2 o = *oc;
             *oc = make_double2(o.x + val.x, o.y + val.y);
           }
         }
