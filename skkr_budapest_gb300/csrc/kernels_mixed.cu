@@ -219,15 +219,18 @@ __device__ __forceinline__ long long tiled(int r, int kk, int rows) {
   return ((long long)(kk >> 5) * rows + r) * 32 + (kk & 31);
 }
 
-// the slice words of four consecutive K indices of one row: w[p] holds the
-// bf16 values of digits dg[0..3][p] scaled by 2^(wshift - DB p)
+// element e (0..3) of four consecutive K indices of one row into the slice
+// words w[p]: the bf16 of digit dg[p] scaled by 2^(wshift - DB p) in half
+// e % 2 of word w[p].x (e < 2) or w[p].y; the words start at zero
 template <int S, int DB>
-__device__ __forceinline__ void pack4(const int (&dg)[4][S], int wshift, uint2 (&w)[S]) {
+__device__ __forceinline__ void pack_elem(const int (&dg)[S], int e, int wshift, uint2 (&w)[S]) {
 #pragma unroll
   for (int p = 0; p < S; p++) {
-    const float sc = pow2f(wshift - DB * p), off = -12582912.0f * sc;
-    w[p].x = pack_bf16(digit_bits(dg[0][p], sc, off), digit_bits(dg[1][p], sc, off));
-    w[p].y = pack_bf16(digit_bits(dg[2][p], sc, off), digit_bits(dg[3][p], sc, off));
+    const float sc = pow2f(wshift - DB * p);
+    const uint32_t u = digit_bits(dg[p], sc, -12582912.0f * sc);
+    const uint32_t h = (e & 1) ? (u & 0xFFFF0000u) : (u >> 16);
+    if (e < 2) w[p].x |= h;
+    else w[p].y |= h;
   }
 }
 // the S words at dst + p sstride, sign bits flipped by `flip` (0 or 0x80008000)
@@ -238,7 +241,7 @@ __device__ __forceinline__ void store_words(const uint2 (&w)[S], uint32_t flip, 
   for (int p = 0; p < S; p++)
     *reinterpret_cast<uint2 *>(dst + p * sstride) = make_uint2(w[p].x ^ flip, w[p].y ^ flip);
 }
-// one element, slices p = 0..S-1 (the shapes pack4 does not cover)
+// one element, slices p = 0..S-1 (the shapes of no four-element group)
 template <int S, int DB>
 __device__ __forceinline__ void store1(const int (&dg)[S], int wshift, uint16_t flip, __nv_bfloat16 *dst,
                                        long long sstride) {
@@ -299,16 +302,18 @@ __global__ void __launch_bounds__(256) k_split_a(MatRef A, int n, int K, int nc,
       const int q = threadIdx.x >> 3, c4 = (threadIdx.x & 7) * 4, r = r0 + q, col = c0 + c4;
       if (r < n && col < K) {
         const int es = sc[q];
-        int dr[4][S], di[4][S];
+        uint2 wr[S], wi[S];
+#pragma unroll
+        for (int p = 0; p < S; p++) wr[p] = wi[p] = make_uint2(0u, 0u);
 #pragma unroll
         for (int e = 0; e < 4; e++) {
           const zd v = T[q][c4 + e];
-          slice_digits<S, DB>(v.x, es, dr[e]);
-          slice_digits<S, DB>(v.y, es, di[e]);
+          int dr[S], di[S];
+          slice_digits<S, DB>(v.x, es, dr);
+          slice_digits<S, DB>(v.y, es, di);
+          pack_elem<S, DB>(dr, e, 0, wr);
+          pack_elem<S, DB>(di, e, 0, wi);
         }
-        uint2 wr[S], wi[S];
-        pack4<S, DB>(dr, 0, wr);
-        pack4<S, DB>(di, 0, wi);
         store_words<S>(wr, 0u, base + tiled(r, col, Mp), sstride);
         store_words<S>(wi, 0u, base + tiled(r, K + col, Mp), sstride);
       }
@@ -338,7 +343,7 @@ __global__ void __launch_bounds__(256) k_split_a(MatRef A, int n, int K, int nc,
 // four, one row otherwise; each digit is formed once and stored twice, -Im
 // with its sign bit flipped.
 template <int S, int DB>
-__global__ void __launch_bounds__(256) k_split_b(MatRef B, int n, int K, int nc, const int *__restrict__ act,
+__global__ void __launch_bounds__(256, 3) k_split_b(MatRef B, int n, int K, int nc, const int *__restrict__ act,
                                                  __nv_bfloat16 *__restrict__ out, int Np, int Kp,
                                                  int *__restrict__ tau) {
   const int item = blockIdx.y, kk0 = item / nc, cc = item % nc;
@@ -364,16 +369,18 @@ __global__ void __launch_bounds__(256) k_split_b(MatRef B, int n, int K, int nc,
   __nv_bfloat16 *base = out + (long long)item * S * sstride;
   if ((K & 3) == 0) {
     for (int k = 4 * lane; k < K; k += 128) {
-      int dr[4][S], di[4][S];
+      uint2 wr[S], wi[S];
+#pragma unroll
+      for (int p = 0; p < S; p++) wr[p] = wi[p] = make_uint2(0u, 0u);
 #pragma unroll
       for (int e = 0; e < 4; e++) {
         const zd v = b[k + e];
-        slice_digits<S, DB>(v.x, es, dr[e]);
-        slice_digits<S, DB>(v.y, es, di[e]);
+        int dr[S], di[S];
+        slice_digits<S, DB>(v.x, es, dr);
+        slice_digits<S, DB>(v.y, es, di);
+        pack_elem<S, DB>(dr, e, 16, wr);
+        pack_elem<S, DB>(di, e, 16, wi);
       }
-      uint2 wr[S], wi[S];
-      pack4<S, DB>(dr, 16, wr);
-      pack4<S, DB>(di, 16, wi);
       store_words<S>(wr, 0u, base + tiled(2 * j, k, Np), sstride);
       store_words<S>(wi, 0x80008000u, base + tiled(2 * j, K + k, Np), sstride);
       store_words<S>(wi, 0u, base + tiled(2 * j + 1, k, Np), sstride);
