@@ -526,8 +526,9 @@ def bsf_radial(ep):
 
 
 def _lms_pairs(lmax: int):
-    """(lm, lm', m) of the lm pairs with l = l' and m = -m' (main/pairing.f's
-    selection), lm in the order l = 0..lmax, m = -l..l."""
+    """(lm, lm', m) of the lm pairs with l = l' and m = -m' (the selection of
+    skkr_dbogo_bsf/rsp-scf/pairing.f:46-200), lm in the order l = 0..lmax,
+    m = -l..l."""
     out = []
     lm = 0
     for l in range(lmax + 1):
@@ -538,11 +539,11 @@ def _lms_pairs(lmax: int):
 
 
 def pairing_kmy(lmax: int) -> dict:
-    """The four pairing operators of rsp-scf/pairing.f in the (kappa,mu)
+    """The four pairing operators of rsp-scf/pairing.f:46-200 in the (kappa,mu)
     basis: singlet (i sigma_y), triplet with unequal spins (T0), and the
     equal-spin triplets (up, down), each built in the (l, m, s)
     representation on l = l', m = -m' and taken to (kappa,mu) with the
-    Clebsch-Gordan matrix as rsp-scf/matlms.f matkmy does (U^T X U, no
+    Clebsch-Gordan matrix as rsp-scf/matlms.f:93-126 (matkmy) does (U^T X U, no
     conjugation; spin index 1 of the reference pairs with u1)."""
     lmmax = (lmax + 1) ** 2
     U = clebsch_u(lmax)
