@@ -146,6 +146,13 @@ int skkr_gpu_set_mixed_policy(skkr_ctx *ctx, double dec_fp64_im, double near_im,
  * whose FP32 start is already that close. */
 int skkr_gpu_set_newton(skkr_ctx *ctx, int steps);
 
+/* The FP32 start of split-precision inverses above 64 rows: blocked != 0
+ * (the default) forms it by 2 x 2 blocks (two 64-row Gauss-Jordan inverses
+ * with pivoting inside each block, six FP32 block products); 0 runs the
+ * Gauss-Jordan of main/gjinv.f's column pivoting on the whole matrix.  The
+ * Newton steps, their acceptance test and the FP64 redo are the same. */
+int skkr_gpu_set_inverse_start(skkr_ctx *ctx, int blocked);
+
 /* Autotuner of the split-precision inverse's FP32 Gauss-Jordan: each size
  * class (n <= 32, 64, 128) has 2-3 thread layouts that give the same inverse
  * bit for bit; the first batch of each (class, batch size) times them once

@@ -60,6 +60,11 @@ class Context:
         """Standard Newton steps of the split-precision inverse (skkr_gpu_set_newton)."""
         N._check(N.lib().skkr_gpu_set_newton(self.h, int(steps)), "skkr_gpu_set_newton")
 
+    def set_inverse_start(self, blocked=True):
+        """FP32 start of split-precision inverses above 64 rows: 2 x 2 blocks
+        (default) or the whole-matrix Gauss-Jordan (skkr_gpu_set_inverse_start)."""
+        N._check(N.lib().skkr_gpu_set_inverse_start(self.h, 1 if blocked else 0), "skkr_gpu_set_inverse_start")
+
     def set_graphs(self, on=True):
         """Decimation loop as one CUDA graph launch per k chunk (the default)
         or one host-driven iteration at a time (skkr_gpu_set_graphs)."""

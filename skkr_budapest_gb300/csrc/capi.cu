@@ -385,6 +385,7 @@ struct skkr_ctx {
   double alg_units = 0.0;       // reference block operations (8 n^3 FLOP each) of this run
   bool graphs = true;           // decimation loop as a CUDA graph WHILE node (skkr_gpu_set_graphs)
   int newton = 2;               // standard Newton steps of the split-precision inverse (skkr_gpu_set_newton)
+  int blocked_start = 1;        // 2 x 2 block FP32 start above 64 rows (skkr_gpu_set_inverse_start)
   DBuf decctl;                  // [0] iteration, [1] items left, [2] half-bodies run (captured loop)
   long long graph_kernels = 0;  // kernels run inside graphs in this run
   long long graph_launches = 0; // graph launches in this run
@@ -838,9 +839,11 @@ static int eng_gemm(skkr_ctx *c, bool mixed, int mode, const MatRef &A, const Ma
 // X = A^-1 (X may be the same matrices as A when inplace)
 static int eng_inv(skkr_ctx *c, bool mixed, const MatRef &A, const MatRef &X, bool inplace, int n, int nk,
                    int nc, const int *act) {
-  if (mixed && n <= 128)
+  if (mixed && n <= 128) {
+    mixed_set_blocked(c->mw, c->blocked_start != 0);
     return mixed_zinv(c->mw, A, X, n, nk, nc, act, c->newton,
                       std::min(8, std::max(c->slices_res, slices_for(c) + 1)), inplace, c->st);
+  }
   if (!inplace) launch_zaxpby(X, A, nullptr, 0, nullptr, 0, n, nk, nc, act, c->st);
   launch_zgj(X, n, nk, nc, act, c->st);
   return SKKR_OK;
@@ -1718,6 +1721,12 @@ extern "C" int skkr_gpu_autotune(int force, char *report, int len) {
 extern "C" int skkr_gpu_set_newton(skkr_ctx *c, int steps) {
   if (!c || steps < 1 || steps > 3) return SKKR_ERR_ARG;
   c->newton = steps;
+  return SKKR_OK;
+}
+
+extern "C" int skkr_gpu_set_inverse_start(skkr_ctx *c, int blocked) {
+  if (!c) return SKKR_ERR_ARG;
+  c->blocked_start = blocked != 0;
   return SKKR_OK;
 }
 

@@ -67,6 +67,12 @@ inline MatRef mref(zd *base, long long sk, long long sc, int ld) {
   for (int i = 0; i < SKKR_MAPN; i++) r.map[i] = i;
   return r;
 }
+// the same batch operand moved by `elems` elements (a sub-block of every item)
+inline MatRef mref_offset(const MatRef &m, long long elems) {
+  MatRef r = m;
+  r.base += elems;
+  return r;
+}
 inline MatRef mref_map(zd *base, long long sk, long long sc, int ld, const int *map, int nmap) {
   MatRef r = mref(base, sk, sc, ld);
   for (int i = 0; i < nmap && i < SKKR_MAPN; i++) r.map[i] = map[i];

@@ -748,8 +748,11 @@ __device__ __forceinline__ void gj_search(const unsigned long long (&m)[RA][RB],
   if (tx == 0) *kp_out = bj;
 }
 
-template <int TY, int RA, int RB>
-__global__ void __launch_bounds__(TY * 16, 1) k_cgj32(MatRef A, MatRef X, int n, int nc,
+// MINB: blocks per SM the register allocation must allow (the 64-row
+// layouts run several matrices per SM, each block's barrier latency hidden by
+// the others)
+template <int TY, int RA, int RB, int MINB = 1>
+__global__ void __launch_bounds__(TY * 16, MINB) k_cgj32(MatRef A, MatRef X, int n, int nc,
                                                       const int *__restrict__ act) {
   constexpr int NR = TY * RA, NCOL = 16 * RB;
   const int item = blockIdx.x, kk = item / nc, cc = item % nc;
@@ -842,6 +845,88 @@ __global__ void __launch_bounds__(TY * 16, 1) k_cgj32(MatRef A, MatRef X, int n,
     }
 }
 
+// ------------------------------------------------------------------ FP32 block products
+// C = A B (m x n, depth k; m, n, k <= 64) of one item per block in complex
+// FP32 from FP64 operands, for the 2 x 2 block start of the split-precision
+// inverse: MODE 0 C = AB, 1 C = D - AB (D read in FP64), 2 C = -AB.  The
+// 16 x 16 threads each hold 4 x 4 outputs (rows ty + 16 i, columns tx + 16 j);
+// the operands pass through shared memory in K chunks of 32, converted to
+// FP32 on the way; the sums run in a fixed order.
+template <int MODE>
+__global__ void __launch_bounds__(256, 2) k_cgemm32(MatRef A, MatRef B, MatRef C, MatRef D, int m, int n, int k,
+                                                 int nc, const int *__restrict__ act) {
+  const int item = blockIdx.x, kk = item / nc, cc = item % nc;
+  if (act && !act[item]) return;
+  __shared__ float2 As[32][64];  // [K index][row]
+  __shared__ float2 Bs[32][65];  // [K index][column], padded against store conflicts
+  const zd *a = mat_ptr(A, kk, cc), *b = mat_ptr(B, kk, cc);
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  float2 acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; i++)
+#pragma unroll
+    for (int j = 0; j < 4; j++) acc[i][j] = make_float2(0.f, 0.f);
+  for (int k0 = 0; k0 < k; k0 += 32) {
+    for (int e = threadIdx.x; e < 64 * 32; e += 256) {
+      const int r = e & 63, q = e >> 6, col = k0 + q;
+      const zd v = (r < m && col < k) ? a[r + (long long)col * A.ld] : make_double2(0.0, 0.0);
+      As[q][r] = make_float2((float)v.x, (float)v.y);
+    }
+    for (int e = threadIdx.x; e < 32 * 64; e += 256) {
+      const int q = e & 31, c = e >> 5, row = k0 + q;
+      const zd v = (row < k && c < n) ? b[row + (long long)c * B.ld] : make_double2(0.0, 0.0);
+      Bs[q][c] = make_float2((float)v.x, (float)v.y);
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int q = 0; q < 32; q++) {
+      float2 av[4], bv[4];
+#pragma unroll
+      for (int i = 0; i < 4; i++) av[i] = As[q][ty + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; j++) bv[j] = Bs[q][tx + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          acc[i][j].x = fmaf(av[i].x, bv[j].x, acc[i][j].x);
+          acc[i][j].x = fmaf(-av[i].y, bv[j].y, acc[i][j].x);
+          acc[i][j].y = fmaf(av[i].x, bv[j].y, acc[i][j].y);
+          acc[i][j].y = fmaf(av[i].y, bv[j].x, acc[i][j].y);
+        }
+    }
+    __syncthreads();
+  }
+  zd *c = mat_ptr(C, kk, cc);
+  const zd *d = MODE == 1 ? mat_ptr(D, kk, cc) : nullptr;
+#pragma unroll
+  for (int i = 0; i < 4; i++)
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      const int r = ty + 16 * i, col = tx + 16 * j;
+      if (r < m && col < n) {
+        const zd p = make_double2((double)acc[i][j].x, (double)acc[i][j].y);
+        zd o;
+        if (MODE == 0) o = p;
+        else if (MODE == 1) {
+          const zd dv = d[r + (long long)col * D.ld];
+          o = make_double2(dv.x - p.x, dv.y - p.y);
+        } else o = make_double2(-p.x, -p.y);
+        c[r + (long long)col * C.ld] = o;
+      }
+    }
+}
+
+static void cgemm32(int mode, const MatRef &A, const MatRef &B, const MatRef &C, const MatRef &D, int m, int n,
+                    int k, int nc, const int *act, unsigned items, cudaStream_t st) {
+  switch (mode) {
+    case 0: k_cgemm32<0><<<items, 256, 0, st>>>(A, B, C, D, m, n, k, nc, act); break;
+    case 1: k_cgemm32<1><<<items, 256, 0, st>>>(A, B, C, D, m, n, k, nc, act); break;
+    default: k_cgemm32<2><<<items, 256, 0, st>>>(A, B, C, D, m, n, k, nc, act); break;
+  }
+  SKKR_LAUNCHED();
+}
+
 // ------------------------------------------------------------------ host side
 
 // resolved once per process (thread-safe static initialisation: contexts may
@@ -915,9 +1000,11 @@ struct MixedWork {
   cudaStream_t side = nullptr;         // captures the bodies of conditional graph nodes
   int smem_set[32] = {0};
   bool precise = false;    // (64, 7) tile: exact levels 0..5 (mixed_set_precise)
+  bool blocked = true;     // 2 x 2 block start of inverses above 64 rows (mixed_set_blocked)
 };
 
 void mixed_set_precise(MixedWork *w, bool on) { w->precise = on; }
+void mixed_set_blocked(MixedWork *w, bool on) { w->blocked = on; }
 
 // the (64, 7) tile serves products of 6 slices and more (the low-slice
 // Newton corrections keep the default tile); split and multiply agree on it
@@ -1308,10 +1395,10 @@ bool stream_capturing(cudaStream_t st) {
 // before a key is tuned takes the first layout.
 using GjLaunch = void (*)(const MatRef &, const MatRef &, int, int, const int *, unsigned, cudaStream_t);
 
-template <int TY, int RA, int RB>
+template <int TY, int RA, int RB, int MINB = 1>
 static void gj_launch(const MatRef &A, const MatRef &X, int n, int nc, const int *act, unsigned items,
                       cudaStream_t st) {
-  k_cgj32<TY, RA, RB><<<items, TY * 16, 0, st>>>(A, X, n, nc, act);
+  k_cgj32<TY, RA, RB, MINB><<<items, TY * 16, 0, st>>>(A, X, n, nc, act);
 }
 
 struct GjClass {
@@ -1323,7 +1410,7 @@ struct GjClass {
 
 static const GjClass GJ_CLASSES[3] = {
     {32, 3, {gj_launch<16, 2, 2>, gj_launch<32, 1, 2>, gj_launch<8, 4, 2>}, {"16x2x2", "32x1x2", "8x4x2"}},
-    {64, 3, {gj_launch<16, 4, 4>, gj_launch<32, 2, 4>, gj_launch<64, 1, 4>}, {"16x4x4", "32x2x4", "64x1x4"}},
+    {64, 3, {gj_launch<16, 4, 4, 3>, gj_launch<32, 2, 4, 2>, gj_launch<64, 1, 4>}, {"16x4x4 (3/SM)", "32x2x4 (2/SM)", "64x1x4"}},
     {128, 2, {gj_launch<32, 4, 8>, gj_launch<64, 2, 8>, nullptr}, {"32x4x8", "64x2x8", ""}},
 };
 
@@ -1388,6 +1475,42 @@ std::string gj_tune_report() {
   return r;
 }
 
+// The FP32 start of an inverse above 64 rows by the 2 x 2 block form: with
+// A = [[A11, A12], [A21, A22]], A11 64 x 64,
+//   X11 = A11^-1, U = X11 A12, S = A22 - A21 U, Y = S^-1, T = A21 X11,
+//   A^-1 = [[X11 - X12 T, X12], [-Y T, Y]],  X12 = -U Y,
+// the two diagonal inverses by the FP32 Gauss-Jordan (pivoting inside each
+// block) at 64 rows, where several matrices share an SM, and the six
+// products by k_cgemm32.  Without pivoting across the blocks the start is
+// a few times less accurate than the whole-matrix Gauss-Jordan on the
+// path's matrices; the Newton steps and their acceptance test are the same.
+// `scratch` holds n^2 elements per item (X11, U, S, T).
+static void block_start(const MatRef &A, const MatRef &X, int n, int nc, const int *act, unsigned items,
+                        zd *scratch, cudaStream_t st) {
+  const int b = 64, n2 = n - 64;
+  const long long MB = (long long)n * n;
+  auto sub = [&](const MatRef &M, int r, int c) { return mref_offset(M, r + (long long)c * M.ld); };
+  auto scr = [&](long long off, int ld) { return mref(scratch + off, (long long)nc * MB, MB, ld); };
+  const MatRef X11 = scr(0, b), U = scr((long long)b * b, b), S = scr((long long)b * b + (long long)b * n2, n2),
+               T = scr((long long)b * b + (long long)b * n2 + (long long)n2 * n2, n2);
+  const MatRef A11 = A, A12 = sub(A, 0, b), A21 = sub(A, b, 0), A22 = sub(A, b, b);
+  const MatRef Xa = X, X12 = sub(X, 0, b), X21 = sub(X, b, 0), X22 = sub(X, b, b);
+  const GjLaunch g1 = gj_choose(b, items, A11, X11, nc, act, st);
+  g1(A11, X11, b, nc, act, items, st);
+  SKKR_LAUNCHED();
+  cgemm32(0, X11, A12, U, U, b, n2, b, nc, act, items, st);    // U = X11 A12
+  cgemm32(1, A21, U, S, A22, n2, n2, b, nc, act, items, st);   // S = A22 - A21 U
+  // Y = S^-1 straight into its place in X (the layout autotuner may run its
+  // candidates on these operands: S is never overwritten)
+  const GjLaunch g2 = gj_choose(n2, items, S, X22, nc, act, st);
+  g2(S, X22, n2, nc, act, items, st);
+  SKKR_LAUNCHED();
+  cgemm32(0, A21, X11, T, T, n2, b, b, nc, act, items, st);      // T = A21 X11
+  cgemm32(2, U, X22, X12, X12, b, n2, n2, nc, act, items, st);   // X12 = -U Y
+  cgemm32(2, X22, T, X21, X21, n2, b, n2, nc, act, items, st);   // X21 = -Y T
+  cgemm32(1, X12, T, Xa, X11, b, b, n2, nc, act, items, st);     // X11 - X12 T
+}
+
 // X = A^-1: FP32 Gauss-Jordan, then `newton` steps X += X (I - A X) with the
 // residual product at S = sres slices and the correction at S = 3.  X may be
 // A itself (`inplace`); otherwise the two must not overlap.
@@ -1421,11 +1544,15 @@ int mixed_zinv(MixedWork *w, const MatRef &A, const MatRef &X, int n, int nk, in
   const MatRef Ac = inplace ? mref(w->acopy, (long long)nc * MB, MB, n) : A;
   MatRef R = mref(w->rbuf, (long long)nc * MB, MB, n);
   if (inplace) launch_zaxpby(Ac, A, nullptr, 0, nullptr, 0, n, nk, nc, act, st);
-  const GjLaunch gj = gj_choose(n, items, Ac, X, nc, act, st);
   kstat_begin(KS_GJ, 8.0 * n * (double)n * n * (double)(act ? skkr_active_items(items) : items), st);
-  gj(Ac, X, n, nc, act, (unsigned)items, st);
+  if (w->blocked && n > 64) {
+    block_start(Ac, X, n, nc, act, (unsigned)items, w->rbuf, st);
+  } else {
+    const GjLaunch gj = gj_choose(n, items, Ac, X, nc, act, st);
+    gj(Ac, X, n, nc, act, (unsigned)items, st);
+    SKKR_LAUNCHED();
+  }
   kstat_end(st);
-  SKKR_LAUNCHED();
   // A is split once (A slot 0) for the residuals of every Newton step
   if ((rc = mixed_split(w, 0, 0, sres, Ac, n, n, nk, nc, act, st))) return rc;
   for (int it = 0; it < newton; it++) {

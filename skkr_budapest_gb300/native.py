@@ -90,6 +90,7 @@ def lib():
         L.skkr_gpu_set_mixed_policy.argtypes = [P, D, D, I, D]
         L.skkr_gpu_set_graphs.argtypes = [P, I]
         L.skkr_gpu_set_newton.argtypes = [P, I]
+        L.skkr_gpu_set_inverse_start.argtypes = [P, I]
         L.skkr_gpu_stage_kambe.argtypes = [P, P]
         L.skkr_gpu_cpacoord_many.argtypes = [I, P, P, P]
         L.skkr_gpu_contour.argtypes = [P, I, P, P]

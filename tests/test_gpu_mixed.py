@@ -140,3 +140,38 @@ def test_gauss_jordan_layouts_are_bit_identical(n):
     tuned = native.zinv_batch(a, "mixed")[0]
     assert np.array_equal(tuned, outs[0])
     assert "n<=" in native.autotune(report=True)
+
+
+@pytest.mark.parametrize("n", [65, 96, 100, 128])
+def test_mixed_inverse_blocked_start_sizes(n):
+    """Inverses above 64 rows start from the 2 x 2 block form (a 64-row
+    leading block, the rest n - 64): refined to FP64 accuracy at every split
+    (1e-11 against numpy's inverse: these random matrices reach condition
+    numbers of a few hundred, and both inverses carry cond x 1e-16)."""
+    a = crand(6, n, n) + 3 * np.eye(n)
+    x, resid = native.zinv_batch(a, precision="mixed", newton=2)
+    for i in range(6):
+        assert rel(x[i], np.linalg.inv(a[i])) < 1e-11, (n, i)
+    assert resid < 1e-5
+
+
+def test_blocked_start_matches_whole_matrix_start():
+    """The block start and the whole-matrix Gauss-Jordan start refine to the
+    same k-summed tau (1e-11) on a strided sample of the benchmarked
+    interface's energy 19, both within the split-precision bound of the
+    oracle."""
+    ep = W.energy_problem(W.rel_bcc(), 19)
+    idx = np.arange(0, ep.nk, 80)
+    sub = ep.with_k(ep.xk[idx], ep.wk[idx] / ep.wk[idx].sum())
+    out = {}
+    for blocked in (True, False):
+        ctx = api.Context.for_problem(sub, "mixed")
+        try:
+            ctx.set_inverse_start(blocked)
+            out[blocked] = ctx.cpacoord(sub)
+        finally:
+            ctx.close()
+        assert out[blocked]["status"] == 0 and out[blocked]["max_refine_resid"] < 1e-6
+    assert rel(out[True]["tauc"], out[False]["tauc"]) < 1e-11
+    o = O.cpacoord(sub, nthreads=8)
+    assert rel(out[True]["tauc"], o["tauc"]) < TOL_MIXED
