@@ -155,8 +155,9 @@ int skkr_gpu_set_inverse_start(skkr_ctx *ctx, int blocked);
 
 /* Autotuner of the split-precision inverse's FP32 Gauss-Jordan: each size
  * class (n <= 32, 64, 128) has 2-3 thread layouts that give the same inverse
- * bit for bit; the first batch of each (class, batch size) times them once
- * and later calls use the fastest (process wide).  report (may be NULL)
+ * bit for bit; the first batch of each (class, batch size) times them (best
+ * of three runs each; a later layout must be 5 % faster to be chosen) and
+ * later calls use the choice (process wide).  report (may be NULL)
  * receives the choices so far, e.g. "n<=128 >=4 waves: 64x2x8; ".
  * force > 0 makes every class use its layout force - 1 (tests); force = 0
  * with report NULL forgets the choices and tunes afresh. */

@@ -1437,17 +1437,24 @@ static GjLaunch gj_choose(int n, long long items, const MatRef &A, const MatRef 
     cudaEventDestroy(e0);
     return C.f[0];
   }
+  // each layout: one warm run, then the best of three timed runs; a later
+  // layout replaces the current choice only when it is 5 % faster (the
+  // layouts are listed in order of preference)
   int best = 0;
   float tbest = 1e30f;
   for (int v = 0; v < C.nv; v++) {
     C.f[v](A, X, n, nc, act, (unsigned)items, st);  // warm (module load, caches)
-    cudaEventRecord(e0, st);
-    C.f[v](A, X, n, nc, act, (unsigned)items, st);
-    cudaEventRecord(e1, st);
-    float ms = 1e30f;
-    if (cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess &&
-        ms < tbest) {
-      tbest = ms;
+    float tv = 1e30f;
+    for (int rep = 0; rep < 3; rep++) {
+      cudaEventRecord(e0, st);
+      C.f[v](A, X, n, nc, act, (unsigned)items, st);
+      cudaEventRecord(e1, st);
+      float ms = 1e30f;
+      if (cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess)
+        tv = std::min(tv, ms);
+    }
+    if (tv < 0.95f * tbest) {
+      tbest = tv;
       best = v;
     }
   }
