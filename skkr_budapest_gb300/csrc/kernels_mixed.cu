@@ -48,7 +48,12 @@ namespace {
 constexpr int NT = 96;            // N tile (TMEM columns per accumulator)
 constexpr int MT = 128;           // M tile (UMMA M)
 constexpr int KB = 32;            // K per k-block (one 64-byte swizzle row of bf16)
-constexpr int NSTAGE = 2;         // shared-memory pipeline stages
+constexpr int OZ_SMEM_MAX = 232448;  // shared memory one CTA may use (opt-in)
+// shared-memory pipeline stages of the sliced GEMM: three where three stages
+// of S A tiles and S B tiles fit (S <= 5 at the 96-column tile), else two
+__host__ __device__ constexpr int oz_stages(int S, int TN) {
+  return 3 * S * (128 * 32 * 2 + TN * 32 * 2) + 1024 <= OZ_SMEM_MAX ? 3 : 2;
+}
 constexpr int NACC = 5;           // TMEM accumulators: one per level p+q = 0..4
 constexpr long long WAIT_LIMIT = 1LL << 22;
 constexpr int OZ_THREADS = 384;   // 12 warps: producer and MMA lanes in warps 0-1, all 12 run the epilogue
@@ -478,6 +483,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_ozaki(const __grid_constant__
   const int mt = blockIdx.x / g.ntiles, nt = blockIdx.x % g.ntiles;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   // NSTAGE stages, each: S A tiles (MT x KB) then S B tiles (TN x KB), 1024-byte aligned
+  constexpr int NSTAGE = oz_stages(S, TN);
   unsigned char *tiles = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   constexpr uint32_t A_BYTES = MT * KB * 2, B_BYTES = TN * KB * 2;
   constexpr uint32_t STAGE_BYTES = S * (A_BYTES + B_BYTES);
@@ -960,7 +966,7 @@ int make_map(CUtensorMap *m, void *base, int rows, long long depth, int boxrows)
 // at least 120 KB so that only one CTA (and one 512-column TMEM allocation)
 // is resident per SM
 size_t oz_smem_bytes(int S, int TN) {
-  size_t b = (size_t)NSTAGE * S * (MT * KB * 2 + TN * KB * 2) + 1024;
+  size_t b = (size_t)oz_stages(S, TN) * S * (MT * KB * 2 + TN * KB * 2) + 1024;
   return b < 120 * 1024 ? 120 * 1024 : b;
 }
 
