@@ -854,18 +854,28 @@ __global__ void __launch_bounds__(TY * 16, MINB) k_cgj32(MatRef A, MatRef X, int
 // ------------------------------------------------------------------ FP32 block products
 // C = A B (m x n, depth k; m, n, k <= 64) of one item per block in complex
 // FP32 from FP64 operands, for the 2 x 2 block start of the split-precision
-// inverse: MODE 0 C = AB, 1 C = D - AB (D read in FP64), 2 C = -AB.  The
-// 16 x 16 threads each hold 4 x 4 outputs (rows ty + 16 i, columns tx + 16 j);
-// the operands pass through shared memory in K chunks of 32, converted to
-// FP32 on the way; the sums run in a fixed order.
-template <int MODE>
-__global__ void __launch_bounds__(256, 2) k_cgemm32(MatRef A, MatRef B, MatRef C, MatRef D, int m, int n, int k,
-                                                 int nc, const int *__restrict__ act) {
+// inverse: mode 0 C = AB, 1 C = D - AB (D read in FP64), 2 C = -AB.  Up to
+// two independent products per launch (blockIdx.y picks one).  The 16 x 16
+// threads each hold 4 x 4 outputs (rows ty + 16 i, columns tx + 16 j); the
+// operands pass through shared memory in K chunks of 32, converted to FP32
+// on the way; the sums run in a fixed order.
+struct G32Job {
+  MatRef A, B, C, D;
+  int m, n, k, mode;
+};
+struct G32Jobs {
+  G32Job j[2];
+};
+
+__global__ void __launch_bounds__(256, 2) k_cgemm32(G32Jobs jobs, int nc, const int *__restrict__ act) {
   const int item = blockIdx.x, kk = item / nc, cc = item % nc;
   if (act && !act[item]) return;
+  const G32Job &J = jobs.j[blockIdx.y];
+  const int m = J.m, n = J.n, k = J.k;
   __shared__ float2 As[32][64];  // [K index][row]
   __shared__ float2 Bs[32][65];  // [K index][column], padded against store conflicts
-  const zd *a = mat_ptr(A, kk, cc), *b = mat_ptr(B, kk, cc);
+  const zd *a = mat_ptr(J.A, kk, cc), *b = mat_ptr(J.B, kk, cc);
+  const int lda = J.A.ld, ldb = J.B.ld;
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
   float2 acc[4][4];
 #pragma unroll
@@ -875,12 +885,12 @@ __global__ void __launch_bounds__(256, 2) k_cgemm32(MatRef A, MatRef B, MatRef C
   for (int k0 = 0; k0 < k; k0 += 32) {
     for (int e = threadIdx.x; e < 64 * 32; e += 256) {
       const int r = e & 63, q = e >> 6, col = k0 + q;
-      const zd v = (r < m && col < k) ? a[r + (long long)col * A.ld] : make_double2(0.0, 0.0);
+      const zd v = (r < m && col < k) ? a[r + (long long)col * lda] : make_double2(0.0, 0.0);
       As[q][r] = make_float2((float)v.x, (float)v.y);
     }
     for (int e = threadIdx.x; e < 32 * 64; e += 256) {
       const int q = e & 31, c = e >> 5, row = k0 + q;
-      const zd v = (row < k && c < n) ? b[row + (long long)c * B.ld] : make_double2(0.0, 0.0);
+      const zd v = (row < k && c < n) ? b[row + (long long)c * ldb] : make_double2(0.0, 0.0);
       Bs[q][c] = make_float2((float)v.x, (float)v.y);
     }
     __syncthreads();
@@ -903,8 +913,10 @@ __global__ void __launch_bounds__(256, 2) k_cgemm32(MatRef A, MatRef B, MatRef C
     }
     __syncthreads();
   }
-  zd *c = mat_ptr(C, kk, cc);
-  const zd *d = MODE == 1 ? mat_ptr(D, kk, cc) : nullptr;
+  zd *c = mat_ptr(J.C, kk, cc);
+  const int ldc = J.C.ld, mode = J.mode;
+  const zd *d = mode == 1 ? mat_ptr(J.D, kk, cc) : nullptr;
+  const int ldd = J.D.ld;
 #pragma unroll
   for (int i = 0; i < 4; i++)
 #pragma unroll
@@ -913,23 +925,36 @@ __global__ void __launch_bounds__(256, 2) k_cgemm32(MatRef A, MatRef B, MatRef C
       if (r < m && col < n) {
         const zd p = make_double2((double)acc[i][j].x, (double)acc[i][j].y);
         zd o;
-        if (MODE == 0) o = p;
-        else if (MODE == 1) {
-          const zd dv = d[r + (long long)col * D.ld];
+        if (mode == 0) o = p;
+        else if (mode == 1) {
+          const zd dv = d[r + (long long)col * ldd];
           o = make_double2(dv.x - p.x, dv.y - p.y);
         } else o = make_double2(-p.x, -p.y);
-        c[r + (long long)col * C.ld] = o;
+        c[r + (long long)col * ldc] = o;
       }
     }
 }
 
-static void cgemm32(int mode, const MatRef &A, const MatRef &B, const MatRef &C, const MatRef &D, int m, int n,
-                    int k, int nc, const int *act, unsigned items, cudaStream_t st) {
-  switch (mode) {
-    case 0: k_cgemm32<0><<<items, 256, 0, st>>>(A, B, C, D, m, n, k, nc, act); break;
-    case 1: k_cgemm32<1><<<items, 256, 0, st>>>(A, B, C, D, m, n, k, nc, act); break;
-    default: k_cgemm32<2><<<items, 256, 0, st>>>(A, B, C, D, m, n, k, nc, act); break;
-  }
+static G32Job g32(int mode, const MatRef &A, const MatRef &B, const MatRef &C, const MatRef &D, int m, int n,
+                  int k) {
+  G32Job j;
+  j.A = A;
+  j.B = B;
+  j.C = C;
+  j.D = D;
+  j.m = m;
+  j.n = n;
+  j.k = k;
+  j.mode = mode;
+  return j;
+}
+
+// one or two products per launch
+static void cgemm32(const G32Job &j0, const G32Job *j1, int nc, const int *act, unsigned items, cudaStream_t st) {
+  G32Jobs js;
+  js.j[0] = j0;
+  js.j[1] = j1 ? *j1 : j0;
+  k_cgemm32<<<dim3(items, j1 ? 2 : 1), 256, 0, st>>>(js, nc, act);
   SKKR_LAUNCHED();
 }
 
@@ -1511,17 +1536,17 @@ static void block_start(const MatRef &A, const MatRef &X, int n, int nc, const i
   const GjLaunch g1 = gj_choose(b, items, A11, X11, nc, act, st);
   g1(A11, X11, b, nc, act, items, st);
   SKKR_LAUNCHED();
-  cgemm32(0, X11, A12, U, U, b, n2, b, nc, act, items, st);    // U = X11 A12
-  cgemm32(1, A21, U, S, A22, n2, n2, b, nc, act, items, st);   // S = A22 - A21 U
+  const G32Job u = g32(0, X11, A12, U, U, b, n2, b), t = g32(0, A21, X11, T, T, n2, b, b);
+  cgemm32(u, &t, nc, act, items, st);                                  // U = X11 A12, T = A21 X11
+  cgemm32(g32(1, A21, U, S, A22, n2, n2, b), nullptr, nc, act, items, st);  // S = A22 - A21 U
   // Y = S^-1 straight into its place in X (the layout autotuner may run its
   // candidates on these operands: S is never overwritten)
   const GjLaunch g2 = gj_choose(n2, items, S, X22, nc, act, st);
   g2(S, X22, n2, nc, act, items, st);
   SKKR_LAUNCHED();
-  cgemm32(0, A21, X11, T, T, n2, b, b, nc, act, items, st);      // T = A21 X11
-  cgemm32(2, U, X22, X12, X12, b, n2, n2, nc, act, items, st);   // X12 = -U Y
-  cgemm32(2, X22, T, X21, X21, n2, b, n2, nc, act, items, st);   // X21 = -Y T
-  cgemm32(1, X12, T, Xa, X11, b, b, n2, nc, act, items, st);     // X11 - X12 T
+  const G32Job x12 = g32(2, U, X22, X12, X12, b, n2, n2), x21 = g32(2, X22, T, X21, X21, n2, b, n2);
+  cgemm32(x12, &x21, nc, act, items, st);                              // X12 = -U Y, X21 = -Y T
+  cgemm32(g32(1, X12, T, Xa, X11, b, b, n2), nullptr, nc, act, items, st);  // X11 - X12 T
 }
 
 // X = A^-1: FP32 Gauss-Jordan, then `newton` steps X += X (I - A X) with the
