@@ -544,6 +544,16 @@ int skkr_gpu_zinv_batch(int precision, int n, int batch, double *a, int ld,
 /* G_scr(k) blocks of nk k points: out [nk][nblk] lm x lm column-major. */
 int skkr_gpu_gk(const skkr_rtable *rt, int lmax, int nk, const double *xk, double *out);
 
+/* tau2d (main/tau2d.f:2-152) for `batch` independent items of nprc principal
+ * layers of n rows (n = layers per PL x lk), FP64, host arrays, column-major
+ * n x n blocks without padding: m00, m01, m10 [batch][nprc] the packed PL
+ * matrices (M00 with the layers' t^-1 blocks added; M01 couples PL p to
+ * p+1, M10 to p-1), x and y [batch] the right and left surface operators.
+ * tau [batch][nprc * n/lk] receives wgeff times the layer-diagonal lk x lk
+ * blocks of the PL-diagonal tau.  batch * nprc <= 65535, n <= 512. */
+int skkr_gpu_tau2d(int batch, int nprc, int n, int lk, double wgeff, const double *m00, const double *m01,
+                   const double *m10, const double *x, const double *y, double *tau);
+
 /* Text of the last CUDA error seen by the library in this process. */
 const char *skkr_gpu_last_error(void);
 

@@ -2217,6 +2217,97 @@ extern "C" int skkr_gpu_gjinv_batch(int n, int batch, double *a, int ld) {
   return download_mats(a, d, batch, n, ld);
 }
 
+// tau2d (main/tau2d.f:2-152) for `batch` independent items of nprc principal
+// layers of n rows each, on host arrays: the forward sweep
+// yy(0) = Y, yy(p) = M10(p) (M00(p-1) - yy(p-1))^-1 M01(p-1), the backward
+// sweep xx(nprc-1) = X, xx(p) = M01(p) (T00(p+1) - xx(p+1))^-1 M10(p+1), and
+// tau(p) = (M00(p) - xx(p) - yy(p))^-1, whose diagonal lk x lk blocks times
+// wgeff are the layer taus.  M00 carries the layers' t^-1 blocks.  FP64.
+extern "C" int skkr_gpu_tau2d(int batch, int nprc, int n, int lk, double wgeff, const double *m00,
+                              const double *m01, const double *m10, const double *x, const double *y, double *tau) {
+  if (batch < 1 || nprc < 1 || n < 1 || n > 512 || lk < 1 || n % lk || !m00 || !m01 || !m10 || !x || !y || !tau ||
+      (long long)batch * nprc > 65535)
+    return SKKR_ERR_ARG;
+  const long long MB = (long long)n * n, per = (long long)nprc * MB;
+  const int nl = n / lk;
+  Scoped s;
+  zd *M00, *M01, *M10, *XX, *YY, *T00, *W;
+  CKR(s.alloc(&M00, batch * per));
+  CKR(s.alloc(&M01, batch * per));
+  CKR(s.alloc(&M10, batch * per));
+  CKR(s.alloc(&XX, batch * per));
+  CKR(s.alloc(&YY, batch * per));
+  CKR(s.alloc(&T00, batch * per));
+  CKR(s.alloc(&W, batch * MB));
+  CKR(upload_mats(M00, m00, batch * nprc, n, n));
+  CKR(upload_mats(M01, m01, batch * nprc, n, n));
+  CKR(upload_mats(M10, m10, batch * nprc, n, n));
+  // item k, PL p at base + k per + p MB; the sweeps run over k for one p
+  auto pl = [&](zd *b, int p) { return mref(b + (long long)p * MB, per, 0, n); };
+  const MatRef w = mref(W, MB, 0, n);
+  {
+    // X and Y of item k into PL nprc-1 of XX and PL 0 of YY
+    Scoped t;
+    zd *xs, *ys;
+    CKR(t.alloc(&xs, batch * MB));
+    CKR(t.alloc(&ys, batch * MB));
+    CKR(upload_mats(xs, x, batch, n, n));
+    CKR(upload_mats(ys, y, batch, n, n));
+    launch_zaxpby(pl(XX, nprc - 1), mref(xs, MB, 0, n), nullptr, 0, nullptr, 0, n, batch, 1, nullptr, 0);
+    launch_zaxpby(pl(YY, 0), mref(ys, MB, 0, n), nullptr, 0, nullptr, 0, n, batch, 1, nullptr, 0);
+    CK(cudaDeviceSynchronize());
+  }
+  for (int p = 0; p < nprc; p++) {
+    MatRef t00 = pl(T00, p), yy = pl(YY, p), m00p = pl(M00, p);
+    launch_zaxpby(t00, m00p, nullptr, 0, nullptr, 0, n, batch, 1, nullptr, 0);
+    if (p > 0) {
+      // yy(p) holds (M00(p-1) - yy(p-1))^-1 M01(p-1): multiply by M10(p)
+      launch_zgemm(0, pl(M10, p), yy, w, w, w, n, n, n, batch, 1, nullptr, 0);
+      launch_zaxpby(yy, w, nullptr, 0, nullptr, 0, n, batch, 1, nullptr, 0);
+    }
+    if (p < nprc - 1) {
+      launch_zaxpby(w, m00p, &yy, -1.0, nullptr, 0, n, batch, 1, nullptr, 0);
+      launch_zgj(w, n, batch, 1, nullptr, 0);
+      launch_zgemm(0, w, pl(M01, p), pl(YY, p + 1), pl(YY, p + 1), pl(YY, p + 1), n, n, n, batch, 1, nullptr, 0);
+    }
+  }
+  for (int p = nprc - 1; p >= 0; p--) {
+    MatRef xx = pl(XX, p);
+    if (p < nprc - 1) {
+      launch_zgemm(0, pl(M01, p), xx, w, w, w, n, n, n, batch, 1, nullptr, 0);
+      launch_zaxpby(xx, w, nullptr, 0, nullptr, 0, n, batch, 1, nullptr, 0);
+    }
+    if (p > 0) {
+      MatRef t00 = pl(T00, p);
+      launch_zaxpby(w, t00, &xx, -1.0, nullptr, 0, n, batch, 1, nullptr, 0);
+      launch_zgj(w, n, batch, 1, nullptr, 0);
+      launch_zgemm(0, w, pl(M10, p), pl(XX, p - 1), pl(XX, p - 1), pl(XX, p - 1), n, n, n, batch, 1, nullptr, 0);
+    }
+  }
+  for (int p = 0; p < nprc; p++) {
+    MatRef t00 = pl(T00, p), xx = pl(XX, p), yy = pl(YY, p);
+    launch_zaxpby(t00, t00, &xx, -1.0, &yy, -1.0, n, batch, 1, nullptr, 0);
+    launch_zgj(t00, n, batch, 1, nullptr, 0);
+  }
+  CK(cudaDeviceSynchronize());
+  CK(cudaGetLastError());
+  // layer blocks: tau[k][p nl + l] = wgeff T00[k][p] block (l, l)
+  std::vector<zd> h((size_t)batch * per);
+  CK(cudaMemcpy(h.data(), T00, (size_t)batch * per * sizeof(zd), cudaMemcpyDeviceToHost));
+  const long long L2 = (long long)lk * lk;
+  for (int k = 0; k < batch; k++)
+    for (int p = 0; p < nprc; p++)
+      for (int l = 0; l < nl; l++)
+        for (int c = 0; c < lk; c++)
+          for (int r = 0; r < lk; r++) {
+            const zd v = h[(size_t)(k * per + p * MB + (long long)(l * lk + r) + (long long)(l * lk + c) * n)];
+            const long long o = (((long long)k * nprc + p) * nl + l) * L2 + r + (long long)c * lk;
+            tau[2 * o] = wgeff * v.x;
+            tau[2 * o + 1] = wgeff * v.y;
+          }
+  return SKKR_OK;
+}
+
 extern "C" int skkr_gpu_gk(const skkr_rtable *rt, int lmax, int nk, const double *xk, double *out) {
   if (!rt || nk < 1 || !xk || !out || lmax < 0 || lmax > 3) return SKKR_ERR_ARG;
   const int lmmax = (lmax + 1) * (lmax + 1), nr = rt->rstart[rt->nblk];

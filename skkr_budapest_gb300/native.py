@@ -85,6 +85,7 @@ def lib():
         L.skkr_gpu_kambe_screened.argtypes = [I, D, D, P, I, P, P, I, P, I, P, I, D, D, D, D, I, I, P]
         L.skkr_gpu_layer_dos.argtypes = [I, I, I, P, I, P, P, I, P, P]
         L.skkr_gpu_bsf.argtypes = [I, I, I, I, P, P, P, P, P, P, P, P, I, P]
+        L.skkr_gpu_tau2d.argtypes = [I, I, I, I, D, P, P, P, P, P, P]
         L.skkr_gpu_set_reduce.argtypes = [P, P, P]
         L.skkr_gpu_set_reduce_device.argtypes = [P, P, P]
         L.skkr_gpu_set_mixed_policy.argtypes = [P, D, D, I, D]
@@ -448,6 +449,18 @@ def layer_dos(tau, F, G, lmax, irel, para=False):
     _check(lib().skkr_gpu_layer_dos(irel, lmax, nlay, _p(t), nd, _p(f), _p(g), int(bool(para)), _p(zm), _p(zl)),
            "skkr_gpu_layer_dos")
     return zm, zl
+
+
+def tau2d(m00, m01, m10, x, y, lk, wgeff=1.0):
+    """tau2d on the device (skkr_gpu_tau2d): m00, m01, m10 [batch, nprc, n, n],
+    x, y [batch, n, n], all [row, col]; returns wgeff times the layer-diagonal
+    blocks [batch, nprc * n / lk, lk, lk]."""
+    m00 = np.asarray(m00, np.complex128)
+    batch, nprc, n = m00.shape[0], m00.shape[1], m00.shape[-1]
+    args = [cm(m00), cm(m01), cm(m10), cm(x), cm(y)]
+    out = np.zeros((batch, nprc * (n // lk), lk, lk), np.complex128)
+    _check(lib().skkr_gpu_tau2d(batch, nprc, n, lk, float(wgeff), *[_p(a) for a in args], _p(out)), "skkr_gpu_tau2d")
+    return uncm(out)
 
 
 def bsf(mode, lmax, conc, tauk, tauc, taua, taub, F, Feh=None, pair=None, para=False):

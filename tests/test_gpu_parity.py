@@ -175,3 +175,39 @@ def test_empty_k_list_is_refused_and_the_context_stays_usable():
         ctx.close()
     assert g["status"] == 0
     assert rel(g["tauc"], api.cpacoord(ep)["tauc"]) < 1e-13
+
+
+def test_tau2d_export_is_the_block_tridiagonal_inverse():
+    """skkr_gpu_tau2d (the Godfrin sweeps of main/tau2d.f on host arrays):
+    each layer block equals the diagonal block of the inverse of the whole
+    block-tridiagonal matrix with the surface operators on its corners,
+    A(p,p) = M00(p), A(p,p+1) = -M01(p), A(p+1,p) = -M10(p+1),
+    A(0,0) -= Y, A(last,last) -= X."""
+    rng = np.random.default_rng(7)
+    batch, nprc, lk, nl = 3, 3, 8, 2
+    n = lk * nl
+
+    def c(*s):
+        return rng.normal(size=s) + 1j * rng.normal(size=s)
+
+    m00 = 0.3 * c(batch, nprc, n, n) + 4 * np.eye(n)
+    m01 = 0.3 * c(batch, nprc, n, n)
+    m10 = 0.3 * c(batch, nprc, n, n)
+    x = 0.3 * c(batch, n, n)
+    y = 0.3 * c(batch, n, n)
+    got = native.tau2d(m00, m01, m10, x, y, lk, wgeff=0.5)
+    for k in range(batch):
+        A = np.zeros((nprc * n, nprc * n), complex)
+        for p in range(nprc):
+            A[p * n:(p + 1) * n, p * n:(p + 1) * n] = m00[k, p]
+            if p + 1 < nprc:
+                A[p * n:(p + 1) * n, (p + 1) * n:(p + 2) * n] = -m01[k, p]
+                A[(p + 1) * n:(p + 2) * n, p * n:(p + 1) * n] = -m10[k, p + 1]
+        A[:n, :n] -= y[k]
+        A[-n:, -n:] -= x[k]
+        inv = np.linalg.inv(A)
+        for p in range(nprc):
+            for l in range(nl):
+                r0 = p * n + l * lk
+                ref = 0.5 * inv[r0:r0 + lk, r0:r0 + lk]
+                assert np.abs(got[k, p * nl + l] - ref).max() < 1e-12 * np.abs(ref).max(), (k, p, l)
