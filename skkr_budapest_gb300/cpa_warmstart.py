@@ -105,19 +105,36 @@ class Family:
         return ep
 
 
-def kappa_groups(lmax: int):
-    """Index arrays of the (kappa,mu) basis grouped by kappa (clebsch.f order)."""
-    _, kv = S.kmy_l_kappa(lmax)
-    kappas = []
-    for k in kv.tolist():
-        if k not in kappas:
-            kappas.append(k)
-    return [np.nonzero(kv == k)[0] for k in kappas]
+class _KGroups:
+    """The (kappa,mu) basis grouped by kappa (clebsch.f order): the index
+    arrays, and the same as one permutation with group starts and sizes for
+    the per-group means."""
+
+    def __init__(self, lmax: int):
+        _, kv = S.kmy_l_kappa(lmax)
+        kappas = []
+        for k in kv.tolist():
+            if k not in kappas:
+                kappas.append(k)
+        self.groups = [np.nonzero(kv == k)[0] for k in kappas]
+        self.order = np.concatenate(self.groups)
+        self.sizes = np.array([len(g) for g in self.groups], float)
+        self.starts = np.concatenate([[0], np.cumsum([len(g) for g in self.groups])[:-1]])
 
 
-def _kdiag(m, groups):
-    d = np.diag(m)
-    return np.array([d[g].mean() for g in groups])
+_KG: dict = {}
+
+
+def kappa_groups(lmax: int) -> _KGroups:
+    if lmax not in _KG:
+        _KG[lmax] = _KGroups(lmax)
+    return _KG[lmax]
+
+
+def _kdiag(m, groups: _KGroups):
+    """Mean of the diagonal of m over each kappa group."""
+    d = np.diag(m)[groups.order]
+    return np.add.reduceat(d, groups.starts) / groups.sizes
 
 
 def invariant_projector(ep):
