@@ -144,6 +144,17 @@ def invariant_projector(ep):
     return lambda m: (rg @ m @ lg).mean(axis=0)
 
 
+def projector_matrix(ep, mask):
+    """The point-group average P restricted to the free elements: the
+    (n*n, nfree) matrix whose column f is P of the unit matrix at the f-th
+    True entry of mask (row-major), so that P(d) = (Pm @ d[mask]) for every d
+    that vanishes off the mask."""
+    lg, rg = np.asarray(ep.lg), np.asarray(ep.rg)
+    j, k = np.nonzero(mask)
+    pm = np.einsum("gif,gfm->imf", rg[:, :, j], lg[:, k, :]) / len(lg)
+    return pm.reshape(-1, len(j))
+
+
 def free_elements(ep):
     """Mask of the matrix elements that invariant matrices can carry."""
     P = invariant_projector(ep)
@@ -174,6 +185,12 @@ def stack_features(ep, fam: Family):
 
 def _scale(ep, li, groups):
     return np.abs(_kdiag(ep.tminva[li], groups) - _kdiag(ep.tminvb[li], groups)).mean() + 1e-30
+
+
+def _scales(ep, layers, groups):
+    """_scale of each of the layers, all at once."""
+    d = np.diagonal(ep.tminva[layers] - ep.tminvb[layers], axis1=1, axis2=2)[:, groups.order]
+    return np.abs(np.add.reduceat(d, groups.starts, axis=1) / groups.sizes).mean(axis=1) + 1e-30
 
 
 def stack_targets(ep, mc, fam: Family, mask):
@@ -230,6 +247,14 @@ class Model:
     def family(self):
         return Family(nset=self.nset, so_split=self.so_split)
 
+    def projector(self, ep):
+        """projector_matrix of ep on the model's mask, kept while problems
+        share the same group matrices (every energy of one lattice does)."""
+        c = getattr(self, "_proj", None)
+        if c is None or c[0] is not ep.lg or c[1] is not ep.rg:
+            c = self._proj = (ep.lg, ep.rg, projector_matrix(ep, self.mask))
+        return c[2]
+
 
 def warm_start(ep, model: Model, fam: Family | None = None, device: str = "gpu"):
     """Starting coherent t^-1: m_ATA + the projected prediction on the alloy
@@ -237,13 +262,12 @@ def warm_start(ep, model: Model, fam: Family | None = None, device: str = "gpu")
     fam = fam or model.family()
     groups = kappa_groups(fam.lmax)
     pred = model.predict(stack_features(ep, fam), device)
-    P = invariant_projector(ep)
-    tm = np.array(ep.tminv, copy=True)
+    al = list(fam.alloy_layers)
+    pm = model.projector(ep)
     nm = int(model.mask.sum())
-    for row, li in zip(pred, fam.alloy_layers):
-        d = np.zeros_like(tm[li])
-        d[model.mask] = (row[:nm] + 1j * row[nm:]) * _scale(ep, li, groups)
-        tm[li] = ep.tminv[li] + P(d)
+    d = (pred[:, :nm] + 1j * pred[:, nm:2 * nm]) * _scales(ep, al, groups)[:, None]
+    tm = np.array(ep.tminv, copy=True)
+    tm[al] += (d @ pm.T).reshape(len(al), *tm.shape[1:])
     return tm
 
 

@@ -72,3 +72,15 @@ def test_bf16_rounding_ties_to_even():
     v = np.float32([1.0 + 2.0 ** -8, 1.0 + 3 * 2.0 ** -9, -2.5, 1.0 + 2.0 ** -7 + 2.0 ** -8])
     r = CW.bf16_round(v)
     assert list(r) == [1.0, np.float32(1.0 + 2.0 ** -7), -2.5, np.float32(1.0 + 2.0 ** -6)]
+
+
+def test_projector_matrix_is_the_group_average_on_the_mask():
+    fam = _family()
+    ep = fam.problem(3, fam.draw(np.random.default_rng(4)))
+    mask = CW.free_elements(ep)
+    pm = CW.projector_matrix(ep, mask)
+    rng = np.random.default_rng(5)
+    d = np.zeros((ep.lkmax, ep.lkmax), complex)
+    d[mask] = rng.normal(size=mask.sum()) + 1j * rng.normal(size=mask.sum())
+    want = CW.invariant_projector(ep)(d)
+    assert np.abs((pm @ d[mask]).reshape(d.shape) - want).max() < 1e-13 * np.abs(want).max()
