@@ -248,12 +248,22 @@ class Model:
         return Family(nset=self.nset, so_split=self.so_split)
 
     def projector(self, ep):
-        """projector_matrix of ep on the model's mask, kept while problems
-        share the same group matrices (every energy of one lattice does)."""
-        c = getattr(self, "_proj", None)
-        if c is None or c[0] is not ep.lg or c[1] is not ep.rg:
-            c = self._proj = (ep.lg, ep.rg, projector_matrix(ep, self.mask))
-        return c[2]
+        """projector_matrix of ep on the model's mask, built once per set of
+        group matrices: every energy of one lattice carries equal ones (as
+        separate arrays), found by identity and else by value."""
+        cache = self.__dict__.setdefault("_proj", [])
+        for lg, rg, pm in cache:
+            if lg is ep.lg and rg is ep.rg:
+                return pm
+        for lg, rg, pm in cache:
+            if np.array_equal(lg, ep.lg) and np.array_equal(rg, ep.rg):
+                cache.append((ep.lg, ep.rg, pm))
+                del cache[:-32]
+                return pm
+        pm = projector_matrix(ep, self.mask)
+        cache.append((ep.lg, ep.rg, pm))
+        del cache[:-32]
+        return pm
 
 
 def warm_start(ep, model: Model, fam: Family | None = None, device: str = "gpu"):
