@@ -153,6 +153,13 @@ int skkr_gpu_set_newton(skkr_ctx *ctx, int steps);
  * Newton steps, their acceptance test and the FP64 redo are the same. */
 int skkr_gpu_set_inverse_start(skkr_ctx *ctx, int blocked);
 
+/* The B operand of every split-precision product on the default tile: on
+ * != 0 (the default) the product reads B in FP64 and forms its BF16 slices in
+ * shared memory, tile by tile, with the warps that later run the epilogue; 0
+ * splits B into a staging buffer first and loads its tiles by TMA.  Both give
+ * the same slices, hence the same result bit for bit. */
+int skkr_gpu_set_fused_split(skkr_ctx *ctx, int on);
+
 /* Autotuner of the split-precision inverse's FP32 Gauss-Jordan: each size
  * class (n <= 32, 64, 128) has 2-3 thread layouts that give the same inverse
  * bit for bit; the first batch of each (class, batch size) times them (best

@@ -65,6 +65,12 @@ class Context:
         (default) or the whole-matrix Gauss-Jordan (skkr_gpu_set_inverse_start)."""
         N._check(N.lib().skkr_gpu_set_inverse_start(self.h, 1 if blocked else 0), "skkr_gpu_set_inverse_start")
 
+    def set_fused_split(self, on=True):
+        """B operands of the split-precision products formed inside the
+        product (default) or split into staging buffers first; the same
+        result bit for bit (skkr_gpu_set_fused_split)."""
+        N._check(N.lib().skkr_gpu_set_fused_split(self.h, 1 if on else 0), "skkr_gpu_set_fused_split")
+
     def set_graphs(self, on=True):
         """Decimation loop as one CUDA graph launch per k chunk (the default)
         or one host-driven iteration at a time (skkr_gpu_set_graphs)."""

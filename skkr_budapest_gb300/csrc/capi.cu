@@ -386,6 +386,7 @@ struct skkr_ctx {
   bool graphs = true;           // decimation loop as a CUDA graph WHILE node (skkr_gpu_set_graphs)
   int newton = 2;               // standard Newton steps of the split-precision inverse (skkr_gpu_set_newton)
   int blocked_start = 1;        // 2 x 2 block FP32 start above 64 rows (skkr_gpu_set_inverse_start)
+  int fused_b = 1;              // B operands formed inside the sliced products (skkr_gpu_set_fused_split)
   DBuf decctl;                  // [0] iteration, [1] items left, [2] half-bodies run (captured loop)
   long long graph_kernels = 0;  // kernels run inside graphs in this run
   long long graph_launches = 0; // graph launches in this run
@@ -1002,13 +1003,13 @@ static int run_decimation(skkr_ctx *c, int k0, int nkc, const std::vector<int> &
       // alfa, beta; A slots 1-4: alfa, beta, P, Q) for the six products
       MixedWork *w = c->mw;
       const int S = slices_for(c);
-      CKR(mixed_split(w, 1, 1, S, y1, n, n, nkc, nc, act, st));
+      CKR(mixed_split(w, 1, 1, S, y1, n, n, nkc, nc, act, st, true));
       CKR(mixed_split(w, 0, 1, S, ac, n, n, nkc, nc, act, st));
       CKR(mixed_split(w, 0, 2, S, bc, n, n, nkc, nc, act, st));
       CKR(mixed_gemm_staged(w, 0, S, 1, 1, P, P, P, n, n, nkc, nc, act, st));        // P = alfa y1
       CKR(mixed_gemm_staged(w, 0, S, 2, 1, Q, Q, Q, n, n, nkc, nc, act, st));        // Q = beta y1
-      CKR(mixed_split(w, 1, 2, S, ac, n, n, nkc, nc, act, st));
-      CKR(mixed_split(w, 1, 3, S, bc, n, n, nkc, nc, act, st));
+      CKR(mixed_split(w, 1, 2, S, ac, n, n, nkc, nc, act, st, true));
+      CKR(mixed_split(w, 1, 3, S, bc, n, n, nkc, nc, act, st, true));
       CKR(mixed_split(w, 0, 3, S, P, n, n, nkc, nc, act, st));
       CKR(mixed_split(w, 0, 4, S, Q, n, n, nkc, nc, act, st));
       CKR(mixed_gemm_staged(w, 0, S, 3, 2, an, an, an, n, n, nkc, nc, act, st));     // alfa' = P alfa
@@ -1135,7 +1136,7 @@ static int run_tau2d(skkr_ctx *c, int k0, int nkc, const std::vector<int> &icls)
   };
   if (staged) {
     CKR(mixed_split(w, 0, 1, S, M10, n, n, nkc, nc, nullptr, st));
-    CKR(mixed_split(w, 1, 1, S, M01, n, n, nkc, nc, nullptr, st));
+    CKR(mixed_split(w, 1, 1, S, M01, n, n, nkc, nc, nullptr, st, true));
   }
   // forward (tau2d.f:53-85)
   for (int p = 0; p < nprc; p++) {
@@ -1163,7 +1164,7 @@ static int run_tau2d(skkr_ctx *c, int k0, int nkc, const std::vector<int> &icls)
   }
   if (staged) {
     CKR(mixed_split(w, 0, 3, S, M01, n, n, nkc, nc, nullptr, st));
-    CKR(mixed_split(w, 1, 3, S, M10, n, n, nkc, nc, nullptr, st));
+    CKR(mixed_split(w, 1, 3, S, M10, n, n, nkc, nc, nullptr, st, true));
   }
   // backward (tau2d.f:89-109)
   for (int p = nprc - 1; p >= 0; p--) {
@@ -1587,6 +1588,7 @@ extern "C" int skkr_gpu_tauij(skkr_ctx *c, int npair, const int *pairs, const do
   if (c->mw) {
     CKR(mixed_resid_reset(c->mw, st));
     mixed_set_precise(c->mw, c->slices_near > 0 && std::fabs(c->ce.y) < c->near_im);
+    mixed_set_fused(c->mw, c->fused_b != 0);
   }
   plan_pack(c);
   CKR(c->jobs.ensure(c->jobs_h.size() * sizeof(PackJob)));
@@ -1730,6 +1732,12 @@ extern "C" int skkr_gpu_set_inverse_start(skkr_ctx *c, int blocked) {
   return SKKR_OK;
 }
 
+extern "C" int skkr_gpu_set_fused_split(skkr_ctx *c, int on) {
+  if (!c) return SKKR_ERR_ARG;
+  c->fused_b = on != 0;
+  return SKKR_OK;
+}
+
 extern "C" int skkr_gpu_set_graphs(skkr_ctx *c, int on) {
   if (!c) return SKKR_ERR_ARG;
   c->graphs = on != 0;
@@ -1828,6 +1836,7 @@ extern "C" int skkr_gpu_run(skkr_ctx *c, skkr_status *status) {
     CKR(mixed_resid_reset(c->mw, st));
     // near the real axis the products also run on the exact-level tile
     mixed_set_precise(c->mw, c->slices_near > 0 && std::fabs(c->ce.y) < c->near_im);
+    mixed_set_fused(c->mw, c->fused_b != 0);
   }
   plan_pack(c);
   CKR(c->jobs.ensure(c->jobs_h.size() * sizeof(PackJob)));

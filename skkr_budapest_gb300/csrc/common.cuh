@@ -2,6 +2,8 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <cstdlib>
+#include <algorithm>
 #include <cstdio>
 
 typedef double2 zd;  // complex*16, interleaved re/im
@@ -77,6 +79,44 @@ inline MatRef mref_map(zd *base, long long sk, long long sc, int ld, const int *
   MatRef r = mref(base, sk, sc, ld);
   for (int i = 0; i < nmap && i < SKKR_MAPN; i++) r.map[i] = map[i];
   return r;
+}
+
+// element range [lo, hi) of an operand's nk x nc items (`cols` columns of at
+// most ld rows each), relative to its base
+inline void mref_span(const MatRef &m, int nk, int nc, int cols, long long *lo, long long *hi) {
+  long long mn = 0, mx = 0;
+  for (int c = 0; c < nc && c < SKKR_MAPN; c++) {
+    const long long o = (long long)m.map[c] * m.sc;
+    mn = c == 0 || o < mn ? o : mn;
+    mx = c == 0 || o > mx ? o : mx;
+  }
+  const long long ks = (long long)(nk - 1) * m.sk;
+  *lo = mn + std::min(0LL, ks);
+  *hi = mx + std::max(0LL, ks) + (long long)cols * m.ld;
+}
+// whether two operands' items may share an element: no when their ranges
+// are apart, or when both sit on the same lattice of item offsets (multiples
+// of g = gcd(sk, sc)) with footprints of cols x ld elements that stay apart
+// modulo g (buffers interleaved item by item in one allocation)
+inline bool mref_overlap(const MatRef &a, const MatRef &b, int nk, int nc, int cols) {
+  long long la, ha, lb, hb;
+  mref_span(a, nk, nc, cols, &la, &ha);
+  mref_span(b, nk, nc, cols, &lb, &hb);
+  const uintptr_t a0 = (uintptr_t)(a.base + la), a1 = (uintptr_t)(a.base + ha);
+  const uintptr_t b0 = (uintptr_t)(b.base + lb), b1 = (uintptr_t)(b.base + hb);
+  if (!(a0 < b1 && b0 < a1)) return false;
+  if (a.sk != b.sk || a.sc != b.sc || a.ld != b.ld) return true;
+  long long g = std::llabs(a.sk), h = std::llabs(a.sc);
+  while (h) {
+    const long long t = g % h;
+    g = h;
+    h = t;
+  }
+  const long long fp = (long long)cols * a.ld;
+  if (g < 2 * fp) return true;
+  const long long d = ((long long)(intptr_t)((uintptr_t)b.base - (uintptr_t)a.base)) / (long long)sizeof(zd);
+  const long long dm = ((d % g) + g) % g;
+  return !(fp <= dm && dm + fp <= g);
 }
 
 // One process-wide lock between CUDA graph capture and the calls that may

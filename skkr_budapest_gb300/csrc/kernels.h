@@ -104,13 +104,18 @@ bool stream_capturing(cudaStream_t st);
 constexpr int MIXED_SLOTS = 6;
 // further Newton steps (at most) for inverses left above the residual limit
 constexpr int NEWTON_EXTRA = 4;
+// A B operand (side 1) is recorded, not split, when products form their B
+// tiles themselves (mixed_set_fused, the default), unless `reused`: an operand
+// that several products read is split once into its slot instead
 int mixed_split(MixedWork *w, int side, int slot, int S, const MatRef &M, int n, int K, int nk, int nc,
-                const int *act, cudaStream_t st);
+                const int *act, cudaStream_t st, bool reused = false);
 // products of 6+ slices on 64-column tiles with 7 TMEM accumulators (levels
 // 0..5 exact): rounding below FP64's, for ill-conditioned energies
 void mixed_set_precise(MixedWork *w, bool on);
 // the 2 x 2 block FP32 start of inverses above 64 rows (default on)
 void mixed_set_blocked(MixedWork *w, bool on);
+// B operands formed by the products themselves (default on)
+void mixed_set_fused(MixedWork *w, bool on);
 int mixed_gemm_staged(MixedWork *w, int mode, int S, int sa, int sb, const MatRef &C, const MatRef &D,
                       const MatRef &E, int n, int K, int nk, int nc, const int *act, cudaStream_t st);
 // C (op) A[:, 0:K] B[0:K, :] for n x K by K x n blocks (A, B already offset

@@ -19,15 +19,20 @@
 // (5 x 96 TMEM columns) and gives about 2^-39 relative to sigma_i tau_j.
 //
 // Complex to real: [Cr Ci] = [Ar Ai] [[Br Bi], [-Bi Br]], i.e. a real GEMM of
-// M = n, N = 2n, K = 2n; the epilogue writes column jj < n into Re C(:,jj) and
-// column n+j into Im C(:,j).
+// M = n, N = 2n, K' = 2K.  The real depth K' runs over groups of 16 complex
+// indices, each group [Re 16 | Im 16] (kpos below), so that one 32-wide
+// k-block holds both parts of 16 complex indices; B' columns 2j and 2j+1
+// are Re and Im of output column j.
 //
 // Staging layouts (bf16, K-major for both UMMA operands, tiled by k-block so
 // that one TMA box is one contiguous block):
-//   A'[item][s][kb][M'][32]   M' = 128 * mtiles, kb < kblocks = ceil(2n/32)
+//   A'[item][s][kb][M'][32]   M' = 128 * mtiles, kb < kblocks = ceil(K/16)
 //   B'[item][s][kb][N'][32]   N' = TN * ntiles (zero padded; TN = 96, or 64
 //                                 for the exact-level tile)
-// Tiles reach shared memory by TMA (3-D tensor maps, 64-byte swizzle).
+// A tiles reach shared memory by TMA (3-D tensor maps, 64-byte swizzle).  B
+// tiles either the same way from B' or, fused, straight from the FP64 B: the
+// ten warps that run the epilogue form each stage's B slices in shared
+// memory while the tensor core works on the previous stage.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
@@ -69,6 +74,9 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
                : "memory");
 }
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
 __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
   uint32_t ok;
   asm volatile(
@@ -92,6 +100,10 @@ __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *tm, in
           "r"(smem_u32(dst)),
       "l"((uint64_t)tm), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
       : "memory");
+}
+// bytes (a multiple of 16, 16-byte aligned) of global memory towards L2
+__device__ __forceinline__ void bulk_prefetch_l2(const void *p, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
 }
 __device__ __forceinline__ void tmem_alloc(uint32_t *dst, uint32_t ncols) {
   asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst)),
@@ -216,13 +228,12 @@ __device__ __forceinline__ void slice_digits(double x, int es, int *dig) {
 __device__ __forceinline__ uint32_t digit_bits(int d, float s, float off) {
   return __float_as_uint(fmaf(__int_as_float(0x4B400000 + d), s, off));
 }
-// the bf16 halves of two such floats as one word, a in the low half
-__device__ __forceinline__ uint32_t pack_bf16(uint32_t a, uint32_t b) { return __byte_perm(a, b, 0x7632); }
-
-// element (row r, K index kk) of one slice region in the k-block tiled layout
+// element (row r, K' index kk) of one slice region in the k-block tiled layout
 __device__ __forceinline__ long long tiled(int r, int kk, int rows) {
   return ((long long)(kk >> 5) * rows + r) * 32 + (kk & 31);
 }
+// K' index of the real (im = 0) or imaginary (im = 1) part of complex index k
+__host__ __device__ __forceinline__ int kpos(int k, int im) { return ((k >> 4) << 5) + (im << 4) + (k & 15); }
 
 // element e (0..3) of four consecutive K indices of one row into the slice
 // words w[p]: the bf16 of digit dg[p] scaled by 2^(wshift - DB p) in half
@@ -258,7 +269,7 @@ __device__ __forceinline__ void store1(const int (&dg)[S], int wshift, uint16_t 
   }
 }
 
-// A' = [Re A, Im A] (n x 2K) from the n x K complex A; rows scaled by their
+// A' = [Re A, Im A] (n x 2K, in the K' order) from the n x K complex A; rows scaled by their
 // max over these K columns.  32 rows per block: the row maxima, then 32 x 32
 // tiles transposed through shared memory, each thread taking four
 // consecutive columns of one row (8-byte stores of every slice) when K is a
@@ -319,8 +330,8 @@ __global__ void __launch_bounds__(256) k_split_a(MatRef A, int n, int K, int nc,
           pack_elem<S, DB>(dr, e, 0, wr);
           pack_elem<S, DB>(di, e, 0, wi);
         }
-        store_words<S>(wr, 0u, base + tiled(r, col, Mp), sstride);
-        store_words<S>(wi, 0u, base + tiled(r, K + col, Mp), sstride);
+        store_words<S>(wr, 0u, base + tiled(r, kpos(col, 0), Mp), sstride);
+        store_words<S>(wi, 0u, base + tiled(r, kpos(col, 1), Mp), sstride);
       }
     } else {
       for (int q = w; q < 32; q += 8) {
@@ -331,8 +342,8 @@ __global__ void __launch_bounds__(256) k_split_a(MatRef A, int n, int K, int nc,
           int dr[S], di[S];
           slice_digits<S, DB>(v.x, es, dr);
           slice_digits<S, DB>(v.y, es, di);
-          store1<S, DB>(dr, 0, 0, base + tiled(r, col, Mp), sstride);
-          store1<S, DB>(di, 0, 0, base + tiled(r, K + col, Mp), sstride);
+          store1<S, DB>(dr, 0, 0, base + tiled(r, kpos(col, 0), Mp), sstride);
+          store1<S, DB>(di, 0, 0, base + tiled(r, kpos(col, 1), Mp), sstride);
         }
       }
     }
@@ -386,10 +397,10 @@ __global__ void __launch_bounds__(256, 3) k_split_b(MatRef B, int n, int K, int 
         pack_elem<S, DB>(dr, e, 16, wr);
         pack_elem<S, DB>(di, e, 16, wi);
       }
-      store_words<S>(wr, 0u, base + tiled(2 * j, k, Np), sstride);
-      store_words<S>(wi, 0x80008000u, base + tiled(2 * j, K + k, Np), sstride);
-      store_words<S>(wi, 0u, base + tiled(2 * j + 1, k, Np), sstride);
-      store_words<S>(wr, 0u, base + tiled(2 * j + 1, K + k, Np), sstride);
+      store_words<S>(wr, 0u, base + tiled(2 * j, kpos(k, 0), Np), sstride);
+      store_words<S>(wi, 0x80008000u, base + tiled(2 * j, kpos(k, 1), Np), sstride);
+      store_words<S>(wi, 0u, base + tiled(2 * j + 1, kpos(k, 0), Np), sstride);
+      store_words<S>(wr, 0u, base + tiled(2 * j + 1, kpos(k, 1), Np), sstride);
     }
   } else {
     for (int k = lane; k < K; k += 32) {
@@ -397,10 +408,10 @@ __global__ void __launch_bounds__(256, 3) k_split_b(MatRef B, int n, int K, int 
       int dr[S], di[S];
       slice_digits<S, DB>(v.x, es, dr);
       slice_digits<S, DB>(v.y, es, di);
-      store1<S, DB>(dr, 16, 0, base + tiled(2 * j, k, Np), sstride);
-      store1<S, DB>(di, 16, 0x8000, base + tiled(2 * j, K + k, Np), sstride);
-      store1<S, DB>(di, 16, 0, base + tiled(2 * j + 1, k, Np), sstride);
-      store1<S, DB>(dr, 16, 0, base + tiled(2 * j + 1, K + k, Np), sstride);
+      store1<S, DB>(dr, 16, 0, base + tiled(2 * j, kpos(k, 0), Np), sstride);
+      store1<S, DB>(di, 16, 0x8000, base + tiled(2 * j, kpos(k, 1), Np), sstride);
+      store1<S, DB>(di, 16, 0, base + tiled(2 * j + 1, kpos(k, 0), Np), sstride);
+      store1<S, DB>(dr, 16, 0, base + tiled(2 * j + 1, kpos(k, 1), Np), sstride);
     }
   }
 }
@@ -411,7 +422,9 @@ struct OzArgs {
   int eoff;             // 32 + 2 (DB - 1): result = acc 2^(sigma_i + tau_j - eoff), acc in 2^-16 units
   int db;               // digit bits DB
   const int *sigma;     // [item][M']  row scale exponents of A
-  const int *tau;       // [item][n]   column scale exponents of B
+  const int *tau;       // [item][n]   column scale exponents of B (staged B)
+  MatRef B;             // the FP64 K x n operand B (fused B)
+  int K;
   MatRef C, D, E;
   const int *act;
   int *err;
@@ -467,6 +480,118 @@ __host__ __device__ constexpr int level_of(int p, int q) { return p + q < NA ? p
 template <int NA>
 __host__ __device__ constexpr int nlevels(int S) { return S < NA ? S : NA; }
 
+// byte offset of bf16 (row r, column t < 32) in a K-major tile of 64-byte rows
+// with the 64-byte swizzle, as TMA lays it out and the UMMA descriptor reads
+// it: the 16-byte chunk index XORed with address bits 7-8 (bits 1-2 of r)
+__device__ __forceinline__ uint32_t sw64_off(int r, int t) {
+  return (uint32_t)(r * 64 + ((((t >> 3) ^ (r >> 1)) & 3) << 4) + ((t & 7) << 1));
+}
+
+// Fused B operand, run by the 320 threads of warps 2-11 of k_ozaki: first
+// the scale exponents of the CTA's TN/2 complex columns over the whole depth
+// K (into col_exp, which the epilogue reads as well), then per k-block the S
+// B tiles of a stage: thread t takes column t/4 and the four complex indices
+// 16 kb + 4 (t%4) .. +3, forms their digits once (as k_split_b does) and
+// stores them four times (rows 2j and 2j+1, the Re and Im halves of the
+// k-block, -Im with flipped sign bits).  The next k-block's values are loaded
+// before the wait for the stage.  Each thread orders its stores before the
+// tensor core's reads (proxy fence) and arrives on the stage's full barrier.
+template <int S, int TN, int DB, int NSTAGE>
+__device__ __forceinline__ void fused_b_tiles(const OzArgs &g, int item, int nt, unsigned char *sb0,
+                                              uint32_t stage_bytes, uint64_t *bar_full, uint64_t *bar_empty,
+                                              int *col_exp, volatile int &failed) {
+  constexpr int NCT = OZ_THREADS - 64;
+  constexpr uint32_t B_BYTES = TN * KB * 2;
+  const int ct = threadIdx.x - 64, lane = threadIdx.x & 31;
+  const zd *bsrc = mat_ptr(g.B, item / g.nc, item % g.nc);
+  const int j0 = (nt * TN) >> 1;
+  // warp w, four columns 4w .. 4w+3 per round (40 per round), 16 loads of
+  // each lane in flight
+  for (int jl0 = 4 * (ct >> 5); jl0 < TN / 2; jl0 += 4 * (NCT / 32)) {
+    unsigned long long m[4] = {0, 0, 0, 0};
+    for (int kc = 0; kc < g.K; kc += 128) {
+      zd v[4][4];
+#pragma unroll
+      for (int c = 0; c < 4; c++)
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+          const int k = kc + lane + 32 * i, j = j0 + jl0 + c;
+          v[c][i] = (k < g.K && j < g.n && jl0 + c < TN / 2) ? bsrc[k + (long long)j * g.B.ld]
+                                                             : make_double2(0.0, 0.0);
+        }
+#pragma unroll
+      for (int c = 0; c < 4; c++)
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+          const unsigned long long bx = abs_bits(v[c][i].x), by = abs_bits(v[c][i].y);
+          m[c] = bx > m[c] ? bx : m[c];
+          m[c] = by > m[c] ? by : m[c];
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long t = __shfl_xor_sync(0xffffffffu, m[c], o);
+        m[c] = t > m[c] ? t : m[c];
+      }
+      const int jl = jl0 + c;
+      if (lane == 0 && jl < TN / 2) col_exp[jl] = j0 + jl < g.n ? scale_exp(m[c]) : 0;
+    }
+  }
+  asm volatile("bar.sync 1, %0;" ::"n"(NCT) : "memory");
+  const int jl = ct >> 2, kq = ct & 3;
+  const bool on = ct < 2 * TN;
+  const bool col_ok = on && j0 + jl < g.n;
+  const zd *bcol = bsrc + (long long)(col_ok ? j0 + jl : 0) * g.B.ld;
+  const int es = on ? col_exp[jl] : 0;
+  zd cur[4], nxt[4];
+  auto fetch = [&](int kb, zd(&v)[4]) {
+    const int k = 16 * kb + 4 * kq;
+#pragma unroll
+    for (int e = 0; e < 4; e++) v[e] = (col_ok && k + e < g.K) ? bcol[k + e] : make_double2(0.0, 0.0);
+  };
+  fetch(0, cur);
+  const int nkb = g.kblocks;
+  for (int kb = 0; kb < nkb && !failed; kb++) {
+    const int st = kb % NSTAGE;
+    if (kb + 1 < nkb) fetch(kb + 1, nxt);
+    if (kb >= NSTAGE && !mbar_wait(&bar_empty[st], ((kb / NSTAGE) - 1) & 1)) {
+      failed = 1;
+      break;
+    }
+    if (on) {
+      uint2 wr[S], wi[S];
+#pragma unroll
+      for (int p = 0; p < S; p++) wr[p] = wi[p] = make_uint2(0u, 0u);
+#pragma unroll
+      for (int e = 0; e < 4; e++) {
+        int dr[S], di[S];
+        slice_digits<S, DB>(cur[e].x, es, dr);
+        slice_digits<S, DB>(cur[e].y, es, di);
+        pack_elem<S, DB>(dr, e, 16, wr);
+        pack_elem<S, DB>(di, e, 16, wi);
+      }
+      unsigned char *sb = sb0 + st * stage_bytes;
+      const int r = 2 * jl, t = 4 * kq;
+      const uint32_t o0 = sw64_off(r, t), o1 = sw64_off(r, t + 16), o2 = sw64_off(r + 1, t),
+                     o3 = sw64_off(r + 1, t + 16);
+#pragma unroll
+      for (int p = 0; p < S; p++) {
+        unsigned char *tp = sb + p * B_BYTES;
+        *reinterpret_cast<uint2 *>(tp + o0) = wr[p];
+        *reinterpret_cast<uint2 *>(tp + o1) = make_uint2(wi[p].x ^ 0x80008000u, wi[p].y ^ 0x80008000u);
+        *reinterpret_cast<uint2 *>(tp + o2) = wi[p];
+        *reinterpret_cast<uint2 *>(tp + o3) = wr[p];
+      }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_arrive(&bar_full[st]);
+#pragma unroll
+    for (int e = 0; e < 4; e++) cur[e] = nxt[e];
+  }
+}
+
 // TN: N tile (TMEM columns per accumulator); NA: TMEM accumulators, one per
 // level p+q = 0..NA-2 and a shared tail for the deeper levels (NA * TN <= 512).
 // (96, 5) is the default tile; (64, 7) keeps levels 0..5 exact and pushes the
@@ -474,10 +599,14 @@ __host__ __device__ constexpr int nlevels(int S) { return S < NA ? S : NA; }
 // levels would not do: with the shared tail from level 3 on, the tensor
 // core's truncating FP32 addition leaves ~2^-47 of the leading level per
 // accumulation step in it (4e-12 over a 128-deep product instead of 7e-14).
-template <int S, int TN, int NA>
+// FB = 0: B tiles by TMA from the staged B'; FB = DB (7 or 8): B fused, its
+// tiles formed from the FP64 g.B by warps 2-11 (tmB unused).
+template <int S, int TN, int NA, int FB>
 __global__ void __launch_bounds__(OZ_THREADS, 1) k_ozaki(const __grid_constant__ CUtensorMap tmA,
                                                   const __grid_constant__ CUtensorMap tmB, OzArgs g) {
   static_assert(NA * TN <= 512 && TN % 32 == 0, "accumulators must fit the 512 TMEM columns");
+  constexpr int NCT = OZ_THREADS - 64;  // threads of warps 2-11
+  static_assert(FB == 0 || 2 * TN <= NCT, "fused B: one (column, four k) group per thread of warps 2-11");
   const int item = blockIdx.y;
   if (g.act && !g.act[item]) return;
   const int mt = blockIdx.x / g.ntiles, nt = blockIdx.x % g.ntiles;
@@ -497,7 +626,16 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_ozaki(const __grid_constant__
     tmem_alloc(&tmem_base, 512);
     tmem_relinquish();
   }
-  if (threadIdx.x >= 64) {  // warps 2-11: column scales of the tile (read by the epilogue)
+  if (FB > 0 && threadIdx.x >= 64 && lane == 0) {
+    // fused B: start the CTA's K x TN/2 block of B towards L2 (one bulk
+    // prefetch per column, lane 0 of warps 2-11)
+    const zd *bsrc = mat_ptr(g.B, item / g.nc, item % g.nc);
+    for (int jl = warp - 2; jl < TN / 2; jl += NCT / 32) {
+      const int j = (nt * TN) / 2 + jl;
+      if (j < g.n) bulk_prefetch_l2(bsrc + (long long)j * g.B.ld, (uint32_t)g.K * (uint32_t)sizeof(zd));
+    }
+  }
+  if (FB == 0 && threadIdx.x >= 64) {  // warps 2-11: column scales of the tile (read by the epilogue)
     for (int t = threadIdx.x - 64; t < TN / 2; t += blockDim.x - 64) {
       const int j = (nt * TN) / 2 + t;
       col_exp[t] = j < g.n ? g.tau[(long long)item * g.n + j] : 0;
@@ -508,7 +646,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_ozaki(const __grid_constant__
     issued_kb = -1;
     consumed_kb = -1;
     for (int i = 0; i < NSTAGE; i++) {
-      mbar_init(&bar_full[i], 1);
+      mbar_init(&bar_full[i], FB ? 1 + NCT : 1);  // fused B: every converting thread arrives too
       mbar_init(&bar_empty[i], 1);
     }
     mbar_init(&bar_acc, 1);
@@ -531,12 +669,12 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_ozaki(const __grid_constant__
         break;
       }
       unsigned char *sA = tiles + st * STAGE_BYTES, *sB = sA + S * A_BYTES;
-      mbar_expect_tx(&bar_full[st], STAGE_BYTES);
+      mbar_expect_tx(&bar_full[st], FB ? S * A_BYTES : STAGE_BYTES);
 #pragma unroll
       for (int sl = 0; sl < S; sl++) {
         const int z = (item * S + sl) * nkb + kb;
         tma_load_3d(sA + sl * A_BYTES, &tmA, 0, mt * MT, z, &bar_full[st]);
-        tma_load_3d(sB + sl * B_BYTES, &tmB, 0, nt * TN, z, &bar_full[st]);
+        if (FB == 0) tma_load_3d(sB + sl * B_BYTES, &tmB, 0, nt * TN, z, &bar_full[st]);
       }
       issued_kb = kb;
     }
@@ -570,6 +708,9 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_ozaki(const __grid_constant__
       consumed_kb = kb;
     }
     umma_commit(&bar_acc);  // accumulators complete
+  } else if (warp >= 2) {
+    if constexpr (FB > 0) fused_b_tiles<S, TN, FB, NSTAGE>(g, item, nt, tiles + S * A_BYTES, STAGE_BYTES,
+                                                           bar_full, bar_empty, col_exp, failed);
   }
   __syncthreads();
   // all MMAs (and with them every TMA load they consumed) are done once
@@ -1006,10 +1147,13 @@ struct Stage {
   size_t cap = 0;
   int *scale = nullptr;    // row (A) / column (B) scale exponents
   size_t scap = 0;
-  int n = -1, K = -1;      // padding layout
+  int n = -1, K = -1;      // padding layout of p
   int tn = 0;              // N tile the B layout is padded to
-  int S = 0, DB = 0;
+  int S = 0, DB = 0;       // the operand held: slices, digit base, dims, items
+  int cn = -1, cK = -1;
   long long items = 0;
+  bool fused = false;      // B only: not split; each product forms its tiles from src
+  MatRef src;
 };
 
 struct MixedWork {
@@ -1029,13 +1173,15 @@ struct MixedWork {
   unsigned long long *nref = nullptr;  // [0] inverses that took further Newton steps, [1] kernels run by the
                                        // IF bodies of captured further steps (device counts)
   cudaStream_t side = nullptr;         // captures the bodies of conditional graph nodes
-  int smem_set[32] = {0};
+  int smem_set[64] = {0};
   bool precise = false;    // (64, 7) tile: exact levels 0..5 (mixed_set_precise)
+  bool fuse_b = true;      // B operands formed inside the product (mixed_set_fused)
   bool blocked = true;     // 2 x 2 block start of inverses above 64 rows (mixed_set_blocked)
 };
 
 void mixed_set_precise(MixedWork *w, bool on) { w->precise = on; }
 void mixed_set_blocked(MixedWork *w, bool on) { w->blocked = on; }
+void mixed_set_fused(MixedWork *w, bool on) { w->fuse_b = on; }
 
 // the (64, 7) tile serves products of 6 slices and more (the low-slice
 // Newton corrections keep the default tile); split and multiply agree on it
@@ -1157,14 +1303,30 @@ static void oz_digits(int S, int K, int *Se, int *DB) {
   *Se = (*DB == 8 && S > 7) ? 7 : S;
 }
 
+// B operands of the default tile are fused into the product unless turned off
+static bool fuses_b(const MixedWork *w, int S) { return w->fuse_b && !use_precise(w, S); }
+
+// side 1 with fuses_b: the slot only records B (the product reads it when it
+// runs: B must not change in between, which every caller keeps); `real`
+// (an operand several products read) splits it all the same
 template <int S, int DB>
 static int split_s(MixedWork *w, int side, int slot, const MatRef &M, int n, int K, int nk, int nc,
-                   const int *act, cudaStream_t st) {
+                   const int *act, cudaStream_t st, bool real = false) {
   int Mp, Np, Kp, mtiles, ntiles, kblocks;
   const int tn = use_precise(w, S) ? 64 : NT;
   oz_dims(n, K, tn, &Mp, &Np, &Kp, &mtiles, &ntiles, &kblocks);
   const long long items = (long long)nk * nc;
   Stage &sg = side == 0 ? w->A[slot] : w->B[slot];
+  sg.S = S;
+  sg.DB = DB;
+  sg.cn = n;
+  sg.cK = K;
+  sg.items = items;
+  sg.fused = side == 1 && !real && fuses_b(w, S);
+  if (sg.fused) {
+    sg.src = M;
+    return 0;
+  }
   const int rows = side == 0 ? Mp : Np;
   int rc;
   // a buffer cannot be reallocated inside a captured graph: the eager run
@@ -1174,7 +1336,7 @@ static int split_s(MixedWork *w, int side, int slot, const MatRef &M, int n, int
   if ((rc = grow((void **)&sg.scale, &sg.scap, (size_t)items * (side == 0 ? Mp : n) * sizeof(int), false)))
     return rc;
   if (sg.n != n || sg.K != K || (side == 1 && sg.tn != tn)) {
-    // padding (rows beyond the operand, columns >= 2K of every slice region)
+    // padding (rows beyond the operand, K' places of complex indices >= K)
     // must be zero; a new layout clears what an earlier one wrote there
     if (cudaMemsetAsync(sg.p, 0, sg.cap, st) != cudaSuccess) return SKKR_ERR_CUDA;
     sg.n = n;
@@ -1195,9 +1357,20 @@ static int split_s(MixedWork *w, int side, int slot, const MatRef &M, int n, int
   }
   kstat_end(st);
   SKKR_LAUNCHED();
-  sg.S = S;
-  sg.DB = DB;
-  sg.items = items;
+  return 0;
+}
+
+template <int S, int TN, int NA, int FB>
+static int oz_launch(MixedWork *w, int key, dim3 grid, const CUtensorMap &ma, const CUtensorMap &mb,
+                     const OzArgs &g, cudaStream_t st) {
+  const size_t smem = oz_smem_bytes(S, TN);
+  if (!w->smem_set[key]) {
+    if (cudaFuncSetAttribute(k_ozaki<S, TN, NA, FB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
+      return SKKR_ERR_CUDA;
+    w->smem_set[key] = 1;
+  }
+  k_ozaki<S, TN, NA, FB><<<grid, OZ_THREADS, smem, st>>>(ma, mb, g);
   return 0;
 }
 
@@ -1208,20 +1381,29 @@ static int gemm_s(MixedWork *w, int mode, int sa, int sb, const MatRef &C, const
   int Mp, Np, Kp, mtiles, ntiles, kblocks;
   oz_dims(n, K, TN, &Mp, &Np, &Kp, &mtiles, &ntiles, &kblocks);
   const long long items = (long long)nk * nc;
-  const Stage &A = w->A[sa], &B = w->B[sb];
-  if (A.S != S || B.S != S || A.DB != B.DB || A.n != n || B.n != n || A.K != K || B.K != K ||
-      A.items != items || B.items != items || B.tn != TN)
+  const Stage &A = w->A[sa];
+  Stage &B = w->B[sb];
+  if (A.fused || A.S != S || B.S != S || A.DB != B.DB || A.cn != n || B.cn != n || A.cK != K || B.cK != K ||
+      A.items != items || B.items != items || (!B.fused && B.tn != TN))
     return SKKR_ERR_ARG;  // the slots do not hold splits of this product's operands
+  // a fused B that the product writes over (C, D or E) is split first, so
+  // that no CTA reads an element another one has already replaced
+  if (B.fused && (mref_overlap(B.src, C, nk, nc, n) || mref_overlap(B.src, D, nk, nc, n) ||
+                  mref_overlap(B.src, E, nk, nc, n))) {
+    int rc;
+    if constexpr (S <= 7)
+      rc = A.DB == 8 ? split_s<S, 8>(w, 1, sb, B.src, n, K, nk, nc, act, st, true)
+                     : split_s<S, 7>(w, 1, sb, B.src, n, K, nk, nc, act, st, true);
+    else
+      rc = split_s<S, 7>(w, 1, sb, B.src, n, K, nk, nc, act, st, true);
+    if (rc) return rc;
+  }
   CUtensorMap ma, mb;
-  if (make_map(&ma, A.p, Mp, items * S * kblocks, MT) || make_map(&mb, B.p, Np, items * S * kblocks, TN))
+  if (make_map(&ma, A.p, Mp, items * S * kblocks, MT)) return SKKR_ERR_CUDA;
+  if (B.fused) {
+    mb = ma;  // unused by the fused kernel
+  } else if (make_map(&mb, B.p, Np, items * S * kblocks, TN)) {
     return SKKR_ERR_CUDA;
-  const size_t smem = oz_smem_bytes(S, TN);
-  const int sk = S + (TN == NT ? 0 : 16);
-  if (!w->smem_set[sk]) {
-    if (cudaFuncSetAttribute(k_ozaki<S, TN, NA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-        cudaSuccess)
-      return SKKR_ERR_CUDA;
-    w->smem_set[sk] = 1;
   }
   OzArgs g;
   g.n = n;
@@ -1234,6 +1416,8 @@ static int gemm_s(MixedWork *w, int mode, int sa, int sb, const MatRef &C, const
   g.db = A.DB;
   g.sigma = A.scale;
   g.tau = B.scale;
+  g.B = B.src;
+  g.K = K;
   g.C = C;
   g.D = D;
   g.E = E;
@@ -1245,14 +1429,28 @@ static int gemm_s(MixedWork *w, int mode, int sa, int sb, const MatRef &C, const
   kstat_begin2(KS_OZAKI, (double)(S * (S + 1) / 2) * 8.0 * n * (double)n * K * (double)active,
                8.0 * n * (double)n * K * (double)active, st);
   dim3 grid(mtiles * ntiles, items);
-  k_ozaki<S, TN, NA><<<grid, OZ_THREADS, smem, st>>>(ma, mb, g);
+  // shared-memory attribute keys: S + 16 x (0 staged, 1 exact-level tile, 2 / 3 fused B at 8 / 7 digit bits)
+  int rc;
+  if (!B.fused) {
+    rc = oz_launch<S, TN, NA, 0>(w, S + (TN == NT ? 0 : 16), grid, ma, mb, g, st);
+  } else if constexpr (TN == NT && NA == NACC) {
+    if (A.DB == 8) {
+      if constexpr (S <= 7) rc = oz_launch<S, TN, NA, 8>(w, S + 32, grid, ma, mb, g, st);
+      else rc = SKKR_ERR_ARG;
+    } else {
+      rc = oz_launch<S, TN, NA, 7>(w, S + 48, grid, ma, mb, g, st);
+    }
+  } else {
+    rc = SKKR_ERR_ARG;  // fused B only on the default tile
+  }
   kstat_end(st);
+  if (rc) return rc;
   SKKR_LAUNCHED();
   return 0;
 }
 
 int mixed_split(MixedWork *w, int side, int slot, int S, const MatRef &M, int n, int K, int nk, int nc,
-                const int *act, cudaStream_t st) {
+                const int *act, cudaStream_t st, bool reused) {
   if (n < 1 || n > 256 || K < 1 || K > 256 || nk * (long long)nc > 65535 || slot < 0 ||
       slot >= MIXED_SLOTS || (side != 0 && side != 1))
     return SKKR_ERR_ARG;
@@ -1260,21 +1458,21 @@ int mixed_split(MixedWork *w, int side, int slot, int S, const MatRef &M, int n,
   oz_digits(S, K, &Se, &DB);
   if (DB == 8) {
     switch (Se) {
-      case 3: return split_s<3, 8>(w, side, slot, M, n, K, nk, nc, act, st);
-      case 4: return split_s<4, 8>(w, side, slot, M, n, K, nk, nc, act, st);
-      case 5: return split_s<5, 8>(w, side, slot, M, n, K, nk, nc, act, st);
-      case 6: return split_s<6, 8>(w, side, slot, M, n, K, nk, nc, act, st);
-      case 7: return split_s<7, 8>(w, side, slot, M, n, K, nk, nc, act, st);
+      case 3: return split_s<3, 8>(w, side, slot, M, n, K, nk, nc, act, st, reused);
+      case 4: return split_s<4, 8>(w, side, slot, M, n, K, nk, nc, act, st, reused);
+      case 5: return split_s<5, 8>(w, side, slot, M, n, K, nk, nc, act, st, reused);
+      case 6: return split_s<6, 8>(w, side, slot, M, n, K, nk, nc, act, st, reused);
+      case 7: return split_s<7, 8>(w, side, slot, M, n, K, nk, nc, act, st, reused);
       default: return SKKR_ERR_ARG;
     }
   }
   switch (Se) {
-    case 3: return split_s<3, 7>(w, side, slot, M, n, K, nk, nc, act, st);
-    case 4: return split_s<4, 7>(w, side, slot, M, n, K, nk, nc, act, st);
-    case 5: return split_s<5, 7>(w, side, slot, M, n, K, nk, nc, act, st);
-    case 6: return split_s<6, 7>(w, side, slot, M, n, K, nk, nc, act, st);
-    case 7: return split_s<7, 7>(w, side, slot, M, n, K, nk, nc, act, st);
-    case 8: return split_s<8, 7>(w, side, slot, M, n, K, nk, nc, act, st);
+    case 3: return split_s<3, 7>(w, side, slot, M, n, K, nk, nc, act, st, reused);
+    case 4: return split_s<4, 7>(w, side, slot, M, n, K, nk, nc, act, st, reused);
+    case 5: return split_s<5, 7>(w, side, slot, M, n, K, nk, nc, act, st, reused);
+    case 6: return split_s<6, 7>(w, side, slot, M, n, K, nk, nc, act, st, reused);
+    case 7: return split_s<7, 7>(w, side, slot, M, n, K, nk, nc, act, st, reused);
+    case 8: return split_s<8, 7>(w, side, slot, M, n, K, nk, nc, act, st, reused);
     default: return SKKR_ERR_ARG;
   }
 }
@@ -1562,12 +1760,14 @@ int mixed_zinv(MixedWork *w, const MatRef &A, const MatRef &X, int n, int nk, in
   if ((rc = grow((void **)&w->rnorm, &w->rn_cap, (size_t)items * sizeof(double), false))) return rc;
   if ((rc = grow((void **)&w->flag, &w->flag_cap, (size_t)items * sizeof(int), false))) return rc;
   if ((rc = grow((void **)&w->mark, &w->mark_cap, (size_t)items * sizeof(int), false))) return rc;
-  // the further Newton steps split X and R into slot 5 at sres slices (the
-  // standard correction uses 3): reserve that size, for either B tile, while
-  // not capturing, so that a captured step never has to grow the slot
+  // the further Newton steps split X (and, unless B is fused, R) into slot 5
+  // at sres slices (the standard correction uses 3): reserve that size, for
+  // either B tile, while not capturing, so that a captured step never has to
+  // grow the slot
+  int Se, DB;
+  oz_digits(sres, n, &Se, &DB);
   if (!stream_capturing(st)) {
-    int Se, DB, Mp, Np, Kp, mt, ntl, kbl;
-    oz_digits(sres, n, &Se, &DB);
+    int Mp, Np, Kp, mt, ntl, kbl;
     size_t bb = 0, ba = 0;
     for (int tn : {NT, 64}) {
       oz_dims(n, n, tn, &Mp, &Np, &Kp, &mt, &ntl, &kbl);
@@ -1575,7 +1775,7 @@ int mixed_zinv(MixedWork *w, const MatRef &A, const MatRef &X, int n, int nk, in
       bb = std::max(bb, (size_t)items * Se * Np * Kp * 2);
     }
     if ((rc = grow(&w->A[5].p, &w->A[5].cap, ba, true))) return rc;
-    if ((rc = grow(&w->B[5].p, &w->B[5].cap, bb, true))) return rc;
+    if (!fuses_b(w, Se) && (rc = grow(&w->B[5].p, &w->B[5].cap, bb, true))) return rc;
   }
   // A itself serves the Gauss-Jordan start, the residuals and the FP64 redo
   // unless X overwrites it (in place): then a copy does
@@ -1614,9 +1814,11 @@ int mixed_zinv(MixedWork *w, const MatRef &A, const MatRef &X, int n, int nk, in
   for (int e = 0; e < NEWTON_EXTRA; e++) {
     cudaGraphConditionalHandle h = 0;
     if (cap && (rc = cond_handle(st, &h))) return rc;
-    // the IF body below launches 6 kernels (3 splits, 2 sliced products, 1 norm)
+    // the IF body below launches 2 sliced products, 1 norm and the splits:
+    // 3, or 1 with the B operands fused
+    const int nbody = fuses_b(w, Se) ? 4 : 6;
     k_newton_select<<<1, 1024, 0, st>>>(w->rnorm, act, (int)items, 1e-6, 0.5, w->mark, w->cnt, w->nref, e == 0,
-                                        h, cap ? 1 : 0, 6);
+                                        h, cap ? 1 : 0, nbody);
     SKKR_LAUNCHED();
     const long long l_body = g_skkr_launches;
     cudaStream_t sx = st;
@@ -1647,7 +1849,7 @@ int mixed_zinv(MixedWork *w, const MatRef &A, const MatRef &X, int n, int nk, in
       if (!rc) rc = rc2;
       // the body's kernels are counted when they run (nref[1]), not here
       g_skkr_launches = l_body;
-      g_skkr_if_captured += 6;
+      g_skkr_if_captured += nbody;
     }
     if (rc) return rc;
     skkr_set_active_items(hint);

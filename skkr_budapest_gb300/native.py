@@ -92,6 +92,7 @@ def lib():
         L.skkr_gpu_set_graphs.argtypes = [P, I]
         L.skkr_gpu_set_newton.argtypes = [P, I]
         L.skkr_gpu_set_inverse_start.argtypes = [P, I]
+        L.skkr_gpu_set_fused_split.argtypes = [P, I]
         L.skkr_gpu_stage_kambe.argtypes = [P, P]
         L.skkr_gpu_cpacoord_many.argtypes = [I, P, P, P]
         L.skkr_gpu_contour.argtypes = [P, I, P, P]

@@ -175,3 +175,37 @@ def test_blocked_start_matches_whole_matrix_start():
     assert rel(out[True]["tauc"], out[False]["tauc"]) < 1e-11
     o = O.cpacoord(sub, nthreads=8)
     assert rel(out[True]["tauc"], o["tauc"]) < TOL_MIXED
+
+
+@pytest.mark.parametrize("case", ["fcc", "rel_pl4", "rel_near_axis", "alloy"])
+def test_fused_b_operand_is_bit_identical_to_staged(case):
+    """The products that form their B slices in shared memory give the same
+    bits as the products that load them from a staging buffer: the same
+    digits in the same tile places.  Covers K = 18 (ragged k-blocks), the
+    128-row interface (decimation, Newton, tau2d), an energy near the real
+    axis (the exact-level tile keeps staged B for its 6-slice products) and a
+    CPA alloy."""
+    if case == "fcc":
+        ep = W.energy_problem(W.plain_fcc(nset=6), 2)
+    elif case == "alloy":
+        spec = W.rel_bcc_cpa(nsets=[2] * 24)
+        spec.lmax = 2
+        ep = W.energy_problem(spec, 14)
+    else:
+        ep = W.energy_problem(W.rel_bcc(), 19 if case == "rel_pl4" else 0)
+        idx = np.arange(0, ep.nk, 97)
+        ep = ep.with_k(ep.xk[idx], ep.wk[idx] / ep.wk[idx].sum())
+    out = {}
+    for fused in (True, False):
+        ctx = api.Context.for_problem(ep, "mixed")
+        try:
+            ctx.set_fused_split(fused)
+            if case == "rel_near_axis":  # Im E = 0.016 Ry: the near-axis policy from 0.05 Ry
+                ctx.set_mixed_policy(near_im=0.05)
+            out[fused] = ctx.cpacoord(ep)
+        finally:
+            ctx.close()
+        assert out[fused]["status"] == 0
+    for key in ("tauc", "taua", "taub", "tminv"):
+        assert np.array_equal(out[True][key], out[False][key]), key
+    assert out[True]["cpa_iterations"] == out[False]["cpa_iterations"]
