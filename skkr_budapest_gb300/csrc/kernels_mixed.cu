@@ -47,6 +47,7 @@
 
 #include "../../include/skkr_gpu.h"
 #include "kernels.h"
+#include "slicing.cuh"
 
 namespace {
 
@@ -165,69 +166,8 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int m, int n) {
 }
 
 // ------------------------------------------------------------------ slicing
-// All element-wise work below uses integer arithmetic on the IEEE bit
-// patterns: this GPU issues about 2 FP64 operations per clock per SM against
-// 64 integer operations, so a single FP64 multiply per element would dominate.
-//
-// Scales are powers of two kept as exponents: sigma = 2^es with
-// es = (biased exponent of max |x|) - 1022, i.e. sigma >= max |x| > sigma/2.
+// (abs_bits, scale_exp, slice_digits, digit_bits, slice4: slicing.cuh)
 
-// |x| bits of a double (non-negative doubles order like their bit patterns)
-__device__ __forceinline__ unsigned long long abs_bits(double x) {
-  return (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
-}
-// log2 of the power-of-two scale for a max-|x| bit pattern (0 for zero)
-__device__ __forceinline__ int scale_exp(unsigned long long amax_bits) {
-  const int ex = (int)(amax_bits >> 52);
-  return ex == 0 ? 0 : ex - 1022;
-}
-// round(x * 2^E) as a signed 64-bit integer (|result| < 2^62 assumed), using
-// only integer operations; zero and subnormal inputs give 0
-__device__ __forceinline__ long long fix_round(double x, int E) {
-  const long long b = __double_as_longlong(x);
-  const int ex = (int)((b >> 52) & 0x7FF);
-  if (ex == 0) return 0;
-  const long long mant = (b & 0xFFFFFFFFFFFFFll) | 0x10000000000000ll;
-  const int sh = ex - 1075 + E;
-  long long m;
-  if (sh >= 0) {
-    m = sh >= 11 ? 0 : mant << sh;  // callers keep |x 2^E| < 2^62
-  } else {
-    const int r = -sh;
-    m = r >= 63 ? 0 : (mant + (1ll << (r - 1))) >> r;
-  }
-  return b < 0 ? -m : m;
-}
-__device__ __forceinline__ float pow2f(int e) { return __int_as_float((127 + e) << 23); }
-
-// balanced base-2^DB digits of Y = round(x 2^((DB-1) + DB(S-1)) / sigma),
-// most significant first (|d| <= 2^(DB-1)).  DB = 8 for K = 2n <= 256; DB = 7
-// above, so that every FP32 level accumulator (at most 4 (p,q) pairs of
-// |d d| <= 2^(2DB-2) over K terms) stays an exact integer below 2^24.
-template <int S, int DB>
-__device__ __forceinline__ void slice_digits(double x, int es, int *dig) {
-  static_assert(DB * S <= 62, "digits must fit the 62-bit fixed-point value");
-  const long long Y = fix_round(x, (DB - 1) + DB * (S - 1) - es);
-  const unsigned long long u = (unsigned long long)(Y < 0 ? -Y : Y);
-  const bool neg = Y < 0;
-  constexpr int HALF = 1 << (DB - 1);
-  int carry = 0;
-#pragma unroll
-  for (int q = 0; q < S; q++) {  // q = 0: least significant digit
-    int d = (int)((u >> (DB * q)) & ((1ull << DB) - 1)) + carry;
-    carry = d > HALF;
-    d -= carry << DB;
-    dig[S - 1 - q] = neg ? -d : d;
-  }
-}
-
-// float bits of d 2^k for an integer digit |d| <= 128, from one integer add
-// and one FMA: (1.5 2^23 + d) 2^k - 1.5 2^23 2^k is exact, and with at most
-// eight significant bits the value is a bf16 held in the upper half of the
-// float (zero digits give +0).  s = 2^k, off = -1.5 2^23 2^k.
-__device__ __forceinline__ uint32_t digit_bits(int d, float s, float off) {
-  return __float_as_uint(fmaf(__int_as_float(0x4B400000 + d), s, off));
-}
 // element (row r, K' index kk) of one slice region in the k-block tiled layout
 __device__ __forceinline__ long long tiled(int r, int kk, int rows) {
   return ((long long)(kk >> 5) * rows + r) * 32 + (kk & 31);
@@ -235,27 +175,13 @@ __device__ __forceinline__ long long tiled(int r, int kk, int rows) {
 // K' index of the real (im = 0) or imaginary (im = 1) part of complex index k
 __host__ __device__ __forceinline__ int kpos(int k, int im) { return ((k >> 4) << 5) + (im << 4) + (k & 15); }
 
-// element e (0..3) of four consecutive K indices of one row into the slice
-// words w[p]: the bf16 of digit dg[p] scaled by 2^(wshift - DB p) in half
-// e % 2 of word w[p].x (e < 2) or w[p].y; the words start at zero
-template <int S, int DB>
-__device__ __forceinline__ void pack_elem(const int (&dg)[S], int e, int wshift, uint2 (&w)[S]) {
-#pragma unroll
-  for (int p = 0; p < S; p++) {
-    const float sc = pow2f(wshift - DB * p);
-    const uint32_t u = digit_bits(dg[p], sc, -12582912.0f * sc);
-    const uint32_t h = (e & 1) ? (u & 0xFFFF0000u) : (u >> 16);
-    if (e < 2) w[p].x |= h;
-    else w[p].y |= h;
-  }
-}
 // the S words at dst + p sstride, sign bits flipped by `flip` (0 or 0x80008000)
 template <int S>
-__device__ __forceinline__ void store_words(const uint2 (&w)[S], uint32_t flip, __nv_bfloat16 *dst,
+__device__ __forceinline__ void store_words(const uint32_t (&w)[S][2], uint32_t flip, __nv_bfloat16 *dst,
                                             long long sstride) {
 #pragma unroll
   for (int p = 0; p < S; p++)
-    *reinterpret_cast<uint2 *>(dst + p * sstride) = make_uint2(w[p].x ^ flip, w[p].y ^ flip);
+    *reinterpret_cast<uint2 *>(dst + p * sstride) = make_uint2(w[p][0] ^ flip, w[p][1] ^ flip);
 }
 // one element, slices p = 0..S-1 (the shapes of no four-element group)
 template <int S, int DB>
@@ -317,19 +243,14 @@ __global__ void __launch_bounds__(256) k_split_a(MatRef A, int n, int K, int nc,
       // thread t: row r0 + t / 8, columns c0 + 4 (t % 8) .. +3
       const int q = threadIdx.x >> 3, c4 = (threadIdx.x & 7) * 4, r = r0 + q, col = c0 + c4;
       if (r < n && col < K) {
-        const int es = sc[q];
-        uint2 wr[S], wi[S];
-#pragma unroll
-        for (int p = 0; p < S; p++) wr[p] = wi[p] = make_uint2(0u, 0u);
+        double re[4], im[4];
 #pragma unroll
         for (int e = 0; e < 4; e++) {
-          const zd v = T[q][c4 + e];
-          int dr[S], di[S];
-          slice_digits<S, DB>(v.x, es, dr);
-          slice_digits<S, DB>(v.y, es, di);
-          pack_elem<S, DB>(dr, e, 0, wr);
-          pack_elem<S, DB>(di, e, 0, wi);
+          re[e] = T[q][c4 + e].x;
+          im[e] = T[q][c4 + e].y;
         }
+        uint32_t wr[S][2], wi[S][2];
+        slice4<S, DB>(re, im, sc[q], 0, wr, wi);
         store_words<S>(wr, 0u, base + tiled(r, kpos(col, 0), Mp), sstride);
         store_words<S>(wi, 0u, base + tiled(r, kpos(col, 1), Mp), sstride);
       }
@@ -385,18 +306,15 @@ __global__ void __launch_bounds__(256, 3) k_split_b(MatRef B, int n, int K, int 
   __nv_bfloat16 *base = out + (long long)item * S * sstride;
   if ((K & 3) == 0) {
     for (int k = 4 * lane; k < K; k += 128) {
-      uint2 wr[S], wi[S];
-#pragma unroll
-      for (int p = 0; p < S; p++) wr[p] = wi[p] = make_uint2(0u, 0u);
+      double re[4], im[4];
 #pragma unroll
       for (int e = 0; e < 4; e++) {
         const zd v = b[k + e];
-        int dr[S], di[S];
-        slice_digits<S, DB>(v.x, es, dr);
-        slice_digits<S, DB>(v.y, es, di);
-        pack_elem<S, DB>(dr, e, 16, wr);
-        pack_elem<S, DB>(di, e, 16, wi);
+        re[e] = v.x;
+        im[e] = v.y;
       }
+      uint32_t wr[S][2], wi[S][2];
+      slice4<S, DB>(re, im, es, 16, wr, wi);
       store_words<S>(wr, 0u, base + tiled(2 * j, kpos(k, 0), Np), sstride);
       store_words<S>(wi, 0x80008000u, base + tiled(2 * j, kpos(k, 1), Np), sstride);
       store_words<S>(wi, 0u, base + tiled(2 * j + 1, kpos(k, 0), Np), sstride);
@@ -561,17 +479,14 @@ __device__ __forceinline__ void fused_b_tiles(const OzArgs &g, int item, int nt,
       break;
     }
     if (on) {
-      uint2 wr[S], wi[S];
-#pragma unroll
-      for (int p = 0; p < S; p++) wr[p] = wi[p] = make_uint2(0u, 0u);
+      double re[4], im[4];
 #pragma unroll
       for (int e = 0; e < 4; e++) {
-        int dr[S], di[S];
-        slice_digits<S, DB>(cur[e].x, es, dr);
-        slice_digits<S, DB>(cur[e].y, es, di);
-        pack_elem<S, DB>(dr, e, 16, wr);
-        pack_elem<S, DB>(di, e, 16, wi);
+        re[e] = cur[e].x;
+        im[e] = cur[e].y;
       }
+      uint32_t wr[S][2], wi[S][2];
+      slice4<S, DB>(re, im, es, 16, wr, wi);
       unsigned char *sb = sb0 + st * stage_bytes;
       const int r = 2 * jl, t = 4 * kq;
       const uint32_t o0 = sw64_off(r, t), o1 = sw64_off(r, t + 16), o2 = sw64_off(r + 1, t),
@@ -579,10 +494,10 @@ __device__ __forceinline__ void fused_b_tiles(const OzArgs &g, int item, int nt,
 #pragma unroll
       for (int p = 0; p < S; p++) {
         unsigned char *tp = sb + p * B_BYTES;
-        *reinterpret_cast<uint2 *>(tp + o0) = wr[p];
-        *reinterpret_cast<uint2 *>(tp + o1) = make_uint2(wi[p].x ^ 0x80008000u, wi[p].y ^ 0x80008000u);
-        *reinterpret_cast<uint2 *>(tp + o2) = wi[p];
-        *reinterpret_cast<uint2 *>(tp + o3) = wr[p];
+        *reinterpret_cast<uint2 *>(tp + o0) = make_uint2(wr[p][0], wr[p][1]);
+        *reinterpret_cast<uint2 *>(tp + o1) = make_uint2(wi[p][0] ^ 0x80008000u, wi[p][1] ^ 0x80008000u);
+        *reinterpret_cast<uint2 *>(tp + o2) = make_uint2(wi[p][0], wi[p][1]);
+        *reinterpret_cast<uint2 *>(tp + o3) = make_uint2(wr[p][0], wr[p][1]);
       }
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
