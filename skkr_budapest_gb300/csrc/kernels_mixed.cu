@@ -413,7 +413,8 @@ __device__ __forceinline__ uint32_t sw64_off(int r, int t) {
 // stores them four times (rows 2j and 2j+1, the Re and Im halves of the
 // k-block, -Im with flipped sign bits).  The next k-block's values are loaded
 // before the wait for the stage.  Each thread orders its stores before the
-// tensor core's reads (proxy fence) and arrives on the stage's full barrier.
+// tensor core's reads (proxy fence); lane 0 of each warp, after the warp's
+// barrier, arrives on the stage's full barrier.
 template <int S, int TN, int DB, int NSTAGE>
 __device__ __forceinline__ void fused_b_tiles(const OzArgs &g, int item, int nt, unsigned char *sb0,
                                               uint32_t stage_bytes, uint64_t *bar_full, uint64_t *bar_empty,
@@ -471,10 +472,17 @@ __device__ __forceinline__ void fused_b_tiles(const OzArgs &g, int item, int nt,
   };
   fetch(0, cur);
   const int nkb = g.kblocks;
-  for (int kb = 0; kb < nkb && !failed; kb++) {
+  for (int kb = 0; kb < nkb; kb++) {
+    // the warp leaves together (lane 0 reads the flag), so its barriers and
+    // shuffles below always see all 32 lanes
+    if (__shfl_sync(0xffffffffu, (int)failed, 0)) break;
     const int st = kb % NSTAGE;
     if (kb + 1 < nkb) fetch(kb + 1, nxt);
-    if (kb >= NSTAGE && !mbar_wait(&bar_empty[st], ((kb / NSTAGE) - 1) & 1)) {
+    // lane 0 waits for the stage, the warp follows it (its stores come after
+    // the tensor core's reads of the stage)
+    int ok = 1;
+    if (kb >= NSTAGE && lane == 0) ok = mbar_wait(&bar_empty[st], ((kb / NSTAGE) - 1) & 1);
+    if (!__shfl_sync(0xffffffffu, ok, 0)) {
       failed = 1;
       break;
     }
@@ -500,8 +508,10 @@ __device__ __forceinline__ void fused_b_tiles(const OzArgs &g, int item, int nt,
         *reinterpret_cast<uint2 *>(tp + o3) = make_uint2(wr[p][0], wr[p][1]);
       }
     }
+    // every lane's stores visible to the tensor core, then one arrival per warp
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    mbar_arrive(&bar_full[st]);
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&bar_full[st]);
 #pragma unroll
     for (int e = 0; e < 4; e++) cur[e] = nxt[e];
   }
@@ -561,7 +571,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_ozaki(const __grid_constant__
     issued_kb = -1;
     consumed_kb = -1;
     for (int i = 0; i < NSTAGE; i++) {
-      mbar_init(&bar_full[i], FB ? 1 + NCT : 1);  // fused B: every converting thread arrives too
+      mbar_init(&bar_full[i], FB ? 1 + NCT / 32 : 1);  // fused B: each converting warp arrives too
       mbar_init(&bar_empty[i], 1);
     }
     mbar_init(&bar_acc, 1);
@@ -912,7 +922,8 @@ __global__ void __launch_bounds__(TY * 16, MINB) k_cgj32(MatRef A, MatRef X, int
 // FP32 from FP64 operands, for the 2 x 2 block start of the split-precision
 // inverse: mode 0 C = AB, 1 C = D - AB (D read in FP64), 2 C = -AB.  Up to
 // two independent products per launch (blockIdx.y picks one).  The 16 x 16
-// threads each hold 4 x 4 outputs (rows ty + 16 i, columns tx + 16 j); the
+// threads each hold 4 x 4 outputs (rows ty + 16 i, columns tx + 16 j) as two
+// packed FP32 pairs each (two fma.rn.f32x2 per complex multiply-add); the
 // operands pass through shared memory in K chunks of 32, converted to FP32
 // on the way; the sums run in a fixed order.
 struct G32Job {
@@ -933,11 +944,14 @@ __global__ void __launch_bounds__(256, 2) k_cgemm32(G32Jobs jobs, int nc, const 
   const zd *a = mat_ptr(J.A, kk, cc), *b = mat_ptr(J.B, kk, cc);
   const int lda = J.A.ld, ldb = J.B.ld;
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  float2 acc[4][4];
+  // packed FP32 pairs: pr = (sum ar br, sum ar bi), pi = (sum ai br, sum ai bi)
+  // on the (br, bi) pair as it sits in shared memory; the product is
+  // (pr.x - pi.y, pr.y + pi.x)
+  unsigned long long pr[4][4], pi[4][4];
 #pragma unroll
   for (int i = 0; i < 4; i++)
 #pragma unroll
-    for (int j = 0; j < 4; j++) acc[i][j] = make_float2(0.f, 0.f);
+    for (int j = 0; j < 4; j++) pr[i][j] = pi[i][j] = 0ull;
   for (int k0 = 0; k0 < k; k0 += 32) {
     for (int e = threadIdx.x; e < 64 * 32; e += 256) {
       const int r = e & 63, q = e >> 6, col = k0 + q;
@@ -952,20 +966,19 @@ __global__ void __launch_bounds__(256, 2) k_cgemm32(G32Jobs jobs, int nc, const 
     __syncthreads();
 #pragma unroll 4
     for (int q = 0; q < 32; q++) {
-      float2 av[4], bv[4];
+      unsigned long long bv[4];
 #pragma unroll
-      for (int i = 0; i < 4; i++) av[i] = As[q][ty + 16 * i];
+      for (int j = 0; j < 4; j++) bv[j] = *reinterpret_cast<const unsigned long long *>(&Bs[q][tx + 16 * j]);
 #pragma unroll
-      for (int j = 0; j < 4; j++) bv[j] = Bs[q][tx + 16 * j];
-#pragma unroll
-      for (int i = 0; i < 4; i++)
+      for (int i = 0; i < 4; i++) {
+        const float2 a = As[q][ty + 16 * i];
+        const unsigned long long ar = pk2(a.x, a.x), ai = pk2(a.y, a.y);
 #pragma unroll
         for (int j = 0; j < 4; j++) {
-          acc[i][j].x = fmaf(av[i].x, bv[j].x, acc[i][j].x);
-          acc[i][j].x = fmaf(-av[i].y, bv[j].y, acc[i][j].x);
-          acc[i][j].y = fmaf(av[i].x, bv[j].y, acc[i][j].y);
-          acc[i][j].y = fmaf(av[i].y, bv[j].x, acc[i][j].y);
+          pr[i][j] = fma2(ar, bv[j], pr[i][j]);
+          pi[i][j] = fma2(ai, bv[j], pi[i][j]);
         }
+      }
     }
     __syncthreads();
   }
@@ -979,7 +992,8 @@ __global__ void __launch_bounds__(256, 2) k_cgemm32(G32Jobs jobs, int nc, const 
     for (int j = 0; j < 4; j++) {
       const int r = ty + 16 * i, col = tx + 16 * j;
       if (r < m && col < n) {
-        const zd p = make_double2((double)acc[i][j].x, (double)acc[i][j].y);
+        const float2 u = upk2(pr[i][j]), v = upk2(pi[i][j]);
+        const zd p = make_double2((double)(u.x - v.y), (double)(u.y + v.x));
         zd o;
         if (mode == 0) o = p;
         else if (mode == 1) {
