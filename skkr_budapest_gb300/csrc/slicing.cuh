@@ -115,6 +115,15 @@ SLC_HD void slice_digits(double x, int es, int *dig) {
   dig[0] = (top ^ sg) - sg;
 }
 
+// float bits of (f - 1.5 2^23) s for the float bits f of 1.5 2^23 + d (the
+// integer add already done): d s, exact
+SLC_HD uint32_t digit_bits_raw(uint32_t f, float s, float off) {
+#ifdef __CUDA_ARCH__
+  return slc_fbits(fmaf(slc_bitsf(f), s, off));
+#else
+  return slc_fbits(slc_bitsf(f) * s + off);
+#endif
+}
 // float bits of d 2^k for an integer digit |d| <= 128, from one integer add
 // and one FMA: (1.5 2^23 + d) 2^k - 1.5 2^23 2^k is exact, and with at most
 // eight significant bits the value is a bf16 held in the upper half of the
@@ -131,22 +140,38 @@ SLC_HD uint32_t digit_bits(int d, float s, float off) {
 // four consecutive complex values (re[e], im[e], e < 4) of one row or column
 // into the slice words: wr[p] / wi[p] hold the bf16 of the digits of the real
 // / imaginary parts scaled by 2^(wshift - DB p), element e in half e % 2 of
-// word .x (e < 2) or .y; two elements' digits are live at a time
+// word .x (e < 2) or .y.  The digits are those of slice_digits, formed from
+// |Y| (each a field of |Y| + digit_bias less 2^(DB-1) - 1, folded into the
+// bf16 construction's integer add) and negated through the bf16 sign bits,
+// one XOR per word; a zero digit of a negative value becomes -0, which
+// changes no product or sum
 template <int S, int DB>
 SLC_HD void slice4(const double (&re)[4], const double (&im)[4], int es, int wshift, uint32_t (&wr)[S][2],
                    uint32_t (&wi)[S][2]) {
+  constexpr int E0 = (DB - 1) + DB * (S - 1);
+  constexpr unsigned long long BIAS = digit_bias<S, DB>();
+  constexpr uint32_t LOW = (1u << (DB - 1)) - 1;
 #pragma unroll
   for (int h = 0; h < 2; h++) {
-    int r0[S], r1[S], i0[S], i1[S];
-    slice_digits<S, DB>(re[2 * h], es, r0);
-    slice_digits<S, DB>(re[2 * h + 1], es, r1);
-    slice_digits<S, DB>(im[2 * h], es, i0);
-    slice_digits<S, DB>(im[2 * h + 1], es, i1);
+    bool s0, s1, t0, t1;
+    const unsigned long long r0 = fix_round_mag(re[2 * h], E0 - es, &s0) + BIAS;
+    const unsigned long long r1 = fix_round_mag(re[2 * h + 1], E0 - es, &s1) + BIAS;
+    const unsigned long long i0 = fix_round_mag(im[2 * h], E0 - es, &t0) + BIAS;
+    const unsigned long long i1 = fix_round_mag(im[2 * h + 1], E0 - es, &t1) + BIAS;
+    const uint32_t sr = (s0 ? 0x8000u : 0u) | (s1 ? 0x80000000u : 0u);
+    const uint32_t si = (t0 ? 0x8000u : 0u) | (t1 ? 0x80000000u : 0u);
 #pragma unroll
     for (int p = 0; p < S; p++) {
       const float sc = pow2f(wshift - DB * p), off = -12582912.0f * sc;
-      wr[p][h] = slc_hi_pair(digit_bits(r0[p], sc, off), digit_bits(r1[p], sc, off));
-      wi[p][h] = slc_hi_pair(digit_bits(i0[p], sc, off), digit_bits(i1[p], sc, off));
+      // digit p (most significant first): the top one is what lies above the
+      // biased fields, the others a field less LOW
+      const int sh = DB * (S - 1 - p);
+      const uint32_t cst = p == 0 ? 0x4B400000u : 0x4B400000u - LOW;
+      const uint32_t msk = p == 0 ? 0xFFFFFFFFu : (1u << DB) - 1;
+      const uint32_t a0 = (uint32_t)(r0 >> sh) & msk, a1 = (uint32_t)(r1 >> sh) & msk;
+      const uint32_t b0 = (uint32_t)(i0 >> sh) & msk, b1 = (uint32_t)(i1 >> sh) & msk;
+      wr[p][h] = slc_hi_pair(digit_bits_raw(cst + a0, sc, off), digit_bits_raw(cst + a1, sc, off)) ^ sr;
+      wi[p][h] = slc_hi_pair(digit_bits_raw(cst + b0, sc, off), digit_bits_raw(cst + b1, sc, off)) ^ si;
     }
   }
 }
