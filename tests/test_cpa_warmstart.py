@@ -84,3 +84,19 @@ def test_projector_matrix_is_the_group_average_on_the_mask():
     d[mask] = rng.normal(size=mask.sum()) + 1j * rng.normal(size=mask.sum())
     want = CW.invariant_projector(ep)(d)
     assert np.abs((pm @ d[mask]).reshape(d.shape) - want).max() < 1e-13 * np.abs(want).max()
+
+
+def test_projector_cache_finds_equal_group_matrices_by_value(tmp_path):
+    fam = _family()
+    rng = np.random.default_rng(6)
+    ep1 = fam.problem(2, fam.draw(rng))
+    ep2 = fam.problem(3, fam.draw(rng))   # another energy: equal lg / rg, separate arrays
+    assert ep1.lg is not ep2.lg and np.array_equal(ep1.lg, ep2.lg)
+    m = _model(tmp_path, fam, ep1, scale=0.1)
+    p1 = m.projector(ep1)
+    p2 = m.projector(ep2)
+    assert p2 is p1                       # found by value, not rebuilt
+    assert m.projector(ep2) is p1         # and by identity from then on
+    ep3 = fam.problem(2, fam.draw(rng))
+    ep3.lg = ep3.lg * (1 + 1e-3)          # other group matrices: a new projector
+    assert m.projector(ep3) is not p1
