@@ -237,9 +237,11 @@ class Model:
                 self._net = N.Mlp16Net(self.layers, max(64, len(h)))
             y = self._net(h)
         else:
+            if getattr(self, "_w16", None) is None:
+                self._w16 = [bf16_round(w) for w, _ in self.layers]
             y = h
-            for i, (w, b) in enumerate(self.layers):
-                y = np.float32(y @ bf16_round(w) + b)
+            for i, (w, (_, b)) in enumerate(zip(self._w16, self.layers)):
+                y = np.float32(y @ w + b)
                 if i < len(self.layers) - 1:
                     y = np.tanh(y)
         return y * self.ystd + self.ymean
